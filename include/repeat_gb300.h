@@ -1,0 +1,141 @@
+/* repeat_gb300 — C ABI of the GB300 (sm_103a) periodic REPEAT charge fit.
+ *
+ * The reference has no C ABI: its fit path is Python (pyREPEAT repeat.py) and
+ * its native programs are executables.  Each entry point below replaces one
+ * step of repeat.py's fit path; the step is cited beside it.  A Python host
+ * (pyrepeat_gb300, via ctypes) and any other FFI bind these symbols.
+ *
+ * Conventions
+ *  - Every function returns RP_OK (0) or a negative RP_E* status and never
+ *    aborts; rp_last_error() gives the message of the last failure on a ctx.
+ *  - Pointers named *_dev are device pointers on the ctx's device; all other
+ *    pointers are host memory.  Device buffers passed in are owned by the
+ *    caller; scratch a call needs is owned by the ctx and counted against its
+ *    HBM budget.
+ *  - Grid values use the reference's flat order flat = i + j*nx + k*nx*ny
+ *    (repeat.py:2086), grid point (i,j,k) = i*axis[0] + j*axis[1] + k*axis[2]
+ *    (origin ignored, repeat.py:2097-2110).
+ *  - A ctx is used by one host thread at a time.  `stream` may be 0 (the
+ *    legacy default stream).
+ */
+#ifndef REPEAT_GB300_H
+#define REPEAT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RP_OK 0
+#define RP_E_ARG -1       /* invalid argument / size */
+#define RP_E_CUDA -2      /* CUDA runtime or driver error */
+#define RP_E_NOMEM -3     /* over the ctx's HBM budget or allocation failed */
+#define RP_E_SINGULAR -4  /* bordered system singular (pivot below threshold) */
+#define RP_E_TIMEOUT -5   /* a bounded device-side wait ran out */
+#define RP_E_STATE -6     /* call out of order (e.g. gram before filter) */
+#define RP_E_UNSUPPORTED -7
+
+/* Arithmetic of the Phi -> normal-equations stage. */
+#define RP_PREC_FP64 0  /* plain FP64: FP64 tables, FP64 real space, FP64 Gram */
+#define RP_PREC_MIXED 1 /* tensor cores: split BF16 k-contraction, FP32 erfc, split FP16 Gram */
+
+typedef void *rp_stream_t; /* a cudaStream_t */
+typedef struct rp_ctx rp_ctx;
+typedef struct rp_ewald rp_ewald;
+
+/* Cube geometry: grid counts and grid step vectors (rows, Bohr). */
+typedef struct {
+    int n_grid[3];
+    double axis[9];
+} rp_grid;
+
+/* Library version, major*10000 + minor*100 + patch. */
+int rp_version(void);
+
+/* Create a context on `device`.  hbm_budget: bytes of scratch the ctx may hold
+ * (0 = 90% of free memory at creation). */
+int rp_ctx_create(int device, size_t hbm_budget, rp_ctx **out);
+int rp_ctx_destroy(rp_ctx *ctx);
+/* Copies the last error message (NUL-terminated, truncated to cap). */
+int rp_last_error(const rp_ctx *ctx, char *buf, size_t cap);
+
+/* vdW grid filter + compaction + centring.
+ * Replaces ChargeCalculator._filter_grid (repeat.py:1922-2113) including its GPU
+ * kernel filter_bins (repeat.py:445-518) and the CPU cdist path
+ * (repeat.py:2115-2180).  Keep rule: every image (27 per atom) has
+ * |g-e|^2 > (vdw_factor*r)^2 and some image has |g-e|^2 <= (vdw_max*r)^2, in FP64
+ * (bit-exact mask).  Outputs kept flat indices in increasing order, the ESP at
+ * kept points minus its mean, and the kept count.
+ *   V_dev        [nx*ny*nz] f64   ESP on the full grid
+ *   atoms        [N*3] f64 (host) atom positions; Z [N] int32 atomic numbers (host)
+ *   kept_idx_dev [capacity] int32 out; Vc_dev [capacity] f64 out
+ *   mask_dev     [nx*ny*nz] u8 out, or NULL
+ *   M_out        kept count (host); RP_E_ARG if it exceeds capacity (M_out still set) */
+int rp_filter(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N,
+              const double *V_dev, double vdw_factor, double vdw_max, int32_t *kept_idx_dev,
+              double *Vc_dev, int64_t capacity, int64_t *M_out, uint8_t *mask_dev,
+              rp_stream_t stream);
+
+/* Ewald setup: alpha = (pi/Rc)^2, the integer-index k-set 0<=kx<=KMAX,
+ * |ky|,|kz|<=KMAX, 0<k^2<KMAX^2 with kcoef = 4pi/V exp(-k^2/4alpha)/k^2, and the
+ * real-space shifts |n_i| <= floor(Rc/|a_i|)+1 pruned by AABB distance.
+ * Replaces EwaldCalculator.__init__/_setup_kspace/prepare_pruned_shifts
+ * (repeat.py:1077-1143, 1708-1731, 1031-1069).  kmax = 7 is the reference. */
+int rp_ewald_setup(rp_ctx *ctx, const rp_grid *grid, double cutoff, int kmax, rp_ewald **out);
+int rp_ewald_destroy(rp_ewald *ew);
+/* K (k vectors), S (shifts before pruning), alpha. Any out pointer may be NULL. */
+int rp_ewald_info(const rp_ewald *ew, int *K, int *S, double *alpha);
+
+/* Mean-removed normal equations of the Ewald basis over the kept points.
+ * Replaces the streaming loop of ChargeCalculator.fit_charges
+ * (repeat.py:2184-2276: Phi via EwaldCalculator._compute_gpu*, repeat.py:1199-1435,
+ * then ATA += Phi^T Phi, ATb += Phi^T V, mean correction).  Phi is produced
+ * tile by tile on the device and never returned.
+ *   A_dev [N*N] f64 out (row-major), b_dev [N] f64 out: A = Phi^T (I - 11^T/M) Phi,
+ *   b = Phi^T (I - 11^T/M) Vc;  sum_phi_dev [N] out: column sums of Phi (may be NULL);
+ *   precision: RP_PREC_FP64 or RP_PREC_MIXED. */
+int rp_gram(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
+            const double *Vc_dev, int64_t M, int precision, double *A_dev, double *b_dev,
+            double *sum_phi_dev, rp_stream_t stream);
+
+/* Constraints and bordered solve on the device, FP64.
+ * Replaces repeat.py:2278-2313 with _apply_symmetry/_expand_charges
+ * (repeat.py:2445-2489) and _apply_resp (repeat.py:2511-2520):
+ * symmetry groups fold columns then rows into the base atom, RESP adds
+ * resp_s[i] to A_ii and resp_s[i]*resp_t[i] to b_i (per original atom, 0 = none),
+ * the (n+1) bordered system [[A, w],[w^T, 0]] [q; l] = [b; qtot] is solved by LU
+ * with partial pivoting plus one step of FP64 iterative refinement, and charges
+ * are expanded back to all N atoms.
+ *   A_dev, b_dev   inputs (not modified)
+ *   group_ptr [n_groups+1], group_idx [group_ptr[n_groups]] (host, 0-based, first = base)
+ *   resp_s, resp_t [N] (host, may be NULL)
+ *   q_dev [N] f64 out;  info (host, may be NULL): [0] residual inf-norm after
+ *   refinement, [1] min |pivot|, [2] max |pivot|. */
+int rp_solve(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups,
+             const int *group_ptr, const int *group_idx, const double *resp_s, const double *resp_t,
+             double qtot, double *q_dev, double *info, rp_stream_t stream);
+
+/* One whole fit from host memory, as repeat.py's main() runs it for
+ * `--fit-type 1 [--gpu]`: H2D of V, filter, Ewald setup, normal equations,
+ * constraints, solve, D2H of the charges.  q_out [N] host. M_out may be NULL. */
+typedef struct {
+    rp_grid grid;
+    const double *V;        /* [nx*ny*nz] host */
+    const double *atoms;    /* [N*3] host */
+    const int *Z;           /* [N] host */
+    int N;
+    double vdw_factor, vdw_max, cutoff, qtot;
+    int kmax;
+    int n_groups;
+    const int *group_ptr, *group_idx;
+    const double *resp_s, *resp_t;
+    int precision;
+} rp_fit_desc;
+int rp_fit(rp_ctx *ctx, const rp_fit_desc *desc, double *q_out, int64_t *M_out, rp_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

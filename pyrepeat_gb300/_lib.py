@@ -1,0 +1,110 @@
+"""ctypes binding of librepeat_gb300.so (the C ABI in include/repeat_gb300.h).
+
+There is no CPU fallback: if the library is missing or cannot be loaded, every
+call raises.  Device buffers are torch CUDA tensors passed by data_ptr().
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librepeat_gb300.so")
+
+RP_OK = 0
+STATUS = {
+    -1: "RP_E_ARG", -2: "RP_E_CUDA", -3: "RP_E_NOMEM", -4: "RP_E_SINGULAR", -5: "RP_E_TIMEOUT",
+    -6: "RP_E_STATE", -7: "RP_E_UNSUPPORTED",
+}
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+# every symbol include/repeat_gb300.h declares
+EXPORTS = ["rp_version", "rp_ctx_create", "rp_ctx_destroy", "rp_last_error", "rp_filter", "rp_ewald_setup",
+           "rp_ewald_destroy", "rp_ewald_info", "rp_gram", "rp_solve", "rp_fit"]
+
+
+class RepeatError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SingularError(RepeatError):
+    pass
+
+
+class RpGrid(ctypes.Structure):
+    _fields_ = [("n_grid", ctypes.c_int * 3), ("axis", ctypes.c_double * 9)]
+
+
+class RpFitDesc(ctypes.Structure):
+    _fields_ = [("grid", RpGrid), ("V", ctypes.c_void_p), ("atoms", ctypes.c_void_p), ("Z", ctypes.c_void_p),
+                ("N", ctypes.c_int), ("vdw_factor", ctypes.c_double), ("vdw_max", ctypes.c_double),
+                ("cutoff", ctypes.c_double), ("qtot", ctypes.c_double), ("kmax", ctypes.c_int),
+                ("n_groups", ctypes.c_int), ("group_ptr", ctypes.c_void_p), ("group_idx", ctypes.c_void_p),
+                ("resp_s", ctypes.c_void_p), ("resp_t", ctypes.c_void_p), ("precision", ctypes.c_int)]
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the CUDA library (building it in-tree first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        from .build import build_cuda
+        build_cuda()
+    if not os.path.exists(path):
+        raise ImportError(f"librepeat_gb300.so not found at {path}; run pyrepeat_gb300.build")
+    L = ctypes.CDLL(path)
+    P, I, D, L64, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int64, ctypes.c_size_t
+    L.rp_version.restype = I
+    L.rp_version.argtypes = []
+    L.rp_ctx_create.restype = I
+    L.rp_ctx_create.argtypes = [I, SZ, ctypes.POINTER(P)]
+    L.rp_ctx_destroy.restype = I
+    L.rp_ctx_destroy.argtypes = [P]
+    L.rp_last_error.restype = I
+    L.rp_last_error.argtypes = [P, ctypes.c_char_p, SZ]
+    L.rp_filter.restype = I
+    L.rp_filter.argtypes = [P, ctypes.POINTER(RpGrid), P, P, I, P, D, D, P, P, L64, ctypes.POINTER(L64), P, P]
+    L.rp_ewald_setup.restype = I
+    L.rp_ewald_setup.argtypes = [P, ctypes.POINTER(RpGrid), D, I, ctypes.POINTER(P)]
+    L.rp_ewald_destroy.restype = I
+    L.rp_ewald_destroy.argtypes = [P]
+    L.rp_ewald_info.restype = I
+    L.rp_ewald_info.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(D)]
+    L.rp_gram.restype = I
+    L.rp_gram.argtypes = [P, P, P, I, P, P, L64, I, P, P, P, P]
+    L.rp_solve.restype = I
+    L.rp_solve.argtypes = [P, P, P, I, I, P, P, P, P, D, P, P, P]
+    L.rp_fit.restype = I
+    L.rp_fit.argtypes = [P, ctypes.POINTER(RpFitDesc), P, ctypes.POINTER(L64), P]
+    _lib = L
+    return L
+
+
+def check(ctx_ptr, rc: int, what: str = ""):
+    if rc == RP_OK:
+        return
+    buf = ctypes.create_string_buffer(1024)
+    if ctx_ptr:
+        load().rp_last_error(ctx_ptr, buf, 1024)
+    msg = buf.value.decode(errors="replace") or what
+    if rc == -4:
+        raise SingularError(rc, msg)
+    raise RepeatError(rc, msg)
+
+
+def make_grid(n_grid, axis) -> RpGrid:
+    g = RpGrid()
+    for i in range(3):
+        g.n_grid[i] = int(n_grid[i])
+    flat = [float(x) for row in axis for x in row]
+    for i in range(9):
+        g.axis[i] = flat[i]
+    return g

@@ -1,0 +1,437 @@
+// vdW grid filter: keep mask, ordered compaction and ESP centring.
+//
+// Replaces ChargeCalculator._filter_grid (repeat.py:1922-2113) and its GPU
+// kernel filter_bins (repeat.py:445-518).  The keep rule is the reference's
+// FP64 squared-distance rule:
+//     keep(g) = all_e |g-e|^2 > rmin_e^2  and  any_e |g-e|^2 <= rmax_e^2
+// over the 27 lattice images e of every atom (clipped like repeat.py:1945-1969),
+// with g = (i*a0 + j*a1) + k*a2 and |d|^2 = (dx*dx + dy*dy) + dz*dz evaluated in
+// IEEE FP64 without contraction.
+//
+// GB300 design: every grid point is classified in FP32 against the atoms of the
+// 27 neighbouring bins of a cell list (bin edge >= max rmin, so no other atom
+// can reject it).  A pair whose FP32 squared distance lies within a proven error
+// band of rmin^2 is re-evaluated in FP64 exactly as above, so the mask is
+// bit-identical to the FP64 rule while almost all work runs on the FP32 pipe.
+// "near" is proved for the whole grid on the host when one image's rmax covers
+// every grid corner (always true at the default vdw_max = 1000); otherwise it
+// is tested the same way (FP32 with an FP64 recheck band) against every image.
+//
+// The kernel is bound by HBM traffic of the mask pass: 1 B mask write per point
+// (plus the compaction pass: 1 B mask read + 8 B V read per point, 4 B index +
+// 8 B V write per kept point).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace rp {
+namespace {
+
+constexpr int kFilterThreads = 256;
+
+// x, y, z and a squared radius, FP64 (32-byte aligned for one vector load)
+struct alignas(32) D4 {
+    double x, y, z, w;
+};
+
+struct FilterParams {
+    int nx, ny, nz;
+    long long n_total;
+    float ax[9];
+    double axd[9];
+    float bmin[3];
+    float inv_bsize;
+    int bn[3];
+    float err_min;   // FP32 band around rmin^2
+    float err_max;   // FP32 band around rmax^2
+    int near_all;
+    int A;
+};
+
+__device__ __forceinline__ double exact_d2(const double *axd, int i, int j, int k, double ex, double ey,
+                                           double ez) {
+    // ((i*a0 + j*a1) + k*a2) and ((dx*dx + dy*dy) + dz*dz), every op rounded (no FMA)
+    double gx = __dadd_rn(__dadd_rn(__dmul_rn((double)i, axd[0]), __dmul_rn((double)j, axd[3])),
+                          __dmul_rn((double)k, axd[6]));
+    double gy = __dadd_rn(__dadd_rn(__dmul_rn((double)i, axd[1]), __dmul_rn((double)j, axd[4])),
+                          __dmul_rn((double)k, axd[7]));
+    double gz = __dadd_rn(__dadd_rn(__dmul_rn((double)i, axd[2]), __dmul_rn((double)j, axd[5])),
+                          __dmul_rn((double)k, axd[8]));
+    double dx = __dsub_rn(gx, ex), dy = __dsub_rn(gy, ey), dz = __dsub_rn(gz, ez);
+    return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+__global__ void __launch_bounds__(kFilterThreads) filter_mask_kernel(
+    FilterParams p, const float4 *__restrict__ eff, const D4 *__restrict__ eff64,
+    const double *__restrict__ rmax2, const float *__restrict__ rmax2f, const int *__restrict__ boff,
+    const int *__restrict__ bidx, uint8_t *__restrict__ mask, int *__restrict__ block_counts,
+    unsigned long long *__restrict__ rechecks) {
+    long long f = (long long)blockIdx.x * kFilterThreads + threadIdx.x;
+    int keep = 0;
+    unsigned nre = 0;
+    if (f < p.n_total) {
+        int layer = p.nx * p.ny;
+        int k = (int)(f / layer);
+        int rem = (int)(f - (long long)k * layer);
+        int j = rem / p.nx;
+        int i = rem - j * p.nx;
+        float gx = (i * p.ax[0] + j * p.ax[3]) + k * p.ax[6];
+        float gy = (i * p.ax[1] + j * p.ax[4]) + k * p.ax[7];
+        float gz = (i * p.ax[2] + j * p.ax[5]) + k * p.ax[8];
+        int bc[3];
+        float g3[3] = {gx, gy, gz};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            float t = (g3[d] - p.bmin[d]) * p.inv_bsize;
+            t = fminf(fmaxf(t, -1.0f), (float)p.bn[d]);
+            bc[d] = min(max((int)floorf(t), 0), p.bn[d] - 1);
+        }
+        bool valid = true;
+        for (int dz = -1; dz <= 1 && valid; ++dz) {
+            int z2 = bc[2] + dz;
+            if (z2 < 0 || z2 >= p.bn[2]) continue;
+            for (int dy = -1; dy <= 1 && valid; ++dy) {
+                int y2 = bc[1] + dy;
+                if (y2 < 0 || y2 >= p.bn[1]) continue;
+                int row = p.bn[0] * (y2 + p.bn[1] * z2);
+                int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, p.bn[0] - 1);
+                int t0 = boff[row + x0], t1 = boff[row + x1 + 1];
+                for (int t = t0; t < t1; ++t) {
+                    int a = bidx[t];
+                    float4 e = eff[a];
+                    float ddx = gx - e.x, ddy = gy - e.y, ddz = gz - e.z;
+                    float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                    if (d2 <= e.w - p.err_min) { valid = false; break; }
+                    if (d2 <= e.w + p.err_min) {
+                        D4 e8 = eff64[a];
+                        ++nre;
+                        if (exact_d2(p.axd, i, j, k, e8.x, e8.y, e8.z) <= e8.w) { valid = false; break; }
+                    }
+                }
+            }
+        }
+        bool near = p.near_all != 0;
+        if (valid && !near) {
+            for (int a = 0; a < p.A && !near; ++a) {
+                float4 e = eff[a];
+                float ddx = gx - e.x, ddy = gy - e.y, ddz = gz - e.z;
+                float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                float r2 = rmax2f[a];
+                if (d2 <= r2 - p.err_max) { near = true; break; }
+                if (d2 <= r2 + p.err_max) {
+                    D4 e8 = eff64[a];
+                    ++nre;
+                    if (exact_d2(p.axd, i, j, k, e8.x, e8.y, e8.z) <= rmax2[a]) near = true;
+                }
+            }
+        }
+        keep = (valid && near) ? 1 : 0;
+        mask[f] = (uint8_t)keep;
+    }
+    int cnt = __syncthreads_count(keep);
+    if (threadIdx.x == 0) block_counts[blockIdx.x] = cnt;
+    if (nre) atomicAdd(rechecks, (unsigned long long)nre);
+}
+
+// Exclusive scan of the per-block counts (one block; nb up to a few 10^5).
+__global__ void __launch_bounds__(1024) scan_counts_kernel(const int *__restrict__ counts, int nb,
+                                                           long long *__restrict__ offsets,
+                                                           long long *__restrict__ total) {
+    __shared__ long long part[1024];
+    int t = threadIdx.x;
+    int per = (nb + 1023) / 1024;
+    int b0 = t * per, b1 = min(b0 + per, nb);
+    long long s = 0;
+    for (int b = b0; b < b1; ++b) s += counts[b];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {  // Hillis-Steele inclusive scan
+        long long v = (t >= off) ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    long long run = (t == 0) ? 0 : part[t - 1];
+    for (int b = b0; b < b1; ++b) {
+        offsets[b] = run;
+        run += counts[b];
+    }
+    if (t == 1023) *total = part[1023];
+}
+
+__global__ void __launch_bounds__(kFilterThreads) compact_kernel(
+    const uint8_t *__restrict__ mask, const double *__restrict__ V, long long n_total,
+    const long long *__restrict__ offsets, long long capacity, int32_t *__restrict__ kept_idx,
+    double *__restrict__ Vc, double *__restrict__ block_vsum) {
+    __shared__ int warp_base[kFilterThreads / 32];
+    __shared__ double warp_sum[kFilterThreads / 32];
+    long long f = (long long)blockIdx.x * kFilterThreads + threadIdx.x;
+    int keep = (f < n_total) ? mask[f] : 0;
+    double v = keep ? V[f] : 0.0;
+    unsigned bal = __ballot_sync(0xffffffffu, keep);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int pos_in_warp = __popc(bal & ((1u << lane) - 1u));
+    // fixed-order FP64 warp sum
+    double s = v;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        warp_base[warp] = __popc(bal);
+        warp_sum[warp] = s;
+    }
+    __syncthreads();
+    int base = 0;
+    for (int w = 0; w < warp; ++w) base += warp_base[w];
+    if (keep) {
+        long long pos = offsets[blockIdx.x] + base + pos_in_warp;
+        if (pos < capacity) {
+            kept_idx[pos] = (int32_t)f;
+            Vc[pos] = v;
+        }
+    }
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kFilterThreads / 32; ++w) t += warp_sum[w];
+        block_vsum[blockIdx.x] = t;
+    }
+}
+
+// Mean of kept V over all blocks in a fixed order (deterministic), one block.
+__global__ void __launch_bounds__(1024) vmean_kernel(const double *__restrict__ block_vsum, int nb,
+                                                     const long long *__restrict__ total,
+                                                     double *__restrict__ mean_out) {
+    __shared__ double part[1024];
+    int t = threadIdx.x;
+    double s = 0.0;
+    for (int b = t; b < nb; b += 1024) s += block_vsum[b];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 512; off > 0; off >>= 1) {
+        if (t < off) part[t] += part[t + off];
+        __syncthreads();
+    }
+    if (t == 0) {
+        long long M = *total;
+        *mean_out = M > 0 ? part[0] / (double)M : 0.0;
+    }
+}
+
+__global__ void center_kernel(double *__restrict__ Vc, long long M, const double *__restrict__ mean) {
+    double m = *mean;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x)
+        Vc[i] -= m;
+}
+
+double radius_of(int z) {
+    static const double VDW[] = {
+        2.72687, 2.23177, 2.31586, 2.59365, 3.85788, 3.63867, 3.45820, 3.30702, 3.17852, 3.06419, 2.81853,
+        2.85443, 4.25094, 4.05819, 3.91835, 3.81252, 3.72937, 3.65473, 3.60182, 3.21159, 3.11332, 2.99994,
+        2.97065, 2.85632, 2.79774, 2.75144, 2.71365, 2.67774, 3.30230, 2.61066, 4.14133, 4.04401, 3.99677,
+        3.97315, 3.95803, 3.91268, 3.88717, 3.44025, 3.16057, 2.95175, 2.99049, 2.88372, 2.83270, 2.79963,
+        2.76750, 2.73916, 2.97443, 2.69097, 4.21692, 4.14984, 4.17629, 4.22354, 4.25188, 4.16118, 4.26795,
+        3.49883, 3.32781, 3.35993, 3.40718, 3.37789, 3.35143, 3.32592, 3.30041, 3.18230, 3.26072, 3.23899,
+        3.22104, 3.20403, 3.18797, 3.17002, 3.43930, 2.96781, 2.99522, 2.89978, 2.79113, 2.94797, 2.68341,
+        2.60215, 3.11143, 2.55585, 4.10732, 4.06008, 4.12905, 4.44936, 4.48810, 4.50227, 4.62983, 3.47426,
+        3.28623, 3.20875, 3.23521, 3.20781, 3.23521, 3.23521, 3.19458, 3.14261, 3.15490, 3.13033, 3.11710,
+        3.10482, 3.09348, 3.06892, 3.05758, 3.04513, 3.03268, 3.02023, 3.00778};
+    const int n = (int)(sizeof(VDW) / sizeof(VDW[0]));
+    return (z >= 1 && z <= n) ? VDW[z - 1] : 3.0;
+}
+
+}  // namespace
+
+void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
+                double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, int64_t capacity,
+                int64_t *M_out, uint8_t *mask_dev, cudaStream_t stream) {
+    RP_REQUIRE(grid && atoms && Z && V_dev && M_out, "rp_filter: null argument");
+    RP_REQUIRE(N >= 0, "rp_filter: N < 0");
+    const int nx = grid->n_grid[0], ny = grid->n_grid[1], nz = grid->n_grid[2];
+    RP_REQUIRE(nx > 0 && ny > 0 && nz > 0, "rp_filter: grid counts must be positive");
+    const long long n_total = (long long)nx * ny * nz;
+    RP_REQUIRE(n_total < (1LL << 31), "rp_filter: grid larger than 2^31 points");
+    RP_REQUIRE(vdw_factor >= 0.0 && vdw_max >= 0.0, "rp_filter: negative vdW factor");
+    const double *ax = grid->axis;
+
+    // ---- effective atoms (repeat.py:1933-1969), FP64, reference operation order
+    double box[9];
+    for (int i = 0; i < 3; ++i)
+        for (int d = 0; d < 3; ++d) box[3 * i + d] = (double)grid->n_grid[i] * ax[3 * i + d];
+    double gmaxr = 5.0;
+    if (N > 0) {
+        gmaxr = -1e300;
+        for (int a = 0; a < N; ++a) gmaxr = std::max(gmaxr, vdw_max * radius_of(Z[a]));
+    }
+    double cmin[3] = {1e300, 1e300, 1e300}, cmax[3] = {-1e300, -1e300, -1e300};
+    for (int c = 0; c < 8; ++c) {  // corners of the grid-step parallelepiped, as the reference forms them
+        int fI = (c >> 2) & 1, fJ = (c >> 1) & 1, fK = c & 1;
+        for (int d = 0; d < 3; ++d) {
+            double v = (fI * ax[d] + fJ * ax[3 + d]) + fK * ax[6 + d];
+            cmin[d] = std::min(cmin[d], v);
+            cmax[d] = std::max(cmax[d], v);
+        }
+    }
+    const double margin = gmaxr + 0.1;
+    std::vector<D4> e64;
+    std::vector<double> rmax2;
+    e64.reserve(27 * (size_t)N);
+    double max_rmin = 0.0, max_rmax = 0.0, emax = 0.0;
+    for (int a = 0; a < N; ++a) {
+        double raw = radius_of(Z[a]);
+        double rn = vdw_factor * raw, rx = vdw_max * raw;
+        for (int kz = -1; kz <= 1; ++kz)
+            for (int ky = -1; ky <= 1; ++ky)
+                for (int kx = -1; kx <= 1; ++kx) {
+                    double p[3];
+                    bool in = true;
+                    for (int d = 0; d < 3; ++d) {
+                        double sh = (kx * box[d] + ky * box[3 + d]) + kz * box[6 + d];
+                        p[d] = atoms[3 * a + d] + sh;
+                        if (!(p[d] >= cmin[d] - margin && p[d] <= cmax[d] + margin)) in = false;
+                    }
+                    if (!in) continue;
+                    e64.push_back(D4{p[0], p[1], p[2], rn * rn});
+                    rmax2.push_back(rx * rx);
+                    max_rmin = std::max(max_rmin, rn);
+                    max_rmax = std::max(max_rmax, rx);
+                    for (int d = 0; d < 3; ++d) emax = std::max(emax, std::fabs(p[d]));
+                }
+    }
+    const int A = (int)e64.size();
+
+    // ---- near proved for every grid point?  (the grid hull is convex: its corners bound it)
+    int near_all = 0;
+    for (int a = 0; a < A && !near_all; ++a) {
+        double worst = 0.0;
+        for (int c = 0; c < 8; ++c) {
+            int f0 = (c & 1) ? nx - 1 : 0, f1 = (c & 2) ? ny - 1 : 0, f2 = (c & 4) ? nz - 1 : 0;
+            double d2 = 0.0;
+            for (int d = 0; d < 3; ++d) {
+                double v = (f0 * ax[d] + f1 * ax[3 + d]) + f2 * ax[6 + d];
+                v -= (d == 0 ? e64[a].x : (d == 1 ? e64[a].y : e64[a].z));
+                d2 += v * v;
+            }
+            worst = std::max(worst, d2);
+        }
+        if (worst * (1.0 + 1e-9) + 1e-9 < rmax2[a]) near_all = 1;
+    }
+
+    // ---- FP32 error band (see header comment): |d2_32 - d2_64| <= err
+    double gs = 0.0;  // bound on |i*a0|+|j*a1|+|k*a2| per component
+    for (int d = 0; d < 3; ++d)
+        gs = std::max(gs, (nx - 1) * std::fabs(ax[d]) + (ny - 1) * std::fabs(ax[3 + d]) + (nz - 1) * std::fabs(ax[6 + d]));
+    const double u = std::ldexp(1.0, -24);
+    const double ddx = 8.0 * u * gs + 2.0 * u * emax + 2.0 * u * (gs + emax);
+    auto band = [&](double r) {
+        return 4.0 * (2.0 * std::sqrt(3.0) * r * 1.01 * ddx + 3.0 * ddx * ddx + 8.0 * u * r * r * 1.02) + 1e-30;
+    };
+    const double err_min = band(max_rmin);
+    const double err_max = band(max_rmax);
+
+    // ---- cell list for the reject test: bin edge >= max rmin + coordinate error
+    double bsize = std::max(max_rmin, 1e-3) * (1.0 + 1e-4) + 16.0 * ddx + 1e-3;
+    double bmin[3] = {1e300, 1e300, 1e300}, bmax[3] = {-1e300, -1e300, -1e300};
+    for (auto &e : e64) {
+        double p[3] = {e.x, e.y, e.z};
+        for (int d = 0; d < 3; ++d) {
+            bmin[d] = std::min(bmin[d], p[d]);
+            bmax[d] = std::max(bmax[d], p[d]);
+        }
+    }
+    if (A == 0)
+        for (int d = 0; d < 3; ++d) bmin[d] = bmax[d] = 0.0;
+    int bn[3];
+    for (int d = 0; d < 3; ++d) bn[d] = std::max(1, (int)std::ceil((bmax[d] - bmin[d]) / bsize) + 1);
+    while ((long long)bn[0] * bn[1] * bn[2] > (1LL << 22)) {  // keep the table small; grow bins
+        bsize *= 1.25;
+        for (int d = 0; d < 3; ++d) bn[d] = std::max(1, (int)std::ceil((bmax[d] - bmin[d]) / bsize) + 1);
+    }
+    const int nb = bn[0] * bn[1] * bn[2];
+    std::vector<int> boff((size_t)nb + 1, 0), bidx((size_t)std::max(A, 1)), binof((size_t)std::max(A, 1));
+    for (int a = 0; a < A; ++a) {
+        double p[3] = {e64[a].x, e64[a].y, e64[a].z};
+        int b = 0, m = 1;
+        for (int d = 0; d < 3; ++d) {
+            int c = (int)std::floor((p[d] - bmin[d]) / bsize);
+            c = std::min(std::max(c, 0), bn[d] - 1);
+            b += m * c;
+            m *= bn[d];
+        }
+        binof[a] = b;
+        boff[b + 1]++;
+    }
+    for (int b = 0; b < nb; ++b) boff[b + 1] += boff[b];
+    {
+        std::vector<int> cur(boff.begin(), boff.end() - 1);
+        for (int a = 0; a < A; ++a) bidx[cur[binof[a]]++] = a;
+    }
+    // FP32 copies, ordered by bin so a bin's atoms are contiguous in memory
+    std::vector<float4> e32((size_t)std::max(A, 1));
+    std::vector<D4> e64s((size_t)std::max(A, 1));
+    std::vector<double> rmax2s((size_t)std::max(A, 1));
+    std::vector<float> rmax2f((size_t)std::max(A, 1));
+    for (int t = 0; t < A; ++t) {
+        int a = bidx[t];
+        e64s[t] = e64[a];
+        rmax2s[t] = rmax2[a];
+        rmax2f[t] = (float)rmax2[a];
+        e32[t] = make_float4((float)e64[a].x, (float)e64[a].y, (float)e64[a].z, (float)e64[a].w);
+        bidx[t] = t;
+    }
+
+    // ---- upload (ctx scratch) and launch
+    const int nblk = (int)((n_total + kFilterThreads - 1) / kFilterThreads);
+    float4 *d_e32 = ctx->buf_t<float4>("flt_e32", e32.size());
+    D4 *d_e64 = ctx->buf_t<D4>("flt_e64", e64s.size());
+    double *d_rmax2 = ctx->buf_t<double>("flt_rmax2", rmax2s.size());
+    float *d_rmax2f = ctx->buf_t<float>("flt_rmax2f", rmax2f.size());
+    int *d_boff = ctx->buf_t<int>("flt_boff", boff.size());
+    int *d_bidx = ctx->buf_t<int>("flt_bidx", bidx.size());
+    uint8_t *d_mask = mask_dev ? mask_dev : ctx->buf_t<uint8_t>("flt_mask", (size_t)n_total);
+    int *d_counts = ctx->buf_t<int>("flt_counts", (size_t)nblk);
+    long long *d_offsets = ctx->buf_t<long long>("flt_offsets", (size_t)nblk);
+    double *d_vsum = ctx->buf_t<double>("flt_vsum", (size_t)nblk);
+    long long *d_total = ctx->buf_t<long long>("flt_total", 1);
+    double *d_mean = ctx->buf_t<double>("flt_mean", 1);
+    unsigned long long *d_re = ctx->buf_t<unsigned long long>("flt_rechecks", 1);
+    RP_CUDA(cudaMemcpyAsync(d_e32, e32.data(), e32.size() * sizeof(float4), cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_e64, e64s.data(), e64s.size() * sizeof(D4), cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_rmax2, rmax2s.data(), rmax2s.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_rmax2f, rmax2f.data(), rmax2f.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_boff, boff.data(), boff.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_bidx, bidx.data(), bidx.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemsetAsync(d_re, 0, sizeof(unsigned long long), stream));
+
+    FilterParams p{};
+    p.nx = nx; p.ny = ny; p.nz = nz; p.n_total = n_total;
+    for (int t = 0; t < 9; ++t) { p.ax[t] = (float)ax[t]; p.axd[t] = ax[t]; }
+    for (int d = 0; d < 3; ++d) { p.bmin[d] = (float)bmin[d]; p.bn[d] = bn[d]; }
+    p.inv_bsize = (float)(1.0 / bsize);
+    p.err_min = (float)err_min;
+    p.err_max = (float)err_max;
+    p.near_all = near_all;
+    p.A = A;
+    filter_mask_kernel<<<nblk, kFilterThreads, 0, stream>>>(p, d_e32, d_e64, d_rmax2, d_rmax2f, d_boff, d_bidx,
+                                                            d_mask, d_counts, d_re);
+    RP_LAUNCH_CHECK();
+    scan_counts_kernel<<<1, 1024, 0, stream>>>(d_counts, nblk, d_offsets, d_total);
+    RP_LAUNCH_CHECK();
+    compact_kernel<<<nblk, kFilterThreads, 0, stream>>>(d_mask, V_dev, n_total, d_offsets, (long long)capacity,
+                                                        kept_idx_dev, Vc_dev, d_vsum);
+    RP_LAUNCH_CHECK();
+    vmean_kernel<<<1, 1024, 0, stream>>>(d_vsum, nblk, d_total, d_mean);
+    RP_LAUNCH_CHECK();
+    long long M = 0;
+    RP_CUDA(cudaMemcpyAsync(&M, d_total, sizeof(long long), cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaStreamSynchronize(stream));
+    *M_out = M;
+    if (M > capacity) fail(RP_E_ARG, "rp_filter: " + std::to_string(M) + " kept points exceed capacity " +
+                                         std::to_string(capacity));
+    if (M > 0) {
+        int cb = (int)std::min<long long>((M + 255) / 256, 4096);
+        center_kernel<<<cb, 256, 0, stream>>>(Vc_dev, M, d_mean);
+        RP_LAUNCH_CHECK();
+    }
+}
+
+}  // namespace rp

@@ -1,0 +1,409 @@
+// Constraints and the bordered solve, on the device in FP64.
+//
+// Replaces repeat.py:2278-2313: symmetry folding (repeat.py:2445-2470: columns
+// of every group into its base, then rows, linked atoms dropped), RESP
+// restraints on the folded diagonal (repeat.py:2511-2520), the (n+1) bordered
+// total-charge system [[A, w],[w^T, 0]] [q; l] = [b; Q] (repeat.py:2296-2304)
+// solved by LU with partial pivoting (scipy.linalg.solve / repeat_cpu_omp.cpp:
+// 466-495), then charges expanded to the linked atoms (repeat.py:2472-2489).
+//
+// For disjoint groups (each atom in at most one group) folding is the gather
+//   A_red[r][c] = sum_{i in G(r)} sum_{j in G(c)} A[i][j],  b_red[r] = sum_{i in G(r)} b[i],
+//   w[r] = |G(r)|
+// which equals the reference's sequential column-then-row folding.  Groups
+// that overlap are folded on the host with the reference's sequential rules.
+//
+// One CTA factors one system (so a batch of systems is one launch), keeps the
+// original bordered matrix for one step of FP64 iterative refinement
+// x += LU^{-1}(b - A x), and reports the refined residual and pivot range.
+#include <algorithm>
+#include <cmath>
+#include <set>
+
+#include "common.cuh"
+
+namespace rp {
+
+struct SolveDesc {
+    const double *A;      // N x N input
+    const double *b;      // N input
+    int N;                // original atoms
+    int n;                // reduced atoms
+    const int *mem_ptr;   // n+1, CSR of members per reduced index
+    const int *mem_idx;   // members (original atom indices)
+    const double *resp_s; // n (per reduced index, already mapped) or null
+    const double *resp_t; // n
+    const int *map;       // N: reduced index of each original atom
+    double qtot;
+    double *As;           // (n+1)^2 work: bordered matrix, then LU
+    double *A0;           // (n+1)^2 copy of the bordered matrix (for refinement)
+    double *bs;           // n+1 rhs
+    double *x;            // n+1 solution
+    double *r;            // n+1 residual / correction
+    int *perm;            // n+1 pivot rows
+    double *q;            // N out
+    double *info;         // 4 out: residual inf-norm, min|piv|, max|piv|, singular flag
+};
+
+namespace {
+
+__global__ void build_bordered_kernel(SolveDesc d) {
+    const int n1 = d.n + 1;
+    long long total = (long long)n1 * n1;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        int r = (int)(t / n1), c = (int)(t - (long long)r * n1);
+        double v;
+        if (r < d.n && c < d.n) {
+            v = 0.0;
+            for (int p = d.mem_ptr[r]; p < d.mem_ptr[r + 1]; ++p) {
+                const double *row = d.A + (size_t)d.mem_idx[p] * d.N;
+                for (int q = d.mem_ptr[c]; q < d.mem_ptr[c + 1]; ++q) v += row[d.mem_idx[q]];
+            }
+            if (r == c && d.resp_s) v += d.resp_s[r];
+        } else if (r < d.n) {
+            v = (double)(d.mem_ptr[r + 1] - d.mem_ptr[r]);
+        } else if (c < d.n) {
+            v = (double)(d.mem_ptr[c + 1] - d.mem_ptr[c]);
+        } else {
+            v = 0.0;
+        }
+        d.As[t] = v;
+        d.A0[t] = v;
+        if (c == 0) {
+            double bv;
+            if (r < d.n) {
+                bv = 0.0;
+                for (int p = d.mem_ptr[r]; p < d.mem_ptr[r + 1]; ++p) bv += d.b[d.mem_idx[p]];
+                if (d.resp_s) bv += d.resp_s[r] * d.resp_t[r];
+            } else {
+                bv = d.qtot;
+            }
+            d.bs[r] = bv;
+        }
+    }
+}
+
+constexpr int kLU = 1024;
+
+__device__ void block_argmax(double v, int idx, double *sv, int *si, double *out_v, int *out_i) {
+    // max |v| with lowest index on ties (deterministic)
+    for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_down_sync(0xffffffffu, v, o);
+        int oi = __shfl_down_sync(0xffffffffu, idx, o);
+        if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { sv[w] = v; si[w] = idx; }
+    __syncthreads();
+    if (w == 0) {
+        v = (lane < kLU / 32) ? sv[lane] : -1.0;
+        idx = (lane < kLU / 32) ? si[lane] : 0x7fffffff;
+        for (int o = 16; o > 0; o >>= 1) {
+            double ov = __shfl_down_sync(0xffffffffu, v, o);
+            int oi = __shfl_down_sync(0xffffffffu, idx, o);
+            if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+        }
+        if (lane == 0) { *out_v = v; *out_i = idx; }
+    }
+    __syncthreads();
+}
+
+__device__ void lu_apply(const double *__restrict__ LU, const int *__restrict__ perm, int n1, double *__restrict__ y,
+                         double *__restrict__ tmp) {
+    // solve (P L U) z = y in place; y is overwritten with z.  Serial substitution
+    // over rows, inner dot products spread over the block.
+    __shared__ double red[kLU / 32];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < n1; ++k) {
+            int p = perm[k];
+            if (p != k) { double t = y[k]; y[k] = y[p]; y[p] = t; }
+        }
+    __syncthreads();
+    for (int i = 0; i < n1; ++i) {  // forward: L unit lower
+        double s = 0.0;
+        for (int c = threadIdx.x; c < i; c += kLU) s += LU[(size_t)i * n1 + c] * y[c];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < kLU / 32; ++w) t += red[w];
+            y[i] -= t;
+        }
+        __syncthreads();
+    }
+    for (int i = n1 - 1; i >= 0; --i) {  // backward: U
+        double s = 0.0;
+        for (int c = i + 1 + threadIdx.x; c < n1; c += kLU) s += LU[(size_t)i * n1 + c] * y[c];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < kLU / 32; ++w) t += red[w];
+            y[i] = (y[i] - t) / LU[(size_t)i * n1 + i];
+        }
+        __syncthreads();
+    }
+    (void)tmp;
+}
+
+__global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *__restrict__ descs) {
+    const SolveDesc d = descs[blockIdx.x];
+    const int n1 = d.n + 1;
+    double *A = d.As;
+    __shared__ double sv[kLU / 32];
+    __shared__ int si[kLU / 32];
+    __shared__ double piv_v;
+    __shared__ int piv_i;
+    double pmin = 1e308, pmax = 0.0;
+    int singular = 0;
+    for (int k = 0; k < n1; ++k) {
+        double best = -1.0;
+        int bi = 0x7fffffff;
+        for (int r = k + threadIdx.x; r < n1; r += kLU) {
+            double v = fabs(A[(size_t)r * n1 + k]);
+            if (v > best || (v == best && r < bi)) { best = v; bi = r; }
+        }
+        block_argmax(best, bi, sv, si, &piv_v, &piv_i);
+        const int p = piv_i;
+        if (threadIdx.x == 0) d.perm[k] = p;
+        if (p != k)
+            for (int c = threadIdx.x; c < n1; c += kLU) {
+                double t = A[(size_t)k * n1 + c];
+                A[(size_t)k * n1 + c] = A[(size_t)p * n1 + c];
+                A[(size_t)p * n1 + c] = t;
+            }
+        __syncthreads();
+        double pv = A[(size_t)k * n1 + k];
+        double apv = fabs(pv);
+        pmin = fmin(pmin, apv);
+        pmax = fmax(pmax, apv);
+        if (!(apv > 1e-300)) {  // exactly singular: keep going with a tiny pivot, flag it
+            singular = 1;
+            pv = (pv < 0 ? -1e-300 : 1e-300);
+            if (threadIdx.x == 0) A[(size_t)k * n1 + k] = pv;
+        }
+        __syncthreads();
+        const double inv = 1.0 / pv;
+        for (int r = k + 1 + threadIdx.x; r < n1; r += kLU) A[(size_t)r * n1 + k] *= inv;
+        __syncthreads();
+        const int m = n1 - k - 1;
+        const long long tot = (long long)m * m;
+        for (long long t = threadIdx.x; t < tot; t += kLU) {
+            int rr = k + 1 + (int)(t / m), cc = k + 1 + (int)(t - (long long)(t / m) * m);
+            A[(size_t)rr * n1 + cc] -= A[(size_t)rr * n1 + k] * A[(size_t)k * n1 + cc];
+        }
+        __syncthreads();
+    }
+    // x = LU^{-1} bs
+    for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] = d.bs[t];
+    lu_apply(A, d.perm, n1, d.x, d.r);
+    // one step of FP64 iterative refinement with the original matrix
+    for (int rr = threadIdx.x; rr < n1; rr += kLU) {
+        double s = d.bs[rr];
+        const double *row = d.A0 + (size_t)rr * n1;
+        for (int c = 0; c < n1; ++c) s -= row[c] * d.x[c];
+        d.r[rr] = s;
+    }
+    lu_apply(A, d.perm, n1, d.r, nullptr);
+    for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] += d.r[t];
+    __syncthreads();
+    // residual after refinement (inf-norm), for the report
+    double rmax = 0.0;
+    for (int rr = threadIdx.x; rr < n1; rr += kLU) {
+        double s = d.bs[rr];
+        const double *row = d.A0 + (size_t)rr * n1;
+        for (int c = 0; c < n1; ++c) s -= row[c] * d.x[c];
+        rmax = fmax(rmax, fabs(s));
+    }
+    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_down_sync(0xffffffffu, rmax, o));
+    if ((threadIdx.x & 31) == 0) sv[threadIdx.x >> 5] = rmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kLU / 32; ++w) t = fmax(t, sv[w]);
+        d.info[0] = t;
+        d.info[1] = pmin;
+        d.info[2] = pmax;
+        d.info[3] = singular;
+    }
+    // expand to all atoms
+    for (int i = threadIdx.x; i < d.N; i += kLU) d.q[i] = d.x[d.map[i]];
+}
+
+}  // namespace
+
+// Host side: reduced-index maps (repeat.py:2445-2470 semantics).
+struct FoldPlan {
+    int n = 0;
+    std::vector<int> map, mem_ptr, mem_idx, ind;
+    bool disjoint = true;
+};
+
+static FoldPlan make_plan(int N, int n_groups, const int *gptr, const int *gidx) {
+    FoldPlan p;
+    std::vector<char> linked((size_t)N, 0);
+    std::vector<int> seen((size_t)N, 0);
+    for (int g = 0; g < n_groups; ++g) {
+        for (int t = gptr[g]; t < gptr[g + 1]; ++t) {
+            int a = gidx[t];
+            RP_REQUIRE(a >= 0 && a < N, "rp_solve: group atom index out of range");
+            if (seen[a]++) p.disjoint = false;
+            if (t > gptr[g]) linked[a] = 1;
+        }
+    }
+    p.map.assign((size_t)N, -1);
+    for (int i = 0; i < N; ++i)
+        if (!linked[i]) {
+            p.map[i] = (int)p.ind.size();
+            p.ind.push_back(i);
+        }
+    p.n = (int)p.ind.size();
+    std::vector<std::vector<int>> mem((size_t)p.n);
+    for (int r = 0; r < p.n; ++r) mem[r].push_back(p.ind[r]);
+    for (int g = 0; g < n_groups; ++g) {
+        int base = gidx[gptr[g]];
+        for (int t = gptr[g] + 1; t < gptr[g + 1]; ++t) {
+            int l = gidx[t];
+            if (p.map[base] >= 0) {
+                mem[p.map[base]].push_back(l);
+                p.map[l] = p.map[base];
+            }
+        }
+    }
+    // linked atoms whose base is itself linked (chains) take the final base's value
+    for (int pass = 0; pass < n_groups + 1; ++pass) {
+        bool changed = false;
+        for (int g = 0; g < n_groups; ++g) {
+            int base = gidx[gptr[g]];
+            for (int t = gptr[g] + 1; t < gptr[g + 1]; ++t)
+                if (p.map[gidx[t]] != p.map[base] && p.map[base] >= 0) {
+                    p.map[gidx[t]] = p.map[base];
+                    changed = true;
+                }
+        }
+        if (!changed) break;
+    }
+    p.mem_ptr.push_back(0);
+    for (auto &m : mem) {
+        p.mem_idx.insert(p.mem_idx.end(), m.begin(), m.end());
+        p.mem_ptr.push_back((int)p.mem_idx.size());
+    }
+    return p;
+}
+
+// Exact sequential folding on the host for overlapping groups.
+static void host_fold(int N, const std::vector<double> &A, const std::vector<double> &b, int n_groups, const int *gptr,
+                      const int *gidx, const FoldPlan &p, std::vector<double> &Ar, std::vector<double> &br,
+                      std::vector<double> &w) {
+    std::vector<double> AA(A), bb(b), ww((size_t)N, 1.0);
+    for (int g = 0; g < n_groups; ++g) {
+        int base = gidx[gptr[g]];
+        for (int t = gptr[g] + 1; t < gptr[g + 1]; ++t) {
+            int l = gidx[t];
+            bb[base] += bb[l];
+            ww[base] += 1.0;
+            for (int r = 0; r < N; ++r) AA[(size_t)r * N + base] += AA[(size_t)r * N + l];
+        }
+    }
+    for (int g = 0; g < n_groups; ++g) {
+        int base = gidx[gptr[g]];
+        for (int t = gptr[g] + 1; t < gptr[g + 1]; ++t) {
+            int l = gidx[t];
+            for (int c = 0; c < N; ++c) AA[(size_t)base * N + c] += AA[(size_t)l * N + c];
+        }
+    }
+    Ar.assign((size_t)p.n * p.n, 0.0);
+    br.assign((size_t)p.n, 0.0);
+    w.assign((size_t)p.n, 0.0);
+    for (int r = 0; r < p.n; ++r) {
+        for (int c = 0; c < p.n; ++c) Ar[(size_t)r * p.n + c] = AA[(size_t)p.ind[r] * N + p.ind[c]];
+        br[r] = bb[p.ind[r]];
+        w[r] = ww[p.ind[r]];
+    }
+}
+
+void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
+               const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,
+               double *info, cudaStream_t stream) {
+    RP_REQUIRE(A_dev && b_dev && q_dev && N > 0, "rp_solve: null argument or N <= 0");
+    RP_REQUIRE(n_groups == 0 || (group_ptr && group_idx), "rp_solve: groups given without arrays");
+    FoldPlan p = make_plan(N, n_groups, group_ptr, group_idx);
+    const int n1 = p.n + 1;
+    std::vector<double> rs, rt;
+    if (resp_s) {
+        rs.assign((size_t)p.n, 0.0);
+        rt.assign((size_t)p.n, 0.0);
+        for (int r = 0; r < p.n; ++r) {
+            rs[r] = resp_s[p.ind[r]];
+            rt[r] = resp_t ? resp_t[p.ind[r]] : 0.0;
+        }
+    }
+    int *d_map = ctx->buf_t<int>("s_map", (size_t)N);
+    int *d_mptr = ctx->buf_t<int>("s_mptr", p.mem_ptr.size());
+    int *d_midx = ctx->buf_t<int>("s_midx", std::max<size_t>(p.mem_idx.size(), 1));
+    double *d_rs = resp_s ? ctx->buf_t<double>("s_rs", (size_t)p.n) : nullptr;
+    double *d_rt = resp_s ? ctx->buf_t<double>("s_rt", (size_t)p.n) : nullptr;
+    double *As = ctx->buf_t<double>("s_As", (size_t)n1 * n1);
+    double *A0 = ctx->buf_t<double>("s_A0", (size_t)n1 * n1);
+    double *bs = ctx->buf_t<double>("s_bs", (size_t)n1);
+    double *x = ctx->buf_t<double>("s_x", (size_t)n1);
+    double *r = ctx->buf_t<double>("s_r", (size_t)n1);
+    int *perm = ctx->buf_t<int>("s_perm", (size_t)n1);
+    double *d_info = ctx->buf_t<double>("s_info", 4);
+    SolveDesc *d_desc = ctx->buf_t<SolveDesc>("s_desc", 1);
+    RP_CUDA(cudaMemcpyAsync(d_map, p.map.data(), sizeof(int) * N, cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_mptr, p.mem_ptr.data(), sizeof(int) * p.mem_ptr.size(), cudaMemcpyHostToDevice, stream));
+    if (!p.mem_idx.empty())
+        RP_CUDA(cudaMemcpyAsync(d_midx, p.mem_idx.data(), sizeof(int) * p.mem_idx.size(), cudaMemcpyHostToDevice, stream));
+    if (resp_s) {
+        RP_CUDA(cudaMemcpyAsync(d_rs, rs.data(), sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
+        RP_CUDA(cudaMemcpyAsync(d_rt, rt.data(), sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
+    }
+    SolveDesc d{};
+    d.A = A_dev; d.b = b_dev; d.N = N; d.n = p.n; d.mem_ptr = d_mptr; d.mem_idx = d_midx;
+    d.resp_s = d_rs; d.resp_t = d_rt; d.map = d_map; d.qtot = qtot;
+    d.As = As; d.A0 = A0; d.bs = bs; d.x = x; d.r = r; d.perm = perm; d.q = q_dev; d.info = d_info;
+    if (p.disjoint) {
+        build_bordered_kernel<<<ceil_div((long long)n1 * n1, 256) > 4096 ? 4096 : ceil_div((long long)n1 * n1, 256), 256,
+                                0, stream>>>(d);
+        RP_LAUNCH_CHECK();
+    } else {
+        // overlapping groups: reference's sequential folding on the host
+        std::vector<double> hA((size_t)N * N), hb((size_t)N), Ar, br, w;
+        RP_CUDA(cudaMemcpyAsync(hA.data(), A_dev, sizeof(double) * hA.size(), cudaMemcpyDeviceToHost, stream));
+        RP_CUDA(cudaMemcpyAsync(hb.data(), b_dev, sizeof(double) * N, cudaMemcpyDeviceToHost, stream));
+        RP_CUDA(cudaStreamSynchronize(stream));
+        host_fold(N, hA, hb, n_groups, group_ptr, group_idx, p, Ar, br, w);
+        std::vector<double> hs((size_t)n1 * n1, 0.0), hbs((size_t)n1, 0.0);
+        for (int rr = 0; rr < p.n; ++rr) {
+            for (int c = 0; c < p.n; ++c) hs[(size_t)rr * n1 + c] = Ar[(size_t)rr * p.n + c];
+            if (resp_s) hs[(size_t)rr * n1 + rr] += rs[rr];
+            hs[(size_t)rr * n1 + p.n] = w[rr];
+            hs[(size_t)p.n * n1 + rr] = w[rr];
+            hbs[rr] = br[rr] + (resp_s ? rs[rr] * rt[rr] : 0.0);
+        }
+        hbs[p.n] = qtot;
+        RP_CUDA(cudaMemcpyAsync(As, hs.data(), sizeof(double) * hs.size(), cudaMemcpyHostToDevice, stream));
+        RP_CUDA(cudaMemcpyAsync(A0, hs.data(), sizeof(double) * hs.size(), cudaMemcpyHostToDevice, stream));
+        RP_CUDA(cudaMemcpyAsync(bs, hbs.data(), sizeof(double) * hbs.size(), cudaMemcpyHostToDevice, stream));
+        RP_CUDA(cudaStreamSynchronize(stream));
+    }
+    RP_CUDA(cudaMemcpyAsync(d_desc, &d, sizeof(SolveDesc), cudaMemcpyHostToDevice, stream));
+    lu_solve_refine_kernel<<<1, kLU, 0, stream>>>(d_desc);
+    RP_LAUNCH_CHECK();
+    double hinfo[4];
+    RP_CUDA(cudaMemcpyAsync(hinfo, d_info, sizeof(hinfo), cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaStreamSynchronize(stream));
+    if (info) {
+        info[0] = hinfo[0];
+        info[1] = hinfo[1];
+        info[2] = hinfo[2];
+    }
+    if (hinfo[3] != 0.0) fail(RP_E_SINGULAR, "rp_solve: bordered system is singular (zero pivot)");
+}
+
+}  // namespace rp

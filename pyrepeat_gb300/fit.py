@@ -1,0 +1,202 @@
+"""Device-side fit pipeline: filter -> Ewald setup -> normal equations -> solve.
+
+``Context`` owns one ``rp_ctx`` (scratch HBM, cuBLAS handle) on one device.
+``fit_cube`` runs one whole fit with the cube's grid values already on the
+device (or copies them there); ``fit_host`` is the end-to-end path from host
+memory through the C ABI's ``rp_fit``.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from .constants import z_to_symbol
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("pyrepeat_gb300 needs a CUDA device (no CPU fallback)")
+    return torch
+
+
+@dataclass
+class FitResult:
+    charges: np.ndarray
+    n_kept: int
+    precision: str
+    A: object = None          # torch tensor (N, N) on the device, mean-removed normal matrix
+    b: object = None          # torch tensor (N,)
+    info: dict = field(default_factory=dict)
+
+
+def constraint_arrays(Z, symm_groups=None, resp=None):
+    """CSR symmetry groups (0-based, base first) and per-atom RESP arrays."""
+    N = len(Z)
+    groups = [list(g) for g in (symm_groups or []) if len(g) >= 1]
+    ptr = np.zeros(len(groups) + 1, dtype=np.int32)
+    idx = []
+    for i, g in enumerate(groups):
+        idx.extend(int(x) for x in g)
+        ptr[i + 1] = len(idx)
+    idx = np.asarray(idx if idx else [0], dtype=np.int32)
+    rs = rt = None
+    if resp:
+        rs = np.zeros(N); rt = np.zeros(N)
+        for i, z in enumerate(Z):
+            sym = z_to_symbol(int(z))
+            if sym in resp:
+                s, t = resp[sym]
+                rs[i], rt[i] = float(s), float(t)
+    return len(groups), ptr, idx, rs, rt
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class Context:
+    """One rp_ctx on one CUDA device."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self.torch = _torch()
+        self.lib = _lib.load()
+        self.device = device
+        self.dev = self.torch.device(f"cuda:{device}")
+        self.torch.cuda.set_device(self.device)
+        p = ctypes.c_void_p()
+        rc = self.lib.rp_ctx_create(device, hbm_budget, ctypes.byref(p))
+        if rc != 0:
+            raise _lib.RepeatError(rc, "rp_ctx_create failed")
+        self.ptr = p
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.lib.rp_ctx_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _stream(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def check(self, rc, what=""):
+        _lib.check(self.ptr, rc, what)
+
+    # ------------------------------------------------------------------ stages
+    def filter(self, n_grid, axis, atoms, Z, V_dev, vdw_factor=1.0, vdw_max=1000.0, want_mask=False):
+        t = self.torch
+        n = int(np.prod(n_grid))
+        kept = t.empty(n, dtype=t.int32, device=self.dev)
+        Vc = t.empty(n, dtype=t.float64, device=self.dev)
+        mask = t.empty(n, dtype=t.uint8, device=self.dev) if want_mask else None
+        M = ctypes.c_int64(0)
+        g = _lib.make_grid(n_grid, axis)
+        atoms = np.ascontiguousarray(atoms, dtype=np.float64)
+        Zi = np.ascontiguousarray(Z, dtype=np.int32)
+        rc = self.lib.rp_filter(self.ptr, ctypes.byref(g), atoms.ctypes.data, Zi.ctypes.data, len(Zi),
+                                V_dev.data_ptr(), float(vdw_factor), float(vdw_max), kept.data_ptr(),
+                                Vc.data_ptr(), n, ctypes.byref(M), mask.data_ptr() if want_mask else None,
+                                self._stream())
+        self.check(rc, "rp_filter")
+        m = int(M.value)
+        return kept[:m], Vc[:m], m, mask
+
+    def ewald(self, n_grid, axis, cutoff=20.0, kmax=7):
+        return Ewald(self, n_grid, axis, cutoff, kmax)
+
+    def gram(self, ew, atoms, kept, Vc, precision=_lib.PREC_MIXED, want_sum_phi=False):
+        t = self.torch
+        atoms = np.ascontiguousarray(atoms, dtype=np.float64)
+        N = len(atoms)
+        A = t.empty((N, N), dtype=t.float64, device=self.dev)
+        b = t.empty(N, dtype=t.float64, device=self.dev)
+        sp = t.empty(N, dtype=t.float64, device=self.dev) if want_sum_phi else None
+        rc = self.lib.rp_gram(self.ptr, ew.ptr, atoms.ctypes.data, N, kept.data_ptr(), Vc.data_ptr(),
+                              int(kept.numel()), int(precision), A.data_ptr(), b.data_ptr(),
+                              sp.data_ptr() if sp is not None else None, self._stream())
+        self.check(rc, "rp_gram")
+        return A, b, sp
+
+    def solve(self, A, b, Z, symm_groups=None, resp=None, qtot=0.0):
+        t = self.torch
+        N = int(b.numel())
+        ng, ptr, idx, rs, rt = constraint_arrays(Z, symm_groups, resp)
+        q = t.empty(N, dtype=t.float64, device=self.dev)
+        info = np.zeros(3)
+        rc = self.lib.rp_solve(self.ptr, A.data_ptr(), b.data_ptr(), N, ng, ptr.ctypes.data, idx.ctypes.data,
+                               _ptr(rs), _ptr(rt), float(qtot), q.data_ptr(), info.ctypes.data, self._stream())
+        self.check(rc, "rp_solve")
+        return q, {"residual": float(info[0]), "pivot_min": float(info[1]), "pivot_max": float(info[2])}
+
+    # ------------------------------------------------------------------ whole fits
+    def fit_cube(self, cube, precision=_lib.PREC_MIXED, V_dev=None, keep_normal=False):
+        """Fit one synth.Cube-like object (atom_index, atom_pos, n_grid, axis_vector, V,
+        symm_groups, resp, kmax, cutoff, vdw_factor, vdw_max, total_charge)."""
+        t = self.torch
+        if V_dev is None:
+            V_dev = t.from_numpy(np.ascontiguousarray(cube.V, dtype=np.float64)).to(self.dev)
+        kept, Vc, M, _ = self.filter(cube.n_grid, cube.axis_vector, cube.atom_pos, cube.atom_index, V_dev,
+                                     cube.vdw_factor, cube.vdw_max)
+        if M == 0:
+            raise _lib.RepeatError(-1, "no grid point survives the vdW filter")
+        ew = self.ewald(cube.n_grid, cube.axis_vector, cube.cutoff, cube.kmax)
+        try:
+            A, b, _ = self.gram(ew, cube.atom_pos, kept, Vc, precision)
+        finally:
+            ew.close()
+        q, info = self.solve(A, b, cube.atom_index, cube.symm_groups, cube.resp, cube.total_charge)
+        res = FitResult(q.cpu().numpy(), M, "fp64" if precision == _lib.PREC_FP64 else "mixed", info=info)
+        if keep_normal:
+            res.A, res.b = A, b
+        return res
+
+    def fit_host(self, cube, precision=_lib.PREC_MIXED):
+        """End to end through rp_fit: host V and atoms in, host charges out."""
+        d = _lib.RpFitDesc()
+        d.grid = _lib.make_grid(cube.n_grid, cube.axis_vector)
+        V = np.ascontiguousarray(cube.V, dtype=np.float64)
+        atoms = np.ascontiguousarray(cube.atom_pos, dtype=np.float64)
+        Z = np.ascontiguousarray(cube.atom_index, dtype=np.int32)
+        ng, ptr, idx, rs, rt = constraint_arrays(Z, cube.symm_groups, cube.resp)
+        d.V, d.atoms, d.Z, d.N = V.ctypes.data, atoms.ctypes.data, Z.ctypes.data, len(Z)
+        d.vdw_factor, d.vdw_max, d.cutoff, d.qtot = cube.vdw_factor, cube.vdw_max, cube.cutoff, cube.total_charge
+        d.kmax, d.n_groups = cube.kmax, ng
+        d.group_ptr, d.group_idx, d.resp_s, d.resp_t = ptr.ctypes.data, idx.ctypes.data, _ptr(rs), _ptr(rt)
+        d.precision = int(precision)
+        q = np.zeros(len(Z))
+        M = ctypes.c_int64(0)
+        rc = self.lib.rp_fit(self.ptr, ctypes.byref(d), q.ctypes.data, ctypes.byref(M), self._stream())
+        self.check(rc, "rp_fit")
+        return FitResult(q, int(M.value), "fp64" if precision == _lib.PREC_FP64 else "mixed")
+
+
+class Ewald:
+    def __init__(self, ctx: Context, n_grid, axis, cutoff, kmax):
+        self.ctx = ctx
+        p = ctypes.c_void_p()
+        g = _lib.make_grid(n_grid, axis)
+        ctx.check(ctx.lib.rp_ewald_setup(ctx.ptr, ctypes.byref(g), float(cutoff), int(kmax), ctypes.byref(p)),
+                  "rp_ewald_setup")
+        self.ptr = p
+        K, S, al = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        ctx.lib.rp_ewald_info(p, ctypes.byref(K), ctypes.byref(S), ctypes.byref(al))
+        self.K, self.S, self.alpha = K.value, S.value, al.value
+
+    def close(self):
+        if self.ptr:
+            self.ctx.lib.rp_ewald_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

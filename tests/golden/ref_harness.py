@@ -1,0 +1,37 @@
+"""Import the reference ``repeat.py`` for fixture generation (this container only).
+
+Two adjustments, neither of which edits the reference:
+
+* ``scipy.spatial.erfc = scipy.special.erfc``: ``repeat.py:965`` calls
+  ``spatial.erfc``, which SciPy does not have, so the NumPy (``--no-jit``) path
+  raises AttributeError without this alias.
+* The per-atom Phi columns and the CPU filter run on the reference's thread
+  strategy (``nogil_threads``, ``repeat.py:1145-1197``, ``2049-2055``) instead
+  of its forkserver/spawn process pools: the arithmetic per column and per
+  layer is the same code, and process pools cannot re-import a ``__main__``
+  that is not a file.
+
+Bytecode writes are disabled so nothing is written under the reference tree.
+"""
+import os
+import sys
+
+REFERENCE_DIR = os.environ.get("PYREPEAT_REFERENCE", "/root/reference")
+
+
+def load_reference():
+    sys.dont_write_bytecode = True
+    import scipy.spatial
+    import scipy.special
+    scipy.spatial.erfc = scipy.special.erfc
+    if REFERENCE_DIR not in sys.path:
+        sys.path.insert(0, REFERENCE_DIR)
+    import repeat as R  # noqa: E402
+    R._NOGIL_ENABLED = True
+    workers = max(1, os.cpu_count() or 1)
+
+    def _threads(n_grid, n_atoms, use_jit=True, force_strategy=None, prefer_gpu=None):
+        return "nogil_threads", workers, False, 0
+
+    R.select_parallel_strategy = _threads
+    return R

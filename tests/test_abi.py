@@ -1,0 +1,49 @@
+"""The C-ABI library builds, loads, and exports every symbol the headers declare."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    out = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            text = open(os.path.join(inc, f)).read()
+            out.update(re.findall(r"^\s*int\s+(rp_\w+)\s*\(", text, flags=re.M))
+    return out
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ("rp_version", "rp_ctx_create", "rp_filter", "rp_ewald_setup", "rp_gram", "rp_solve", "rp_fit"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol():
+    from pyrepeat_gb300 import _lib
+    from pyrepeat_gb300.build import build_cuda
+    build_cuda()
+    L = ctypes.CDLL(_lib.LIB_PATH)
+    missing = [s for s in declared_symbols() if not hasattr(L, s)]
+    assert not missing, missing
+    assert set(_lib.EXPORTS) >= declared_symbols()
+
+
+def test_version_without_gpu():
+    from pyrepeat_gb300 import _lib
+    assert _lib.load().rp_version() >= 10000
+
+
+def test_ctx_create_without_gpu_fails_cleanly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from pyrepeat_gb300 import _lib
+    p = ctypes.c_void_p()
+    rc = _lib.load().rp_ctx_create(0, 0, ctypes.byref(p))
+    assert rc == -2 and not p.value
