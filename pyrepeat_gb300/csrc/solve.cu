@@ -287,6 +287,8 @@ static FoldPlan make_plan(int N, int n_groups, const int *gptr, const int *gidx)
         }
         if (!changed) break;
     }
+    for (int i = 0; i < N; ++i)
+        RP_REQUIRE(p.map[i] >= 0 && p.map[i] < p.n, "rp_solve: symmetry groups link atoms in a cycle");
     p.mem_ptr.push_back(0);
     for (auto &m : mem) {
         p.mem_idx.insert(p.mem_idx.end(), m.begin(), m.end());
