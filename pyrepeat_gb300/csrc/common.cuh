@@ -109,6 +109,11 @@ struct rp_ewald {
     int *d_kidx = nullptr;        // 3K
     double *d_kcoef = nullptr;    // K
     double *d_kvec = nullptr;     // 3K
+    // the same k-set ordered by increasing kcoef (used by the tensor-core path so
+    // that small terms are accumulated before large ones)
+    int *d_kidx_s = nullptr;
+    double *d_kcoef_s = nullptr;
+    double *d_kvec_s = nullptr;
     double2 *d_ex = nullptr;      // (kmax+1) * nx   e^{2 pi i n1 i / nx}
     double2 *d_ey = nullptr;      // (2kmax+1) * ny  e^{2 pi i n2 j / ny}, n2 offset by kmax
     double2 *d_ez = nullptr;      // (2kmax+1) * nz

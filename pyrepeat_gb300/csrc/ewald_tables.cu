@@ -107,6 +107,26 @@ void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax) {
     RP_CUDA(cudaMemcpy(ew->d_kidx, ew->kidx.data(), sizeof(int) * ew->kidx.size(), cudaMemcpyHostToDevice));
     RP_CUDA(cudaMemcpy(ew->d_kcoef, ew->kcoef.data(), sizeof(double) * ew->kcoef.size(), cudaMemcpyHostToDevice));
     RP_CUDA(cudaMemcpy(ew->d_kvec, ew->kvec.data(), sizeof(double) * ew->kvec.size(), cudaMemcpyHostToDevice));
+    {
+        std::vector<int> perm((size_t)ew->K);
+        for (int k = 0; k < ew->K; ++k) perm[k] = k;
+        std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return ew->kcoef[x] < ew->kcoef[y]; });
+        std::vector<int> ki((size_t)3 * ew->K);
+        std::vector<double> kc((size_t)ew->K), kv((size_t)3 * ew->K);
+        for (int k = 0; k < ew->K; ++k) {
+            kc[k] = ew->kcoef[perm[k]];
+            for (int d = 0; d < 3; ++d) {
+                ki[3 * k + d] = ew->kidx[3 * perm[k] + d];
+                kv[3 * k + d] = ew->kvec[3 * perm[k] + d];
+            }
+        }
+        RP_CUDA(cudaMalloc(&ew->d_kidx_s, sizeof(int) * ki.size()));
+        RP_CUDA(cudaMalloc(&ew->d_kcoef_s, sizeof(double) * kc.size()));
+        RP_CUDA(cudaMalloc(&ew->d_kvec_s, sizeof(double) * kv.size()));
+        RP_CUDA(cudaMemcpy(ew->d_kidx_s, ki.data(), sizeof(int) * ki.size(), cudaMemcpyHostToDevice));
+        RP_CUDA(cudaMemcpy(ew->d_kcoef_s, kc.data(), sizeof(double) * kc.size(), cudaMemcpyHostToDevice));
+        RP_CUDA(cudaMemcpy(ew->d_kvec_s, kv.data(), sizeof(double) * kv.size(), cudaMemcpyHostToDevice));
+    }
     RP_CUDA(cudaMemcpy(ew->d_ex, ex.data(), sizeof(double2) * ex.size(), cudaMemcpyHostToDevice));
     RP_CUDA(cudaMemcpy(ew->d_ey, ey.data(), sizeof(double2) * ey.size(), cudaMemcpyHostToDevice));
     RP_CUDA(cudaMemcpy(ew->d_ez, ez.data(), sizeof(double2) * ez.size(), cudaMemcpyHostToDevice));
@@ -116,6 +136,9 @@ void ewald_free(rp_ewald *ew) {
     cudaFree(ew->d_kidx);
     cudaFree(ew->d_kcoef);
     cudaFree(ew->d_kvec);
+    cudaFree(ew->d_kidx_s);
+    cudaFree(ew->d_kcoef_s);
+    cudaFree(ew->d_kvec_s);
     cudaFree(ew->d_ex);
     cudaFree(ew->d_ey);
     cudaFree(ew->d_ez);

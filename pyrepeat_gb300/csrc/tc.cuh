@@ -48,17 +48,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 // ~2 s at 2 GHz; a healthy wait here lasts microseconds
 constexpr long long kWaitBudgetCycles = 4000000000LL;
 
-// Bounded wait on a phase parity. Returns false (and records a timeout) when the
-// budget runs out or another thread of the kernel already gave up.
+// Bounded wait on a phase parity. Returns false when the budget runs out or
+// (with a status word) another thread of the kernel already gave up; a timeout
+// is recorded in *status.  status may be null (unwinding: wait, record nothing).
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status) {
     if (mbar_try_wait(bar, parity)) return true;
     long long t0 = clock64();
     for (uint32_t it = 1;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 255u) == 0) {
-            if (*reinterpret_cast<volatile int *>(status) != 0) return false;
+            if (status && *reinterpret_cast<volatile int *>(status) != 0) return false;
             if (clock64() - t0 > kWaitBudgetCycles) {
-                atomicCAS(status, 0, RP_E_TIMEOUT);
+                if (status) atomicCAS(status, 0, RP_E_TIMEOUT);
                 return false;
             }
         }
