@@ -1,0 +1,391 @@
+#!/usr/bin/env python3
+"""Benchmark of the periodic REPEAT charge fit on GB300.
+
+Workload (default): the batched configuration — 256 independent seeded cubes
+(20-300 atoms, cubic or orthorhombic 12-30 Bohr cells, 40^3-96^3 grids at
+0.2-0.3 Bohr, neutral charges N(0, 0.5), ESP = Ewald potential + N(0, 1e-4),
+half with symmetry groups, half with RESP), fitted by one ``rp_fit_batch`` call
+per step: every filter, the normal equations of every cube and one launch of
+all bordered solves.  A step is one batch; ``value`` is fits/s with the grids
+resident in HBM, ``e2e`` the same through the public API from pinned host
+memory (H2D of every grid and D2H of the charges inside the timed region).
+
+Beside it, in the same run: the plain FP64 GPU fit of a subset of the cubes
+(fits/s and max|dq| of the mixed path against it), single-fit p50/p99 latency,
+the dominant kernel's roofline from live CUDA-event stage timings, SM clocks
+sampled during the timed region, and the CPU oracle timed on a bounded sample.
+
+``--impl reference`` times the reference algorithm on the host cores (the C
+oracle restatement of repeat.py / repeat_cpu_omp.cpp; the reference's own
+compiled program cannot be built where its sources are absent).
+
+Multi-GPU (torchrun): every rank fits its own 256 cubes (weak scaling, no
+data-path collective); the step time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fits/s & p50/p99 latency vs plain FP64 GPU fit at max|dq|<=1e-5 e"
+
+
+# ----------------------------------------------------------------------------- distributed helpers
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            backend = os.environ.get("REPEAT_BENCH_BACKEND", "nccl")
+            if backend == "nccl":
+                import torch
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    """Largest value over all ranks (the step time of a weak-scaled job)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                smax.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- workloads
+
+def make_workload(name: str, n_cubes: int, seed0: int, ctx):
+    from pyrepeat_gb300 import synth
+    if name == "batch":
+        return [synth.make_batch_item(seed0 + i, ctx=ctx) for i in range(n_cubes)], (
+            f"batch-{n_cubes}: {n_cubes} independent cubes, 20-300 atoms, cubic/orthorhombic 12-30 Bohr, "
+            f"40^3-96^3 grids at 0.2-0.3 Bohr, KMAX 7 (K=754), Rc 20, half symmetry groups, half RESP")
+    if name == "mof":
+        return [synth.make_mof(seed0, ctx=ctx)], "mof: cubic 25.8 Bohr, 128^3 grid, 424 atoms, KMAX 12 (K=3779)"
+    if name == "water":
+        return [synth.make_water(seed0, ctx=ctx)], "water: cubic 18 Bohr, 72^3 grid, 9 atoms, K=754"
+    raise SystemExit(f"unknown workload {name}")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 1900.0, 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------- CPU oracle timing
+
+def cpu_oracle_sample(cube, sample: int, threads: int):
+    """Time the C oracle (restatement of the reference fit) on `sample` kept points
+    of one cube; returns (seconds, sample, kept count of the cube)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    cube.host_V()
+    of = oracle.OracleFit(cube, threads=threads, sample=sample, seed=0)
+    t0 = time.perf_counter()
+    of.fit()
+    dt = time.perf_counter() - t0
+    return dt, min(sample, of.M_total), of.M_total
+
+
+def reference_arm(args, world, rank):
+    """Reference CPU implementation of the path on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    import torch
+    threads = max(1, os.cpu_count() or 1)
+    ctx = None
+    if torch.cuda.is_available():
+        from pyrepeat_gb300.fit import Context
+        ctx = Context(0)
+    cubes, desc = make_workload(args.workload, min(args.n_cubes, 8), 1000, ctx)
+    sample = args.cpu_sample
+    times = []
+    for step in range(args.warmup + args.steps):
+        c = cubes[step % len(cubes)]
+        dt, s, M = cpu_oracle_sample(c, sample, threads)
+        if step >= args.warmup:
+            times.append(dt * M / s)   # seconds for the whole cube, linear in kept points
+    per_fit = statistics.mean(times)
+    value = 1.0 / per_fit
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_fit * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc},
+        "cpu_baseline": {"value": value, "unit": "fits/s", "cores": threads, "kind": "port",
+                         "sample": f"one cube per step, {sample} seeded kept points, extrapolated linearly to "
+                                   f"the cube's kept count"},
+        "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU arm
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "mof", "water"])
+    ap.add_argument("--n-cubes", type=int, default=256)
+    ap.add_argument("--fp64-cubes", type=int, default=8, help="cubes of the plain FP64 comparator")
+    ap.add_argument("--latency-fits", type=int, default=32, help="single fits timed for p50/p99")
+    ap.add_argument("--cpu-sample", type=int, default=2000, help="kept points of the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+        return
+
+    import torch
+    from pyrepeat_gb300 import _lib
+    from pyrepeat_gb300.fit import Context
+    torch.cuda.set_device(local)
+    ctx = Context(local)
+    dev = torch.device(f"cuda:{local}")
+
+    t0 = time.time()
+    cubes, desc = make_workload(args.workload, args.n_cubes, 1000 + 100000 * rank, ctx)
+    gen_s = time.time() - t0
+    n = len(cubes)
+    V_dev = [c.V_dev for c in cubes]
+    grid_bytes = sum(c.n_points * 8 for c in cubes)
+
+    def step(prec=_lib.PREC_MIXED, sel=None):
+        cs = cubes if sel is None else [cubes[i] for i in sel]
+        vs = V_dev if sel is None else [V_dev[i] for i in sel]
+        return ctx.fit_batch(cs, prec, V_dev=vs)
+
+    # warm-up
+    for _ in range(max(args.warmup, 1)):
+        q_mixed, M, info = step()
+    torch.cuda.synchronize()
+
+    # timed region: K batched steps, events on the stream the library runs on
+    clock = ClockSampler(local)
+    clock.start()
+    launches0 = _lib.launch_count()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        q_mixed, M, info = step()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    launches = _lib.launch_count() - launches0
+    clocks = clock.stop()
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(ms, world, dev)
+    value = n * args.steps * world / (ms / 1e3)
+    q_mixed = [q.copy() for q in q_mixed]
+
+    # end to end: grids from pinned host memory, charges back to the host
+    pinned = [c.V_dev.cpu().pin_memory() for c in cubes]
+    host_cubes = []
+    for c, p in zip(cubes, pinned):
+        hc = type(c)(**{k: getattr(c, k) for k in c.__dataclass_fields__})
+        hc.V = p.numpy()
+        hc.V_dev = None
+        host_cubes.append(hc)
+    qbuf = torch.zeros(sum(c.n_atoms for c in cubes), dtype=torch.float64).pin_memory().numpy()
+    ctx.fit_batch(host_cubes, _lib.PREC_MIXED, out=qbuf)
+    torch.cuda.synchronize()
+    barrier(world)
+    t_e2e = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.fit_batch(host_cubes, _lib.PREC_MIXED, out=qbuf)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t_e2e, world, dev)
+    e2e_value = n * args.steps * world / e2e_s
+
+    # plain FP64 GPU fit of a subset: speed and the accuracy of the mixed path against it
+    nf = min(args.fp64_cubes, n)
+    sel = list(range(nf))
+    step(_lib.PREC_FP64, sel[:1])
+    torch.cuda.synchronize()
+    tf = time.perf_counter()
+    q64, _, _ = step(_lib.PREC_FP64, sel)
+    torch.cuda.synchronize()
+    fp64_s = time.perf_counter() - tf
+    fp64_value = nf / fp64_s
+    mixed_sub = [q_mixed[i] for i in sel]
+    dq = max(float(np.abs(a - b).max()) for a, b in zip(mixed_sub, q64))
+    mixed_sub_value = None
+    tm = time.perf_counter()
+    step(_lib.PREC_MIXED, sel)
+    torch.cuda.synchronize()
+    mixed_sub_value = nf / (time.perf_counter() - tm)
+
+    # single-fit latency (each cube alone through the batch entry point)
+    lat = []
+    for i in range(min(args.latency_fits, n)):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        step(_lib.PREC_MIXED, [i])
+        b.record()
+        torch.cuda.synchronize()
+        lat.append(a.elapsed_time(b))
+    lat.sort()
+    p50 = lat[len(lat) // 2]
+    p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
+
+    # roofline of the dominant stage from live CUDA-event stage timings of one more step
+    ctx.set_timing(True)
+    ctx.stage_times()
+    step()
+    stages = ctx.stage_times()
+    ctx.set_timing(False)
+    bf16_peak, hbm_peak, peak_kind = peaks()
+    Ms = [int(m) for m in M]
+    from pyrepeat_gb300.fit import plan_kblocks_py
+    flops_float, flops_exact, flops_gram = 0.0, 0.0, 0.0
+    for c, m in zip(cubes, Ms):
+        ntop, nfloat = plan_kblocks_py(c)
+        flops_float += 2.0 * m * c.n_atoms * 2 * nfloat
+        flops_exact += 2.0 * m * c.n_atoms * 2 * ntop
+        flops_gram += 2.0 * m * (c.n_atoms + 1) ** 2 / 2
+    dom = max(stages.items(), key=lambda kv: kv[1][0]) if stages else ("none", (0.0, 0))
+    dom_name, (dom_ms, dom_n) = dom
+    algo = {"recip_gemm_f16x3": flops_float, "recip_gemm_exact_top": flops_exact, "gram_exact": flops_gram}
+    if dom_name in algo and dom_ms > 0:
+        achieved = algo[dom_name] / (dom_ms / 1e3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": achieved / bf16_peak, "traffic": None, "kernel": dom_name, "launches": dom_n,
+                "avg_launch_ms": dom_ms / max(dom_n, 1), "peak_kind": f"bf16 dense, {peak_kind}"}
+    else:
+        roof = {"bound": "hbm" if dom_name in ("filter", "center_slice") else "tensor", "achieved": None,
+                "peak": hbm_peak if dom_name in ("filter", "center_slice") else bf16_peak,
+                "unit": "GB/s" if dom_name in ("filter", "center_slice") else "TFLOP/s", "frac": None,
+                "traffic": None, "kernel": dom_name, "launches": dom_n, "avg_launch_ms": dom_ms / max(dom_n, 1)}
+    stage_share = {k: round(v[0], 3) for k, v in sorted(stages.items(), key=lambda kv: -kv[1][0])}
+
+    # CPU oracle on a bounded sample (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = max(1, os.cpu_count() or 1)
+        c0 = cubes[0]
+        dt, s, Mc = cpu_oracle_sample(c0, args.cpu_sample, threads)
+        per_cube = dt * Mc / s
+        mean_M = statistics.mean(Ms)
+        cpu_value = 1.0 / (per_cube * mean_M / Mc)
+        cpu = {"value": cpu_value, "unit": "fits/s", "cores": threads, "kind": "port",
+               "sample": f"cube 0 (N={c0.n_atoms}, M={Mc}), {s} seeded kept points, {dt:.2f} s; extrapolated "
+                         f"linearly to the batch's mean kept count {mean_M:.0f}"}
+
+    if rank != 0:
+        return
+    h2d = grid_bytes
+    d2h = sum(c.n_atoms for c in cubes) * 8
+    line = {
+        "metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f16-split+exact-int+f64",
+        "data": "synthetic: seeded cubes, ESP = Ewald potential of planted charges + N(0,1e-4) (rp_potential)",
+        "config": {"workload": desc, "n_cubes": n, "grid_bytes": grid_bytes,
+                   "l2": "inputs larger than L2 (%.2f GB of grids per step)" % (grid_bytes / 1e9),
+                   "generation_s": round(gen_s, 1)},
+        "p50_ms": p50, "p99_ms": p99, "latency": "single-fit, each cube alone through rp_fit_batch",
+        "fp64": {"fits_per_s": fp64_value, "cubes": nf, "mixed_fits_per_s_same_cubes": mixed_sub_value,
+                 "speedup": mixed_sub_value / fp64_value, "max_dq_mixed_vs_fp64_e": dq},
+        "e2e": {"value": e2e_value, "unit": "fits/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": roof,
+        "stage_ms_one_step": stage_share,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

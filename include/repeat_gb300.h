@@ -117,6 +117,15 @@ int rp_solve(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n
              const int *group_ptr, const int *group_idx, const double *resp_s, const double *resp_t,
              double qtot, double *q_dev, double *info, rp_stream_t stream);
 
+/* Ewald potential of point charges q at grid points (no Phi matrix):
+ * out[m] = sum_a q_a phi_a(g_m) with the same k-set, weights and real-space
+ * images as the fit.  Replaces the V_coul = Phi q pass of compute_stats
+ * (repeat.py:2326-2441) used by --stats and --output.
+ *   atoms [N*3], q [N] host; idx_dev [npts] int32 flat grid indices, or NULL for
+ *   every grid point (npts = nx*ny*nz); out_dev [npts] f64. */
+int rp_potential(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const double *q, int N,
+                 const int32_t *idx_dev, int64_t npts, double *out_dev, rp_stream_t stream);
+
 /* One whole fit from host memory, as repeat.py's main() runs it for
  * `--fit-type 1 [--gpu]`: H2D of V, filter, Ewald setup, normal equations,
  * constraints, solve, D2H of the charges.  q_out [N] host. M_out may be NULL. */
@@ -134,6 +143,29 @@ typedef struct {
     int precision;
 } rp_fit_desc;
 int rp_fit(rp_ctx *ctx, const rp_fit_desc *desc, double *q_out, int64_t *M_out, rp_stream_t stream);
+
+/* Many independent fits in one call (the batched workload).  All Ewald setups,
+ * then every filter asynchronously, one read of the kept counts, the normal
+ * equations of every cube back to back on `stream`, and one launch that folds
+ * and solves all bordered systems (one CTA per system).  No reference
+ * counterpart: repeat.py fits one cube per process.
+ *   descs[n]     as for rp_fit (each with its own precision)
+ *   V_dev        NULL, or n device pointers (an entry may be NULL: use descs[i].V on the host)
+ *   q_out        host, the charges of all cubes concatenated (sum of N_i doubles)
+ *   M_out[n]     host kept counts (may be NULL); info_out[4n] host (may be NULL):
+ *                per cube refined residual, min |pivot|, max |pivot|, singular flag */
+int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
+                 int64_t *M_out, double *info_out, rp_stream_t stream);
+
+/* Profiling hooks (no reference counterpart).  With timing on, every stage
+ * records CUDA events on the stream it runs on; rp_stage_times synchronises,
+ * returns per stage name the summed milliseconds and launch count
+ * (ms[2k], ms[2k+1]), names '\n'-separated, and clears the record.
+ * *count_inout: capacity in, stages written out. */
+int rp_set_timing(rp_ctx *ctx, int enable);
+/* Total kernel launches the library has issued in this process. */
+int rp_launch_count(long long *out);
+int rp_stage_times(rp_ctx *ctx, char *names, size_t names_cap, double *ms, int *count_inout);
 
 #ifdef __cplusplus
 }

@@ -21,7 +21,8 @@ PREC_MIXED = 1
 
 # every symbol include/repeat_gb300.h declares
 EXPORTS = ["rp_version", "rp_ctx_create", "rp_ctx_destroy", "rp_last_error", "rp_filter", "rp_ewald_setup",
-           "rp_ewald_destroy", "rp_ewald_info", "rp_gram", "rp_solve", "rp_fit"]
+           "rp_ewald_destroy", "rp_ewald_info", "rp_gram", "rp_solve", "rp_potential", "rp_fit",
+           "rp_fit_batch", "rp_set_timing", "rp_stage_times", "rp_launch_count"]
 
 
 class RepeatError(RuntimeError):
@@ -82,8 +83,18 @@ def load(path: str | None = None):
     L.rp_gram.argtypes = [P, P, P, I, P, P, L64, I, P, P, P, P]
     L.rp_solve.restype = I
     L.rp_solve.argtypes = [P, P, P, I, I, P, P, P, P, D, P, P, P]
+    L.rp_potential.restype = I
+    L.rp_potential.argtypes = [P, P, P, P, I, P, L64, P, P]
     L.rp_fit.restype = I
     L.rp_fit.argtypes = [P, ctypes.POINTER(RpFitDesc), P, ctypes.POINTER(L64), P]
+    L.rp_launch_count.restype = I
+    L.rp_launch_count.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
+    L.rp_set_timing.restype = I
+    L.rp_set_timing.argtypes = [P, I]
+    L.rp_stage_times.restype = I
+    L.rp_stage_times.argtypes = [P, ctypes.c_char_p, SZ, P, ctypes.POINTER(I)]
+    L.rp_fit_batch.restype = I
+    L.rp_fit_batch.argtypes = [P, I, P, P, P, P, P, P]
     _lib = L
     return L
 
@@ -98,6 +109,12 @@ def check(ctx_ptr, rc: int, what: str = ""):
     if rc == -4:
         raise SingularError(rc, msg)
     raise RepeatError(rc, msg)
+
+
+def launch_count() -> int:
+    v = ctypes.c_longlong(0)
+    load().rp_launch_count(ctypes.byref(v))
+    return int(v.value)
 
 
 def make_grid(n_grid, axis) -> RpGrid:

@@ -30,6 +30,7 @@ CUDA_SOURCES = [
     "phi_fp64.cu",
     "gram_mixed.cu",
     "solve.cu",
+    "potential.cu",
 ]
 
 

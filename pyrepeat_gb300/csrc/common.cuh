@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cublas_v2.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -41,8 +42,15 @@ struct Error {
         if (!(cond)) ::rp::fail(RP_E_ARG, msg);                                             \
     } while (0)
 
-// Check a kernel launch (configuration errors surface here, not later).
-#define RP_LAUNCH_CHECK() RP_CUDA(cudaGetLastError())
+// Kernel launches issued by the library (read with rp_launch_count).
+extern std::atomic<long long> g_launches;
+
+// Check a kernel launch (configuration errors surface here, not later) and count it.
+#define RP_LAUNCH_CHECK()                     \
+    do {                                      \
+        ::rp::g_launches.fetch_add(1);        \
+        RP_CUDA(cudaGetLastError());          \
+    } while (0)
 
 struct Buffer {
     void *ptr = nullptr;
@@ -60,6 +68,13 @@ struct rp_ctx {
     cublasHandle_t cublas = nullptr;
     std::unordered_map<std::string, rp::Buffer> scratch;
     int *d_status = nullptr;  // device status word for bounded waits / singular flags
+    // optional per-stage CUDA-event timing (rp_set_timing / rp_stage_times)
+    bool timing = false;
+    struct Mark {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Mark> marks;
 
     // Grow-only named scratch buffer owned by the ctx.
     void *buf(const std::string &name, size_t bytes) {
@@ -68,6 +83,7 @@ struct rp_ctx {
         auto &b = scratch[name];
         if (b.bytes >= bytes) return b.ptr;
         if (b.ptr) {
+            cudaDeviceSynchronize();  // queued work may still read the old buffer
             cudaFree(b.ptr);
             used -= b.bytes;
             b.ptr = nullptr;
@@ -124,10 +140,19 @@ namespace rp {
 // Host helpers shared by the stages.
 void prune_shifts(const rp_ewald *ew, const double *atoms, int N, std::vector<double> &out, int &zero_idx);
 
+// Device status words: [0] a bounded wait ran out, [1] fixed-point range overflows.
+void status_clear(rp_ctx *ctx, cudaStream_t s);
+void status_check(rp_ctx *ctx, cudaStream_t s);  // synchronises s
+
 // Stage launchers (each enqueues on `stream`).
 void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
                 double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, int64_t capacity,
                 int64_t *M_out, uint8_t *mask_dev, cudaStream_t stream);
+// Asynchronous form: the kept count lands in *M_dev; kept_idx_dev and Vc_dev hold a
+// whole grid (capacity = nx*ny*nz).  `tag` keeps the scratch of concurrent calls apart.
+void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
+                  double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev,
+                  uint8_t *mask_dev, cudaStream_t stream, const std::string &tag);
 void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
                cudaStream_t stream);
@@ -137,6 +162,16 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
 void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
                const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,
                double *info, cudaStream_t stream);
+// Batched constraints + bordered solves: one CTA per system, one launch.
+struct SolveJob {
+    const double *A, *b;
+    int N, n_groups;
+    const int *group_ptr, *group_idx;
+    const double *resp_s, *resp_t;
+    double qtot;
+    double *q;
+};
+void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream);
 
 // Device table builders (ewald_tables.cu).
 void atom_tables_fp64(const rp_ewald *ew, const double *d_atoms, int N, double *d_B, int ldb, cudaStream_t s);
@@ -150,5 +185,24 @@ void finish_normal_equations(const double *G, const double *r, const double *s_c
                              int N, double *A, double *b, cudaStream_t s);
 
 inline unsigned ceil_div(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+
+// Records CUDA events around a stage on its stream when the ctx is timing.
+struct StageTimer {
+    rp_ctx *ctx;
+    cudaStream_t s;
+    size_t slot = (size_t)-1;
+    StageTimer(rp_ctx *c, const char *name, cudaStream_t st) : ctx(c), s(st) {
+        if (!ctx->timing) return;
+        rp_ctx::Mark m{name, nullptr, nullptr};
+        cudaEventCreate(&m.a);
+        cudaEventCreate(&m.b);
+        cudaEventRecord(m.a, s);
+        ctx->marks.push_back(m);
+        slot = ctx->marks.size() - 1;
+    }
+    ~StageTimer() {
+        if (slot != (size_t)-1) cudaEventRecord(ctx->marks[slot].b, s);
+    }
+};
 
 }  // namespace rp

@@ -217,8 +217,9 @@ __global__ void __launch_bounds__(1024) vmean_kernel(const double *__restrict__ 
     }
 }
 
-__global__ void center_kernel(double *__restrict__ Vc, long long M, const double *__restrict__ mean) {
-    double m = *mean;
+__global__ void center_kernel(double *__restrict__ Vc, const long long *__restrict__ Mp, const double *__restrict__ mean) {
+    const double m = *mean;
+    const long long M = *Mp;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x)
         Vc[i] -= m;
 }
@@ -241,10 +242,11 @@ double radius_of(int z) {
 
 }  // namespace
 
-void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
-                double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, int64_t capacity,
-                int64_t *M_out, uint8_t *mask_dev, cudaStream_t stream) {
-    RP_REQUIRE(grid && atoms && Z && V_dev && M_out, "rp_filter: null argument");
+void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
+                  double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev,
+                  uint8_t *mask_dev, cudaStream_t stream, const std::string &tag) {
+    RP_REQUIRE(grid && atoms && Z && V_dev && M_dev, "rp_filter: null argument");
+    const long long capacity = (long long)grid->n_grid[0] * grid->n_grid[1] * grid->n_grid[2];
     RP_REQUIRE(N >= 0, "rp_filter: N < 0");
     const int nx = grid->n_grid[0], ny = grid->n_grid[1], nz = grid->n_grid[2];
     RP_REQUIRE(nx > 0 && ny > 0 && nz > 0, "rp_filter: grid counts must be positive");
@@ -381,19 +383,19 @@ void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int
 
     // ---- upload (ctx scratch) and launch
     const int nblk = (int)((n_total + kFilterThreads - 1) / kFilterThreads);
-    float4 *d_e32 = ctx->buf_t<float4>("flt_e32", e32.size());
-    D4 *d_e64 = ctx->buf_t<D4>("flt_e64", e64s.size());
-    double *d_rmax2 = ctx->buf_t<double>("flt_rmax2", rmax2s.size());
-    float *d_rmax2f = ctx->buf_t<float>("flt_rmax2f", rmax2f.size());
-    int *d_boff = ctx->buf_t<int>("flt_boff", boff.size());
-    int *d_bidx = ctx->buf_t<int>("flt_bidx", bidx.size());
-    uint8_t *d_mask = mask_dev ? mask_dev : ctx->buf_t<uint8_t>("flt_mask", (size_t)n_total);
-    int *d_counts = ctx->buf_t<int>("flt_counts", (size_t)nblk);
-    long long *d_offsets = ctx->buf_t<long long>("flt_offsets", (size_t)nblk);
-    double *d_vsum = ctx->buf_t<double>("flt_vsum", (size_t)nblk);
-    long long *d_total = ctx->buf_t<long long>("flt_total", 1);
-    double *d_mean = ctx->buf_t<double>("flt_mean", 1);
-    unsigned long long *d_re = ctx->buf_t<unsigned long long>("flt_rechecks", 1);
+    float4 *d_e32 = ctx->buf_t<float4>("flt_e32" + tag, e32.size());
+    D4 *d_e64 = ctx->buf_t<D4>("flt_e64" + tag, e64s.size());
+    double *d_rmax2 = ctx->buf_t<double>("flt_rmax2" + tag, rmax2s.size());
+    float *d_rmax2f = ctx->buf_t<float>("flt_rmax2f" + tag, rmax2f.size());
+    int *d_boff = ctx->buf_t<int>("flt_boff" + tag, boff.size());
+    int *d_bidx = ctx->buf_t<int>("flt_bidx" + tag, bidx.size());
+    uint8_t *d_mask = mask_dev ? mask_dev : ctx->buf_t<uint8_t>("flt_mask" + tag, (size_t)n_total);
+    int *d_counts = ctx->buf_t<int>("flt_counts" + tag, (size_t)nblk);
+    long long *d_offsets = ctx->buf_t<long long>("flt_offsets" + tag, (size_t)nblk);
+    double *d_vsum = ctx->buf_t<double>("flt_vsum" + tag, (size_t)nblk);
+    long long *d_total = M_dev;
+    double *d_mean = ctx->buf_t<double>("flt_mean" + tag, 1);
+    unsigned long long *d_re = ctx->buf_t<unsigned long long>("flt_rechecks" + tag, 1);
     RP_CUDA(cudaMemcpyAsync(d_e32, e32.data(), e32.size() * sizeof(float4), cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_e64, e64s.data(), e64s.size() * sizeof(D4), cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_rmax2, rmax2s.data(), rmax2s.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
@@ -402,6 +404,7 @@ void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int
     RP_CUDA(cudaMemcpyAsync(d_bidx, bidx.data(), bidx.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemsetAsync(d_re, 0, sizeof(unsigned long long), stream));
 
+    StageTimer t_f(ctx, "filter", stream);
     FilterParams p{};
     p.nx = nx; p.ny = ny; p.nz = nz; p.n_total = n_total;
     for (int t = 0; t < 9; ++t) { p.ax[t] = (float)ax[t]; p.axd[t] = ax[t]; }
@@ -416,21 +419,36 @@ void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int
     RP_LAUNCH_CHECK();
     scan_counts_kernel<<<1, 1024, 0, stream>>>(d_counts, nblk, d_offsets, d_total);
     RP_LAUNCH_CHECK();
-    compact_kernel<<<nblk, kFilterThreads, 0, stream>>>(d_mask, V_dev, n_total, d_offsets, (long long)capacity,
+    compact_kernel<<<nblk, kFilterThreads, 0, stream>>>(d_mask, V_dev, n_total, d_offsets, capacity,
                                                         kept_idx_dev, Vc_dev, d_vsum);
     RP_LAUNCH_CHECK();
     vmean_kernel<<<1, 1024, 0, stream>>>(d_vsum, nblk, d_total, d_mean);
     RP_LAUNCH_CHECK();
+    center_kernel<<<ctx->sm_count * 4, 256, 0, stream>>>(Vc_dev, d_total, d_mean);
+    RP_LAUNCH_CHECK();
+}
+
+void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
+                double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, int64_t capacity,
+                int64_t *M_out, uint8_t *mask_dev, cudaStream_t stream) {
+    RP_REQUIRE(grid && M_out, "rp_filter: null argument");
+    const long long npts = (long long)grid->n_grid[0] * grid->n_grid[1] * grid->n_grid[2];
+    // the compaction writes every kept point, so the caller's buffers must hold the
+    // whole grid unless the kept count is known to fit; stage through ctx scratch otherwise
+    const bool direct = capacity >= npts;
+    int32_t *kid = direct ? kept_idx_dev : ctx->buf_t<int32_t>("flt_kept_stage", (size_t)npts);
+    double *vc = direct ? Vc_dev : ctx->buf_t<double>("flt_vc_stage", (size_t)npts);
+    long long *d_M = ctx->buf_t<long long>("flt_total", 1);
+    filter_async(ctx, grid, atoms, Z, N, V_dev, vdw_factor, vdw_max, kid, vc, d_M, mask_dev, stream, "");
     long long M = 0;
-    RP_CUDA(cudaMemcpyAsync(&M, d_total, sizeof(long long), cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaMemcpyAsync(&M, d_M, sizeof(long long), cudaMemcpyDeviceToHost, stream));
     RP_CUDA(cudaStreamSynchronize(stream));
     *M_out = M;
-    if (M > capacity) fail(RP_E_ARG, "rp_filter: " + std::to_string(M) + " kept points exceed capacity " +
-                                         std::to_string(capacity));
-    if (M > 0) {
-        int cb = (int)std::min<long long>((M + 255) / 256, 4096);
-        center_kernel<<<cb, 256, 0, stream>>>(Vc_dev, M, d_mean);
-        RP_LAUNCH_CHECK();
+    if (M > capacity)
+        fail(RP_E_ARG, "rp_filter: " + std::to_string(M) + " kept points exceed capacity " + std::to_string(capacity));
+    if (!direct && M > 0) {
+        RP_CUDA(cudaMemcpyAsync(kept_idx_dev, kid, sizeof(int32_t) * M, cudaMemcpyDeviceToDevice, stream));
+        RP_CUDA(cudaMemcpyAsync(Vc_dev, vc, sizeof(double) * M, cudaMemcpyDeviceToDevice, stream));
     }
 }
 

@@ -791,9 +791,10 @@ __global__ void colstats_finish_kernel(const double *__restrict__ psum, const fl
 // x = 2^-6 (x0 + 2^-7 x1 + 2^-14 x2 + 2^-21 x3), x_s integers in [-64, 64], exact in FP16.
 __global__ void slice_rows_kernel(const double *__restrict__ phit, long long ld, long long rows, long long rows_pad,
                                   int N, int Np_pad, const double *__restrict__ c, const float *__restrict__ scale,
-                                  const double *__restrict__ Vc, long long m0, float vscale, __half *__restrict__ X0,
-                                  __half *__restrict__ X1, __half *__restrict__ X2, __half *__restrict__ X3,
-                                  int *__restrict__ clamped) {
+                                  const double *__restrict__ Vc, long long m0, const float *__restrict__ vscale_p,
+                                  __half *__restrict__ X0, __half *__restrict__ X1, __half *__restrict__ X2,
+                                  __half *__restrict__ X3, int *__restrict__ clamped) {
+    const float vscale = *vscale_p;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)Np_pad * rows_pad) return;
     int a = (int)(t / rows_pad);
@@ -814,7 +815,9 @@ __global__ void slice_rows_kernel(const double *__restrict__ phit, long long ld,
 // partial is an exact integer) and add them, unscaled, into G (Np x Np).  Tiles
 // inside a 128-row block already hold both (a,b) and (b,a); the others are mirrored.
 __global__ void gram_reduce_kernel(const double *__restrict__ part, int ntiles, int nsplit, int nt, int Np,
-                                   const float *__restrict__ scale, float vscale, int N, double *__restrict__ G) {
+                                   const float *__restrict__ scale, const float *__restrict__ vscale_p, int N,
+                                   double *__restrict__ G) {
+    const float vscale = *vscale_p;
     const int tile = blockIdx.y;
     int ti, tj;
     gram_tile_decode(tile, nt, ti, tj);
@@ -860,6 +863,13 @@ __global__ void __launch_bounds__(1024) absmax_kernel(const double *__restrict__
         __syncthreads();
     }
     if (threadIdx.x == 0) *out = sm[0];
+}
+
+// ESP row scale 2^(-e-1) with max|Vc| in [2^(e-1), 2^e), so |V * scale| < 1/2
+__global__ void vscale_kernel(const double *__restrict__ vmax, float *__restrict__ vscale) {
+    int e = 0;
+    if (*vmax > 0.0) frexp(*vmax, &e);
+    *vscale = ldexpf(1.0f, -e - 1);
 }
 
 __global__ void to_float2_kernel(const double2 *__restrict__ in, float2 *__restrict__ out, int n) {
@@ -1005,8 +1015,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     RP_CUDA(cudaMemcpyAsync(d_atoms, atoms, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_shifts, sh.data(), sizeof(double) * sh.size(), cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice, stream));
-    int *d_status = ctx->d_status;
-    RP_CUDA(cudaMemsetAsync(d_status, 0, sizeof(int), stream));
+    int *d_status = ctx->d_status;  // cleared by the caller (rp_gram / the batch driver)
 
     // FP32 per-axis phase tables and sqrt weights for the float block
     const int nex = (kmax + 1) * nx, ney = (2 * kmax + 1) * ny, nez = (2 * kmax + 1) * nz;
@@ -1015,8 +1024,11 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     float2 *ez = ctx->buf_t<float2>("m_ez", nez);
     float *swk = ctx->buf_t<float>("m_swk", K);
     to_float2_kernel<<<ceil_div(nex, 256), 256, 0, stream>>>(ew->d_ex, ex, nex);
+    RP_LAUNCH_CHECK();
     to_float2_kernel<<<ceil_div(ney, 256), 256, 0, stream>>>(ew->d_ey, ey, ney);
+    RP_LAUNCH_CHECK();
     to_float2_kernel<<<ceil_div(nez, 256), 256, 0, stream>>>(ew->d_ez, ez, nez);
+    RP_LAUNCH_CHECK();
     sqrt_weights_kernel<<<ceil_div(K, 256), 256, 0, stream>>>(ew->d_kcoef_s, swk, K);
     RP_LAUNCH_CHECK();
 
@@ -1028,10 +1040,12 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     const double sTop = std::ldexp(1.0, -et - 1);
 
     // atom tables (once per fit)
+    StageTimer t_atab(ctx, "atom_tables", stream);
     __half *Bh = ctx->buf_t<__half>("m_Bh", (size_t)N * fl.width);
     __half *Bl = ctx->buf_t<__half>("m_Bl", (size_t)N * fl.width);
     atom_tables_f16_kernel<<<ceil_div((long long)N * fl.width, 256), 256, 0, stream>>>(ew->d_kvec_s, ew->d_kcoef_s, fl,
                                                                                        d_atoms, N, Bh, Bl);
+    RP_LAUNCH_CHECK();
     __half *Bt[4];
     for (int q = 0; q < 4; ++q) Bt[q] = ctx->buf_t<__half>("m_Bt" + std::to_string(q), (size_t)N * top.width);
     atom_tables_top_kernel<<<ceil_div((long long)N * top.width, 256), 256, 0, stream>>>(
@@ -1054,8 +1068,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     double *phit = ctx->buf_t<double>("m_phit", (size_t)N * chunk_pad);
     __half *X[kGSlices];
     for (int q = 0; q < kGSlices; ++q) X[q] = ctx->buf_t<__half>("m_X" + std::to_string(q), (size_t)Np_pad * chunk_pad);
-    int *d_clamped = ctx->buf_t<int>("m_clamped", 1);
-    RP_CUDA(cudaMemsetAsync(d_clamped, 0, sizeof(int), stream));
+    int *d_clamped = ctx->d_status + 1;  // second status word: fixed-point range overflows
     const int nslab = (int)((chunk + kStatSlab - 1) / kStatSlab);
     double *psum = ctx->buf_t<double>("m_psum", (size_t)N * nslab);
     float *pmax = ctx->buf_t<float>("m_pmax", (size_t)N * nslab);
@@ -1067,19 +1080,15 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     double *sumV = ctx->buf_t<double>("m_sumV", 1);
     RP_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * Np * Np, stream));
 
-    // ESP row scale: power of two from the largest |Vc| (host read of one reduction)
-    float vscale = 1.0f;
+    // ESP row scale: power of two from the largest |Vc|, computed on the device
+    float *vscale = ctx->buf_t<float>("m_vscale", 1);
     {
         column_sums_fp64(Vc_dev, M, 1, 1, sumV, false, ctx, stream);
         double *d_vmax = ctx->buf_t<double>("m_vmax", 1);
         absmax_kernel<<<1, 1024, 0, stream>>>(Vc_dev, M, d_vmax);
         RP_LAUNCH_CHECK();
-        double vmax = 0.0;
-        RP_CUDA(cudaMemcpyAsync(&vmax, d_vmax, sizeof(double), cudaMemcpyDeviceToHost, stream));
-        RP_CUDA(cudaStreamSynchronize(stream));
-        int e = 0;
-        if (vmax > 0.0) std::frexp(vmax, &e);
-        vscale = std::ldexp(1.0f, -e - 1);
+        vscale_kernel<<<1, 1, 0, stream>>>(d_vmax, vscale);
+        RP_LAUNCH_CHECK();
     }
 
     const int nt = Np_pad / kBM;
@@ -1091,14 +1100,17 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         const long long rows_tpad = round_up(rows, kBM);
         const long long rows_kpad = round_up(rows, kBK);
         // 1. grid tables of both blocks
+        StageTimer t_tab(ctx, "grid_tables", stream);
         grid_tables_f16_kernel<<<ceil_div(rows_tpad * (fl.width / 2), 256), 256, 0, stream>>>(
             ew->d_kidx_s, swk, fl, kmax, ex, ey, ez, nx, ny, nz, kept_idx_dev, m0, rows, rows_tpad, Th, Tl);
+        RP_LAUNCH_CHECK();
         grid_tables_top_kernel<<<ceil_div(rows_tpad * (top.width / 2), 256), 256, 0, stream>>>(
             ew->d_kidx_s, ew->d_kcoef_s, top, kmax, ew->d_ex, ew->d_ey, ew->d_ez, nx, ny, nz, kept_idx_dev, m0, rows,
             rows_tpad, sTop, Tt[0], Tt[1], Tt[2], Tt[3]);
         RP_LAUNCH_CHECK();
         // 2a. GEMM-1 over the float block: Phi_t = T B^T (atom-major, ld chunk_pad)
         {
+            StageTimer tt(ctx, "recip_gemm_f16x3", stream);
             const CUtensorMap mTh = make_map(Th, rows_tpad, fl.width, kBM), mTl = make_map(Tl, rows_tpad, fl.width, kBM);
             RecArgs g{};
             g.m_tiles = (int)(rows_tpad / kBM);
@@ -1113,6 +1125,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         }
         // 2b. exact GEMM over the heaviest k: Phi_t += T_top B_top^T
         {
+            StageTimer tt(ctx, "recip_gemm_exact_top", stream);
             TopArgs g{};
             g.m_tiles = (int)(rows_tpad / kBM);
             g.kb_total = top.width / kBK;
@@ -1128,6 +1141,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         }
         // 3. real space
         {
+            StageTimer tt(ctx, "realspace", stream);
             dim3 grd(ceil_div(rows, kRealPts), ceil_div(N, kRealAtoms));
             realspace_kernel<<<grd, kRealPts, 0, stream>>>(kept_idx_dev, m0, rows, d_axis, nx, ny, d_atoms, N,
                                                            d_shifts, S, zero_idx, ew->cutoff, ew->sqrt_alpha,
@@ -1136,6 +1150,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         }
         // 4. column statistics, centre/scale on the first chunk, fixed-point slices of X
         {
+            StageTimer tt(ctx, "center_slice", stream);
             const int ns = (int)((rows + kStatSlab - 1) / kStatSlab);
             colstats_kernel<<<dim3(ns, N), 256, 0, stream>>>(phit, chunk_pad, rows, N, psum, pmax);
             RP_LAUNCH_CHECK();
@@ -1160,7 +1175,11 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
             g.out = part;
             g.status = d_status;
             const __half *Xq[kGSlices] = {X[0], X[1], X[2], X[3]};
-            launch_gram(Xq, Np_pad, rows_kpad, g, ntri * nsplit, stream);
+            {
+                StageTimer tt(ctx, "gram_exact", stream);
+                launch_gram(Xq, Np_pad, rows_kpad, g, ntri * nsplit, stream);
+            }
+            StageTimer tr(ctx, "gram_reduce_fp64", stream);
             gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256, 0, stream>>>(part, ntri, nsplit, nt, Np,
                                                                                          scale, vscale, N, G);
             RP_LAUNCH_CHECK();
@@ -1169,14 +1188,6 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     finish_mixed_kernel<<<ceil_div(std::max<long long>((long long)N * N, N), 256), 256, 0, stream>>>(
         G, Np, sphi, cvec, sumV, M, N, A_dev, b_dev);
     RP_LAUNCH_CHECK();
-    int st[2] = {0, 0};
-    RP_CUDA(cudaMemcpyAsync(&st[0], d_status, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    RP_CUDA(cudaMemcpyAsync(&st[1], d_clamped, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    RP_CUDA(cudaStreamSynchronize(stream));
-    if (st[0] != 0) fail(st[0], "rp_gram: a tensor-core pipeline wait timed out");
-    if (st[1] != 0)
-        fail(RP_E_STATE, "rp_gram: " + std::to_string(st[1]) +
-                             " Phi values exceeded the fixed-point range set on the first chunk");
 }
 
 }  // namespace rp
@@ -1213,9 +1224,13 @@ extern "C" int rp_debug_mixed_phi_parts(rp_ctx *ctx, const rp_ewald *ew, const d
                *ez = ctx->buf_t<float2>("m_ez", nez);
         float *swk = ctx->buf_t<float>("m_swk", K);
         to_float2_kernel<<<ceil_div(nex, 256), 256>>>(ew->d_ex, ex, nex);
+        RP_LAUNCH_CHECK();
         to_float2_kernel<<<ceil_div(ney, 256), 256>>>(ew->d_ey, ey, ney);
+        RP_LAUNCH_CHECK();
         to_float2_kernel<<<ceil_div(nez, 256), 256>>>(ew->d_ez, ez, nez);
+        RP_LAUNCH_CHECK();
         sqrt_weights_kernel<<<ceil_div(K, 256), 256>>>(ew->d_kcoef_s, swk, K);
+        RP_LAUNCH_CHECK();
         double wmax = 0.0;
         for (double w : ew->kcoef) wmax = std::max(wmax, w);
         int et = 0;
@@ -1224,6 +1239,7 @@ extern "C" int rp_debug_mixed_phi_parts(rp_ctx *ctx, const rp_ewald *ew, const d
         __half *Bh = ctx->buf_t<__half>("m_Bh", (size_t)N * fl.width), *Bl = ctx->buf_t<__half>("m_Bl", (size_t)N * fl.width);
         atom_tables_f16_kernel<<<ceil_div((long long)N * fl.width, 256), 256>>>(ew->d_kvec_s, ew->d_kcoef_s, fl, d_atoms,
                                                                                 N, Bh, Bl);
+        RP_LAUNCH_CHECK();
         __half *Bt[4], *Tt[4];
         const long long rows_tpad = round_up(rows, kBM);
         for (int q = 0; q < 4; ++q) {
@@ -1232,10 +1248,12 @@ extern "C" int rp_debug_mixed_phi_parts(rp_ctx *ctx, const rp_ewald *ew, const d
         }
         atom_tables_top_kernel<<<ceil_div((long long)N * top.width, 256), 256>>>(ew->d_kvec_s, ew->d_kcoef_s, top,
                                                                                  d_atoms, N, sTop, Bt[0], Bt[1], Bt[2], Bt[3]);
+        RP_LAUNCH_CHECK();
         __half *Th = ctx->buf_t<__half>("m_Th", (size_t)rows_tpad * fl.width),
                *Tl = ctx->buf_t<__half>("m_Tl", (size_t)rows_tpad * fl.width);
         grid_tables_f16_kernel<<<ceil_div(rows_tpad * (fl.width / 2), 256), 256>>>(
             ew->d_kidx_s, swk, fl, kmax, ex, ey, ez, nx, ny, nz, kept_idx_dev, 0, rows, rows_tpad, Th, Tl);
+        RP_LAUNCH_CHECK();
         grid_tables_top_kernel<<<ceil_div(rows_tpad * (top.width / 2), 256), 256>>>(
             ew->d_kidx_s, ew->d_kcoef_s, top, kmax, ew->d_ex, ew->d_ey, ew->d_ez, nx, ny, nz, kept_idx_dev, 0, rows,
             rows_tpad, sTop, Tt[0], Tt[1], Tt[2], Tt[3]);
@@ -1303,7 +1321,7 @@ extern "C" int rp_debug_gram_slices(rp_ctx *ctx, const void *X0, const void *X1,
         std::vector<float> h((size_t)Np, 1.0f);
         RP_CUDA(cudaMemcpy(ones, h.data(), sizeof(float) * Np, cudaMemcpyHostToDevice));
         RP_CUDA(cudaMemset(I_dev, 0, sizeof(double) * Np * Np));
-        gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256>>>(part, ntri, nsplit, nt, Np, ones, 1.0f, Np, I_dev);
+        gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256>>>(part, ntri, nsplit, nt, Np, ones, ones, Np, I_dev);
         RP_LAUNCH_CHECK();
         RP_CUDA(cudaDeviceSynchronize());
         int st = 0;

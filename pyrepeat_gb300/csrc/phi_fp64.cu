@@ -163,8 +163,15 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
     const double one = 1.0, zero = 0.0;
     for (int64_t m0 = 0; m0 < M; m0 += chunk) {
         const int64_t rows = std::min<int64_t>(chunk, M - m0);
-        grid_tables_fp64(ew, kept_idx_dev, m0, rows, T, K2, stream);
-        RP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, N, (int)rows, K2, &one, B, K2, T, K2, &zero, P, N));
+        {
+            StageTimer tt(ctx, "fp64_tables", stream);
+            grid_tables_fp64(ew, kept_idx_dev, m0, rows, T, K2, stream);
+        }
+        {
+            StageTimer tt(ctx, "fp64_recip_dgemm", stream);
+            RP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, N, (int)rows, K2, &one, B, K2, T, K2, &zero, P, N));
+        }
+        StageTimer t_r(ctx, "fp64_realspace", stream);
         realspace_fp64_kernel<<<ceil_div(rows * N, 128), 128, 0, stream>>>(
             kept_idx_dev, m0, rows, d_axis, ew->grid.n_grid[0], ew->grid.n_grid[1], d_atoms, N, d_shifts, S,
             zero_idx, ew->cutoff, ew->sqrt_alpha, P);
@@ -182,6 +189,7 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
         shift_columns_kernel<<<ceil_div(rows * N, 256), 256, 0, stream>>>(P, rows, N, c);
         RP_LAUNCH_CHECK();
         // column-major view: X = P^T is N x rows with ld N;  G += X X^T,  r += X Vc
+        StageTimer t_g(ctx, "fp64_gram_dgemm", stream);
         RP_CUBLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_T, N, N, (int)rows, &one, P, N, P, N, &one, G, N));
         RP_CUBLAS(cublasDgemv(h, CUBLAS_OP_N, N, (int)rows, &one, P, N, Vc_dev + m0, 1, &one, r, 1));
     }

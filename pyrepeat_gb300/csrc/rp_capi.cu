@@ -1,12 +1,28 @@
 // C ABI of librepeat_gb300 (include/repeat_gb300.h): argument checks, the
 // context, and the translation of internal errors into status codes.
 #include <cstring>
+#include <unordered_map>
 
 #include "common.cuh"
 
 namespace rp {
 void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax);
 void ewald_free(rp_ewald *ew);
+void potential_run(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const double *q, int N,
+                   const int32_t *idx_dev, int64_t npts, double *out_dev, cudaStream_t stream);
+}  // namespace rp
+
+namespace rp {
+std::atomic<long long> g_launches{0};
+void status_clear(rp_ctx *ctx, cudaStream_t s) { RP_CUDA(cudaMemsetAsync(ctx->d_status, 0, 2 * sizeof(int), s)); }
+void status_check(rp_ctx *ctx, cudaStream_t s) {
+    int st[2] = {0, 0};
+    RP_CUDA(cudaMemcpyAsync(st, ctx->d_status, sizeof(st), cudaMemcpyDeviceToHost, s));
+    RP_CUDA(cudaStreamSynchronize(s));
+    if (st[0] != 0) fail(st[0], "a tensor-core pipeline wait ran out of time");
+    if (st[1] != 0)
+        fail(RP_E_STATE, std::to_string(st[1]) + " Phi values exceeded the fixed-point range set on the first chunk");
+}
 }  // namespace rp
 
 cublasHandle_t rp_ctx::blas() {
@@ -35,13 +51,6 @@ int guarded(rp_ctx *ctx, F &&f) {
     }
 }
 
-struct DeviceBuf {  // RAII device buffer for rp_fit's own inputs/outputs
-    void *p = nullptr;
-    explicit DeviceBuf(size_t bytes) { RP_CUDA(cudaMalloc(&p, bytes ? bytes : 256)); }
-    ~DeviceBuf() { cudaFree(p); }
-    template <class T>
-    T *as() { return static_cast<T *>(p); }
-};
 
 }  // namespace
 
@@ -142,12 +151,13 @@ int rp_gram(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const i
     return guarded(ctx, [&] {
         RP_REQUIRE(atoms && kept_idx_dev && Vc_dev && A_dev && b_dev, "rp_gram: null argument");
         RP_REQUIRE(ew->device == ctx->device, "rp_gram: ewald built on another device");
+        RP_REQUIRE(precision == RP_PREC_FP64 || precision == RP_PREC_MIXED, "rp_gram: unknown precision");
+        rp::status_clear(ctx, (cudaStream_t)stream);
         if (precision == RP_PREC_FP64)
             rp::gram_fp64(ctx, ew, atoms, N, kept_idx_dev, Vc_dev, M, A_dev, b_dev, sum_phi_dev, (cudaStream_t)stream);
-        else if (precision == RP_PREC_MIXED)
-            rp::gram_mixed(ctx, ew, atoms, N, kept_idx_dev, Vc_dev, M, A_dev, b_dev, sum_phi_dev, (cudaStream_t)stream);
         else
-            rp::fail(RP_E_ARG, "rp_gram: unknown precision");
+            rp::gram_mixed(ctx, ew, atoms, N, kept_idx_dev, Vc_dev, M, A_dev, b_dev, sum_phi_dev, (cudaStream_t)stream);
+        rp::status_check(ctx, (cudaStream_t)stream);
     });
 }
 
@@ -161,44 +171,156 @@ int rp_solve(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n
     });
 }
 
-int rp_fit(rp_ctx *ctx, const rp_fit_desc *d, double *q_out, int64_t *M_out, rp_stream_t stream_) {
-    if (!ctx || !d || !q_out) return RP_E_ARG;
-    cudaStream_t stream = (cudaStream_t)stream_;
-    rp_ewald *ew = nullptr;
-    int rc = guarded(ctx, [&] {
-        RP_REQUIRE(d->V && d->atoms && d->Z && d->N > 0, "rp_fit: null input or N <= 0");
-        const long long npts = (long long)d->grid.n_grid[0] * d->grid.n_grid[1] * d->grid.n_grid[2];
-        RP_REQUIRE(npts > 0, "rp_fit: empty grid");
-        const int N = d->N;
-        double *V = ctx->buf_t<double>("fit_V", (size_t)npts);
-        int32_t *kept = ctx->buf_t<int32_t>("fit_kept", (size_t)npts);
-        double *Vc = ctx->buf_t<double>("fit_Vc", (size_t)npts);
-        double *A = ctx->buf_t<double>("fit_A", (size_t)N * N);
-        double *b = ctx->buf_t<double>("fit_b", (size_t)N);
-        double *q = ctx->buf_t<double>("fit_q", (size_t)N);
-        RP_CUDA(cudaMemcpyAsync(V, d->V, sizeof(double) * npts, cudaMemcpyHostToDevice, stream));
-        int64_t M = 0;
-        rp::filter_run(ctx, &d->grid, d->atoms, d->Z, N, V, d->vdw_factor, d->vdw_max, kept, Vc, npts, &M, nullptr,
-                       stream);
-        if (M_out) *M_out = M;
-        RP_REQUIRE(M > 0, "rp_fit: no grid point survives the vdW filter");
-        ew = new rp_ewald();
-        ew->device = ctx->device;
-        rp::ewald_build(ew, &d->grid, d->cutoff, d->kmax);
-        if (d->precision == RP_PREC_MIXED)
-            rp::gram_mixed(ctx, ew, d->atoms, N, kept, Vc, M, A, b, nullptr, stream);
-        else
-            rp::gram_fp64(ctx, ew, d->atoms, N, kept, Vc, M, A, b, nullptr, stream);
-        rp::solve_run(ctx, A, b, N, d->n_groups, d->group_ptr, d->group_idx, d->resp_s, d->resp_t, d->qtot, q, nullptr,
-                      stream);
-        RP_CUDA(cudaMemcpyAsync(q_out, q, sizeof(double) * N, cudaMemcpyDeviceToHost, stream));
-        RP_CUDA(cudaStreamSynchronize(stream));
+int rp_potential(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const double *q, int N,
+                 const int32_t *idx_dev, int64_t npts, double *out_dev, rp_stream_t stream) {
+    if (!ctx || !ew) return RP_E_ARG;
+    return guarded(ctx, [&] {
+        RP_REQUIRE(ew->device == ctx->device, "rp_potential: ewald built on another device");
+        rp::potential_run(ctx, ew, atoms, q, N, idx_dev, npts, out_dev, (cudaStream_t)stream);
     });
-    if (ew) {
-        rp::ewald_free(ew);
-        delete ew;
-    }
+}
+
+int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
+                 int64_t *M_out, double *info_out, rp_stream_t stream_) {
+    if (!ctx || n < 0 || (n > 0 && (!descs || !q_out))) return RP_E_ARG;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    std::vector<rp_ewald *> ews((size_t)n, nullptr);
+    int rc = guarded(ctx, [&] {
+        if (n == 0) return;
+        std::vector<long long> npts((size_t)n), off_pts((size_t)n + 1, 0), off_n((size_t)n + 1, 0),
+            off_nn((size_t)n + 1, 0);
+        for (int i = 0; i < n; ++i) {
+            const rp_fit_desc &d = descs[i];
+            RP_REQUIRE(d.atoms && d.Z && d.N > 0, "rp_fit: null input or N <= 0");
+            RP_REQUIRE(d.precision == RP_PREC_FP64 || d.precision == RP_PREC_MIXED, "rp_fit: unknown precision");
+            RP_REQUIRE((V_dev && V_dev[i]) || d.V, "rp_fit: no ESP values");
+            npts[i] = (long long)d.grid.n_grid[0] * d.grid.n_grid[1] * d.grid.n_grid[2];
+            RP_REQUIRE(npts[i] > 0 && npts[i] < (1LL << 31), "rp_fit: bad grid");
+            off_pts[i + 1] = off_pts[i] + npts[i];
+            off_n[i + 1] = off_n[i] + d.N;
+            off_nn[i + 1] = off_nn[i] + (long long)d.N * d.N;
+        }
+        // Ewald setups first: they make small synchronous uploads, so they go
+        // before any long GPU work is queued on the stream
+        for (int i = 0; i < n; ++i) {
+            ews[i] = new rp_ewald();
+            ews[i]->device = ctx->device;
+            rp::ewald_build(ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax);
+        }
+        int32_t *kept = ctx->buf_t<int32_t>("fit_kept", (size_t)off_pts[n]);
+        double *Vc = ctx->buf_t<double>("fit_Vc", (size_t)off_pts[n]);
+        double *Vh = nullptr;
+        bool any_host = false;
+        for (int i = 0; i < n; ++i) any_host |= !(V_dev && V_dev[i]);
+        if (any_host) Vh = ctx->buf_t<double>("fit_V", (size_t)off_pts[n]);
+        long long *Md = ctx->buf_t<long long>("fit_M", (size_t)n);
+        double *A = ctx->buf_t<double>("fit_A", (size_t)off_nn[n]);
+        double *b = ctx->buf_t<double>("fit_b", (size_t)off_n[n]);
+        double *q = ctx->buf_t<double>("fit_q", (size_t)off_n[n]);
+        rp::status_clear(ctx, stream);
+        // 1. filters (asynchronous; kept counts stay on the device)
+        for (int i = 0; i < n; ++i) {
+            const rp_fit_desc &d = descs[i];
+            const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
+            if (!(V_dev && V_dev[i]))
+                RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], d.V, sizeof(double) * npts[i], cudaMemcpyHostToDevice, stream));
+            rp::filter_async(ctx, &d.grid, d.atoms, d.Z, d.N, V, d.vdw_factor, d.vdw_max, kept + off_pts[i],
+                             Vc + off_pts[i], Md + i, nullptr, stream, "");
+        }
+        // 2. one read of all kept counts (sizes every later launch)
+        std::vector<long long> M((size_t)n);
+        RP_CUDA(cudaMemcpyAsync(M.data(), Md, sizeof(long long) * n, cudaMemcpyDeviceToHost, stream));
+        RP_CUDA(cudaStreamSynchronize(stream));
+        for (int i = 0; i < n; ++i) {
+            if (M_out) M_out[i] = M[i];
+            RP_REQUIRE(M[i] > 0, "rp_fit: no grid point of cube " + std::to_string(i) + " survives the vdW filter");
+        }
+        // 3. normal equations of every cube, back to back on the stream
+        for (int i = 0; i < n; ++i) {
+            const rp_fit_desc &d = descs[i];
+            if (d.precision == RP_PREC_MIXED)
+                rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
+                               b + off_n[i], nullptr, stream);
+            else
+                rp::gram_fp64(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
+                              b + off_n[i], nullptr, stream);
+        }
+        // 4. all constraint folds and bordered solves, one launch
+        std::vector<rp::SolveJob> jobs((size_t)n);
+        for (int i = 0; i < n; ++i) {
+            const rp_fit_desc &d = descs[i];
+            jobs[i] = rp::SolveJob{A + off_nn[i], b + off_n[i], d.N, d.n_groups, d.group_ptr, d.group_idx,
+                                   d.resp_s, d.resp_t, d.qtot, q + off_n[i]};
+        }
+        std::vector<double> info;
+        rp::solve_batch(ctx, jobs, info, stream);
+        rp::status_check(ctx, stream);
+        RP_CUDA(cudaMemcpyAsync(q_out, q, sizeof(double) * off_n[n], cudaMemcpyDeviceToHost, stream));
+        RP_CUDA(cudaStreamSynchronize(stream));
+        if (info_out) std::copy(info.begin(), info.end(), info_out);
+        for (int i = 0; i < n; ++i)
+            if (info[4 * (size_t)i + 3] != 0.0)
+                rp::fail(RP_E_SINGULAR, "rp_fit: bordered system of cube " + std::to_string(i) + " is singular");
+    });
+    for (rp_ewald *ew : ews)
+        if (ew) {
+            rp::ewald_free(ew);
+            delete ew;
+        }
     return rc;
+}
+
+int rp_launch_count(long long *out) {
+    if (!out) return RP_E_ARG;
+    *out = rp::g_launches.load();
+    return RP_OK;
+}
+
+int rp_set_timing(rp_ctx *ctx, int enable) {
+    if (!ctx) return RP_E_ARG;
+    ctx->timing = enable != 0;
+    return RP_OK;
+}
+
+int rp_stage_times(rp_ctx *ctx, char *names, size_t names_cap, double *ms, int *count_inout) {
+    if (!ctx || !count_inout) return RP_E_ARG;
+    return guarded(ctx, [&] {
+        std::vector<std::string> order;
+        std::unordered_map<std::string, std::pair<double, int>> acc;
+        for (auto &m : ctx->marks) {
+            RP_CUDA(cudaEventSynchronize(m.b));
+            float t = 0.f;
+            RP_CUDA(cudaEventElapsedTime(&t, m.a, m.b));
+            if (!acc.count(m.name)) order.push_back(m.name);
+            acc[m.name].first += t;
+            acc[m.name].second += 1;
+            cudaEventDestroy(m.a);
+            cudaEventDestroy(m.b);
+        }
+        ctx->marks.clear();
+        std::string joined;
+        int cap = *count_inout, k = 0;
+        for (auto &nm : order) {
+            if (k >= cap) break;
+            if (ms) {
+                ms[2 * k] = acc[nm].first;
+                ms[2 * k + 1] = acc[nm].second;
+            }
+            joined += nm + "\n";
+            ++k;
+        }
+        *count_inout = k;
+        if (names && names_cap) {
+            size_t n = std::min(names_cap - 1, joined.size());
+            std::memcpy(names, joined.data(), n);
+            names[n] = 0;
+        }
+    });
+}
+
+int rp_fit(rp_ctx *ctx, const rp_fit_desc *d, double *q_out, int64_t *M_out, rp_stream_t stream) {
+    if (!ctx || !d || !q_out) return RP_E_ARG;
+    return rp_fit_batch(ctx, 1, d, nullptr, q_out, M_out, nullptr, stream);
 }
 
 }  // extern "C"

@@ -328,78 +328,121 @@ static void host_fold(int N, const std::vector<double> &A, const std::vector<dou
     }
 }
 
+void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream) {
+    const int nj = (int)jobs.size();
+    info.assign((size_t)nj * 4, 0.0);
+    if (nj == 0) return;
+    std::vector<FoldPlan> plans((size_t)nj);
+    size_t n_map = 0, n_mptr = 0, n_midx = 0, n_red = 0, n_sq = 0;
+    for (int j = 0; j < nj; ++j) {
+        const SolveJob &J = jobs[j];
+        RP_REQUIRE(J.A && J.b && J.q && J.N > 0, "rp_solve: null argument or N <= 0");
+        RP_REQUIRE(J.n_groups == 0 || (J.group_ptr && J.group_idx), "rp_solve: groups given without arrays");
+        plans[j] = make_plan(J.N, J.n_groups, J.group_ptr, J.group_idx);
+        const size_t n1 = (size_t)plans[j].n + 1;
+        n_map += J.N;
+        n_mptr += plans[j].mem_ptr.size();
+        n_midx += std::max<size_t>(plans[j].mem_idx.size(), 1);
+        n_red += n1;
+        n_sq += n1 * n1;
+    }
+    int *d_map = ctx->buf_t<int>("s_map", n_map);
+    int *d_mptr = ctx->buf_t<int>("s_mptr", n_mptr);
+    int *d_midx = ctx->buf_t<int>("s_midx", n_midx);
+    double *d_rs = ctx->buf_t<double>("s_rs", n_red);
+    double *d_rt = ctx->buf_t<double>("s_rt", n_red);
+    double *As = ctx->buf_t<double>("s_As", n_sq);
+    double *A0 = ctx->buf_t<double>("s_A0", n_sq);
+    double *bs = ctx->buf_t<double>("s_bs", n_red);
+    double *x = ctx->buf_t<double>("s_x", n_red);
+    double *r = ctx->buf_t<double>("s_r", n_red);
+    int *perm = ctx->buf_t<int>("s_perm", n_red);
+    double *d_info = ctx->buf_t<double>("s_info", (size_t)nj * 4);
+    SolveDesc *d_desc = ctx->buf_t<SolveDesc>("s_desc", (size_t)nj);
+    // host staging of the small per-system tables, one upload each
+    std::vector<int> h_map(n_map), h_mptr(n_mptr), h_midx(n_midx, 0);
+    std::vector<double> h_rs(n_red, 0.0), h_rt(n_red, 0.0);
+    std::vector<SolveDesc> descs((size_t)nj);
+    size_t o_map = 0, o_mptr = 0, o_midx = 0, o_red = 0, o_sq = 0;
+    for (int j = 0; j < nj; ++j) {
+        const SolveJob &J = jobs[j];
+        const FoldPlan &p = plans[j];
+        const int n1 = p.n + 1;
+        std::copy(p.map.begin(), p.map.end(), h_map.begin() + o_map);
+        std::copy(p.mem_ptr.begin(), p.mem_ptr.end(), h_mptr.begin() + o_mptr);
+        std::copy(p.mem_idx.begin(), p.mem_idx.end(), h_midx.begin() + o_midx);
+        if (J.resp_s)
+            for (int rr = 0; rr < p.n; ++rr) {
+                h_rs[o_red + rr] = J.resp_s[p.ind[rr]];
+                h_rt[o_red + rr] = J.resp_t ? J.resp_t[p.ind[rr]] : 0.0;
+            }
+        SolveDesc &d = descs[j];
+        d.A = J.A; d.b = J.b; d.N = J.N; d.n = p.n;
+        d.mem_ptr = d_mptr + o_mptr; d.mem_idx = d_midx + o_midx;
+        d.resp_s = J.resp_s ? d_rs + o_red : nullptr; d.resp_t = J.resp_s ? d_rt + o_red : nullptr;
+        d.map = d_map + o_map; d.qtot = J.qtot;
+        d.As = As + o_sq; d.A0 = A0 + o_sq; d.bs = bs + o_red; d.x = x + o_red; d.r = r + o_red;
+        d.perm = perm + o_red; d.q = J.q; d.info = d_info + 4 * (size_t)j;
+        o_map += J.N;
+        o_mptr += p.mem_ptr.size();
+        o_midx += std::max<size_t>(p.mem_idx.size(), 1);
+        o_red += (size_t)n1;
+        o_sq += (size_t)n1 * n1;
+    }
+    RP_CUDA(cudaMemcpyAsync(d_map, h_map.data(), sizeof(int) * n_map, cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_mptr, h_mptr.data(), sizeof(int) * n_mptr, cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_midx, h_midx.data(), sizeof(int) * n_midx, cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_rs, h_rs.data(), sizeof(double) * n_red, cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_rt, h_rt.data(), sizeof(double) * n_red, cudaMemcpyHostToDevice, stream));
+    for (int j = 0; j < nj; ++j) {
+        const SolveJob &J = jobs[j];
+        const FoldPlan &p = plans[j];
+        const int n1 = p.n + 1;
+        if (p.disjoint) {
+            long long tot = (long long)n1 * n1;
+            build_bordered_kernel<<<std::min<long long>(ceil_div(tot, 256), 4096), 256, 0, stream>>>(descs[j]);
+            RP_LAUNCH_CHECK();
+        } else {
+            // overlapping groups: the reference's sequential folding on the host
+            std::vector<double> hA((size_t)J.N * J.N), hb((size_t)J.N), Ar, br, w;
+            RP_CUDA(cudaMemcpyAsync(hA.data(), J.A, sizeof(double) * hA.size(), cudaMemcpyDeviceToHost, stream));
+            RP_CUDA(cudaMemcpyAsync(hb.data(), J.b, sizeof(double) * J.N, cudaMemcpyDeviceToHost, stream));
+            RP_CUDA(cudaStreamSynchronize(stream));
+            host_fold(J.N, hA, hb, J.n_groups, J.group_ptr, J.group_idx, p, Ar, br, w);
+            std::vector<double> hs((size_t)n1 * n1, 0.0), hbs((size_t)n1, 0.0);
+            for (int rr = 0; rr < p.n; ++rr) {
+                for (int c = 0; c < p.n; ++c) hs[(size_t)rr * n1 + c] = Ar[(size_t)rr * p.n + c];
+                double rsv = J.resp_s ? J.resp_s[p.ind[rr]] : 0.0;
+                double rtv = (J.resp_s && J.resp_t) ? J.resp_t[p.ind[rr]] : 0.0;
+                hs[(size_t)rr * n1 + rr] += rsv;
+                hs[(size_t)rr * n1 + p.n] = w[rr];
+                hs[(size_t)p.n * n1 + rr] = w[rr];
+                hbs[rr] = br[rr] + rsv * rtv;
+            }
+            hbs[p.n] = J.qtot;
+            RP_CUDA(cudaMemcpyAsync(descs[j].As, hs.data(), sizeof(double) * hs.size(), cudaMemcpyHostToDevice, stream));
+            RP_CUDA(cudaMemcpyAsync(descs[j].A0, hs.data(), sizeof(double) * hs.size(), cudaMemcpyHostToDevice, stream));
+            RP_CUDA(cudaMemcpyAsync(descs[j].bs, hbs.data(), sizeof(double) * hbs.size(), cudaMemcpyHostToDevice, stream));
+            RP_CUDA(cudaStreamSynchronize(stream));
+        }
+    }
+    RP_CUDA(cudaMemcpyAsync(d_desc, descs.data(), sizeof(SolveDesc) * nj, cudaMemcpyHostToDevice, stream));
+    {
+        StageTimer tt(ctx, "solve_lu", stream);
+        lu_solve_refine_kernel<<<nj, kLU, 0, stream>>>(d_desc);
+        RP_LAUNCH_CHECK();
+    }
+    RP_CUDA(cudaMemcpyAsync(info.data(), d_info, sizeof(double) * 4 * nj, cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaStreamSynchronize(stream));
+}
+
 void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
                const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,
                double *info, cudaStream_t stream) {
-    RP_REQUIRE(A_dev && b_dev && q_dev && N > 0, "rp_solve: null argument or N <= 0");
-    RP_REQUIRE(n_groups == 0 || (group_ptr && group_idx), "rp_solve: groups given without arrays");
-    FoldPlan p = make_plan(N, n_groups, group_ptr, group_idx);
-    const int n1 = p.n + 1;
-    std::vector<double> rs, rt;
-    if (resp_s) {
-        rs.assign((size_t)p.n, 0.0);
-        rt.assign((size_t)p.n, 0.0);
-        for (int r = 0; r < p.n; ++r) {
-            rs[r] = resp_s[p.ind[r]];
-            rt[r] = resp_t ? resp_t[p.ind[r]] : 0.0;
-        }
-    }
-    int *d_map = ctx->buf_t<int>("s_map", (size_t)N);
-    int *d_mptr = ctx->buf_t<int>("s_mptr", p.mem_ptr.size());
-    int *d_midx = ctx->buf_t<int>("s_midx", std::max<size_t>(p.mem_idx.size(), 1));
-    double *d_rs = resp_s ? ctx->buf_t<double>("s_rs", (size_t)p.n) : nullptr;
-    double *d_rt = resp_s ? ctx->buf_t<double>("s_rt", (size_t)p.n) : nullptr;
-    double *As = ctx->buf_t<double>("s_As", (size_t)n1 * n1);
-    double *A0 = ctx->buf_t<double>("s_A0", (size_t)n1 * n1);
-    double *bs = ctx->buf_t<double>("s_bs", (size_t)n1);
-    double *x = ctx->buf_t<double>("s_x", (size_t)n1);
-    double *r = ctx->buf_t<double>("s_r", (size_t)n1);
-    int *perm = ctx->buf_t<int>("s_perm", (size_t)n1);
-    double *d_info = ctx->buf_t<double>("s_info", 4);
-    SolveDesc *d_desc = ctx->buf_t<SolveDesc>("s_desc", 1);
-    RP_CUDA(cudaMemcpyAsync(d_map, p.map.data(), sizeof(int) * N, cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemcpyAsync(d_mptr, p.mem_ptr.data(), sizeof(int) * p.mem_ptr.size(), cudaMemcpyHostToDevice, stream));
-    if (!p.mem_idx.empty())
-        RP_CUDA(cudaMemcpyAsync(d_midx, p.mem_idx.data(), sizeof(int) * p.mem_idx.size(), cudaMemcpyHostToDevice, stream));
-    if (resp_s) {
-        RP_CUDA(cudaMemcpyAsync(d_rs, rs.data(), sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
-        RP_CUDA(cudaMemcpyAsync(d_rt, rt.data(), sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
-    }
-    SolveDesc d{};
-    d.A = A_dev; d.b = b_dev; d.N = N; d.n = p.n; d.mem_ptr = d_mptr; d.mem_idx = d_midx;
-    d.resp_s = d_rs; d.resp_t = d_rt; d.map = d_map; d.qtot = qtot;
-    d.As = As; d.A0 = A0; d.bs = bs; d.x = x; d.r = r; d.perm = perm; d.q = q_dev; d.info = d_info;
-    if (p.disjoint) {
-        build_bordered_kernel<<<ceil_div((long long)n1 * n1, 256) > 4096 ? 4096 : ceil_div((long long)n1 * n1, 256), 256,
-                                0, stream>>>(d);
-        RP_LAUNCH_CHECK();
-    } else {
-        // overlapping groups: reference's sequential folding on the host
-        std::vector<double> hA((size_t)N * N), hb((size_t)N), Ar, br, w;
-        RP_CUDA(cudaMemcpyAsync(hA.data(), A_dev, sizeof(double) * hA.size(), cudaMemcpyDeviceToHost, stream));
-        RP_CUDA(cudaMemcpyAsync(hb.data(), b_dev, sizeof(double) * N, cudaMemcpyDeviceToHost, stream));
-        RP_CUDA(cudaStreamSynchronize(stream));
-        host_fold(N, hA, hb, n_groups, group_ptr, group_idx, p, Ar, br, w);
-        std::vector<double> hs((size_t)n1 * n1, 0.0), hbs((size_t)n1, 0.0);
-        for (int rr = 0; rr < p.n; ++rr) {
-            for (int c = 0; c < p.n; ++c) hs[(size_t)rr * n1 + c] = Ar[(size_t)rr * p.n + c];
-            if (resp_s) hs[(size_t)rr * n1 + rr] += rs[rr];
-            hs[(size_t)rr * n1 + p.n] = w[rr];
-            hs[(size_t)p.n * n1 + rr] = w[rr];
-            hbs[rr] = br[rr] + (resp_s ? rs[rr] * rt[rr] : 0.0);
-        }
-        hbs[p.n] = qtot;
-        RP_CUDA(cudaMemcpyAsync(As, hs.data(), sizeof(double) * hs.size(), cudaMemcpyHostToDevice, stream));
-        RP_CUDA(cudaMemcpyAsync(A0, hs.data(), sizeof(double) * hs.size(), cudaMemcpyHostToDevice, stream));
-        RP_CUDA(cudaMemcpyAsync(bs, hbs.data(), sizeof(double) * hbs.size(), cudaMemcpyHostToDevice, stream));
-        RP_CUDA(cudaStreamSynchronize(stream));
-    }
-    RP_CUDA(cudaMemcpyAsync(d_desc, &d, sizeof(SolveDesc), cudaMemcpyHostToDevice, stream));
-    lu_solve_refine_kernel<<<1, kLU, 0, stream>>>(d_desc);
-    RP_LAUNCH_CHECK();
-    double hinfo[4];
-    RP_CUDA(cudaMemcpyAsync(hinfo, d_info, sizeof(hinfo), cudaMemcpyDeviceToHost, stream));
-    RP_CUDA(cudaStreamSynchronize(stream));
+    std::vector<SolveJob> jobs(1);
+    jobs[0] = SolveJob{A_dev, b_dev, N, n_groups, group_ptr, group_idx, resp_s, resp_t, qtot, q_dev};
+    std::vector<double> hinfo;
+    solve_batch(ctx, jobs, hinfo, stream);
     if (info) {
         info[0] = hinfo[0];
         info[1] = hinfo[1];

@@ -29,14 +29,30 @@ typedef struct {
 static void *work(void *p) {
     job_t *j = (job_t *)p;
     const double *ax = j->ax;
+    int *cand = (int *)malloc(sizeof(int) * (size_t)(j->nimg > 0 ? j->nimg : 1));
+    const double rc = sqrt(j->rc2);
+    /* per grid row (fixed j, k): only images within Rc of the row's segment can
+     * contribute, so each point scans that short candidate list */
+    double L2 = ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2];
     for (int k = j->k0; k < j->k1; ++k) {
         for (int jj = 0; jj < j->ny; ++jj) {
+            double bx = ax[3] * jj + ax[6] * k, by = ax[4] * jj + ax[7] * k, bz = ax[5] * jj + ax[8] * k;
+            int nc = 0;
+            for (int t = 0; t < j->nimg; ++t) {
+                double px = j->img[3 * t] - bx, py = j->img[3 * t + 1] - by, pz = j->img[3 * t + 2] - bz;
+                double u = (px * ax[0] + py * ax[1] + pz * ax[2]) / L2;   /* position along the row */
+                if (u < 0) u = 0;
+                if (u > j->nx - 1) u = j->nx - 1;
+                double dx = px - u * ax[0], dy = py - u * ax[1], dz = pz - u * ax[2];
+                if (dx * dx + dy * dy + dz * dz <= (rc + 1e-9) * (rc + 1e-9)) cand[nc++] = t;
+            }
             for (int i = 0; i < j->nx; ++i) {
                 double gx = ax[0] * i + ax[3] * jj + ax[6] * k;
                 double gy = ax[1] * i + ax[4] * jj + ax[7] * k;
                 double gz = ax[2] * i + ax[5] * jj + ax[8] * k;
                 double acc = 0.0;
-                for (int t = 0; t < j->nimg; ++t) {
+                for (int c = 0; c < nc; ++c) {
+                    int t = cand[c];
                     double dx = gx - j->img[3 * t];
                     double dy = gy - j->img[3 * t + 1];
                     double dz = gz - j->img[3 * t + 2];
@@ -50,6 +66,7 @@ static void *work(void *p) {
             }
         }
     }
+    free(cand);
     return NULL;
 }
 

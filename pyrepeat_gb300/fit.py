@@ -58,6 +58,21 @@ def _ptr(a):
     return None if a is None else a.ctypes.data
 
 
+TOP_REL = 1e-5      # k with kcoef >= TOP_REL * max kcoef go to the exact block
+TOP_MAX_K = 256     # at most 8 stages of 64 columns (cos + sin)
+
+
+def plan_kblocks_py(cube):
+    """(k in the exact block, k in the FP16 block) for a cube, as the library plans them."""
+    from .synth import kspace
+    _, _, kc = kspace(cube.box_vectors, cube.cutoff, cube.kmax)
+    K = len(kc)
+    heavy = int((kc >= TOP_REL * kc.max()).sum())
+    ntop = min(K, max(32, -(-heavy // 32) * 32))
+    ntop = min(ntop, TOP_MAX_K)
+    return ntop, K - ntop
+
+
 class Context:
     """One rp_ctx on one CUDA device."""
 
@@ -136,11 +151,43 @@ class Context:
         self.check(rc, "rp_solve")
         return q, {"residual": float(info[0]), "pivot_min": float(info[1]), "pivot_max": float(info[2])}
 
+    def set_timing(self, on: bool = True):
+        self.check(self.lib.rp_set_timing(self.ptr, 1 if on else 0), "rp_set_timing")
+
+    def stage_times(self) -> dict:
+        """{stage: (total ms, launches)} since the last call (CUDA events on each stage's stream)."""
+        names = ctypes.create_string_buffer(8192)
+        ms = np.zeros(2 * 64)
+        cnt = ctypes.c_int(64)
+        self.check(self.lib.rp_stage_times(self.ptr, names, 8192, ms.ctypes.data, ctypes.byref(cnt)),
+                   "rp_stage_times")
+        labels = names.value.decode().split("\n")[:cnt.value]
+        return {lab: (float(ms[2 * i]), int(ms[2 * i + 1])) for i, lab in enumerate(labels)}
+
+    def potential(self, ew, atoms, q, idx=None, npts=None):
+        """Ewald potential of charges q at grid points (all points when idx is None)."""
+        t = self.torch
+        atoms = np.ascontiguousarray(atoms, dtype=np.float64)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        if idx is None:
+            if npts is None:
+                raise ValueError("npts needed when idx is None")
+        else:
+            npts = int(idx.numel())
+        out = t.zeros(int(npts), dtype=t.float64, device=self.dev)
+        rc = self.lib.rp_potential(self.ptr, ew.ptr, atoms.ctypes.data, q.ctypes.data, len(q),
+                                   idx.data_ptr() if idx is not None else None, int(npts), out.data_ptr(),
+                                   self._stream())
+        self.check(rc, "rp_potential")
+        return out
+
     # ------------------------------------------------------------------ whole fits
     def fit_cube(self, cube, precision=_lib.PREC_MIXED, V_dev=None, keep_normal=False):
         """Fit one synth.Cube-like object (atom_index, atom_pos, n_grid, axis_vector, V,
         symm_groups, resp, kmax, cutoff, vdw_factor, vdw_max, total_charge)."""
         t = self.torch
+        if V_dev is None:
+            V_dev = getattr(cube, "V_dev", None)
         if V_dev is None:
             V_dev = t.from_numpy(np.ascontiguousarray(cube.V, dtype=np.float64)).to(self.dev)
         kept, Vc, M, _ = self.filter(cube.n_grid, cube.axis_vector, cube.atom_pos, cube.atom_index, V_dev,
@@ -158,24 +205,59 @@ class Context:
             res.A, res.b = A, b
         return res
 
-    def fit_host(self, cube, precision=_lib.PREC_MIXED):
-        """End to end through rp_fit: host V and atoms in, host charges out."""
+    def _desc(self, cube, precision, keep):
+        """rp_fit_desc for a cube; arrays it points to are appended to `keep`."""
         d = _lib.RpFitDesc()
         d.grid = _lib.make_grid(cube.n_grid, cube.axis_vector)
-        V = np.ascontiguousarray(cube.V, dtype=np.float64)
         atoms = np.ascontiguousarray(cube.atom_pos, dtype=np.float64)
         Z = np.ascontiguousarray(cube.atom_index, dtype=np.int32)
         ng, ptr, idx, rs, rt = constraint_arrays(Z, cube.symm_groups, cube.resp)
-        d.V, d.atoms, d.Z, d.N = V.ctypes.data, atoms.ctypes.data, Z.ctypes.data, len(Z)
+        V = None
+        if cube.V is not None and not hasattr(cube.V, "data_ptr"):
+            V = np.ascontiguousarray(cube.V, dtype=np.float64)
+        keep.extend([atoms, Z, ptr, idx, rs, rt, V])
+        d.V = V.ctypes.data if V is not None else None
+        d.atoms, d.Z, d.N = atoms.ctypes.data, Z.ctypes.data, len(Z)
         d.vdw_factor, d.vdw_max, d.cutoff, d.qtot = cube.vdw_factor, cube.vdw_max, cube.cutoff, cube.total_charge
         d.kmax, d.n_groups = cube.kmax, ng
         d.group_ptr, d.group_idx, d.resp_s, d.resp_t = ptr.ctypes.data, idx.ctypes.data, _ptr(rs), _ptr(rt)
         d.precision = int(precision)
-        q = np.zeros(len(Z))
+        return d
+
+    def fit_host(self, cube, precision=_lib.PREC_MIXED):
+        """End to end through rp_fit: host V and atoms in, host charges out."""
+        keep = []
+        d = self._desc(cube, precision, keep)
+        q = np.zeros(cube.n_atoms)
         M = ctypes.c_int64(0)
         rc = self.lib.rp_fit(self.ptr, ctypes.byref(d), q.ctypes.data, ctypes.byref(M), self._stream())
         self.check(rc, "rp_fit")
         return FitResult(q, int(M.value), "fp64" if precision == _lib.PREC_FP64 else "mixed")
+
+    def fit_batch(self, cubes, precision=_lib.PREC_MIXED, V_dev=None, out=None):
+        """Fit many cubes in one rp_fit_batch call.  V_dev: optional list of device
+        tensors holding each cube's grid values (else cube.V is read from the host).
+        Returns a list of charge arrays (views into one buffer) and the kept counts."""
+        n = len(cubes)
+        keep = []
+        arr = (_lib.RpFitDesc * n)()
+        for i, c in enumerate(cubes):
+            arr[i] = self._desc(c, precision[i] if isinstance(precision, (list, tuple)) else precision, keep)
+        vptr = None
+        if V_dev is not None:
+            vptr = (ctypes.c_void_p * n)(*[v.data_ptr() if v is not None else None for v in V_dev])
+        total = sum(c.n_atoms for c in cubes)
+        q = out if out is not None else np.zeros(total)
+        M = np.zeros(n, dtype=np.int64)
+        info = np.zeros(4 * n)
+        rc = self.lib.rp_fit_batch(self.ptr, n, ctypes.cast(arr, ctypes.c_void_p), vptr, q.ctypes.data,
+                                   M.ctypes.data, info.ctypes.data, self._stream())
+        self.check(rc, "rp_fit_batch")
+        res, o = [], 0
+        for c in cubes:
+            res.append(q[o:o + c.n_atoms])
+            o += c.n_atoms
+        return res, M, info.reshape(n, 4)
 
 
 class Ewald:

@@ -57,6 +57,12 @@ class Cube:
     vdw_max: float = 1000.0
     total_charge: float = 0.0
     name: str = ""
+    V_dev: object = None              # optional device copy of V (torch tensor)
+
+    def host_V(self) -> np.ndarray:
+        if self.V is None and self.V_dev is not None:
+            self.V = self.V_dev.cpu().numpy()
+        return self.V
 
     @property
     def n_atoms(self) -> int:
@@ -247,14 +253,30 @@ def ewald_potential_grid(n_grid, axis, atom_pos, q, cutoff, kmax, threads=None) 
 
 # ----------------------------------------------------------------------------- workloads
 
-def _finish(cube: Cube, rng: np.random.Generator, noise: float, threads=None) -> Cube:
+def _finish(cube: Cube, rng: np.random.Generator, noise: float, threads=None, ctx=None) -> Cube:
+    """ESP = Ewald potential of the planted charges + N(0, noise).  With a
+    pyrepeat_gb300.fit.Context the potential is evaluated on its GPU (rp_potential)
+    and the cube keeps V only on the device (V_dev); otherwise on the host."""
+    if ctx is not None:
+        import torch
+        ew = ctx.ewald(cube.n_grid, cube.axis_vector, cube.cutoff, cube.kmax)
+        try:
+            V = ctx.potential(ew, cube.atom_pos, cube.charges_true, npts=cube.n_points)
+        finally:
+            ew.close()
+        gen = torch.Generator(device=V.device)
+        gen.manual_seed(int(rng.integers(0, 2**62)))
+        V += noise * torch.randn(V.shape, dtype=V.dtype, device=V.device, generator=gen)
+        cube.V_dev = V
+        cube.V = None
+        return cube
     V = ewald_potential_grid(cube.n_grid, cube.axis_vector, cube.atom_pos, cube.charges_true,
                              cube.cutoff, cube.kmax, threads)
     cube.V = V + rng.normal(0.0, noise, size=V.shape)
     return cube
 
 
-def make_water(seed: int = 1, n_grid: int = 72, noise: float = 1e-4, threads=None) -> Cube:
+def make_water(seed: int = 1, n_grid: int = 72, noise: float = 1e-4, threads=None, ctx=None) -> Cube:
     """3 waters in a cubic 18.0 Bohr cell (O separated by >= 5 Bohr; H at 1.81
     Bohr and 104.5 deg, random orientation; q_O ~ N(-0.8, 0.05), H = -q_O/2)."""
     rng = np.random.default_rng(seed)
@@ -278,7 +300,7 @@ def make_water(seed: int = 1, n_grid: int = 72, noise: float = 1e-4, threads=Non
     axis = cell / n_grid
     cube = Cube(np.array(Z), pos, np.array([n_grid] * 3), axis, None,
                 charges_true=np.array(q), kmax=7, name=f"water-{n_grid}")
-    return _finish(cube, rng, noise, threads)
+    return _finish(cube, rng, noise, threads, ctx)
 
 
 def _random_neutral(rng, n, sigma):
@@ -287,7 +309,7 @@ def _random_neutral(rng, n, sigma):
 
 
 def make_mof(seed: int = 2, n_grid: int = 128, kmax: int = 12, noise: float = 1e-4,
-             L: float = 25.8, counts=(32, 104, 192, 96), threads=None) -> Cube:
+             L: float = 25.8, counts=(32, 104, 192, 96), threads=None, ctx=None) -> Cube:
     """MOF-like cubic cell: Zn:O:C:H = 4:13:24:12 (x8 = 424 atoms) at >= 2.2 Bohr."""
     rng = np.random.default_rng(seed)
     cell = lower_triangular_cell(L, L, L)
@@ -298,7 +320,7 @@ def make_mof(seed: int = 2, n_grid: int = 128, kmax: int = 12, noise: float = 1e
     axis = cell / n_grid
     cube = Cube(Z, pos, np.array([n_grid] * 3), axis, None, charges_true=q, kmax=kmax,
                 name=f"mof-{len(Z)}-{n_grid}-k{kmax}")
-    return _finish(cube, rng, noise, threads)
+    return _finish(cube, rng, noise, threads, ctx)
 
 
 def random_symmetry_groups(rng, n_atoms, n_groups, lo=2, hi=6):
@@ -316,7 +338,7 @@ def random_symmetry_groups(rng, n_atoms, n_groups, lo=2, hi=6):
 
 def make_tric(seed: int = 3, n_grid=(200, 210, 225), n_atoms: int = 2000, noise: float = 1e-4,
               n_groups: int = 150, threads=None, lengths=(40.0, 42.0, 45.0),
-              angles=(85.0, 95.0, 100.0), kmax: int = 7) -> Cube:
+              angles=(85.0, 95.0, 100.0), kmax: int = 7, ctx=None) -> Cube:
     """Triclinic cell 40 x 42 x 45 Bohr, 85/95/100 deg; C/H/N/O 40/40/10/10%;
     150 symmetry groups of 2-6 atoms; RESP 0.1 -> 0 on C, N, O."""
     rng = np.random.default_rng(seed)
@@ -338,14 +360,14 @@ def make_tric(seed: int = 3, n_grid=(200, 210, 225), n_atoms: int = 2000, noise:
     cube = Cube(Z, pos, ng, axis, None, charges_true=q, symm_groups=groups,
                 resp={"C": (0.1, 0.0), "N": (0.1, 0.0), "O": (0.1, 0.0)}, kmax=kmax,
                 name=f"tric-{len(Z)}-{'x'.join(map(str, n_grid))}")
-    return _finish(cube, rng, noise, threads)
+    return _finish(cube, rng, noise, threads, ctx)
 
 
 BATCH_ELEMENTS = (1, 6, 7, 8, 16, 30)
 
 
 def make_batch_item(seed: int, large: bool = False, noise: float = 1e-4, threads=None,
-                    with_symmetry: bool | None = None) -> Cube:
+                    with_symmetry: bool | None = None, ctx=None) -> Cube:
     """One cube of the batched distribution: 20-300 atoms (800-1500 and 160^3
     when large), cubic or orthorhombic 12-30 Bohr, spacing 0.2-0.3 Bohr
     clamped to 40..96 points per axis; q ~ N(0, 0.5) neutral; half carry
@@ -384,7 +406,7 @@ def make_batch_item(seed: int, large: bool = False, noise: float = 1e-4, threads
     axis = cell / ng[:, None]
     cube = Cube(Z, pos, ng, axis, None, charges_true=q, symm_groups=groups, resp=resp, kmax=7,
                 name=f"batch-{seed}")
-    return _finish(cube, rng, noise, threads)
+    return _finish(cube, rng, noise, threads, ctx)
 
 
 # ----------------------------------------------------------------------------- files
