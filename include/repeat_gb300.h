@@ -126,6 +126,20 @@ int rp_solve(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n
 int rp_potential(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const double *q, int N,
                  const int32_t *idx_dev, int64_t npts, double *out_dev, rp_stream_t stream);
 
+/* rp_solve without any device allocation, for callers that cannot allocate
+ * device memory while they run (a serving loop that must not stall on the
+ * device-wide synchronisation cudaMalloc/cudaFree may cause, or an embedder whose
+ * device memory is owned by its own allocator).  Same arguments and results as
+ * rp_solve, but no ctx: its scratch is a static 4.5 MiB device array inside the
+ * library, so N is limited to 512 atoms (RP_E_ARG beyond that).  No counterpart in
+ * the reference.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make it before any stream
+ * capture.  Every call shares the array: calls that overlap on the GPU race, so
+ * serialise them.  Returns RP_E_SINGULAR for a singular bordered system. */
+int rp_solve_noalloc(const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
+                     const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,
+                     double *info, rp_stream_t stream);
+
 /* One whole fit from host memory, as repeat.py's main() runs it for
  * `--fit-type 1 [--gpu]`: H2D of V, filter, Ewald setup, normal equations,
  * constraints, solve, D2H of the charges.  q_out [N] host. M_out may be NULL. */

@@ -22,7 +22,7 @@ PREC_MIXED = 1
 # every symbol include/repeat_gb300.h declares
 EXPORTS = ["rp_version", "rp_ctx_create", "rp_ctx_destroy", "rp_last_error", "rp_filter", "rp_ewald_setup",
            "rp_ewald_destroy", "rp_ewald_info", "rp_gram", "rp_solve", "rp_potential", "rp_fit",
-           "rp_fit_batch", "rp_set_timing", "rp_stage_times", "rp_launch_count"]
+           "rp_fit_batch", "rp_set_timing", "rp_stage_times", "rp_launch_count", "rp_solve_noalloc"]
 
 
 class RepeatError(RuntimeError):
@@ -87,6 +87,8 @@ def load(path: str | None = None):
     L.rp_potential.argtypes = [P, P, P, P, I, P, L64, P, P]
     L.rp_fit.restype = I
     L.rp_fit.argtypes = [P, ctypes.POINTER(RpFitDesc), P, ctypes.POINTER(L64), P]
+    L.rp_solve_noalloc.restype = I
+    L.rp_solve_noalloc.argtypes = [P, P, I, I, P, P, P, P, D, P, P, P]
     L.rp_launch_count.restype = I
     L.rp_launch_count.argtypes = [ctypes.POINTER(ctypes.c_longlong)]
     L.rp_set_timing.restype = I

@@ -18,6 +18,7 @@
 // x += LU^{-1}(b - A x), and reports the refined residual and pivot range.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <set>
 
 #include "common.cuh"
@@ -452,3 +453,142 @@ void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int
 }
 
 }  // namespace rp
+
+// ---------------------------------------------------------------------------
+// No-allocation variant of the constrained bordered solve.
+//
+// For callers that must not allocate device memory while they run: a serving
+// loop that cannot afford the device-wide synchronisation cudaMalloc/cudaFree
+// may cause, or an embedder whose device memory is owned entirely by its own
+// allocator.  Its scratch is the file-scope array below (kNoAllocScratchBytes,
+// enough for N <= kNoAllocMaxN atoms), which every GPU that loads this library
+// keeps until the process exits.  Host code only sees a host-side stand-in for
+// that symbol; the device address comes from cudaGetSymbolAddress, looked up once
+// per device with that device current, on the first call made on it (make that
+// first call before any stream capture).  All calls share the array and it keeps
+// the last call's contents (every region is fully rewritten before it is read),
+// so calls that overlap on the GPU race: serialise them on one stream.
+namespace rp {
+namespace {
+
+constexpr int kNoAllocMaxN = 512;
+constexpr size_t kNoAllocScratchBytes = 4718592;  // 4.5 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+unsigned char *noalloc_scratch_device() {
+    static std::mutex mu;
+    static unsigned char *addr[256] = {};
+    int dev = 0;
+    RP_CUDA(cudaGetDevice(&dev));
+    RP_REQUIRE(dev >= 0 && dev < 256, "rp_solve_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) fail(RP_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        addr[dev] = static_cast<unsigned char *>(p);
+    }
+    return addr[dev];
+}
+
+// Bump allocator over the static array (256-byte aligned slices).
+struct Carve {
+    unsigned char *base;
+    size_t off = 0;
+    template <class T>
+    T *take(size_t count) {
+        size_t bytes = (count * sizeof(T) + 255) & ~size_t(255);
+        if (off + bytes > kNoAllocScratchBytes) fail(RP_E_NOMEM, "rp_solve_noalloc: static scratch exhausted");
+        T *p = reinterpret_cast<T *>(base + off);
+        off += bytes;
+        return p;
+    }
+};
+
+}  // namespace
+}  // namespace rp
+
+extern "C" int rp_solve_noalloc(const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
+                                const int *group_idx, const double *resp_s, const double *resp_t, double qtot,
+                                double *q_dev, double *info, rp_stream_t stream_) {
+    using namespace rp;
+    cudaStream_t stream = (cudaStream_t)stream_;
+    try {
+        RP_REQUIRE(A_dev && b_dev && q_dev, "rp_solve_noalloc: null argument");
+        if (N <= 0 || N > kNoAllocMaxN) return RP_E_ARG;  // N must be in 1..512
+        RP_REQUIRE(n_groups == 0 || (group_ptr && group_idx), "rp_solve_noalloc: groups given without arrays");
+        FoldPlan p = make_plan(N, n_groups, group_ptr, group_idx);
+        const int n1 = p.n + 1;
+        Carve cv{noalloc_scratch_device()};
+        int *d_map = cv.take<int>((size_t)N);
+        int *d_mptr = cv.take<int>(p.mem_ptr.size());
+        int *d_midx = cv.take<int>(std::max<size_t>(p.mem_idx.size(), 1));
+        double *d_rs = cv.take<double>((size_t)p.n);
+        double *d_rt = cv.take<double>((size_t)p.n);
+        double *As = cv.take<double>((size_t)n1 * n1);
+        double *A0 = cv.take<double>((size_t)n1 * n1);
+        double *bs = cv.take<double>((size_t)n1);
+        double *x = cv.take<double>((size_t)n1);
+        double *r = cv.take<double>((size_t)n1);
+        int *perm = cv.take<int>((size_t)n1);
+        double *d_info = cv.take<double>(4);
+        SolveDesc *d_desc = cv.take<SolveDesc>(1);
+        std::vector<double> rs((size_t)p.n, 0.0), rt((size_t)p.n, 0.0);
+        if (resp_s)
+            for (int k = 0; k < p.n; ++k) {
+                rs[k] = resp_s[p.ind[k]];
+                rt[k] = resp_t ? resp_t[p.ind[k]] : 0.0;
+            }
+        RP_CUDA(cudaMemcpyAsync(d_map, p.map.data(), sizeof(int) * N, cudaMemcpyHostToDevice, stream));
+        RP_CUDA(cudaMemcpyAsync(d_mptr, p.mem_ptr.data(), sizeof(int) * p.mem_ptr.size(), cudaMemcpyHostToDevice, stream));
+        if (!p.mem_idx.empty())
+            RP_CUDA(cudaMemcpyAsync(d_midx, p.mem_idx.data(), sizeof(int) * p.mem_idx.size(), cudaMemcpyHostToDevice,
+                                    stream));
+        if (p.n > 0) {
+            RP_CUDA(cudaMemcpyAsync(d_rs, rs.data(), sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
+            RP_CUDA(cudaMemcpyAsync(d_rt, rt.data(), sizeof(double) * p.n, cudaMemcpyHostToDevice, stream));
+        }
+        SolveDesc d{};
+        d.A = A_dev; d.b = b_dev; d.N = N; d.n = p.n; d.mem_ptr = d_mptr; d.mem_idx = d_midx;
+        d.resp_s = resp_s ? d_rs : nullptr; d.resp_t = resp_s ? d_rt : nullptr; d.map = d_map; d.qtot = qtot;
+        d.As = As; d.A0 = A0; d.bs = bs; d.x = x; d.r = r; d.perm = perm; d.q = q_dev; d.info = d_info;
+        if (p.disjoint) {
+            build_bordered_kernel<<<std::min<long long>(ceil_div((long long)n1 * n1, 256), 4096), 256, 0, stream>>>(d);
+            RP_LAUNCH_CHECK();
+        } else {
+            std::vector<double> hA((size_t)N * N), hb((size_t)N), Ar, br, w;
+            RP_CUDA(cudaMemcpyAsync(hA.data(), A_dev, sizeof(double) * hA.size(), cudaMemcpyDeviceToHost, stream));
+            RP_CUDA(cudaMemcpyAsync(hb.data(), b_dev, sizeof(double) * N, cudaMemcpyDeviceToHost, stream));
+            RP_CUDA(cudaStreamSynchronize(stream));
+            host_fold(N, hA, hb, n_groups, group_ptr, group_idx, p, Ar, br, w);
+            std::vector<double> hs((size_t)n1 * n1, 0.0), hbs((size_t)n1, 0.0);
+            for (int k = 0; k < p.n; ++k) {
+                for (int c = 0; c < p.n; ++c) hs[(size_t)k * n1 + c] = Ar[(size_t)k * p.n + c];
+                hs[(size_t)k * n1 + k] += rs[k];
+                hs[(size_t)k * n1 + p.n] = w[k];
+                hs[(size_t)p.n * n1 + k] = w[k];
+                hbs[k] = br[k] + rs[k] * rt[k];
+            }
+            hbs[p.n] = qtot;
+            RP_CUDA(cudaMemcpyAsync(As, hs.data(), sizeof(double) * hs.size(), cudaMemcpyHostToDevice, stream));
+            RP_CUDA(cudaMemcpyAsync(A0, hs.data(), sizeof(double) * hs.size(), cudaMemcpyHostToDevice, stream));
+            RP_CUDA(cudaMemcpyAsync(bs, hbs.data(), sizeof(double) * hbs.size(), cudaMemcpyHostToDevice, stream));
+        }
+        RP_CUDA(cudaMemcpyAsync(d_desc, &d, sizeof(SolveDesc), cudaMemcpyHostToDevice, stream));
+        lu_solve_refine_kernel<<<1, kLU, 0, stream>>>(d_desc);
+        RP_LAUNCH_CHECK();
+        double hinfo[4];
+        RP_CUDA(cudaMemcpyAsync(hinfo, d_info, sizeof(hinfo), cudaMemcpyDeviceToHost, stream));
+        RP_CUDA(cudaStreamSynchronize(stream));
+        if (info) {
+            info[0] = hinfo[0];
+            info[1] = hinfo[1];
+            info[2] = hinfo[2];
+        }
+        return hinfo[3] != 0.0 ? RP_E_SINGULAR : RP_OK;
+    } catch (const rp::Error &e) {
+        return e.code;
+    } catch (const std::exception &) {
+        return RP_E_ARG;
+    }
+}
