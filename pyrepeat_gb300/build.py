@@ -28,6 +28,7 @@ CUDA_SOURCES = [
     "filter.cu",
     "ewald_tables.cu",
     "phi_fp64.cu",
+    "recip_sep.cu",
     "gram_mixed.cu",
     "solve.cu",
     "potential.cu",

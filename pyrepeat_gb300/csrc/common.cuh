@@ -125,14 +125,14 @@ struct rp_ewald {
     int *d_kidx = nullptr;        // 3K
     double *d_kcoef = nullptr;    // K
     double *d_kvec = nullptr;     // 3K
-    // the same k-set ordered by increasing kcoef (used by the tensor-core path so
-    // that small terms are accumulated before large ones)
-    int *d_kidx_s = nullptr;
-    double *d_kcoef_s = nullptr;
-    double *d_kvec_s = nullptr;
     double2 *d_ex = nullptr;      // (kmax+1) * nx   e^{2 pi i n1 i / nx}
     double2 *d_ey = nullptr;      // (2kmax+1) * ny  e^{2 pi i n2 j / ny}, n2 offset by kmax
     double2 *d_ez = nullptr;      // (2kmax+1) * nz
+    // the same phases as double-float float4 (re_h, re_l, im_h, im_l) over the index
+    // range the k-set uses, n in [-(kmax-1), kmax-1] (offset kmax-1; n1 >= 0 only)
+    float4 *d_exf = nullptr;      // kmax * nx
+    float4 *d_eyf = nullptr;      // (2kmax-1) * ny
+    float4 *d_ezf = nullptr;      // (2kmax-1) * nz
 };
 
 namespace rp {
@@ -177,6 +177,12 @@ void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<dou
 void atom_tables_fp64(const rp_ewald *ew, const double *d_atoms, int N, double *d_B, int ldb, cudaStream_t s);
 void grid_tables_fp64(const rp_ewald *ew, const int32_t *d_kept, int64_t m0, int64_t rows, double *d_T, int ldt,
                       cudaStream_t s);
+
+// Reciprocal sum by separable lattice phases (recip_sep.cu): E[r][col][n1] for every
+// grid row r = j + l*ny, col = atom (d_q == nullptr) or one charge-weighted column.
+size_t recip_rows_bytes(const rp_ewald *ew, int ncols);
+void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const double *d_q, int N, float4 *E,
+                cudaStream_t stream);
 
 // Shared epilogue kernels (phi_fp64.cu).
 void column_sums_fp64(const double *X, int64_t rows, int cols, int ld, double *out, bool accumulate,

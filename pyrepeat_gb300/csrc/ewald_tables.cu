@@ -15,6 +15,7 @@
 #include <cmath>
 
 #include "common.cuh"
+#include "df.cuh"
 
 namespace rp {
 
@@ -107,41 +108,46 @@ void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax) {
     RP_CUDA(cudaMemcpy(ew->d_kidx, ew->kidx.data(), sizeof(int) * ew->kidx.size(), cudaMemcpyHostToDevice));
     RP_CUDA(cudaMemcpy(ew->d_kcoef, ew->kcoef.data(), sizeof(double) * ew->kcoef.size(), cudaMemcpyHostToDevice));
     RP_CUDA(cudaMemcpy(ew->d_kvec, ew->kvec.data(), sizeof(double) * ew->kvec.size(), cudaMemcpyHostToDevice));
-    {
-        std::vector<int> perm((size_t)ew->K);
-        for (int k = 0; k < ew->K; ++k) perm[k] = k;
-        std::stable_sort(perm.begin(), perm.end(), [&](int x, int y) { return ew->kcoef[x] < ew->kcoef[y]; });
-        std::vector<int> ki((size_t)3 * ew->K);
-        std::vector<double> kc((size_t)ew->K), kv((size_t)3 * ew->K);
-        for (int k = 0; k < ew->K; ++k) {
-            kc[k] = ew->kcoef[perm[k]];
-            for (int d = 0; d < 3; ++d) {
-                ki[3 * k + d] = ew->kidx[3 * perm[k] + d];
-                kv[3 * k + d] = ew->kvec[3 * perm[k] + d];
-            }
-        }
-        RP_CUDA(cudaMalloc(&ew->d_kidx_s, sizeof(int) * ki.size()));
-        RP_CUDA(cudaMalloc(&ew->d_kcoef_s, sizeof(double) * kc.size()));
-        RP_CUDA(cudaMalloc(&ew->d_kvec_s, sizeof(double) * kv.size()));
-        RP_CUDA(cudaMemcpy(ew->d_kidx_s, ki.data(), sizeof(int) * ki.size(), cudaMemcpyHostToDevice));
-        RP_CUDA(cudaMemcpy(ew->d_kcoef_s, kc.data(), sizeof(double) * kc.size(), cudaMemcpyHostToDevice));
-        RP_CUDA(cudaMemcpy(ew->d_kvec_s, kv.data(), sizeof(double) * kv.size(), cudaMemcpyHostToDevice));
-    }
     RP_CUDA(cudaMemcpy(ew->d_ex, ex.data(), sizeof(double2) * ex.size(), cudaMemcpyHostToDevice));
     RP_CUDA(cudaMemcpy(ew->d_ey, ey.data(), sizeof(double2) * ey.size(), cudaMemcpyHostToDevice));
     RP_CUDA(cudaMemcpy(ew->d_ez, ez.data(), sizeof(double2) * ez.size(), cudaMemcpyHostToDevice));
+
+    // double-float copies over n in [-(kmax-1), kmax-1] for the separable reciprocal sum
+    const int P = kmax - 1, nw = 2 * P + 1;
+    std::vector<float4> exf((size_t)(P + 1) * nx), eyf((size_t)nw * ny), ezf((size_t)nw * nz);
+    for (int n = 0; n <= P; ++n)
+        for (int i = 0; i < nx; ++i) {
+            const double2 v = ex[(size_t)n * nx + i];
+            exf[(size_t)n * nx + i] = dfa::split(v.x, v.y);
+        }
+    for (int n = -P; n <= P; ++n) {
+        for (int j = 0; j < ny; ++j) {
+            const double2 v = ey[(size_t)(n + kmax) * ny + j];
+            eyf[(size_t)(n + P) * ny + j] = dfa::split(v.x, v.y);
+        }
+        for (int l = 0; l < nz; ++l) {
+            const double2 v = ez[(size_t)(n + kmax) * nz + l];
+            ezf[(size_t)(n + P) * nz + l] = dfa::split(v.x, v.y);
+        }
+    }
+    RP_CUDA(cudaMalloc(&ew->d_exf, sizeof(float4) * exf.size()));
+    RP_CUDA(cudaMalloc(&ew->d_eyf, sizeof(float4) * eyf.size()));
+    RP_CUDA(cudaMalloc(&ew->d_ezf, sizeof(float4) * ezf.size()));
+    RP_CUDA(cudaMemcpy(ew->d_exf, exf.data(), sizeof(float4) * exf.size(), cudaMemcpyHostToDevice));
+    RP_CUDA(cudaMemcpy(ew->d_eyf, eyf.data(), sizeof(float4) * eyf.size(), cudaMemcpyHostToDevice));
+    RP_CUDA(cudaMemcpy(ew->d_ezf, ezf.data(), sizeof(float4) * ezf.size(), cudaMemcpyHostToDevice));
 }
 
 void ewald_free(rp_ewald *ew) {
     cudaFree(ew->d_kidx);
     cudaFree(ew->d_kcoef);
     cudaFree(ew->d_kvec);
-    cudaFree(ew->d_kidx_s);
-    cudaFree(ew->d_kcoef_s);
-    cudaFree(ew->d_kvec_s);
     cudaFree(ew->d_ex);
     cudaFree(ew->d_ey);
     cudaFree(ew->d_ez);
+    cudaFree(ew->d_exf);
+    cudaFree(ew->d_eyf);
+    cudaFree(ew->d_ezf);
 }
 
 void prune_shifts(const rp_ewald *ew, const double *atoms, int N, std::vector<double> &out, int &zero_idx) {

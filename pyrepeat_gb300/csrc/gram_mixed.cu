@@ -1,29 +1,34 @@
-// Mixed-precision Phi -> normal equations on the sm_103a tensor cores.
+// Mixed-precision Phi -> normal equations on GB300.
 //
 // Replaces, on the device, the Phi build of EwaldCalculator._compute_gpu*
 // (repeat.py:1199-1435) and the Gram accumulation of fit_charges
-// (repeat.py:2246-2276).  Per chunk of kept points:
+// (repeat.py:2246-2276).  Once per fit:
 //
-//  1. tables  T[m][k'] = sqrt(w_k) 2^10 [cos(k.g_m) | sin(k.g_m)] and
-//             B[a][k'] = sqrt(w_k) 2^10 [cos(k.r_a) | sin(k.r_a)], each split into
-//             an FP16 pair hi + lo (22 significant bits; sqrt(w) on both sides keeps
-//             every term inside FP16 range).  Grid phases are exact per-axis tables.
-//  2. GEMM-1  Phi_recip = T B^T on tcgen05 (kind::f16, FP32 accumulator in TMEM)
-//             as hi*hi + hi*lo + lo*hi, written atom-major (Phi_t[a][m]).
-//  3. real    Phi_t[a][m] += sum_s [r <= Rc] erfc(sqrt(alpha) r)/r in FP32, with
-//             coordinates taken relative to a per-tile origin.
-//  4. split   X[a][m] = (Phi_t[a][m] - c_a) * 2^e_a as FP16 hi + lo, plus a row for
-//             the centred ESP: c_a is the column mean of the first chunk (a per-
-//             column shift corrected exactly later), 2^e_a a power-of-two row scale.
-//  5. GEMM-2  G = X X^T on tcgen05 (upper-triangle tiles), split over points so each
-//             FP32 run is short; partial tiles are summed in FP64 in a fixed order.
-//  6. finish  A = G - s s^T/M, b = G[:,V] - s sum(V)/M with s = sum_m (Phi - c)
+//  0. recip   E[r][a][n1] for every grid row r (separable reciprocal sum, stages A
+//             and B in recip_sep.cu, double-float on the FP32 pipe).
+//
+// Then per chunk of kept points (Phi exists for one chunk only):
+//
+//  1. Phi     Phi_t[a][m] = real-space erfc sum (FP32 terms from double-float
+//             coordinates, FP64 at the cutoff, FP64 per-pair sums)
+//             + Re sum_n1 ex[n1][i_m] E[r_m][a][n1] (double-float), written once,
+//             atom-major (phi_chunk_kernel).
+//  2. split   X[a][m] = (Phi_t[a][m] - c_a) * 2^e_a cut into four 7-bit fixed-point
+//             digits, plus a row for the centred ESP: c_a is the column mean of the
+//             first chunk (a per-column shift corrected exactly later), 2^e_a a
+//             power-of-two row scale.
+//  3. Gram    G = X X^T on tcgen05 (kind::f16, FP32 accumulators in TMEM) with all
+//             16 digit products kept: every partial sum is an integer below 2^24,
+//             so the Gram of the staged Phi is exact; partial tiles of point splits
+//             are summed in FP64 in a fixed order.
+//  4. finish  A = G - s s^T/M, b = G[:,V] - s sum(V)/M with s = sum_m (Phi - c)
 //             (FP64), i.e. repeat.py:2266-2276 for the shifted columns.
 //
-// Dropping lo*lo costs ~2^-22 relative per product; measured on the synthetic
-// workloads the charges move by <~2e-7 e against the FP64 fit (BF16 hi+lo, with
-// 16 significant bits and the atom-table error coherent across all points, moved
-// them by ~5e-6 e, which is why the split type is FP16).
+// Error budget: Phi carries the FP32 real-space terms (~1e-7 relative, unbiased)
+// and the 28-bit digit quantisation of the Gram input (~2^-29 of each row's
+// range, unbiased); the reciprocal sum is exact to ~2^-44.  The tensor cores'
+// FP32 accumulation truncates, which is why the Gram is done in exact integer
+// digits instead of as an FP16/BF16 hi+lo product.
 #include <cuda.h>
 #include <cuda_fp16.h>
 
@@ -32,26 +37,15 @@
 #include <cstdlib>
 
 #include "common.cuh"
+#include "df.cuh"
 #include "tc.cuh"
 
 namespace rp {
 namespace {
 
-constexpr int kBM = 128;       // tile rows (TMEM lanes)
-constexpr int kBN = 128;       // tile columns
+constexpr int kBM = 128;       // Gram tile rows (TMEM lanes)
 constexpr int kBK = 64;        // K elements per stage (128 B of FP16 = one swizzle row)
 constexpr int kTileBytes = kBM * kBK * 2;  // 16 KB per operand tile
-constexpr float kTableScale = 1024.0f;     // 2^10 on each table side
-
-// ---- GEMM-1 (k-contraction): FP16 hi+lo operands, 3 products, 4 TMEM accumulators
-// Stage kb accumulates into accumulator kb % 4, so each FP32 accumulator sees a
-// quarter of the additions (the tensor core's FP32 accumulation truncates; fewer
-// additions per accumulator means less drift).  The epilogue adds the four.
-constexpr int kRecStages = 3;
-constexpr int kRecAcc = 4;
-constexpr int kRecThreads = 192;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2-5 epilogue
-constexpr int kRecStageBytes = 4 * kTileBytes;
-constexpr int kRecSmem = kRecStages * kRecStageBytes + 1024 + 256;
 
 // ---- GEMM-2 (Gram): exact integer products of four 7-bit fixed-point slices
 // x = 2^-6 (x0 + 2^-7 x1 + 2^-14 x2 + 2^-21 x3), x_s integers with |x0| <= 32,
@@ -75,144 +69,15 @@ constexpr int kBTileBytes = kGN * kBK * 2;             // 8 KB
 constexpr int kGramStageBytes = kGSlices * kTileBytes + kGSlices * kBTileBytes;
 constexpr int kGramSmem = kGramStages * kGramStageBytes + 1024 + 256;
 
-struct RecArgs {
-    int m_tiles, kb_total, rows_m, rows_n;
-    double out_scale;
-    double *out;
-    long long ld_out;
-    int *status;
-};
-
 struct GramArgs {
     int nt, ntri, kb_total, kb_per_split, flush;  // flush: stages per exact FP32 run (<= kGramFlush)
     double *out;  // partial tiles [split*ntri + tri][col][row], FP64 (exact integers)
     int *status;
 };
 
-__device__ __forceinline__ void tri_decode(int t, int nt, int &ti, int &tj) {
-    // upper-triangle tile t -> (ti <= tj), row-major over ti
-    ti = 0;
-    int rowlen = nt;
-    while (t >= rowlen) {
-        t -= rowlen;
-        ++ti;
-        --rowlen;
-    }
-    tj = ti + t;
-}
-
 __device__ __forceinline__ uint8_t *align1024(uint8_t *raw) {
     const uint32_t s = tc::smem_u32(raw);
     return raw + (((s + 1023u) & ~1023u) - s);
-}
-
-__global__ void __launch_bounds__(kRecThreads, 1) recip_gemm_kernel(const __grid_constant__ CUtensorMap tmAh,
-                                                                      const __grid_constant__ CUtensorMap tmAl,
-                                                                      const __grid_constant__ CUtensorMap tmBh,
-                                                                      const __grid_constant__ CUtensorMap tmBl,
-                                                                      RecArgs g) {
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t *smem = align1024(smem_raw);
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kRecStages * kRecStageBytes);
-    uint64_t *empty = full + kRecStages;
-    uint64_t *accb = empty + kRecStages;
-    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(accb + 1);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int a_row0 = (blockIdx.x % g.m_tiles) * kBM, b_row0 = (blockIdx.x / g.m_tiles) * kBN;
-    const int nkb = g.kb_total;  // >= 1
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kRecStages; ++s) {
-            tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], 1);
-        }
-        tc::mbar_init(accb, 1);
-        tc::fence_mbar_init();
-    }
-    if (warp == 1) tc::tmem_alloc(tmem_holder, kRecAcc * kBN);
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    const uint32_t tmem = *tmem_holder;
-
-    if (warp == 0 && lane == 0) {
-        tc::prefetch_tmap(&tmAh);
-        tc::prefetch_tmap(&tmAl);
-        tc::prefetch_tmap(&tmBh);
-        tc::prefetch_tmap(&tmBl);
-        int issued = 0;
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % kRecStages, u = kb / kRecStages;
-            if (u > 0 && !tc::mbar_wait(&empty[s], (u - 1) & 1, g.status)) break;
-            uint8_t *st = smem + s * kRecStageBytes;
-            tc::mbar_arrive_expect_tx(&full[s], kRecStageBytes);
-            const int x = kb * kBK;
-            tc::tma_load_2d(st, &tmAh, x, a_row0, &full[s]);
-            tc::tma_load_2d(st + kTileBytes, &tmAl, x, a_row0, &full[s]);
-            tc::tma_load_2d(st + 2 * kTileBytes, &tmBh, x, b_row0, &full[s]);
-            tc::tma_load_2d(st + 3 * kTileBytes, &tmBl, x, b_row0, &full[s]);
-            issued = kb + 1;
-        }
-        if (*reinterpret_cast<volatile int *>(g.status) != 0)
-            for (int kb = max(0, issued - kRecStages); kb < issued; ++kb)
-                tc::mbar_wait(&full[kb % kRecStages], (kb / kRecStages) & 1, nullptr);
-    } else if (warp == 1 && lane == 0) {
-        const uint32_t idesc = tc::idesc_f16_f32(kBM, kBN);
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % kRecStages, u = kb / kRecStages;
-            if (!tc::mbar_wait(&full[s], u & 1, g.status)) break;
-            tc::fence_after_sync();
-            const uint32_t st = tc::smem_u32(smem + s * kRecStageBytes);
-            const uint64_t ah = tc::sdesc_k_sw128(st), al = tc::sdesc_k_sw128(st + kTileBytes);
-            const uint64_t bh = tc::sdesc_k_sw128(st + 2 * kTileBytes), bl = tc::sdesc_k_sw128(st + 3 * kTileBytes);
-            const uint32_t d = tmem + (uint32_t)((kb % kRecAcc) * kBN);
-            const uint32_t first = (kb < kRecAcc) ? 1u : 0u;  // first use of this accumulator
-#pragma unroll
-            for (int kk = 0; kk < kBK / 16; ++kk) {
-                const uint64_t o = (uint64_t)(kk * 2);  // 32 B per K=16 step, in 16-B units
-                tc::umma_f16(d, ah + o, bh + o, idesc, (first && kk == 0) ? 0u : 1u);
-                tc::umma_f16(d, ah + o, bl + o, idesc, 1u);
-                tc::umma_f16(d, al + o, bh + o, idesc, 1u);
-            }
-            tc::umma_commit(&empty[s]);
-        }
-        tc::umma_commit(accb);
-    } else if (warp >= 2) {
-        if (tc::mbar_wait(accb, 0, g.status) && *reinterpret_cast<volatile int *>(g.status) == 0) {
-            tc::fence_after_sync();
-            const int lane_base = (warp & 3) * 32;
-            const int m = a_row0 + lane_base + lane;
-            const int nacc = min(nkb, kRecAcc);
-#pragma unroll 1
-            for (int c = 0; c < kBN / 32; ++c) {
-                double v[32];
-                {
-                    float w[32];
-                    tc::tmem_ld_32x32(tmem + ((uint32_t)lane_base << 16) + (uint32_t)(c * 32), w);
-#pragma unroll
-                    for (int i = 0; i < 32; ++i) v[i] = (double)w[i];
-                }
-                for (int q = 1; q < nacc; ++q) {
-                    float w[32];
-                    tc::tmem_ld_32x32(tmem + ((uint32_t)lane_base << 16) + (uint32_t)(q * kBN + c * 32), w);
-#pragma unroll
-                    for (int i = 0; i < 32; ++i) v[i] += (double)w[i];
-                }
-                if (m < g.rows_m) {
-#pragma unroll
-                    for (int i = 0; i < 32; ++i) {
-                        const int n = b_row0 + c * 32 + i;
-                        if (n < g.rows_n) g.out[(long long)n * g.ld_out + m] = v[i] * g.out_scale;
-                    }
-                }
-            }
-        }
-    }
-    if (warp == 1 && lane == 0) tc::mbar_wait(accb, 0, nullptr);  // last MMAs landed before TMEM is freed
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (warp == 1) tc::tmem_dealloc(tmem, kRecAcc * kBN);
 }
 
 // Gram tile t -> (ti, tj): rows [128 ti, +128), columns [64 tj, +64), tj >= 2 ti.
@@ -370,415 +235,313 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
     if (warp == 1) tc::tmem_dealloc(tmem, 512);
 }
 
-// ---- GEMM-1b (heaviest k columns): exact products of four 7-bit fixed-point
-// slices of T (points) and B (atoms), 16 products in 7 weight groups (TMEM 448
-// columns of a 128 x 64 tile).  A group gets at most 16 MMAs per stage, each
-// adding <= 2^16, and the block has <= kTopMaxStages stages, so every FP32 sum is
-// an exact integer; the epilogue folds the groups into an int64 and adds
-// 2^-54 * I * out_scale to Phi_t (FP64).
-constexpr int kTopSlices = 4;
-constexpr int kTopGroups = 7;
-constexpr int kTopMaxStages = 8;
-constexpr int kTopStages = 2;
-constexpr int kTopThreads = 64 + 32 * 8;
-constexpr int kTopStageBytes = kTopSlices * kTileBytes + kTopSlices * kBTileBytes;
-constexpr int kTopSmem = kTopStages * kTopStageBytes + 1024 + 256;
-
-struct TopArgs {
-    int m_tiles, kb_total, rows_m, rows_n;
-    double out_scale;
-    double *out;
-    long long ld_out;
-    int *status;
-};
-
-__global__ void __launch_bounds__(kTopThreads, 1) recip_top_kernel(
-    const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
-    const __grid_constant__ CUtensorMap ta2, const __grid_constant__ CUtensorMap ta3,
-    const __grid_constant__ CUtensorMap tb0, const __grid_constant__ CUtensorMap tb1,
-    const __grid_constant__ CUtensorMap tb2, const __grid_constant__ CUtensorMap tb3, TopArgs g) {
-    extern __shared__ uint8_t smem_raw[];
-    uint8_t *smem = align1024(smem_raw);
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kTopStages * kTopStageBytes);
-    uint64_t *empty = full + kTopStages;
-    uint64_t *accf = empty + kTopStages;
-    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(accf + 1);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int a_row0 = (blockIdx.x % g.m_tiles) * kBM, b_row0 = (blockIdx.x / g.m_tiles) * kGN;
-    const int nkb = g.kb_total;  // 1..kTopMaxStages
-    const CUtensorMap *ta[4] = {&ta0, &ta1, &ta2, &ta3};
-    const CUtensorMap *tb[4] = {&tb0, &tb1, &tb2, &tb3};
-
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kTopStages; ++s) {
-            tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], 1);
-        }
-        tc::mbar_init(accf, 1);
-        tc::fence_mbar_init();
-    }
-    if (warp == 1) tc::tmem_alloc(tmem_holder, 512);
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    const uint32_t tmem = *tmem_holder;
-
-    if (warp == 0 && lane == 0) {
-        int issued = 0;
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % kTopStages, u = kb / kTopStages;
-            if (u > 0 && !tc::mbar_wait(&empty[s], (u - 1) & 1, g.status)) break;
-            uint8_t *st = smem + s * kTopStageBytes;
-            tc::mbar_arrive_expect_tx(&full[s], kTopStageBytes);
-            const int x = kb * kBK;
-#pragma unroll
-            for (int q = 0; q < kTopSlices; ++q) {
-                tc::tma_load_2d(st + q * kTileBytes, ta[q], x, a_row0, &full[s]);
-                tc::tma_load_2d(st + kTopSlices * kTileBytes + q * kBTileBytes, tb[q], x, b_row0, &full[s]);
-            }
-            issued = kb + 1;
-        }
-        if (*reinterpret_cast<volatile int *>(g.status) != 0)
-            for (int kb = max(0, issued - kTopStages); kb < issued; ++kb)
-                tc::mbar_wait(&full[kb % kTopStages], (kb / kTopStages) & 1, nullptr);
-    } else if (warp == 1 && lane == 0) {
-        const uint32_t idesc = tc::idesc_f16_f32(kBM, kGN);
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % kTopStages, u = kb / kTopStages;
-            if (!tc::mbar_wait(&full[s], u & 1, g.status)) break;
-            tc::fence_after_sync();
-            const uint32_t st = tc::smem_u32(smem + s * kTopStageBytes);
-            uint64_t x[kTopSlices], y[kTopSlices];
-#pragma unroll
-            for (int q = 0; q < kTopSlices; ++q) {
-                x[q] = tc::sdesc_k_sw128(st + q * kTileBytes);
-                y[q] = tc::sdesc_k_sw128(st + kTopSlices * kTileBytes + q * kBTileBytes);
-            }
-#pragma unroll
-            for (int kk = 0; kk < kBK / 16; ++kk) {
-                const uint64_t o = (uint64_t)(kk * 2);
-                bool started[kTopGroups] = {false, false, false, false, false, false, false};
-#pragma unroll
-                for (int a = 0; a < kTopSlices; ++a)
-#pragma unroll
-                    for (int b = 0; b < kTopSlices; ++b) {
-                        const int grp = a + b;
-                        const uint32_t acc = (kb == 0 && kk == 0 && !started[grp]) ? 0u : 1u;
-                        started[grp] = true;
-                        tc::umma_f16(tmem + (uint32_t)(grp * kGN), x[a] + o, y[b] + o, idesc, acc);
-                    }
-            }
-            tc::umma_commit(&empty[s]);
-        }
-        tc::umma_commit(accf);
-    } else if (warp >= 2) {
-        const int ew = warp - 2;
-        const int lane_base = (warp & 3) * 32;
-        const int col0 = (ew >> 2) * 32;
-        if (tc::mbar_wait(accf, 0, g.status) && *reinterpret_cast<volatile int *>(g.status) == 0) {
-            tc::fence_after_sync();
-            long long acc[32];
-#pragma unroll
-            for (int i = 0; i < 32; ++i) acc[i] = 0;
-            const uint32_t base = tmem + ((uint32_t)lane_base << 16) + (uint32_t)col0;
-#pragma unroll
-            for (int q = 0; q < kTopGroups; ++q) {
-                float v[32];
-                tc::tmem_ld_32x32(base + (uint32_t)(q * kGN), v);
-                const int sh = 7 * (kTopGroups - 1 - q);
-#pragma unroll
-                for (int i = 0; i < 32; ++i) acc[i] += (long long)__float2int_rn(v[i]) << sh;
-            }
-            const int m = a_row0 + lane_base + lane;
-            if (m < g.rows_m) {
-#pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const int n = b_row0 + col0 + i;
-                    if (n < g.rows_n) g.out[(long long)n * g.ld_out + m] += ldexp((double)acc[i], -54) * g.out_scale;
-                }
-            }
-        }
-    }
-    if (warp == 1 && lane == 0) tc::mbar_wait(accf, 0, nullptr);
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (warp == 1) tc::tmem_dealloc(tmem, 512);
+// Four 7-bit signed digits of an integer I = round(x 2^27), |x| <= 1:
+// x ~ 2^-6 (s0 + 2^-7 s1 + 2^-14 s2 + 2^-21 s3), digits rounded half up so |s| <= 64,
+// each exact in FP16.  Integer shifts only (no FP64 on the per-element path).
+__device__ __forceinline__ void digits4(int v, __half *o0, __half *o1, __half *o2, __half *o3, long long idx) {
+    const int s0 = (v + (1 << 20)) >> 21;
+    int r = v - (s0 << 21);  // [-2^20, 2^20)
+    const int s1 = (r + (1 << 13)) >> 14;
+    r -= s1 << 14;           // [-2^13, 2^13)
+    const int s2 = (r + (1 << 6)) >> 7;
+    const int s3 = r - (s2 << 7);  // [-64, 64)
+    o0[idx] = __int2half_rn(s0);
+    o1[idx] = __int2half_rn(s1);
+    o2[idx] = __int2half_rn(s2);
+    o3[idx] = __int2half_rn(s3);
 }
 
-// ------------------------------------------------------------------ tables
-
-__device__ __forceinline__ void split_f16(float x, __half &hi, __half &lo) {
-    hi = __float2half_rn(x);
-    lo = __float2half_rn(x - __half2float(hi));
+// round((h + l) * sc) for a double-float (h, l) and a power of two sc, |(h + l) sc| <= 2^27:
+// rint of the high part is exact, the remainder (h sc - I1) is exact (Sterbenz), and the
+// low part decides the last unit.
+__device__ __forceinline__ int round_df(float h, float l, float sc) {
+    const float H = h * sc, L = l * sc;
+    const float I1 = rintf(H);
+    const float I2 = rintf(__fadd_rn(__fadd_rn(H, -I1), L));
+    return (int)I1 + (int)I2;
 }
 
-// k columns: the sorted (ascending kcoef) k-set is split into a "float" block
-// (all but the ntop heaviest k) and a "top" block (the ntop heaviest).  Within a
-// block, sorted k index q occupies columns cos, sin at (width - 2*count + 2*(q-q0)),
-// so the block ends with its heaviest k and starts with zero padding.
-struct KBlock {
-    int q0, count, width;  // sorted k range [q0, q0+count), width columns (multiple of 64)
-};
-
-__device__ __forceinline__ int kcol_to_q(const KBlock &b, int c, int &is_sin) {
-    const int off = c - (b.width - 2 * b.count);
-    if (off < 0) return -1;
-    is_sin = off & 1;
-    return b.q0 + (off >> 1);
+// Pairs closer than this radius (Bohr) get the FP64 real-space term; tunable with
+// RP_REAL_FP64_R.  Default 0: with double-float image coordinates the FP32 terms
+// keep the fitted charges within ~3e-7 e of the FP64 fit on the synthetic
+// workloads, so FP64 is used only to decide images that sit at the cutoff.
+float real_near2() {
+    static float v = [] {
+        const char *e = getenv("RP_REAL_FP64_R");
+        double r = e ? atof(e) : 0.0;
+        return (float)(r * r);
+    }();
+    return v;
 }
 
-// FP16 hi + lo atom table of the float block
-__global__ void atom_tables_f16_kernel(const double *__restrict__ kvec, const double *__restrict__ kcoef, KBlock blk,
-                                       const double *__restrict__ atoms, int N, __half *__restrict__ Bh,
-                                       __half *__restrict__ Bl) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)N * blk.width) return;
-    int a = (int)(t / blk.width), c = (int)(t - (long long)a * blk.width);
-    int is_sin = 0;
-    int q = kcol_to_q(blk, c, is_sin);
-    float val = 0.0f;
-    if (q >= 0) {
-        double kr = (atoms[3 * a] * kvec[3 * q] + atoms[3 * a + 1] * kvec[3 * q + 1]) + atoms[3 * a + 2] * kvec[3 * q + 2];
-        double sn, cs;
-        sincos(kr, &sn, &cs);
-        val = (float)(sqrt(kcoef[q]) * (double)kTableScale * (is_sin ? sn : cs));
-    }
-    __half h, l;
-    split_f16(val, h, l);
-    Bh[t] = h;
-    Bl[t] = l;
+// ------------------------------------------------------------------ Phi of one chunk
+
+constexpr int kPhiPts = 128;     // points per CTA (one per thread)
+constexpr int kPhiAtoms = 16;    // atoms per CTA
+constexpr int kMaxShifts = 128;  // pruned real-space shifts (checked on the host)
+
+// Image positions atom + shift as double-float, [N][S] x {hi (x, y, z, shift index), lo}
+__global__ void images_df_kernel(const double *__restrict__ atoms, int N, const double *__restrict__ shifts, int S,
+                                 float4 *__restrict__ img) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * S) return;
+    const int a = t / S, s = t - a * S;
+    double q[3];
+    for (int d = 0; d < 3; ++d) q[d] = atoms[3 * a + d] + shifts[3 * s + d];
+    const float hx = (float)q[0], hy = (float)q[1], hz = (float)q[2];
+    img[2 * t] = make_float4(hx, hy, hz, __int_as_float(s));
+    img[2 * t + 1] = make_float4((float)(q[0] - (double)hx), (float)(q[1] - (double)hy), (float)(q[2] - (double)hz), 0.f);
 }
 
-// FP16 hi + lo grid table of the float block (FP32 phase products)
-__global__ void grid_tables_f16_kernel(const int *__restrict__ kidx, const float *__restrict__ swk, KBlock blk,
-                                       int kmax, const float2 *__restrict__ ex, const float2 *__restrict__ ey,
-                                       const float2 *__restrict__ ez, int nx, int ny, int nz,
-                                       const int32_t *__restrict__ kept, long long m0, long long rows,
-                                       long long rows_pad, __half *__restrict__ Th, __half *__restrict__ Tl) {
-    // one thread per (point, column pair)
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int pairs = blk.width / 2;
-    if (t >= rows_pad * pairs) return;
-    long long m = t / pairs;
-    int cp = (int)(t - m * pairs);
-    int is_sin = 0;
-    int q = kcol_to_q(blk, 2 * cp, is_sin);
-    float re = 0.f, im = 0.f;
-    if (m < rows && q >= 0) {
-        int f = kept[m0 + m];
-        int layer = nx * ny;
-        int l = f / layer, rem = f - l * layer, j = rem / nx, i = rem - j * nx;
-        int n1 = kidx[3 * q], n2 = kidx[3 * q + 1], n3 = kidx[3 * q + 2];
-        float2 a = ex[n1 * nx + i], b = ey[(n2 + kmax) * ny + j], c = ez[(n3 + kmax) * nz + l];
-        float r1 = a.x * b.x - a.y * b.y, i1 = a.x * b.y + a.y * b.x;
-        float sw = swk[q];
-        re = (r1 * c.x - i1 * c.y) * sw;
-        im = (r1 * c.y + i1 * c.x) * sw;
-    }
-    __half h, l;
-    const long long base = m * (long long)blk.width + 2 * cp;
-    split_f16(re, h, l);
-    Th[base] = h;
-    Tl[base] = l;
-    split_f16(im, h, l);
-    Th[base + 1] = h;
-    Tl[base + 1] = l;
+// (ah + al) - (bh + bl) as a normalised double-float
+__device__ __forceinline__ float2 df_sub(float ah, float al, float bh, float bl) {
+    float s, e;
+    dfa::two_sum(ah, -bh, s, e);
+    e = __fadd_rn(e, __fadd_rn(al, -bl));
+    const float h = __fadd_rn(s, e);
+    return make_float2(h, __fadd_rn(e, -__fadd_rn(h, -s)));
 }
 
-// Four 7-bit fixed-point slices of x (|x| <= 1): x = 2^-6 (s0 + 2^-7 s1 + 2^-14 s2 + 2^-21 s3)
-// up to 2^-28.  One FP64 multiply and one rounding conversion give the 27-bit
-// integer round(x 2^27); the signed digits (round-half-up per digit, so
-// |s0| <= 64, |s1..s3| <= 64) then come from integer shifts.
-__device__ __forceinline__ void slice4(double x, __half *o0, __half *o1, __half *o2, __half *o3, long long idx) {
-    long long v = __double2ll_rn(x * 134217728.0);  // 2^27
-    long long s0 = (v + (1LL << 20)) >> 21;
-    long long r = v - (s0 << 21);                   // [-2^20, 2^20)
-    long long s1 = (r + (1LL << 13)) >> 14;
-    r -= s1 << 14;                                  // [-2^13, 2^13)
-    long long s2 = (r + (1LL << 6)) >> 7;
-    long long s3 = r - (s2 << 7);                   // [-64, 64)
-    o0[idx] = __int2half_rn((int)s0);
-    o1[idx] = __int2half_rn((int)s1);
-    o2[idx] = __int2half_rn((int)s2);
-    o3[idx] = __int2half_rn((int)s3);
-}
-
-// Fixed-point slices of the top block, atom side (FP64 values, scaled by sB)
-__global__ void atom_tables_top_kernel(const double *__restrict__ kvec, const double *__restrict__ kcoef, KBlock blk,
-                                       const double *__restrict__ atoms, int N, double sB, __half *__restrict__ B0,
-                                       __half *__restrict__ B1, __half *__restrict__ B2, __half *__restrict__ B3) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)N * blk.width) return;
-    int a = (int)(t / blk.width), c = (int)(t - (long long)a * blk.width);
-    int is_sin = 0;
-    int q = kcol_to_q(blk, c, is_sin);
-    double val = 0.0;
-    if (q >= 0) {
-        double kr = (atoms[3 * a] * kvec[3 * q] + atoms[3 * a + 1] * kvec[3 * q + 1]) + atoms[3 * a + 2] * kvec[3 * q + 2];
-        double sn, cs;
-        sincos(kr, &sn, &cs);
-        val = sqrt(kcoef[q]) * (double)kTableScale * (is_sin ? sn : cs) * sB;
-    }
-    slice4(val, B0, B1, B2, B3, t);
-}
-
-// Fixed-point slices of the top block, grid side (FP64 phase products, scaled by sT)
-__global__ void grid_tables_top_kernel(const int *__restrict__ kidx, const double *__restrict__ wtop, KBlock blk,
-                                       int kmax, const double2 *__restrict__ ex, const double2 *__restrict__ ey,
-                                       const double2 *__restrict__ ez, int nx, int ny, int nz,
-                                       const int32_t *__restrict__ kept, long long m0, long long rows,
-                                       long long rows_pad, double sT, __half *__restrict__ T0, __half *__restrict__ T1,
-                                       __half *__restrict__ T2, __half *__restrict__ T3) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int pairs = blk.width / 2;
-    if (t >= rows_pad * pairs) return;
-    long long m = t / pairs;
-    int cp = (int)(t - m * pairs);
-    int is_sin = 0;
-    int q = kcol_to_q(blk, 2 * cp, is_sin);
-    double re = 0.0, im = 0.0;
-    if (m < rows && q >= 0) {
-        int f = kept[m0 + m];
-        int layer = nx * ny;
-        int l = f / layer, rem = f - l * layer, j = rem / nx, i = rem - j * nx;
-        int n1 = kidx[3 * q], n2 = kidx[3 * q + 1], n3 = kidx[3 * q + 2];
-        double2 a = ex[n1 * nx + i], b = ey[(n2 + kmax) * ny + j], c = ez[(n3 + kmax) * nz + l];
-        double r1 = a.x * b.x - a.y * b.y, i1 = a.x * b.y + a.y * b.x;
-        double sw = wtop[q - blk.q0];  // sqrt(kcoef) 2^10 sT
-        re = (r1 * c.x - i1 * c.y) * sw;
-        im = (r1 * c.y + i1 * c.x) * sw;
-    }
-    const long long base = m * (long long)blk.width + 2 * cp;
-    slice4(re, T0, T1, T2, T3, base);
-    slice4(im, T0, T1, T2, T3, base + 1);
-}
-
-// ------------------------------------------------------------------ real space (FP32)
-
-constexpr int kRealPts = 128;   // points per CTA (one per thread)
-constexpr int kRealAtoms = 16;  // atoms per CTA
-
-// Phi_t[a][m] += sum_s erfc(sqrt(alpha) r)/r over images within Rc.  Distances
-// are formed in FP32 from double-float image coordinates taken relative to the
-// CTA's first point, so no coordinate rounding enters; pairs closer than
-// kNearR (where the term is large) are re-evaluated entirely in FP64, the rest
-// use FP32 erfcf.  The sum per (point, atom) is kept in FP64.
-
-__global__ void __launch_bounds__(kRealPts) realspace_kernel(
+// Phi_t[a][m] = sum over the images of atom a within Rc of erfc(sqrt(alpha) r)/r
+//             + Re sum_n1 ex[n1][i_m] E[r_m][a][n1],   stored as double-float (hi, lo).
+// Real space (repeat.py:944-966): the CTA first culls the images of its atoms to
+// those within Rc + 1e-3 Bohr of the bounding box of its points, in shift order
+// (warp-ballot compaction, so the summation order is fixed).  Distances are formed
+// in FP32 from double-float coordinates relative to the CTA's first point; images
+// within 0.05 % of Rc (where the reference's FP64 cutoff decision is made) and
+// pairs closer than sqrt(near2) are evaluated in FP64 with the reference's
+// expressions, the rest with FP32 erfcf.  Reciprocal part: stage C of the
+// separable sum in double-float.  `parts`: bit 0 real space, bit 1 reciprocal.
+// With psum/pmax given, the CTA also writes each atom's sum and max |Phi| over its
+// points (fixed-order reductions), the column statistics of the centring step.
+__global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
     const int32_t *__restrict__ kept, long long m0, long long rows, const double *__restrict__ axis, int nx, int ny,
-    const double *__restrict__ atoms, int N, const double *__restrict__ shifts, int S, int zero_idx, double rc,
-    double sa, float near2, double *__restrict__ phit, long long ld) {
-    __shared__ float3 img_hi[kRealAtoms * 128];   // S <= 128 images per atom (host checks)
-    __shared__ float3 img_lo[kRealAtoms * 128];
-    __shared__ double origin[3];
-    const long long mb = (long long)blockIdx.x * kRealPts;
-    const int a0 = blockIdx.y * kRealAtoms;
-    const int na = min(kRealAtoms, N - a0);
+    const double *__restrict__ atoms, int N, const double *__restrict__ shifts, int S, int scap, int zero_idx,
+    double rc, double sa, float near2, const float4 *__restrict__ img, const float4 *__restrict__ EX,
+    const float4 *__restrict__ E, int n1c, int parts, float2 *__restrict__ phit, long long ld,
+    double *__restrict__ psum, float *__restrict__ pmax) {
+    extern __shared__ float4 dsm[];
+    float4 *exs = dsm;                                    // [n1c][kPhiPts]   this thread's ex[n1][i]
+    float4 *img_hi = exs + (size_t)n1c * kPhiPts;         // [kPhiAtoms][scap] (x, y, z, shift index)
+    float4 *img_lo = img_hi + (size_t)kPhiAtoms * scap;   // [kPhiAtoms][scap]
+    __shared__ int ncand[kPhiAtoms];
+    __shared__ float bb[2][3][kPhiPts / 32];
+    __shared__ float2 wsum[kPhiPts / 32][kPhiAtoms];
+    __shared__ float wmax[kPhiPts / 32][kPhiAtoms];
+    const long long mb = (long long)blockIdx.x * kPhiPts;
+    const int a0 = blockIdx.y * kPhiAtoms;
+    const int na = min(kPhiAtoms, N - a0);
     const int layer = nx * ny;
-    if (threadIdx.x == 0) {
-        int f = kept[m0 + mb];
-        int l = f / layer, rem = f - l * layer, j = rem / nx, i = rem - j * nx;
-        for (int d = 0; d < 3; ++d) origin[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)l * axis[6 + d];
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < na * S; t += kRealPts) {
-        int a = t / S, s = t - a * S;
-        const double *p = atoms + 3 * (a0 + a);
-        double q[3];
-        for (int d = 0; d < 3; ++d) q[d] = (p[d] + shifts[3 * s + d]) - origin[d];
-        float3 h = make_float3((float)q[0], (float)q[1], (float)q[2]);
-        img_hi[a * S + s] = h;
-        img_lo[a * S + s] = make_float3((float)(q[0] - h.x), (float)(q[1] - h.y), (float)(q[2] - h.z));
-    }
-    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long m = mb + threadIdx.x;
-    if (m >= rows) return;
-    const int f = kept[m0 + m];
+    const bool valid = m < rows;
+
+    double origin[3];
+    {
+        const int f0 = kept[m0 + mb];
+        const int l = f0 / layer, rem = f0 - l * layer, j = rem / nx, i = rem - j * nx;
+        for (int d = 0; d < 3; ++d)
+            origin[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)l * axis[6 + d];
+    }
+    const int f = kept[m0 + (valid ? m : mb)];
     const int l = f / layer, rem = f - l * layer, j = rem / nx, i = rem - j * nx;
-    double gabs[3], gd[3];
+    double gabs[3];
+    float gh[3], gl[3], oh[3], ol[3];
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
         gabs[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)l * axis[6 + d];
-        gd[d] = gabs[d] - origin[d];
+        const double gd = gabs[d] - origin[d];
+        gh[d] = (float)gd;
+        gl[d] = (float)(gd - (double)gh[d]);
+        oh[d] = (float)origin[d];
+        ol[d] = (float)(origin[d] - (double)oh[d]);
     }
-    const float gx = (float)gd[0], gy = (float)gd[1], gz = (float)gd[2];
-    const float gxl = (float)(gd[0] - gx), gyl = (float)(gd[1] - gy), gzl = (float)(gd[2] - gz);
-    const float rc2 = (float)(rc * rc) * 1.0001f, saf = (float)sa;
-    for (int a = 0; a < na; ++a) {
-        double acc = 0.0;
-        float acc32 = 0.f;
-        const float3 *ih = img_hi + a * S, *il = img_lo + a * S;
-        const double *p = atoms + 3 * (a0 + a);
-        for (int s = 0; s < S; ++s) {
-            float dx = (gx - ih[s].x) + (gxl - il[s].x), dy = (gy - ih[s].y) + (gyl - il[s].y),
-                  dz = (gz - ih[s].z) + (gzl - il[s].z);
-            float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 > rc2) continue;
-            if (r2 < near2 || fabsf(r2 - (float)(rc * rc)) < 1e-3f * (float)(rc * rc)) {
-                double ex = gabs[0] - (p[0] + shifts[3 * s]), ey = gabs[1] - (p[1] + shifts[3 * s + 1]),
-                       ez = gabs[2] - (p[2] + shifts[3 * s + 2]);
-                double r = sqrt(ex * ex + ey * ey + ez * ez);
-                if (r <= rc && (s != zero_idx || r > 1e-10)) acc += erfc(sa * r) / r;
-            } else {
-                float r = sqrtf(r2);
-                if ((double)r <= rc) acc32 += erfcf(saf * r) / r;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float mn = gh[d], mx = gh[d];
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        }
+        if (lane == 0) {
+            bb[0][d][warp] = mn;
+            bb[1][d][warp] = mx;
+        }
+    }
+    if (parts & 2)
+        for (int n = 0; n < n1c; ++n) exs[n * kPhiPts + threadIdx.x] = EX[(long long)n * nx + i];
+    __syncthreads();
+
+    if (parts & 1) {
+        float bmin[3], bmax[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            bmin[d] = bb[0][d][0];
+            bmax[d] = bb[1][d][0];
+            for (int w = 1; w < kPhiPts / 32; ++w) {
+                bmin[d] = fminf(bmin[d], bb[0][d][w]);
+                bmax[d] = fmaxf(bmax[d], bb[1][d][w]);
             }
         }
-        phit[(long long)(a0 + a) * ld + m] += acc + (double)acc32;
+        const float reach = (float)rc + 1e-3f, reach2 = reach * reach;
+        for (int a = warp; a < kPhiAtoms; a += kPhiPts / 32) {
+            int base = 0;
+            if (a < na) {
+                const float4 *src = img + 2 * (size_t)(a0 + a) * S;
+                for (int s0 = 0; s0 < S; s0 += 32) {
+                    const int s = s0 + lane;
+                    bool keep = false;
+                    float4 h = make_float4(0.f, 0.f, 0.f, 0.f), lo = h;
+                    if (s < S) {
+                        const float4 ph = src[2 * s], pl = src[2 * s + 1];
+                        const float2 qx = df_sub(ph.x, pl.x, oh[0], ol[0]), qy = df_sub(ph.y, pl.y, oh[1], ol[1]),
+                                     qz = df_sub(ph.z, pl.z, oh[2], ol[2]);
+                        h = make_float4(qx.x, qy.x, qz.x, ph.w);
+                        lo = make_float4(qx.y, qy.y, qz.y, 0.f);
+                        const float dx = fmaxf(fmaxf(bmin[0] - h.x, h.x - bmax[0]), 0.f);
+                        const float dy = fmaxf(fmaxf(bmin[1] - h.y, h.y - bmax[1]), 0.f);
+                        const float dz = fmaxf(fmaxf(bmin[2] - h.z, h.z - bmax[2]), 0.f);
+                        keep = dx * dx + dy * dy + dz * dz <= reach2;
+                    }
+                    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                    if (keep) {
+                        const int pos = base + __popc(bal & ((1u << lane) - 1u));
+                        img_hi[a * scap + pos] = h;
+                        img_lo[a * scap + pos] = lo;
+                    }
+                    base += __popc(bal);
+                }
+            }
+            if (lane == 0) ncand[a] = base;
+        }
     }
+    __syncthreads();
+
+    const float rcc = (float)(rc * rc), rc2 = rcc * 1.0001f, saf = (float)sa;
+    const float fp64_below = fmaxf(near2, 1e-6f);
+    const long long row = f / nx;  // j + l * ny
+    for (int a = 0; a < na; ++a) {
+        dfa::acc v{0.f, 0.f};
+        double acc64 = 0.0;
+        bool used64 = false;
+        if (valid && (parts & 2)) {
+            const float4 *e = E + (row * N + a0 + a) * n1c;
+            for (int n = 0; n < n1c; ++n) dfa::cmac_re(v, exs[n * kPhiPts + threadIdx.x], e[n]);
+        }
+        if (valid && (parts & 1)) {
+            const float4 *ih = img_hi + a * scap, *il = img_lo + a * scap;
+            const int nc = ncand[a];
+            float acc32 = 0.f;
+            for (int c = 0; c < nc; ++c) {
+                const float4 h = ih[c], lo = il[c];
+                const float dx = (gh[0] - h.x) + (gl[0] - lo.x), dy = (gh[1] - h.y) + (gl[1] - lo.y),
+                            dz = (gh[2] - h.z) + (gl[2] - lo.z);
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 > rc2) continue;
+                if (r2 < fp64_below || fabsf(r2 - rcc) < 1e-3f * rcc) {
+                    const int s = __float_as_int(h.w);
+                    const double *p = atoms + 3 * (a0 + a);
+                    const double ex = gabs[0] - (p[0] + shifts[3 * s]), ey = gabs[1] - (p[1] + shifts[3 * s + 1]),
+                                 ez = gabs[2] - (p[2] + shifts[3 * s + 2]);
+                    const double r = sqrt(ex * ex + ey * ey + ez * ez);
+                    if (r <= rc && (s != zero_idx || r > 1e-10)) {
+                        acc64 += erfc(sa * r) / r;
+                        used64 = true;
+                    }
+                } else {
+                    const float rinv = rsqrtf(r2);
+                    acc32 += erfcf(saf * (r2 * rinv)) * rinv;
+                }
+            }
+            float s_, e_;
+            dfa::two_sum(v.s, acc32, s_, e_);
+            v.s = s_;
+            v.e = __fadd_rn(v.e, e_);
+        }
+        float2 out = dfa::norm(v);
+        if (used64) {  // rare: fold the FP64 terms in FP64
+            const double t = ((double)out.x + (double)out.y) + acc64;
+            out.x = (float)t;
+            out.y = (float)(t - (double)out.x);
+        }
+        if (valid) phit[(long long)(a0 + a) * ld + m] = out;
+        if (psum) {  // column statistics over the CTA's points (invalid lanes add zero)
+            float sh = valid ? out.x : 0.f, sl = valid ? out.y : 0.f;
+            float mx = valid ? fabsf(out.x) : 0.f;
+            for (int o = 16; o > 0; o >>= 1) {
+                const float oh2 = __shfl_xor_sync(0xffffffffu, sh, o), ol2 = __shfl_xor_sync(0xffffffffu, sl, o);
+                float s2, e2;
+                dfa::two_sum(sh, oh2, s2, e2);
+                sh = s2;
+                sl = __fadd_rn(__fadd_rn(sl, ol2), e2);
+                mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            }
+            if (lane == 0) {
+                wsum[warp][a] = make_float2(sh, sl);
+                wmax[warp][a] = mx;
+            }
+        }
+    }
+    if (psum) {
+        __syncthreads();
+        if (threadIdx.x < na) {
+            const int a = threadIdx.x;
+            double s = 0.0;
+            float mx = 0.f;
+            for (int w = 0; w < kPhiPts / 32; ++w) {
+                s += (double)wsum[w][a].x + (double)wsum[w][a].y;
+                mx = fmaxf(mx, wmax[w][a]);
+            }
+            psum[(size_t)(a0 + a) * gridDim.x + blockIdx.x] = s;
+            pmax[(size_t)(a0 + a) * gridDim.x + blockIdx.x] = mx;
+        }
+    }
+}
+
+size_t phi_smem_bytes(int n1c, int scap) {
+    return sizeof(float4) * ((size_t)n1c * kPhiPts + 2 * (size_t)kPhiAtoms * scap);
+}
+
+void launch_phi(const int32_t *kept, long long m0, long long rows, const double *d_axis, int nx, int ny,
+                const double *d_atoms, int N, const double *d_shifts, int S, int zero_idx, double rc, double sa,
+                const float4 *img, const float4 *EX, const float4 *E, int n1c, int parts, float2 *phit, long long ld,
+                double *psum, float *pmax, cudaStream_t s) {
+    RP_REQUIRE(S >= 1 && S <= kMaxShifts, "more than 128 real-space shifts after pruning (cutoff too large for the cell)");
+    const int scap = (S + 31) / 32 * 32;
+    const size_t smem = phi_smem_bytes(n1c, scap);
+    static size_t attr = 0;
+    if (smem > 48 * 1024 && smem > attr) {
+        RP_REQUIRE(smem <= 200 * 1024, "phi kernel: KMAX too large for shared memory");
+        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = smem;
+    }
+    dim3 grd(ceil_div(rows, kPhiPts), ceil_div(N, kPhiAtoms));
+    phi_chunk_kernel<<<grd, kPhiPts, smem, s>>>(kept, m0, rows, d_axis, nx, ny, d_atoms, N, d_shifts, S, scap, zero_idx,
+                                                rc, sa, real_near2(), img, EX, E, n1c, parts, phit, ld, psum, pmax);
+    RP_LAUNCH_CHECK();
 }
 
 // ------------------------------------------------------------------ column statistics and the split
 
-// Per-atom sums (FP64) and max |Phi| over a chunk: stage 1 per (atom, slab of points)
-constexpr int kStatSlab = 4096;
-__global__ void colstats_kernel(const double *__restrict__ phit, long long ld, long long rows, int N,
-                                double *__restrict__ psum, float *__restrict__ pmax) {
-    const int a = blockIdx.y;
-    const long long r0 = (long long)blockIdx.x * kStatSlab;
-    const long long r1 = min(r0 + kStatSlab, rows);
-    double s = 0.0;
-    float mx = 0.f;
-    for (long long r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        double v = phit[(long long)a * ld + r];
-        s += v;
-        mx = fmaxf(mx, (float)fabs(v));
-    }
-    __shared__ double ss[256];
-    __shared__ float sm[256];
-    ss[threadIdx.x] = s;
-    sm[threadIdx.x] = mx;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) {
-            ss[threadIdx.x] += ss[threadIdx.x + o];
-            sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + o]);
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        psum[(size_t)a * gridDim.x + blockIdx.x] = ss[0];
-        pmax[(size_t)a * gridDim.x + blockIdx.x] = sm[0];
-    }
-}
-
-// Per-atom: chunk sum (into sphi), and on the first chunk the centre c and scale.
-__global__ void colstats_finish_kernel(const double *__restrict__ psum, const float *__restrict__ pmax, int nslab,
+// Per atom: the chunk's sum (into sphi) from the phi kernel's per-CTA partials, and on
+// the first chunk the centre c (a double-float, cvec = its exact FP64 value) and scale.
+__global__ void colstats_finish_kernel(const double *__restrict__ psum, const float *__restrict__ pmax, int nblk,
                                        int N, long long rows, int first, double *__restrict__ sphi,
-                                       double *__restrict__ c, float *__restrict__ cf, float *__restrict__ scale) {
+                                       double *__restrict__ c, float2 *__restrict__ cdf, float *__restrict__ scale) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= N) return;
     double s = 0.0;
     float mx = 0.f;
-    for (int k = 0; k < nslab; ++k) {
-        s += psum[(size_t)a * nslab + k];
-        mx = fmaxf(mx, pmax[(size_t)a * nslab + k]);
+    for (int k = 0; k < nblk; ++k) {
+        s += psum[(size_t)a * nblk + k];
+        mx = fmaxf(mx, pmax[(size_t)a * nblk + k]);
     }
     sphi[a] = first ? s : sphi[a] + s;
     if (first) {
-        double mean = s / (double)rows;
-        c[a] = mean;
-        cf[a] = (float)mean;
+        const double mean = s / (double)rows;
+        const float ch = (float)mean, cl = (float)(mean - (double)ch);
+        cdf[a] = make_float2(ch, cl);
+        c[a] = (double)ch + (double)cl;  // the shift actually applied, exactly
         // |Phi - c| <= 2 max|Phi| =: bound in [2^(e-1), 2^e); scale 2^(-e-1) puts |x| below 1/2,
         // so the fixed-point slices stay within |x_s| <= 64 even if a later chunk doubles the range
         float bound = 2.f * mx;
@@ -789,28 +552,41 @@ __global__ void colstats_finish_kernel(const double *__restrict__ psum, const fl
 }
 
 // X rows: a < N: (Phi_t[a][m] - c_a) * scale_a;  a == N: Vc[m] * scale_V;  rest zero.
-// Each value x (|x| <= 1) is cut into four 7-bit fixed-point slices
-// x = 2^-6 (x0 + 2^-7 x1 + 2^-14 x2 + 2^-21 x3), x_s integers in [-64, 64], exact in FP16.
-__global__ void slice_rows_kernel(const double *__restrict__ phit, long long ld, long long rows, long long rows_pad,
-                                  int N, int Np_pad, const double *__restrict__ c, const float *__restrict__ scale,
+// Each value x (|x| <= 1) becomes I = round(x 2^27) and four 7-bit digits
+// x ~ 2^-6 (x0 + 2^-7 x1 + 2^-14 x2 + 2^-21 x3), x_s integers in [-64, 64], exact in FP16.
+__global__ void slice_rows_kernel(const float2 *__restrict__ phit, long long ld, long long rows, long long rows_pad,
+                                  int N, int Np_pad, const float2 *__restrict__ cdf, const float *__restrict__ scale,
                                   const double *__restrict__ Vc, long long m0, const float *__restrict__ vscale_p,
                                   __half *__restrict__ X0, __half *__restrict__ X1, __half *__restrict__ X2,
                                   __half *__restrict__ X3, int *__restrict__ clamped) {
-    const float vscale = *vscale_p;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)Np_pad * rows_pad) return;
-    int a = (int)(t / rows_pad);
-    long long m = t - (long long)a * rows_pad;
-    double v = 0.0;
+    const int a = (int)(t / rows_pad);
+    const long long m = t - (long long)a * rows_pad;
+    float h = 0.f, l = 0.f, sc = 0.f;
     if (m < rows) {
-        if (a < N) v = (phit[(long long)a * ld + m] - c[a]) * (double)scale[a];
-        else if (a == N) v = Vc[m0 + m] * (double)vscale;
+        if (a < N) {
+            const float2 v = phit[(long long)a * ld + m], c = cdf[a];
+            const float2 d = df_sub(v.x, v.y, c.x, c.y);
+            h = d.x;
+            l = d.y;
+            sc = scale[a];
+        } else if (a == N) {
+            const double v = Vc[m0 + m];
+            h = (float)v;
+            l = (float)(v - (double)h);
+            sc = *vscale_p;
+        }
     }
-    if (fabs(v) > 1.0) {
+    sc *= 134217728.0f;  // 2^27
+    int I;
+    if (fabsf(h * sc) > 134217728.0f) {  // |x| beyond ~1: clamp (counted; the fit reports it)
         atomicAdd(clamped, 1);
-        v = fmin(fmax(v, -1.0), 1.0);
+        I = h > 0.f ? (1 << 27) : -(1 << 27);
+    } else {
+        I = round_df(h, l, sc);
     }
-    slice4(v, X0, X1, X2, X3, t);
+    digits4(I, X0, X1, X2, X3, t);
 }
 
 // Sum the partial Gram tiles of all point splits in a fixed order (FP64; each
@@ -853,6 +629,11 @@ __global__ void finish_mixed_kernel(const double *__restrict__ G, int Np, const 
     }
 }
 
+__global__ void df_to_double_kernel(const float2 *__restrict__ x, long long n, double *__restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = (double)x[t].x + (double)x[t].y;
+}
+
 __global__ void __launch_bounds__(1024) absmax_kernel(const double *__restrict__ x, long long n,
                                                      double *__restrict__ out) {
     __shared__ double sm[1024];
@@ -872,16 +653,6 @@ __global__ void vscale_kernel(const double *__restrict__ vmax, float *__restrict
     int e = 0;
     if (*vmax > 0.0) frexp(*vmax, &e);
     *vscale = ldexpf(1.0f, -e - 1);
-}
-
-__global__ void to_float2_kernel(const double2 *__restrict__ in, float2 *__restrict__ out, int n) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) out[t] = make_float2((float)in[t].x, (float)in[t].y);
-}
-
-__global__ void sqrt_weights_kernel(const double *__restrict__ kc, float *__restrict__ out, int K) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < K) out[t] = (float)(sqrt(kc[t]) * (double)kTableScale);
 }
 
 // ------------------------------------------------------------------ host helpers
@@ -918,17 +689,6 @@ CUtensorMap make_map(const void *ptr, long long rows, long long cols, int box_ro
     return m;
 }
 
-void launch_recip(const CUtensorMap &ah, const CUtensorMap &al, const CUtensorMap &bh, const CUtensorMap &bl,
-                  const RecArgs &g, int grid, cudaStream_t s) {
-    static bool attr = false;
-    if (!attr) {
-        RP_CUDA(cudaFuncSetAttribute(recip_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kRecSmem));
-        attr = true;
-    }
-    recip_gemm_kernel<<<grid, kRecThreads, kRecSmem, s>>>(ah, al, bh, bl, g);
-    RP_LAUNCH_CHECK();
-}
-
 void launch_gram(const __half *const *X, int Np_pad, long long cols, const GramArgs &g, int grid, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
@@ -944,74 +704,22 @@ void launch_gram(const __half *const *X, int Np_pad, long long cols, const GramA
     RP_LAUNCH_CHECK();
 }
 
-void launch_top(const __half *const *T, long long rows_pad, const __half *const *B, int N, int width, const TopArgs &g,
-                int grid, cudaStream_t s) {
-    static bool attr = false;
-    if (!attr) {
-        RP_CUDA(cudaFuncSetAttribute(recip_top_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopSmem));
-        attr = true;
-    }
-    CUtensorMap a[4], b[4];
-    for (int q = 0; q < 4; ++q) {
-        a[q] = make_map(T[q], rows_pad, width, kBM);
-        b[q] = make_map(B[q], N, width, kGN);
-    }
-    recip_top_kernel<<<grid, kTopThreads, kTopSmem, s>>>(a[0], a[1], a[2], a[3], b[0], b[1], b[2], b[3], g);
-    RP_LAUNCH_CHECK();
-}
 
 inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
 
 }  // namespace
 
-// Pairs closer than this radius (Bohr) get the FP64 real-space term; tunable with
-// RP_REAL_FP64_R.  Default 0: with double-float image coordinates the FP32 terms
-// keep the fitted charges within ~3e-7 e of the FP64 fit on the synthetic
-// workloads, so FP64 is used only to decide images that sit at the cutoff.
-float real_near2() {
-    static float v = [] {
-        const char *e = getenv("RP_REAL_FP64_R");
-        double r = e ? atof(e) : 0.0;
-        return (float)(r * r);
-    }();
-    return v;
-}
-
-// Split the sorted k-set into the float block and the exact top block: the top
-// block takes every k with kcoef >= kTopRel * max kcoef (at least 32, at most
-// kTopMaxStages*32 k), so the terms that carry the sum are accumulated exactly.
-constexpr double kTopRel = 1e-5;
-
-void plan_kblocks(const rp_ewald *ew, KBlock &fl, KBlock &top) {
-    const int K = ew->K;
-    double wmax = 0.0;
-    for (double w : ew->kcoef) wmax = std::max(wmax, w);
-    int heavy = 0;
-    for (double w : ew->kcoef) heavy += (w >= kTopRel * wmax) ? 1 : 0;
-    int ntop = std::min(K, std::max(32, (int)round_up(heavy, 32)));
-    ntop = std::min(ntop, kTopMaxStages * kBK / 2);
-    top.q0 = K - ntop;
-    top.count = ntop;
-    top.width = (int)round_up(2LL * ntop, kBK);
-    fl.q0 = 0;
-    fl.count = K - ntop;
-    fl.width = std::max<int>((int)round_up(2LL * fl.count, kBK), kBK);
-}
-
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
                 cudaStream_t stream) {
     RP_REQUIRE(N > 0 && M > 0, "rp_gram: need N > 0 and M > 0");
-    const int K = ew->K;
-    KBlock fl, top;
-    plan_kblocks(ew, fl, top);
     std::vector<double> sh;
     int zero_idx = -1;
     prune_shifts(ew, atoms, N, sh, zero_idx);
     const int S = (int)(sh.size() / 3);
-    RP_REQUIRE(S <= 128, "rp_gram: more than 128 real-space shifts after pruning (cutoff too large for the cell)");
-    const int nx = ew->grid.n_grid[0], ny = ew->grid.n_grid[1], nz = ew->grid.n_grid[2];
-    const int kmax = ew->kmax;
+    RP_REQUIRE(S <= kMaxShifts, "rp_gram: more than 128 real-space shifts after pruning (cutoff too large for the cell)");
+    const int nx = ew->grid.n_grid[0], ny = ew->grid.n_grid[1];
+    const int n1c = ew->kmax;
 
     double *d_atoms = ctx->buf_t<double>("g_atoms", 3 * (size_t)N);
     double *d_shifts = ctx->buf_t<double>("g_shifts", sh.size());
@@ -1021,71 +729,34 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     RP_CUDA(cudaMemcpyAsync(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice, stream));
     int *d_status = ctx->d_status;  // cleared by the caller (rp_gram / the batch driver)
 
-    // FP32 per-axis phase tables and sqrt weights for the float block
-    const int nex = (kmax + 1) * nx, ney = (2 * kmax + 1) * ny, nez = (2 * kmax + 1) * nz;
-    float2 *ex = ctx->buf_t<float2>("m_ex", nex);
-    float2 *ey = ctx->buf_t<float2>("m_ey", ney);
-    float2 *ez = ctx->buf_t<float2>("m_ez", nez);
-    float *swk = ctx->buf_t<float>("m_swk", K);
-    to_float2_kernel<<<ceil_div(nex, 256), 256, 0, stream>>>(ew->d_ex, ex, nex);
-    RP_LAUNCH_CHECK();
-    to_float2_kernel<<<ceil_div(ney, 256), 256, 0, stream>>>(ew->d_ey, ey, ney);
-    RP_LAUNCH_CHECK();
-    to_float2_kernel<<<ceil_div(nez, 256), 256, 0, stream>>>(ew->d_ez, ez, nez);
-    RP_LAUNCH_CHECK();
-    sqrt_weights_kernel<<<ceil_div(K, 256), 256, 0, stream>>>(ew->d_kcoef_s, swk, K);
-    RP_LAUNCH_CHECK();
-
-    // table scales of the exact block: |sqrt(w) 2^10 cos| * s <= 1/2
-    double wmax = 0.0;
-    for (double w : ew->kcoef) wmax = std::max(wmax, w);
-    int et = 0;
-    std::frexp(std::sqrt(wmax) * (double)kTableScale, &et);
-    const double sTop = std::ldexp(1.0, -et - 1);
-    double *wtop = ctx->buf_t<double>("m_wtop", (size_t)top.count);
+    // reciprocal rows of every atom (stages A and B) and the double-float images, once per fit
+    float4 *E = ctx->buf_t<float4>("m_E", recip_rows_bytes(ew, N) / sizeof(float4));
+    float4 *img = ctx->buf_t<float4>("m_img", 2 * (size_t)N * S);
     {
-        std::vector<double> kc(ew->kcoef);
-        std::sort(kc.begin(), kc.end());  // the device tables use the ascending order
-        std::vector<double> w((size_t)top.count);
-        for (int q = 0; q < top.count; ++q) w[q] = std::sqrt(kc[top.q0 + q]) * (double)kTableScale * sTop;
-        RP_CUDA(cudaMemcpyAsync(wtop, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice, stream));
+        StageTimer tt(ctx, "recip_rows", stream);
+        recip_rows(ctx, ew, d_atoms, nullptr, N, E, stream);
+        images_df_kernel<<<ceil_div((long long)N * S, 128), 128, 0, stream>>>(d_atoms, N, d_shifts, S, img);
+        RP_LAUNCH_CHECK();
     }
-
-    // atom tables (once per fit)
-    __half *Bh = ctx->buf_t<__half>("m_Bh", (size_t)N * fl.width);
-    __half *Bl = ctx->buf_t<__half>("m_Bl", (size_t)N * fl.width);
-    atom_tables_f16_kernel<<<ceil_div((long long)N * fl.width, 256), 256, 0, stream>>>(ew->d_kvec_s, ew->d_kcoef_s, fl,
-                                                                                       d_atoms, N, Bh, Bl);
-    RP_LAUNCH_CHECK();
-    __half *Bt[4];
-    for (int q = 0; q < 4; ++q) Bt[q] = ctx->buf_t<__half>("m_Bt" + std::to_string(q), (size_t)N * top.width);
-    atom_tables_top_kernel<<<ceil_div((long long)N * top.width, 256), 256, 0, stream>>>(
-        ew->d_kvec_s, ew->d_kcoef_s, top, d_atoms, N, sTop, Bt[0], Bt[1], Bt[2], Bt[3]);
-    RP_LAUNCH_CHECK();
-    const CUtensorMap mBh = make_map(Bh, N, fl.width, kBN), mBl = make_map(Bl, N, fl.width, kBN);
 
     // chunk the points so the per-chunk staging stays below ~6 GB
     const int Np = N + 1;                       // atoms + the ESP row
     const int Np_pad = (int)round_up(Np, kBM);
-    const long long per_point = 4LL * fl.width + 8LL * top.width + 8LL * N + 8LL * Np_pad;
+    const long long per_point = 8LL * N + 8LL * Np_pad;  // Phi (double-float) + four FP16 digits
     long long chunk = std::max<long long>(kBM, ((6LL << 30) / per_point) / kBM * kBM);
     chunk = std::min<long long>(chunk, round_up(M, kBM));
     const long long chunk_pad = round_up(chunk, kBK);
 
-    __half *Th = ctx->buf_t<__half>("m_Th", (size_t)chunk * fl.width);
-    __half *Tl = ctx->buf_t<__half>("m_Tl", (size_t)chunk * fl.width);
-    __half *Tt[4];
-    for (int q = 0; q < 4; ++q) Tt[q] = ctx->buf_t<__half>("m_Tt" + std::to_string(q), (size_t)chunk * top.width);
-    double *phit = ctx->buf_t<double>("m_phit", (size_t)N * chunk_pad);
+    float2 *phit = ctx->buf_t<float2>("m_phit", (size_t)N * chunk_pad);
     __half *X[kGSlices];
     for (int q = 0; q < kGSlices; ++q) X[q] = ctx->buf_t<__half>("m_X" + std::to_string(q), (size_t)Np_pad * chunk_pad);
     int *d_clamped = ctx->d_status + 1;  // second status word: fixed-point range overflows
-    const int nslab = (int)((chunk + kStatSlab - 1) / kStatSlab);
-    double *psum = ctx->buf_t<double>("m_psum", (size_t)N * nslab);
-    float *pmax = ctx->buf_t<float>("m_pmax", (size_t)N * nslab);
+    const int nblk = (int)ceil_div(chunk, kPhiPts);
+    double *psum = ctx->buf_t<double>("m_psum", (size_t)N * nblk);
+    float *pmax = ctx->buf_t<float>("m_pmax", (size_t)N * nblk);
     double *sphi = sum_phi_dev ? sum_phi_dev : ctx->buf_t<double>("m_sphi", N);
     double *cvec = ctx->buf_t<double>("m_c", N);
-    float *cf = ctx->buf_t<float>("m_cf", N);
+    float2 *cdf = ctx->buf_t<float2>("m_cdf", N);
     float *scale = ctx->buf_t<float>("m_scale", N);
     double *G = ctx->buf_t<double>("m_G", (size_t)Np * Np);
     double *sumV = ctx->buf_t<double>("m_sumV", 1);
@@ -1108,73 +779,26 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
 
     for (long long m0 = 0; m0 < M; m0 += chunk) {
         const long long rows = std::min<long long>(chunk, M - m0);
-        const long long rows_tpad = round_up(rows, kBM);
         const long long rows_kpad = round_up(rows, kBK);
-        // 1. grid tables of both blocks
+        // 1. Phi of the chunk (real space + reciprocal stage C) and its column statistics
+        const int nb = (int)ceil_div(rows, kPhiPts);
         {
-        StageTimer t_tab(ctx, "grid_tables", stream);
-        grid_tables_f16_kernel<<<ceil_div(rows_tpad * (fl.width / 2), 256), 256, 0, stream>>>(
-            ew->d_kidx_s, swk, fl, kmax, ex, ey, ez, nx, ny, nz, kept_idx_dev, m0, rows, rows_tpad, Th, Tl);
-        RP_LAUNCH_CHECK();
-        grid_tables_top_kernel<<<ceil_div(rows_tpad * (top.width / 2), 256), 256, 0, stream>>>(
-            ew->d_kidx_s, wtop, top, kmax, ew->d_ex, ew->d_ey, ew->d_ez, nx, ny, nz, kept_idx_dev, m0, rows,
-            rows_tpad, sTop, Tt[0], Tt[1], Tt[2], Tt[3]);
-        RP_LAUNCH_CHECK();
+            StageTimer tt(ctx, "phi", stream);
+            launch_phi(kept_idx_dev, m0, rows, d_axis, nx, ny, d_atoms, N, d_shifts, S, zero_idx, ew->cutoff,
+                       ew->sqrt_alpha, img, ew->d_exf, E, n1c, 3, phit, chunk_pad, psum, pmax, stream);
         }
-        // 2a. GEMM-1 over the float block: Phi_t = T B^T (atom-major, ld chunk_pad)
-        {
-            StageTimer tt(ctx, "recip_gemm_f16x3", stream);
-            const CUtensorMap mTh = make_map(Th, rows_tpad, fl.width, kBM), mTl = make_map(Tl, rows_tpad, fl.width, kBM);
-            RecArgs g{};
-            g.m_tiles = (int)(rows_tpad / kBM);
-            g.kb_total = fl.width / kBK;
-            g.rows_m = (int)rows;
-            g.rows_n = N;
-            g.out_scale = 1.0 / ((double)kTableScale * (double)kTableScale);
-            g.out = phit;
-            g.ld_out = chunk_pad;
-            g.status = d_status;
-            launch_recip(mTh, mTl, mBh, mBl, g, g.m_tiles * ((N + kBN - 1) / kBN), stream);
-        }
-        // 2b. exact GEMM over the heaviest k: Phi_t += T_top B_top^T
-        {
-            StageTimer tt(ctx, "recip_gemm_exact_top", stream);
-            TopArgs g{};
-            g.m_tiles = (int)(rows_tpad / kBM);
-            g.kb_total = top.width / kBK;
-            g.rows_m = (int)rows;
-            g.rows_n = N;
-            g.out_scale = 1.0 / ((double)kTableScale * (double)kTableScale * sTop * sTop);
-            g.out = phit;
-            g.ld_out = chunk_pad;
-            g.status = d_status;
-            const __half *Tq[4] = {Tt[0], Tt[1], Tt[2], Tt[3]};
-            const __half *Bq[4] = {Bt[0], Bt[1], Bt[2], Bt[3]};
-            launch_top(Tq, rows_tpad, Bq, N, top.width, g, g.m_tiles * ((N + kGN - 1) / kGN), stream);
-        }
-        // 3. real space
-        {
-            StageTimer tt(ctx, "realspace", stream);
-            dim3 grd(ceil_div(rows, kRealPts), ceil_div(N, kRealAtoms));
-            realspace_kernel<<<grd, kRealPts, 0, stream>>>(kept_idx_dev, m0, rows, d_axis, nx, ny, d_atoms, N,
-                                                           d_shifts, S, zero_idx, ew->cutoff, ew->sqrt_alpha,
-                                                           real_near2(), phit, chunk_pad);
-            RP_LAUNCH_CHECK();
-        }
-        // 4. column statistics, centre/scale on the first chunk, fixed-point slices of X
+        // 2. centre/scale on the first chunk, fixed-point digits of X
         {
             StageTimer tt(ctx, "center_slice", stream);
-            const int ns = (int)((rows + kStatSlab - 1) / kStatSlab);
-            colstats_kernel<<<dim3(ns, N), 256, 0, stream>>>(phit, chunk_pad, rows, N, psum, pmax);
-            RP_LAUNCH_CHECK();
-            colstats_finish_kernel<<<ceil_div(N, 128), 128, 0, stream>>>(psum, pmax, ns, N, rows, m0 == 0 ? 1 : 0, sphi,
-                                                                         cvec, cf, scale);
+            colstats_finish_kernel<<<ceil_div(N, 128), 128, 0, stream>>>(psum, pmax, nb, N, rows, m0 == 0 ? 1 : 0, sphi,
+                                                                         cvec, cdf, scale);
             RP_LAUNCH_CHECK();
             slice_rows_kernel<<<ceil_div((long long)Np_pad * rows_kpad, 256), 256, 0, stream>>>(
-                phit, chunk_pad, rows, rows_kpad, N, Np_pad, cvec, scale, Vc_dev, m0, vscale, X[0], X[1], X[2], X[3], d_clamped);
+                phit, chunk_pad, rows, rows_kpad, N, Np_pad, cdf, scale, Vc_dev, m0, vscale, X[0], X[1], X[2], X[3],
+                d_clamped);
             RP_LAUNCH_CHECK();
         }
-        // 5. GEMM-2: exact Gram partial tiles over point splits, then the fixed-order FP64 reduction
+        // 3. exact Gram partial tiles over point splits, then the fixed-order FP64 reduction
         {
             const int kb_total = (int)(rows_kpad / kBK);
             const int nsplit = (kb_total + kb_split - 1) / kb_split;
@@ -1205,112 +829,37 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
 
 }  // namespace rp
 
-// Diagnostics (not part of the public ABI): the two FP32 Phi parts of the mixed
-// path for the first `rows` kept points, atom-major [N][rows].  Used to check the
-// tensor-core k-contraction and the FP32 real-space sum against FP64 separately.
-extern "C" int rp_debug_mixed_phi_parts(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N,
-                                        const int32_t *kept_idx_dev, int64_t rows, double *recip_dev,
-                                        double *real_dev) {
+// Diagnostics (not part of the public ABI): the mixed path's Phi for the first
+// `rows` kept points, atom-major [N][rows]; parts = 1 real space, 2 reciprocal,
+// 3 both.  Used to check each part against FP64 separately.
+extern "C" int rp_debug_mixed_phi(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N,
+                                  const int32_t *kept_idx_dev, int64_t rows, int parts, double *phi_dev) {
     using namespace rp;
     try {
         RP_CUDA(cudaSetDevice(ctx->device));
-        RP_REQUIRE(rows > 0 && rows <= (1LL << 30), "bad rows");
-        // run the real pipeline pieces through gram_mixed's staging by calling it on a
-        // zero ESP would also solve; instead reuse its stages directly on one chunk
-        const int K = ew->K;
-        KBlock fl, top;
-        plan_kblocks(ew, fl, top);
+        RP_REQUIRE(N > 0 && rows > 0 && rows <= (1LL << 30) && parts >= 1 && parts <= 3, "bad arguments");
         std::vector<double> sh;
         int zero_idx = -1;
         prune_shifts(ew, atoms, N, sh, zero_idx);
         const int S = (int)(sh.size() / 3);
-        const int nx = ew->grid.n_grid[0], ny = ew->grid.n_grid[1], nz = ew->grid.n_grid[2], kmax = ew->kmax;
         double *d_atoms = ctx->buf_t<double>("g_atoms", 3 * (size_t)N);
         double *d_shifts = ctx->buf_t<double>("g_shifts", sh.size());
         double *d_axis = ctx->buf_t<double>("g_axis", 9);
         RP_CUDA(cudaMemcpy(d_atoms, atoms, sizeof(double) * 3 * N, cudaMemcpyHostToDevice));
         RP_CUDA(cudaMemcpy(d_shifts, sh.data(), sizeof(double) * sh.size(), cudaMemcpyHostToDevice));
         RP_CUDA(cudaMemcpy(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice));
-        RP_CUDA(cudaMemset(ctx->d_status, 0, sizeof(int)));
-        const int nex = (kmax + 1) * nx, ney = (2 * kmax + 1) * ny, nez = (2 * kmax + 1) * nz;
-        float2 *ex = ctx->buf_t<float2>("m_ex", nex), *ey = ctx->buf_t<float2>("m_ey", ney),
-               *ez = ctx->buf_t<float2>("m_ez", nez);
-        float *swk = ctx->buf_t<float>("m_swk", K);
-        to_float2_kernel<<<ceil_div(nex, 256), 256>>>(ew->d_ex, ex, nex);
+        float4 *E = ctx->buf_t<float4>("m_E", recip_rows_bytes(ew, N) / sizeof(float4));
+        float4 *img = ctx->buf_t<float4>("m_img", 2 * (size_t)N * S);
+        recip_rows(ctx, ew, d_atoms, nullptr, N, E, 0);
+        images_df_kernel<<<ceil_div((long long)N * S, 128), 128>>>(d_atoms, N, d_shifts, S, img);
         RP_LAUNCH_CHECK();
-        to_float2_kernel<<<ceil_div(ney, 256), 256>>>(ew->d_ey, ey, ney);
-        RP_LAUNCH_CHECK();
-        to_float2_kernel<<<ceil_div(nez, 256), 256>>>(ew->d_ez, ez, nez);
-        RP_LAUNCH_CHECK();
-        sqrt_weights_kernel<<<ceil_div(K, 256), 256>>>(ew->d_kcoef_s, swk, K);
-        RP_LAUNCH_CHECK();
-        double wmax = 0.0;
-        for (double w : ew->kcoef) wmax = std::max(wmax, w);
-        int et = 0;
-        std::frexp(std::sqrt(wmax) * (double)kTableScale, &et);
-        const double sTop = std::ldexp(1.0, -et - 1);
-        double *wtop = ctx->buf_t<double>("m_wtop", (size_t)top.count);
-        {
-            std::vector<double> kc(ew->kcoef);
-            std::sort(kc.begin(), kc.end());
-            std::vector<double> w((size_t)top.count);
-            for (int q = 0; q < top.count; ++q) w[q] = std::sqrt(kc[top.q0 + q]) * (double)kTableScale * sTop;
-            RP_CUDA(cudaMemcpy(wtop, w.data(), sizeof(double) * w.size(), cudaMemcpyHostToDevice));
-        }
-        __half *Bh = ctx->buf_t<__half>("m_Bh", (size_t)N * fl.width), *Bl = ctx->buf_t<__half>("m_Bl", (size_t)N * fl.width);
-        atom_tables_f16_kernel<<<ceil_div((long long)N * fl.width, 256), 256>>>(ew->d_kvec_s, ew->d_kcoef_s, fl, d_atoms,
-                                                                                N, Bh, Bl);
-        RP_LAUNCH_CHECK();
-        __half *Bt[4], *Tt[4];
-        const long long rows_tpad = round_up(rows, kBM);
-        for (int q = 0; q < 4; ++q) {
-            Bt[q] = ctx->buf_t<__half>("m_Bt" + std::to_string(q), (size_t)N * top.width);
-            Tt[q] = ctx->buf_t<__half>("m_Tt" + std::to_string(q), (size_t)rows_tpad * top.width);
-        }
-        atom_tables_top_kernel<<<ceil_div((long long)N * top.width, 256), 256>>>(ew->d_kvec_s, ew->d_kcoef_s, top,
-                                                                                 d_atoms, N, sTop, Bt[0], Bt[1], Bt[2], Bt[3]);
-        RP_LAUNCH_CHECK();
-        __half *Th = ctx->buf_t<__half>("m_Th", (size_t)rows_tpad * fl.width),
-               *Tl = ctx->buf_t<__half>("m_Tl", (size_t)rows_tpad * fl.width);
-        grid_tables_f16_kernel<<<ceil_div(rows_tpad * (fl.width / 2), 256), 256>>>(
-            ew->d_kidx_s, swk, fl, kmax, ex, ey, ez, nx, ny, nz, kept_idx_dev, 0, rows, rows_tpad, Th, Tl);
-        RP_LAUNCH_CHECK();
-        grid_tables_top_kernel<<<ceil_div(rows_tpad * (top.width / 2), 256), 256>>>(
-            ew->d_kidx_s, wtop, top, kmax, ew->d_ex, ew->d_ey, ew->d_ez, nx, ny, nz, kept_idx_dev, 0, rows,
-            rows_tpad, sTop, Tt[0], Tt[1], Tt[2], Tt[3]);
-        RP_LAUNCH_CHECK();
-        RecArgs g{};
-        g.m_tiles = (int)(rows_tpad / kBM);
-        g.kb_total = fl.width / kBK;
-        g.rows_m = (int)rows;
-        g.rows_n = N;
-        g.out_scale = 1.0 / ((double)kTableScale * (double)kTableScale);
-        g.out = recip_dev;
-        g.ld_out = rows;
-        g.status = ctx->d_status;
-        launch_recip(make_map(Th, rows_tpad, fl.width, kBM), make_map(Tl, rows_tpad, fl.width, kBM),
-                     make_map(Bh, N, fl.width, kBN), make_map(Bl, N, fl.width, kBN), g, g.m_tiles * ((N + kBN - 1) / kBN), 0);
-        TopArgs tg{};
-        tg.m_tiles = (int)(rows_tpad / kBM);
-        tg.kb_total = top.width / kBK;
-        tg.rows_m = (int)rows;
-        tg.rows_n = N;
-        tg.out_scale = 1.0 / ((double)kTableScale * (double)kTableScale * sTop * sTop);
-        tg.out = recip_dev;
-        tg.ld_out = rows;
-        tg.status = ctx->d_status;
-        const __half *Tq[4] = {Tt[0], Tt[1], Tt[2], Tt[3]};
-        const __half *Bq[4] = {Bt[0], Bt[1], Bt[2], Bt[3]};
-        launch_top(Tq, rows_tpad, Bq, N, top.width, tg, tg.m_tiles * ((N + kGN - 1) / kGN), 0);
-        RP_CUDA(cudaMemset(real_dev, 0, sizeof(double) * (size_t)N * rows));
-        realspace_kernel<<<dim3(ceil_div(rows, kRealPts), ceil_div(N, kRealAtoms)), kRealPts>>>(
-            kept_idx_dev, 0, rows, d_axis, nx, ny, d_atoms, N, d_shifts, S, zero_idx, ew->cutoff, ew->sqrt_alpha,
-            real_near2(), real_dev, rows);
+        float2 *ph = ctx->buf_t<float2>("dbg_phi", (size_t)N * rows);
+        launch_phi(kept_idx_dev, 0, rows, d_axis, ew->grid.n_grid[0], ew->grid.n_grid[1], d_atoms, N, d_shifts, S,
+                   zero_idx, ew->cutoff, ew->sqrt_alpha, img, ew->d_exf, E, ew->kmax, parts, ph, rows, nullptr,
+                   nullptr, 0);
+        df_to_double_kernel<<<ceil_div((long long)N * rows, 256), 256>>>(ph, (long long)N * rows, phi_dev);
         RP_LAUNCH_CHECK();
         RP_CUDA(cudaDeviceSynchronize());
-        int st = 0;
-        RP_CUDA(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
-        if (st) fail(st, "pipeline wait timed out");
         return RP_OK;
     } catch (const rp::Error &e) {
         ctx->last_error = e.msg;
@@ -1354,3 +903,4 @@ extern "C" int rp_debug_gram_slices(rp_ctx *ctx, const void *X0, const void *X1,
         return e.code;
     }
 }
+

@@ -2,17 +2,20 @@
 //
 // Replaces the V_coul = Phi q evaluation of ChargeCalculator.compute_stats
 // (repeat.py:2326-2441, used for --stats and --output) without forming Phi:
-//   reciprocal  V_r(g) = sum_k w_k Re(e^{i k.g} conj(S_k)),  S_k = sum_a q_a e^{i k.r_a}
-//               (structure factors in FP64 once; per point the exact per-axis phases)
+//   reciprocal  V_r(g) = Re sum_n1 ex[n1][i] E_q[r][n1]: the separable reciprocal
+//               sum of recip_sep.cu applied to the structure factor
+//               S(k) = sum_a q_a w_k e^{-i k.r_a} (one charge-weighted column)
 //   real space  V_s(g) = sum_a q_a sum_s [|g-r_a-s| <= Rc] erfc(sqrt(alpha) r)/r
 //               over a per-CTA candidate list of images near the CTA's points.
-// Cost per point is O(K + images within Rc) instead of O(N K).  The sums use
-// FP32 terms with FP64 accumulation (relative error ~1e-7), which is what an
-// RMS of the fitted ESP or a synthetic ESP needs.
+// Cost per point is O(KMAX + images within Rc) instead of O(N K).  The real-space
+// terms are FP32 with FP64 accumulation (relative error ~1e-7), which is what an
+// RMS of the fitted ESP or a synthetic ESP needs; the reciprocal part is
+// double-float.
 #include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
+#include "df.cuh"
 
 namespace rp {
 namespace {
@@ -20,41 +23,18 @@ namespace {
 constexpr int kPotPts = 128;
 constexpr int kPotCand = 4096;  // images per candidate batch in shared memory
 
-__global__ void structure_factors_kernel(const double *__restrict__ kvec, int K, const double *__restrict__ atoms,
-                                         const double *__restrict__ q, int N, double2 *__restrict__ Sk) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= K) return;
-    double re = 0.0, im = 0.0;
-    for (int a = 0; a < N; ++a) {
-        double kr = (atoms[3 * a] * kvec[3 * k] + atoms[3 * a + 1] * kvec[3 * k + 1]) + atoms[3 * a + 2] * kvec[3 * k + 2];
-        double s, c;
-        sincos(kr, &s, &c);
-        re += q[a] * c;
-        im += q[a] * s;
-    }
-    Sk[k] = make_double2(re, im);
-}
-
-// one thread per point; the k loop reads the (w_k S_k) table and the per-axis phases
-__global__ void __launch_bounds__(kPotPts) potential_recip_kernel(
-    const int *__restrict__ kidx, const double *__restrict__ kcoef, const double2 *__restrict__ Sk, int K, int kmax,
-    const double2 *__restrict__ ex, const double2 *__restrict__ ey, const double2 *__restrict__ ez, int nx, int ny,
-    int nz, const int32_t *__restrict__ idx, long long npts, double *__restrict__ out) {
-    long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// one thread per point: V_r = Re sum_n1 ex[n1][i] E_q[r][n1]
+__global__ void __launch_bounds__(kPotPts) potential_recip_kernel(const float4 *__restrict__ EX,
+                                                                  const float4 *__restrict__ Eq, int n1c, int nx,
+                                                                  const int32_t *__restrict__ idx, long long npts,
+                                                                  double *__restrict__ out) {
+    const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= npts) return;
     const int f = idx ? idx[m] : (int)m;
-    const int layer = nx * ny;
-    const int l = f / layer, rem = f - l * layer, j = rem / nx, i = rem - j * nx;
-    double acc = 0.0;
-    for (int k = 0; k < K; ++k) {
-        const int n1 = kidx[3 * k], n2 = kidx[3 * k + 1], n3 = kidx[3 * k + 2];
-        const double2 a = ex[n1 * nx + i], b = ey[(n2 + kmax) * ny + j], c = ez[(n3 + kmax) * nz + l];
-        const float r1 = (float)(a.x * b.x - a.y * b.y), i1 = (float)(a.x * b.y + a.y * b.x);
-        const float cr = r1 * (float)c.x - i1 * (float)c.y, ci = r1 * (float)c.y + i1 * (float)c.x;
-        const double2 s = Sk[k];
-        acc += kcoef[k] * ((double)cr * s.x + (double)ci * s.y);
-    }
-    out[m] = acc;
+    const int row = f / nx, i = f - row * nx;
+    dfa::acc rs{0.f, 0.f};
+    for (int n = 0; n < n1c; ++n) dfa::cmac_re(rs, EX[(long long)n * nx + i], Eq[(long long)row * n1c + n]);
+    out[m] = dfa::to_double(rs);
 }
 
 __global__ void __launch_bounds__(kPotPts) potential_real_kernel(
@@ -130,17 +110,15 @@ void potential_run(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const d
     double *d_q = ctx->buf_t<double>("p_q", (size_t)N);
     double *d_shifts = ctx->buf_t<double>("p_shifts", sh.size());
     double *d_axis = ctx->buf_t<double>("p_axis", 9);
-    double2 *Sk = ctx->buf_t<double2>("p_Sk", (size_t)ew->K);
     RP_CUDA(cudaMemcpyAsync(d_atoms, atoms, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_q, q, sizeof(double) * N, cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_shifts, sh.data(), sizeof(double) * sh.size(), cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice, stream));
-    structure_factors_kernel<<<ceil_div(ew->K, 128), 128, 0, stream>>>(ew->d_kvec_s, ew->K, d_atoms, d_q, N, Sk);
-    RP_LAUNCH_CHECK();
-    const int nx = ew->grid.n_grid[0], ny = ew->grid.n_grid[1], nz = ew->grid.n_grid[2];
-    potential_recip_kernel<<<ceil_div(npts, kPotPts), kPotPts, 0, stream>>>(
-        ew->d_kidx_s, ew->d_kcoef_s, Sk, ew->K, ew->kmax, ew->d_ex, ew->d_ey, ew->d_ez, nx, ny, nz, idx_dev, npts,
-        out_dev);
+    const int nx = ew->grid.n_grid[0], ny = ew->grid.n_grid[1];
+    float4 *Eq = ctx->buf_t<float4>("p_Eq", recip_rows_bytes(ew, 1) / sizeof(float4));
+    recip_rows(ctx, ew, d_atoms, d_q, N, Eq, stream);
+    potential_recip_kernel<<<ceil_div(npts, kPotPts), kPotPts, 0, stream>>>(ew->d_exf, Eq, ew->kmax, nx, idx_dev, npts,
+                                                                           out_dev);
     RP_LAUNCH_CHECK();
     potential_real_kernel<<<ceil_div(npts, kPotPts), kPotPts, 0, stream>>>(d_axis, nx, ny, idx_dev, npts, d_atoms, d_q,
                                                                           N, d_shifts, S, ew->cutoff, ew->sqrt_alpha,

@@ -58,21 +58,6 @@ def _ptr(a):
     return None if a is None else a.ctypes.data
 
 
-TOP_REL = 1e-5      # k with kcoef >= TOP_REL * max kcoef go to the exact block
-TOP_MAX_K = 256     # at most 8 stages of 64 columns (cos + sin)
-
-
-def plan_kblocks_py(cube):
-    """(k in the exact block, k in the FP16 block) for a cube, as the library plans them."""
-    from .synth import kspace
-    _, _, kc = kspace(cube.box_vectors, cube.cutoff, cube.kmax)
-    K = len(kc)
-    heavy = int((kc >= TOP_REL * kc.max()).sum())
-    ntop = min(K, max(32, -(-heavy // 32) * 32))
-    ntop = min(ntop, TOP_MAX_K)
-    return ntop, K - ntop
-
-
 class Context:
     """One rp_ctx on one CUDA device."""
 

@@ -1,6 +1,7 @@
-"""GPU parity of the mixed-precision tensor-core fit (FP16 hi+lo k-contraction,
-exact fixed-point top-k block and Gram, FP64 near-pair real space) against the
-reference's golden charges and the FP64 path, through the C ABI.
+"""GPU parity of the mixed-precision fit (separable double-float reciprocal sum,
+FP32 real space with FP64 cutoff decisions, exact fixed-point Gram on the
+tensor cores) against the reference's golden charges, the oracle's Phi and the
+FP64 path, through the C ABI.
 
 Tolerance: max|dq| <= 1e-5 e on well-conditioned fits (the target the fit is
 specified to); measured margins are far larger (~1e-7 e or better)."""
@@ -36,6 +37,33 @@ def test_mixed_normal_equations_close_to_fp64(name, gpu_ctx):
     b64, bm = a.b.cpu().numpy(), b.b.cpu().numpy()
     assert np.abs(Am - A64).max() <= 1e-6 * np.abs(A64).max()
     assert np.abs(bm - b64).max() <= 1e-6 * np.abs(b64).max()
+
+
+@pytest.mark.parametrize("name", ["water24", "tricmini"])
+def test_mixed_phi_parts_match_oracle(name, gpu_ctx, oracle_mod):
+    """Each part of the mixed Phi against the oracle's FP64 Phi on the same kept points.
+    Real space: FP32 terms, so 1e-6 of max|Phi|; reciprocal: double-float, 1e-10."""
+    import torch
+    L = gpu_ctx.lib
+    L.rp_debug_mixed_phi.restype = ctypes.c_int
+    L.rp_debug_mixed_phi.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                     ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_void_p]
+    cube, _ = load_golden(name)
+    V = torch.from_numpy(cube.V).cuda()
+    kept, Vc, M, _ = gpu_ctx.filter(cube.n_grid, cube.axis_vector, cube.atom_pos, cube.atom_index, V)
+    ew = gpu_ctx.ewald(cube.n_grid, cube.axis_vector, cube.cutoff, cube.kmax)
+    of = oracle_mod.OracleFit(cube)
+    atoms = np.ascontiguousarray(cube.atom_pos, dtype=np.float64)
+    real_ref = oracle_mod.phi(of.grid, atoms, of.kv[:0], of.kc[:0], of.shifts, of.zero_idx, cube.cutoff)
+    rec_ref = oracle_mod.phi(of.grid, atoms, of.kv, of.kc, of.shifts[:0], -1, cube.cutoff)
+    N = len(atoms)
+    for parts, ref, tol in ((1, real_ref, 1e-6), (2, rec_ref, 1e-10), (3, real_ref + rec_ref, 1e-6)):
+        out = torch.zeros((N, M), dtype=torch.float64, device="cuda")
+        gpu_ctx.check(L.rp_debug_mixed_phi(gpu_ctx.ptr, ew.ptr, atoms.ctypes.data, N, kept.data_ptr(), M, parts,
+                                           out.data_ptr()))
+        err = np.abs(out.cpu().numpy().T - ref).max() / np.abs(ref).max()
+        assert err <= tol, (parts, err)
+    ew.close()
 
 
 def test_mixed_fit_is_deterministic(gpu_ctx):
