@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cublas_v2.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
@@ -106,6 +107,24 @@ struct rp_ctx {
     T *buf_t(const std::string &name, size_t count) {
         return static_cast<T *>(buf(name, count * sizeof(T)));
     }
+    // Grow-only pinned host staging buffer (one H2D copy per batch instead of many
+    // small pageable ones); callers synchronise their stream before it is reused.
+    std::unordered_map<std::string, rp::Buffer> host_scratch;
+    void *host_buf(const std::string &name, size_t bytes) {
+        bytes = std::max<size_t>(256, (bytes + 255) & ~size_t(255));
+        auto &b = host_scratch[name];
+        if (b.bytes >= bytes) return b.ptr;
+        if (b.ptr) cudaFreeHost(b.ptr);
+        b.ptr = nullptr;
+        b.bytes = 0;
+        cudaError_t e = cudaMallocHost(&b.ptr, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            rp::fail(RP_E_NOMEM, "cudaMallocHost(" + std::to_string(bytes) + ") failed: " + cudaGetErrorString(e));
+        }
+        b.bytes = bytes;
+        return b.ptr;
+    }
     cublasHandle_t blas();
 };
 
@@ -114,6 +133,7 @@ struct rp_ewald {
     rp_grid grid{};
     double cutoff = 20.0, alpha = 0.0, sqrt_alpha = 0.0, volume = 0.0;
     double box[9]{};
+    double rec[9]{};  // reciprocal basis b1, b2, b3 (rows), b_i . box_j = 2 pi delta_ij
     int kmax = 7;
     int K = 0;
     std::vector<double> kvec;    // 3K
@@ -133,9 +153,22 @@ struct rp_ewald {
     float4 *d_exf = nullptr;      // kmax * nx
     float4 *d_eyf = nullptr;      // (2kmax-1) * ny
     float4 *d_ezf = nullptr;      // (2kmax-1) * nz
+    // every device table above lives in one block: `image` is its host copy, `off` the
+    // table offsets; d_block is owned (rp_ewald_setup) or borrowed from a ctx arena (batches)
+    std::vector<char> image;
+    size_t off[9]{};
+    void *d_block = nullptr;
+    bool owns = false;
 };
 
 namespace rp {
+
+// Ewald tables (ewald_tables.cu): host part, device image size, placement in a device block.
+void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax);
+size_t ewald_device_bytes(const rp_ewald *ew);
+void ewald_place(rp_ewald *ew, void *dev);
+void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax);  // owns one cudaMalloc block
+void ewald_free(rp_ewald *ew);
 
 // Host helpers shared by the stages.
 void prune_shifts(const rp_ewald *ew, const double *atoms, int N, std::vector<double> &out, int &zero_idx);
@@ -150,15 +183,20 @@ void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int
                 int64_t *M_out, uint8_t *mask_dev, cudaStream_t stream);
 // Asynchronous form: the kept count lands in *M_dev; kept_idx_dev and Vc_dev hold a
 // whole grid (capacity = nx*ny*nz).  `tag` keeps the scratch of concurrent calls apart.
+// brick_order: kept points in 8x4x4 brick order instead of flat order (the mixed fit
+// is order-independent and culls real-space images per compact tile).
+// vstats_dev (optional, 2 doubles): sum and max |.| of the centred ESP.
 void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
                   double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev,
-                  uint8_t *mask_dev, cudaStream_t stream, const std::string &tag);
+                  uint8_t *mask_dev, cudaStream_t stream, const std::string &tag, bool brick_order,
+                  double *vstats_dev);
 void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
                cudaStream_t stream);
+// vstats_dev: the filter's (sum, max |.|) of Vc, or nullptr to compute them here.
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
-                cudaStream_t stream);
+                cudaStream_t stream, const double *vstats_dev = nullptr);
 void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
                const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,
                double *info, cudaStream_t stream);

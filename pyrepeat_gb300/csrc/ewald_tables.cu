@@ -13,6 +13,7 @@
 // large-argument sincos is needed; atom phases k.r_a take one FP64 sincos each.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "common.cuh"
 #include "df.cuh"
@@ -25,7 +26,7 @@ static void cross3(const double *a, const double *b, double *c) {
     c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax) {
+void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax) {
     RP_REQUIRE(cutoff > 0.0, "rp_ewald_setup: cutoff must be > 0");
     RP_REQUIRE(kmax >= 1 && kmax <= 64, "rp_ewald_setup: kmax must be in 1..64");
     for (int i = 0; i < 3; ++i) RP_REQUIRE(grid->n_grid[i] > 0, "rp_ewald_setup: grid counts must be > 0");
@@ -43,7 +44,7 @@ void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax) {
     RP_REQUIRE(std::fabs(vol) > 1e-12, "rp_ewald_setup: degenerate cell");
     ew->volume = vol;
     const double PI = 3.14159265358979323846;
-    double rec[9];
+    double *rec = ew->rec;
     for (int d = 0; d < 3; ++d) {
         rec[d] = 2 * PI * bc[d] / vol;
         rec[3 + d] = 2 * PI * ca[d] / vol;
@@ -99,19 +100,6 @@ void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax) {
         for (int j = 0; j < ny; ++j) ey[(size_t)(n + kmax) * ny + j] = phase(n, j, ny);
         for (int l = 0; l < nz; ++l) ez[(size_t)(n + kmax) * nz + l] = phase(n, l, nz);
     }
-    RP_CUDA(cudaMalloc(&ew->d_kidx, sizeof(int) * 3 * (size_t)ew->K));
-    RP_CUDA(cudaMalloc(&ew->d_kcoef, sizeof(double) * (size_t)ew->K));
-    RP_CUDA(cudaMalloc(&ew->d_kvec, sizeof(double) * 3 * (size_t)ew->K));
-    RP_CUDA(cudaMalloc(&ew->d_ex, sizeof(double2) * ex.size()));
-    RP_CUDA(cudaMalloc(&ew->d_ey, sizeof(double2) * ey.size()));
-    RP_CUDA(cudaMalloc(&ew->d_ez, sizeof(double2) * ez.size()));
-    RP_CUDA(cudaMemcpy(ew->d_kidx, ew->kidx.data(), sizeof(int) * ew->kidx.size(), cudaMemcpyHostToDevice));
-    RP_CUDA(cudaMemcpy(ew->d_kcoef, ew->kcoef.data(), sizeof(double) * ew->kcoef.size(), cudaMemcpyHostToDevice));
-    RP_CUDA(cudaMemcpy(ew->d_kvec, ew->kvec.data(), sizeof(double) * ew->kvec.size(), cudaMemcpyHostToDevice));
-    RP_CUDA(cudaMemcpy(ew->d_ex, ex.data(), sizeof(double2) * ex.size(), cudaMemcpyHostToDevice));
-    RP_CUDA(cudaMemcpy(ew->d_ey, ey.data(), sizeof(double2) * ey.size(), cudaMemcpyHostToDevice));
-    RP_CUDA(cudaMemcpy(ew->d_ez, ez.data(), sizeof(double2) * ez.size(), cudaMemcpyHostToDevice));
-
     // double-float copies over n in [-(kmax-1), kmax-1] for the separable reciprocal sum
     const int P = kmax - 1, nw = 2 * P + 1;
     std::vector<float4> exf((size_t)(P + 1) * nx), eyf((size_t)nw * ny), ezf((size_t)nw * nz);
@@ -130,24 +118,52 @@ void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax) {
             ezf[(size_t)(n + P) * nz + l] = dfa::split(v.x, v.y);
         }
     }
-    RP_CUDA(cudaMalloc(&ew->d_exf, sizeof(float4) * exf.size()));
-    RP_CUDA(cudaMalloc(&ew->d_eyf, sizeof(float4) * eyf.size()));
-    RP_CUDA(cudaMalloc(&ew->d_ezf, sizeof(float4) * ezf.size()));
-    RP_CUDA(cudaMemcpy(ew->d_exf, exf.data(), sizeof(float4) * exf.size(), cudaMemcpyHostToDevice));
-    RP_CUDA(cudaMemcpy(ew->d_eyf, eyf.data(), sizeof(float4) * eyf.size(), cudaMemcpyHostToDevice));
-    RP_CUDA(cudaMemcpy(ew->d_ezf, ezf.data(), sizeof(float4) * ezf.size(), cudaMemcpyHostToDevice));
+    // one contiguous image of every device table (placed by ewald_place)
+    ew->image.clear();
+    auto put = [&](const void *src, size_t bytes) {
+        const size_t off = (ew->image.size() + 255) & ~size_t(255);
+        ew->image.resize(off + bytes);
+        if (bytes) std::memcpy(ew->image.data() + off, src, bytes);
+        return off;
+    };
+    ew->off[0] = put(ew->kidx.data(), sizeof(int) * ew->kidx.size());
+    ew->off[1] = put(ew->kcoef.data(), sizeof(double) * ew->kcoef.size());
+    ew->off[2] = put(ew->kvec.data(), sizeof(double) * ew->kvec.size());
+    ew->off[3] = put(ex.data(), sizeof(double2) * ex.size());
+    ew->off[4] = put(ey.data(), sizeof(double2) * ey.size());
+    ew->off[5] = put(ez.data(), sizeof(double2) * ez.size());
+    ew->off[6] = put(exf.data(), sizeof(float4) * exf.size());
+    ew->off[7] = put(eyf.data(), sizeof(float4) * eyf.size());
+    ew->off[8] = put(ezf.data(), sizeof(float4) * ezf.size());
+    ew->image.resize((ew->image.size() + 255) & ~size_t(255));
+}
+
+size_t ewald_device_bytes(const rp_ewald *ew) { return ew->image.size(); }
+
+void ewald_place(rp_ewald *ew, void *dev) {
+    char *b = static_cast<char *>(dev);
+    ew->d_kidx = reinterpret_cast<int *>(b + ew->off[0]);
+    ew->d_kcoef = reinterpret_cast<double *>(b + ew->off[1]);
+    ew->d_kvec = reinterpret_cast<double *>(b + ew->off[2]);
+    ew->d_ex = reinterpret_cast<double2 *>(b + ew->off[3]);
+    ew->d_ey = reinterpret_cast<double2 *>(b + ew->off[4]);
+    ew->d_ez = reinterpret_cast<double2 *>(b + ew->off[5]);
+    ew->d_exf = reinterpret_cast<float4 *>(b + ew->off[6]);
+    ew->d_eyf = reinterpret_cast<float4 *>(b + ew->off[7]);
+    ew->d_ezf = reinterpret_cast<float4 *>(b + ew->off[8]);
+}
+
+void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax) {
+    ewald_build_host(ew, grid, cutoff, kmax);
+    RP_CUDA(cudaMalloc(&ew->d_block, ewald_device_bytes(ew)));
+    ew->owns = true;
+    ewald_place(ew, ew->d_block);
+    RP_CUDA(cudaMemcpy(ew->d_block, ew->image.data(), ew->image.size(), cudaMemcpyHostToDevice));
 }
 
 void ewald_free(rp_ewald *ew) {
-    cudaFree(ew->d_kidx);
-    cudaFree(ew->d_kcoef);
-    cudaFree(ew->d_kvec);
-    cudaFree(ew->d_ex);
-    cudaFree(ew->d_ey);
-    cudaFree(ew->d_ez);
-    cudaFree(ew->d_exf);
-    cudaFree(ew->d_eyf);
-    cudaFree(ew->d_ezf);
+    if (ew->owns && ew->d_block) cudaFree(ew->d_block);
+    ew->d_block = nullptr;
 }
 
 void prune_shifts(const rp_ewald *ew, const double *atoms, int N, std::vector<double> &out, int &zero_idx) {

@@ -197,6 +197,65 @@ __global__ void __launch_bounds__(kFilterThreads) compact_kernel(
     }
 }
 
+// Brick-ordered compaction: bricks of 8 x 4 x 4 grid points (one CTA of 128 threads
+// each, x fastest), bricks in x-then-y-then-z order, points inside a brick in the
+// same order.  The kept points of a brick are contiguous, so any 128 consecutive
+// kept points span a compact region of the cell (the real-space culling of the
+// mixed fit keeps fewer images for compact tiles).  Deterministic (ballots only).
+constexpr int kBrickX = 8, kBrickY = 4, kBrickZ = 4;
+constexpr int kBrickPts = kBrickX * kBrickY * kBrickZ;  // 128
+
+__device__ __forceinline__ long long brick_point(int b, int t, int nx, int ny, int nz, int nbx, int nby) {
+    const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+    const int i = bx * kBrickX + (t % kBrickX), j = by * kBrickY + ((t / kBrickX) % kBrickY),
+              l = bz * kBrickZ + t / (kBrickX * kBrickY);
+    if (i >= nx || j >= ny || l >= nz) return -1;
+    return (long long)i + (long long)nx * (j + (long long)ny * l);
+}
+
+__global__ void __launch_bounds__(kBrickPts) brick_count_kernel(const uint8_t *__restrict__ mask, int nx, int ny,
+                                                                int nz, int nbx, int nby, int *__restrict__ counts) {
+    const long long f = brick_point(blockIdx.x, threadIdx.x, nx, ny, nz, nbx, nby);
+    const int keep = (f >= 0) ? mask[f] : 0;
+    const int cnt = __syncthreads_count(keep);
+    if (threadIdx.x == 0) counts[blockIdx.x] = cnt;
+}
+
+__global__ void __launch_bounds__(kBrickPts) brick_compact_kernel(
+    const uint8_t *__restrict__ mask, const double *__restrict__ V, int nx, int ny, int nz, int nbx, int nby,
+    const long long *__restrict__ offsets, long long capacity, int32_t *__restrict__ kept_idx,
+    double *__restrict__ Vc, double *__restrict__ block_vsum) {
+    __shared__ int warp_base[kBrickPts / 32];
+    __shared__ double warp_sum[kBrickPts / 32];
+    const long long f = brick_point(blockIdx.x, threadIdx.x, nx, ny, nz, nbx, nby);
+    const int keep = (f >= 0) ? mask[f] : 0;
+    const double v = keep ? V[f] : 0.0;
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int pos_in_warp = __popc(bal & ((1u << lane) - 1u));
+    double s = v;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        warp_base[warp] = __popc(bal);
+        warp_sum[warp] = s;
+    }
+    __syncthreads();
+    int base = 0;
+    for (int w = 0; w < warp; ++w) base += warp_base[w];
+    if (keep) {
+        const long long pos = offsets[blockIdx.x] + base + pos_in_warp;
+        if (pos < capacity) {
+            kept_idx[pos] = (int32_t)f;
+            Vc[pos] = v;
+        }
+    }
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < kBrickPts / 32; ++w) t += warp_sum[w];
+        block_vsum[blockIdx.x] = t;
+    }
+}
+
 // Mean of kept V over all blocks in a fixed order (deterministic), one block.
 __global__ void __launch_bounds__(1024) vmean_kernel(const double *__restrict__ block_vsum, int nb,
                                                      const long long *__restrict__ total,
@@ -217,11 +276,53 @@ __global__ void __launch_bounds__(1024) vmean_kernel(const double *__restrict__ 
     }
 }
 
-__global__ void center_kernel(double *__restrict__ Vc, const long long *__restrict__ Mp, const double *__restrict__ mean) {
+// Centre the kept ESP (Vc -= mean) and, when part != nullptr, write each block's sum of
+// the centred values and their largest magnitude (the ESP row statistics of the mixed
+// Gram), reduced in a fixed order by vstats_kernel.
+constexpr int kCenterThreads = 256;
+__global__ void __launch_bounds__(kCenterThreads) center_kernel(double *__restrict__ Vc,
+                                                                const long long *__restrict__ Mp,
+                                                                const double *__restrict__ mean,
+                                                                double2 *__restrict__ part) {
     const double m = *mean;
     const long long M = *Mp;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x)
-        Vc[i] -= m;
+    double s = 0.0, mx = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
+        const double v = Vc[i] - m;
+        Vc[i] = v;
+        s += v;
+        mx = fmax(mx, fabs(v));
+    }
+    if (!part) return;
+    __shared__ double ss[kCenterThreads / 32], sm[kCenterThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        ss[threadIdx.x >> 5] = s;
+        sm[threadIdx.x >> 5] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0, u = 0.0;
+        for (int w = 0; w < kCenterThreads / 32; ++w) {
+            t += ss[w];
+            u = fmax(u, sm[w]);
+        }
+        part[blockIdx.x] = make_double2(t, u);
+    }
+}
+
+__global__ void vstats_kernel(const double2 *__restrict__ part, int nb, double *__restrict__ vstats) {
+    if (threadIdx.x != 0) return;
+    double t = 0.0, u = 0.0;
+    for (int b = 0; b < nb; ++b) {
+        t += part[b].x;
+        u = fmax(u, part[b].y);
+    }
+    vstats[0] = t;
+    vstats[1] = u;
 }
 
 double radius_of(int z) {
@@ -244,7 +345,8 @@ double radius_of(int z) {
 
 void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
                   double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev,
-                  uint8_t *mask_dev, cudaStream_t stream, const std::string &tag) {
+                  uint8_t *mask_dev, cudaStream_t stream, const std::string &tag, bool brick_order,
+                  double *vstats_dev) {
     RP_REQUIRE(grid && atoms && Z && V_dev && M_dev, "rp_filter: null argument");
     const long long capacity = (long long)grid->n_grid[0] * grid->n_grid[1] * grid->n_grid[2];
     RP_REQUIRE(N >= 0, "rp_filter: N < 0");
@@ -417,15 +519,39 @@ void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const i
     filter_mask_kernel<<<nblk, kFilterThreads, 0, stream>>>(p, d_e32, d_e64, d_rmax2, d_rmax2f, d_boff, d_bidx,
                                                             d_mask, d_counts, d_re);
     RP_LAUNCH_CHECK();
-    scan_counts_kernel<<<1, 1024, 0, stream>>>(d_counts, nblk, d_offsets, d_total);
+    if (!brick_order) {
+        scan_counts_kernel<<<1, 1024, 0, stream>>>(d_counts, nblk, d_offsets, d_total);
+        RP_LAUNCH_CHECK();
+        compact_kernel<<<nblk, kFilterThreads, 0, stream>>>(d_mask, V_dev, n_total, d_offsets, capacity,
+                                                            kept_idx_dev, Vc_dev, d_vsum);
+        RP_LAUNCH_CHECK();
+        vmean_kernel<<<1, 1024, 0, stream>>>(d_vsum, nblk, d_total, d_mean);
+        RP_LAUNCH_CHECK();
+    } else {
+        const int nbx = (nx + kBrickX - 1) / kBrickX, nby = (ny + kBrickY - 1) / kBrickY,
+                  nbz = (nz + kBrickZ - 1) / kBrickZ;
+        const int nbr = nbx * nby * nbz;
+        int *d_bc = ctx->buf_t<int>("flt_bcounts" + tag, (size_t)nbr);
+        long long *d_bo = ctx->buf_t<long long>("flt_boffsets" + tag, (size_t)nbr);
+        double *d_bv = ctx->buf_t<double>("flt_bvsum" + tag, (size_t)nbr);
+        brick_count_kernel<<<nbr, kBrickPts, 0, stream>>>(d_mask, nx, ny, nz, nbx, nby, d_bc);
+        RP_LAUNCH_CHECK();
+        scan_counts_kernel<<<1, 1024, 0, stream>>>(d_bc, nbr, d_bo, d_total);
+        RP_LAUNCH_CHECK();
+        brick_compact_kernel<<<nbr, kBrickPts, 0, stream>>>(d_mask, V_dev, nx, ny, nz, nbx, nby, d_bo, capacity,
+                                                            kept_idx_dev, Vc_dev, d_bv);
+        RP_LAUNCH_CHECK();
+        vmean_kernel<<<1, 1024, 0, stream>>>(d_bv, nbr, d_total, d_mean);
+        RP_LAUNCH_CHECK();
+    }
+    const int ncb = ctx->sm_count * 4;
+    double2 *d_part = vstats_dev ? ctx->buf_t<double2>("flt_vpart" + tag, (size_t)ncb) : nullptr;
+    center_kernel<<<ncb, kCenterThreads, 0, stream>>>(Vc_dev, d_total, d_mean, d_part);
     RP_LAUNCH_CHECK();
-    compact_kernel<<<nblk, kFilterThreads, 0, stream>>>(d_mask, V_dev, n_total, d_offsets, capacity,
-                                                        kept_idx_dev, Vc_dev, d_vsum);
-    RP_LAUNCH_CHECK();
-    vmean_kernel<<<1, 1024, 0, stream>>>(d_vsum, nblk, d_total, d_mean);
-    RP_LAUNCH_CHECK();
-    center_kernel<<<ctx->sm_count * 4, 256, 0, stream>>>(Vc_dev, d_total, d_mean);
-    RP_LAUNCH_CHECK();
+    if (vstats_dev) {
+        vstats_kernel<<<1, 32, 0, stream>>>(d_part, ncb, vstats_dev);
+        RP_LAUNCH_CHECK();
+    }
 }
 
 void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
@@ -439,7 +565,8 @@ void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int
     int32_t *kid = direct ? kept_idx_dev : ctx->buf_t<int32_t>("flt_kept_stage", (size_t)npts);
     double *vc = direct ? Vc_dev : ctx->buf_t<double>("flt_vc_stage", (size_t)npts);
     long long *d_M = ctx->buf_t<long long>("flt_total", 1);
-    filter_async(ctx, grid, atoms, Z, N, V_dev, vdw_factor, vdw_max, kid, vc, d_M, mask_dev, stream, "");
+    filter_async(ctx, grid, atoms, Z, N, V_dev, vdw_factor, vdw_max, kid, vc, d_M, mask_dev, stream, "", false,
+                 nullptr);
     long long M = 0;
     RP_CUDA(cudaMemcpyAsync(&M, d_M, sizeof(long long), cudaMemcpyDeviceToHost, stream));
     RP_CUDA(cudaStreamSynchronize(stream));

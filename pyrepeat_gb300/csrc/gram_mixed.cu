@@ -235,6 +235,13 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
     if (warp == 1) tc::tmem_dealloc(tmem, 512);
 }
 
+// ESP row scale 2^(-e-1) with max|Vc| in [2^(e-1), 2^e), so |V * scale| < 1/2
+__device__ __forceinline__ float vscale_of(double vmax) {
+    int e = 0;
+    if (vmax > 0.0) frexp(vmax, &e);
+    return ldexpf(1.0f, -e - 1);
+}
+
 // Four 7-bit signed digits of an integer I = round(x 2^27), |x| <= 1:
 // x ~ 2^-6 (s0 + 2^-7 s1 + 2^-14 s2 + 2^-21 s3), digits rounded half up so |s| <= 64,
 // each exact in FP16.  Integer shifts only (no FP64 on the per-element path).
@@ -308,14 +315,27 @@ __device__ __forceinline__ float2 df_sub(float ah, float al, float bh, float bl)
 // those within Rc + 1e-3 Bohr of the bounding box of its points, in shift order
 // (warp-ballot compaction, so the summation order is fixed).  Distances are formed
 // in FP32 from double-float coordinates relative to the CTA's first point; images
-// within 0.05 % of Rc (where the reference's FP64 cutoff decision is made) and
+// within 1e-5 of Rc (where the reference's FP64 cutoff decision is made) and
 // pairs closer than sqrt(near2) are evaluated in FP64 with the reference's
 // expressions, the rest with FP32 erfcf.  Reciprocal part: stage C of the
 // separable sum in double-float.  `parts`: bit 0 real space, bit 1 reciprocal.
 // With psum/pmax given, the CTA also writes each atom's sum and max |Phi| over its
 // points (fixed-order reductions), the column statistics of the centring step.
+// The grid step vectors as double-float (a[d] = h[d] + l[d]), passed by value.
+struct AxisDF {
+    float h[9], l[9];
+};
+
+// k * (ah + al) for a small integer k, as an unevaluated pair (p, e)
+__device__ __forceinline__ void int_times_df(float k, float ah, float al, float &p, float &e) {
+    p = __fmul_rn(k, ah);
+    e = __fmaf_rn(k, ah, -p);
+    e = __fmaf_rn(k, al, e);
+}
+
 __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
-    const int32_t *__restrict__ kept, long long m0, long long rows, const double *__restrict__ axis, int nx, int ny,
+    const int32_t *__restrict__ kept, long long m0, long long rows, const double *__restrict__ axis, AxisDF adf,
+    int nx, int ny,
     const double *__restrict__ atoms, int N, const double *__restrict__ shifts, int S, int scap, int zero_idx,
     double rc, double sa, float near2, const float4 *__restrict__ img, const float4 *__restrict__ EX,
     const float4 *__restrict__ E, int n1c, int parts, float2 *__restrict__ phit, long long ld,
@@ -336,25 +356,43 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
     const long long m = mb + threadIdx.x;
     const bool valid = m < rows;
 
-    double origin[3];
-    {
+    // CTA origin: the first point of the tile (FP64 once, shared as a double-float)
+    __shared__ float org[6];
+    __shared__ int org_idx[3];
+    if (threadIdx.x == 0) {
         const int f0 = kept[m0 + mb];
-        const int l = f0 / layer, rem = f0 - l * layer, j = rem / nx, i = rem - j * nx;
-        for (int d = 0; d < 3; ++d)
-            origin[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)l * axis[6 + d];
+        const int l0 = f0 / layer, r0 = f0 - l0 * layer, j0 = r0 / nx, i0 = r0 - j0 * nx;
+        for (int d = 0; d < 3; ++d) {
+            const double o = ((double)i0 * axis[d] + (double)j0 * axis[3 + d]) + (double)l0 * axis[6 + d];
+            org[d] = (float)o;
+            org[3 + d] = (float)(o - (double)org[d]);
+        }
+        org_idx[0] = i0;
+        org_idx[1] = j0;
+        org_idx[2] = l0;
     }
+    __syncthreads();
     const int f = kept[m0 + (valid ? m : mb)];
     const int l = f / layer, rem = f - l * layer, j = rem / nx, i = rem - j * nx;
-    double gabs[3];
+    // point - origin = di a0 + dj a1 + dl a2 with small integers: double-float on the FP32 pipe
     float gh[3], gl[3], oh[3], ol[3];
+    {
+        const float di = (float)(i - org_idx[0]), dj = (float)(j - org_idx[1]), dl = (float)(l - org_idx[2]);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        gabs[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)l * axis[6 + d];
-        const double gd = gabs[d] - origin[d];
-        gh[d] = (float)gd;
-        gl[d] = (float)(gd - (double)gh[d]);
-        oh[d] = (float)origin[d];
-        ol[d] = (float)(origin[d] - (double)oh[d]);
+        for (int d = 0; d < 3; ++d) {
+            float p0, e0, p1, e1, p2, e2, s, t;
+            int_times_df(di, adf.h[d], adf.l[d], p0, e0);
+            int_times_df(dj, adf.h[3 + d], adf.l[3 + d], p1, e1);
+            int_times_df(dl, adf.h[6 + d], adf.l[6 + d], p2, e2);
+            dfa::two_sum(p0, p1, s, t);
+            float s2, t2;
+            dfa::two_sum(s, p2, s2, t2);
+            const float e = __fadd_rn(__fadd_rn(__fadd_rn(e0, e1), e2), __fadd_rn(t, t2));
+            gh[d] = __fadd_rn(s2, e);
+            gl[d] = __fadd_rn(e, -__fadd_rn(gh[d], -s2));
+            oh[d] = org[d];
+            ol[d] = org[3 + d];
+        }
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -417,7 +455,11 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
     }
     __syncthreads();
 
-    const float rcc = (float)(rc * rc), rc2 = rcc * 1.0001f, saf = (float)sa;
+    // FP64 decides every image whose FP32 squared distance lies within +-2e-5 Rc^2 of the
+    // cutoff: with coordinates exact to ~2^-48, |r2_fp32 - r2| stays below ~8 ulp(r2) (5e-7
+    // relative), so the band covers the FP32 error 40-fold while keeping the FP64 path rare
+    // (a wider band makes whole warps take it and the FP64 pipe becomes the bottleneck).
+    const float rcc = (float)(rc * rc), band = 2e-5f * rcc, saf = (float)sa;
     const float fp64_below = fmaxf(near2, 1e-6f);
     const long long row = f / nx;  // j + l * ny
     for (int a = 0; a < na; ++a) {
@@ -437,10 +479,13 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
                 const float dx = (gh[0] - h.x) + (gl[0] - lo.x), dy = (gh[1] - h.y) + (gl[1] - lo.y),
                             dz = (gh[2] - h.z) + (gl[2] - lo.z);
                 const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 > rc2) continue;
-                if (r2 < fp64_below || fabsf(r2 - rcc) < 1e-3f * rcc) {
+                if (r2 > rcc + band) continue;
+                if (r2 < fp64_below || r2 > rcc - band) {
                     const int s = __float_as_int(h.w);
                     const double *p = atoms + 3 * (a0 + a);
+                    double gabs[3];
+                    for (int d = 0; d < 3; ++d)
+                        gabs[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)l * axis[6 + d];
                     const double ex = gabs[0] - (p[0] + shifts[3 * s]), ey = gabs[1] - (p[1] + shifts[3 * s + 1]),
                                  ez = gabs[2] - (p[2] + shifts[3 * s + 2]);
                     const double r = sqrt(ex * ex + ey * ey + ez * ez);
@@ -502,7 +547,7 @@ size_t phi_smem_bytes(int n1c, int scap) {
     return sizeof(float4) * ((size_t)n1c * kPhiPts + 2 * (size_t)kPhiAtoms * scap);
 }
 
-void launch_phi(const int32_t *kept, long long m0, long long rows, const double *d_axis, int nx, int ny,
+void launch_phi(const int32_t *kept, long long m0, long long rows, const double *d_axis, const double *h_axis, int nx, int ny,
                 const double *d_atoms, int N, const double *d_shifts, int S, int zero_idx, double rc, double sa,
                 const float4 *img, const float4 *EX, const float4 *E, int n1c, int parts, float2 *phit, long long ld,
                 double *psum, float *pmax, cudaStream_t s) {
@@ -515,27 +560,38 @@ void launch_phi(const int32_t *kept, long long m0, long long rows, const double 
         RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = smem;
     }
+    AxisDF adf;
+    for (int q = 0; q < 9; ++q) {
+        adf.h[q] = (float)h_axis[q];
+        adf.l[q] = (float)(h_axis[q] - (double)adf.h[q]);
+    }
     dim3 grd(ceil_div(rows, kPhiPts), ceil_div(N, kPhiAtoms));
-    phi_chunk_kernel<<<grd, kPhiPts, smem, s>>>(kept, m0, rows, d_axis, nx, ny, d_atoms, N, d_shifts, S, scap, zero_idx,
+    phi_chunk_kernel<<<grd, kPhiPts, smem, s>>>(kept, m0, rows, d_axis, adf, nx, ny, d_atoms, N, d_shifts, S, scap, zero_idx,
                                                 rc, sa, real_near2(), img, EX, E, n1c, parts, phit, ld, psum, pmax);
     RP_LAUNCH_CHECK();
 }
 
 // ------------------------------------------------------------------ column statistics and the split
 
-// Per atom: the chunk's sum (into sphi) from the phi kernel's per-CTA partials, and on
-// the first chunk the centre c (a double-float, cvec = its exact FP64 value) and scale.
+// Per atom (one warp each): the chunk's sum (into sphi) from the phi kernel's per-CTA
+// partials in a fixed order, and on the first chunk the centre c (a double-float; cvec
+// holds its exact FP64 value) and the power-of-two scale.
 __global__ void colstats_finish_kernel(const double *__restrict__ psum, const float *__restrict__ pmax, int nblk,
                                        int N, long long rows, int first, double *__restrict__ sphi,
                                        double *__restrict__ c, float2 *__restrict__ cdf, float *__restrict__ scale) {
-    int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= N) return;
+    const int a = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (a >= N) return;  // whole warp
     double s = 0.0;
     float mx = 0.f;
-    for (int k = 0; k < nblk; ++k) {
+    for (int k = lane; k < nblk; k += 32) {
         s += psum[(size_t)a * nblk + k];
         mx = fmaxf(mx, pmax[(size_t)a * nblk + k]);
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if (lane != 0) return;
     sphi[a] = first ? s : sphi[a] + s;
     if (first) {
         const double mean = s / (double)rows;
@@ -551,51 +607,72 @@ __global__ void colstats_finish_kernel(const double *__restrict__ psum, const fl
     }
 }
 
+// I = round(x 2^27) of one element of X (x = (Phi - c) scale, or the scaled ESP), |x| <= 1
+__device__ __forceinline__ int x_fixed(float h, float l, float sc, int *clamped) {
+    sc *= 134217728.0f;  // 2^27
+    if (fabsf(h * sc) > 134217728.0f) {  // |x| beyond 1: clamp (counted; the fit reports it)
+        atomicAdd(clamped, 1);
+        return h > 0.f ? (1 << 27) : -(1 << 27);
+    }
+    return round_df(h, l, sc);
+}
+
 // X rows: a < N: (Phi_t[a][m] - c_a) * scale_a;  a == N: Vc[m] * scale_V;  rest zero.
 // Each value x (|x| <= 1) becomes I = round(x 2^27) and four 7-bit digits
 // x ~ 2^-6 (x0 + 2^-7 x1 + 2^-14 x2 + 2^-21 x3), x_s integers in [-64, 64], exact in FP16.
+// One thread per two consecutive points of one row (16-B loads, 4-B stores).
 __global__ void slice_rows_kernel(const float2 *__restrict__ phit, long long ld, long long rows, long long rows_pad,
-                                  int N, int Np_pad, const float2 *__restrict__ cdf, const float *__restrict__ scale,
-                                  const double *__restrict__ Vc, long long m0, const float *__restrict__ vscale_p,
+                                  int N, const float2 *__restrict__ cdf, const float *__restrict__ scale,
+                                  const double *__restrict__ Vc, long long m0, const double *__restrict__ vmax_p,
                                   __half *__restrict__ X0, __half *__restrict__ X1, __half *__restrict__ X2,
                                   __half *__restrict__ X3, int *__restrict__ clamped) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)Np_pad * rows_pad) return;
-    const int a = (int)(t / rows_pad);
-    const long long m = t - (long long)a * rows_pad;
-    float h = 0.f, l = 0.f, sc = 0.f;
-    if (m < rows) {
-        if (a < N) {
-            const float2 v = phit[(long long)a * ld + m], c = cdf[a];
-            const float2 d = df_sub(v.x, v.y, c.x, c.y);
-            h = d.x;
-            l = d.y;
-            sc = scale[a];
-        } else if (a == N) {
-            const double v = Vc[m0 + m];
-            h = (float)v;
-            l = (float)(v - (double)h);
-            sc = *vscale_p;
+    const int a = blockIdx.y;
+    const long long m = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+    if (m >= rows_pad) return;
+    int I[2] = {0, 0};
+    if (a < N) {
+        const float2 c = cdf[a];
+        const float sc = scale[a];
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (m + 1 < rows) v = *reinterpret_cast<const float4 *>(phit + (long long)a * ld + m);
+        else if (m < rows) {
+            const float2 v0 = phit[(long long)a * ld + m];
+            v.x = v0.x;
+            v.y = v0.y;
         }
+        if (m < rows) {
+            const float2 d = df_sub(v.x, v.y, c.x, c.y);
+            I[0] = x_fixed(d.x, d.y, sc, clamped);
+        }
+        if (m + 1 < rows) {
+            const float2 d = df_sub(v.z, v.w, c.x, c.y);
+            I[1] = x_fixed(d.x, d.y, sc, clamped);
+        }
+    } else if (a == N) {
+        const float sc = vscale_of(*vmax_p);
+        for (int u = 0; u < 2; ++u)
+            if (m + u < rows) {
+                const double v = Vc[m0 + m + u];
+                const float h = (float)v;
+                I[u] = x_fixed(h, (float)(v - (double)h), sc, clamped);
+            }
     }
-    sc *= 134217728.0f;  // 2^27
-    int I;
-    if (fabsf(h * sc) > 134217728.0f) {  // |x| beyond ~1: clamp (counted; the fit reports it)
-        atomicAdd(clamped, 1);
-        I = h > 0.f ? (1 << 27) : -(1 << 27);
-    } else {
-        I = round_df(h, l, sc);
-    }
-    digits4(I, X0, X1, X2, X3, t);
+    __half d0[2], d1[2], d2[2], d3[2];
+    for (int u = 0; u < 2; ++u) digits4(I[u], d0, d1, d2, d3, u);
+    const long long idx = (long long)a * rows_pad + m;
+    *reinterpret_cast<__half2 *>(X0 + idx) = __halves2half2(d0[0], d0[1]);
+    *reinterpret_cast<__half2 *>(X1 + idx) = __halves2half2(d1[0], d1[1]);
+    *reinterpret_cast<__half2 *>(X2 + idx) = __halves2half2(d2[0], d2[1]);
+    *reinterpret_cast<__half2 *>(X3 + idx) = __halves2half2(d3[0], d3[1]);
 }
 
 // Sum the partial Gram tiles of all point splits in a fixed order (FP64; each
 // partial is an exact integer) and add them, unscaled, into G (Np x Np).  Tiles
 // inside a 128-row block already hold both (a,b) and (b,a); the others are mirrored.
 __global__ void gram_reduce_kernel(const double *__restrict__ part, int ntiles, int nsplit, int nt, int Np,
-                                   const float *__restrict__ scale, const float *__restrict__ vscale_p, int N,
+                                   const float *__restrict__ scale, const double *__restrict__ vmax_p, int N,
                                    double *__restrict__ G) {
-    const float vscale = *vscale_p;
+    const float vscale = vscale_of(*vmax_p);
     const int tile = blockIdx.y;
     int ti, tj;
     gram_tile_decode(tile, nt, ti, tj);
@@ -646,13 +723,6 @@ __global__ void __launch_bounds__(1024) absmax_kernel(const double *__restrict__
         __syncthreads();
     }
     if (threadIdx.x == 0) *out = sm[0];
-}
-
-// ESP row scale 2^(-e-1) with max|Vc| in [2^(e-1), 2^e), so |V * scale| < 1/2
-__global__ void vscale_kernel(const double *__restrict__ vmax, float *__restrict__ vscale) {
-    int e = 0;
-    if (*vmax > 0.0) frexp(*vmax, &e);
-    *vscale = ldexpf(1.0f, -e - 1);
 }
 
 // ------------------------------------------------------------------ host helpers
@@ -711,7 +781,7 @@ inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b
 
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
-                cudaStream_t stream) {
+                cudaStream_t stream, const double *vstats_dev) {
     RP_REQUIRE(N > 0 && M > 0, "rp_gram: need N > 0 and M > 0");
     std::vector<double> sh;
     int zero_idx = -1;
@@ -759,18 +829,17 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     float2 *cdf = ctx->buf_t<float2>("m_cdf", N);
     float *scale = ctx->buf_t<float>("m_scale", N);
     double *G = ctx->buf_t<double>("m_G", (size_t)Np * Np);
-    double *sumV = ctx->buf_t<double>("m_sumV", 1);
     RP_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * Np * Np, stream));
 
-    // ESP row scale: power of two from the largest |Vc|, computed on the device
-    float *vscale = ctx->buf_t<float>("m_vscale", 1);
-    {
-        column_sums_fp64(Vc_dev, M, 1, 1, sumV, false, ctx, stream);
-        double *d_vmax = ctx->buf_t<double>("m_vmax", 1);
-        absmax_kernel<<<1, 1024, 0, stream>>>(Vc_dev, M, d_vmax);
+    // ESP row statistics: sum of Vc (mean correction) and max |Vc| (row scale)
+    const double *sumV = vstats_dev, *vmax = vstats_dev ? vstats_dev + 1 : nullptr;
+    if (!vstats_dev) {
+        double *st = ctx->buf_t<double>("m_vstats", 2);
+        column_sums_fp64(Vc_dev, M, 1, 1, st, false, ctx, stream);
+        absmax_kernel<<<1, 1024, 0, stream>>>(Vc_dev, M, st + 1);
         RP_LAUNCH_CHECK();
-        vscale_kernel<<<1, 1, 0, stream>>>(d_vmax, vscale);
-        RP_LAUNCH_CHECK();
+        sumV = st;
+        vmax = st + 1;
     }
 
     const int nt = Np_pad / kBM;
@@ -784,18 +853,17 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         const int nb = (int)ceil_div(rows, kPhiPts);
         {
             StageTimer tt(ctx, "phi", stream);
-            launch_phi(kept_idx_dev, m0, rows, d_axis, nx, ny, d_atoms, N, d_shifts, S, zero_idx, ew->cutoff,
+            launch_phi(kept_idx_dev, m0, rows, d_axis, ew->grid.axis, nx, ny, d_atoms, N, d_shifts, S, zero_idx, ew->cutoff,
                        ew->sqrt_alpha, img, ew->d_exf, E, n1c, 3, phit, chunk_pad, psum, pmax, stream);
         }
         // 2. centre/scale on the first chunk, fixed-point digits of X
         {
             StageTimer tt(ctx, "center_slice", stream);
-            colstats_finish_kernel<<<ceil_div(N, 128), 128, 0, stream>>>(psum, pmax, nb, N, rows, m0 == 0 ? 1 : 0, sphi,
-                                                                         cvec, cdf, scale);
+            colstats_finish_kernel<<<ceil_div(N, 4), 128, 0, stream>>>(psum, pmax, nb, N, rows, m0 == 0 ? 1 : 0, sphi,
+                                                                       cvec, cdf, scale);
             RP_LAUNCH_CHECK();
-            slice_rows_kernel<<<ceil_div((long long)Np_pad * rows_kpad, 256), 256, 0, stream>>>(
-                phit, chunk_pad, rows, rows_kpad, N, Np_pad, cdf, scale, Vc_dev, m0, vscale, X[0], X[1], X[2], X[3],
-                d_clamped);
+            slice_rows_kernel<<<dim3(ceil_div(rows_kpad / 2, 256), Np_pad), 256, 0, stream>>>(
+                phit, chunk_pad, rows, rows_kpad, N, cdf, scale, Vc_dev, m0, vmax, X[0], X[1], X[2], X[3], d_clamped);
             RP_LAUNCH_CHECK();
         }
         // 3. exact Gram partial tiles over point splits, then the fixed-order FP64 reduction
@@ -818,7 +886,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
             }
             StageTimer tr(ctx, "gram_reduce_fp64", stream);
             gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256, 0, stream>>>(part, ntri, nsplit, nt, Np,
-                                                                                         scale, vscale, N, G);
+                                                                                         scale, vmax, N, G);
             RP_LAUNCH_CHECK();
         }
     }
@@ -854,7 +922,7 @@ extern "C" int rp_debug_mixed_phi(rp_ctx *ctx, const rp_ewald *ew, const double 
         images_df_kernel<<<ceil_div((long long)N * S, 128), 128>>>(d_atoms, N, d_shifts, S, img);
         RP_LAUNCH_CHECK();
         float2 *ph = ctx->buf_t<float2>("dbg_phi", (size_t)N * rows);
-        launch_phi(kept_idx_dev, 0, rows, d_axis, ew->grid.n_grid[0], ew->grid.n_grid[1], d_atoms, N, d_shifts, S,
+        launch_phi(kept_idx_dev, 0, rows, d_axis, ew->grid.axis, ew->grid.n_grid[0], ew->grid.n_grid[1], d_atoms, N, d_shifts, S,
                    zero_idx, ew->cutoff, ew->sqrt_alpha, img, ew->d_exf, E, ew->kmax, parts, ph, rows, nullptr,
                    nullptr, 0);
         df_to_double_kernel<<<ceil_div((long long)N * rows, 256), 256>>>(ph, (long long)N * rows, phi_dev);
@@ -891,7 +959,9 @@ extern "C" int rp_debug_gram_slices(rp_ctx *ctx, const void *X0, const void *X1,
         std::vector<float> h((size_t)Np, 1.0f);
         RP_CUDA(cudaMemcpy(ones, h.data(), sizeof(float) * Np, cudaMemcpyHostToDevice));
         RP_CUDA(cudaMemset(I_dev, 0, sizeof(double) * Np * Np));
-        gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256>>>(part, ntri, nsplit, nt, Np, ones, ones, Np, I_dev);
+        double *vmax = ctx->buf_t<double>("dbg_vmax", 1);  // unused: every row is an atom row (N = Np)
+        RP_CUDA(cudaMemset(vmax, 0, sizeof(double)));
+        gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256>>>(part, ntri, nsplit, nt, Np, ones, vmax, Np, I_dev);
         RP_LAUNCH_CHECK();
         RP_CUDA(cudaDeviceSynchronize());
         int st = 0;

@@ -6,8 +6,6 @@
 #include "common.cuh"
 
 namespace rp {
-void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax);
-void ewald_free(rp_ewald *ew);
 void potential_run(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const double *q, int N,
                    const int32_t *idx_dev, int64_t npts, double *out_dev, cudaStream_t stream);
 }  // namespace rp
@@ -88,6 +86,7 @@ int rp_ctx_destroy(rp_ctx *ctx) {
     if (!ctx) return RP_E_ARG;
     cudaSetDevice(ctx->device);
     for (auto &kv : ctx->scratch) cudaFree(kv.second.ptr);
+    for (auto &kv : ctx->host_scratch) cudaFreeHost(kv.second.ptr);
     if (ctx->cublas) cublasDestroy(ctx->cublas);
     cudaFree(ctx->d_status);
     delete ctx;
@@ -200,13 +199,24 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             off_n[i + 1] = off_n[i] + d.N;
             off_nn[i + 1] = off_nn[i] + (long long)d.N * d.N;
         }
-        // Ewald setups first: they make small synchronous uploads, so they go
-        // before any long GPU work is queued on the stream
+        // Ewald tables of every cube: built on the host, placed in one ctx arena and
+        // uploaded with a single copy from pinned memory (no per-fit allocation)
+        size_t ew_total = 0;
+        std::vector<size_t> ew_off((size_t)n);
         for (int i = 0; i < n; ++i) {
             ews[i] = new rp_ewald();
             ews[i]->device = ctx->device;
-            rp::ewald_build(ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax);
+            rp::ewald_build_host(ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax);
+            ew_off[i] = ew_total;
+            ew_total += rp::ewald_device_bytes(ews[i]);
         }
+        char *ew_dev = static_cast<char *>(ctx->buf("fit_ewald", ew_total));
+        char *ew_host = static_cast<char *>(ctx->host_buf("fit_ewald", ew_total));
+        for (int i = 0; i < n; ++i) {
+            std::memcpy(ew_host + ew_off[i], ews[i]->image.data(), ews[i]->image.size());
+            rp::ewald_place(ews[i], ew_dev + ew_off[i]);
+        }
+        RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, ew_total, cudaMemcpyHostToDevice, stream));
         int32_t *kept = ctx->buf_t<int32_t>("fit_kept", (size_t)off_pts[n]);
         double *Vc = ctx->buf_t<double>("fit_Vc", (size_t)off_pts[n]);
         double *Vh = nullptr;
@@ -217,6 +227,7 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
         double *A = ctx->buf_t<double>("fit_A", (size_t)off_nn[n]);
         double *b = ctx->buf_t<double>("fit_b", (size_t)off_n[n]);
         double *q = ctx->buf_t<double>("fit_q", (size_t)off_n[n]);
+        double *vst = ctx->buf_t<double>("fit_vstats", 2 * (size_t)n);
         rp::status_clear(ctx, stream);
         // 1. filters (asynchronous; kept counts stay on the device)
         for (int i = 0; i < n; ++i) {
@@ -225,7 +236,8 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             if (!(V_dev && V_dev[i]))
                 RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], d.V, sizeof(double) * npts[i], cudaMemcpyHostToDevice, stream));
             rp::filter_async(ctx, &d.grid, d.atoms, d.Z, d.N, V, d.vdw_factor, d.vdw_max, kept + off_pts[i],
-                             Vc + off_pts[i], Md + i, nullptr, stream, "");
+                             Vc + off_pts[i], Md + i, nullptr, stream, "", d.precision == RP_PREC_MIXED,
+                             vst + 2 * i);
         }
         // 2. one read of all kept counts (sizes every later launch)
         std::vector<long long> M((size_t)n);
@@ -240,7 +252,7 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             const rp_fit_desc &d = descs[i];
             if (d.precision == RP_PREC_MIXED)
                 rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
-                               b + off_n[i], nullptr, stream);
+                               b + off_n[i], nullptr, stream, vst + 2 * i);
             else
                 rp::gram_fp64(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
                               b + off_n[i], nullptr, stream);

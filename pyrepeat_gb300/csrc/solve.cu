@@ -13,9 +13,14 @@
 // which equals the reference's sequential column-then-row folding.  Groups
 // that overlap are folded on the host with the reference's sequential rules.
 //
-// One CTA factors one system (so a batch of systems is one launch), keeps the
-// original bordered matrix for one step of FP64 iterative refinement
-// x += LU^{-1}(b - A x), and reports the refined residual and pivot range.
+// One CTA solves one system (so a batch of systems is one launch).  It factors the
+// bordered matrix in FP32 (LU with partial pivoting) and refines x += LU32^{-1}(b - A x)
+// with FP64 residuals until the backward error |b - A x| <= n eps64 |A| |x| (the
+// classic mixed-precision iterative refinement; FP64 runs at a small fraction of
+// the FP32 rate on this part).  If the FP32 factorisation meets a zero pivot or the
+// refinement does not reach that bound in kRefineMax steps (cond(A) near 1/eps32),
+// the system is factored again in FP64 with one step of FP64 refinement.  Either
+// way the refined residual and the pivot range are reported.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -151,89 +156,221 @@ __device__ void lu_apply(const double *__restrict__ LU, const int *__restrict__ 
     (void)tmp;
 }
 
-__global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *__restrict__ descs) {
-    const SolveDesc d = descs[blockIdx.x];
-    const int n1 = d.n + 1;
-    double *A = d.As;
-    __shared__ double sv[kLU / 32];
-    __shared__ int si[kLU / 32];
-    __shared__ double piv_v;
-    __shared__ int piv_i;
-    double pmin = 1e308, pmax = 0.0;
-    int singular = 0;
+// max over the block (every thread gets the result)
+__device__ double block_max(double v, double *sv) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sv[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = sv[0];
+    for (int w = 1; w < kLU / 32; ++w) t = fmax(t, sv[w]);
+    return t;
+}
+
+// FP32 LU with partial pivoting in place (row-major n1 x n1).  Returns false on a
+// zero or non-finite pivot (the same value in every thread).
+__device__ bool lu_factor_f32(float *A, int *perm, int n1, double *sv, int *si, double *piv_v, int *piv_i,
+                              double &pmin, double &pmax) {
     for (int k = 0; k < n1; ++k) {
         double best = -1.0;
         int bi = 0x7fffffff;
         for (int r = k + threadIdx.x; r < n1; r += kLU) {
-            double v = fabs(A[(size_t)r * n1 + k]);
+            const double v = fabs((double)A[(size_t)r * n1 + k]);
             if (v > best || (v == best && r < bi)) { best = v; bi = r; }
         }
-        block_argmax(best, bi, sv, si, &piv_v, &piv_i);
-        const int p = piv_i;
-        if (threadIdx.x == 0) d.perm[k] = p;
+        block_argmax(best, bi, sv, si, piv_v, piv_i);
+        const int p = *piv_i;
+        if (threadIdx.x == 0) perm[k] = p;
         if (p != k)
             for (int c = threadIdx.x; c < n1; c += kLU) {
-                double t = A[(size_t)k * n1 + c];
+                const float t = A[(size_t)k * n1 + c];
                 A[(size_t)k * n1 + c] = A[(size_t)p * n1 + c];
                 A[(size_t)p * n1 + c] = t;
             }
         __syncthreads();
-        double pv = A[(size_t)k * n1 + k];
-        double apv = fabs(pv);
+        const float pv = A[(size_t)k * n1 + k];
+        const double apv = fabs((double)pv);
+        if (!(apv > 0.0) || !isfinite(pv)) return false;
         pmin = fmin(pmin, apv);
         pmax = fmax(pmax, apv);
-        if (!(apv > 1e-300)) {  // exactly singular: keep going with a tiny pivot, flag it
-            singular = 1;
-            pv = (pv < 0 ? -1e-300 : 1e-300);
-            if (threadIdx.x == 0) A[(size_t)k * n1 + k] = pv;
-        }
-        __syncthreads();
-        const double inv = 1.0 / pv;
+        const float inv = 1.0f / pv;
         for (int r = k + 1 + threadIdx.x; r < n1; r += kLU) A[(size_t)r * n1 + k] *= inv;
         __syncthreads();
         const int m = n1 - k - 1;
         const long long tot = (long long)m * m;
         for (long long t = threadIdx.x; t < tot; t += kLU) {
-            int rr = k + 1 + (int)(t / m), cc = k + 1 + (int)(t - (long long)(t / m) * m);
+            const int rr = k + 1 + (int)(t / m), cc = k + 1 + (int)(t - (long long)(t / m) * m);
             A[(size_t)rr * n1 + cc] -= A[(size_t)rr * n1 + k] * A[(size_t)k * n1 + cc];
         }
         __syncthreads();
     }
-    // x = LU^{-1} bs
-    for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] = d.bs[t];
-    lu_apply(A, d.perm, n1, d.x, d.r);
-    // one step of FP64 iterative refinement with the original matrix
-    for (int rr = threadIdx.x; rr < n1; rr += kLU) {
-        double s = d.bs[rr];
-        const double *row = d.A0 + (size_t)rr * n1;
-        for (int c = 0; c < n1; ++c) s -= row[c] * d.x[c];
-        d.r[rr] = s;
-    }
-    lu_apply(A, d.perm, n1, d.r, nullptr);
-    for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] += d.r[t];
+    return true;
+}
+
+// x = (P L U)^{-1} y with the FP32 factors; y (overwritten) and x in shared memory.
+// One barrier per column: forward elimination updates y below the column, backward
+// substitution writes x[c] and updates y above it.
+__device__ void lu_apply_f32(const float *__restrict__ LU, const int *__restrict__ perm, int n1, float *y, float *x) {
     __syncthreads();
-    // residual after refinement (inf-norm), for the report
-    double rmax = 0.0;
-    for (int rr = threadIdx.x; rr < n1; rr += kLU) {
-        double s = d.bs[rr];
-        const double *row = d.A0 + (size_t)rr * n1;
-        for (int c = 0; c < n1; ++c) s -= row[c] * d.x[c];
-        rmax = fmax(rmax, fabs(s));
-    }
-    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_down_sync(0xffffffffu, rmax, o));
-    if ((threadIdx.x & 31) == 0) sv[threadIdx.x >> 5] = rmax;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < n1; ++k) {
+            const int p = perm[k];
+            if (p != k) { const float t = y[k]; y[k] = y[p]; y[p] = t; }
+        }
     __syncthreads();
+    for (int c = 0; c < n1; ++c) {
+        const float yc = y[c];
+        for (int r = c + 1 + threadIdx.x; r < n1; r += kLU) y[r] -= LU[(size_t)r * n1 + c] * yc;
+        __syncthreads();
+    }
+    for (int c = n1 - 1; c >= 0; --c) {
+        const float xc = y[c] / LU[(size_t)c * n1 + c];
+        if (threadIdx.x == 0) x[c] = xc;
+        for (int r = threadIdx.x; r < c; r += kLU) y[r] -= LU[(size_t)r * n1 + c] * xc;
+        __syncthreads();
+    }
+}
+
+constexpr int kRefineMax = 30;
+
+__global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *__restrict__ descs) {
+    const SolveDesc d = descs[blockIdx.x];
+    const int n1 = d.n + 1;
+    extern __shared__ float fsh[];  // [2 * n1]: right-hand side / correction in FP32
+    float *ys = fsh, *xs = fsh + n1;
+    __shared__ double sv[kLU / 32];
+    __shared__ int si[kLU / 32];
+    __shared__ double piv_v;
+    __shared__ int piv_i;
+    double pmin = 1e308, pmax = 0.0, res = 0.0;
+    int singular = 0;
+    bool done = false;
+
+    // ---- FP32 LU + FP64-residual refinement
+    {
+        float *L = reinterpret_cast<float *>(d.As);  // the first half of the FP64 work matrix
+        for (long long t = threadIdx.x; t < (long long)n1 * n1; t += kLU) L[t] = (float)d.A0[t];
+        for (int t = threadIdx.x; t < n1; t += kLU) {
+            d.x[t] = 0.0;
+            d.r[t] = d.bs[t];
+        }
+        __syncthreads();
+        if (lu_factor_f32(L, d.perm, n1, sv, si, &piv_v, &piv_i, pmin, pmax)) {
+            double an = 0.0;  // |A| (max row sum)
+            for (int rr = threadIdx.x; rr < n1; rr += kLU) {
+                double s = 0.0;
+                for (int c = 0; c < n1; ++c) s += fabs(d.A0[(size_t)rr * n1 + c]);
+                an = fmax(an, s);
+            }
+            an = block_max(an, sv);
+            for (int it = 0; it < kRefineMax && !done; ++it) {
+                double rm = 0.0;
+                for (int t = threadIdx.x; t < n1; t += kLU) rm = fmax(rm, fabs(d.r[t]));
+                rm = block_max(rm, sv);
+                if (rm == 0.0) {
+                    done = true;
+                    break;
+                }
+                const double inv = 1.0 / rm;
+                for (int t = threadIdx.x; t < n1; t += kLU) ys[t] = (float)(d.r[t] * inv);
+                lu_apply_f32(L, d.perm, n1, ys, xs);
+                for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] += (double)xs[t] * rm;
+                __syncthreads();
+                double rn = 0.0, xn = 0.0;
+                for (int rr = threadIdx.x; rr < n1; rr += kLU) {
+                    double s = d.bs[rr];
+                    const double *row = d.A0 + (size_t)rr * n1;
+                    for (int c = 0; c < n1; ++c) s -= row[c] * d.x[c];
+                    d.r[rr] = s;
+                    rn = fmax(rn, fabs(s));
+                    xn = fmax(xn, fabs(d.x[rr]));
+                }
+                rn = block_max(rn, sv);
+                xn = block_max(xn, sv);
+                res = rn;
+                if (rn <= (double)n1 * 1.1102230246251565e-16 * an * xn) done = true;
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---- fallback: FP64 LU with one step of FP64 refinement
+    if (!done) {
+        double *A = d.As;
+        for (long long t = threadIdx.x; t < (long long)n1 * n1; t += kLU) A[t] = d.A0[t];
+        __syncthreads();
+        pmin = 1e308;
+        pmax = 0.0;
+        for (int k = 0; k < n1; ++k) {
+            double best = -1.0;
+            int bi = 0x7fffffff;
+            for (int r = k + threadIdx.x; r < n1; r += kLU) {
+                double v = fabs(A[(size_t)r * n1 + k]);
+                if (v > best || (v == best && r < bi)) { best = v; bi = r; }
+            }
+            block_argmax(best, bi, sv, si, &piv_v, &piv_i);
+            const int p = piv_i;
+            if (threadIdx.x == 0) d.perm[k] = p;
+            if (p != k)
+                for (int c = threadIdx.x; c < n1; c += kLU) {
+                    double t = A[(size_t)k * n1 + c];
+                    A[(size_t)k * n1 + c] = A[(size_t)p * n1 + c];
+                    A[(size_t)p * n1 + c] = t;
+                }
+            __syncthreads();
+            double pv = A[(size_t)k * n1 + k];
+            double apv = fabs(pv);
+            pmin = fmin(pmin, apv);
+            pmax = fmax(pmax, apv);
+            if (!(apv > 1e-300)) {  // exactly singular: keep going with a tiny pivot, flag it
+                singular = 1;
+                pv = (pv < 0 ? -1e-300 : 1e-300);
+                if (threadIdx.x == 0) A[(size_t)k * n1 + k] = pv;
+            }
+            __syncthreads();
+            const double inv = 1.0 / pv;
+            for (int r = k + 1 + threadIdx.x; r < n1; r += kLU) A[(size_t)r * n1 + k] *= inv;
+            __syncthreads();
+            const int m = n1 - k - 1;
+            const long long tot = (long long)m * m;
+            for (long long t = threadIdx.x; t < tot; t += kLU) {
+                int rr = k + 1 + (int)(t / m), cc = k + 1 + (int)(t - (long long)(t / m) * m);
+                A[(size_t)rr * n1 + cc] -= A[(size_t)rr * n1 + k] * A[(size_t)k * n1 + cc];
+            }
+            __syncthreads();
+        }
+        for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] = d.bs[t];
+        lu_apply(A, d.perm, n1, d.x, d.r);
+        for (int rr = threadIdx.x; rr < n1; rr += kLU) {
+            double s = d.bs[rr];
+            const double *row = d.A0 + (size_t)rr * n1;
+            for (int c = 0; c < n1; ++c) s -= row[c] * d.x[c];
+            d.r[rr] = s;
+        }
+        lu_apply(A, d.perm, n1, d.r, nullptr);
+        for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] += d.r[t];
+        __syncthreads();
+        double rmax = 0.0;
+        for (int rr = threadIdx.x; rr < n1; rr += kLU) {
+            double s = d.bs[rr];
+            const double *row = d.A0 + (size_t)rr * n1;
+            for (int c = 0; c < n1; ++c) s -= row[c] * d.x[c];
+            rmax = fmax(rmax, fabs(s));
+        }
+        res = block_max(rmax, sv);
+    }
     if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < kLU / 32; ++w) t = fmax(t, sv[w]);
-        d.info[0] = t;
+        d.info[0] = res;
         d.info[1] = pmin;
         d.info[2] = pmax;
         d.info[3] = singular;
     }
+    __syncthreads();
     // expand to all atoms
     for (int i = threadIdx.x; i < d.N; i += kLU) d.q[i] = d.x[d.map[i]];
 }
+
+size_t solve_smem_bytes(int n1) { return sizeof(float) * 2 * (size_t)n1; }
 
 }  // namespace
 
@@ -430,7 +567,9 @@ void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<dou
     RP_CUDA(cudaMemcpyAsync(d_desc, descs.data(), sizeof(SolveDesc) * nj, cudaMemcpyHostToDevice, stream));
     {
         StageTimer tt(ctx, "solve_lu", stream);
-        lu_solve_refine_kernel<<<nj, kLU, 0, stream>>>(d_desc);
+        int n1max = 1;
+        for (const FoldPlan &p : plans) n1max = std::max(n1max, p.n + 1);
+        lu_solve_refine_kernel<<<nj, kLU, solve_smem_bytes(n1max), stream>>>(d_desc);
         RP_LAUNCH_CHECK();
     }
     RP_CUDA(cudaMemcpyAsync(info.data(), d_info, sizeof(double) * 4 * nj, cudaMemcpyDeviceToHost, stream));
@@ -575,7 +714,7 @@ extern "C" int rp_solve_noalloc(const double *A_dev, const double *b_dev, int N,
             RP_CUDA(cudaMemcpyAsync(bs, hbs.data(), sizeof(double) * hbs.size(), cudaMemcpyHostToDevice, stream));
         }
         RP_CUDA(cudaMemcpyAsync(d_desc, &d, sizeof(SolveDesc), cudaMemcpyHostToDevice, stream));
-        lu_solve_refine_kernel<<<1, kLU, 0, stream>>>(d_desc);
+        lu_solve_refine_kernel<<<1, kLU, solve_smem_bytes(n1), stream>>>(d_desc);
         RP_LAUNCH_CHECK();
         double hinfo[4];
         RP_CUDA(cudaMemcpyAsync(hinfo, d_info, sizeof(hinfo), cudaMemcpyDeviceToHost, stream));
