@@ -219,7 +219,7 @@ void grid_tables_fp64(const rp_ewald *ew, const int32_t *d_kept, int64_t m0, int
 // Reciprocal sum by separable lattice phases (recip_sep.cu): E[r][col][n1] for every
 // grid row r = j + l*ny, col = atom (d_q == nullptr) or one charge-weighted column.
 size_t recip_rows_bytes(const rp_ewald *ew, int ncols);
-void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const double *d_q, int N, float4 *E,
+void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const double *d_q, int N, float2 *E,
                 cudaStream_t stream);
 
 // Shared epilogue kernels (phi_fp64.cu).

@@ -314,15 +314,21 @@ __global__ void __launch_bounds__(kCenterThreads) center_kernel(double *__restri
     }
 }
 
+// One warp: lane-strided partial sums, then a fixed shuffle tree (deterministic).
 __global__ void vstats_kernel(const double2 *__restrict__ part, int nb, double *__restrict__ vstats) {
-    if (threadIdx.x != 0) return;
     double t = 0.0, u = 0.0;
-    for (int b = 0; b < nb; ++b) {
+    for (int b = threadIdx.x; b < nb; b += 32) {
         t += part[b].x;
         u = fmax(u, part[b].y);
     }
-    vstats[0] = t;
-    vstats[1] = u;
+    for (int o = 16; o > 0; o >>= 1) {
+        t += __shfl_xor_sync(0xffffffffu, t, o);
+        u = fmax(u, __shfl_xor_sync(0xffffffffu, u, o));
+    }
+    if (threadIdx.x == 0) {
+        vstats[0] = t;
+        vstats[1] = u;
+    }
 }
 
 double radius_of(int z) {

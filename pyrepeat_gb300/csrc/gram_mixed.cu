@@ -5,13 +5,13 @@
 // (repeat.py:2246-2276).  Once per fit:
 //
 //  0. recip   E[r][a][n1] for every grid row r (separable reciprocal sum, stages A
-//             and B in recip_sep.cu, double-float on the FP32 pipe).
+//             and B in recip_sep.cu, on the FP32 pipe).
 //
 // Then per chunk of kept points (Phi exists for one chunk only):
 //
 //  1. Phi     Phi_t[a][m] = real-space erfc sum (FP32 terms from double-float
-//             coordinates, FP64 at the cutoff, FP64 per-pair sums)
-//             + Re sum_n1 ex[n1][i_m] E[r_m][a][n1] (double-float), written once,
+//             coordinates, FP64 at the cutoff, double-float per-pair sums)
+//             + Re sum_n1 ex[n1][i_m] E[r_m][a][n1] (FP32), written once,
 //             atom-major (phi_chunk_kernel).
 //  2. split   X[a][m] = (Phi_t[a][m] - c_a) * 2^e_a cut into four 7-bit fixed-point
 //             digits, plus a row for the centred ESP: c_a is the column mean of the
@@ -24,11 +24,11 @@
 //  4. finish  A = G - s s^T/M, b = G[:,V] - s sum(V)/M with s = sum_m (Phi - c)
 //             (FP64), i.e. repeat.py:2266-2276 for the shifted columns.
 //
-// Error budget: Phi carries the FP32 real-space terms (~1e-7 relative, unbiased)
-// and the 28-bit digit quantisation of the Gram input (~2^-29 of each row's
-// range, unbiased); the reciprocal sum is exact to ~2^-44.  The tensor cores'
-// FP32 accumulation truncates, which is why the Gram is done in exact integer
-// digits instead of as an FP16/BF16 hi+lo product.
+// Error budget: Phi carries the FP32 real-space terms and the FP32 reciprocal
+// stages B and C (~1e-7 relative each, unbiased rounding) and the 28-bit digit
+// quantisation of the Gram input (~2^-29 of each row's range, unbiased).  The
+// tensor cores' FP32 accumulation truncates, which is why the Gram is done in
+// exact integer digits instead of as an FP16/BF16 hi+lo product.
 #include <cuda.h>
 #include <cuda_fp16.h>
 
@@ -315,10 +315,10 @@ __device__ __forceinline__ float2 df_sub(float ah, float al, float bh, float bl)
 // those within Rc + 1e-3 Bohr of the bounding box of its points, in shift order
 // (warp-ballot compaction, so the summation order is fixed).  Distances are formed
 // in FP32 from double-float coordinates relative to the CTA's first point; images
-// within 1e-5 of Rc (where the reference's FP64 cutoff decision is made) and
-// pairs closer than sqrt(near2) are evaluated in FP64 with the reference's
-// expressions, the rest with FP32 erfcf.  Reciprocal part: stage C of the
-// separable sum in double-float.  `parts`: bit 0 real space, bit 1 reciprocal.
+// within 2e-6 of Rc are decided in FP64 with the reference's expressions (the term
+// is the FP32 one), pairs closer than sqrt(near2) are evaluated entirely in FP64,
+// the rest with FP32 erfcf.  Reciprocal part: stage C of the
+// separable sum in FP32.  `parts`: bit 0 real space, bit 1 reciprocal.
 // With psum/pmax given, the CTA also writes each atom's sum and max |Phi| over its
 // points (fixed-order reductions), the column statistics of the centring step.
 // The grid step vectors as double-float (a[d] = h[d] + l[d]), passed by value.
@@ -337,13 +337,14 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
     const int32_t *__restrict__ kept, long long m0, long long rows, const double *__restrict__ axis, AxisDF adf,
     int nx, int ny,
     const double *__restrict__ atoms, int N, const double *__restrict__ shifts, int S, int scap, int zero_idx,
-    double rc, double sa, float near2, const float4 *__restrict__ img, const float4 *__restrict__ EX,
-    const float4 *__restrict__ E, int n1c, int parts, float2 *__restrict__ phit, long long ld,
+    double rc, double sa, float rcf, float saf_in, float near2, const float4 *__restrict__ img,
+    const float4 *__restrict__ EX,
+    const float2 *__restrict__ E, int n1c, int parts, float2 *__restrict__ phit, long long ld,
     double *__restrict__ psum, float *__restrict__ pmax) {
     extern __shared__ float4 dsm[];
-    float4 *exs = dsm;                                    // [n1c][kPhiPts]   this thread's ex[n1][i]
-    float4 *img_hi = exs + (size_t)n1c * kPhiPts;         // [kPhiAtoms][scap] (x, y, z, shift index)
+    float4 *img_hi = dsm;                                 // [kPhiAtoms][scap] (x, y, z, shift index)
     float4 *img_lo = img_hi + (size_t)kPhiAtoms * scap;   // [kPhiAtoms][scap]
+    float2 *exs = reinterpret_cast<float2 *>(img_lo + (size_t)kPhiAtoms * scap);  // [n1c][kPhiPts] ex[n1][i]
     __shared__ int ncand[kPhiAtoms];
     __shared__ float bb[2][3][kPhiPts / 32];
     __shared__ float2 wsum[kPhiPts / 32][kPhiAtoms];
@@ -407,7 +408,10 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
         }
     }
     if (parts & 2)
-        for (int n = 0; n < n1c; ++n) exs[n * kPhiPts + threadIdx.x] = EX[(long long)n * nx + i];
+        for (int n = 0; n < n1c; ++n) {
+            const float4 x = EX[(long long)n * nx + i];
+            exs[n * kPhiPts + threadIdx.x] = make_float2(x.x, x.z);
+        }
     __syncthreads();
 
     if (parts & 1) {
@@ -421,7 +425,7 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
                 bmax[d] = fmaxf(bmax[d], bb[1][d][w]);
             }
         }
-        const float reach = (float)rc + 1e-3f, reach2 = reach * reach;
+        const float reach = rcf + 1e-3f, reach2 = reach * reach;
         for (int a = warp; a < kPhiAtoms; a += kPhiPts / 32) {
             int base = 0;
             if (a < na) {
@@ -455,11 +459,13 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
     }
     __syncthreads();
 
-    // FP64 decides every image whose FP32 squared distance lies within +-2e-5 Rc^2 of the
-    // cutoff: with coordinates exact to ~2^-48, |r2_fp32 - r2| stays below ~8 ulp(r2) (5e-7
-    // relative), so the band covers the FP32 error 40-fold while keeping the FP64 path rare
-    // (a wider band makes whole warps take it and the FP64 pipe becomes the bottleneck).
-    const float rcc = (float)(rc * rc), band = 2e-5f * rcc, saf = (float)sa;
+    // FP64 decides every image whose FP32 squared distance lies within +-4e-6 Rc^2 of the
+    // cutoff: with coordinates exact to ~2^-48, dx carries <= 2^-23 relative error and
+    // r2 <= 2^-21 (4.8e-7), so the band covers the FP32 error 8-fold.  Only the decision
+    // r <= Rc is made in FP64 (the reference's expressions); the term itself, ~erfc(pi)/Rc
+    // there, is the FP32 one.  FP64 runs at 1/64 of the FP32 rate per lane on this part,
+    // and one lane in the band makes its whole warp run the FP64 code, so it stays short.
+    const float rcc = rcf * rcf, band = 4e-6f * rcc, saf = saf_in;
     const float fp64_below = fmaxf(near2, 1e-6f);
     const long long row = f / nx;  // j + l * ny
     for (int a = 0; a < na; ++a) {
@@ -467,17 +473,26 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
         double acc64 = 0.0;
         bool used64 = false;
         if (valid && (parts & 2)) {
-            const float4 *e = E + (row * N + a0 + a) * n1c;
-            for (int n = 0; n < n1c; ++n) dfa::cmac_re(v, exs[n * kPhiPts + threadIdx.x], e[n]);
+            const float2 *e = E + (row * N + a0 + a) * n1c;
+            float rs = 0.f;
+            for (int n = 0; n < n1c; ++n) {
+                const float2 x = exs[n * kPhiPts + threadIdx.x], y = e[n];
+                rs = fmaf(x.x, y.x, rs);
+                rs = fmaf(-x.y, y.y, rs);
+            }
+            v.s = rs;
         }
         if (valid && (parts & 1)) {
             const float4 *ih = img_hi + a * scap, *il = img_lo + a * scap;
             const int nc = ncand[a];
             float acc32 = 0.f;
+            const float rej = rcc * 1.0001f + 1e-3f;  // hi parts alone decide clear misses
             for (int c = 0; c < nc; ++c) {
-                const float4 h = ih[c], lo = il[c];
-                const float dx = (gh[0] - h.x) + (gl[0] - lo.x), dy = (gh[1] - h.y) + (gl[1] - lo.y),
-                            dz = (gh[2] - h.z) + (gl[2] - lo.z);
+                const float4 h = ih[c];
+                const float hx = gh[0] - h.x, hy = gh[1] - h.y, hz = gh[2] - h.z;
+                if (hx * hx + hy * hy + hz * hz > rej) continue;
+                const float4 lo = il[c];
+                const float dx = hx + (gl[0] - lo.x), dy = hy + (gl[1] - lo.y), dz = hz + (gl[2] - lo.z);
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 > rcc + band) continue;
                 if (r2 < fp64_below || r2 > rcc - band) {
@@ -489,14 +504,15 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
                     const double ex = gabs[0] - (p[0] + shifts[3 * s]), ey = gabs[1] - (p[1] + shifts[3 * s + 1]),
                                  ez = gabs[2] - (p[2] + shifts[3 * s + 2]);
                     const double r = sqrt(ex * ex + ey * ey + ez * ez);
-                    if (r <= rc && (s != zero_idx || r > 1e-10)) {
+                    if (!(r <= rc) || (s == zero_idx && !(r > 1e-10))) continue;
+                    if (r2 < fp64_below) {  // a point on top of an image: the large term in FP64
                         acc64 += erfc(sa * r) / r;
                         used64 = true;
+                        continue;
                     }
-                } else {
-                    const float rinv = rsqrtf(r2);
-                    acc32 += erfcf(saf * (r2 * rinv)) * rinv;
                 }
+                const float rinv = rsqrtf(r2);
+                acc32 += erfcf(saf * (r2 * rinv)) * rinv;
             }
             float s_, e_;
             dfa::two_sum(v.s, acc32, s_, e_);
@@ -544,12 +560,12 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
 }
 
 size_t phi_smem_bytes(int n1c, int scap) {
-    return sizeof(float4) * ((size_t)n1c * kPhiPts + 2 * (size_t)kPhiAtoms * scap);
+    return sizeof(float4) * 2 * (size_t)kPhiAtoms * scap + sizeof(float2) * (size_t)n1c * kPhiPts;
 }
 
 void launch_phi(const int32_t *kept, long long m0, long long rows, const double *d_axis, const double *h_axis, int nx, int ny,
                 const double *d_atoms, int N, const double *d_shifts, int S, int zero_idx, double rc, double sa,
-                const float4 *img, const float4 *EX, const float4 *E, int n1c, int parts, float2 *phit, long long ld,
+                const float4 *img, const float4 *EX, const float2 *E, int n1c, int parts, float2 *phit, long long ld,
                 double *psum, float *pmax, cudaStream_t s) {
     RP_REQUIRE(S >= 1 && S <= kMaxShifts, "more than 128 real-space shifts after pruning (cutoff too large for the cell)");
     const int scap = (S + 31) / 32 * 32;
@@ -567,7 +583,8 @@ void launch_phi(const int32_t *kept, long long m0, long long rows, const double 
     }
     dim3 grd(ceil_div(rows, kPhiPts), ceil_div(N, kPhiAtoms));
     phi_chunk_kernel<<<grd, kPhiPts, smem, s>>>(kept, m0, rows, d_axis, adf, nx, ny, d_atoms, N, d_shifts, S, scap, zero_idx,
-                                                rc, sa, real_near2(), img, EX, E, n1c, parts, phit, ld, psum, pmax);
+                                                rc, sa, (float)rc, (float)sa, real_near2(), img, EX, E, n1c, parts,
+                                                phit, ld, psum, pmax);
     RP_LAUNCH_CHECK();
 }
 
@@ -800,7 +817,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     int *d_status = ctx->d_status;  // cleared by the caller (rp_gram / the batch driver)
 
     // reciprocal rows of every atom (stages A and B) and the double-float images, once per fit
-    float4 *E = ctx->buf_t<float4>("m_E", recip_rows_bytes(ew, N) / sizeof(float4));
+    float2 *E = ctx->buf_t<float2>("m_E", recip_rows_bytes(ew, N) / sizeof(float2));
     float4 *img = ctx->buf_t<float4>("m_img", 2 * (size_t)N * S);
     {
         StageTimer tt(ctx, "recip_rows", stream);
@@ -916,7 +933,7 @@ extern "C" int rp_debug_mixed_phi(rp_ctx *ctx, const rp_ewald *ew, const double 
         RP_CUDA(cudaMemcpy(d_atoms, atoms, sizeof(double) * 3 * N, cudaMemcpyHostToDevice));
         RP_CUDA(cudaMemcpy(d_shifts, sh.data(), sizeof(double) * sh.size(), cudaMemcpyHostToDevice));
         RP_CUDA(cudaMemcpy(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice));
-        float4 *E = ctx->buf_t<float4>("m_E", recip_rows_bytes(ew, N) / sizeof(float4));
+        float2 *E = ctx->buf_t<float2>("m_E", recip_rows_bytes(ew, N) / sizeof(float2));
         float4 *img = ctx->buf_t<float4>("m_img", 2 * (size_t)N * S);
         recip_rows(ctx, ew, d_atoms, nullptr, N, E, 0);
         images_df_kernel<<<ceil_div((long long)N * S, 128), 128>>>(d_atoms, N, d_shifts, S, img);

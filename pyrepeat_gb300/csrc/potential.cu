@@ -8,9 +8,9 @@
 //   real space  V_s(g) = sum_a q_a sum_s [|g-r_a-s| <= Rc] erfc(sqrt(alpha) r)/r
 //               over a per-CTA candidate list of images near the CTA's points.
 // Cost per point is O(KMAX + images within Rc) instead of O(N K).  The real-space
-// terms are FP32 with FP64 accumulation (relative error ~1e-7), which is what an
-// RMS of the fitted ESP or a synthetic ESP needs; the reciprocal part is
-// double-float.
+// terms are FP32 with double-float accumulation and the reciprocal part FP32
+// (relative error ~1e-7), which is what an RMS of the fitted ESP or a synthetic
+// ESP needs.
 #include <algorithm>
 #include <cmath>
 
@@ -25,16 +25,19 @@ constexpr int kPotCand = 4096;  // images per candidate batch in shared memory
 
 // one thread per point: V_r = Re sum_n1 ex[n1][i] E_q[r][n1]
 __global__ void __launch_bounds__(kPotPts) potential_recip_kernel(const float4 *__restrict__ EX,
-                                                                  const float4 *__restrict__ Eq, int n1c, int nx,
+                                                                  const float2 *__restrict__ Eq, int n1c, int nx,
                                                                   const int32_t *__restrict__ idx, long long npts,
                                                                   double *__restrict__ out) {
     const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= npts) return;
     const int f = idx ? idx[m] : (int)m;
     const int row = f / nx, i = f - row * nx;
-    dfa::acc rs{0.f, 0.f};
-    for (int n = 0; n < n1c; ++n) dfa::cmac_re(rs, EX[(long long)n * nx + i], Eq[(long long)row * n1c + n]);
-    out[m] = dfa::to_double(rs);
+    float rs = 0.f;
+    for (int n = 0; n < n1c; ++n) {
+        const float2 e = Eq[(long long)row * n1c + n];
+        rs = dfa::cre32(rs, EX[(long long)n * nx + i], make_float4(e.x, 0.f, e.y, 0.f));
+    }
+    out[m] = (double)rs;
 }
 
 __global__ void __launch_bounds__(kPotPts) potential_real_kernel(
@@ -64,8 +67,8 @@ __global__ void __launch_bounds__(kPotPts) potential_real_kernel(
     if (valid) atomicMax(reinterpret_cast<int *>(&tile_r), __float_as_int(sqrtf(gl.x * gl.x + gl.y * gl.y + gl.z * gl.z)));
     __syncthreads();
     const float reach = (float)rc + tile_r + 1e-3f;
-    const float reach2 = reach * reach, rc2 = (float)(rc * rc);
-    double acc = 0.0;
+    const float reach2 = reach * reach, rc2 = (float)(rc * rc), saf = (float)sa;
+    dfa::acc acc{0.f, 0.f};  // double-float sum of FP32 terms (no FP64 per pair)
     const int total = N * S;
     for (int base = 0; base < total; base += kPotCand) {
         if (threadIdx.x == 0) ncand = 0;
@@ -88,12 +91,15 @@ __global__ void __launch_bounds__(kPotPts) potential_real_kernel(
                 const float dx = gl.x - p.x, dy = gl.y - p.y, dz = gl.z - p.z;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 > rc2 || r2 <= 1e-20f) continue;
-                const float r = sqrtf(r2);
-                acc += (double)(p.w * (erfcf((float)sa * r) / r));
+                const float rinv = rsqrtf(r2);
+                float t, e;
+                dfa::two_sum(acc.s, p.w * (erfcf(saf * (r2 * rinv)) * rinv), t, e);
+                acc.s = t;
+                acc.e = __fadd_rn(acc.e, e);
             }
         __syncthreads();
     }
-    if (valid) out[m] += acc;
+    if (valid) out[m] += dfa::to_double(acc);
 }
 
 }  // namespace
@@ -115,7 +121,7 @@ void potential_run(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const d
     RP_CUDA(cudaMemcpyAsync(d_shifts, sh.data(), sizeof(double) * sh.size(), cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice, stream));
     const int nx = ew->grid.n_grid[0], ny = ew->grid.n_grid[1];
-    float4 *Eq = ctx->buf_t<float4>("p_Eq", recip_rows_bytes(ew, 1) / sizeof(float4));
+    float2 *Eq = ctx->buf_t<float2>("p_Eq", recip_rows_bytes(ew, 1) / sizeof(float2));
     recip_rows(ctx, ew, d_atoms, d_q, N, Eq, stream);
     potential_recip_kernel<<<ceil_div(npts, kPotPts), kPotPts, 0, stream>>>(ew->d_exf, Eq, ew->kmax, nx, idx_dev, npts,
                                                                            out_dev);

@@ -15,8 +15,10 @@
 //                                                                        the real-space kernel)
 // Stage C costs 2 KMAX real multiply-adds per point-atom instead of the 4 K of a dense
 // point x k table contraction (K = 754 at KMAX 7): ~50x fewer operations, so the
-// whole sum runs on the FP32 pipe in double-float arithmetic (about 44 bits,
-// more than the fit needs) instead of as a low-precision tensor-core GEMM.
+// whole sum runs on the FP32 pipe instead of as a tensor-core GEMM.  The weights W
+// and stage A are double-float (exact to ~2^-44); stages B and C use FP32 products
+// (unbiased rounding, ~1e-7 relative like the FP32 real-space terms), stored as
+// float2 E rows.
 // Indices n1 in [0, P], n2, n3 in [-P, P] with P = KMAX - 1 (the k-set keeps
 // n1^2 + n2^2 + n3^2 < KMAX^2); stored with offset P on n2 and n3.
 #include <algorithm>
@@ -83,17 +85,19 @@ __global__ void build_w_kernel(const int *__restrict__ kidx, const double *__res
 // loaded once per term.
 constexpr int kN1B = 8;
 
+// Stage A, one thread per (n2, column, n1 block, plane l) with l fastest: a warp reads
+// one W row (broadcast) and consecutive ez phases (coalesced).
 __global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 *__restrict__ EZ, int ncols, int P,
                                      int nz, float4 *__restrict__ F) {
     const int n1c = P + 1, nw = 2 * P + 1, nb = (n1c + kN1B - 1) / kN1B;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nz * nw * ncols * nb) return;
+    const int l = (int)(t % nz);
+    t /= nz;
     const int b = (int)(t % nb);
     t /= nb;
     const int a = (int)(t % ncols);
-    t /= ncols;
-    const int n2 = (int)(t % nw);
-    const int l = (int)(t / nw);
+    const int n2 = (int)(t / ncols);
     const int n10 = b * kN1B, cnt = min(kN1B, n1c - n10);
     dfa::acc re[kN1B], im[kN1B];
 #pragma unroll
@@ -116,7 +120,7 @@ __global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 
 // columns is staged in shared memory once and reused by every row j of the plane.
 __global__ void __launch_bounds__(128) recip_stage_b_kernel(const float4 *__restrict__ F,
                                                             const float4 *__restrict__ EY, int ncols, int P, int ny,
-                                                            int ab, float4 *__restrict__ E) {
+                                                            int ab, float2 *__restrict__ E) {
     extern __shared__ float4 fs[];  // [nw][ab][n1c]
     const int n1c = P + 1, nw = 2 * P + 1;
     const int l = blockIdx.y, a0 = blockIdx.x * ab, na = min(ab, ncols - a0);
@@ -129,22 +133,22 @@ __global__ void __launch_bounds__(128) recip_stage_b_kernel(const float4 *__rest
     const int items = na * ny;  // (a, j), j fastest: a warp reads one column's slab (broadcast)
     for (int it = threadIdx.x; it < items; it += blockDim.x) {
         const int a = it / ny, j = it - a * ny;
-        float4 *o = E + (((long long)l * ny + j) * ncols + a0 + a) * n1c;
+        float2 *o = E + (((long long)l * ny + j) * ncols + a0 + a) * n1c;
         for (int n10 = 0; n10 < n1c; n10 += kN1B) {
             const int cnt = min(kN1B, n1c - n10);
-            dfa::acc re[kN1B], im[kN1B];
+            float re[kN1B], im[kN1B];
 #pragma unroll
-            for (int u = 0; u < kN1B; ++u) re[u] = im[u] = dfa::acc{0.f, 0.f};
+            for (int u = 0; u < kN1B; ++u) re[u] = im[u] = 0.f;
             for (int n2 = 0; n2 < nw; ++n2) {
                 const float4 y = EY[(long long)n2 * ny + j];
                 const float4 *fr = fs + ((size_t)n2 * ab + a) * n1c + n10;
 #pragma unroll
                 for (int u = 0; u < kN1B; ++u)
-                    if (u < cnt) dfa::cmac(re[u], im[u], y, fr[u]);
+                    if (u < cnt) dfa::cmac32(re[u], im[u], y, fr[u]);
             }
 #pragma unroll
             for (int u = 0; u < kN1B; ++u)
-                if (u < cnt) o[n10 + u] = dfa::pack(re[u], im[u]);
+                if (u < cnt) o[n10 + u] = make_float2(re[u], im[u]);
         }
     }
 }
@@ -154,10 +158,10 @@ __global__ void __launch_bounds__(128) recip_stage_b_kernel(const float4 *__rest
 size_t recip_rows_bytes(const rp_ewald *ew, int ncols) {
     const int P = ew->kmax - 1, n1c = P + 1;
     const long long nrows = (long long)ew->grid.n_grid[1] * ew->grid.n_grid[2];
-    return sizeof(float4) * (size_t)nrows * ncols * n1c;
+    return sizeof(float2) * (size_t)nrows * ncols * n1c;
 }
 
-void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const double *d_q, int N, float4 *E,
+void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const double *d_q, int N, float2 *E,
                 cudaStream_t stream) {
     const int P = ew->kmax - 1, n1c = P + 1, nw = 2 * P + 1;
     const int ny = ew->grid.n_grid[1], nz = ew->grid.n_grid[2];

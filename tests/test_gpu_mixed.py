@@ -42,7 +42,8 @@ def test_mixed_normal_equations_close_to_fp64(name, gpu_ctx):
 @pytest.mark.parametrize("name", ["water24", "tricmini"])
 def test_mixed_phi_parts_match_oracle(name, gpu_ctx, oracle_mod):
     """Each part of the mixed Phi against the oracle's FP64 Phi on the same kept points.
-    Real space: FP32 terms, so 1e-6 of max|Phi|; reciprocal: double-float, 1e-10."""
+    Both parts carry FP32 rounding (the real-space terms, reciprocal stages B and C),
+    so the bound is 1e-6 of max|Phi| (measured 2-4e-7)."""
     import torch
     L = gpu_ctx.lib
     L.rp_debug_mixed_phi.restype = ctypes.c_int
@@ -57,7 +58,7 @@ def test_mixed_phi_parts_match_oracle(name, gpu_ctx, oracle_mod):
     real_ref = oracle_mod.phi(of.grid, atoms, of.kv[:0], of.kc[:0], of.shifts, of.zero_idx, cube.cutoff)
     rec_ref = oracle_mod.phi(of.grid, atoms, of.kv, of.kc, of.shifts[:0], -1, cube.cutoff)
     N = len(atoms)
-    for parts, ref, tol in ((1, real_ref, 1e-6), (2, rec_ref, 1e-10), (3, real_ref + rec_ref, 1e-6)):
+    for parts, ref, tol in ((1, real_ref, 1e-6), (2, rec_ref, 1e-6), (3, real_ref + rec_ref, 1e-6)):
         out = torch.zeros((N, M), dtype=torch.float64, device="cuda")
         gpu_ctx.check(L.rp_debug_mixed_phi(gpu_ctx.ptr, ew.ptr, atoms.ctypes.data, N, kept.data_ptr(), M, parts,
                                            out.data_ptr()))
