@@ -193,7 +193,8 @@ void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const i
 void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
                cudaStream_t stream);
-// vstats_dev: the filter's (sum, max |.|) of Vc, or nullptr to compute them here.
+// vstats_dev: the filter's (sum, max |.|) of Vc (only the max is used), or nullptr to
+// compute the max here.
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
                 cudaStream_t stream, const double *vstats_dev = nullptr);

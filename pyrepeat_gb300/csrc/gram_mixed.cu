@@ -283,6 +283,26 @@ float real_near2() {
 
 // ------------------------------------------------------------------ Phi of one chunk
 
+// erfc(x), x >= 0, in FP32 by the Chebyshev fit "erfcc" of Press, Teukolsky, Vetterling
+// and Flannery, Numerical Recipes in C (2nd ed., section 6.2): erfc(x) = t exp(-x^2 + P(t)),
+// t = 1/(1 + x/2), fractional error below 1.2e-7.  Evaluated with the fast reciprocal and
+// exponential it is ~15 instructions and, for the real-space range x = sqrt(alpha) r <= pi,
+// within 5e-7 (x < 1.5) and 1.3e-6 (x near pi, terms ~1e-6 of the largest) of FP64 erfc.
+__device__ __forceinline__ float erfc_nr(float x) {
+    const float t = __fdividef(1.0f, fmaf(0.5f, x, 1.0f));
+    float p = 0.17087277f;
+    p = fmaf(t, p, -0.82215223f);
+    p = fmaf(t, p, 1.48851587f);
+    p = fmaf(t, p, -1.13520398f);
+    p = fmaf(t, p, 0.27886807f);
+    p = fmaf(t, p, -0.18628806f);
+    p = fmaf(t, p, 0.09678418f);
+    p = fmaf(t, p, 0.37409196f);
+    p = fmaf(t, p, 1.00002368f);
+    p = fmaf(t, p, -1.26551223f);
+    return t * __expf(fmaf(-x, x, p));
+}
+
 constexpr int kPhiPts = 128;     // points per CTA (one per thread)
 constexpr int kPhiAtoms = 16;    // atoms per CTA
 constexpr int kMaxShifts = 128;  // pruned real-space shifts (checked on the host)
@@ -347,7 +367,7 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
     float2 *exs = reinterpret_cast<float2 *>(img_lo + (size_t)kPhiAtoms * scap);  // [n1c][kPhiPts] ex[n1][i]
     __shared__ int ncand[kPhiAtoms];
     __shared__ float bb[2][3][kPhiPts / 32];
-    __shared__ float2 wsum[kPhiPts / 32][kPhiAtoms];
+    __shared__ float wsum[kPhiPts / 32][kPhiAtoms];
     __shared__ float wmax[kPhiPts / 32][kPhiAtoms];
     const long long mb = (long long)blockIdx.x * kPhiPts;
     const int a0 = blockIdx.y * kPhiAtoms;
@@ -470,8 +490,7 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
     const long long row = f / nx;  // j + l * ny
     for (int a = 0; a < na; ++a) {
         dfa::acc v{0.f, 0.f};
-        double acc64 = 0.0;
-        bool used64 = false;
+        float x64h = 0.f, x64l = 0.f;  // rare FP64 terms, folded in as double-float pairs
         if (valid && (parts & 2)) {
             const float2 *e = E + (row * N + a0 + a) * n1c;
             float rs = 0.f;
@@ -506,39 +525,37 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
                     const double r = sqrt(ex * ex + ey * ey + ez * ez);
                     if (!(r <= rc) || (s == zero_idx && !(r > 1e-10))) continue;
                     if (r2 < fp64_below) {  // a point on top of an image: the large term in FP64
-                        acc64 += erfc(sa * r) / r;
-                        used64 = true;
+                        const double t = erfc(sa * r) / r;
+                        const float th = (float)t, tl = (float)(t - (double)th);
+                        float s2, e2;
+                        dfa::two_sum(x64h, th, s2, e2);
+                        x64h = s2;
+                        x64l = __fadd_rn(x64l, __fadd_rn(e2, tl));
                         continue;
                     }
                 }
                 const float rinv = rsqrtf(r2);
-                acc32 += erfcf(saf * (r2 * rinv)) * rinv;
+                acc32 = fmaf(erfc_nr(saf * (r2 * rinv)), rinv, acc32);
             }
             float s_, e_;
             dfa::two_sum(v.s, acc32, s_, e_);
             v.s = s_;
             v.e = __fadd_rn(v.e, e_);
+            dfa::two_sum(v.s, x64h, s_, e_);
+            v.s = s_;
+            v.e = __fadd_rn(v.e, __fadd_rn(e_, x64l));
         }
-        float2 out = dfa::norm(v);
-        if (used64) {  // rare: fold the FP64 terms in FP64
-            const double t = ((double)out.x + (double)out.y) + acc64;
-            out.x = (float)t;
-            out.y = (float)(t - (double)out.x);
-        }
+        const float2 out = dfa::norm(v);
         if (valid) phit[(long long)(a0 + a) * ld + m] = out;
-        if (psum) {  // column statistics over the CTA's points (invalid lanes add zero)
-            float sh = valid ? out.x : 0.f, sl = valid ? out.y : 0.f;
-            float mx = valid ? fabsf(out.x) : 0.f;
+        if (psum) {  // column statistics for the centre and the scale: FP32 is enough (any
+                     // centre is corrected exactly; the max is exact)
+            float sh = valid ? out.x : 0.f, mx = valid ? fabsf(out.x) : 0.f;
             for (int o = 16; o > 0; o >>= 1) {
-                const float oh2 = __shfl_xor_sync(0xffffffffu, sh, o), ol2 = __shfl_xor_sync(0xffffffffu, sl, o);
-                float s2, e2;
-                dfa::two_sum(sh, oh2, s2, e2);
-                sh = s2;
-                sl = __fadd_rn(__fadd_rn(sl, ol2), e2);
+                sh += __shfl_xor_sync(0xffffffffu, sh, o);
                 mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
             }
             if (lane == 0) {
-                wsum[warp][a] = make_float2(sh, sl);
+                wsum[warp][a] = sh;
                 wmax[warp][a] = mx;
             }
         }
@@ -550,7 +567,7 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
             double s = 0.0;
             float mx = 0.f;
             for (int w = 0; w < kPhiPts / 32; ++w) {
-                s += (double)wsum[w][a].x + (double)wsum[w][a].y;
+                s += (double)wsum[w][a];
                 mx = fmaxf(mx, wmax[w][a]);
             }
             psum[(size_t)(a0 + a) * gridDim.x + blockIdx.x] = s;
@@ -570,11 +587,14 @@ void launch_phi(const int32_t *kept, long long m0, long long rows, const double 
     RP_REQUIRE(S >= 1 && S <= kMaxShifts, "more than 128 real-space shifts after pruning (cutoff too large for the cell)");
     const int scap = (S + 31) / 32 * 32;
     const size_t smem = phi_smem_bytes(n1c, scap);
+    // the static shared memory (the statistics tile, ~18 KB) counts against the same 48 KB
+    // default, so the opt-in is raised whenever the dynamic part could cross it
     static size_t attr = 0;
-    if (smem > 48 * 1024 && smem > attr) {
-        RP_REQUIRE(smem <= 200 * 1024, "phi kernel: KMAX too large for shared memory");
-        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = smem;
+    if (smem > attr) {
+        RP_REQUIRE(smem <= 192 * 1024, "phi kernel: KMAX too large for shared memory");
+        const size_t want = std::max<size_t>(smem, 96 * 1024);
+        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
+        attr = want;
     }
     AxisDF adf;
     for (int q = 0; q < 9; ++q) {
@@ -590,12 +610,13 @@ void launch_phi(const int32_t *kept, long long m0, long long rows, const double 
 
 // ------------------------------------------------------------------ column statistics and the split
 
-// Per atom (one warp each): the chunk's sum (into sphi) from the phi kernel's per-CTA
-// partials in a fixed order, and on the first chunk the centre c (a double-float; cvec
-// holds its exact FP64 value) and the power-of-two scale.
+// Per atom (one warp each), on the first chunk: the centre c (the chunk mean, as a
+// double-float; cvec holds its exact FP64 value) and the power-of-two scale, from the
+// phi kernel's per-CTA partial sums and maxima.  Any centre works: the mean correction
+// uses the exact sums of the fixed-point rows (slice_rows_kernel).
 __global__ void colstats_finish_kernel(const double *__restrict__ psum, const float *__restrict__ pmax, int nblk,
-                                       int N, long long rows, int first, double *__restrict__ sphi,
-                                       double *__restrict__ c, float2 *__restrict__ cdf, float *__restrict__ scale) {
+                                       int N, long long rows, double *__restrict__ c, float2 *__restrict__ cdf,
+                                       float *__restrict__ scale) {
     const int a = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (a >= N) return;  // whole warp
     double s = 0.0;
@@ -609,19 +630,16 @@ __global__ void colstats_finish_kernel(const double *__restrict__ psum, const fl
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     }
     if (lane != 0) return;
-    sphi[a] = first ? s : sphi[a] + s;
-    if (first) {
-        const double mean = s / (double)rows;
-        const float ch = (float)mean, cl = (float)(mean - (double)ch);
-        cdf[a] = make_float2(ch, cl);
-        c[a] = (double)ch + (double)cl;  // the shift actually applied, exactly
-        // |Phi - c| <= 2 max|Phi| =: bound in [2^(e-1), 2^e); scale 2^(-e-1) puts |x| below 1/2,
-        // so the fixed-point slices stay within |x_s| <= 64 even if a later chunk doubles the range
-        float bound = 2.f * mx;
-        int e = 0;
-        if (bound > 0.f) frexpf(bound, &e);
-        scale[a] = ldexpf(1.f, -e - 1);
-    }
+    const double mean = s / (double)rows;
+    const float ch = (float)mean, cl = (float)(mean - (double)ch);
+    cdf[a] = make_float2(ch, cl);
+    c[a] = (double)ch + (double)cl;  // the shift actually applied, exactly
+    // |Phi - c| <= 2 max|Phi| =: bound in [2^(e-1), 2^e); scale 2^(-e-1) puts |x| below 1/2,
+    // so the fixed-point slices stay within |x_s| <= 64 even if a later chunk doubles the range
+    float bound = 2.f * mx;
+    int e = 0;
+    if (bound > 0.f) frexpf(bound, &e);
+    scale[a] = ldexpf(1.f, -e - 1);
 }
 
 // I = round(x 2^27) of one element of X (x = (Phi - c) scale, or the scaled ESP), |x| <= 1
@@ -634,20 +652,32 @@ __device__ __forceinline__ int x_fixed(float h, float l, float sc, int *clamped)
     return round_df(h, l, sc);
 }
 
+constexpr int kSliceThreads = 256;
+
 // X rows: a < N: (Phi_t[a][m] - c_a) * scale_a;  a == N: Vc[m] * scale_V;  rest zero.
 // Each value x (|x| <= 1) becomes I = round(x 2^27) and four 7-bit digits
 // x ~ 2^-6 (x0 + 2^-7 x1 + 2^-14 x2 + 2^-21 x3), x_s integers in [-64, 64], exact in FP16.
 // One thread per two consecutive points of one row (16-B loads, 4-B stores).
-__global__ void slice_rows_kernel(const float2 *__restrict__ phit, long long ld, long long rows, long long rows_pad,
+__global__ void __launch_bounds__(kSliceThreads) slice_rows_kernel(const float2 *__restrict__ phit, long long ld, long long rows, long long rows_pad,
                                   int N, const float2 *__restrict__ cdf, const float *__restrict__ scale,
                                   const double *__restrict__ Vc, long long m0, const double *__restrict__ vmax_p,
                                   __half *__restrict__ X0, __half *__restrict__ X1, __half *__restrict__ X2,
-                                  __half *__restrict__ X3, int *__restrict__ clamped) {
-    const int a = blockIdx.y;
+                                  __half *__restrict__ X3, int *__restrict__ clamped,
+                                  unsigned long long *__restrict__ rowsum) {
+    const int a = blockIdx.y;  // uniform per CTA: the ESP row and the padding rows branch as a whole
     const long long m = 2 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
-    if (m >= rows_pad) return;
     int I[2] = {0, 0};
-    if (a < N) {
+    if (m >= rows_pad) {
+        // lanes past the row end only join the shuffle
+    } else if (a == N) {
+        const float sc = vscale_of(*vmax_p);
+        for (int u = 0; u < 2; ++u)
+            if (m + u < rows) {
+                const double v = Vc[m0 + m + u];
+                const float h = (float)v;
+                I[u] = x_fixed(h, (float)(v - (double)h), sc, clamped);
+            }
+    } else if (a < N) {
         const float2 c = cdf[a];
         const float sc = scale[a];
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -665,15 +695,20 @@ __global__ void slice_rows_kernel(const float2 *__restrict__ phit, long long ld,
             const float2 d = df_sub(v.z, v.w, c.x, c.y);
             I[1] = x_fixed(d.x, d.y, sc, clamped);
         }
-    } else if (a == N) {
-        const float sc = vscale_of(*vmax_p);
-        for (int u = 0; u < 2; ++u)
-            if (m + u < rows) {
-                const double v = Vc[m0 + m + u];
-                const float h = (float)v;
-                I[u] = x_fixed(h, (float)(v - (double)h), sc, clamped);
-            }
     }
+    // exact sum of the row's fixed-point values (two's complement int64 atomics: exact and
+    // order-independent, so the mean correction sees exactly the values the Gram sees)
+    __shared__ long long wpart[kSliceThreads / 32];
+    long long rs = (long long)I[0] + (long long)I[1];
+    for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);
+    if ((threadIdx.x & 31) == 0) wpart[threadIdx.x >> 5] = rs;
+    __syncthreads();
+    if (threadIdx.x == 0 && a <= N) {
+        long long t = 0;
+        for (int w = 0; w < kSliceThreads / 32; ++w) t += wpart[w];
+        if (t != 0) atomicAdd(rowsum + a, (unsigned long long)t);  // one per CTA and row
+    }
+    if (m >= rows_pad) return;
     __half d0[2], d1[2], d2[2], d3[2];
     for (int u = 0; u < 2; ++u) digits4(I[u], d0, d1, d2, d3, u);
     const long long idx = (long long)a * rows_pad + m;
@@ -707,19 +742,26 @@ __global__ void gram_reduce_kernel(const double *__restrict__ part, int ntiles, 
     if (tj >= 2 * ti + 2) G[(size_t)b * Np + a] += s;
 }
 
-__global__ void finish_mixed_kernel(const double *__restrict__ G, int Np, const double *__restrict__ sphi,
-                                    const double *__restrict__ c, const double *__restrict__ sumV, long long M, int N,
-                                    double *__restrict__ A, double *__restrict__ b) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+// A = G - s s^T / M, b = G[:, V] - s s_V / M with s the exact column sums of the
+// fixed-point rows (value = digits sum 2^-27 / scale), i.e. repeat.py:2266-2276 for the
+// shifted, quantised columns; optionally sum_phi = s + M c.
+__global__ void finish_mixed_kernel(const double *__restrict__ G, int Np, const unsigned long long *__restrict__ rowsum,
+                                    const float *__restrict__ scale, const double *__restrict__ vmax_p,
+                                    const double *__restrict__ c, long long M, int N, double *__restrict__ A,
+                                    double *__restrict__ b, double *__restrict__ sum_phi) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const double invM = 1.0 / (double)M;
+    const double sv = ldexp((double)(long long)rowsum[N], -27) / (double)vscale_of(*vmax_p);
     if (t < (long long)N * N) {
-        int i = (int)(t / N), j = (int)(t - (long long)i * N);
-        double si = sphi[i] - (double)M * c[i], sj = sphi[j] - (double)M * c[j];
+        const int i = (int)(t / N), j = (int)(t - (long long)i * N);
+        const double si = ldexp((double)(long long)rowsum[i], -27) / (double)scale[i];
+        const double sj = ldexp((double)(long long)rowsum[j], -27) / (double)scale[j];
         A[t] = G[(size_t)i * Np + j] - si * sj * invM;
     }
     if (t < N) {
-        double si = sphi[t] - (double)M * c[t];
-        b[t] = G[(size_t)t * Np + N] - si * (*sumV) * invM;
+        const double si = ldexp((double)(long long)rowsum[t], -27) / (double)scale[t];
+        b[t] = G[(size_t)t * Np + N] - si * sv * invM;
+        if (sum_phi) sum_phi[t] = si + (double)M * c[t];
     }
 }
 
@@ -841,22 +883,21 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     const int nblk = (int)ceil_div(chunk, kPhiPts);
     double *psum = ctx->buf_t<double>("m_psum", (size_t)N * nblk);
     float *pmax = ctx->buf_t<float>("m_pmax", (size_t)N * nblk);
-    double *sphi = sum_phi_dev ? sum_phi_dev : ctx->buf_t<double>("m_sphi", N);
+    unsigned long long *rowsum = ctx->buf_t<unsigned long long>("m_rowsum", (size_t)Np);
     double *cvec = ctx->buf_t<double>("m_c", N);
     float2 *cdf = ctx->buf_t<float2>("m_cdf", N);
     float *scale = ctx->buf_t<float>("m_scale", N);
     double *G = ctx->buf_t<double>("m_G", (size_t)Np * Np);
     RP_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * Np * Np, stream));
+    RP_CUDA(cudaMemsetAsync(rowsum, 0, sizeof(unsigned long long) * Np, stream));
 
-    // ESP row statistics: sum of Vc (mean correction) and max |Vc| (row scale)
-    const double *sumV = vstats_dev, *vmax = vstats_dev ? vstats_dev + 1 : nullptr;
+    // ESP row scale from max |Vc| (the filter's, or computed here)
+    const double *vmax = vstats_dev ? vstats_dev + 1 : nullptr;
     if (!vstats_dev) {
-        double *st = ctx->buf_t<double>("m_vstats", 2);
-        column_sums_fp64(Vc_dev, M, 1, 1, st, false, ctx, stream);
-        absmax_kernel<<<1, 1024, 0, stream>>>(Vc_dev, M, st + 1);
+        double *st = ctx->buf_t<double>("m_vmax", 1);
+        absmax_kernel<<<1, 1024, 0, stream>>>(Vc_dev, M, st);
         RP_LAUNCH_CHECK();
-        sumV = st;
-        vmax = st + 1;
+        vmax = st;
     }
 
     const int nt = Np_pad / kBM;
@@ -876,11 +917,13 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         // 2. centre/scale on the first chunk, fixed-point digits of X
         {
             StageTimer tt(ctx, "center_slice", stream);
-            colstats_finish_kernel<<<ceil_div(N, 4), 128, 0, stream>>>(psum, pmax, nb, N, rows, m0 == 0 ? 1 : 0, sphi,
-                                                                       cvec, cdf, scale);
-            RP_LAUNCH_CHECK();
-            slice_rows_kernel<<<dim3(ceil_div(rows_kpad / 2, 256), Np_pad), 256, 0, stream>>>(
-                phit, chunk_pad, rows, rows_kpad, N, cdf, scale, Vc_dev, m0, vmax, X[0], X[1], X[2], X[3], d_clamped);
+            if (m0 == 0) {
+                colstats_finish_kernel<<<ceil_div(N, 4), 128, 0, stream>>>(psum, pmax, nb, N, rows, cvec, cdf, scale);
+                RP_LAUNCH_CHECK();
+            }
+            slice_rows_kernel<<<dim3(ceil_div(rows_kpad / 2, kSliceThreads), Np_pad), kSliceThreads, 0, stream>>>(
+                phit, chunk_pad, rows, rows_kpad, N, cdf, scale, Vc_dev, m0, vmax, X[0], X[1], X[2], X[3], d_clamped,
+                rowsum);
             RP_LAUNCH_CHECK();
         }
         // 3. exact Gram partial tiles over point splits, then the fixed-order FP64 reduction
@@ -908,7 +951,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         }
     }
     finish_mixed_kernel<<<ceil_div(std::max<long long>((long long)N * N, N), 256), 256, 0, stream>>>(
-        G, Np, sphi, cvec, sumV, M, N, A_dev, b_dev);
+        G, Np, rowsum, scale, vmax, cvec, M, N, A_dev, b_dev, sum_phi_dev);
     RP_LAUNCH_CHECK();
 }
 
