@@ -3,6 +3,7 @@
 * ``librepeat_gb300.so``  the CUDA kernels behind the C ABI (``include/repeat_gb300.h``),
   compiled by nvcc for sm_103a only.
 * ``_synth_host.so``      host helper of the synthetic-cube generator (gcc, pthreads).
+* ``_cube_io.so``         parallel parser of cube / LOCPOT value blocks (gcc, pthreads).
 
 Translation units are compiled in parallel; nothing here needs a GPU.
 """
@@ -21,6 +22,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "librepeat_gb300.so")
 SYNTH_PATH = os.path.join(HERE, "_synth_host.so")
+CUBE_IO_PATH = os.path.join(HERE, "_cube_io.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = [
@@ -63,6 +65,9 @@ def build_host_helpers(force: bool = False) -> str:
     src = os.path.join(CSRC, "synth_host.c")
     if force or _stale(SYNTH_PATH, [src]):
         _run(["gcc", "-O2", "-fPIC", "-shared", "-o", SYNTH_PATH, src, "-lm", "-lpthread"])
+    src = os.path.join(CSRC, "cube_io.c")
+    if force or _stale(CUBE_IO_PATH, [src]):
+        _run(["gcc", "-O2", "-fPIC", "-shared", "-o", CUBE_IO_PATH, src, "-lpthread"])
     return SYNTH_PATH
 
 
