@@ -50,8 +50,11 @@ struct FilterParams {
     int A;
 };
 
-__device__ __forceinline__ double exact_d2(const double *axd, int i, int j, int k, double ex, double ey,
-                                           double ez) {
+// Not inlined on purpose: the call sits in a branch that almost never runs, and as an
+// inlined body the compiler may evaluate it speculatively for every candidate, which puts
+// the FP64 pipe (a small fraction of the FP32 rate on this part) on the critical path.
+__device__ __noinline__ double exact_d2(const double *axd, int i, int j, int k, double ex, double ey,
+                                        double ez) {
     // ((i*a0 + j*a1) + k*a2) and ((dx*dx + dy*dy) + dz*dz), every op rounded (no FMA)
     double gx = __dadd_rn(__dadd_rn(__dmul_rn((double)i, axd[0]), __dmul_rn((double)j, axd[3])),
                           __dmul_rn((double)k, axd[6]));

@@ -307,6 +307,28 @@ constexpr int kPhiPts = 128;     // points per CTA (one per thread)
 constexpr int kPhiAtoms = 16;    // atoms per CTA
 constexpr int kMaxShifts = 128;  // pruned real-space shifts (checked on the host)
 
+// The reference's FP64 cutoff decision for one (point, image) pair (repeat.py:944-966:
+// r = |g - (a + s)| with g = (i a0 + j a1) + k a2, r <= Rc, the self image skipped at
+// r <= 1e-10).  Returns 0 (outside), 1 (inside: the caller adds the FP32 term) or, with
+// full = true, 2 and the FP64 term as a double-float (th, tl).  Not inlined on purpose:
+// it runs for a few pairs in a million, and inlined the compiler may evaluate it
+// speculatively for every pair on the slow FP64 pipe.
+__device__ __noinline__ int fp64_pair(const double *axis, int i, int j, int k, const double *p,
+                                      const double *shifts, int s, int zero_idx, double rc, double sa, bool full,
+                                      float &th, float &tl) {
+    double g[3];
+    for (int d = 0; d < 3; ++d) g[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)k * axis[6 + d];
+    const double ex = g[0] - (p[0] + shifts[3 * s]), ey = g[1] - (p[1] + shifts[3 * s + 1]),
+                 ez = g[2] - (p[2] + shifts[3 * s + 2]);
+    const double r = sqrt(ex * ex + ey * ey + ez * ez);
+    if (!(r <= rc) || (s == zero_idx && !(r > 1e-10))) return 0;
+    if (!full) return 1;
+    const double t = erfc(sa * r) / r;
+    th = (float)t;
+    tl = (float)(t - (double)th);
+    return 2;
+}
+
 // Image positions atom + shift as double-float, [N][S] x {hi (x, y, z, shift index), lo}
 __global__ void images_df_kernel(const double *__restrict__ atoms, int N, const double *__restrict__ shifts, int S,
                                  float4 *__restrict__ img) {
@@ -515,18 +537,11 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 > rcc + band) continue;
                 if (r2 < fp64_below || r2 > rcc - band) {
-                    const int s = __float_as_int(h.w);
-                    const double *p = atoms + 3 * (a0 + a);
-                    double gabs[3];
-                    for (int d = 0; d < 3; ++d)
-                        gabs[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)l * axis[6 + d];
-                    const double ex = gabs[0] - (p[0] + shifts[3 * s]), ey = gabs[1] - (p[1] + shifts[3 * s + 1]),
-                                 ez = gabs[2] - (p[2] + shifts[3 * s + 2]);
-                    const double r = sqrt(ex * ex + ey * ey + ez * ez);
-                    if (!(r <= rc) || (s == zero_idx && !(r > 1e-10))) continue;
-                    if (r2 < fp64_below) {  // a point on top of an image: the large term in FP64
-                        const double t = erfc(sa * r) / r;
-                        const float th = (float)t, tl = (float)(t - (double)th);
+                    float th, tl;
+                    const int dec = fp64_pair(axis, i, j, l, atoms + 3 * (a0 + a), shifts, __float_as_int(h.w),
+                                              zero_idx, rc, sa, r2 < fp64_below, th, tl);
+                    if (dec == 0) continue;
+                    if (dec == 2) {  // a point on top of an image: the large term in FP64
                         float s2, e2;
                         dfa::two_sum(x64h, th, s2, e2);
                         x64h = s2;

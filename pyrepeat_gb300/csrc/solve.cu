@@ -196,11 +196,12 @@ __device__ bool lu_factor_f32(float *A, int *perm, int n1, double *sv, int *si, 
         const float inv = 1.0f / pv;
         for (int r = k + 1 + threadIdx.x; r < n1; r += kLU) A[(size_t)r * n1 + k] *= inv;
         __syncthreads();
-        const int m = n1 - k - 1;
-        const long long tot = (long long)m * m;
-        for (long long t = threadIdx.x; t < tot; t += kLU) {
-            const int rr = k + 1 + (int)(t / m), cc = k + 1 + (int)(t - (long long)(t / m) * m);
-            A[(size_t)rr * n1 + cc] -= A[(size_t)rr * n1 + k] * A[(size_t)k * n1 + cc];
+        // rank-1 update: a warp per row, lanes along the row (coalesced, no index division)
+        const float *prow = A + (size_t)k * n1;
+        for (int rr = k + 1 + (threadIdx.x >> 5); rr < n1; rr += kLU / 32) {
+            float *row = A + (size_t)rr * n1;
+            const float l = row[k];
+            for (int cc = k + 1 + (threadIdx.x & 31); cc < n1; cc += 32) row[cc] -= l * prow[cc];
         }
         __syncthreads();
     }
@@ -232,6 +233,20 @@ __device__ void lu_apply_f32(const float *__restrict__ LU, const int *__restrict
 }
 
 constexpr int kRefineMax = 30;
+
+// r = bs - A0 x in FP64: a warp per row, lanes along the row, fixed-order shuffle sum
+__device__ void residual(const SolveDesc &d, int n1) {
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (int rr = threadIdx.x >> 5; rr < n1; rr += kLU / 32) {
+        const double *row = d.A0 + (size_t)rr * n1;
+        double s = 0.0;
+        for (int c = lane; c < n1; c += 32) s += row[c] * d.x[c];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) d.r[rr] = d.bs[rr] - s;
+    }
+    __syncthreads();
+}
 
 __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *__restrict__ descs) {
     const SolveDesc d = descs[blockIdx.x];
@@ -277,12 +292,9 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
                 for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] += (double)xs[t] * rm;
                 __syncthreads();
                 double rn = 0.0, xn = 0.0;
+                residual(d, n1);
                 for (int rr = threadIdx.x; rr < n1; rr += kLU) {
-                    double s = d.bs[rr];
-                    const double *row = d.A0 + (size_t)rr * n1;
-                    for (int c = 0; c < n1; ++c) s -= row[c] * d.x[c];
-                    d.r[rr] = s;
-                    rn = fmax(rn, fabs(s));
+                    rn = fmax(rn, fabs(d.r[rr]));
                     xn = fmax(xn, fabs(d.x[rr]));
                 }
                 rn = block_max(rn, sv);
@@ -331,11 +343,11 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
             const double inv = 1.0 / pv;
             for (int r = k + 1 + threadIdx.x; r < n1; r += kLU) A[(size_t)r * n1 + k] *= inv;
             __syncthreads();
-            const int m = n1 - k - 1;
-            const long long tot = (long long)m * m;
-            for (long long t = threadIdx.x; t < tot; t += kLU) {
-                int rr = k + 1 + (int)(t / m), cc = k + 1 + (int)(t - (long long)(t / m) * m);
-                A[(size_t)rr * n1 + cc] -= A[(size_t)rr * n1 + k] * A[(size_t)k * n1 + cc];
+            const double *prow = A + (size_t)k * n1;
+            for (int rr = k + 1 + (threadIdx.x >> 5); rr < n1; rr += kLU / 32) {
+                double *row = A + (size_t)rr * n1;
+                const double l = row[k];
+                for (int cc = k + 1 + (threadIdx.x & 31); cc < n1; cc += 32) row[cc] -= l * prow[cc];
             }
             __syncthreads();
         }
