@@ -41,6 +41,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "fits/s & p50/p99 latency vs plain FP64 GPU fit at max|dq|<=1e-5 e"
 
+# ncu figures of phi_chunk_kernel (profiles/phi_chunk_kernel_batch8.txt): DRAM bytes and
+# thread instructions per point-atom pair of the captured launch
+PHI_DRAM_PER_PAIR = 10.10
+PHI_INST_PER_PAIR = 389.0
+
 
 # ----------------------------------------------------------------------------- distributed helpers
 
@@ -356,8 +361,21 @@ def main():
     roof["kernel"] = dom_name
     roof["traffic"] = None
     if dom_name == "phi":
-        # the real-space + reciprocal kernel is bound by the FP32 pipe, not by HBM: report its rate
+        # phi_chunk_kernel: one ncu capture (profiles/phi_chunk_kernel_batch8.txt) measured
+        # PHI_DRAM_PER_PAIR DRAM bytes and PHI_INST_PER_PAIR thread instructions per point-atom
+        # pair; traffic is that times the pairs of an average launch.  The kernel is bound by
+        # instruction issue (FP32/ALU pipes), not by HBM: "issue" relates its live instruction
+        # rate to the nominal issue peak (4 warp instructions per clock per SM at the SM clock).
+        n_l = max(stages["phi"][1], 1)
+        roof["kernel"] = "phi_chunk_kernel"
+        roof["traffic"] = PHI_DRAM_PER_PAIR * pairs / n_l
         roof["point_atom_evals_per_s"] = pairs / (stages["phi"][0] / 1e3)
+        sm_mhz = clocks.get("sm_mhz") or 2070.0
+        peak_inst = 152 * 4 * 32 * sm_mhz * 1e6
+        ach_inst = PHI_INST_PER_PAIR * pairs / (stages["phi"][0] / 1e3)
+        roof["issue"] = {"achieved_thread_inst_per_s": ach_inst, "peak_thread_inst_per_s": peak_inst,
+                         "frac": ach_inst / peak_inst, "peak_kind": "nominal issue rate at the sampled SM clock",
+                         "inst_per_pair": PHI_INST_PER_PAIR}
     stage_share = {k: round(v[0], 3) for k, v in sorted(stages.items(), key=lambda kv: -kv[1][0])}
 
     # CPU oracle on a bounded sample (rank 0, N = 1 only)
