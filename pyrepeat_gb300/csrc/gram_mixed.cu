@@ -70,7 +70,7 @@ constexpr int kGramStageBytes = kGSlices * kTileBytes + kGSlices * kBTileBytes;
 constexpr int kGramSmem = kGramStages * kGramStageBytes + 1024 + 256;
 
 struct GramArgs {
-    int nt, ntri, kb_total, kb_per_split, flush;  // flush: stages per exact FP32 run (<= kGramFlush)
+    int nt, ntj, ntri, kb_total, kb_per_split, flush;  // flush: stages per exact FP32 run (<= kGramFlush)
     double *out;  // partial tiles [split*ntri + tri][col][row], FP64 (exact integers)
     int *status;
 };
@@ -80,10 +80,12 @@ __device__ __forceinline__ uint8_t *align1024(uint8_t *raw) {
     return raw + (((s + 1023u) & ~1023u) - s);
 }
 
-// Gram tile t -> (ti, tj): rows [128 ti, +128), columns [64 tj, +64), tj >= 2 ti.
-__device__ __forceinline__ void gram_tile_decode(int t, int nt, int &ti, int &tj) {
+// Gram tile t -> (ti, tj): rows [128 ti, +128), columns [64 tj, +64), 2 ti <= tj < ntj,
+// ntj = ceil(rows / 64): tiles wholly beyond the last row are never computed, and rows
+// past the end of the digit arrays read as zeros (the tensor maps' out-of-bounds fill).
+__device__ __forceinline__ void gram_tile_decode(int t, int ntj, int &ti, int &tj) {
     ti = 0;
-    int len = 2 * nt;
+    int len = ntj;
     while (t >= len) {
         t -= len;
         ++ti;
@@ -107,7 +109,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile = blockIdx.x % g.ntri, split = blockIdx.x / g.ntri;
     int ti, tj;
-    gram_tile_decode(tile, g.nt, ti, tj);
+    gram_tile_decode(tile, g.ntj, ti, tj);
     const bool inblock = (tj < 2 * ti + 2);       // columns inside the row block: B rows are part of A's tile
     const uint32_t b_in_a = (uint32_t)(tj - 2 * ti) * (kGN * 128);  // byte offset of B's rows inside A's tile
     const int a_row0 = ti * kBM, b_row0 = tj * kGN;
@@ -736,13 +738,13 @@ __global__ void __launch_bounds__(kSliceThreads) slice_rows_kernel(const float2 
 // Sum the partial Gram tiles of all point splits in a fixed order (FP64; each
 // partial is an exact integer) and add them, unscaled, into G (Np x Np).  Tiles
 // inside a 128-row block already hold both (a,b) and (b,a); the others are mirrored.
-__global__ void gram_reduce_kernel(const double *__restrict__ part, int ntiles, int nsplit, int nt, int Np,
+__global__ void gram_reduce_kernel(const double *__restrict__ part, int ntiles, int nsplit, int ntj, int Np,
                                    const float *__restrict__ scale, const double *__restrict__ vmax_p, int N,
                                    double *__restrict__ G) {
     const float vscale = vscale_of(*vmax_p);
     const int tile = blockIdx.y;
     int ti, tj;
-    gram_tile_decode(tile, nt, ti, tj);
+    gram_tile_decode(tile, ntj, ti, tj);
     const int e = blockIdx.x * blockDim.x + threadIdx.x;  // element in tile, column-major (c*128 + r)
     if (e >= kBM * kGN) return;
     const int c = e / kBM, r = e - c * kBM;
@@ -833,7 +835,7 @@ CUtensorMap make_map(const void *ptr, long long rows, long long cols, int box_ro
     return m;
 }
 
-void launch_gram(const __half *const *X, int Np_pad, long long cols, const GramArgs &g, int grid, cudaStream_t s) {
+void launch_gram(const __half *const *X, int rows, long long cols, const GramArgs &g, int grid, cudaStream_t s) {
     static bool attr = false;
     if (!attr) {
         RP_CUDA(cudaFuncSetAttribute(gram_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmem));
@@ -841,8 +843,8 @@ void launch_gram(const __half *const *X, int Np_pad, long long cols, const GramA
     }
     CUtensorMap a[kGSlices], b[kGSlices];
     for (int q = 0; q < kGSlices; ++q) {
-        a[q] = make_map(X[q], Np_pad, cols, kBM);
-        b[q] = make_map(X[q], Np_pad, cols, kGN);
+        a[q] = make_map(X[q], rows, cols, kBM);   // rows past `rows` read as zeros
+        b[q] = make_map(X[q], rows, cols, kGN);
     }
     gram_exact_kernel<<<grid, kGramThreads, kGramSmem, s>>>(a[0], a[1], a[2], a[3], b[0], b[1], b[2], b[3], g);
     RP_LAUNCH_CHECK();
@@ -885,15 +887,14 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
 
     // chunk the points so the per-chunk staging stays below ~6 GB
     const int Np = N + 1;                       // atoms + the ESP row
-    const int Np_pad = (int)round_up(Np, kBM);
-    const long long per_point = 8LL * N + 8LL * Np_pad;  // Phi (double-float) + four FP16 digits
+    const long long per_point = 8LL * N + 8LL * Np;  // Phi (double-float) + four FP16 digits
     long long chunk = std::max<long long>(kBM, ((6LL << 30) / per_point) / kBM * kBM);
     chunk = std::min<long long>(chunk, round_up(M, kBM));
     const long long chunk_pad = round_up(chunk, kBK);
 
     float2 *phit = ctx->buf_t<float2>("m_phit", (size_t)N * chunk_pad);
     __half *X[kGSlices];
-    for (int q = 0; q < kGSlices; ++q) X[q] = ctx->buf_t<__half>("m_X" + std::to_string(q), (size_t)Np_pad * chunk_pad);
+    for (int q = 0; q < kGSlices; ++q) X[q] = ctx->buf_t<__half>("m_X" + std::to_string(q), (size_t)Np * chunk_pad);
     int *d_clamped = ctx->d_status + 1;  // second status word: fixed-point range overflows
     const int nblk = (int)ceil_div(chunk, kPhiPts);
     double *psum = ctx->buf_t<double>("m_psum", (size_t)N * nblk);
@@ -915,8 +916,9 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         vmax = st;
     }
 
-    const int nt = Np_pad / kBM;
-    const int ntri = nt * (nt + 1);  // 128 x 64 Gram tiles with columns at or right of the row block
+    const int nt = (int)ceil_div(Np, kBM), ntj = (int)ceil_div(Np, kGN);
+    int ntri = 0;  // 128 x 64 Gram tiles with columns at or right of the row block, up to the last row
+    for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
     const int kb_split = 2 * kGramFlush;  // 1024 points per CTA (int64 headroom), exact sums flushed every 512
 
     for (long long m0 = 0; m0 < M; m0 += chunk) {
@@ -936,7 +938,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
                 colstats_finish_kernel<<<ceil_div(N, 4), 128, 0, stream>>>(psum, pmax, nb, N, rows, cvec, cdf, scale);
                 RP_LAUNCH_CHECK();
             }
-            slice_rows_kernel<<<dim3(ceil_div(rows_kpad / 2, kSliceThreads), Np_pad), kSliceThreads, 0, stream>>>(
+            slice_rows_kernel<<<dim3(ceil_div(rows_kpad / 2, kSliceThreads), Np), kSliceThreads, 0, stream>>>(
                 phit, chunk_pad, rows, rows_kpad, N, cdf, scale, Vc_dev, m0, vmax, X[0], X[1], X[2], X[3], d_clamped,
                 rowsum);
             RP_LAUNCH_CHECK();
@@ -948,6 +950,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
             double *part = ctx->buf_t<double>("m_part", (size_t)nsplit * ntri * kBM * kGN);
             GramArgs g{};
             g.nt = nt;
+            g.ntj = ntj;
             g.ntri = ntri;
             g.kb_total = kb_total;
             g.kb_per_split = kb_split;
@@ -957,10 +960,10 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
             const __half *Xq[kGSlices] = {X[0], X[1], X[2], X[3]};
             {
                 StageTimer tt(ctx, "gram_exact", stream);
-                launch_gram(Xq, Np_pad, rows_kpad, g, ntri * nsplit, stream);
+                launch_gram(Xq, Np, rows_kpad, g, ntri * nsplit, stream);
             }
             StageTimer tr(ctx, "gram_reduce_fp64", stream);
-            gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256, 0, stream>>>(part, ntri, nsplit, nt, Np,
+            gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256, 0, stream>>>(part, ntri, nsplit, ntj, Np,
                                                                                          scale, vmax, N, G);
             RP_LAUNCH_CHECK();
         }
@@ -1018,25 +1021,26 @@ extern "C" int rp_debug_gram_slices(rp_ctx *ctx, const void *X0, const void *X1,
     using namespace rp;
     try {
         RP_CUDA(cudaSetDevice(ctx->device));
-        const int Np_pad = (int)round_up(Np, kBM);
-        const int nt = Np_pad / kBM, ntri = nt * (nt + 1);
+        const int nt = (int)ceil_div(Np, kBM), ntj = (int)ceil_div(Np, kGN);
+        int ntri = 0;
+        for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
         const int kb_total = (int)(cols / kBK);
         const int nsplit = (kb_total + kb_split - 1) / kb_split;
         double *part = ctx->buf_t<double>("dbg_part", (size_t)nsplit * ntri * kBM * kGN);
         RP_CUDA(cudaMemset(ctx->d_status, 0, sizeof(int)));
         GramArgs g{};
-        g.nt = nt; g.ntri = ntri; g.kb_total = kb_total; g.kb_per_split = kb_split;
+        g.nt = nt; g.ntj = ntj; g.ntri = ntri; g.kb_total = kb_total; g.kb_per_split = kb_split;
         g.flush = std::min(std::max(flush, 1), kGramFlush);
         g.out = part; g.status = ctx->d_status;
         const __half *Xq[kGSlices] = {(const __half *)X0, (const __half *)X1, (const __half *)X2, (const __half *)X3};
-        launch_gram(Xq, Np_pad, cols, g, ntri * nsplit, 0);
+        launch_gram(Xq, Np, cols, g, ntri * nsplit, 0);
         float *ones = ctx->buf_t<float>("dbg_ones", Np);
         std::vector<float> h((size_t)Np, 1.0f);
         RP_CUDA(cudaMemcpy(ones, h.data(), sizeof(float) * Np, cudaMemcpyHostToDevice));
         RP_CUDA(cudaMemset(I_dev, 0, sizeof(double) * Np * Np));
         double *vmax = ctx->buf_t<double>("dbg_vmax", 1);  // unused: every row is an atom row (N = Np)
         RP_CUDA(cudaMemset(vmax, 0, sizeof(double)));
-        gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256>>>(part, ntri, nsplit, nt, Np, ones, vmax, Np, I_dev);
+        gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256>>>(part, ntri, nsplit, ntj, Np, ones, vmax, Np, I_dev);
         RP_LAUNCH_CHECK();
         RP_CUDA(cudaDeviceSynchronize());
         int st = 0;

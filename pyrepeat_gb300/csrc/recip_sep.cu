@@ -89,7 +89,10 @@ constexpr int kN1B = 8;
 // one W row (broadcast) and consecutive ez phases (coalesced).
 __global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 *__restrict__ EZ, int ncols, int P,
                                      int nz, float4 *__restrict__ F) {
+    extern __shared__ float4 ezs[];  // the whole ez table [nw][nz], read once per CTA
     const int n1c = P + 1, nw = 2 * P + 1, nb = (n1c + kN1B - 1) / kN1B;
+    for (int q = threadIdx.x; q < nw * nz; q += blockDim.x) ezs[q] = EZ[q];
+    __syncthreads();
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nz * nw * ncols * nb) return;
     const int l = (int)(t % nz);
@@ -104,7 +107,7 @@ __global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 
     for (int u = 0; u < kN1B; ++u) re[u] = im[u] = dfa::acc{0.f, 0.f};
     const float4 *w = W + ((long long)a * nw + n2) * nw * n1c + n10;
     for (int n3 = 0; n3 < nw; ++n3) {
-        const float4 z = EZ[(long long)n3 * nz + l];
+        const float4 z = ezs[n3 * nz + l];
         const float4 *wr = w + (long long)n3 * n1c;
 #pragma unroll
         for (int u = 0; u < kN1B; ++u)
@@ -121,14 +124,16 @@ __global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 
 __global__ void __launch_bounds__(128) recip_stage_b_kernel(const float4 *__restrict__ F,
                                                             const float4 *__restrict__ EY, int ncols, int P, int ny,
                                                             int ab, float2 *__restrict__ E) {
-    extern __shared__ float4 fs[];  // [nw][ab][n1c]
+    extern __shared__ float4 fs[];  // [nw][ab][n1c] F slab, then the ey table [nw][ny]
     const int n1c = P + 1, nw = 2 * P + 1;
     const int l = blockIdx.y, a0 = blockIdx.x * ab, na = min(ab, ncols - a0);
     const int slab = nw * ab * n1c;
+    float4 *eys = fs + slab;
     for (int t = threadIdx.x; t < slab; t += blockDim.x) {
         const int n1 = t % n1c, u = t / n1c, a = u % ab, n2 = u / ab;
         fs[t] = (a < na) ? F[(((long long)l * nw + n2) * ncols + a0 + a) * n1c + n1] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
+    for (int q = threadIdx.x; q < nw * ny; q += blockDim.x) eys[q] = EY[q];
     __syncthreads();
     const int items = na * ny;  // (a, j), j fastest: a warp reads one column's slab (broadcast)
     for (int it = threadIdx.x; it < items; it += blockDim.x) {
@@ -140,7 +145,7 @@ __global__ void __launch_bounds__(128) recip_stage_b_kernel(const float4 *__rest
 #pragma unroll
             for (int u = 0; u < kN1B; ++u) re[u] = im[u] = 0.f;
             for (int n2 = 0; n2 < nw; ++n2) {
-                const float4 y = EY[(long long)n2 * ny + j];
+                const float4 y = eys[n2 * ny + j];
                 const float4 *fr = fs + ((size_t)n2 * ab + a) * n1c + n10;
 #pragma unroll
                 for (int u = 0; u < kN1B; ++u)
@@ -184,13 +189,20 @@ void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const do
     build_w_kernel<<<ceil_div(nk, 128), 128, 0, stream>>>(ew->d_kidx, ew->d_kcoef, ew->K, P, U, d_q, N, ncols, W);
     RP_LAUNCH_CHECK();
     const int nb = (n1c + kN1B - 1) / kN1B;
-    recip_stage_a_kernel<<<ceil_div((long long)nz * nw * ncols * nb, 128), 128, 0, stream>>>(W, ew->d_ezf, ncols, P,
-                                                                                             nz, F);
+    const size_t smem_a = sizeof(float4) * (size_t)nw * nz;
+    RP_REQUIRE(smem_a <= (200u << 10), "recip_rows: grid too large along z for KMAX");
+    static size_t attr_a = 0;
+    if (smem_a > (48u << 10) && smem_a > attr_a) {
+        RP_CUDA(cudaFuncSetAttribute(recip_stage_a_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a));
+        attr_a = smem_a;
+    }
+    recip_stage_a_kernel<<<ceil_div((long long)nz * nw * ncols * nb, 128), 128, smem_a, stream>>>(W, ew->d_ezf, ncols,
+                                                                                                  P, nz, F);
     RP_LAUNCH_CHECK();
     // stage B: as many columns per CTA as fit 96 KB of shared memory (at most 16)
     const size_t col_bytes = sizeof(float4) * (size_t)nw * n1c;
     const int ab = (int)std::max<size_t>(1, std::min<size_t>(16, (96u << 10) / col_bytes));
-    const size_t smem = col_bytes * ab;
+    const size_t smem = col_bytes * ab + sizeof(float4) * (size_t)nw * ny;
     RP_REQUIRE(smem <= (200u << 10), "recip_rows: KMAX too large");
     static size_t attr = 0;
     if (smem > (48u << 10) && smem > attr) {
