@@ -325,6 +325,8 @@ def main():
     p99 = lat[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]
 
     # roofline of the dominant stage from live CUDA-event stage timings of one more step
+    # (with timing on, the library runs the batch's fits on one stream, so every stage is
+    # timed alone; the timed steps above overlap fits on four streams)
     ctx.set_timing(True)
     ctx.stage_times()
     step()

@@ -126,6 +126,18 @@ struct rp_ctx {
         return b.ptr;
     }
     cublasHandle_t blas();
+    // Worker streams for fits that run concurrently inside one batch (created on first use,
+    // non-blocking, destroyed with the ctx).
+    std::vector<cudaStream_t> lanes;
+    cudaStream_t lane(int i) {
+        while ((int)lanes.size() <= i) {
+            cudaStream_t st = nullptr;
+            cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+            if (e != cudaSuccess) rp::fail(RP_E_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+            lanes.push_back(st);
+        }
+        return lanes[i];
+    }
 };
 
 struct rp_ewald {
@@ -197,7 +209,7 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
 // compute the max here.
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
-                cudaStream_t stream, const double *vstats_dev = nullptr);
+                cudaStream_t stream, const double *vstats_dev = nullptr, const std::string &slot = "");
 void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
                const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,
                double *info, cudaStream_t stream);
@@ -220,8 +232,9 @@ void grid_tables_fp64(const rp_ewald *ew, const int32_t *d_kept, int64_t m0, int
 // Reciprocal sum by separable lattice phases (recip_sep.cu): E[r][col][n1] for every
 // grid row r = j + l*ny, col = atom (d_q == nullptr) or one charge-weighted column.
 size_t recip_rows_bytes(const rp_ewald *ew, int ncols);
+// `slot` keeps the scratch of fits running concurrently on different streams apart.
 void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const double *d_q, int N, float2 *E,
-                cudaStream_t stream);
+                cudaStream_t stream, const std::string &slot = "");
 
 // Shared epilogue kernels (phi_fp64.cu).
 void column_sums_fp64(const double *X, int64_t rows, int cols, int ld, double *out, bool accumulate,

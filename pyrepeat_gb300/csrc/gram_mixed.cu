@@ -857,7 +857,7 @@ inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b
 
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
-                cudaStream_t stream, const double *vstats_dev) {
+                cudaStream_t stream, const double *vstats_dev, const std::string &slot) {
     RP_REQUIRE(N > 0 && M > 0, "rp_gram: need N > 0 and M > 0");
     std::vector<double> sh;
     int zero_idx = -1;
@@ -867,20 +867,20 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     const int nx = ew->grid.n_grid[0], ny = ew->grid.n_grid[1];
     const int n1c = ew->kmax;
 
-    double *d_atoms = ctx->buf_t<double>("g_atoms", 3 * (size_t)N);
-    double *d_shifts = ctx->buf_t<double>("g_shifts", sh.size());
-    double *d_axis = ctx->buf_t<double>("g_axis", 9);
+    double *d_atoms = ctx->buf_t<double>("g_atoms" + slot, 3 * (size_t)N);
+    double *d_shifts = ctx->buf_t<double>("g_shifts" + slot, sh.size());
+    double *d_axis = ctx->buf_t<double>("g_axis" + slot, 9);
     RP_CUDA(cudaMemcpyAsync(d_atoms, atoms, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_shifts, sh.data(), sizeof(double) * sh.size(), cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice, stream));
     int *d_status = ctx->d_status;  // cleared by the caller (rp_gram / the batch driver)
 
     // reciprocal rows of every atom (stages A and B) and the double-float images, once per fit
-    float2 *E = ctx->buf_t<float2>("m_E", recip_rows_bytes(ew, N) / sizeof(float2));
-    float4 *img = ctx->buf_t<float4>("m_img", 2 * (size_t)N * S);
+    float2 *E = ctx->buf_t<float2>("m_E" + slot, recip_rows_bytes(ew, N) / sizeof(float2));
+    float4 *img = ctx->buf_t<float4>("m_img" + slot, 2 * (size_t)N * S);
     {
         StageTimer tt(ctx, "recip_rows", stream);
-        recip_rows(ctx, ew, d_atoms, nullptr, N, E, stream);
+        recip_rows(ctx, ew, d_atoms, nullptr, N, E, stream, slot);
         images_df_kernel<<<ceil_div((long long)N * S, 128), 128, 0, stream>>>(d_atoms, N, d_shifts, S, img);
         RP_LAUNCH_CHECK();
     }
@@ -892,25 +892,25 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     chunk = std::min<long long>(chunk, round_up(M, kBM));
     const long long chunk_pad = round_up(chunk, kBK);
 
-    float2 *phit = ctx->buf_t<float2>("m_phit", (size_t)N * chunk_pad);
+    float2 *phit = ctx->buf_t<float2>("m_phit" + slot, (size_t)N * chunk_pad);
     __half *X[kGSlices];
-    for (int q = 0; q < kGSlices; ++q) X[q] = ctx->buf_t<__half>("m_X" + std::to_string(q), (size_t)Np * chunk_pad);
+    for (int q = 0; q < kGSlices; ++q) X[q] = ctx->buf_t<__half>("m_X" + slot + std::to_string(q), (size_t)Np * chunk_pad);
     int *d_clamped = ctx->d_status + 1;  // second status word: fixed-point range overflows
     const int nblk = (int)ceil_div(chunk, kPhiPts);
-    double *psum = ctx->buf_t<double>("m_psum", (size_t)N * nblk);
-    float *pmax = ctx->buf_t<float>("m_pmax", (size_t)N * nblk);
-    unsigned long long *rowsum = ctx->buf_t<unsigned long long>("m_rowsum", (size_t)Np);
-    double *cvec = ctx->buf_t<double>("m_c", N);
-    float2 *cdf = ctx->buf_t<float2>("m_cdf", N);
-    float *scale = ctx->buf_t<float>("m_scale", N);
-    double *G = ctx->buf_t<double>("m_G", (size_t)Np * Np);
+    double *psum = ctx->buf_t<double>("m_psum" + slot, (size_t)N * nblk);
+    float *pmax = ctx->buf_t<float>("m_pmax" + slot, (size_t)N * nblk);
+    unsigned long long *rowsum = ctx->buf_t<unsigned long long>("m_rowsum" + slot, (size_t)Np);
+    double *cvec = ctx->buf_t<double>("m_c" + slot, N);
+    float2 *cdf = ctx->buf_t<float2>("m_cdf" + slot, N);
+    float *scale = ctx->buf_t<float>("m_scale" + slot, N);
+    double *G = ctx->buf_t<double>("m_G" + slot, (size_t)Np * Np);
     RP_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * Np * Np, stream));
     RP_CUDA(cudaMemsetAsync(rowsum, 0, sizeof(unsigned long long) * Np, stream));
 
     // ESP row scale from max |Vc| (the filter's, or computed here)
     const double *vmax = vstats_dev ? vstats_dev + 1 : nullptr;
     if (!vstats_dev) {
-        double *st = ctx->buf_t<double>("m_vmax", 1);
+        double *st = ctx->buf_t<double>("m_vmax" + slot, 1);
         absmax_kernel<<<1, 1024, 0, stream>>>(Vc_dev, M, st);
         RP_LAUNCH_CHECK();
         vmax = st;
@@ -947,7 +947,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         {
             const int kb_total = (int)(rows_kpad / kBK);
             const int nsplit = (kb_total + kb_split - 1) / kb_split;
-            double *part = ctx->buf_t<double>("m_part", (size_t)nsplit * ntri * kBM * kGN);
+            double *part = ctx->buf_t<double>("m_part" + slot, (size_t)nsplit * ntri * kBM * kGN);
             GramArgs g{};
             g.nt = nt;
             g.ntj = ntj;

@@ -167,7 +167,7 @@ size_t recip_rows_bytes(const rp_ewald *ew, int ncols) {
 }
 
 void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const double *d_q, int N, float2 *E,
-                cudaStream_t stream) {
+                cudaStream_t stream, const std::string &slot) {
     const int P = ew->kmax - 1, n1c = P + 1, nw = 2 * P + 1;
     const int ny = ew->grid.n_grid[1], nz = ew->grid.n_grid[2];
     const int ncols = d_q ? 1 : N;
@@ -177,9 +177,9 @@ void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const do
         return;
     }
     const size_t nW = (size_t)ncols * nw * nw * n1c, nF = (size_t)nz * nw * ncols * n1c;
-    float4 *W = ctx->buf_t<float4>("rs_W", nW);
-    float4 *F = ctx->buf_t<float4>("rs_F", nF);
-    double2 *U = ctx->buf_t<double2>("rs_U", (size_t)N * 3 * nw);
+    float4 *W = ctx->buf_t<float4>("rs_W" + slot, nW);
+    float4 *F = ctx->buf_t<float4>("rs_F" + slot, nF);
+    double2 *U = ctx->buf_t<double2>("rs_U" + slot, (size_t)N * 3 * nw);
     RP_CUDA(cudaMemsetAsync(W, 0, sizeof(float4) * nW, stream));
     Rec9 rb;
     for (int q = 0; q < 9; ++q) rb.b[q] = ew->rec[q];

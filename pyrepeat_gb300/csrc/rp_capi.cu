@@ -87,6 +87,7 @@ int rp_ctx_destroy(rp_ctx *ctx) {
     cudaSetDevice(ctx->device);
     for (auto &kv : ctx->scratch) cudaFree(kv.second.ptr);
     for (auto &kv : ctx->host_scratch) cudaFreeHost(kv.second.ptr);
+    for (cudaStream_t st : ctx->lanes) cudaStreamDestroy(st);
     if (ctx->cublas) cublasDestroy(ctx->cublas);
     cudaFree(ctx->d_status);
     delete ctx;
@@ -247,16 +248,35 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             if (M_out) M_out[i] = M[i];
             RP_REQUIRE(M[i] > 0, "rp_fit: no grid point of cube " + std::to_string(i) + " survives the vdW filter");
         }
-        // 3. normal equations of every cube, back to back on the stream
+        // 3. normal equations of every cube.  Mixed-precision fits are spread over kLanes
+        //    worker streams (each with its own scratch), so one cube's small kernels and
+        //    launch gaps overlap another's; the FP64 comparator stays on the caller's
+        //    stream (its cuBLAS handle is shared).  Every cube's result is independent of
+        //    the lane it ran on.
+        //    With stage timing on, one lane: the timers then measure each stage alone.
+        constexpr int kLanes = 4;
+        const int lanes = ctx->timing ? 1 : kLanes;
+        bool used[kLanes] = {false, false, false, false};
         for (int i = 0; i < n; ++i) {
             const rp_fit_desc &d = descs[i];
-            if (d.precision == RP_PREC_MIXED)
+            if (d.precision == RP_PREC_MIXED) {
+                const int ln = i % lanes;
+                used[ln] = true;
                 rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
-                               b + off_n[i], nullptr, stream, vst + 2 * i);
-            else
+                               b + off_n[i], nullptr, ctx->lane(ln), vst + 2 * i, "#" + std::to_string(ln));
+            } else {
                 rp::gram_fp64(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
                               b + off_n[i], nullptr, stream);
+            }
         }
+        for (int ln = 0; ln < kLanes; ++ln)
+            if (used[ln]) {  // the solve on the caller's stream waits for every lane
+                cudaEvent_t ev;
+                RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                RP_CUDA(cudaEventRecord(ev, ctx->lane(ln)));
+                RP_CUDA(cudaStreamWaitEvent(stream, ev, 0));
+                RP_CUDA(cudaEventDestroy(ev));
+            }
         // 4. all constraint folds and bordered solves, one launch
         std::vector<rp::SolveJob> jobs((size_t)n);
         for (int i = 0; i < n; ++i) {
