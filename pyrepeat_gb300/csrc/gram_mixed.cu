@@ -377,7 +377,12 @@ __device__ __forceinline__ void int_times_df(float k, float ah, float al, float 
     e = __fmaf_rn(k, al, e);
 }
 
-__global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
+// NC > 0: the number of n1 terms is the compile-time constant NC (KMAX = NC, the
+// reference's default 7): an atom's NC E values are loaded at the top of its iteration
+// and used after the real-space loop, which hides their L2 latency; stage C is unrolled.
+// NC = 0: any KMAX, loads in the loop.  The register cap keeps 7 CTAs per SM.
+template <int NC>
+__global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
     const int32_t *__restrict__ kept, long long m0, long long rows, const double *__restrict__ axis, AxisDF adf,
     int nx, int ny,
     const double *__restrict__ atoms, int N, const double *__restrict__ shifts, int S, int scap, int zero_idx,
@@ -512,18 +517,15 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
     const float rcc = rcf * rcf, band = 4e-6f * rcc, saf = saf_in;
     const float fp64_below = fmaxf(near2, 1e-6f);
     const long long row = f / nx;  // j + l * ny
-    for (int a = 0; a < na; ++a) {
+    const float2 *erow = E + (row * N + a0) * (NC > 0 ? NC : n1c);
+    float2 *prow = phit + (long long)a0 * ld + m;
+    for (int a = 0; a < na; ++a, erow += (NC > 0 ? NC : n1c), prow += ld) {
         dfa::acc v{0.f, 0.f};
         float x64h = 0.f, x64l = 0.f;  // rare FP64 terms, folded in as double-float pairs
-        if (valid && (parts & 2)) {
-            const float2 *e = E + (row * N + a0 + a) * n1c;
-            float rs = 0.f;
-            for (int n = 0; n < n1c; ++n) {
-                const float2 x = exs[n * kPhiPts + threadIdx.x], y = e[n];
-                rs = fmaf(x.x, y.x, rs);
-                rs = fmaf(-x.y, y.y, rs);
-            }
-            v.s = rs;
+        float2 ey[NC > 0 ? NC : 1];  // this atom's E values, in flight during the real-space loop
+        if (NC > 0 && valid && (parts & 2)) {
+#pragma unroll
+            for (int n = 0; n < (NC > 0 ? NC : 1); ++n) ey[n] = erow[n];
         }
         if (valid && (parts & 1)) {
             const float4 *ih = img_hi + a * scap, *il = img_lo + a * scap;
@@ -562,8 +564,29 @@ __global__ void __launch_bounds__(kPhiPts) phi_chunk_kernel(
             v.s = s_;
             v.e = __fadd_rn(v.e, __fadd_rn(e_, x64l));
         }
+        if (valid && (parts & 2)) {  // stage C: Re sum_n1 ex[n1][i] E[row][a][n1]
+            float rs = 0.f;
+            if (NC > 0) {
+#pragma unroll
+                for (int n = 0; n < (NC > 0 ? NC : 1); ++n) {
+                    const float2 x = exs[n * kPhiPts + threadIdx.x];
+                    rs = fmaf(x.x, ey[n].x, rs);
+                    rs = fmaf(-x.y, ey[n].y, rs);
+                }
+            } else {
+                for (int n = 0; n < n1c; ++n) {
+                    const float2 x = exs[n * kPhiPts + threadIdx.x], y = erow[n];
+                    rs = fmaf(x.x, y.x, rs);
+                    rs = fmaf(-x.y, y.y, rs);
+                }
+            }
+            float s_, e_;
+            dfa::two_sum(v.s, rs, s_, e_);
+            v.s = s_;
+            v.e = __fadd_rn(v.e, e_);
+        }
         const float2 out = dfa::norm(v);
-        if (valid) phit[(long long)(a0 + a) * ld + m] = out;
+        if (valid) *prow = out;
         if (psum) {  // column statistics for the centre and the scale: FP32 is enough (any
                      // centre is corrected exactly; the max is exact)
             float sh = valid ? out.x : 0.f, mx = valid ? fabsf(out.x) : 0.f;
@@ -603,6 +626,7 @@ void launch_phi(const int32_t *kept, long long m0, long long rows, const double 
                 double *psum, float *pmax, cudaStream_t s) {
     RP_REQUIRE(S >= 1 && S <= kMaxShifts, "more than 128 real-space shifts after pruning (cutoff too large for the cell)");
     const int scap = (S + 31) / 32 * 32;
+    const bool regs = (n1c == 7);  // KMAX 7: the specialised kernel
     const size_t smem = phi_smem_bytes(n1c, scap);
     // the static shared memory (the statistics tile, ~18 KB) counts against the same 48 KB
     // default, so the opt-in is raised whenever the dynamic part could cross it
@@ -610,7 +634,8 @@ void launch_phi(const int32_t *kept, long long m0, long long rows, const double 
     if (smem > attr) {
         RP_REQUIRE(smem <= 192 * 1024, "phi kernel: KMAX too large for shared memory");
         const size_t want = std::max<size_t>(smem, 96 * 1024);
-        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
+        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
+        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
         attr = want;
     }
     AxisDF adf;
@@ -619,7 +644,7 @@ void launch_phi(const int32_t *kept, long long m0, long long rows, const double 
         adf.l[q] = (float)(h_axis[q] - (double)adf.h[q]);
     }
     dim3 grd(ceil_div(rows, kPhiPts), ceil_div(N, kPhiAtoms));
-    phi_chunk_kernel<<<grd, kPhiPts, smem, s>>>(kept, m0, rows, d_axis, adf, nx, ny, d_atoms, N, d_shifts, S, scap, zero_idx,
+    (regs ? phi_chunk_kernel<7> : phi_chunk_kernel<0>)<<<grd, kPhiPts, smem, s>>>(kept, m0, rows, d_axis, adf, nx, ny, d_atoms, N, d_shifts, S, scap, zero_idx,
                                                 rc, sa, (float)rc, (float)sa, real_near2(), img, EX, E, n1c, parts,
                                                 phit, ld, psum, pmax);
     RP_LAUNCH_CHECK();
