@@ -285,24 +285,48 @@ float real_near2() {
 
 // ------------------------------------------------------------------ Phi of one chunk
 
+// The approximate reciprocal, reciprocal square root and base-2 exponential of the
+// multi-function unit, flushing subnormals (the arguments here are normal numbers), so
+// that each is one instruction with no subnormal fix-up around it.
+__device__ __forceinline__ float rcp_ftz(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float ex2_ftz(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // erfc(x), x >= 0, in FP32 by the Chebyshev fit "erfcc" of Press, Teukolsky, Vetterling
 // and Flannery, Numerical Recipes in C (2nd ed., section 6.2): erfc(x) = t exp(-x^2 + P(t)),
-// t = 1/(1 + x/2), fractional error below 1.2e-7.  Evaluated with the fast reciprocal and
-// exponential it is ~15 instructions and, for the real-space range x = sqrt(alpha) r <= pi,
-// within 5e-7 (x < 1.5) and 1.3e-6 (x near pi, terms ~1e-6 of the largest) of FP64 erfc.
-__device__ __forceinline__ float erfc_nr(float x) {
-    const float t = __fdividef(1.0f, fmaf(0.5f, x, 1.0f));
-    float p = 0.17087277f;
-    p = fmaf(t, p, -0.82215223f);
-    p = fmaf(t, p, 1.48851587f);
-    p = fmaf(t, p, -1.13520398f);
-    p = fmaf(t, p, 0.27886807f);
-    p = fmaf(t, p, -0.18628806f);
-    p = fmaf(t, p, 0.09678418f);
-    p = fmaf(t, p, 0.37409196f);
-    p = fmaf(t, p, 1.00002368f);
-    p = fmaf(t, p, -1.26551223f);
-    return t * __expf(fmaf(-x, x, p));
+// t = 1/(1 + x/2), fractional error below 1.2e-7.  It is evaluated in base 2: the argument
+// comes pre-scaled, xs = sqrt(log2 e) x, and log2(e) is folded into the coefficients, so
+//   erfc(x) = t 2^(-xs^2 + log2(e) P(t)),   t = 1 / (1 + xs / (2 sqrt(log2 e))),
+// 14 instructions (one reciprocal, one exponential).  For the real-space range
+// x = sqrt(alpha) r <= pi it is within 5e-7 (x < 1.5) and 1.3e-6 (x near pi, terms ~1e-6
+// of the largest) of FP64 erfc.
+constexpr double kLog2e = 1.4426950408889634074;
+constexpr double kSqrtLog2e = 1.2011224087864498;  // sqrt(log2 e)
+__device__ __forceinline__ float erfc_nr2(float xs) {
+    const float t = rcp_ftz(fmaf((float)(0.5 / kSqrtLog2e), xs, 1.0f));
+    float p = (float)(kLog2e * 0.17087277);
+    p = fmaf(t, p, (float)(kLog2e * -0.82215223));
+    p = fmaf(t, p, (float)(kLog2e * 1.48851587));
+    p = fmaf(t, p, (float)(kLog2e * -1.13520398));
+    p = fmaf(t, p, (float)(kLog2e * 0.27886807));
+    p = fmaf(t, p, (float)(kLog2e * -0.18628806));
+    p = fmaf(t, p, (float)(kLog2e * 0.09678418));
+    p = fmaf(t, p, (float)(kLog2e * 0.37409196));
+    p = fmaf(t, p, (float)(kLog2e * 1.00002368));
+    p = fmaf(t, p, (float)(kLog2e * -1.26551223));
+    return t * ex2_ftz(fmaf(-xs, xs, p));
 }
 
 constexpr int kPhiPts = 128;     // points per CTA (one per thread)
@@ -514,7 +538,7 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
     // r <= Rc is made in FP64 (the reference's expressions); the term itself, ~erfc(pi)/Rc
     // there, is the FP32 one.  FP64 runs at 1/64 of the FP32 rate per lane on this part,
     // and one lane in the band makes its whole warp run the FP64 code, so it stays short.
-    const float rcc = rcf * rcf, band = 4e-6f * rcc, saf = saf_in;
+    const float rcc = rcf * rcf, band = 4e-6f * rcc, saf = saf_in;  // sqrt(alpha log2 e), the argument scale of erfc_nr2
     const float fp64_below = fmaxf(near2, 1e-6f);
     const long long row = f / nx;  // j + l * ny
     const float2 *erow = E + (row * N + a0) * (NC > 0 ? NC : n1c);
@@ -527,34 +551,46 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
 #pragma unroll
             for (int n = 0; n < (NC > 0 ? NC : 1); ++n) ey[n] = erow[n];
         }
-        if (valid && (parts & 1)) {
+        if (parts & 1) {  // every lane runs the loop (a lane past the end repeats the tile's first point)
             const float4 *ih = img_hi + a * scap, *il = img_lo + a * scap;
             const int nc = ncand[a];
             float acc32 = 0.f;
-            const float rej = rcc * 1.0001f + 1e-3f;  // hi parts alone decide clear misses
+            // Branch-free over the candidates: most of them are inside the cutoff for some lane of
+            // the warp, so the term is computed for all and selected.  Images whose decision needs
+            // FP64 (within the band around Rc, or on top of the point) are skipped here and taken
+            // in a second pass, which a warp runs only when one of its lanes met one.
+            bool spec_any = false;
             for (int c = 0; c < nc; ++c) {
-                const float4 h = ih[c];
+                const float4 h = ih[c], lo = il[c];
                 const float hx = gh[0] - h.x, hy = gh[1] - h.y, hz = gh[2] - h.z;
-                if (hx * hx + hy * hy + hz * hz > rej) continue;
-                const float4 lo = il[c];
                 const float dx = hx + (gl[0] - lo.x), dy = hy + (gl[1] - lo.y), dz = hz + (gl[2] - lo.z);
                 const float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 > rcc + band) continue;
-                if (r2 < fp64_below || r2 > rcc - band) {
+                const bool ok = r2 >= fp64_below && r2 <= rcc - band;
+                spec_any |= !ok && r2 <= rcc + band;
+                const float rinv = rsqrt_ftz(r2);
+                const float t = fmaf(erfc_nr2(saf * (r2 * rinv)), rinv, acc32);
+                acc32 = ok ? t : acc32;
+            }
+            if (__any_sync(0xffffffffu, spec_any)) {
+                for (int c = 0; c < nc; ++c) {
+                    const float4 h = ih[c], lo = il[c];
+                    const float hx = gh[0] - h.x, hy = gh[1] - h.y, hz = gh[2] - h.z;
+                    const float dx = hx + (gl[0] - lo.x), dy = hy + (gl[1] - lo.y), dz = hz + (gl[2] - lo.z);
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    if (!(r2 < fp64_below || (r2 > rcc - band && r2 <= rcc + band))) continue;
                     float th, tl;
                     const int dec = fp64_pair(axis, i, j, l, atoms + 3 * (a0 + a), shifts, __float_as_int(h.w),
                                               zero_idx, rc, sa, r2 < fp64_below, th, tl);
-                    if (dec == 0) continue;
-                    if (dec == 2) {  // a point on top of an image: the large term in FP64
+                    if (dec == 1) {  // inside the cutoff: the FP32 term
+                        const float rinv = rsqrt_ftz(r2);
+                        acc32 = fmaf(erfc_nr2(saf * (r2 * rinv)), rinv, acc32);
+                    } else if (dec == 2) {  // a point on top of an image: the large term in FP64
                         float s2, e2;
                         dfa::two_sum(x64h, th, s2, e2);
                         x64h = s2;
                         x64l = __fadd_rn(x64l, __fadd_rn(e2, tl));
-                        continue;
                     }
                 }
-                const float rinv = rsqrtf(r2);
-                acc32 = fmaf(erfc_nr(saf * (r2 * rinv)), rinv, acc32);
             }
             float s_, e_;
             dfa::two_sum(v.s, acc32, s_, e_);
@@ -645,7 +681,7 @@ void launch_phi(const int32_t *kept, long long m0, long long rows, const double 
     }
     dim3 grd(ceil_div(rows, kPhiPts), ceil_div(N, kPhiAtoms));
     (regs ? phi_chunk_kernel<7> : phi_chunk_kernel<0>)<<<grd, kPhiPts, smem, s>>>(kept, m0, rows, d_axis, adf, nx, ny, d_atoms, N, d_shifts, S, scap, zero_idx,
-                                                rc, sa, (float)rc, (float)sa, real_near2(), img, EX, E, n1c, parts,
+                                                rc, sa, (float)rc, (float)(sa * kSqrtLog2e), real_near2(), img, EX, E, n1c, parts,
                                                 phit, ld, psum, pmax);
     RP_LAUNCH_CHECK();
 }

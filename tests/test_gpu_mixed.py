@@ -39,11 +39,13 @@ def test_mixed_normal_equations_close_to_fp64(name, gpu_ctx):
     assert np.abs(bm - b64).max() <= 1e-6 * np.abs(b64).max()
 
 
-@pytest.mark.parametrize("name", ["water24", "tricmini"])
-def test_mixed_phi_parts_match_oracle(name, gpu_ctx, oracle_mod):
+@pytest.mark.parametrize("name,order", [("water24", "flat"), ("tricmini", "flat"), ("tricmini", "shuffled")])
+def test_mixed_phi_parts_match_oracle(name, order, gpu_ctx, oracle_mod):
     """Each part of the mixed Phi against the oracle's FP64 Phi on the same kept points.
     Both parts carry FP32 rounding (the real-space terms, reciprocal stages B and C),
-    so the bound is 1e-6 of max|Phi| (measured 2-4e-7)."""
+    so the bound is 1e-6 of max|Phi| (measured 2-4e-7).  The kernel takes the points in
+    any order (the batched fit passes them brick by brick); a shuffled order gives every
+    128-point tile a bounding box of the whole cell, the widest image culling."""
     import torch
     L = gpu_ctx.lib
     L.rp_debug_mixed_phi.restype = ctypes.c_int
@@ -54,9 +56,14 @@ def test_mixed_phi_parts_match_oracle(name, gpu_ctx, oracle_mod):
     kept, Vc, M, _ = gpu_ctx.filter(cube.n_grid, cube.axis_vector, cube.atom_pos, cube.atom_index, V)
     ew = gpu_ctx.ewald(cube.n_grid, cube.axis_vector, cube.cutoff, cube.kmax)
     of = oracle_mod.OracleFit(cube)
+    grid = of.grid
+    if order == "shuffled":
+        perm = np.random.default_rng(5).permutation(M)
+        kept = kept[torch.from_numpy(perm).cuda()].contiguous()
+        grid = grid[perm]
     atoms = np.ascontiguousarray(cube.atom_pos, dtype=np.float64)
-    real_ref = oracle_mod.phi(of.grid, atoms, of.kv[:0], of.kc[:0], of.shifts, of.zero_idx, cube.cutoff)
-    rec_ref = oracle_mod.phi(of.grid, atoms, of.kv, of.kc, of.shifts[:0], -1, cube.cutoff)
+    real_ref = oracle_mod.phi(grid, atoms, of.kv[:0], of.kc[:0], of.shifts, of.zero_idx, cube.cutoff)
+    rec_ref = oracle_mod.phi(grid, atoms, of.kv, of.kc, of.shifts[:0], -1, cube.cutoff)
     N = len(atoms)
     for parts, ref, tol in ((1, real_ref, 1e-6), (2, rec_ref, 1e-6), (3, real_ref + rec_ref, 1e-6)):
         out = torch.zeros((N, M), dtype=torch.float64, device="cuda")
