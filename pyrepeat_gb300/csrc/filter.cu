@@ -200,46 +200,37 @@ __global__ void __launch_bounds__(kFilterThreads) compact_kernel(
     }
 }
 
-// Brick-ordered compaction: bricks of 4 x 4 x 4 grid points (one CTA of 64 threads each,
-// points x fastest inside a brick), bricks in Morton (Z-curve) order inside tiles of
-// 8 x 8 x 8 bricks, tiles in x-then-y-then-z order.  The kept points of a brick are
-// contiguous and consecutive bricks are neighbours at every scale, so any 128 consecutive
-// kept points span a near-cubic region of the cell: the real-space culling of the mixed
-// fit keeps ~20% fewer images than for bricks taken row by row.  Deterministic (ballots
-// only).
-constexpr int kBrickX = 4, kBrickY = 4, kBrickZ = 4;
-constexpr int kBrickPts = kBrickX * kBrickY * kBrickZ;  // 64
-constexpr int kTileBricks = 8;                          // Morton tiles of 8^3 bricks (9 bits)
+// Brick-ordered compaction: bricks of 8 x 4 x 4 grid points (one CTA of 128 threads
+// each, x fastest), bricks in x-then-y-then-z order, points inside a brick in the
+// same order.  The kept points of a brick are contiguous, so any 128 consecutive
+// kept points span a compact region of the cell (the real-space culling of the
+// mixed fit keeps fewer images for compact tiles).  Deterministic (ballots only).
+constexpr int kBrickX = 8, kBrickY = 4, kBrickZ = 4;
+constexpr int kBrickPts = kBrickX * kBrickY * kBrickZ;  // 128
 
-// bits 0, 3, 6 of v as bits 0, 1, 2
-__device__ __forceinline__ int morton_compact3(int v) { return (v & 1) | ((v >> 2) & 2) | ((v >> 4) & 4); }
-
-// brick b (tile-major, Morton inside a tile), thread t -> flat grid index, or -1 outside
-__device__ __forceinline__ long long brick_point(int b, int t, int nx, int ny, int nz, int ntx, int nty) {
-    const int tile = b >> 9, w = b & 511;
-    const int tx = tile % ntx, ty = (tile / ntx) % nty, tz = tile / (ntx * nty);
-    const int bx = tx * kTileBricks + morton_compact3(w), by = ty * kTileBricks + morton_compact3(w >> 1),
-              bz = tz * kTileBricks + morton_compact3(w >> 2);
-    const int i = bx * kBrickX + (t & 3), j = by * kBrickY + ((t >> 2) & 3), l = bz * kBrickZ + (t >> 4);
+__device__ __forceinline__ long long brick_point(int b, int t, int nx, int ny, int nz, int nbx, int nby) {
+    const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+    const int i = bx * kBrickX + (t % kBrickX), j = by * kBrickY + ((t / kBrickX) % kBrickY),
+              l = bz * kBrickZ + t / (kBrickX * kBrickY);
     if (i >= nx || j >= ny || l >= nz) return -1;
     return (long long)i + (long long)nx * (j + (long long)ny * l);
 }
 
 __global__ void __launch_bounds__(kBrickPts) brick_count_kernel(const uint8_t *__restrict__ mask, int nx, int ny,
-                                                                int nz, int ntx, int nty, int *__restrict__ counts) {
-    const long long f = brick_point(blockIdx.x, threadIdx.x, nx, ny, nz, ntx, nty);
+                                                                int nz, int nbx, int nby, int *__restrict__ counts) {
+    const long long f = brick_point(blockIdx.x, threadIdx.x, nx, ny, nz, nbx, nby);
     const int keep = (f >= 0) ? mask[f] : 0;
     const int cnt = __syncthreads_count(keep);
     if (threadIdx.x == 0) counts[blockIdx.x] = cnt;
 }
 
 __global__ void __launch_bounds__(kBrickPts) brick_compact_kernel(
-    const uint8_t *__restrict__ mask, const double *__restrict__ V, int nx, int ny, int nz, int ntx, int nty,
+    const uint8_t *__restrict__ mask, const double *__restrict__ V, int nx, int ny, int nz, int nbx, int nby,
     const long long *__restrict__ offsets, long long capacity, int32_t *__restrict__ kept_idx,
     double *__restrict__ Vc, double *__restrict__ block_vsum) {
     __shared__ int warp_base[kBrickPts / 32];
     __shared__ double warp_sum[kBrickPts / 32];
-    const long long f = brick_point(blockIdx.x, threadIdx.x, nx, ny, nz, ntx, nty);
+    const long long f = brick_point(blockIdx.x, threadIdx.x, nx, ny, nz, nbx, nby);
     const int keep = (f >= 0) ? mask[f] : 0;
     const double v = keep ? V[f] : 0.0;
     const unsigned bal = __ballot_sync(0xffffffffu, keep);
@@ -546,18 +537,17 @@ void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const i
         vmean_kernel<<<1, 1024, 0, stream>>>(d_vsum, nblk, d_total, d_mean);
         RP_LAUNCH_CHECK();
     } else {
-        constexpr int kTilePts = kTileBricks * kBrickX;  // 32 grid points per tile edge
-        const int ntx = (nx + kTilePts - 1) / kTilePts, nty = (ny + kTilePts - 1) / kTilePts,
-                  ntz = (nz + kTilePts - 1) / kTilePts;  // tiles per axis
-        const int nbr = ntx * nty * ntz * kTileBricks * kTileBricks * kTileBricks;
+        const int nbx = (nx + kBrickX - 1) / kBrickX, nby = (ny + kBrickY - 1) / kBrickY,
+                  nbz = (nz + kBrickZ - 1) / kBrickZ;
+        const int nbr = nbx * nby * nbz;
         int *d_bc = ctx->buf_t<int>("flt_bcounts" + tag, (size_t)nbr);
         long long *d_bo = ctx->buf_t<long long>("flt_boffsets" + tag, (size_t)nbr);
         double *d_bv = ctx->buf_t<double>("flt_bvsum" + tag, (size_t)nbr);
-        brick_count_kernel<<<nbr, kBrickPts, 0, stream>>>(d_mask, nx, ny, nz, ntx, nty, d_bc);
+        brick_count_kernel<<<nbr, kBrickPts, 0, stream>>>(d_mask, nx, ny, nz, nbx, nby, d_bc);
         RP_LAUNCH_CHECK();
         scan_counts_kernel<<<1, 1024, 0, stream>>>(d_bc, nbr, d_bo, d_total);
         RP_LAUNCH_CHECK();
-        brick_compact_kernel<<<nbr, kBrickPts, 0, stream>>>(d_mask, V_dev, nx, ny, nz, ntx, nty, d_bo, capacity,
+        brick_compact_kernel<<<nbr, kBrickPts, 0, stream>>>(d_mask, V_dev, nx, ny, nz, nbx, nby, d_bo, capacity,
                                                             kept_idx_dev, Vc_dev, d_bv);
         RP_LAUNCH_CHECK();
         vmean_kernel<<<1, 1024, 0, stream>>>(d_bv, nbr, d_total, d_mean);

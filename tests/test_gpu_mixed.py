@@ -39,7 +39,20 @@ def test_mixed_normal_equations_close_to_fp64(name, gpu_ctx):
     assert np.abs(bm - b64).max() <= 1e-6 * np.abs(b64).max()
 
 
-@pytest.mark.parametrize("name,order", [("water24", "flat"), ("tricmini", "flat"), ("tricmini", "shuffled")])
+def _brick_order(kept, n_grid):
+    """The batched fit's point order: bricks of 8 x 4 x 4 grid points, x fastest, bricks
+    row by row, points inside a brick in the same order."""
+    nx, ny, _nz = (int(v) for v in n_grid)
+    f = kept.astype(np.int64)
+    k, j, i = f // (nx * ny), (f // nx) % ny, f % nx
+    nbx, nby = (nx + 7) // 8, (ny + 3) // 4
+    brick = (i // 8) + nbx * ((j // 4) + nby * (k // 4))
+    inner = (i % 8) + 8 * ((j % 4) + 4 * (k % 4))
+    return np.lexsort((inner, brick))
+
+
+@pytest.mark.parametrize("name,order", [("water24", "flat"), ("tricmini", "flat"), ("tricmini", "shuffled"),
+                                        ("tricmini", "brick"), ("mofmini", "brick")])
 def test_mixed_phi_parts_match_oracle(name, order, gpu_ctx, oracle_mod):
     """Each part of the mixed Phi against the oracle's FP64 Phi on the same kept points.
     Both parts carry FP32 rounding (the real-space terms, reciprocal stages B and C),
@@ -57,8 +70,9 @@ def test_mixed_phi_parts_match_oracle(name, order, gpu_ctx, oracle_mod):
     ew = gpu_ctx.ewald(cube.n_grid, cube.axis_vector, cube.cutoff, cube.kmax)
     of = oracle_mod.OracleFit(cube)
     grid = of.grid
-    if order == "shuffled":
-        perm = np.random.default_rng(5).permutation(M)
+    if order != "flat":
+        perm = (np.random.default_rng(5).permutation(M) if order == "shuffled"
+                else _brick_order(kept.cpu().numpy(), cube.n_grid))
         kept = kept[torch.from_numpy(perm).cuda()].contiguous()
         grid = grid[perm]
     atoms = np.ascontiguousarray(cube.atom_pos, dtype=np.float64)
