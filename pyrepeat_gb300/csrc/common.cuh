@@ -8,7 +8,10 @@
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
+#include <exception>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -183,6 +186,38 @@ void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax);  /
 void ewald_free(rp_ewald *ew);
 
 // Host helpers shared by the stages.
+
+// f(i) for i in [0, n) on up to 16 host threads (the cubes of a batch are independent);
+// the first exception thrown is rethrown on the calling thread once all have joined.
+template <class F>
+void parallel_for(int n, F &&f) {
+    const int hw = std::max(1, (int)std::thread::hardware_concurrency());
+    const int nt = std::min(n, std::min(16, hw));
+    if (nt <= 1) {
+        for (int i = 0; i < n; ++i) f(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::exception_ptr err;
+    std::mutex mu;
+    auto work = [&] {
+        for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1)) {
+            try {
+                f(i);
+            } catch (...) {
+                std::lock_guard<std::mutex> g(mu);
+                if (!err) err = std::current_exception();
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    th.reserve((size_t)nt - 1);
+    for (int t = 1; t < nt; ++t) th.emplace_back(work);
+    work();
+    for (auto &t : th) t.join();
+    if (err) std::rethrow_exception(err);
+}
+
 void prune_shifts(const rp_ewald *ew, const double *atoms, int N, std::vector<double> &out, int &zero_idx);
 
 // Device status words: [0] a bounded wait ran out, [1] fixed-point range overflows.
@@ -193,6 +228,46 @@ void status_check(rp_ctx *ctx, cudaStream_t s);  // synchronises s
 void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
                 double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, int64_t capacity,
                 int64_t *M_out, uint8_t *mask_dev, cudaStream_t stream);
+// x, y, z and a squared radius, FP64 (32-byte aligned for one vector load)
+struct alignas(32) D4 {
+    double x, y, z, w;
+};
+
+// Launch parameters of the vdW mask kernel.
+struct FilterParams {
+    int nx, ny, nz;
+    long long n_total;
+    float ax[9];
+    double axd[9];
+    float bmin[3];
+    float inv_bsize;
+    int bn[3];
+    float err_min;   // FP32 band around rmin^2
+    float err_max;   // FP32 band around rmax^2
+    int near_all;
+    int A;
+};
+
+// Host half of one cube's vdW filter: the effective atoms (repeat.py:1933-1969), the
+// FP32 error bands and the cell list, computed without touching the device, so that a
+// batch plans its cubes on several threads and uploads every plan with one copy.
+struct FilterPlan {
+    FilterParams p{};
+    std::vector<float4> e32;
+    std::vector<D4> e64;
+    std::vector<double> rmax2;
+    std::vector<float> rmax2f;
+    std::vector<int> boff, bidx;
+    size_t bytes() const;        // packed size: the arrays in order, each at a 32-byte offset
+    void pack(char *dst) const;  // host image of the packed arrays
+};
+void filter_plan(const rp_grid *grid, const double *atoms, const int *Z, int N, double vdw_factor, double vdw_max,
+                 FilterPlan &plan);
+// Device half: mask, compaction and centring from a plan whose packed image is at
+// packed_dev (same stream order as the copy that put it there).
+void filter_launch(rp_ctx *ctx, const FilterPlan &plan, const char *packed_dev, const double *V_dev,
+                   int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev, uint8_t *mask_dev, cudaStream_t stream,
+                   const std::string &tag, bool brick_order, double *vstats_dev);
 // Asynchronous form: the kept count lands in *M_dev; kept_idx_dev and Vc_dev hold a
 // whole grid (capacity = nx*ny*nz).  `tag` keeps the scratch of concurrent calls apart.
 // brick_order: kept points in 8x4x4 brick order instead of flat order (the mixed fit

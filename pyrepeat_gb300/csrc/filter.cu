@@ -31,24 +31,6 @@ namespace {
 
 constexpr int kFilterThreads = 256;
 
-// x, y, z and a squared radius, FP64 (32-byte aligned for one vector load)
-struct alignas(32) D4 {
-    double x, y, z, w;
-};
-
-struct FilterParams {
-    int nx, ny, nz;
-    long long n_total;
-    float ax[9];
-    double axd[9];
-    float bmin[3];
-    float inv_bsize;
-    int bn[3];
-    float err_min;   // FP32 band around rmin^2
-    float err_max;   // FP32 band around rmax^2
-    int near_all;
-    int A;
-};
 
 // Not inlined on purpose: the call sits in a branch that almost never runs, and as an
 // inlined body the compiler may evaluate it speculatively for every candidate, which puts
@@ -352,12 +334,9 @@ double radius_of(int z) {
 
 }  // namespace
 
-void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
-                  double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev,
-                  uint8_t *mask_dev, cudaStream_t stream, const std::string &tag, bool brick_order,
-                  double *vstats_dev) {
-    RP_REQUIRE(grid && atoms && Z && V_dev && M_dev, "rp_filter: null argument");
-    const long long capacity = (long long)grid->n_grid[0] * grid->n_grid[1] * grid->n_grid[2];
+void filter_plan(const rp_grid *grid, const double *atoms, const int *Z, int N, double vdw_factor, double vdw_max,
+                 FilterPlan &plan) {
+    RP_REQUIRE(grid && atoms && Z, "rp_filter: null argument");
     RP_REQUIRE(N >= 0, "rp_filter: N < 0");
     const int nx = grid->n_grid[0], ny = grid->n_grid[1], nz = grid->n_grid[2];
     RP_REQUIRE(nx > 0 && ny > 0 && nz > 0, "rp_filter: grid counts must be positive");
@@ -492,31 +471,9 @@ void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const i
         bidx[t] = t;
     }
 
-    // ---- upload (ctx scratch) and launch
-    const int nblk = (int)((n_total + kFilterThreads - 1) / kFilterThreads);
-    float4 *d_e32 = ctx->buf_t<float4>("flt_e32" + tag, e32.size());
-    D4 *d_e64 = ctx->buf_t<D4>("flt_e64" + tag, e64s.size());
-    double *d_rmax2 = ctx->buf_t<double>("flt_rmax2" + tag, rmax2s.size());
-    float *d_rmax2f = ctx->buf_t<float>("flt_rmax2f" + tag, rmax2f.size());
-    int *d_boff = ctx->buf_t<int>("flt_boff" + tag, boff.size());
-    int *d_bidx = ctx->buf_t<int>("flt_bidx" + tag, bidx.size());
-    uint8_t *d_mask = mask_dev ? mask_dev : ctx->buf_t<uint8_t>("flt_mask" + tag, (size_t)n_total);
-    int *d_counts = ctx->buf_t<int>("flt_counts" + tag, (size_t)nblk);
-    long long *d_offsets = ctx->buf_t<long long>("flt_offsets" + tag, (size_t)nblk);
-    double *d_vsum = ctx->buf_t<double>("flt_vsum" + tag, (size_t)nblk);
-    long long *d_total = M_dev;
-    double *d_mean = ctx->buf_t<double>("flt_mean" + tag, 1);
-    unsigned long long *d_re = ctx->buf_t<unsigned long long>("flt_rechecks" + tag, 1);
-    RP_CUDA(cudaMemcpyAsync(d_e32, e32.data(), e32.size() * sizeof(float4), cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemcpyAsync(d_e64, e64s.data(), e64s.size() * sizeof(D4), cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemcpyAsync(d_rmax2, rmax2s.data(), rmax2s.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemcpyAsync(d_rmax2f, rmax2f.data(), rmax2f.size() * sizeof(float), cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemcpyAsync(d_boff, boff.data(), boff.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemcpyAsync(d_bidx, bidx.data(), bidx.size() * sizeof(int), cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemsetAsync(d_re, 0, sizeof(unsigned long long), stream));
-
-    StageTimer t_f(ctx, "filter", stream);
-    FilterParams p{};
+    // FP32 copies, ordered by bin (above); the launch parameters
+    FilterParams &p = plan.p;
+    p = FilterParams{};
     p.nx = nx; p.ny = ny; p.nz = nz; p.n_total = n_total;
     for (int t = 0; t < 9; ++t) { p.ax[t] = (float)ax[t]; p.axd[t] = ax[t]; }
     for (int d = 0; d < 3; ++d) { p.bmin[d] = (float)bmin[d]; p.bn[d] = bn[d]; }
@@ -525,6 +482,67 @@ void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const i
     p.err_max = (float)err_max;
     p.near_all = near_all;
     p.A = A;
+    plan.e32 = std::move(e32);
+    plan.e64 = std::move(e64s);
+    plan.rmax2 = std::move(rmax2s);
+    plan.rmax2f = std::move(rmax2f);
+    plan.boff = std::move(boff);
+    plan.bidx = std::move(bidx);
+}
+
+namespace {
+// every packed array starts on a 32-byte boundary: D4 is read with one 32-byte vector load
+size_t al32(size_t n) { return (n + 31) / 32 * 32; }
+}  // namespace
+
+size_t FilterPlan::bytes() const {
+    return al32(e32.size() * sizeof(float4)) + al32(e64.size() * sizeof(D4)) + al32(rmax2.size() * sizeof(double)) +
+           al32(rmax2f.size() * sizeof(float)) + al32(boff.size() * sizeof(int)) + al32(bidx.size() * sizeof(int));
+}
+
+void FilterPlan::pack(char *dst) const {
+    auto put = [&](const void *src, size_t n) {
+        std::memcpy(dst, src, n);
+        dst += al32(n);
+    };
+    put(e32.data(), e32.size() * sizeof(float4));
+    put(e64.data(), e64.size() * sizeof(D4));
+    put(rmax2.data(), rmax2.size() * sizeof(double));
+    put(rmax2f.data(), rmax2f.size() * sizeof(float));
+    put(boff.data(), boff.size() * sizeof(int));
+    put(bidx.data(), bidx.size() * sizeof(int));
+}
+
+void filter_launch(rp_ctx *ctx, const FilterPlan &plan, const char *packed_dev, const double *V_dev,
+                   int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev, uint8_t *mask_dev, cudaStream_t stream,
+                   const std::string &tag, bool brick_order, double *vstats_dev) {
+    RP_REQUIRE(V_dev && M_dev && packed_dev, "rp_filter: null argument");
+    const FilterParams &p = plan.p;
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const long long n_total = p.n_total, capacity = n_total;
+    const char *src = packed_dev;
+    auto take = [&](size_t n) {
+        const char *r = src;
+        src += al32(n);
+        return r;
+    };
+    const float4 *d_e32 = reinterpret_cast<const float4 *>(take(plan.e32.size() * sizeof(float4)));
+    const D4 *d_e64 = reinterpret_cast<const D4 *>(take(plan.e64.size() * sizeof(D4)));
+    const double *d_rmax2 = reinterpret_cast<const double *>(take(plan.rmax2.size() * sizeof(double)));
+    const float *d_rmax2f = reinterpret_cast<const float *>(take(plan.rmax2f.size() * sizeof(float)));
+    const int *d_boff = reinterpret_cast<const int *>(take(plan.boff.size() * sizeof(int)));
+    const int *d_bidx = reinterpret_cast<const int *>(take(plan.bidx.size() * sizeof(int)));
+    const int nblk = (int)((n_total + kFilterThreads - 1) / kFilterThreads);
+    uint8_t *d_mask = mask_dev ? mask_dev : ctx->buf_t<uint8_t>("flt_mask" + tag, (size_t)n_total);
+    int *d_counts = ctx->buf_t<int>("flt_counts" + tag, (size_t)nblk);
+    long long *d_offsets = ctx->buf_t<long long>("flt_offsets" + tag, (size_t)nblk);
+    double *d_vsum = ctx->buf_t<double>("flt_vsum" + tag, (size_t)nblk);
+    long long *d_total = M_dev;
+    double *d_mean = ctx->buf_t<double>("flt_mean" + tag, 1);
+    unsigned long long *d_re = ctx->buf_t<unsigned long long>("flt_rechecks" + tag, 1);
+    RP_CUDA(cudaMemsetAsync(d_re, 0, sizeof(unsigned long long), stream));
+
+    StageTimer t_f(ctx, "filter", stream);
     filter_mask_kernel<<<nblk, kFilterThreads, 0, stream>>>(p, d_e32, d_e64, d_rmax2, d_rmax2f, d_boff, d_bidx,
                                                             d_mask, d_counts, d_re);
     RP_LAUNCH_CHECK();
@@ -561,6 +579,21 @@ void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const i
         vstats_kernel<<<1, 32, 0, stream>>>(d_part, ncb, vstats_dev);
         RP_LAUNCH_CHECK();
     }
+}
+
+void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,
+                  double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev,
+                  uint8_t *mask_dev, cudaStream_t stream, const std::string &tag, bool brick_order,
+                  double *vstats_dev) {
+    RP_REQUIRE(grid && atoms && Z && V_dev && M_dev, "rp_filter: null argument");
+    FilterPlan plan;
+    filter_plan(grid, atoms, Z, N, vdw_factor, vdw_max, plan);
+    std::vector<char> host(plan.bytes());
+    plan.pack(host.data());
+    char *dev = static_cast<char *>(ctx->buf("flt_plan" + tag, host.size()));
+    RP_CUDA(cudaMemcpyAsync(dev, host.data(), host.size(), cudaMemcpyHostToDevice, stream));
+    filter_launch(ctx, plan, dev, V_dev, kept_idx_dev, Vc_dev, M_dev, mask_dev, stream, tag, brick_order,
+                  vstats_dev);
 }
 
 void filter_run(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,

@@ -200,24 +200,13 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             off_n[i + 1] = off_n[i] + d.N;
             off_nn[i + 1] = off_nn[i] + (long long)d.N * d.N;
         }
-        // Ewald tables of every cube: built on the host, placed in one ctx arena and
-        // uploaded with a single copy from pinned memory (no per-fit allocation)
-        size_t ew_total = 0;
-        std::vector<size_t> ew_off((size_t)n);
-        for (int i = 0; i < n; ++i) {
-            ews[i] = new rp_ewald();
-            ews[i]->device = ctx->device;
-            rp::ewald_build_host(ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax);
-            ew_off[i] = ew_total;
-            ew_total += rp::ewald_device_bytes(ews[i]);
-        }
-        char *ew_dev = static_cast<char *>(ctx->buf("fit_ewald", ew_total));
-        char *ew_host = static_cast<char *>(ctx->host_buf("fit_ewald", ew_total));
-        for (int i = 0; i < n; ++i) {
-            std::memcpy(ew_host + ew_off[i], ews[i]->image.data(), ews[i]->image.size());
-            rp::ewald_place(ews[i], ew_dev + ew_off[i]);
-        }
-        RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, ew_total, cudaMemcpyHostToDevice, stream));
+        // Work splits into host preparation and device stages so that the device never waits
+        // on the host inside the batch: (1) the filters' host halves, on all host threads,
+        // one pinned upload, and the filter launches spread over the lanes; (2) while they
+        // run, the Ewald tables of every cube, on all host threads, one pinned upload;
+        // (3) one read of the kept counts, which sizes every later launch.
+        constexpr int kLanes = 4;
+        const int lanes = ctx->timing ? 1 : kLanes;  // stage timing: one lane, each stage alone
         int32_t *kept = ctx->buf_t<int32_t>("fit_kept", (size_t)off_pts[n]);
         double *Vc = ctx->buf_t<double>("fit_Vc", (size_t)off_pts[n]);
         double *Vh = nullptr;
@@ -230,38 +219,82 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
         double *q = ctx->buf_t<double>("fit_q", (size_t)off_n[n]);
         double *vst = ctx->buf_t<double>("fit_vstats", 2 * (size_t)n);
         rp::status_clear(ctx, stream);
-        // 1. filters (asynchronous; kept counts stay on the device)
+        // 1. filters
+        std::vector<rp::FilterPlan> plans((size_t)n);
+        rp::parallel_for(n, [&](int i) {
+            const rp_fit_desc &d = descs[i];
+            rp::filter_plan(&d.grid, d.atoms, d.Z, d.N, d.vdw_factor, d.vdw_max, plans[i]);
+        });
+        std::vector<size_t> pl_off((size_t)n + 1, 0);
+        for (int i = 0; i < n; ++i) pl_off[i + 1] = pl_off[i] + plans[i].bytes();
+        char *pl_dev = static_cast<char *>(ctx->buf("fit_filter", pl_off[n]));
+        char *pl_host = static_cast<char *>(ctx->host_buf("fit_filter", pl_off[n]));
+        rp::parallel_for(n, [&](int i) { plans[i].pack(pl_host + pl_off[i]); });
+        RP_CUDA(cudaMemcpyAsync(pl_dev, pl_host, pl_off[n], cudaMemcpyHostToDevice, stream));
+        for (int i = 0; i < n; ++i)
+            if (!(V_dev && V_dev[i]))
+                RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], descs[i].V, sizeof(double) * npts[i],
+                                        cudaMemcpyHostToDevice, stream));
+        auto fork = [&] {  // every lane waits for what the caller's stream holds so far
+            cudaEvent_t ev;
+            RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            RP_CUDA(cudaEventRecord(ev, stream));
+            for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(ctx->lane(ln), ev, 0));
+            RP_CUDA(cudaEventDestroy(ev));
+        };
+        auto join = [&] {  // the caller's stream waits for every lane
+            for (int ln = 0; ln < lanes; ++ln) {
+                cudaEvent_t ev;
+                RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                RP_CUDA(cudaEventRecord(ev, ctx->lane(ln)));
+                RP_CUDA(cudaStreamWaitEvent(stream, ev, 0));
+                RP_CUDA(cudaEventDestroy(ev));
+            }
+        };
+        fork();
         for (int i = 0; i < n; ++i) {
             const rp_fit_desc &d = descs[i];
             const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
-            if (!(V_dev && V_dev[i]))
-                RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], d.V, sizeof(double) * npts[i], cudaMemcpyHostToDevice, stream));
-            rp::filter_async(ctx, &d.grid, d.atoms, d.Z, d.N, V, d.vdw_factor, d.vdw_max, kept + off_pts[i],
-                             Vc + off_pts[i], Md + i, nullptr, stream, "", d.precision == RP_PREC_MIXED,
-                             vst + 2 * i);
+            const int ln = i % lanes;
+            rp::filter_launch(ctx, plans[i], pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i], Md + i,
+                              nullptr, ctx->lane(ln), "#" + std::to_string(ln), d.precision == RP_PREC_MIXED,
+                              vst + 2 * i);
         }
-        // 2. one read of all kept counts (sizes every later launch)
+        join();
         std::vector<long long> M((size_t)n);
         RP_CUDA(cudaMemcpyAsync(M.data(), Md, sizeof(long long) * n, cudaMemcpyDeviceToHost, stream));
+        // 2. Ewald tables, placed in one ctx arena, uploaded with a single copy
+        std::vector<size_t> ew_off((size_t)n + 1, 0);
+        for (int i = 0; i < n; ++i) {
+            ews[i] = new rp_ewald();
+            ews[i]->device = ctx->device;
+        }
+        rp::parallel_for(n, [&](int i) {
+            rp::ewald_build_host(ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax);
+        });
+        for (int i = 0; i < n; ++i) ew_off[i + 1] = ew_off[i] + rp::ewald_device_bytes(ews[i]);
+        char *ew_dev = static_cast<char *>(ctx->buf("fit_ewald", ew_off[n]));
+        char *ew_host = static_cast<char *>(ctx->host_buf("fit_ewald", ew_off[n]));
+        rp::parallel_for(n, [&](int i) {
+            std::memcpy(ew_host + ew_off[i], ews[i]->image.data(), ews[i]->image.size());
+        });
+        for (int i = 0; i < n; ++i) rp::ewald_place(ews[i], ew_dev + ew_off[i]);
+        RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, ew_off[n], cudaMemcpyHostToDevice, stream));
+        // 3. the kept counts (and the tables) are on hand after one synchronisation
         RP_CUDA(cudaStreamSynchronize(stream));
         for (int i = 0; i < n; ++i) {
             if (M_out) M_out[i] = M[i];
             RP_REQUIRE(M[i] > 0, "rp_fit: no grid point of cube " + std::to_string(i) + " survives the vdW filter");
         }
-        // 3. normal equations of every cube.  Mixed-precision fits are spread over kLanes
-        //    worker streams (each with its own scratch), so one cube's small kernels and
-        //    launch gaps overlap another's; the FP64 comparator stays on the caller's
+        // 4. normal equations of every cube.  Mixed-precision fits are spread over the
+        //    lanes (worker streams, each with its own scratch), so one cube's small kernels
+        //    and launch gaps overlap another's; the FP64 comparator stays on the caller's
         //    stream (its cuBLAS handle is shared).  Every cube's result is independent of
         //    the lane it ran on.
-        //    With stage timing on, one lane: the timers then measure each stage alone.
-        constexpr int kLanes = 4;
-        const int lanes = ctx->timing ? 1 : kLanes;
-        bool used[kLanes] = {false, false, false, false};
         for (int i = 0; i < n; ++i) {
             const rp_fit_desc &d = descs[i];
             if (d.precision == RP_PREC_MIXED) {
                 const int ln = i % lanes;
-                used[ln] = true;
                 rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
                                b + off_n[i], nullptr, ctx->lane(ln), vst + 2 * i, "#" + std::to_string(ln));
             } else {
@@ -269,15 +302,8 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
                               b + off_n[i], nullptr, stream);
             }
         }
-        for (int ln = 0; ln < kLanes; ++ln)
-            if (used[ln]) {  // the solve on the caller's stream waits for every lane
-                cudaEvent_t ev;
-                RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-                RP_CUDA(cudaEventRecord(ev, ctx->lane(ln)));
-                RP_CUDA(cudaStreamWaitEvent(stream, ev, 0));
-                RP_CUDA(cudaEventDestroy(ev));
-            }
-        // 4. all constraint folds and bordered solves, one launch
+        join();  // the solve on the caller's stream waits for every lane
+        // 5. all constraint folds and bordered solves, one launch
         std::vector<rp::SolveJob> jobs((size_t)n);
         for (int i = 0; i < n; ++i) {
             const rp_fit_desc &d = descs[i];
