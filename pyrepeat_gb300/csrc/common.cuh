@@ -113,6 +113,8 @@ struct rp_ctx {
     // Grow-only pinned host staging buffer (one H2D copy per batch instead of many
     // small pageable ones); callers synchronise their stream before it is reused.
     std::unordered_map<std::string, rp::Buffer> host_scratch;
+    double bound_scale = 1.0;  // factor on the single-pass Phi bounds (tests shrink it to force clamps)
+    int last_fallbacks = 0;    // cubes of the last batch redone in two passes after a clamp
     void *host_buf(const std::string &name, size_t bytes) {
         bytes = std::max<size_t>(256, (bytes + 255) & ~size_t(255));
         auto &b = host_scratch[name];
@@ -281,10 +283,15 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
                const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
                cudaStream_t stream);
 // vstats_dev: the filter's (sum, max |.|) of Vc (only the max is used), or nullptr to
-// compute the max here.
+// compute the max here.  rn (host, N) and clamp_dev (one device counter): the atoms'
+// scaled vdW radii, which bound |Phi| a priori, so Phi goes straight to fixed-point
+// digits in one pass; clamped values are counted in *clamp_dev (the caller then redoes
+// the fit without rn).  Without them: two passes (Phi, then its centre and scale).
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
-                cudaStream_t stream, const double *vstats_dev = nullptr, const std::string &slot = "");
+                cudaStream_t stream, const double *vstats_dev = nullptr, const std::string &slot = "",
+                const double *rn = nullptr, int *clamp_dev = nullptr);
+double radius_of(int z);  // vdW radius (Bohr) of element z, the filter's table
 void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
                const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,
                double *info, cudaStream_t stream);

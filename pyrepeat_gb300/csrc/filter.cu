@@ -316,6 +316,8 @@ __global__ void vstats_kernel(const double2 *__restrict__ part, int nb, double *
     }
 }
 
+}  // namespace
+
 double radius_of(int z) {
     static const double VDW[] = {
         2.72687, 2.23177, 2.31586, 2.59365, 3.85788, 3.63867, 3.45820, 3.30702, 3.17852, 3.06419, 2.81853,
@@ -331,8 +333,6 @@ double radius_of(int z) {
     const int n = (int)(sizeof(VDW) / sizeof(VDW[0]));
     return (z >= 1 && z <= n) ? VDW[z - 1] : 3.0;
 }
-
-}  // namespace
 
 void filter_plan(const rp_grid *grid, const double *atoms, const int *Z, int N, double vdw_factor, double vdw_max,
                  FilterPlan &plan) {

@@ -247,6 +247,15 @@ __device__ __forceinline__ float vscale_of(double vmax) {
 // Four 7-bit signed digits of an integer I = round(x 2^27), |x| <= 1:
 // x ~ 2^-6 (s0 + 2^-7 s1 + 2^-14 s2 + 2^-21 s3), digits rounded half up so |s| <= 64,
 // each exact in FP16.  Integer shifts only (no FP64 on the per-element path).
+// Exact warp sum of fixed-point values |I| <= 2^27: two 32-bit warp reductions of the
+// 14-bit halves (each sum stays below 2^19), recombined in 64 bits.
+__device__ __forceinline__ long long warp_sum_fixed(int I) {
+    const int hi = I >> 14, lo = I - (hi << 14);  // I = hi 2^14 + lo, lo in [0, 2^14)
+    const int shi = __reduce_add_sync(0xffffffffu, hi);
+    const int slo = __reduce_add_sync(0xffffffffu, lo);
+    return (long long)shi * 16384 + slo;
+}
+
 __device__ __forceinline__ void digits4(int v, __half *o0, __half *o1, __half *o2, __half *o3, long long idx) {
     const int s0 = (v + (1 << 20)) >> 21;
     int r = v - (s0 << 21);  // [-2^20, 2^20)
@@ -281,6 +290,16 @@ float real_near2() {
         return (float)(r * r);
     }();
     return v;
+}
+
+// I = round(x 2^27) of one element of X (x = (Phi - c) scale, or the scaled ESP), |x| <= 1
+__device__ __forceinline__ int x_fixed(float h, float l, float sc, int *clamped) {
+    sc *= 134217728.0f;  // 2^27
+    if (fabsf(h * sc) > 134217728.0f) {  // |x| beyond 1: clamp (counted; the fit reports it)
+        atomicAdd(clamped, 1);
+        return h > 0.f ? (1 << 27) : -(1 << 27);
+    }
+    return round_df(h, l, sc);
 }
 
 // ------------------------------------------------------------------ Phi of one chunk
@@ -401,11 +420,28 @@ __device__ __forceinline__ void int_times_df(float k, float ah, float al, float 
     e = __fmaf_rn(k, al, e);
 }
 
+// Digit output of the Phi kernel (single pass): instead of Phi_t, the kernel writes the
+// four fixed-point digit slices of X rows a0..a0+na-1 (x = Phi * scale_a, centre 0) and,
+// from the CTAs of the first atom block, the ESP row N (x = Vc * scale_V); columns
+// rows..rows_kpad-1 get zero digits.  Exact row sums go to rowsum (one atomic per CTA
+// and row), values beyond |x| = 1 are clamped and counted in *clamped.
+struct PhiDigits {
+    __half *X0, *X1, *X2, *X3;
+    long long ldx;        // row stride of the slices
+    long long rows_kpad;  // columns written (the chunk padded to the Gram's K step)
+    const float *scale;   // per atom, a power of two
+    const double *Vc;     // the chunk's centred ESP
+    const double *vmax_p; // max |Vc| (the ESP row scale)
+    unsigned long long *rowsum;
+    int *clamped;
+    int N;
+};
+
 // NC > 0: the number of n1 terms is the compile-time constant NC (KMAX = NC, the
 // reference's default 7): an atom's NC E values are loaded at the top of its iteration
 // and used after the real-space loop, which hides their L2 latency; stage C is unrolled.
 // NC = 0: any KMAX, loads in the loop.  The register cap keeps 7 CTAs per SM.
-template <int NC>
+template <int NC, bool DIG>
 __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
     const int32_t *__restrict__ kept, long long m0, long long rows, const double *__restrict__ axis, AxisDF adf,
     int nx, int ny,
@@ -413,7 +449,7 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
     double rc, double sa, float rcf, float saf_in, float near2, const float4 *__restrict__ img,
     const float4 *__restrict__ EX,
     const float2 *__restrict__ E, int n1c, int parts, float2 *__restrict__ phit, long long ld,
-    double *__restrict__ psum, float *__restrict__ pmax) {
+    double *__restrict__ psum, float *__restrict__ pmax, PhiDigits dg) {
     extern __shared__ float4 dsm[];
     float4 *img_hi = dsm;                                 // [kPhiAtoms][scap] (x, y, z, shift index)
     float4 *img_lo = img_hi + (size_t)kPhiAtoms * scap;   // [kPhiAtoms][scap]
@@ -422,6 +458,7 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
     __shared__ float bb[2][3][kPhiPts / 32];
     __shared__ float wsum[kPhiPts / 32][kPhiAtoms];
     __shared__ float wmax[kPhiPts / 32][kPhiAtoms];
+    __shared__ long long wrow[kPhiPts / 32][kPhiAtoms + 1];  // digit-row partial sums (DIG)
     const long long mb = (long long)blockIdx.x * kPhiPts;
     const int a0 = blockIdx.y * kPhiAtoms;
     const int na = min(kPhiAtoms, N - a0);
@@ -622,8 +659,16 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
             v.e = __fadd_rn(v.e, e_);
         }
         const float2 out = dfa::norm(v);
-        if (valid) *prow = out;
-        if (psum) {  // column statistics for the centre and the scale: FP32 is enough (any
+        if (DIG) {
+            int I = 0;
+            if (valid) I = x_fixed(out.x, out.y, dg.scale[a0 + a], dg.clamped);
+            const long long rs = warp_sum_fixed(I);
+            if (lane == 0) wrow[warp][a] = rs;
+            if (m < dg.rows_kpad) digits4(I, dg.X0, dg.X1, dg.X2, dg.X3, (long long)(a0 + a) * dg.ldx + m);
+        } else if (valid) {
+            *prow = out;
+        }
+        if (!DIG && psum) {  // column statistics for the centre and the scale: FP32 is enough (any
                      // centre is corrected exactly; the max is exact)
             float sh = valid ? out.x : 0.f, mx = valid ? fabsf(out.x) : 0.f;
             for (int o = 16; o > 0; o >>= 1) {
@@ -636,7 +681,28 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
             }
         }
     }
-    if (psum) {
+    if (DIG) {
+        // the ESP row, from the CTAs of the first atom block
+        if (blockIdx.y == 0) {
+            int I = 0;
+            if (valid) {
+                const double v = dg.Vc[m];
+                const float h = (float)v;
+                I = x_fixed(h, (float)(v - (double)h), vscale_of(*dg.vmax_p), dg.clamped);
+            }
+            const long long rs = warp_sum_fixed(I);
+            if (lane == 0) wrow[warp][kPhiAtoms] = rs;
+            if (m < dg.rows_kpad) digits4(I, dg.X0, dg.X1, dg.X2, dg.X3, (long long)dg.N * dg.ldx + m);
+        }
+        __syncthreads();
+        // exact row sums (two's complement int64 atomics: order-independent), one per CTA and row
+        if (threadIdx.x < na || (blockIdx.y == 0 && threadIdx.x == kPhiAtoms)) {
+            const int a = threadIdx.x;
+            long long t = 0;
+            for (int w = 0; w < kPhiPts / 32; ++w) t += wrow[w][a];
+            if (t != 0) atomicAdd(dg.rowsum + (a == kPhiAtoms ? dg.N : a0 + a), (unsigned long long)t);
+        }
+    } else if (psum) {
         __syncthreads();
         if (threadIdx.x < na) {
             const int a = threadIdx.x;
@@ -659,19 +725,21 @@ size_t phi_smem_bytes(int n1c, int scap) {
 void launch_phi(const int32_t *kept, long long m0, long long rows, const double *d_axis, const double *h_axis, int nx, int ny,
                 const double *d_atoms, int N, const double *d_shifts, int S, int zero_idx, double rc, double sa,
                 const float4 *img, const float4 *EX, const float2 *E, int n1c, int parts, float2 *phit, long long ld,
-                double *psum, float *pmax, cudaStream_t s) {
+                double *psum, float *pmax, const PhiDigits *dig, cudaStream_t s) {
     RP_REQUIRE(S >= 1 && S <= kMaxShifts, "more than 128 real-space shifts after pruning (cutoff too large for the cell)");
     const int scap = (S + 31) / 32 * 32;
     const bool regs = (n1c == 7);  // KMAX 7: the specialised kernel
     const size_t smem = phi_smem_bytes(n1c, scap);
-    // the static shared memory (the statistics tile, ~18 KB) counts against the same 48 KB
-    // default, so the opt-in is raised whenever the dynamic part could cross it
+    // the static shared memory (the statistics and row-sum tiles, ~1.3 KB) counts against
+    // the same 48 KB default, so the opt-in is raised whenever the dynamic part could cross it
     static size_t attr = 0;
     if (smem > attr) {
         RP_REQUIRE(smem <= 192 * 1024, "phi kernel: KMAX too large for shared memory");
         const size_t want = std::max<size_t>(smem, 96 * 1024);
-        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
-        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
+        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<7, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
+        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
+        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<7, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
+        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
         attr = want;
     }
     AxisDF adf;
@@ -680,9 +748,12 @@ void launch_phi(const int32_t *kept, long long m0, long long rows, const double 
         adf.l[q] = (float)(h_axis[q] - (double)adf.h[q]);
     }
     dim3 grd(ceil_div(rows, kPhiPts), ceil_div(N, kPhiAtoms));
-    (regs ? phi_chunk_kernel<7> : phi_chunk_kernel<0>)<<<grd, kPhiPts, smem, s>>>(kept, m0, rows, d_axis, adf, nx, ny, d_atoms, N, d_shifts, S, scap, zero_idx,
-                                                rc, sa, (float)rc, (float)(sa * kSqrtLog2e), real_near2(), img, EX, E, n1c, parts,
-                                                phit, ld, psum, pmax);
+    const PhiDigits dg = dig ? *dig : PhiDigits{};
+    auto kern = dig ? (regs ? phi_chunk_kernel<7, true> : phi_chunk_kernel<0, true>)
+                    : (regs ? phi_chunk_kernel<7, false> : phi_chunk_kernel<0, false>);
+    kern<<<grd, kPhiPts, smem, s>>>(kept, m0, rows, d_axis, adf, nx, ny, d_atoms, N, d_shifts, S, scap, zero_idx, rc,
+                                    sa, (float)rc, (float)(sa * kSqrtLog2e), real_near2(), img, EX, E, n1c, parts,
+                                    phit, ld, psum, pmax, dg);
     RP_LAUNCH_CHECK();
 }
 
@@ -718,16 +789,6 @@ __global__ void colstats_finish_kernel(const double *__restrict__ psum, const fl
     int e = 0;
     if (bound > 0.f) frexpf(bound, &e);
     scale[a] = ldexpf(1.f, -e - 1);
-}
-
-// I = round(x 2^27) of one element of X (x = (Phi - c) scale, or the scaled ESP), |x| <= 1
-__device__ __forceinline__ int x_fixed(float h, float l, float sc, int *clamped) {
-    sc *= 134217728.0f;  // 2^27
-    if (fabsf(h * sc) > 134217728.0f) {  // |x| beyond 1: clamp (counted; the fit reports it)
-        atomicAdd(clamped, 1);
-        return h > 0.f ? (1 << 27) : -(1 << 27);
-    }
-    return round_df(h, l, sc);
 }
 
 constexpr int kSliceThreads = 256;
@@ -916,9 +977,45 @@ inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b
 
 }  // namespace
 
+// Upper bound B_a on |Phi[a][m]| over the kept points, which sets the digit scale of the
+// single-pass path (false: an exclusion radius below 0.5 Bohr makes the bound useless).
+//   Real space: the filter keeps no point within rn_a (the scaled vdW radius) of an image
+//   of atom a, and two images are a lattice vector apart, at least the smallest
+//   interplanar spacing d, so at most one image is nearer than d/2; hence
+//   sum <= erfc(s rn)/rn + (S - 1) erfc(s d/2)/(d/2), erfc(s x)/x decreasing.
+//   Reciprocal space: |sum_k c_k cos(k.r)| <= sum_k |c_k|.
+// Should a cell defeat the argument (an image outside the filter's 27 nearest to a
+// point), the kernel counts the clamped values and the caller redoes the fit in two passes.
+static bool phi_bounds(const rp_ewald *ew, int S, const double *rn, int N, double bound_scale,
+                       std::vector<float> &scale) {
+    const double *b = ew->box;
+    double d = 1e300;
+    for (int q = 0; q < 3; ++q) {
+        const double *u = b + 3 * ((q + 1) % 3), *v = b + 3 * ((q + 2) % 3), *w = b + 3 * q;
+        const double cx = u[1] * v[2] - u[2] * v[1], cy = u[2] * v[0] - u[0] * v[2], cz = u[0] * v[1] - u[1] * v[0];
+        const double area = std::sqrt(cx * cx + cy * cy + cz * cz);
+        const double vol = std::fabs(w[0] * cx + w[1] * cy + w[2] * cz);
+        if (area > 0.0) d = std::min(d, vol / area);
+    }
+    double rec = 0.0;
+    for (double c : ew->kcoef) rec += std::fabs(c);
+    const double sa = ew->sqrt_alpha, h = 0.5 * d;
+    const double tail = (S > 1 && h > 0.0) ? (S - 1) * std::erfc(sa * h) / h : 0.0;
+    scale.resize((size_t)N);
+    for (int a = 0; a < N; ++a) {
+        if (!(rn[a] >= 0.5)) return false;
+        const double B = (std::erfc(sa * rn[a]) / rn[a] + tail + rec) * bound_scale;
+        int e = 0;
+        std::frexp(B, &e);  // B in [2^(e-1), 2^e): |x| = |Phi| 2^(-e-1) < 1/2
+        scale[a] = std::ldexp(1.0f, -e - 1);
+    }
+    return true;
+}
+
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
-                cudaStream_t stream, const double *vstats_dev, const std::string &slot) {
+                cudaStream_t stream, const double *vstats_dev, const std::string &slot, const double *rn,
+                int *clamp_dev) {
     RP_REQUIRE(N > 0 && M > 0, "rp_gram: need N > 0 and M > 0");
     std::vector<double> sh;
     int zero_idx = -1;
@@ -948,18 +1045,21 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
 
     // chunk the points so the per-chunk staging stays below ~6 GB
     const int Np = N + 1;                       // atoms + the ESP row
-    const long long per_point = 8LL * N + 8LL * Np;  // Phi (double-float) + four FP16 digits
+    const long long per_point = 8LL * N + 8LL * Np;  // Phi (double-float, two-pass) + four FP16 digits
     long long chunk = std::max<long long>(kBM, ((6LL << 30) / per_point) / kBM * kBM);
     chunk = std::min<long long>(chunk, round_up(M, kBM));
     const long long chunk_pad = round_up(chunk, kBK);
 
-    float2 *phit = ctx->buf_t<float2>("m_phit" + slot, (size_t)N * chunk_pad);
+    // single pass: Phi goes straight to digits, scaled by the a-priori bounds, centre 0
+    std::vector<float> hscale;
+    const bool single = rn && clamp_dev && phi_bounds(ew, S, rn, N, ctx->bound_scale, hscale);
+    float2 *phit = single ? nullptr : ctx->buf_t<float2>("m_phit" + slot, (size_t)N * chunk_pad);
     __half *X[kGSlices];
     for (int q = 0; q < kGSlices; ++q) X[q] = ctx->buf_t<__half>("m_X" + slot + std::to_string(q), (size_t)Np * chunk_pad);
     int *d_clamped = ctx->d_status + 1;  // second status word: fixed-point range overflows
     const int nblk = (int)ceil_div(chunk, kPhiPts);
-    double *psum = ctx->buf_t<double>("m_psum" + slot, (size_t)N * nblk);
-    float *pmax = ctx->buf_t<float>("m_pmax" + slot, (size_t)N * nblk);
+    double *psum = single ? nullptr : ctx->buf_t<double>("m_psum" + slot, (size_t)N * nblk);
+    float *pmax = single ? nullptr : ctx->buf_t<float>("m_pmax" + slot, (size_t)N * nblk);
     unsigned long long *rowsum = ctx->buf_t<unsigned long long>("m_rowsum" + slot, (size_t)Np);
     double *cvec = ctx->buf_t<double>("m_c" + slot, N);
     float2 *cdf = ctx->buf_t<float2>("m_cdf" + slot, N);
@@ -977,6 +1077,11 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         vmax = st;
     }
 
+    if (single) {
+        RP_CUDA(cudaMemcpyAsync(scale, hscale.data(), sizeof(float) * N, cudaMemcpyHostToDevice, stream));
+        RP_CUDA(cudaMemsetAsync(cvec, 0, sizeof(double) * N, stream));
+    }
+
     const int nt = (int)ceil_div(Np, kBM), ntj = (int)ceil_div(Np, kGN);
     int ntri = 0;  // 128 x 64 Gram tiles with columns at or right of the row block, up to the last row
     for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
@@ -987,13 +1092,21 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
         const long long rows_kpad = round_up(rows, kBK);
         // 1. Phi of the chunk (real space + reciprocal stage C) and its column statistics
         const int nb = (int)ceil_div(rows, kPhiPts);
-        {
+        if (single) {  // Phi of the chunk straight to the digits of X
+            StageTimer tt(ctx, "phi", stream);
+            // the slices' row stride is the chunk's padded length, as the Gram's tensor maps read them
+            const PhiDigits dg{X[0], X[1], X[2], X[3], rows_kpad, rows_kpad, scale, Vc_dev + m0, vmax,
+                               rowsum, clamp_dev, N};
+            launch_phi(kept_idx_dev, m0, rows, d_axis, ew->grid.axis, nx, ny, d_atoms, N, d_shifts, S, zero_idx,
+                       ew->cutoff, ew->sqrt_alpha, img, ew->d_exf, E, n1c, 3, nullptr, chunk_pad, nullptr, nullptr,
+                       &dg, stream);
+        } else {
             StageTimer tt(ctx, "phi", stream);
             launch_phi(kept_idx_dev, m0, rows, d_axis, ew->grid.axis, nx, ny, d_atoms, N, d_shifts, S, zero_idx, ew->cutoff,
-                       ew->sqrt_alpha, img, ew->d_exf, E, n1c, 3, phit, chunk_pad, psum, pmax, stream);
+                       ew->sqrt_alpha, img, ew->d_exf, E, n1c, 3, phit, chunk_pad, psum, pmax, nullptr, stream);
         }
         // 2. centre/scale on the first chunk, fixed-point digits of X
-        {
+        if (!single) {
             StageTimer tt(ctx, "center_slice", stream);
             if (m0 == 0) {
                 colstats_finish_kernel<<<ceil_div(N, 4), 128, 0, stream>>>(psum, pmax, nb, N, rows, cvec, cdf, scale);
@@ -1036,6 +1149,18 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
 
 }  // namespace rp
 
+// Diagnostics (not part of the public ABI): a factor on the single-pass Phi bounds of
+// the batched fit (1 = the analytic bounds).  A factor far below 1 makes every cube clamp
+// and fall back to the two-pass fit, which a test compares with the normal path.
+extern "C" int rp_debug_bound_scale(rp_ctx *ctx, double factor) {
+    if (!ctx || !(factor > 0.0)) return RP_E_ARG;
+    ctx->bound_scale = factor;
+    return RP_OK;
+}
+
+// Diagnostics: how many cubes of the last batched fit were redone in two passes.
+extern "C" int rp_debug_last_fallbacks(const rp_ctx *ctx) { return ctx ? ctx->last_fallbacks : RP_E_ARG; }
+
 // Diagnostics (not part of the public ABI): the mixed path's Phi for the first
 // `rows` kept points, atom-major [N][rows]; parts = 1 real space, 2 reciprocal,
 // 3 both.  Used to check each part against FP64 separately.
@@ -1063,7 +1188,7 @@ extern "C" int rp_debug_mixed_phi(rp_ctx *ctx, const rp_ewald *ew, const double 
         float2 *ph = ctx->buf_t<float2>("dbg_phi", (size_t)N * rows);
         launch_phi(kept_idx_dev, 0, rows, d_axis, ew->grid.axis, ew->grid.n_grid[0], ew->grid.n_grid[1], d_atoms, N, d_shifts, S,
                    zero_idx, ew->cutoff, ew->sqrt_alpha, img, ew->d_exf, E, ew->kmax, parts, ph, rows, nullptr,
-                   nullptr, 0);
+                   nullptr, nullptr, 0);
         df_to_double_kernel<<<ceil_div((long long)N * rows, 256), 256>>>(ph, (long long)N * rows, phi_dev);
         RP_LAUNCH_CHECK();
         RP_CUDA(cudaDeviceSynchronize());

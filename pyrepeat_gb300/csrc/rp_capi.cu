@@ -291,18 +291,40 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
         //    and launch gaps overlap another's; the FP64 comparator stays on the caller's
         //    stream (its cuBLAS handle is shared).  Every cube's result is independent of
         //    the lane it ran on.
+        //    A mixed fit takes the single pass (Phi straight to digits, scaled by the a-priori
+        //    bounds from the scaled vdW radii); a cube whose values clamp (a cell the bound's
+        //    argument does not cover) is redone below in two passes.
+        std::vector<double> rn((size_t)off_n[n]);
+        for (int i = 0; i < n; ++i)
+            for (int a = 0; a < descs[i].N; ++a)
+                rn[off_n[i] + a] = descs[i].vdw_factor * rp::radius_of(descs[i].Z[a]);
+        int *clamps = ctx->buf_t<int>("fit_clamps", (size_t)n);
+        RP_CUDA(cudaMemsetAsync(clamps, 0, sizeof(int) * n, stream));
+        fork();
         for (int i = 0; i < n; ++i) {
             const rp_fit_desc &d = descs[i];
             if (d.precision == RP_PREC_MIXED) {
                 const int ln = i % lanes;
                 rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
-                               b + off_n[i], nullptr, ctx->lane(ln), vst + 2 * i, "#" + std::to_string(ln));
+                               b + off_n[i], nullptr, ctx->lane(ln), vst + 2 * i, "#" + std::to_string(ln),
+                               rn.data() + off_n[i], clamps + i);
             } else {
                 rp::gram_fp64(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
                               b + off_n[i], nullptr, stream);
             }
         }
         join();  // the solve on the caller's stream waits for every lane
+        std::vector<int> hclamps((size_t)n);
+        RP_CUDA(cudaMemcpyAsync(hclamps.data(), clamps, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
+        RP_CUDA(cudaStreamSynchronize(stream));
+        ctx->last_fallbacks = 0;
+        for (int i = 0; i < n; ++i)
+            if (hclamps[i] != 0) {  // the two-pass fit, centred and scaled by the data
+                ++ctx->last_fallbacks;
+                const rp_fit_desc &d = descs[i];
+                rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
+                               b + off_n[i], nullptr, stream, vst + 2 * i, "");
+            }
         // 5. all constraint folds and bordered solves, one launch
         std::vector<rp::SolveJob> jobs((size_t)n);
         for (int i = 0; i < n; ++i) {

@@ -88,6 +88,30 @@ def test_mixed_phi_parts_match_oracle(name, order, gpu_ctx, oracle_mod):
     ew.close()
 
 
+def test_single_pass_clamp_falls_back_to_two_passes(gpu_ctx):
+    """The batched fit scales Phi by a-priori bounds and writes its digits in one pass.
+    Bounds shrunk 1000-fold make values clamp: each such cube is redone in two passes
+    (centre and scale from the data), and its charges agree with the single-pass ones."""
+    from pyrepeat_gb300 import _lib
+    L = gpu_ctx.lib
+    L.rp_debug_bound_scale.restype = ctypes.c_int
+    L.rp_debug_bound_scale.argtypes = [ctypes.c_void_p, ctypes.c_double]
+    L.rp_debug_last_fallbacks.restype = ctypes.c_int
+    L.rp_debug_last_fallbacks.argtypes = [ctypes.c_void_p]
+    cubes = [load_golden(n)[0] for n in ("water24", "tricmini")]
+    q0, _, _ = gpu_ctx.fit_batch(cubes, _lib.PREC_MIXED)
+    assert L.rp_debug_last_fallbacks(gpu_ctx.ptr) == 0
+    assert L.rp_debug_bound_scale(gpu_ctx.ptr, 1e-3) == 0
+    try:
+        q1, _, _ = gpu_ctx.fit_batch(cubes, _lib.PREC_MIXED)
+        fell_back = L.rp_debug_last_fallbacks(gpu_ctx.ptr)
+    finally:
+        L.rp_debug_bound_scale(gpu_ctx.ptr, 1.0)
+    assert fell_back == len(cubes)
+    for a, b in zip(q0, q1):
+        assert np.abs(np.asarray(a) - np.asarray(b)).max() <= 1e-6
+
+
 def test_mixed_fit_is_deterministic(gpu_ctx):
     from pyrepeat_gb300 import _lib
     cube, _ = load_golden("tricmini")
