@@ -37,7 +37,7 @@ struct Rec9 {
 // U[a][d][n + P] = e^{-i n (b_d . r_a)} for n in [-P, P]: the per-axis atom phases, so that
 // e^{-i k.r_a} = U[a][0][n1] U[a][1][n2] U[a][2][n3] needs 3 (2P+1) sincos per atom instead of K.
 __global__ void atom_phases_kernel(const double *__restrict__ atoms, int N, Rec9 rb, int P,
-                                   double2 *__restrict__ U) {
+                                   double2 *__restrict__ U, float4 *__restrict__ Udf) {
     const int nw = 2 * P + 1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N * 3 * nw) return;
@@ -47,6 +47,7 @@ __global__ void atom_phases_kernel(const double *__restrict__ atoms, int N, Rec9
     double s, c;
     sincos((double)n * th, &s, &c);
     U[t] = make_double2(c, -s);
+    Udf[t] = dfa::split(c, -s);
 }
 
 __device__ __forceinline__ double2 cmul(double2 x, double2 y) {
@@ -54,10 +55,12 @@ __device__ __forceinline__ double2 cmul(double2 x, double2 y) {
 }
 
 // W[col][n2'][n3'][n1] = w_k e^{-i k.r} (col = atom), or sum_a q_a w_k e^{-i k.r_a} (one
-// charge-weighted column when q != nullptr); FP64, stored as double-float
+// charge-weighted column when q != nullptr), stored as double-float.  Per atom the two
+// phase products and the weight are double-float products on the FP32 pipe (~2^-44
+// relative); the charge-weighted sum stays FP64.
 __global__ void build_w_kernel(const int *__restrict__ kidx, const double *__restrict__ kcoef, int K, int P,
-                               const double2 *__restrict__ U, const double *__restrict__ q, int N, int ncols,
-                               float4 *__restrict__ W) {
+                               const double2 *__restrict__ U, const float4 *__restrict__ Udf,
+                               const double *__restrict__ q, int N, int ncols, float4 *__restrict__ W) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)ncols * K) return;
     const int col = (int)(t / K), k = (int)(t - (long long)col * K);
@@ -65,8 +68,20 @@ __global__ void build_w_kernel(const int *__restrict__ kidx, const double *__res
     const int n1 = kidx[3 * k], n2 = kidx[3 * k + 1] + P, n3 = kidx[3 * k + 2] + P;
     double2 z;
     if (q == nullptr) {
-        const double2 *u = U + (size_t)col * 3 * nw;
-        z = cmul(cmul(u[n1 + P], u[nw + n2]), u[2 * nw + n3]);
+        const float4 *u = Udf + (size_t)col * 3 * nw;
+        dfa::acc re{0.f, 0.f}, im{0.f, 0.f};
+        dfa::cmac(re, im, u[n1 + P], u[nw + n2]);
+        const float4 z12 = dfa::pack(re, im);
+        re = im = dfa::acc{0.f, 0.f};
+        dfa::cmac(re, im, z12, u[2 * nw + n3]);
+        const float4 z3 = dfa::pack(re, im);
+        const double w = kcoef[k];
+        const float wh = (float)w, wl = (float)(w - (double)wh);
+        re = im = dfa::acc{0.f, 0.f};
+        dfa::mac(re, wh, wl, z3.x, z3.y);
+        dfa::mac(im, wh, wl, z3.z, z3.w);
+        W[(((long long)col * nw + n2) * nw + n3) * n1c + n1] = dfa::pack(re, im);
+        return;
     } else {
         z = make_double2(0.0, 0.0);
         for (int a = 0; a < N; ++a) {
@@ -80,15 +95,15 @@ __global__ void build_w_kernel(const int *__restrict__ kidx, const double *__res
     W[(((long long)col * nw + n2) * nw + n3) * n1c + n1] = dfa::split(w * z.x, w * z.y);
 }
 
-// Each thread produces up to kN1B consecutive n1 outputs of one (plane, n2, column) or
-// (row, column): kN1B independent accumulator chains, and the shared phase factor is
+// Each stage-A thread produces up to kN1B consecutive n1 outputs of one (plane, n2,
+// column): kN1B independent accumulator chains, and the shared phase factor is
 // loaded once per term.
 constexpr int kN1B = 8;
 
 // Stage A, one thread per (n2, column, n1 block, plane l) with l fastest: a warp reads
 // one W row (broadcast) and consecutive ez phases (coalesced).
 __global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 *__restrict__ EZ, int ncols, int P,
-                                     int nz, float4 *__restrict__ F) {
+                                     int nz, float2 *__restrict__ F) {
     extern __shared__ float4 ezs[];  // the whole ez table [nw][nz], read once per CTA
     const int n1c = P + 1, nw = 2 * P + 1, nb = (n1c + kN1B - 1) / kN1B;
     for (int q = threadIdx.x; q < nw * nz; q += blockDim.x) ezs[q] = EZ[q];
@@ -113,48 +128,65 @@ __global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 
         for (int u = 0; u < kN1B; ++u)
             if (u < cnt) dfa::cmac(re[u], im[u], z, wr[u]);
     }
-    float4 *o = F + (((long long)l * nw + n2) * ncols + a) * n1c + n10;
+    float2 *o = F + (((long long)l * nw + n2) * ncols + a) * n1c + n10;
 #pragma unroll
     for (int u = 0; u < kN1B; ++u)
-        if (u < cnt) o[u] = dfa::pack(re[u], im[u]);
+        if (u < cnt) o[u] = make_float2(dfa::norm(re[u]).x, dfa::norm(im[u]).x);  // stage B takes FP32
 }
 
-// Stage B, one CTA per (plane l, block of `ab` columns): the plane's F slab for those
-// columns is staged in shared memory once and reused by every row j of the plane.
-__global__ void __launch_bounds__(128) recip_stage_b_kernel(const float4 *__restrict__ F,
+// Stage B, one CTA per (plane l, block of `ab` columns).  The plane's F slab for those
+// columns ([n2][a][n1], FP32) and the ey phases ([n2][j], rows padded to kJB) sit in shared
+// memory.  A thread owns one (column, n1) and kJB consecutive rows j: its F value is one
+// load per n2, the ey values are warp broadcasts read two rows at a time, and a warp's
+// stores of E land on consecutive (column, n1) of one row, contiguous in memory.
+constexpr int kJB = 8;
+__global__ void __launch_bounds__(128) recip_stage_b_kernel(const float2 *__restrict__ F,
                                                             const float4 *__restrict__ EY, int ncols, int P, int ny,
                                                             int ab, float2 *__restrict__ E) {
-    extern __shared__ float4 fs[];  // [nw][ab][n1c] F slab, then the ey table [nw][ny]
+    extern __shared__ float4 smem_b[];
     const int n1c = P + 1, nw = 2 * P + 1;
     const int l = blockIdx.y, a0 = blockIdx.x * ab, na = min(ab, ncols - a0);
-    const int slab = nw * ab * n1c;
-    float4 *eys = fs + slab;
-    for (int t = threadIdx.x; t < slab; t += blockDim.x) {
-        const int n1 = t % n1c, u = t / n1c, a = u % ab, n2 = u / ab;
-        fs[t] = (a < na) ? F[(((long long)l * nw + n2) * ncols + a0 + a) * n1c + n1] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int an = na * n1c;                                  // (column, n1) pairs of the CTA
+    const int nyp = (ny + kJB - 1) / kJB * kJB;
+    float2 *fs = reinterpret_cast<float2 *>(smem_b);          // [nw][an]
+    float2 *eys = fs + ((nw * ab * n1c + 1) & ~1);           // [nw][nyp], 16-byte aligned rows
+    for (int t = threadIdx.x; t < nw * an; t += blockDim.x) {
+        const int n2 = t / an, r = t - n2 * an;
+        fs[t] = F[(((long long)l * nw + n2) * ncols + a0) * n1c + r];
     }
-    for (int q = threadIdx.x; q < nw * ny; q += blockDim.x) eys[q] = EY[q];
+    for (int q = threadIdx.x; q < nw * nyp; q += blockDim.x) {
+        const int n2 = q / nyp, j = q - n2 * nyp;
+        const float4 y = j < ny ? EY[n2 * ny + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        eys[q] = make_float2(y.x, y.z);
+    }
     __syncthreads();
-    const int items = na * ny;  // (a, j), j fastest: a warp reads one column's slab (broadcast)
-    for (int it = threadIdx.x; it < items; it += blockDim.x) {
-        const int a = it / ny, j = it - a * ny;
-        float2 *o = E + (((long long)l * ny + j) * ncols + a0 + a) * n1c;
-        for (int n10 = 0; n10 < n1c; n10 += kN1B) {
-            const int cnt = min(kN1B, n1c - n10);
-            float re[kN1B], im[kN1B];
+    const int tasks = an * (nyp / kJB);
+    for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+        const int jb = task / an, r = task - jb * an;  // r = a n1c + n1
+        float re[kJB], im[kJB];
 #pragma unroll
-            for (int u = 0; u < kN1B; ++u) re[u] = im[u] = 0.f;
-            for (int n2 = 0; n2 < nw; ++n2) {
-                const float4 y = eys[n2 * ny + j];
-                const float4 *fr = fs + ((size_t)n2 * ab + a) * n1c + n10;
+        for (int u = 0; u < kJB; ++u) re[u] = im[u] = 0.f;
+        for (int n2 = 0; n2 < nw; ++n2) {
+            const float2 f = fs[n2 * an + r];
+            const float4 *yp = reinterpret_cast<const float4 *>(eys + n2 * nyp + jb * kJB);
 #pragma unroll
-                for (int u = 0; u < kN1B; ++u)
-                    if (u < cnt) dfa::cmac32(re[u], im[u], y, fr[u]);
+            for (int u = 0; u < kJB / 2; ++u) {
+                const float4 y = yp[u];  // rows 2u and 2u+1: (re, im, re, im)
+                re[2 * u] = fmaf(y.x, f.x, re[2 * u]);
+                re[2 * u] = fmaf(-y.y, f.y, re[2 * u]);
+                im[2 * u] = fmaf(y.x, f.y, im[2 * u]);
+                im[2 * u] = fmaf(y.y, f.x, im[2 * u]);
+                re[2 * u + 1] = fmaf(y.z, f.x, re[2 * u + 1]);
+                re[2 * u + 1] = fmaf(-y.w, f.y, re[2 * u + 1]);
+                im[2 * u + 1] = fmaf(y.z, f.y, im[2 * u + 1]);
+                im[2 * u + 1] = fmaf(y.w, f.x, im[2 * u + 1]);
             }
-#pragma unroll
-            for (int u = 0; u < kN1B; ++u)
-                if (u < cnt) o[n10 + u] = make_float2(re[u], im[u]);
         }
+        float2 *o = E + (((long long)l * ny + jb * kJB) * ncols + a0) * n1c + r;
+        const long long row_stride = (long long)ncols * n1c;
+#pragma unroll
+        for (int u = 0; u < kJB; ++u)
+            if (jb * kJB + u < ny) o[u * row_stride] = make_float2(re[u], im[u]);
     }
 }
 
@@ -178,15 +210,17 @@ void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const do
     }
     const size_t nW = (size_t)ncols * nw * nw * n1c, nF = (size_t)nz * nw * ncols * n1c;
     float4 *W = ctx->buf_t<float4>("rs_W" + slot, nW);
-    float4 *F = ctx->buf_t<float4>("rs_F" + slot, nF);
+    float2 *F = ctx->buf_t<float2>("rs_F" + slot, nF);
     double2 *U = ctx->buf_t<double2>("rs_U" + slot, (size_t)N * 3 * nw);
+    float4 *Udf = ctx->buf_t<float4>("rs_Udf" + slot, (size_t)N * 3 * nw);
     RP_CUDA(cudaMemsetAsync(W, 0, sizeof(float4) * nW, stream));
     Rec9 rb;
     for (int q = 0; q < 9; ++q) rb.b[q] = ew->rec[q];
-    atom_phases_kernel<<<ceil_div((long long)N * 3 * nw, 128), 128, 0, stream>>>(d_atoms, N, rb, P, U);
+    atom_phases_kernel<<<ceil_div((long long)N * 3 * nw, 128), 128, 0, stream>>>(d_atoms, N, rb, P, U, Udf);
     RP_LAUNCH_CHECK();
     const long long nk = (long long)ncols * ew->K;
-    build_w_kernel<<<ceil_div(nk, 128), 128, 0, stream>>>(ew->d_kidx, ew->d_kcoef, ew->K, P, U, d_q, N, ncols, W);
+    build_w_kernel<<<ceil_div(nk, 128), 128, 0, stream>>>(ew->d_kidx, ew->d_kcoef, ew->K, P, U, Udf, d_q, N,
+                                                      ncols, W);
     RP_LAUNCH_CHECK();
     const int nb = (n1c + kN1B - 1) / kN1B;
     const size_t smem_a = sizeof(float4) * (size_t)nw * nz;
@@ -199,10 +233,11 @@ void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const do
     recip_stage_a_kernel<<<ceil_div((long long)nz * nw * ncols * nb, 128), 128, smem_a, stream>>>(W, ew->d_ezf, ncols,
                                                                                                   P, nz, F);
     RP_LAUNCH_CHECK();
-    // stage B: as many columns per CTA as fit 96 KB of shared memory (at most 16)
-    const size_t col_bytes = sizeof(float4) * (size_t)nw * n1c;
-    const int ab = (int)std::max<size_t>(1, std::min<size_t>(16, (96u << 10) / col_bytes));
-    const size_t smem = col_bytes * ab + sizeof(float4) * (size_t)nw * ny;
+    // stage B: as many columns per CTA as fit 48 KB of shared memory (at most 16)
+    const size_t col_bytes = sizeof(float2) * (size_t)nw * n1c;
+    const int ab = (int)std::max<size_t>(1, std::min<size_t>(16, (48u << 10) / col_bytes));
+    const size_t nyp = (size_t)(ny + kJB - 1) / kJB * kJB;
+    const size_t smem = sizeof(float2) * (((size_t)nw * ab * n1c + 1) & ~(size_t)1) + sizeof(float2) * (size_t)nw * nyp;
     RP_REQUIRE(smem <= (200u << 10), "recip_rows: KMAX too large");
     static size_t attr = 0;
     if (smem > (48u << 10) && smem > attr) {
