@@ -8,7 +8,10 @@
 #include <atomic>
 #include <cstdint>
 #include <cstdio>
+#include <condition_variable>
 #include <exception>
+#include <functional>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -59,6 +62,91 @@ extern std::atomic<long long> g_launches;
 struct Buffer {
     void *ptr = nullptr;
     size_t bytes = 0;
+};
+
+}  // namespace rp
+
+// Host worker threads owned by a context, started on first use: run(n, f) calls f(i) for
+// i in [0, n) on the workers and the calling thread (the cubes of a batch are independent)
+// and returns when all are done, rethrowing the first exception.  No thread is created per
+// batch, and the per-cube host work (filter plans, Ewald tables) is spread over the cores.
+namespace rp {
+struct FilterPlan;
+
+class HostPool {
+  public:
+    explicit HostPool(int workers) {
+        for (int t = 0; t < workers; ++t) th_.emplace_back([this] { loop(); });
+    }
+    ~HostPool() {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : th_) t.join();
+    }
+    void run(int n, const std::function<void(int)> &f) {
+        if (n <= 0) return;
+        if (th_.empty() || n == 1) {
+            for (int i = 0; i < n; ++i) f(i);
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            job_ = &f;
+            count_ = n;
+            next_.store(0);
+            err_ = nullptr;
+            pending_ = (int)th_.size();
+            ++gen_;
+        }
+        cv_.notify_all();
+        drain();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_.wait(lk, [&] { return pending_ == 0; });  // every worker is past this job
+        job_ = nullptr;
+        if (err_) {
+            std::exception_ptr e = err_;
+            err_ = nullptr;
+            lk.unlock();
+            std::rethrow_exception(e);
+        }
+    }
+
+  private:
+    void loop() {
+        long long seen = 0;
+        std::unique_lock<std::mutex> lk(mu_);
+        for (;;) {
+            cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+            if (stop_) return;
+            seen = gen_;
+            lk.unlock();
+            drain();
+            lk.lock();
+            if (--pending_ == 0) done_.notify_all();
+        }
+    }
+    void drain() {
+        for (int i = next_.fetch_add(1); i < count_; i = next_.fetch_add(1)) {
+            try {
+                (*job_)(i);
+            } catch (...) {
+                std::lock_guard<std::mutex> g(mu_);
+                if (!err_) err_ = std::current_exception();
+            }
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)> *job_ = nullptr;
+    std::atomic<int> next_{0};
+    int count_ = 0, pending_ = 0;
+    long long gen_ = 0;
+    bool stop_ = false;
+    std::exception_ptr err_;
 };
 
 }  // namespace rp
@@ -114,6 +202,17 @@ struct rp_ctx {
     // small pageable ones); callers synchronise their stream before it is reused.
     std::unordered_map<std::string, rp::Buffer> host_scratch;
     double bound_scale = 1.0;  // factor on the single-pass Phi bounds (tests shrink it to force clamps)
+    std::unique_ptr<rp::HostPool> pool;  // host workers (created on first use)
+    // per-cube host objects of the batched fit, kept across batches for their capacity
+    std::vector<std::unique_ptr<rp_ewald>> ew_pool;
+    std::vector<std::unique_ptr<rp::FilterPlan>> plan_pool;
+    void parallel(int n, const std::function<void(int)> &f) {
+        if (!pool) {
+            const int hw = std::max(1, (int)std::thread::hardware_concurrency());
+            pool.reset(new rp::HostPool(std::min(16, hw) - 1));
+        }
+        pool->run(n, f);
+    }
     int last_fallbacks = 0;    // cubes of the last batch redone in two passes after a clamp
     void *host_buf(const std::string &name, size_t bytes) {
         bytes = std::max<size_t>(256, (bytes + 255) & ~size_t(255));
@@ -172,7 +271,8 @@ struct rp_ewald {
     float4 *d_ezf = nullptr;      // (2kmax-1) * nz
     // every device table above lives in one block: `image` is its host copy, `off` the
     // table offsets; d_block is owned (rp_ewald_setup) or borrowed from a ctx arena (batches)
-    std::vector<char> image;
+    std::vector<char> image;  // empty when the image was written into a caller's arena
+    size_t image_bytes = 0;
     size_t off[9]{};
     void *d_block = nullptr;
     bool owns = false;
@@ -181,7 +281,10 @@ struct rp_ewald {
 namespace rp {
 
 // Ewald tables (ewald_tables.cu): host part, device image size, placement in a device block.
-void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax);
+// dst (optional, ewald_layout bytes): where the device image is written; else ew->image
+void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax, char *dst = nullptr);
+// offsets of the device tables in one image for this grid and KMAX, and its size
+size_t ewald_layout(const rp_grid *grid, int kmax, size_t off[9], int *K_out = nullptr);
 size_t ewald_device_bytes(const rp_ewald *ew);
 void ewald_place(rp_ewald *ew, void *dev);
 void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax);  // owns one cudaMalloc block
@@ -189,36 +292,6 @@ void ewald_free(rp_ewald *ew);
 
 // Host helpers shared by the stages.
 
-// f(i) for i in [0, n) on up to 16 host threads (the cubes of a batch are independent);
-// the first exception thrown is rethrown on the calling thread once all have joined.
-template <class F>
-void parallel_for(int n, F &&f) {
-    const int hw = std::max(1, (int)std::thread::hardware_concurrency());
-    const int nt = std::min(n, std::min(16, hw));
-    if (nt <= 1) {
-        for (int i = 0; i < n; ++i) f(i);
-        return;
-    }
-    std::atomic<int> next{0};
-    std::exception_ptr err;
-    std::mutex mu;
-    auto work = [&] {
-        for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1)) {
-            try {
-                f(i);
-            } catch (...) {
-                std::lock_guard<std::mutex> g(mu);
-                if (!err) err = std::current_exception();
-            }
-        }
-    };
-    std::vector<std::thread> th;
-    th.reserve((size_t)nt - 1);
-    for (int t = 1; t < nt; ++t) th.emplace_back(work);
-    work();
-    for (auto &t : th) t.join();
-    if (err) std::rethrow_exception(err);
-}
 
 void prune_shifts(const rp_ewald *ew, const double *atoms, int N, std::vector<double> &out, int &zero_idx);
 
@@ -260,6 +333,9 @@ struct FilterPlan {
     std::vector<double> rmax2;
     std::vector<float> rmax2f;
     std::vector<int> boff, bidx;
+    std::vector<D4> w_e64;       // working arrays of filter_plan (kept for their capacity)
+    std::vector<double> w_rmax2;
+    std::vector<int> w_binof, w_cur;
     size_t bytes() const;        // packed size: the arrays in order, each at a 32-byte offset
     void pack(char *dst) const;  // host image of the packed arrays
 };

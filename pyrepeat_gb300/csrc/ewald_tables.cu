@@ -26,7 +26,7 @@ static void cross3(const double *a, const double *b, double *c) {
     c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax) {
+void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax, char *dst) {
     RP_REQUIRE(cutoff > 0.0, "rp_ewald_setup: cutoff must be > 0");
     RP_REQUIRE(kmax >= 1 && kmax <= 64, "rp_ewald_setup: kmax must be in 1..64");
     for (int i = 0; i < 3; ++i) RP_REQUIRE(grid->n_grid[i] > 0, "rp_ewald_setup: grid counts must be > 0");
@@ -86,23 +86,54 @@ void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax
                     ew->shifts.push_back((ix * ew->box[d] + iy * ew->box[3 + d]) + iz * ew->box[6 + d]);
     ew->S = (int)(ew->shifts.size() / 3);
 
-    // per-axis phase tables, exact integer reduction of n*i mod n_axis
+    // the device image: tables at the offsets of ewald_layout, written straight into `dst`
+    // (a caller's arena) or into ew->image
     const int nx = grid->n_grid[0], ny = grid->n_grid[1], nz = grid->n_grid[2];
-    std::vector<double2> ex((size_t)(kmax + 1) * nx), ey((size_t)(2 * kmax + 1) * ny), ez((size_t)(2 * kmax + 1) * nz);
-    auto phase = [&](long long n, long long i, long long L) {
-        long long r = ((n * i) % L + L) % L;
-        double t = 2.0 * PI * (double)r / (double)L;
-        return make_double2(std::cos(t), std::sin(t));
-    };
-    for (int n = 0; n <= kmax; ++n)
-        for (int i = 0; i < nx; ++i) ex[(size_t)n * nx + i] = phase(n, i, nx);
-    for (int n = -kmax; n <= kmax; ++n) {
-        for (int j = 0; j < ny; ++j) ey[(size_t)(n + kmax) * ny + j] = phase(n, j, ny);
-        for (int l = 0; l < nz; ++l) ez[(size_t)(n + kmax) * nz + l] = phase(n, l, nz);
+    int K_layout = 0;
+    const size_t total = ewald_layout(grid, kmax, ew->off, &K_layout);
+    RP_REQUIRE(K_layout == ew->K, "rp_ewald_setup: k-set size mismatch");
+    ew->image_bytes = total;
+    char *img = dst;
+    if (!img) {
+        ew->image.assign(total, 0);
+        img = ew->image.data();
     }
+    std::memcpy(img + ew->off[0], ew->kidx.data(), sizeof(int) * ew->kidx.size());
+    std::memcpy(img + ew->off[1], ew->kcoef.data(), sizeof(double) * ew->kcoef.size());
+    std::memcpy(img + ew->off[2], ew->kvec.data(), sizeof(double) * ew->kvec.size());
+    double2 *ex = reinterpret_cast<double2 *>(img + ew->off[3]);
+    double2 *ey = reinterpret_cast<double2 *>(img + ew->off[4]);
+    double2 *ez = reinterpret_cast<double2 *>(img + ew->off[5]);
+    // per-axis phase tables: out[i] = e^{2 pi i (n i mod L) / L}, the residue stepped exactly in
+    // integers, from one table of the L roots of unity per axis
+    std::vector<double2> unit;
+    auto fill = [&](double2 *out, int n, int L) {
+        const int step = ((n % L) + L) % L;
+        int r = 0;
+        for (int i = 0; i < L; ++i) {
+            out[i] = unit[(size_t)r];
+            r += step;
+            if (r >= L) r -= L;
+        }
+    };
+    auto roots = [&](int L) {
+        unit.resize((size_t)L);
+        for (int r = 0; r < L; ++r) {
+            const double t = 2.0 * PI * (double)r / (double)L;
+            unit[(size_t)r] = make_double2(std::cos(t), std::sin(t));
+        }
+    };
+    roots(nx);
+    for (int n = 0; n <= kmax; ++n) fill(ex + (size_t)n * nx, n, nx);
+    roots(ny);
+    for (int n = -kmax; n <= kmax; ++n) fill(ey + (size_t)(n + kmax) * ny, n, ny);
+    roots(nz);
+    for (int n = -kmax; n <= kmax; ++n) fill(ez + (size_t)(n + kmax) * nz, n, nz);
     // double-float copies over n in [-(kmax-1), kmax-1] for the separable reciprocal sum
-    const int P = kmax - 1, nw = 2 * P + 1;
-    std::vector<float4> exf((size_t)(P + 1) * nx), eyf((size_t)nw * ny), ezf((size_t)nw * nz);
+    const int P = kmax - 1;
+    float4 *exf = reinterpret_cast<float4 *>(img + ew->off[6]);
+    float4 *eyf = reinterpret_cast<float4 *>(img + ew->off[7]);
+    float4 *ezf = reinterpret_cast<float4 *>(img + ew->off[8]);
     for (int n = 0; n <= P; ++n)
         for (int i = 0; i < nx; ++i) {
             const double2 v = ex[(size_t)n * nx + i];
@@ -118,27 +149,33 @@ void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax
             ezf[(size_t)(n + P) * nz + l] = dfa::split(v.x, v.y);
         }
     }
-    // one contiguous image of every device table (placed by ewald_place)
-    ew->image.clear();
-    auto put = [&](const void *src, size_t bytes) {
-        const size_t off = (ew->image.size() + 255) & ~size_t(255);
-        ew->image.resize(off + bytes);
-        if (bytes) std::memcpy(ew->image.data() + off, src, bytes);
-        return off;
-    };
-    ew->off[0] = put(ew->kidx.data(), sizeof(int) * ew->kidx.size());
-    ew->off[1] = put(ew->kcoef.data(), sizeof(double) * ew->kcoef.size());
-    ew->off[2] = put(ew->kvec.data(), sizeof(double) * ew->kvec.size());
-    ew->off[3] = put(ex.data(), sizeof(double2) * ex.size());
-    ew->off[4] = put(ey.data(), sizeof(double2) * ey.size());
-    ew->off[5] = put(ez.data(), sizeof(double2) * ez.size());
-    ew->off[6] = put(exf.data(), sizeof(float4) * exf.size());
-    ew->off[7] = put(eyf.data(), sizeof(float4) * eyf.size());
-    ew->off[8] = put(ezf.data(), sizeof(float4) * ezf.size());
-    ew->image.resize((ew->image.size() + 255) & ~size_t(255));
 }
 
-size_t ewald_device_bytes(const rp_ewald *ew) { return ew->image.size(); }
+size_t ewald_layout(const rp_grid *grid, int kmax, size_t off[9], int *K_out) {
+    int K = 0;
+    const int ksqmax = kmax * kmax;
+    for (int kx = 0; kx <= kmax; ++kx)
+        for (int ky = -kmax; ky <= kmax; ++ky)
+            for (int kz = -kmax; kz <= kmax; ++kz) {
+                const int s = kx * kx + ky * ky + kz * kz;
+                if (s < ksqmax && s != 0) ++K;
+            }
+    if (K_out) *K_out = K;
+    const size_t nx = grid->n_grid[0], ny = grid->n_grid[1], nz = grid->n_grid[2];
+    const size_t P = kmax - 1, nw = 2 * P + 1;
+    const size_t bytes[9] = {sizeof(int) * 3 * K, sizeof(double) * K, sizeof(double) * 3 * K,
+                             sizeof(double2) * (kmax + 1) * nx, sizeof(double2) * (2 * kmax + 1) * ny,
+                             sizeof(double2) * (2 * kmax + 1) * nz, sizeof(float4) * (P + 1) * nx,
+                             sizeof(float4) * nw * ny, sizeof(float4) * nw * nz};
+    size_t end = 0;
+    for (int t = 0; t < 9; ++t) {
+        off[t] = (end + 255) & ~size_t(255);
+        end = off[t] + bytes[t];
+    }
+    return (end + 255) & ~size_t(255);
+}
+
+size_t ewald_device_bytes(const rp_ewald *ew) { return ew->image_bytes; }
 
 void ewald_place(rp_ewald *ew, void *dev) {
     char *b = static_cast<char *>(dev);

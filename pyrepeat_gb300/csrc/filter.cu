@@ -364,8 +364,11 @@ void filter_plan(const rp_grid *grid, const double *atoms, const int *Z, int N, 
         }
     }
     const double margin = gmaxr + 0.1;
-    std::vector<D4> e64;
-    std::vector<double> rmax2;
+    // working arrays live in the plan, so a plan reused across batches allocates nothing
+    std::vector<D4> &e64 = plan.w_e64;
+    std::vector<double> &rmax2 = plan.w_rmax2;
+    e64.clear();
+    rmax2.clear();
     e64.reserve(27 * (size_t)N);
     double max_rmin = 0.0, max_rmax = 0.0, emax = 0.0;
     for (int a = 0; a < N; ++a) {
@@ -439,7 +442,10 @@ void filter_plan(const rp_grid *grid, const double *atoms, const int *Z, int N, 
         for (int d = 0; d < 3; ++d) bn[d] = std::max(1, (int)std::ceil((bmax[d] - bmin[d]) / bsize) + 1);
     }
     const int nb = bn[0] * bn[1] * bn[2];
-    std::vector<int> boff((size_t)nb + 1, 0), bidx((size_t)std::max(A, 1)), binof((size_t)std::max(A, 1));
+    std::vector<int> &boff = plan.boff, &bidx = plan.bidx, &binof = plan.w_binof;
+    boff.assign((size_t)nb + 1, 0);
+    bidx.resize((size_t)std::max(A, 1));
+    binof.resize((size_t)std::max(A, 1));
     for (int a = 0; a < A; ++a) {
         double p[3] = {e64[a].x, e64[a].y, e64[a].z};
         int b = 0, m = 1;
@@ -454,14 +460,19 @@ void filter_plan(const rp_grid *grid, const double *atoms, const int *Z, int N, 
     }
     for (int b = 0; b < nb; ++b) boff[b + 1] += boff[b];
     {
-        std::vector<int> cur(boff.begin(), boff.end() - 1);
+        std::vector<int> &cur = plan.w_cur;
+        cur.assign(boff.begin(), boff.end() - 1);
         for (int a = 0; a < A; ++a) bidx[cur[binof[a]]++] = a;
     }
     // FP32 copies, ordered by bin so a bin's atoms are contiguous in memory
-    std::vector<float4> e32((size_t)std::max(A, 1));
-    std::vector<D4> e64s((size_t)std::max(A, 1));
-    std::vector<double> rmax2s((size_t)std::max(A, 1));
-    std::vector<float> rmax2f((size_t)std::max(A, 1));
+    std::vector<float4> &e32 = plan.e32;
+    std::vector<D4> &e64s = plan.e64;
+    std::vector<double> &rmax2s = plan.rmax2;
+    std::vector<float> &rmax2f = plan.rmax2f;
+    e32.resize((size_t)std::max(A, 1));
+    e64s.resize((size_t)std::max(A, 1));
+    rmax2s.resize((size_t)std::max(A, 1));
+    rmax2f.resize((size_t)std::max(A, 1));
     for (int t = 0; t < A; ++t) {
         int a = bidx[t];
         e64s[t] = e64[a];
@@ -482,12 +493,6 @@ void filter_plan(const rp_grid *grid, const double *atoms, const int *Z, int N, 
     p.err_max = (float)err_max;
     p.near_all = near_all;
     p.A = A;
-    plan.e32 = std::move(e32);
-    plan.e64 = std::move(e64s);
-    plan.rmax2 = std::move(rmax2s);
-    plan.rmax2f = std::move(rmax2f);
-    plan.boff = std::move(boff);
-    plan.bidx = std::move(bidx);
 }
 
 namespace {

@@ -220,16 +220,17 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
         double *vst = ctx->buf_t<double>("fit_vstats", 2 * (size_t)n);
         rp::status_clear(ctx, stream);
         // 1. filters
-        std::vector<rp::FilterPlan> plans((size_t)n);
-        rp::parallel_for(n, [&](int i) {
+        while ((int)ctx->plan_pool.size() < n) ctx->plan_pool.emplace_back(new rp::FilterPlan());
+        auto plan = [&](int i) -> rp::FilterPlan & { return *ctx->plan_pool[(size_t)i]; };
+        ctx->parallel(n, [&](int i) {
             const rp_fit_desc &d = descs[i];
-            rp::filter_plan(&d.grid, d.atoms, d.Z, d.N, d.vdw_factor, d.vdw_max, plans[i]);
+            rp::filter_plan(&d.grid, d.atoms, d.Z, d.N, d.vdw_factor, d.vdw_max, plan(i));
         });
         std::vector<size_t> pl_off((size_t)n + 1, 0);
-        for (int i = 0; i < n; ++i) pl_off[i + 1] = pl_off[i] + plans[i].bytes();
+        for (int i = 0; i < n; ++i) pl_off[i + 1] = pl_off[i] + plan(i).bytes();
         char *pl_dev = static_cast<char *>(ctx->buf("fit_filter", pl_off[n]));
         char *pl_host = static_cast<char *>(ctx->host_buf("fit_filter", pl_off[n]));
-        rp::parallel_for(n, [&](int i) { plans[i].pack(pl_host + pl_off[i]); });
+        ctx->parallel(n, [&](int i) { plan(i).pack(pl_host + pl_off[i]); });
         RP_CUDA(cudaMemcpyAsync(pl_dev, pl_host, pl_off[n], cudaMemcpyHostToDevice, stream));
         for (int i = 0; i < n; ++i)
             if (!(V_dev && V_dev[i]))
@@ -256,27 +257,27 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             const rp_fit_desc &d = descs[i];
             const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
             const int ln = i % lanes;
-            rp::filter_launch(ctx, plans[i], pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i], Md + i,
+            rp::filter_launch(ctx, plan(i), pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i], Md + i,
                               nullptr, ctx->lane(ln), "#" + std::to_string(ln), d.precision == RP_PREC_MIXED,
                               vst + 2 * i);
         }
         join();
         std::vector<long long> M((size_t)n);
         RP_CUDA(cudaMemcpyAsync(M.data(), Md, sizeof(long long) * n, cudaMemcpyDeviceToHost, stream));
-        // 2. Ewald tables, placed in one ctx arena, uploaded with a single copy
+        // 2. Ewald tables, written by the host workers straight into one pinned arena,
+        //    uploaded with a single copy
         std::vector<size_t> ew_off((size_t)n + 1, 0);
+        while ((int)ctx->ew_pool.size() < n) ctx->ew_pool.emplace_back(new rp_ewald());
         for (int i = 0; i < n; ++i) {
-            ews[i] = new rp_ewald();
+            size_t off9[9];
+            ews[i] = ctx->ew_pool[(size_t)i].get();
             ews[i]->device = ctx->device;
+            ew_off[i + 1] = ew_off[i] + rp::ewald_layout(&descs[i].grid, descs[i].kmax, off9);
         }
-        rp::parallel_for(n, [&](int i) {
-            rp::ewald_build_host(ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax);
-        });
-        for (int i = 0; i < n; ++i) ew_off[i + 1] = ew_off[i] + rp::ewald_device_bytes(ews[i]);
         char *ew_dev = static_cast<char *>(ctx->buf("fit_ewald", ew_off[n]));
         char *ew_host = static_cast<char *>(ctx->host_buf("fit_ewald", ew_off[n]));
-        rp::parallel_for(n, [&](int i) {
-            std::memcpy(ew_host + ew_off[i], ews[i]->image.data(), ews[i]->image.size());
+        ctx->parallel(n, [&](int i) {
+            rp::ewald_build_host(ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax, ew_host + ew_off[i]);
         });
         for (int i = 0; i < n; ++i) rp::ewald_place(ews[i], ew_dev + ew_off[i]);
         RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, ew_off[n], cudaMemcpyHostToDevice, stream));
@@ -342,12 +343,7 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             if (info[4 * (size_t)i + 3] != 0.0)
                 rp::fail(RP_E_SINGULAR, "rp_fit: bordered system of cube " + std::to_string(i) + " is singular");
     });
-    for (rp_ewald *ew : ews)
-        if (ew) {
-            rp::ewald_free(ew);
-            delete ew;
-        }
-    return rc;
+    return rc;  // the pooled Ewald objects borrow the arena: nothing to free
 }
 
 int rp_launch_count(long long *out) {
