@@ -201,12 +201,19 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             off_nn[i + 1] = off_nn[i] + (long long)d.N * d.N;
         }
         // Work splits into host preparation and device stages so that the device never waits
-        // on the host inside the batch: (1) the filters' host halves, on all host threads,
-        // one pinned upload, and the filter launches spread over the lanes; (2) while they
-        // run, the Ewald tables of every cube, on all host threads, one pinned upload;
-        // (3) one read of the kept counts, which sizes every later launch.
+        // on the host inside the batch, and the cubes run as a pipeline of up to four groups:
+        // (1) the filters' host halves on the host workers, one pinned upload, and the filter
+        // launches of every group on their own streams; (2) while they run, the Ewald tables
+        // of every cube on the host workers, one pinned upload; (3) as each group's kept
+        // counts arrive, its normal equations go to the gram streams, so later groups'
+        // filters overlap earlier groups' grams.
         constexpr int kLanes = 4;
         const int lanes = ctx->timing ? 1 : kLanes;  // stage timing: one lane, each stage alone
+        auto glane = [&](int i) { return ctx->lane(i % lanes); };
+        auto flane = [&](int i) { return ctx->timing ? ctx->lane(0) : ctx->lane(kLanes + i % kLanes); };
+        const int ngroups = (n >= 64 && !ctx->timing) ? 4 : 1;
+        std::vector<int> g0((size_t)ngroups + 1);
+        for (int g = 0; g <= ngroups; ++g) g0[g] = (int)((long long)n * g / ngroups);
         int32_t *kept = ctx->buf_t<int32_t>("fit_kept", (size_t)off_pts[n]);
         double *Vc = ctx->buf_t<double>("fit_Vc", (size_t)off_pts[n]);
         double *Vh = nullptr;
@@ -214,11 +221,28 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
         for (int i = 0; i < n; ++i) any_host |= !(V_dev && V_dev[i]);
         if (any_host) Vh = ctx->buf_t<double>("fit_V", (size_t)off_pts[n]);
         long long *Md = ctx->buf_t<long long>("fit_M", (size_t)n);
+        long long *Mh = static_cast<long long *>(ctx->host_buf("fit_M", sizeof(long long) * n));
         double *A = ctx->buf_t<double>("fit_A", (size_t)off_nn[n]);
         double *b = ctx->buf_t<double>("fit_b", (size_t)off_n[n]);
         double *q = ctx->buf_t<double>("fit_q", (size_t)off_n[n]);
         double *vst = ctx->buf_t<double>("fit_vstats", 2 * (size_t)n);
+        int *clamps = ctx->buf_t<int>("fit_clamps", (size_t)n);
         rp::status_clear(ctx, stream);
+        RP_CUDA(cudaMemsetAsync(clamps, 0, sizeof(int) * n, stream));
+        std::vector<cudaEvent_t> events;
+        auto record = [&](cudaStream_t st) {
+            cudaEvent_t ev;
+            RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            events.push_back(ev);
+            RP_CUDA(cudaEventRecord(ev, st));
+            return ev;
+        };
+        struct EventGuard {  // destroyed on every exit (a recorded event may still be pending)
+            std::vector<cudaEvent_t> &e;
+            ~EventGuard() {
+                for (cudaEvent_t ev : e) cudaEventDestroy(ev);
+            }
+        } guard{events};
         // 1. filters
         while ((int)ctx->plan_pool.size() < n) ctx->plan_pool.emplace_back(new rp::FilterPlan());
         auto plan = [&](int i) -> rp::FilterPlan & { return *ctx->plan_pool[(size_t)i]; };
@@ -236,36 +260,30 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             if (!(V_dev && V_dev[i]))
                 RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], descs[i].V, sizeof(double) * npts[i],
                                         cudaMemcpyHostToDevice, stream));
-        auto fork = [&] {  // every lane waits for what the caller's stream holds so far
-            cudaEvent_t ev;
-            RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-            RP_CUDA(cudaEventRecord(ev, stream));
-            for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(ctx->lane(ln), ev, 0));
-            RP_CUDA(cudaEventDestroy(ev));
-        };
-        auto join = [&] {  // the caller's stream waits for every lane
-            for (int ln = 0; ln < lanes; ++ln) {
-                cudaEvent_t ev;
-                RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-                RP_CUDA(cudaEventRecord(ev, ctx->lane(ln)));
-                RP_CUDA(cudaStreamWaitEvent(stream, ev, 0));
-                RP_CUDA(cudaEventDestroy(ev));
+        {
+            const cudaEvent_t up = record(stream);  // every stream starts after the uploads
+            for (int ln = 0; ln < kLanes; ++ln) {
+                RP_CUDA(cudaStreamWaitEvent(ctx->lane(ln), up, 0));
+                RP_CUDA(cudaStreamWaitEvent(flane(ln), up, 0));
             }
-        };
-        fork();
-        for (int i = 0; i < n; ++i) {
-            const rp_fit_desc &d = descs[i];
-            const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
-            const int ln = i % lanes;
-            rp::filter_launch(ctx, plan(i), pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i], Md + i,
-                              nullptr, ctx->lane(ln), "#" + std::to_string(ln), d.precision == RP_PREC_MIXED,
-                              vst + 2 * i);
         }
-        join();
-        std::vector<long long> M((size_t)n);
-        RP_CUDA(cudaMemcpyAsync(M.data(), Md, sizeof(long long) * n, cudaMemcpyDeviceToHost, stream));
+        std::vector<cudaEvent_t> kept_ready((size_t)ngroups);
+        for (int g = 0; g < ngroups; ++g) {
+            for (int i = g0[g]; i < g0[g + 1]; ++i) {
+                const rp_fit_desc &d = descs[i];
+                const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
+                const int ln = i % lanes;
+                rp::filter_launch(ctx, plan(i), pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i], Md + i,
+                                  nullptr, flane(i), "#f" + std::to_string(ln), d.precision == RP_PREC_MIXED,
+                                  vst + 2 * i);
+            }
+            for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(stream, record(flane(ln)), 0));
+            RP_CUDA(cudaMemcpyAsync(Mh + g0[g], Md + g0[g], sizeof(long long) * (g0[g + 1] - g0[g]),
+                                    cudaMemcpyDeviceToHost, stream));
+            kept_ready[g] = record(stream);
+        }
         // 2. Ewald tables, written by the host workers straight into one pinned arena,
-        //    uploaded with a single copy
+        //    uploaded with a single copy on a stream of its own
         std::vector<size_t> ew_off((size_t)n + 1, 0);
         while ((int)ctx->ew_pool.size() < n) ctx->ew_pool.emplace_back(new rp_ewald());
         for (int i = 0; i < n; ++i) {
@@ -280,43 +298,49 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             rp::ewald_build_host(ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax, ew_host + ew_off[i]);
         });
         for (int i = 0; i < n; ++i) rp::ewald_place(ews[i], ew_dev + ew_off[i]);
-        RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, ew_off[n], cudaMemcpyHostToDevice, stream));
-        // 3. the kept counts (and the tables) are on hand after one synchronisation
-        RP_CUDA(cudaStreamSynchronize(stream));
-        for (int i = 0; i < n; ++i) {
-            if (M_out) M_out[i] = M[i];
-            RP_REQUIRE(M[i] > 0, "rp_fit: no grid point of cube " + std::to_string(i) + " survives the vdW filter");
-        }
-        // 4. normal equations of every cube.  Mixed-precision fits are spread over the
-        //    lanes (worker streams, each with its own scratch), so one cube's small kernels
-        //    and launch gaps overlap another's; the FP64 comparator stays on the caller's
-        //    stream (its cuBLAS handle is shared).  Every cube's result is independent of
-        //    the lane it ran on.
-        //    A mixed fit takes the single pass (Phi straight to digits, scaled by the a-priori
-        //    bounds from the scaled vdW radii); a cube whose values clamp (a cell the bound's
-        //    argument does not cover) is redone below in two passes.
+        const cudaStream_t copy_lane = ctx->lane(2 * kLanes);
+        RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, ew_off[n], cudaMemcpyHostToDevice, copy_lane));
+        const cudaEvent_t tables = record(copy_lane);
+        for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(glane(ln), tables, 0));
+        RP_CUDA(cudaStreamWaitEvent(stream, tables, 0));
+        // 3. normal equations, group by group as the kept counts arrive.  Mixed-precision fits
+        //    are spread over the gram streams (each with its own scratch), so one cube's small
+        //    kernels and launch gaps overlap another's; the FP64 comparator stays on the
+        //    caller's stream (its cuBLAS handle is shared).  Every cube's result is independent
+        //    of the stream it ran on.  A mixed fit takes the single pass (Phi straight to
+        //    digits, scaled by the a-priori bounds from the scaled vdW radii); a cube whose
+        //    values clamp (a cell the bound's argument does not cover) is redone below in
+        //    two passes.
         std::vector<double> rn((size_t)off_n[n]);
         for (int i = 0; i < n; ++i)
             for (int a = 0; a < descs[i].N; ++a)
                 rn[off_n[i] + a] = descs[i].vdw_factor * rp::radius_of(descs[i].Z[a]);
-        int *clamps = ctx->buf_t<int>("fit_clamps", (size_t)n);
-        RP_CUDA(cudaMemsetAsync(clamps, 0, sizeof(int) * n, stream));
-        fork();
-        for (int i = 0; i < n; ++i) {
-            const rp_fit_desc &d = descs[i];
-            if (d.precision == RP_PREC_MIXED) {
-                const int ln = i % lanes;
-                rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
-                               b + off_n[i], nullptr, ctx->lane(ln), vst + 2 * i, "#" + std::to_string(ln),
-                               rn.data() + off_n[i], clamps + i);
-            } else {
-                rp::gram_fp64(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
-                              b + off_n[i], nullptr, stream);
+        std::vector<long long> M((size_t)n);
+        for (int g = 0; g < ngroups; ++g) {
+            RP_CUDA(cudaEventSynchronize(kept_ready[g]));
+            for (int i = g0[g]; i < g0[g + 1]; ++i) {
+                M[i] = Mh[i];
+                if (M_out) M_out[i] = M[i];
+                RP_REQUIRE(M[i] > 0, "rp_fit: no grid point of cube " + std::to_string(i) + " survives the vdW filter");
+            }
+            for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(glane(ln), kept_ready[g], 0));
+            for (int i = g0[g]; i < g0[g + 1]; ++i) {
+                const rp_fit_desc &d = descs[i];
+                if (d.precision == RP_PREC_MIXED) {
+                    const int ln = i % lanes;
+                    rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i],
+                                   A + off_nn[i], b + off_n[i], nullptr, glane(ln), vst + 2 * i,
+                                   "#" + std::to_string(ln), rn.data() + off_n[i], clamps + i);
+                } else {
+                    rp::gram_fp64(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
+                                  b + off_n[i], nullptr, stream);
+                }
             }
         }
-        join();  // the solve on the caller's stream waits for every lane
-        std::vector<int> hclamps((size_t)n);
-        RP_CUDA(cudaMemcpyAsync(hclamps.data(), clamps, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
+        for (int ln = 0; ln < lanes; ++ln)  // the solve on the caller's stream waits for every lane
+            RP_CUDA(cudaStreamWaitEvent(stream, record(glane(ln)), 0));
+        int *hclamps = static_cast<int *>(ctx->host_buf("fit_clamps", sizeof(int) * n));
+        RP_CUDA(cudaMemcpyAsync(hclamps, clamps, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
         RP_CUDA(cudaStreamSynchronize(stream));
         ctx->last_fallbacks = 0;
         for (int i = 0; i < n; ++i)
