@@ -220,7 +220,8 @@ def main():
     ap.add_argument("--n-cubes", type=int, default=256)
     ap.add_argument("--fp64-cubes", type=int, default=8, help="cubes of the plain FP64 comparator")
     ap.add_argument("--latency-fits", type=int, default=32, help="single fits timed for p50/p99")
-    ap.add_argument("--cpu-sample", type=int, default=2000, help="kept points of the CPU baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=120000,
+                    help="kept points of the CPU baseline sample (capped at the cube's kept count; ~5-10 s of CPU)")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
 
