@@ -256,10 +256,6 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
         char *pl_host = static_cast<char *>(ctx->host_buf("fit_filter", pl_off[n]));
         ctx->parallel(n, [&](int i) { plan(i).pack(pl_host + pl_off[i]); });
         RP_CUDA(cudaMemcpyAsync(pl_dev, pl_host, pl_off[n], cudaMemcpyHostToDevice, stream));
-        for (int i = 0; i < n; ++i)
-            if (!(V_dev && V_dev[i]))
-                RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], descs[i].V, sizeof(double) * npts[i],
-                                        cudaMemcpyHostToDevice, stream));
         {
             const cudaEvent_t up = record(stream);  // every stream starts after the uploads
             for (int ln = 0; ln < kLanes; ++ln) {
@@ -267,8 +263,23 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
                 RP_CUDA(cudaStreamWaitEvent(flane(ln), up, 0));
             }
         }
+        // grids from host memory: one group at a time on the copy stream, so a group's filters
+        // start as soon as its own grids are on the device
+        const cudaStream_t copy_lane = ctx->lane(2 * kLanes);
+        RP_CUDA(cudaStreamWaitEvent(copy_lane, events.back(), 0));
         std::vector<cudaEvent_t> kept_ready((size_t)ngroups);
         for (int g = 0; g < ngroups; ++g) {
+            bool copied = false;
+            for (int i = g0[g]; i < g0[g + 1]; ++i)
+                if (!(V_dev && V_dev[i])) {
+                    RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], descs[i].V, sizeof(double) * npts[i],
+                                            cudaMemcpyHostToDevice, copy_lane));
+                    copied = true;
+                }
+            if (copied) {
+                const cudaEvent_t grids = record(copy_lane);
+                for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(flane(ln), grids, 0));
+            }
             for (int i = g0[g]; i < g0[g + 1]; ++i) {
                 const rp_fit_desc &d = descs[i];
                 const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
@@ -298,7 +309,6 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             rp::ewald_build_host(ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax, ew_host + ew_off[i]);
         });
         for (int i = 0; i < n; ++i) rp::ewald_place(ews[i], ew_dev + ew_off[i]);
-        const cudaStream_t copy_lane = ctx->lane(2 * kLanes);
         RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, ew_off[n], cudaMemcpyHostToDevice, copy_lane));
         const cudaEvent_t tables = record(copy_lane);
         for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(glane(ln), tables, 0));
