@@ -381,6 +381,11 @@ struct SolveJob {
     double *q;
 };
 void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream);
+// The same without waiting: returns the pinned host copy of the 4 info words per job, valid
+// once `stream` has reached this point.  `tag` keeps the scratch of solves in flight apart.
+// (Systems with overlapping symmetry groups are folded on the host, which waits.)
+const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, cudaStream_t stream,
+                                const std::string &tag);
 
 // Device table builders (ewald_tables.cu).
 void atom_tables_fp64(const rp_ewald *ew, const double *d_atoms, int N, double *d_B, int ldb, cudaStream_t s);

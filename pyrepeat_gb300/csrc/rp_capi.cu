@@ -326,6 +326,12 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
             for (int a = 0; a < descs[i].N; ++a)
                 rn[off_n[i] + a] = descs[i].vdw_factor * rp::radius_of(descs[i].Z[a]);
         std::vector<long long> M((size_t)n);
+        auto job = [&](int i) {
+            const rp_fit_desc &d = descs[i];
+            return rp::SolveJob{A + off_nn[i], b + off_n[i], d.N, d.n_groups, d.group_ptr, d.group_idx,
+                                d.resp_s, d.resp_t, d.qtot, q + off_n[i]};
+        };
+        std::vector<const double *> ginfo((size_t)ngroups);
         for (int g = 0; g < ngroups; ++g) {
             RP_CUDA(cudaEventSynchronize(kept_ready[g]));
             for (int i = g0[g]; i < g0[g + 1]; ++i) {
@@ -346,29 +352,39 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
                                   b + off_n[i], nullptr, stream);
                 }
             }
+            // 4. the group's constraint folds and bordered solves (one launch) on the caller's
+            //    stream, behind its normal equations and overlapping the next group's
+            for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(stream, record(glane(ln)), 0));
+            std::vector<rp::SolveJob> jobs;
+            for (int i = g0[g]; i < g0[g + 1]; ++i) jobs.push_back(job(i));
+            ginfo[g] = rp::solve_batch_async(ctx, jobs, stream, "#g" + std::to_string(g));
         }
-        for (int ln = 0; ln < lanes; ++ln)  // the solve on the caller's stream waits for every lane
-            RP_CUDA(cudaStreamWaitEvent(stream, record(glane(ln)), 0));
         int *hclamps = static_cast<int *>(ctx->host_buf("fit_clamps", sizeof(int) * n));
         RP_CUDA(cudaMemcpyAsync(hclamps, clamps, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
         RP_CUDA(cudaStreamSynchronize(stream));
+        std::vector<double> info((size_t)n * 4);
+        for (int g = 0; g < ngroups; ++g)
+            std::copy(ginfo[g], ginfo[g] + 4 * (size_t)(g0[g + 1] - g0[g]), info.begin() + 4 * (size_t)g0[g]);
+        // 5. a cube whose values clamped: the two-pass fit, centred and scaled by the data, and
+        //    its solve again
         ctx->last_fallbacks = 0;
+        std::vector<int> redo;
         for (int i = 0; i < n; ++i)
-            if (hclamps[i] != 0) {  // the two-pass fit, centred and scaled by the data
+            if (hclamps[i] != 0) {
                 ++ctx->last_fallbacks;
+                redo.push_back(i);
                 const rp_fit_desc &d = descs[i];
                 rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
                                b + off_n[i], nullptr, stream, vst + 2 * i, "");
             }
-        // 5. all constraint folds and bordered solves, one launch
-        std::vector<rp::SolveJob> jobs((size_t)n);
-        for (int i = 0; i < n; ++i) {
-            const rp_fit_desc &d = descs[i];
-            jobs[i] = rp::SolveJob{A + off_nn[i], b + off_n[i], d.N, d.n_groups, d.group_ptr, d.group_idx,
-                                   d.resp_s, d.resp_t, d.qtot, q + off_n[i]};
+        if (!redo.empty()) {
+            std::vector<rp::SolveJob> jobs;
+            for (int i : redo) jobs.push_back(job(i));
+            std::vector<double> rinfo;
+            rp::solve_batch(ctx, jobs, rinfo, stream);
+            for (size_t t = 0; t < redo.size(); ++t)
+                std::copy(rinfo.begin() + 4 * t, rinfo.begin() + 4 * t + 4, info.begin() + 4 * (size_t)redo[t]);
         }
-        std::vector<double> info;
-        rp::solve_batch(ctx, jobs, info, stream);
         rp::status_check(ctx, stream);
         RP_CUDA(cudaMemcpyAsync(q_out, q, sizeof(double) * off_n[n], cudaMemcpyDeviceToHost, stream));
         RP_CUDA(cudaStreamSynchronize(stream));

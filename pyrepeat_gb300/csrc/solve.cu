@@ -23,6 +23,7 @@
 // way the refined residual and the pivot range are reported.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <set>
 
@@ -478,10 +479,10 @@ static void host_fold(int N, const std::vector<double> &A, const std::vector<dou
     }
 }
 
-void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream) {
+const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, cudaStream_t stream,
+                                const std::string &tag) {
     const int nj = (int)jobs.size();
-    info.assign((size_t)nj * 4, 0.0);
-    if (nj == 0) return;
+    if (nj == 0) return nullptr;
     std::vector<FoldPlan> plans((size_t)nj);
     size_t n_map = 0, n_mptr = 0, n_midx = 0, n_red = 0, n_sq = 0;
     for (int j = 0; j < nj; ++j) {
@@ -496,19 +497,19 @@ void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<dou
         n_red += n1;
         n_sq += n1 * n1;
     }
-    int *d_map = ctx->buf_t<int>("s_map", n_map);
-    int *d_mptr = ctx->buf_t<int>("s_mptr", n_mptr);
-    int *d_midx = ctx->buf_t<int>("s_midx", n_midx);
-    double *d_rs = ctx->buf_t<double>("s_rs", n_red);
-    double *d_rt = ctx->buf_t<double>("s_rt", n_red);
-    double *As = ctx->buf_t<double>("s_As", n_sq);
-    double *A0 = ctx->buf_t<double>("s_A0", n_sq);
-    double *bs = ctx->buf_t<double>("s_bs", n_red);
-    double *x = ctx->buf_t<double>("s_x", n_red);
-    double *r = ctx->buf_t<double>("s_r", n_red);
-    int *perm = ctx->buf_t<int>("s_perm", n_red);
-    double *d_info = ctx->buf_t<double>("s_info", (size_t)nj * 4);
-    SolveDesc *d_desc = ctx->buf_t<SolveDesc>("s_desc", (size_t)nj);
+    int *d_map = ctx->buf_t<int>("s_map" + tag, n_map);
+    int *d_mptr = ctx->buf_t<int>("s_mptr" + tag, n_mptr);
+    int *d_midx = ctx->buf_t<int>("s_midx" + tag, n_midx);
+    double *d_rs = ctx->buf_t<double>("s_rs" + tag, n_red);
+    double *d_rt = ctx->buf_t<double>("s_rt" + tag, n_red);
+    double *As = ctx->buf_t<double>("s_As" + tag, n_sq);
+    double *A0 = ctx->buf_t<double>("s_A0" + tag, n_sq);
+    double *bs = ctx->buf_t<double>("s_bs" + tag, n_red);
+    double *x = ctx->buf_t<double>("s_x" + tag, n_red);
+    double *r = ctx->buf_t<double>("s_r" + tag, n_red);
+    int *perm = ctx->buf_t<int>("s_perm" + tag, n_red);
+    double *d_info = ctx->buf_t<double>("s_info" + tag, (size_t)nj * 4);
+    SolveDesc *d_desc = ctx->buf_t<SolveDesc>("s_desc" + tag, (size_t)nj);
     // host staging of the small per-system tables, one upload each
     std::vector<int> h_map(n_map), h_mptr(n_mptr), h_midx(n_midx, 0);
     std::vector<double> h_rs(n_red, 0.0), h_rt(n_red, 0.0);
@@ -539,11 +540,26 @@ void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<dou
         o_red += (size_t)n1;
         o_sq += (size_t)n1 * n1;
     }
-    RP_CUDA(cudaMemcpyAsync(d_map, h_map.data(), sizeof(int) * n_map, cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemcpyAsync(d_mptr, h_mptr.data(), sizeof(int) * n_mptr, cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemcpyAsync(d_midx, h_midx.data(), sizeof(int) * n_midx, cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemcpyAsync(d_rs, h_rs.data(), sizeof(double) * n_red, cudaMemcpyHostToDevice, stream));
-    RP_CUDA(cudaMemcpyAsync(d_rt, h_rt.data(), sizeof(double) * n_red, cudaMemcpyHostToDevice, stream));
+    // the small tables go up from one pinned staging block per tag (asynchronous copies that
+    // never wait for the stream; a later solve with another tag cannot overwrite them)
+    const size_t st_bytes[6] = {sizeof(int) * n_map, sizeof(int) * n_mptr, sizeof(int) * n_midx,
+                                sizeof(double) * n_red, sizeof(double) * n_red, sizeof(SolveDesc) * nj};
+    size_t st_off[6], st_end = 0;
+    for (int t = 0; t < 6; ++t) {
+        st_off[t] = st_end;
+        st_end += (st_bytes[t] + 15) / 16 * 16;
+    }
+    char *stage = static_cast<char *>(ctx->host_buf("s_stage" + tag, st_end));
+    std::memcpy(stage + st_off[0], h_map.data(), st_bytes[0]);
+    std::memcpy(stage + st_off[1], h_mptr.data(), st_bytes[1]);
+    std::memcpy(stage + st_off[2], h_midx.data(), st_bytes[2]);
+    std::memcpy(stage + st_off[3], h_rs.data(), st_bytes[3]);
+    std::memcpy(stage + st_off[4], h_rt.data(), st_bytes[4]);
+    RP_CUDA(cudaMemcpyAsync(d_map, stage + st_off[0], st_bytes[0], cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_mptr, stage + st_off[1], st_bytes[1], cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_midx, stage + st_off[2], st_bytes[2], cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_rs, stage + st_off[3], st_bytes[3], cudaMemcpyHostToDevice, stream));
+    RP_CUDA(cudaMemcpyAsync(d_rt, stage + st_off[4], st_bytes[4], cudaMemcpyHostToDevice, stream));
     for (int j = 0; j < nj; ++j) {
         const SolveJob &J = jobs[j];
         const FoldPlan &p = plans[j];
@@ -576,7 +592,8 @@ void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<dou
             RP_CUDA(cudaStreamSynchronize(stream));
         }
     }
-    RP_CUDA(cudaMemcpyAsync(d_desc, descs.data(), sizeof(SolveDesc) * nj, cudaMemcpyHostToDevice, stream));
+    std::memcpy(stage + st_off[5], descs.data(), st_bytes[5]);
+    RP_CUDA(cudaMemcpyAsync(d_desc, stage + st_off[5], st_bytes[5], cudaMemcpyHostToDevice, stream));
     {
         StageTimer tt(ctx, "solve_lu", stream);
         int n1max = 1;
@@ -584,8 +601,18 @@ void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<dou
         lu_solve_refine_kernel<<<nj, kLU, solve_smem_bytes(n1max), stream>>>(d_desc);
         RP_LAUNCH_CHECK();
     }
-    RP_CUDA(cudaMemcpyAsync(info.data(), d_info, sizeof(double) * 4 * nj, cudaMemcpyDeviceToHost, stream));
+    double *h_info = static_cast<double *>(ctx->host_buf("s_info" + tag, sizeof(double) * 4 * nj));
+    RP_CUDA(cudaMemcpyAsync(h_info, d_info, sizeof(double) * 4 * nj, cudaMemcpyDeviceToHost, stream));
+    return h_info;
+}
+
+void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream) {
+    const int nj = (int)jobs.size();
+    info.assign((size_t)nj * 4, 0.0);
+    if (nj == 0) return;
+    const double *h = solve_batch_async(ctx, jobs, stream, "");
     RP_CUDA(cudaStreamSynchronize(stream));
+    std::copy(h, h + 4 * (size_t)nj, info.begin());
 }
 
 void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
