@@ -212,7 +212,13 @@ __device__ bool lu_factor_f32(float *A, int *perm, int n1, double *sv, int *si, 
 // x = (P L U)^{-1} y with the FP32 factors; y (overwritten) and x in shared memory.
 // One barrier per column: forward elimination updates y below the column, backward
 // substitution writes x[c] and updates y above it.
+// Solve LU x = P y in FP32 (unit lower L, upper U, both in LU), blocked by 32 columns: the
+// 32x32 diagonal block is staged in shared memory and solved by one warp (shuffles, no block
+// barrier), then every warp updates the remaining rows with the block's 32 values (a warp per
+// row, coalesced).  Three block barriers per 32 columns instead of one per column.
 __device__ void lu_apply_f32(const float *__restrict__ LU, const int *__restrict__ perm, int n1, float *y, float *x) {
+    __shared__ float blk[32][33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __syncthreads();
     if (threadIdx.x == 0)
         for (int k = 0; k < n1; ++k) {
@@ -220,19 +226,59 @@ __device__ void lu_apply_f32(const float *__restrict__ LU, const int *__restrict
             if (p != k) { const float t = y[k]; y[k] = y[p]; y[p] = t; }
         }
     __syncthreads();
-    for (int c = 0; c < n1; ++c) {
-        const float yc = y[c];
-        for (int r = c + 1 + threadIdx.x; r < n1; r += kLU) y[r] -= LU[(size_t)r * n1 + c] * yc;
+    // forward: L (unit diagonal)
+    for (int c0 = 0; c0 < n1; c0 += 32) {
+        const int bs = min(32, n1 - c0);
+        for (int t = threadIdx.x; t < bs * 32; t += kLU) {
+            const int r = t >> 5, c = t & 31;
+            blk[r][c] = c < bs ? LU[(size_t)(c0 + r) * n1 + c0 + c] : 0.f;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            float yv = lane < bs ? y[c0 + lane] : 0.f;
+            for (int c = 0; c < bs - 1; ++c) {
+                const float yc = __shfl_sync(0xffffffffu, yv, c);
+                if (lane > c && lane < bs) yv -= blk[lane][c] * yc;
+            }
+            if (lane < bs) y[c0 + lane] = yv;
+        }
+        __syncthreads();
+        for (int r = c0 + bs + warp; r < n1; r += kLU / 32) {
+            float t = lane < bs ? LU[(size_t)r * n1 + c0 + lane] * y[c0 + lane] : 0.f;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) y[r] -= t;
+        }
         __syncthreads();
     }
-    for (int c = n1 - 1; c >= 0; --c) {
-        const float xc = y[c] / LU[(size_t)c * n1 + c];
-        if (threadIdx.x == 0) x[c] = xc;
-        for (int r = threadIdx.x; r < c; r += kLU) y[r] -= LU[(size_t)r * n1 + c] * xc;
+    // backward: U
+    for (int c1 = n1; c1 > 0; c1 -= 32) {
+        const int c0 = max(0, c1 - 32), bs = c1 - c0;
+        for (int t = threadIdx.x; t < bs * 32; t += kLU) {
+            const int r = t >> 5, c = t & 31;
+            blk[r][c] = c < bs ? LU[(size_t)(c0 + r) * n1 + c0 + c] : 0.f;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            float yv = lane < bs ? y[c0 + lane] : 0.f;
+            for (int c = bs - 1; c >= 0; --c) {
+                if (lane == c) yv = yv / blk[c][c];
+                const float xc = __shfl_sync(0xffffffffu, yv, c);
+                if (lane < c) yv -= blk[lane][c] * xc;
+            }
+            if (lane < bs) {
+                y[c0 + lane] = yv;
+                x[c0 + lane] = yv;
+            }
+        }
+        __syncthreads();
+        for (int r = warp; r < c0; r += kLU / 32) {
+            float t = lane < bs ? LU[(size_t)r * n1 + c0 + lane] * x[c0 + lane] : 0.f;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) y[r] -= t;
+        }
         __syncthreads();
     }
 }
-
 constexpr int kRefineMax = 30;
 
 // r = bs - A0 x in FP64: a warp per row, lanes along the row, fixed-order shuffle sum
