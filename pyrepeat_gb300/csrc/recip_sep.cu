@@ -16,9 +16,9 @@
 // Stage C costs 2 KMAX real multiply-adds per point-atom instead of the 4 K of a dense
 // point x k table contraction (K = 754 at KMAX 7): ~50x fewer operations, so the
 // whole sum runs on the FP32 pipe instead of as a tensor-core GEMM.  The weights W
-// and stage A are double-float (exact to ~2^-44); stages B and C use FP32 products
-// (unbiased rounding, ~1e-7 relative like the FP32 real-space terms), stored as
-// float2 E rows.
+// are double-float (exact to ~2^-44); stages A, B and C use FP32 products of their
+// high parts (unbiased rounding, ~1e-7 relative like the FP32 real-space terms;
+// measured 2.6-3.1e-7 of max|Phi| against FP64), with F and E stored as float2.
 // Indices n1 in [0, P], n2, n3 in [-P, P] with P = KMAX - 1 (the k-set keeps
 // n1^2 + n2^2 + n3^2 < KMAX^2); stored with offset P on n2 and n3.
 #include <algorithm>
@@ -101,7 +101,7 @@ __global__ void build_w_kernel(const int *__restrict__ kidx, const double *__res
 constexpr int kN1B = 8;
 
 // Stage A, one thread per (n2, column, n1 block, plane l) with l fastest: a warp reads
-// one W row (broadcast) and consecutive ez phases (coalesced).
+// one W row (broadcast) and consecutive ez phases (coalesced); FP32 products.
 __global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 *__restrict__ EZ, int ncols, int P,
                                      int nz, float2 *__restrict__ F) {
     extern __shared__ float4 ezs[];  // the whole ez table [nw][nz], read once per CTA
@@ -117,21 +117,21 @@ __global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 
     const int a = (int)(t % ncols);
     const int n2 = (int)(t / ncols);
     const int n10 = b * kN1B, cnt = min(kN1B, n1c - n10);
-    dfa::acc re[kN1B], im[kN1B];
+    float re[kN1B], im[kN1B];
 #pragma unroll
-    for (int u = 0; u < kN1B; ++u) re[u] = im[u] = dfa::acc{0.f, 0.f};
+    for (int u = 0; u < kN1B; ++u) re[u] = im[u] = 0.f;
     const float4 *w = W + ((long long)a * nw + n2) * nw * n1c + n10;
     for (int n3 = 0; n3 < nw; ++n3) {
         const float4 z = ezs[n3 * nz + l];
         const float4 *wr = w + (long long)n3 * n1c;
 #pragma unroll
         for (int u = 0; u < kN1B; ++u)
-            if (u < cnt) dfa::cmac(re[u], im[u], z, wr[u]);
+            if (u < cnt) dfa::cmac32(re[u], im[u], z, wr[u]);
     }
     float2 *o = F + (((long long)l * nw + n2) * ncols + a) * n1c + n10;
 #pragma unroll
     for (int u = 0; u < kN1B; ++u)
-        if (u < cnt) o[u] = make_float2(dfa::norm(re[u]).x, dfa::norm(im[u]).x);  // stage B takes FP32
+        if (u < cnt) o[u] = make_float2(re[u], im[u]);
 }
 
 // Stage B, one CTA per (plane l, block of `ab` columns).  The plane's F slab for those
