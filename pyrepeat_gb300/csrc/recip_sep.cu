@@ -16,8 +16,8 @@
 // Stage C costs 2 KMAX real multiply-adds per point-atom instead of the 4 K of a dense
 // point x k table contraction (K = 754 at KMAX 7): ~50x fewer operations, so the
 // whole sum runs on the FP32 pipe instead of as a tensor-core GEMM.  The weights W
-// are double-float (exact to ~2^-44); stages A, B and C use FP32 products of their
-// high parts (unbiased rounding, ~1e-7 relative like the FP32 real-space terms;
+// are computed in double-float (~2^-44) and stored rounded to FP32; stages A, B and C
+// use FP32 products (unbiased rounding, ~1e-7 relative like the FP32 real-space terms;
 // measured 2.6-3.1e-7 of max|Phi| against FP64), with F and E stored as float2.
 // Indices n1 in [0, P], n2, n3 in [-P, P] with P = KMAX - 1 (the k-set keeps
 // n1^2 + n2^2 + n3^2 < KMAX^2); stored with offset P on n2 and n3.
@@ -55,12 +55,12 @@ __device__ __forceinline__ double2 cmul(double2 x, double2 y) {
 }
 
 // W[col][n2'][n3'][n1] = w_k e^{-i k.r} (col = atom), or sum_a q_a w_k e^{-i k.r_a} (one
-// charge-weighted column when q != nullptr), stored as double-float.  Per atom the two
+// charge-weighted column when q != nullptr), stored rounded to FP32.  Per atom the two
 // phase products and the weight are double-float products on the FP32 pipe (~2^-44
 // relative); the charge-weighted sum stays FP64.
 __global__ void build_w_kernel(const int *__restrict__ kidx, const double *__restrict__ kcoef, int K, int P,
                                const double2 *__restrict__ U, const float4 *__restrict__ Udf,
-                               const double *__restrict__ q, int N, int ncols, float4 *__restrict__ W) {
+                               const double *__restrict__ q, int N, int ncols, float2 *__restrict__ W) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)ncols * K) return;
     const int col = (int)(t / K), k = (int)(t - (long long)col * K);
@@ -80,7 +80,7 @@ __global__ void build_w_kernel(const int *__restrict__ kidx, const double *__res
         re = im = dfa::acc{0.f, 0.f};
         dfa::mac(re, wh, wl, z3.x, z3.y);
         dfa::mac(im, wh, wl, z3.z, z3.w);
-        W[(((long long)col * nw + n2) * nw + n3) * n1c + n1] = dfa::pack(re, im);
+        W[(((long long)col * nw + n2) * nw + n3) * n1c + n1] = make_float2(dfa::norm(re).x, dfa::norm(im).x);
         return;
     } else {
         z = make_double2(0.0, 0.0);
@@ -92,7 +92,7 @@ __global__ void build_w_kernel(const int *__restrict__ kidx, const double *__res
         }
     }
     const double w = kcoef[k];
-    W[(((long long)col * nw + n2) * nw + n3) * n1c + n1] = dfa::split(w * z.x, w * z.y);
+    W[(((long long)col * nw + n2) * nw + n3) * n1c + n1] = make_float2((float)(w * z.x), (float)(w * z.y));
 }
 
 // Each stage-A thread produces up to kN1B consecutive n1 outputs of one (plane, n2,
@@ -102,11 +102,14 @@ constexpr int kN1B = 8;
 
 // Stage A, one thread per (n2, column, n1 block, plane l) with l fastest: a warp reads
 // one W row (broadcast) and consecutive ez phases (coalesced); FP32 products.
-__global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 *__restrict__ EZ, int ncols, int P,
+__global__ void recip_stage_a_kernel(const float2 *__restrict__ W, const float4 *__restrict__ EZ, int ncols, int P,
                                      int nz, float2 *__restrict__ F) {
-    extern __shared__ float4 ezs[];  // the whole ez table [nw][nz], read once per CTA
+    extern __shared__ float2 ezs[];  // the whole ez table [nw][nz] (FP32), read once per CTA
     const int n1c = P + 1, nw = 2 * P + 1, nb = (n1c + kN1B - 1) / kN1B;
-    for (int q = threadIdx.x; q < nw * nz; q += blockDim.x) ezs[q] = EZ[q];
+    for (int q = threadIdx.x; q < nw * nz; q += blockDim.x) {
+        const float4 e = EZ[q];
+        ezs[q] = make_float2(e.x, e.z);
+    }
     __syncthreads();
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nz * nw * ncols * nb) return;
@@ -120,13 +123,19 @@ __global__ void recip_stage_a_kernel(const float4 *__restrict__ W, const float4 
     float re[kN1B], im[kN1B];
 #pragma unroll
     for (int u = 0; u < kN1B; ++u) re[u] = im[u] = 0.f;
-    const float4 *w = W + ((long long)a * nw + n2) * nw * n1c + n10;
+    const float2 *w = W + ((long long)a * nw + n2) * nw * n1c + n10;
     for (int n3 = 0; n3 < nw; ++n3) {
-        const float4 z = ezs[n3 * nz + l];
-        const float4 *wr = w + (long long)n3 * n1c;
+        const float2 z = ezs[n3 * nz + l];
+        const float2 *wr = w + (long long)n3 * n1c;
 #pragma unroll
         for (int u = 0; u < kN1B; ++u)
-            if (u < cnt) dfa::cmac32(re[u], im[u], z, wr[u]);
+            if (u < cnt) {
+                const float2 v = wr[u];
+                re[u] = fmaf(z.x, v.x, re[u]);
+                re[u] = fmaf(-z.y, v.y, re[u]);
+                im[u] = fmaf(z.x, v.y, im[u]);
+                im[u] = fmaf(z.y, v.x, im[u]);
+            }
     }
     float2 *o = F + (((long long)l * nw + n2) * ncols + a) * n1c + n10;
 #pragma unroll
@@ -209,11 +218,11 @@ void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const do
         return;
     }
     const size_t nW = (size_t)ncols * nw * nw * n1c, nF = (size_t)nz * nw * ncols * n1c;
-    float4 *W = ctx->buf_t<float4>("rs_W" + slot, nW);
+    float2 *W = ctx->buf_t<float2>("rs_W" + slot, nW);
     float2 *F = ctx->buf_t<float2>("rs_F" + slot, nF);
     double2 *U = ctx->buf_t<double2>("rs_U" + slot, (size_t)N * 3 * nw);
     float4 *Udf = ctx->buf_t<float4>("rs_Udf" + slot, (size_t)N * 3 * nw);
-    RP_CUDA(cudaMemsetAsync(W, 0, sizeof(float4) * nW, stream));
+    RP_CUDA(cudaMemsetAsync(W, 0, sizeof(float2) * nW, stream));
     Rec9 rb;
     for (int q = 0; q < 9; ++q) rb.b[q] = ew->rec[q];
     atom_phases_kernel<<<ceil_div((long long)N * 3 * nw, 128), 128, 0, stream>>>(d_atoms, N, rb, P, U, Udf);
@@ -223,7 +232,7 @@ void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const do
                                                       ncols, W);
     RP_LAUNCH_CHECK();
     const int nb = (n1c + kN1B - 1) / kN1B;
-    const size_t smem_a = sizeof(float4) * (size_t)nw * nz;
+    const size_t smem_a = sizeof(float2) * (size_t)nw * nz;
     RP_REQUIRE(smem_a <= (200u << 10), "recip_rows: grid too large along z for KMAX");
     static size_t attr_a = 0;
     if (smem_a > (48u << 10) && smem_a > attr_a) {
