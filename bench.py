@@ -43,8 +43,8 @@ METRIC = "fits/s & p50/p99 latency vs plain FP64 GPU fit at max|dq|<=1e-5 e"
 
 # ncu figures of phi_chunk_kernel (profiles/phi_chunk_kernel_batch8.txt): DRAM bytes and
 # thread instructions per point-atom pair of the captured launch
-PHI_DRAM_PER_PAIR = 10.10
-PHI_INST_PER_PAIR = 389.0
+PHI_DRAM_PER_PAIR = 10.12
+PHI_INST_PER_PAIR = 344.0
 
 
 # ----------------------------------------------------------------------------- distributed helpers

@@ -170,16 +170,44 @@ __device__ double block_max(double v, double *sv) {
 
 // FP32 LU with partial pivoting in place (row-major n1 x n1).  Returns false on a
 // zero or non-finite pivot (the same value in every thread).
+// max |v| with the lowest index on ties (deterministic), FP32: the FP32 factorisation's
+// pivot search stays off the FP64 pipe (a warp-wide FP64 compare holds that pipe for
+// 16 cycles, and every warp of the CTA runs this at every column)
+__device__ void block_argmax_f(float v, int idx, float *sv, int *si, int *out_i) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_down_sync(0xffffffffu, v, o);
+        const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+        if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { sv[w] = v; si[w] = idx; }
+    __syncthreads();
+    if (w == 0) {
+        v = (lane < kLU / 32) ? sv[lane] : -1.0f;
+        idx = (lane < kLU / 32) ? si[lane] : 0x7fffffff;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_down_sync(0xffffffffu, v, o);
+            const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+            if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+        }
+        if (lane == 0) *out_i = idx;
+    }
+    __syncthreads();
+}
+
+// FP32 LU with partial pivoting, in place; false on a zero or non-finite pivot
 __device__ bool lu_factor_f32(float *A, int *perm, int n1, double *sv, int *si, double *piv_v, int *piv_i,
                               double &pmin, double &pmax) {
+    float *svf = reinterpret_cast<float *>(sv);
+    float fmin_p = 3.0e38f, fmax_p = 0.f;
     for (int k = 0; k < n1; ++k) {
-        double best = -1.0;
+        float best = -1.0f;
         int bi = 0x7fffffff;
         for (int r = k + threadIdx.x; r < n1; r += kLU) {
-            const double v = fabs((double)A[(size_t)r * n1 + k]);
+            const float v = fabsf(A[(size_t)r * n1 + k]);
             if (v > best || (v == best && r < bi)) { best = v; bi = r; }
         }
-        block_argmax(best, bi, sv, si, piv_v, piv_i);
+        block_argmax_f(best, bi, svf, si, piv_i);
         const int p = *piv_i;
         if (threadIdx.x == 0) perm[k] = p;
         if (p != k)
@@ -190,10 +218,10 @@ __device__ bool lu_factor_f32(float *A, int *perm, int n1, double *sv, int *si, 
             }
         __syncthreads();
         const float pv = A[(size_t)k * n1 + k];
-        const double apv = fabs((double)pv);
-        if (!(apv > 0.0) || !isfinite(pv)) return false;
-        pmin = fmin(pmin, apv);
-        pmax = fmax(pmax, apv);
+        const float apv = fabsf(pv);
+        if (!(apv > 0.f) || !isfinite(pv)) return false;
+        fmin_p = fminf(fmin_p, apv);
+        fmax_p = fmaxf(fmax_p, apv);
         const float inv = 1.0f / pv;
         for (int r = k + 1 + threadIdx.x; r < n1; r += kLU) A[(size_t)r * n1 + k] *= inv;
         __syncthreads();
@@ -206,6 +234,9 @@ __device__ bool lu_factor_f32(float *A, int *perm, int n1, double *sv, int *si, 
         }
         __syncthreads();
     }
+    pmin = fmin(pmin, (double)fmin_p);
+    pmax = fmax(pmax, (double)fmax_p);
+    (void)piv_v;
     return true;
 }
 
