@@ -243,44 +243,42 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
                 for (cudaEvent_t ev : e) cudaEventDestroy(ev);
             }
         } guard{events};
-        // 1. filters
+        // 1. filters, group by group: the host plans a group (its workers), packs it into the
+        //    group's pinned arena and queues the upload, the grids and the filter launches, then
+        //    plans the next group while the device runs this one
         while ((int)ctx->plan_pool.size() < n) ctx->plan_pool.emplace_back(new rp::FilterPlan());
         auto plan = [&](int i) -> rp::FilterPlan & { return *ctx->plan_pool[(size_t)i]; };
-        ctx->parallel(n, [&](int i) {
-            const rp_fit_desc &d = descs[i];
-            rp::filter_plan(&d.grid, d.atoms, d.Z, d.N, d.vdw_factor, d.vdw_max, plan(i));
-        });
-        std::vector<size_t> pl_off((size_t)n + 1, 0);
-        for (int i = 0; i < n; ++i) pl_off[i + 1] = pl_off[i] + plan(i).bytes();
-        char *pl_dev = static_cast<char *>(ctx->buf("fit_filter", pl_off[n]));
-        char *pl_host = static_cast<char *>(ctx->host_buf("fit_filter", pl_off[n]));
-        ctx->parallel(n, [&](int i) { plan(i).pack(pl_host + pl_off[i]); });
-        RP_CUDA(cudaMemcpyAsync(pl_dev, pl_host, pl_off[n], cudaMemcpyHostToDevice, stream));
         {
-            const cudaEvent_t up = record(stream);  // every stream starts after the uploads
+            const cudaEvent_t up = record(stream);  // every stream starts after the caller's work so far
             for (int ln = 0; ln < kLanes; ++ln) {
                 RP_CUDA(cudaStreamWaitEvent(ctx->lane(ln), up, 0));
                 RP_CUDA(cudaStreamWaitEvent(flane(ln), up, 0));
             }
         }
-        // grids from host memory: one group at a time on the copy stream, so a group's filters
-        // start as soon as its own grids are on the device
-        const cudaStream_t copy_lane = ctx->lane(2 * kLanes);
+        const cudaStream_t copy_lane = ctx->lane(2 * kLanes);  // uploads: plans, grids, tables
         RP_CUDA(cudaStreamWaitEvent(copy_lane, events.back(), 0));
+        std::vector<size_t> pl_off((size_t)n + 1, 0);
         std::vector<cudaEvent_t> kept_ready((size_t)ngroups);
         for (int g = 0; g < ngroups; ++g) {
-            bool copied = false;
-            for (int i = g0[g]; i < g0[g + 1]; ++i)
-                if (!(V_dev && V_dev[i])) {
+            const int i0 = g0[g], i1 = g0[g + 1];
+            ctx->parallel(i1 - i0, [&](int t) {
+                const rp_fit_desc &d = descs[i0 + t];
+                rp::filter_plan(&d.grid, d.atoms, d.Z, d.N, d.vdw_factor, d.vdw_max, plan(i0 + t));
+            });
+            pl_off[i0] = 0;
+            for (int i = i0; i < i1; ++i) pl_off[i + 1] = pl_off[i] + plan(i).bytes();
+            const std::string gtag = "fit_filter#" + std::to_string(g);
+            char *pl_dev = static_cast<char *>(ctx->buf(gtag, pl_off[i1]));
+            char *pl_host = static_cast<char *>(ctx->host_buf(gtag, pl_off[i1]));
+            ctx->parallel(i1 - i0, [&](int t) { plan(i0 + t).pack(pl_host + pl_off[i0 + t]); });
+            RP_CUDA(cudaMemcpyAsync(pl_dev, pl_host, pl_off[i1], cudaMemcpyHostToDevice, copy_lane));
+            for (int i = i0; i < i1; ++i)  // grids from host memory, this group's only
+                if (!(V_dev && V_dev[i]))
                     RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], descs[i].V, sizeof(double) * npts[i],
                                             cudaMemcpyHostToDevice, copy_lane));
-                    copied = true;
-                }
-            if (copied) {
-                const cudaEvent_t grids = record(copy_lane);
-                for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(flane(ln), grids, 0));
-            }
-            for (int i = g0[g]; i < g0[g + 1]; ++i) {
+            const cudaEvent_t inputs = record(copy_lane);
+            for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(flane(ln), inputs, 0));
+            for (int i = i0; i < i1; ++i) {
                 const rp_fit_desc &d = descs[i];
                 const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
                 const int ln = i % lanes;
@@ -289,8 +287,7 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
                                   vst + 2 * i);
             }
             for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(stream, record(flane(ln)), 0));
-            RP_CUDA(cudaMemcpyAsync(Mh + g0[g], Md + g0[g], sizeof(long long) * (g0[g + 1] - g0[g]),
-                                    cudaMemcpyDeviceToHost, stream));
+            RP_CUDA(cudaMemcpyAsync(Mh + i0, Md + i0, sizeof(long long) * (i1 - i0), cudaMemcpyDeviceToHost, stream));
             kept_ready[g] = record(stream);
         }
         // 2. Ewald tables, written by the host workers straight into one pinned arena,

@@ -158,6 +158,21 @@ def test_batch_equals_single_fits(gpu_ctx):
         assert np.abs(staged - b).max() <= 1e-6
 
 
+def test_pipelined_batch_equals_single_fits(gpu_ctx):
+    """A batch of 64 or more cubes runs as four pipeline groups (filters, normal equations
+    and solves of different groups in flight on different streams).  Every cube's charges
+    equal its fit alone, bitwise, and the per-group kept counts come back in order."""
+    from pyrepeat_gb300 import _lib
+    names = ("water24", "tricmini", "mofmini")
+    cubes = [load_golden(names[i % 3])[0] for i in range(66)]
+    alone = {n: gpu_ctx.fit_host(load_golden(n)[0], precision=_lib.PREC_MIXED).charges for n in names}
+    batch, M, info = gpu_ctx.fit_batch(cubes, _lib.PREC_MIXED)
+    for i, (q, m) in enumerate(zip(batch, M)):
+        name = names[i % 3]
+        assert np.array_equal(q, alone[name]), (i, name)
+        assert m == load_golden(name)[1]["kept"]
+
+
 def test_potential_matches_phi_q(gpu_ctx, oracle_mod):
     """rp_potential (the stats pass) equals the oracle's Phi q at kept points."""
     import torch
