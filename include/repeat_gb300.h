@@ -158,11 +158,13 @@ typedef struct {
 } rp_fit_desc;
 int rp_fit(rp_ctx *ctx, const rp_fit_desc *desc, double *q_out, int64_t *M_out, rp_stream_t stream);
 
-/* Many independent fits in one call (the batched workload).  All Ewald setups,
- * then every filter asynchronously, one read of the kept counts, the normal
- * equations of every cube back to back on `stream`, and one launch that folds
- * and solves all bordered systems (one CTA per system).  No reference
- * counterpart: repeat.py fits one cube per process.
+/* Many independent fits in one call (the batched workload).  The cubes run as a
+ * pipeline of up to four groups: each group's filters (their host halves on the
+ * ctx's host workers, one pinned upload), then, as its kept counts arrive, its
+ * normal equations on four worker streams and its folds and bordered solves (one
+ * launch, one CTA per system) on `stream`, while the next group's filters run.  The
+ * call returns when every charge is on the host.  No reference counterpart:
+ * repeat.py fits one cube per process.
  *   descs[n]     as for rp_fit (each with its own precision)
  *   V_dev        NULL, or n device pointers (an entry may be NULL: use descs[i].V on the host)
  *   q_out        host, the charges of all cubes concatenated (sum of N_i doubles)
@@ -170,6 +172,22 @@ int rp_fit(rp_ctx *ctx, const rp_fit_desc *desc, double *q_out, int64_t *M_out, 
  *                per cube refined residual, min |pivot|, max |pivot|, singular flag */
 int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
                  int64_t *M_out, double *info_out, rp_stream_t stream);
+
+/* Asynchronous batches, the serving interface (no reference counterpart: repeat.py
+ * is a one-shot program).  rp_batch_submit queues a batch for the ctx's worker
+ * thread, which runs queued batches in order as rp_fit_batch does (on a stream of
+ * its own), and returns a ticket.  The descriptor array is copied; the arrays it
+ * points to, V_dev and the outputs must stay valid until the ticket is retired.
+ * While tickets are outstanding the ctx belongs to the worker: only submit, poll,
+ * wait and rp_last_error may be called on it.  rp_batch_poll sets *done (and, when
+ * done, *status = the batch's rp_fit_batch status, its message in rp_last_error)
+ * without blocking; rp_batch_wait blocks.  A finished ticket is retired by the poll
+ * or wait that reports it; rp_ctx_destroy lets the running batch finish and drops
+ * the queued ones. */
+int rp_batch_submit(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
+                    int64_t *M_out, double *info_out, long long *ticket);
+int rp_batch_poll(rp_ctx *ctx, long long ticket, int *done, int *status);
+int rp_batch_wait(rp_ctx *ctx, long long ticket, int *status);
 
 /* Profiling hooks (no reference counterpart).  With timing on, every stage
  * records CUDA events on the stream it runs on; rp_stage_times synchronises,

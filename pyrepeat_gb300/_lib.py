@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "librepeat_gb300.so")
 
 RP_OK = 0
+RP_E_ARG = -1
 STATUS = {
     -1: "RP_E_ARG", -2: "RP_E_CUDA", -3: "RP_E_NOMEM", -4: "RP_E_SINGULAR", -5: "RP_E_TIMEOUT",
     -6: "RP_E_STATE", -7: "RP_E_UNSUPPORTED",
@@ -22,7 +23,8 @@ PREC_MIXED = 1
 # every symbol include/repeat_gb300.h declares
 EXPORTS = ["rp_version", "rp_ctx_create", "rp_ctx_destroy", "rp_last_error", "rp_filter", "rp_ewald_setup",
            "rp_ewald_destroy", "rp_ewald_info", "rp_gram", "rp_solve", "rp_potential", "rp_fit",
-           "rp_fit_batch", "rp_set_timing", "rp_stage_times", "rp_launch_count", "rp_solve_noalloc"]
+           "rp_fit_batch", "rp_set_timing", "rp_stage_times", "rp_launch_count", "rp_solve_noalloc",
+           "rp_batch_submit", "rp_batch_poll", "rp_batch_wait"]
 
 
 class RepeatError(RuntimeError):
@@ -97,6 +99,12 @@ def load(path: str | None = None):
     L.rp_stage_times.argtypes = [P, ctypes.c_char_p, SZ, P, ctypes.POINTER(I)]
     L.rp_fit_batch.restype = I
     L.rp_fit_batch.argtypes = [P, I, P, P, P, P, P, P]
+    L.rp_batch_submit.restype = I
+    L.rp_batch_submit.argtypes = [P, I, P, P, P, P, P, ctypes.POINTER(ctypes.c_longlong)]
+    L.rp_batch_poll.restype = I
+    L.rp_batch_poll.argtypes = [P, ctypes.c_longlong, ctypes.POINTER(I), ctypes.POINTER(I)]
+    L.rp_batch_wait.restype = I
+    L.rp_batch_wait.argtypes = [P, ctypes.c_longlong, ctypes.POINTER(I)]
     _lib = L
     return L
 

@@ -9,10 +9,12 @@
 #include <cstdint>
 #include <cstdio>
 #include <condition_variable>
+#include <deque>
 #include <exception>
 #include <functional>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -72,6 +74,27 @@ struct Buffer {
 // batch, and the per-cube host work (filter plans, Ewald tables) is spread over the cores.
 namespace rp {
 struct FilterPlan;
+
+// Queue and worker thread of the asynchronous batches (rp_batch_submit / poll / wait).
+struct BatchServer {
+    struct Job {
+        long long ticket = 0;
+        std::vector<rp_fit_desc> descs;
+        std::vector<const double *> vdev;
+        bool has_vdev = false;
+        double *q_out = nullptr;
+        int64_t *M_out = nullptr;
+        double *info_out = nullptr;
+    };
+    std::thread th;
+    std::mutex mu;
+    std::condition_variable cv, finished;
+    std::deque<Job> queue;
+    std::set<long long> pending;                                   // submitted, not yet retired
+    std::unordered_map<long long, std::pair<int, std::string>> done;  // ticket -> status, message
+    long long next = 1;
+    bool stop = false;
+};
 
 class HostPool {
   public:
@@ -203,6 +226,7 @@ struct rp_ctx {
     std::unordered_map<std::string, rp::Buffer> host_scratch;
     double bound_scale = 1.0;  // factor on the single-pass Phi bounds (tests shrink it to force clamps)
     std::unique_ptr<rp::HostPool> pool;  // host workers (created on first use)
+    std::unique_ptr<rp::BatchServer> server;  // asynchronous batches (created on first submit)
     // per-cube host objects of the batched fit, kept across batches for their capacity
     std::vector<std::unique_ptr<rp_ewald>> ew_pool;
     std::vector<std::unique_ptr<rp::FilterPlan>> plan_pool;
@@ -289,6 +313,9 @@ size_t ewald_device_bytes(const rp_ewald *ew);
 void ewald_place(rp_ewald *ew, void *dev);
 void ewald_build(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax);  // owns one cudaMalloc block
 void ewald_free(rp_ewald *ew);
+
+// Stops the ctx's asynchronous batch worker (rp_capi.cu): the running batch finishes.
+void batch_server_stop(rp_ctx *ctx);
 
 // Host helpers shared by the stages.
 

@@ -84,6 +84,7 @@ int rp_ctx_create(int device, size_t hbm_budget, rp_ctx **out) {
 
 int rp_ctx_destroy(rp_ctx *ctx) {
     if (!ctx) return RP_E_ARG;
+    rp::batch_server_stop(ctx);  // the batch running now finishes; queued ones are dropped
     cudaSetDevice(ctx->device);
     for (auto &kv : ctx->scratch) cudaFree(kv.second.ptr);
     for (auto &kv : ctx->host_scratch) cudaFreeHost(kv.second.ptr);
@@ -180,12 +181,15 @@ int rp_potential(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const dou
     });
 }
 
-int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
-                 int64_t *M_out, double *info_out, rp_stream_t stream_) {
-    if (!ctx || n < 0 || (n > 0 && (!descs || !q_out))) return RP_E_ARG;
-    cudaStream_t stream = (cudaStream_t)stream_;
+}  // extern "C"
+
+namespace rp {
+// The batched fit; throws rp::Error.  Used by rp_fit_batch (on the caller's thread) and by
+// the asynchronous batch server (on its worker thread).
+void fit_batch_body(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
+                    int64_t *M_out, double *info_out, cudaStream_t stream) {
     std::vector<rp_ewald *> ews((size_t)n, nullptr);
-    int rc = guarded(ctx, [&] {
+    {
         if (n == 0) return;
         std::vector<long long> npts((size_t)n), off_pts((size_t)n + 1, 0), off_n((size_t)n + 1, 0),
             off_nn((size_t)n + 1, 0);
@@ -389,9 +393,120 @@ int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *con
         for (int i = 0; i < n; ++i)
             if (info[4 * (size_t)i + 3] != 0.0)
                 rp::fail(RP_E_SINGULAR, "rp_fit: bordered system of cube " + std::to_string(i) + " is singular");
-    });
-    return rc;  // the pooled Ewald objects borrow the arena: nothing to free
+    }
+    // the pooled Ewald objects borrow the arena: nothing to free
 }
+
+// Worker of the asynchronous batches: runs the queued batches in order on the ctx's device.
+void batch_server_loop(rp_ctx *ctx) {
+    BatchServer &sv = *ctx->server;
+    cudaSetDevice(ctx->device);
+    std::unique_lock<std::mutex> lk(sv.mu);
+    for (;;) {
+        sv.cv.wait(lk, [&] { return sv.stop || !sv.queue.empty(); });
+        if (sv.stop) return;
+        BatchServer::Job job = std::move(sv.queue.front());
+        sv.queue.pop_front();
+        lk.unlock();
+        int status = RP_OK;
+        std::string msg;
+        try {
+            fit_batch_body(ctx, (int)job.descs.size(), job.descs.data(), job.has_vdev ? job.vdev.data() : nullptr,
+                           job.q_out, job.M_out, job.info_out, ctx->lane(2 * 4 + 1));
+        } catch (const Error &e) {
+            status = e.code;
+            msg = e.msg;
+        } catch (const std::exception &e) {
+            status = RP_E_ARG;
+            msg = e.what();
+        }
+        lk.lock();
+        sv.done[job.ticket] = {status, msg};
+        sv.finished.notify_all();
+    }
+}
+
+void batch_server_stop(rp_ctx *ctx) {
+    if (!ctx->server) return;
+    {
+        std::lock_guard<std::mutex> g(ctx->server->mu);
+        ctx->server->stop = true;
+    }
+    ctx->server->cv.notify_all();
+    if (ctx->server->th.joinable()) ctx->server->th.join();
+    ctx->server.reset();
+}
+}  // namespace rp
+
+extern "C" {
+
+int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
+                 int64_t *M_out, double *info_out, rp_stream_t stream) {
+    if (!ctx || n < 0 || (n > 0 && (!descs || !q_out))) return RP_E_ARG;
+    return guarded(ctx, [&] { rp::fit_batch_body(ctx, n, descs, V_dev, q_out, M_out, info_out, (cudaStream_t)stream); });
+}
+
+int rp_batch_submit(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
+                    int64_t *M_out, double *info_out, long long *ticket) {
+    if (!ctx || n <= 0 || !descs || !q_out || !ticket) return RP_E_ARG;
+    // no CUDA call here, and ctx->last_error is not touched: submit, poll and wait may be
+    // called from different host threads (the server's lock orders them)
+    {
+        static std::mutex create;
+        std::lock_guard<std::mutex> g(create);
+        if (!ctx->server) {
+            ctx->server.reset(new rp::BatchServer());
+            ctx->server->th = std::thread(rp::batch_server_loop, ctx);
+        }
+    }
+    try {
+        rp::BatchServer::Job job;
+        job.descs.assign(descs, descs + n);
+        job.has_vdev = V_dev != nullptr;
+        if (V_dev) job.vdev.assign(V_dev, V_dev + n);
+        job.q_out = q_out;
+        job.M_out = M_out;
+        job.info_out = info_out;
+        {
+            std::lock_guard<std::mutex> g(ctx->server->mu);
+            job.ticket = ctx->server->next++;
+            *ticket = job.ticket;
+            ctx->server->pending.insert(job.ticket);
+            ctx->server->queue.push_back(std::move(job));
+        }
+        ctx->server->cv.notify_all();
+        return RP_OK;
+    } catch (const std::exception &) {
+        return RP_E_NOMEM;
+    }
+}
+
+// done = 1 once the batch has finished; *status is then its rp_fit_batch status (the
+// message, if any, becomes rp_last_error) and the ticket is retired.
+static int batch_result(rp_ctx *ctx, long long ticket, bool wait, int *done, int *status) {
+    if (!ctx || !ctx->server) return RP_E_ARG;
+    rp::BatchServer &sv = *ctx->server;
+    std::unique_lock<std::mutex> lk(sv.mu);
+    if (!sv.pending.count(ticket)) return RP_E_ARG;
+    if (wait) sv.finished.wait(lk, [&] { return sv.done.count(ticket) > 0; });
+    auto it = sv.done.find(ticket);
+    if (it == sv.done.end()) {
+        if (done) *done = 0;
+        return RP_OK;
+    }
+    if (done) *done = 1;
+    if (status) *status = it->second.first;
+    ctx->last_error = it->second.second;
+    sv.done.erase(it);
+    sv.pending.erase(ticket);
+    return RP_OK;
+}
+
+int rp_batch_poll(rp_ctx *ctx, long long ticket, int *done, int *status) {
+    return batch_result(ctx, ticket, false, done, status);
+}
+
+int rp_batch_wait(rp_ctx *ctx, long long ticket, int *status) { return batch_result(ctx, ticket, true, nullptr, status); }
 
 int rp_launch_count(long long *out) {
     if (!out) return RP_E_ARG;

@@ -244,6 +244,59 @@ class Context:
             o += c.n_atoms
         return res, M, info.reshape(n, 4)
 
+    def batch_submit(self, cubes, precision=_lib.PREC_MIXED, V_dev=None) -> "PendingBatch":
+        """Queue a batch on the context's worker thread (rp_batch_submit) and return at once.
+        The returned handle keeps every array the worker reads alive until it is done."""
+        n = len(cubes)
+        keep = []
+        arr = (_lib.RpFitDesc * n)()
+        for i, c in enumerate(cubes):
+            arr[i] = self._desc(c, precision[i] if isinstance(precision, (list, tuple)) else precision, keep)
+        vptr = None
+        if V_dev is not None:
+            vptr = (ctypes.c_void_p * n)(*[v.data_ptr() if v is not None else None for v in V_dev])
+        pb = PendingBatch(self, cubes, keep + [arr, vptr, V_dev])
+        t = ctypes.c_longlong()
+        rc = self.lib.rp_batch_submit(self.ptr, n, ctypes.cast(arr, ctypes.c_void_p), vptr, pb.q.ctypes.data,
+                                      pb.M.ctypes.data, pb.info.ctypes.data, ctypes.byref(t))
+        self.check(rc, "rp_batch_submit")
+        pb.ticket = t.value
+        return pb
+
+
+class PendingBatch:
+    """A batch queued with rp_batch_submit: poll() without blocking, result() waits."""
+
+    def __init__(self, ctx: Context, cubes, keep):
+        self.ctx, self.cubes, self._keep = ctx, cubes, keep
+        self.q = np.zeros(sum(c.n_atoms for c in cubes))
+        self.M = np.zeros(len(cubes), dtype=np.int64)
+        self.info = np.zeros(4 * len(cubes))
+        self.ticket = None
+        self.status = None
+
+    def poll(self) -> bool:
+        if self.status is None:
+            done, st = ctypes.c_int(), ctypes.c_int()
+            self.ctx.check(self.ctx.lib.rp_batch_poll(self.ctx.ptr, self.ticket, ctypes.byref(done),
+                                                      ctypes.byref(st)), "rp_batch_poll")
+            if done.value:
+                self.status = st.value
+        return self.status is not None
+
+    def result(self):
+        """(charges per cube, kept counts, info[n, 4]); raises the batch's error."""
+        if self.status is None:
+            st = ctypes.c_int()
+            self.ctx.check(self.ctx.lib.rp_batch_wait(self.ctx.ptr, self.ticket, ctypes.byref(st)), "rp_batch_wait")
+            self.status = st.value
+        self.ctx.check(self.status, "batch")
+        res, o = [], 0
+        for c in self.cubes:
+            res.append(self.q[o:o + c.n_atoms])
+            o += c.n_atoms
+        return res, self.M, self.info.reshape(-1, 4)
+
 
 class Ewald:
     def __init__(self, ctx: Context, n_grid, axis, cutoff, kmax):

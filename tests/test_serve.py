@@ -1,0 +1,116 @@
+"""The serving layer: asynchronous batches (rp_batch_submit / poll / wait) and the
+micro-batching FitServer.
+
+CPU: the dispatcher's batching rules (batch size, wait bound, HBM admission and
+rejection) against a fake context.  GPU: requests served from two threads in mixed
+batches give exactly the charges of each cube fitted alone, and the C-ABI tickets
+retire as documented."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from pyrepeat_gb300 import serve
+
+
+class _FakeCube:
+    def __init__(self, n_atoms, n_grid=(10, 10, 10), kmax=7):
+        self.n_atoms = n_atoms
+        self.n_grid = np.array(n_grid)
+        self.kmax = kmax
+
+
+class _FakePending:
+    def __init__(self, cubes):
+        self.cubes = cubes
+
+    def result(self):
+        return [np.full(c.n_atoms, float(c.n_atoms)) for c in self.cubes], np.zeros(len(self.cubes)), None
+
+
+class _FakeCtx:
+    """Records the batches the server submits; results are available at once."""
+
+    def __init__(self):
+        self.batches = []
+
+    def batch_submit(self, cubes, precision, V_dev):
+        self.batches.append([c.n_atoms for c in cubes])
+        return _FakePending(cubes)
+
+
+def test_batches_respect_size_and_admission():
+    ctx = _FakeCtx()
+    one = serve.device_bytes(_FakeCube(5))
+    srv = serve.FitServer(ctx, max_batch=4, max_wait_s=0.2, hbm_budget=3.5 * one)
+    futs = [srv.submit(_FakeCube(5)) for _ in range(7)]
+    srv.close()
+    assert [f.result()[0] for f in futs] == [5.0] * 7
+    assert sum(len(b) for b in ctx.batches) == 7
+    assert max(len(b) for b in ctx.batches) <= 3           # admission: 3 cubes fit the budget, not 4
+    assert len(srv.latencies) == 7 and srv.batch_sizes == [len(b) for b in ctx.batches]
+
+
+def test_oversize_request_is_rejected():
+    ctx = _FakeCtx()
+    srv = serve.FitServer(ctx, hbm_budget=1e3)
+    f = srv.submit(_FakeCube(50))
+    with pytest.raises(MemoryError):
+        f.result(timeout=5)
+    srv.close()
+    assert ctx.batches == []
+
+
+def test_wait_bound_closes_a_partial_batch():
+    ctx = _FakeCtx()
+    srv = serve.FitServer(ctx, max_batch=64, max_wait_s=0.01)
+    f1 = srv.submit(_FakeCube(3))
+    assert f1.result(timeout=5)[0] == 3.0                  # served without a full batch
+    f2 = srv.submit(_FakeCube(4))
+    assert f2.result(timeout=5)[0] == 4.0
+    srv.close()
+    assert ctx.batches == [[3], [4]]
+
+
+@pytest.mark.gpu
+def test_served_fits_equal_fits_alone(gpu_ctx):
+    """Alone vs mixed: each request's charges equal the cube fitted alone, bitwise."""
+    from pyrepeat_gb300 import _lib
+    names = ("water24", "tricmini", "mofmini")
+    alone = {n: gpu_ctx.fit_host(load_golden(n)[0], precision=_lib.PREC_MIXED).charges for n in names}
+    srv = serve.FitServer(gpu_ctx, max_batch=8, max_wait_s=0.003)
+    results = {}
+
+    def client(k):
+        rng = np.random.default_rng(k)
+        for t in range(12):
+            name = names[int(rng.integers(3))]
+            results[(k, t)] = (name, srv.submit(load_golden(name)[0]))
+            time.sleep(float(rng.uniform(0, 0.002)))
+
+    th = [threading.Thread(target=client, args=(k,)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    srv.close()
+    for (name, fut) in results.values():
+        assert np.array_equal(fut.result(timeout=60), alone[name]), name
+    assert sum(srv.batch_sizes) == 24 and len(srv.latencies) == 24
+
+
+@pytest.mark.gpu
+def test_batch_tickets(gpu_ctx):
+    import ctypes
+    from pyrepeat_gb300 import _lib
+    cube, _ = load_golden("water24")
+    pb1 = gpu_ctx.batch_submit([cube], _lib.PREC_MIXED)
+    pb2 = gpu_ctx.batch_submit([cube, cube], _lib.PREC_MIXED)
+    q2, M2, _ = pb2.result()
+    q1, M1, _ = pb1.result()
+    assert np.array_equal(q1[0], q2[0]) and np.array_equal(q2[0], q2[1]) and M1[0] == M2[1]
+    done, st = ctypes.c_int(), ctypes.c_int()
+    # a retired ticket is unknown
+    assert gpu_ctx.lib.rp_batch_poll(gpu_ctx.ptr, pb1.ticket, ctypes.byref(done), ctypes.byref(st)) == _lib.RP_E_ARG
