@@ -210,13 +210,82 @@ def reference_arm(args, world, rank):
 
 # ----------------------------------------------------------------------------- GPU arm
 
+def serve_arm(args, world, rank, local):
+    """Served fits (SURVEY's serve workload, scaled to a few seconds): Poisson arrivals
+    drawn from the batch distribution with a share of large cubes (800-1500 atoms, 160^3)
+    go through a FitServer (micro-batches, HBM admission, asynchronous batches);
+    reported: completed fits/s and p50/p99 latency from arrival to charges on the host.
+    A secondary measurement; the default bench line is the batched workload."""
+    import torch
+    from pyrepeat_gb300 import _lib, synth
+    from pyrepeat_gb300.fit import Context
+    from pyrepeat_gb300.serve import FitServer
+    torch.cuda.set_device(local)
+    ctx = Context(local)
+    t0 = time.time()
+    small = [synth.make_batch_item(20000 + 1000 * rank + i, ctx=ctx) for i in range(args.serve_pool)]
+    large = [synth.make_batch_item(90000 + 1000 * rank + i, large=True, ctx=ctx) for i in range(args.serve_large)]
+    gen_s = time.time() - t0
+    pool = small + large
+    # warm-up: every cube of the pool once, so buffers are sized before the clock starts
+    for c in pool:
+        ctx.fit_batch([c], _lib.PREC_MIXED, V_dev=[c.V_dev])
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(11 + rank)
+    n_req = args.serve_requests
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=n_req))
+    pick_large = rng.random(n_req) < args.serve_large_share
+    picks = [large[int(rng.integers(len(large)))] if (pl and large) else small[int(rng.integers(len(small)))]
+             for pl in pick_large]
+    srv = FitServer(ctx, max_batch=args.serve_batch, max_wait_s=args.serve_wait_ms / 1e3,
+                    hbm_budget=args.serve_budget_gb * 1e9)
+    barrier(world)
+    start = time.perf_counter()
+    futs = []
+    for k in range(n_req):
+        delay = start + arrivals[k] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        futs.append(srv.submit(picks[k], V_dev=picks[k].V_dev))
+    for f in futs:
+        f.result()
+    wall = time.perf_counter() - start
+    srv.close()
+    wall = max_over_ranks(wall, world, "cuda")
+    lat = np.array(srv.latencies) * 1e3
+    if rank != 0:
+        return
+    nl = int(np.sum(pick_large))
+    line = {
+        "metric": "served fits/s & p50/p99 latency (arrival to charges on the host)", "value": n_req * world / wall,
+        "unit": "fits/s", "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": wall * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+double-float+exact-int+f64",
+        "data": "synthetic", "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "mean_batch": float(np.mean(srv.batch_sizes)), "batches": len(srv.batch_sizes),
+        "config": {"workload": f"serve: {n_req} requests, Poisson {args.serve_rate:.0f}/s, {nl} large "
+                               f"(pool of {len(small)} batch-distribution cubes and {len(large)} large cubes, "
+                               f"800-1500 atoms at 160^3), max batch {args.serve_batch}, max wait "
+                               f"{args.serve_wait_ms} ms, admission budget {args.serve_budget_gb} GB",
+                   "generation_s": round(gen_s, 1)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "mof", "water"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "mof", "water", "serve"])
+    ap.add_argument("--serve-requests", type=int, default=600)
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate, requests/s")
+    ap.add_argument("--serve-pool", type=int, default=48, help="distinct batch-distribution cubes")
+    ap.add_argument("--serve-large", type=int, default=2, help="distinct large cubes (800-1500 atoms, 160^3)")
+    ap.add_argument("--serve-large-share", type=float, default=0.05)
+    ap.add_argument("--serve-batch", type=int, default=64)
+    ap.add_argument("--serve-wait-ms", type=float, default=4.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--n-cubes", type=int, default=256)
     ap.add_argument("--fp64-cubes", type=int, default=8, help="cubes of the plain FP64 comparator")
     ap.add_argument("--latency-fits", type=int, default=32, help="single fits timed for p50/p99")
@@ -228,6 +297,9 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         reference_arm(args, world, rank)
+        return
+    if args.workload == "serve":
+        serve_arm(args, world, rank, local)
         return
 
     import torch

@@ -243,6 +243,128 @@ __device__ bool lu_factor_f32(float *A, int *perm, int n1, double *sv, int *si, 
 // x = (P L U)^{-1} y with the FP32 factors; y (overwritten) and x in shared memory.
 // One barrier per column: forward elimination updates y below the column, backward
 // substitution writes x[c] and updates y above it.
+// Blocked FP32 LU with partial pivoting (right-looking, panels of 32 columns), in place, for
+// n1 <= kLUBlockedMax.  Per panel: the panel's rows (32 columns, stride 33 against bank
+// conflicts) are factored in shared memory with the same partial pivoting; its row swaps
+// are applied to the other columns (one thread per column, the swaps in order); U12 is
+// solved against the panel's unit-lower block; and the trailing matrix takes one rank-32
+// update per panel, staged through a 32 x 64 tile of U12, instead of 32 rank-1 updates
+// that each re-read it from L2.  smem: n1 * 33 + 32 * 64 floats.  false on a zero pivot.
+constexpr int kLUNB = 32;
+constexpr int kLUBlockedMax = 1536;
+constexpr int kLUTile = 64;
+__device__ bool lu_factor_f32_blocked(float *A, int *perm, int n1, float *smem, float *svf, int *si, int *piv_i,
+                                      double &pmin, double &pmax) {
+    float *P = smem;                                  // [n1][33] panel rows k0..n1-1
+    float *U = smem + (size_t)n1 * (kLUNB + 1);       // [32][kLUTile] tile of U12
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float fmin_p = 3.0e38f, fmax_p = 0.f;
+    bool ok = true;
+    for (int k0 = 0; k0 < n1; k0 += kLUNB) {
+        const int nb = min(kLUNB, n1 - k0), m = n1 - k0;
+        // 1. the panel into shared memory
+        for (int t = threadIdx.x; t < m * kLUNB; t += kLU) {
+            const int r = t >> 5, c = t & 31;
+            P[r * (kLUNB + 1) + c] = c < nb ? A[(size_t)(k0 + r) * n1 + k0 + c] : 0.f;
+        }
+        __syncthreads();
+        // 2. factor the panel (partial pivoting over all its rows)
+        for (int j = 0; j < nb; ++j) {
+            float best = -1.0f;
+            int bi = 0x7fffffff;
+            for (int r = j + threadIdx.x; r < m; r += kLU) {
+                const float v = fabsf(P[r * (kLUNB + 1) + j]);
+                if (v > best || (v == best && r < bi)) { best = v; bi = r; }
+            }
+            block_argmax_f(best, bi, svf, si, piv_i);
+            const int p = *piv_i;
+            if (threadIdx.x == 0) perm[k0 + j] = k0 + p;
+            if (p != j && threadIdx.x < kLUNB) {
+                const float t = P[j * (kLUNB + 1) + threadIdx.x];
+                P[j * (kLUNB + 1) + threadIdx.x] = P[p * (kLUNB + 1) + threadIdx.x];
+                P[p * (kLUNB + 1) + threadIdx.x] = t;
+            }
+            __syncthreads();
+            const float pv = P[j * (kLUNB + 1) + j];
+            const float apv = fabsf(pv);
+            if (!(apv > 0.f) || !isfinite(pv)) {
+                ok = false;
+                break;  // uniform: every thread read the same pivot
+            }
+            fmin_p = fminf(fmin_p, apv);
+            fmax_p = fmaxf(fmax_p, apv);
+            const float inv = 1.0f / pv;
+            // scale the column and update the panel's remaining columns: a warp per row
+            for (int r = j + 1 + warp; r < m; r += kLU / 32) {
+                float *row = P + r * (kLUNB + 1);
+                const float l = row[j] * inv;  // every lane computes it; lane j+... writes it below
+                if (lane > j && lane < nb) row[lane] -= l * P[j * (kLUNB + 1) + lane];
+                __syncwarp();
+                if (lane == 0) row[j] = l;
+            }
+            __syncthreads();
+        }
+        if (!ok) break;
+        // 3. the factored panel back to global memory
+        for (int t = threadIdx.x; t < m * kLUNB; t += kLU) {
+            const int r = t >> 5, c = t & 31;
+            if (c < nb) A[(size_t)(k0 + r) * n1 + k0 + c] = P[r * (kLUNB + 1) + c];
+        }
+        // 4. the panel's row swaps on every other column (a thread per column, swaps in order)
+        for (int c = threadIdx.x; c < n1; c += kLU) {
+            if (c >= k0 && c < k0 + nb) continue;
+            for (int j = 0; j < nb; ++j) {
+                const int p = perm[k0 + j];
+                if (p != k0 + j) {
+                    const float t = A[(size_t)(k0 + j) * n1 + c];
+                    A[(size_t)(k0 + j) * n1 + c] = A[(size_t)p * n1 + c];
+                    A[(size_t)p * n1 + c] = t;
+                }
+            }
+        }
+        __syncthreads();
+        const int c1 = k0 + nb;
+        if (c1 >= n1) break;
+        // 5. U12 = L11^-1 A12 (unit lower L11 from the panel), a thread per column
+        for (int c = c1 + threadIdx.x; c < n1; c += kLU) {
+            float u[kLUNB];
+#pragma unroll
+            for (int j = 0; j < kLUNB; ++j) u[j] = j < nb ? A[(size_t)(k0 + j) * n1 + c] : 0.f;
+#pragma unroll
+            for (int j = 0; j < kLUNB; ++j)
+#pragma unroll
+                for (int i = j + 1; i < kLUNB; ++i) u[i] -= P[i * (kLUNB + 1) + j] * u[j];
+#pragma unroll
+            for (int j = 0; j < kLUNB; ++j)
+                if (j < nb) A[(size_t)(k0 + j) * n1 + c] = u[j];
+        }
+        __syncthreads();
+        // 6. A22 -= L21 U12, column tiles of kLUTile staged in shared memory
+        for (int t0 = c1; t0 < n1; t0 += kLUTile) {
+            const int w = min(kLUTile, n1 - t0);
+            for (int t = threadIdx.x; t < kLUNB * kLUTile; t += kLU) {
+                const int j = t / kLUTile, c = t - j * kLUTile;
+                U[t] = (j < nb && c < w) ? A[(size_t)(k0 + j) * n1 + t0 + c] : 0.f;
+            }
+            __syncthreads();
+            const int c = threadIdx.x % kLUTile;
+            if (c < w)
+                for (int r = nb + threadIdx.x / kLUTile; r < m; r += kLU / kLUTile) {
+                    const float *l = P + r * (kLUNB + 1);
+                    float acc = A[(size_t)(k0 + r) * n1 + t0 + c];
+#pragma unroll
+                    for (int j = 0; j < kLUNB; ++j) acc -= l[j] * U[j * kLUTile + c];
+                    A[(size_t)(k0 + r) * n1 + t0 + c] = acc;
+                }
+            __syncthreads();
+        }
+    }
+    pmin = fmin(pmin, (double)fmin_p);
+    pmax = fmax(pmax, (double)fmax_p);
+    __syncthreads();
+    return ok;
+}
+
 // Solve LU x = P y in FP32 (unit lower L, upper U, both in LU), blocked by 32 columns: the
 // 32x32 diagonal block is staged in shared memory and solved by one warp (shuffles, no block
 // barrier), then every warp updates the remaining rows with the block's 32 values (a warp per
@@ -348,7 +470,11 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
             d.r[t] = d.bs[t];
         }
         __syncthreads();
-        if (lu_factor_f32(L, d.perm, n1, sv, si, &piv_v, &piv_i, pmin, pmax)) {
+        const bool factored = n1 <= kLUBlockedMax
+                                  ? lu_factor_f32_blocked(L, d.perm, n1, fsh, reinterpret_cast<float *>(sv), si,
+                                                          &piv_i, pmin, pmax)
+                                  : lu_factor_f32(L, d.perm, n1, sv, si, &piv_v, &piv_i, pmin, pmax);
+        if (factored) {
             double an = 0.0;  // |A| (max row sum)
             for (int rr = threadIdx.x; rr < n1; rr += kLU) {
                 double s = 0.0;
@@ -460,7 +586,23 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
     for (int i = threadIdx.x; i < d.N; i += kLU) d.q[i] = d.x[d.map[i]];
 }
 
-size_t solve_smem_bytes(int n1) { return sizeof(float) * 2 * (size_t)n1; }
+// dynamic shared memory of lu_solve_refine_kernel: the right-hand side and correction in
+// FP32 (2 n1 floats) and, for the blocked factorisation, the panel and the U12 tile
+size_t solve_smem_bytes(int n1) {
+    size_t b = sizeof(float) * 2 * (size_t)n1;
+    if (n1 <= kLUBlockedMax) b = std::max(b, sizeof(float) * ((size_t)n1 * (kLUNB + 1) + kLUNB * kLUTile));
+    return b;
+}
+
+// the launch's shared memory opt-in, raised once to the largest the kernel can ask for
+void lu_smem_optin() {
+    static bool done = false;
+    if (!done) {
+        const size_t most = std::max(solve_smem_bytes(kLUBlockedMax), solve_smem_bytes(1));
+        RP_CUDA(cudaFuncSetAttribute(lu_solve_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most));
+        done = true;
+    }
+}
 
 }  // namespace
 
@@ -675,6 +817,7 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
         StageTimer tt(ctx, "solve_lu", stream);
         int n1max = 1;
         for (const FoldPlan &p : plans) n1max = std::max(n1max, p.n + 1);
+        lu_smem_optin();
         lu_solve_refine_kernel<<<nj, kLU, solve_smem_bytes(n1max), stream>>>(d_desc);
         RP_LAUNCH_CHECK();
     }
@@ -830,6 +973,7 @@ extern "C" int rp_solve_noalloc(const double *A_dev, const double *b_dev, int N,
             RP_CUDA(cudaMemcpyAsync(bs, hbs.data(), sizeof(double) * hbs.size(), cudaMemcpyHostToDevice, stream));
         }
         RP_CUDA(cudaMemcpyAsync(d_desc, &d, sizeof(SolveDesc), cudaMemcpyHostToDevice, stream));
+        lu_smem_optin();
         lu_solve_refine_kernel<<<1, kLU, solve_smem_bytes(n1), stream>>>(d_desc);
         RP_LAUNCH_CHECK();
         double hinfo[4];

@@ -375,7 +375,8 @@ def make_batch_item(seed: int, large: bool = False, noise: float = 1e-4, threads
     rng = np.random.default_rng(seed)
     if large:
         n = int(rng.integers(800, 1501))
-        L = float(rng.uniform(26.0, 30.0))
+        # at most one atom per 90 Bohr^3 here too, so the vdW spheres leave ESP points
+        L = max(float(rng.uniform(26.0, 30.0)), (n * 90.0) ** (1 / 3))
         lengths = np.array([L, L, L])
         ng = np.array([160, 160, 160])
     else:

@@ -185,3 +185,25 @@ def test_potential_matches_phi_q(gpu_ctx, oracle_mod):
     of = oracle_mod.OracleFit(cube)
     ref = of.phi() @ cube.charges_true
     assert np.abs(pot - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("N", [61, 700, 1600])
+def test_bordered_solve_large_systems(gpu_ctx, N):
+    """The bordered solve on systems of many 32-column panels (the blocked FP32 LU with
+    FP64 refinement; N = 1600 takes the unblocked factorisation) against an FP64 LU of
+    the same bordered system."""
+    import scipy.linalg as sl
+    import torch
+    rng = np.random.default_rng(N)
+    X = rng.normal(size=(3 * N, N)) + 0.3 * rng.normal(size=(1, N))
+    A = X.T @ X / (3 * N)
+    b = rng.normal(size=N)
+    Z = np.full(N, 6)
+    q, _ = gpu_ctx.solve(torch.from_numpy(A).cuda(), torch.from_numpy(b).cuda(), Z, qtot=0.5)
+    K = np.zeros((N + 1, N + 1))
+    K[:N, :N] = A
+    K[:N, N] = K[N, :N] = 1.0
+    ref = sl.solve(K, np.concatenate([b, [0.5]]))[:N]
+    q = q.cpu().numpy()
+    assert np.abs(q - ref).max() <= 1e-9 * max(1.0, np.abs(ref).max())
