@@ -82,7 +82,11 @@ int rp_filter(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *
  * |ky|,|kz|<=KMAX, 0<k^2<KMAX^2 with kcoef = 4pi/V exp(-k^2/4alpha)/k^2, and the
  * real-space shifts |n_i| <= floor(Rc/|a_i|)+1 pruned by AABB distance.
  * Replaces EwaldCalculator.__init__/_setup_kspace/prepare_pruned_shifts
- * (repeat.py:1077-1143, 1708-1731, 1031-1069).  kmax = 7 is the reference. */
+ * (repeat.py:1077-1143, 1708-1731, 1031-1069).  kmax = 7 is the reference.
+ * kmax = 0 selects the non-periodic basis of --fit-type 0 (repeat.py:991-994,
+ * 1263-1270): Phi = 1/|g - r_a| for the atom itself (0 at r <= 1e-10), no k-set and
+ * no images; the cutoff is ignored.  Every consumer (rp_gram, rp_potential, rp_fit
+ * and rp_fit_batch through rp_fit_desc.kmax) then fits or evaluates that basis. */
 int rp_ewald_setup(rp_ctx *ctx, const rp_grid *grid, double cutoff, int kmax, rp_ewald **out);
 int rp_ewald_destroy(rp_ewald *ew);
 /* K (k vectors), S (shifts before pruning), alpha. Any out pointer may be NULL. */
@@ -150,7 +154,7 @@ typedef struct {
     const int *Z;           /* [N] host */
     int N;
     double vdw_factor, vdw_max, cutoff, qtot;
-    int kmax;
+    int kmax;               /* 7 = the reference; 0 = the non-periodic fit (--fit-type 0) */
     int n_groups;
     const int *group_ptr, *group_idx;
     const double *resp_s, *resp_t;

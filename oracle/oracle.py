@@ -195,15 +195,24 @@ class OracleFit:
             sel = np.sort(rng.choice(len(self.kept), size=sample, replace=False))
             self.grid = self.grid[sel]; self.Vc = self.Vc[sel] - self.Vc[sel].mean()
         box = c.box_vectors
-        self.kv, self.kc = kspace(box, c.cutoff, c.kmax)
-        full = shifts(box, c.cutoff)
-        self.shifts, self.zero_idx = prune_shifts(full, self.grid, c.atom_pos, c.cutoff)
+        if c.kmax == 0:
+            # the non-periodic basis of --fit-type 0 (repeat.py:991-994): 1/|g - r_a| for the
+            # atom itself (0 at r <= 1e-10), i.e. the real-space term with alpha 0, one zero
+            # shift and no cutoff, and no k-vectors
+            self.kv, self.kc = np.zeros((0, 3)), np.zeros(0)
+            self.shifts, self.zero_idx = np.zeros((1, 3)), 0
+            self.cutoff = math.inf
+        else:
+            self.kv, self.kc = kspace(box, c.cutoff, c.kmax)
+            full = shifts(box, c.cutoff)
+            self.shifts, self.zero_idx = prune_shifts(full, self.grid, c.atom_pos, c.cutoff)
+            self.cutoff = c.cutoff
         self.cube = c
 
     def normal_equations(self):
         c = self.cube
         return normal_equations(self.grid, self.Vc, c.atom_pos, self.kv, self.kc, self.shifts,
-                                self.zero_idx, c.cutoff, self.threads)
+                                self.zero_idx, self.cutoff, self.threads)
 
     def fit(self):
         c = self.cube
@@ -215,7 +224,7 @@ class OracleFit:
 
     def phi(self):
         c = self.cube
-        return phi(self.grid, c.atom_pos, self.kv, self.kc, self.shifts, self.zero_idx, c.cutoff, self.threads)
+        return phi(self.grid, c.atom_pos, self.kv, self.kc, self.shifts, self.zero_idx, self.cutoff, self.threads)
 
 
 def run_reference_binary(cube_path: str, timeout: int = 3600) -> np.ndarray | None:

@@ -12,8 +12,9 @@ such as ``0,1`` is rejected: one fit uses one GPU); ``--fp64`` selects the plain
 FP64 fit instead of the mixed-precision one; ``--kmax`` (new, default 7, the
 reference's KMAX) sets the k-space cutoff; ``--cores``, ``--block-k`` and
 ``--no-jit`` steer the reference's CPU backends and are accepted without effect;
-``--fit-type 0`` and ``--charge qeq`` are not part of this path and exit with a
-message.
+``--fit-type 0`` fits the non-periodic 1/r basis (the same filter, normal
+equations and constraints, no Ewald sum); ``--charge qeq`` is not part of this path
+and exits with a message.
 """
 from __future__ import annotations
 
@@ -64,9 +65,6 @@ def parse_device(spec: str | None) -> int:
 def main(argv=None) -> int:
     args = build_parser().parse_args(argv)
     device = parse_device(args.gpu)
-    if args.fit_type != 1:
-        print("Error: --fit-type 0 (non-periodic fit) is not part of the GB300 path; use --fit-type 1")
-        return 2
     if args.charge == "qeq":
         print("Error: --charge qeq is not part of the GB300 path; use --charge repeat")
         return 2

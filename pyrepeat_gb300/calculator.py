@@ -10,8 +10,9 @@ solve on the device (no Phi matrix, no host Gram), and ``rp_potential`` gives
 Phi q for the statistics without forming Phi.
 
 Arguments that only steer the reference's CPU backends (``n_cores``,
-``block_k``, ``use_jit``) are accepted and have no effect.  The non-periodic fit
-(``fit_flag=0``) and QEq charges are not part of this path: they raise
+``block_k``, ``use_jit``) are accepted and have no effect.  ``fit_flag=0`` fits the
+non-periodic 1/r basis (repeat.py:991-994) with the same machinery (KMAX 0 in the
+device library).  QEq charges are not part of this path: they raise
 NotImplementedError.  There is no CPU fallback: without a CUDA device every
 call raises.
 """
@@ -40,9 +41,8 @@ class ChargeCalculator:
                  device: int = 0, fp64: bool = False, kmax: int = 7, verbose: bool = False):
         self.cube_file = cube_file
         self.fit_flag = int(fit_flag)
-        if self.fit_flag != 1:
-            raise NotImplementedError("fit_flag=0 (the non-periodic 1/r fit) is not part of the GB300 path; "
-                                      "use the periodic fit (fit_flag=1)")
+        if self.fit_flag not in (0, 1):
+            raise ValueError("fit_flag must be 0 (non-periodic 1/r basis) or 1 (periodic Ewald)")
         self.vdw_factor = float(vdw_factor)
         self.vdw_max = float(vdw_max)
         self.R_cutoff = float(R_cutoff)
@@ -89,7 +89,8 @@ class ChargeCalculator:
         return Cube(np.asarray(c["atom_index"], dtype=np.int64), np.asarray(c["atom_pos"], dtype=np.float64),
                     np.asarray(c["n_grid"], dtype=np.int64), np.asarray(c["axis_vector"], dtype=np.float64),
                     np.ascontiguousarray(c["V_flat"], dtype=np.float64), symm_groups=self._groups, resp=self._resp,
-                    kmax=self.kmax, cutoff=self.R_cutoff, vdw_factor=self.vdw_factor, vdw_max=self.vdw_max,
+                    kmax=self.kmax if self.fit_flag == 1 else 0, cutoff=self.R_cutoff,
+                    vdw_factor=self.vdw_factor, vdw_max=self.vdw_max,
                     total_charge=self.q_tot, name=str(self.cube_file))
 
     def _filtered(self):
@@ -144,7 +145,7 @@ class ChargeCalculator:
         sqrt(sum d^2 / sum Vc^2).  V_coul = Phi q comes from rp_potential."""
         kept, Vc = self._filtered()
         c = self.cube
-        ew = self.ctx.ewald(c["n_grid"], c["axis_vector"], self.R_cutoff, self.kmax)
+        ew = self.ctx.ewald(c["n_grid"], c["axis_vector"], self.R_cutoff, self.kmax if self.fit_flag == 1 else 0)
         try:
             vcoul = self.ctx.potential(ew, c["atom_pos"], np.asarray(charges, dtype=np.float64), kept)
         finally:

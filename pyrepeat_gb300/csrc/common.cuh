@@ -317,6 +317,9 @@ void ewald_free(rp_ewald *ew);
 // Stops the ctx's asynchronous batch worker (rp_capi.cu): the running batch finishes.
 void batch_server_stop(rp_ctx *ctx);
 
+// Cutoff of the non-periodic basis (KMAX 0): beyond every distance, finite in FP32 squared.
+constexpr double kNonPeriodicCutoff = 1e15;
+
 // Host helpers shared by the stages.
 
 

@@ -27,9 +27,14 @@ static void cross3(const double *a, const double *b, double *c) {
 }
 
 void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax, char *dst) {
-    RP_REQUIRE(cutoff > 0.0, "rp_ewald_setup: cutoff must be > 0");
-    RP_REQUIRE(kmax >= 1 && kmax <= 64, "rp_ewald_setup: kmax must be in 1..64");
+    RP_REQUIRE(kmax >= 0 && kmax <= 64, "rp_ewald_setup: kmax must be in 0..64");
+    RP_REQUIRE(kmax == 0 || cutoff > 0.0, "rp_ewald_setup: cutoff must be > 0");
     for (int i = 0; i < 3; ++i) RP_REQUIRE(grid->n_grid[i] > 0, "rp_ewald_setup: grid counts must be > 0");
+    // kmax 0: the non-periodic basis of --fit-type 0, 1/|g - r_a| with the atom itself only
+    // (repeat.py:991-994, 1263-1270): no k-vectors, the zero shift alone, alpha 0 (so the
+    // real-space term erfc(0 r)/r is 1/r everywhere) and a cutoff no distance reaches
+    const bool nonperiodic = kmax == 0;
+    if (nonperiodic) cutoff = kNonPeriodicCutoff;
     ew->grid = *grid;
     ew->cutoff = cutoff;
     ew->kmax = kmax;
@@ -50,7 +55,7 @@ void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax
         rec[3 + d] = 2 * PI * ca[d] / vol;
         rec[6 + d] = 2 * PI * ab[d] / vol;
     }
-    ew->alpha = (PI / cutoff) * (PI / cutoff);
+    ew->alpha = nonperiodic ? 0.0 : (PI / cutoff) * (PI / cutoff);
     ew->sqrt_alpha = std::sqrt(ew->alpha);
     const double beta = 1.0 / (4.0 * ew->alpha);
     ew->kvec.clear();
@@ -76,7 +81,7 @@ void ewald_build_host(rp_ewald *ew, const rp_grid *grid, double cutoff, int kmax
     for (int i = 0; i < 3; ++i) {
         double len = std::sqrt(ew->box[3 * i] * ew->box[3 * i] + ew->box[3 * i + 1] * ew->box[3 * i + 1] +
                                ew->box[3 * i + 2] * ew->box[3 * i + 2]);
-        nmax[i] = (int)std::floor(cutoff / len) + 1;
+        nmax[i] = nonperiodic ? 0 : (int)std::floor(cutoff / len) + 1;
     }
     ew->shifts.clear();
     for (int ix = -nmax[0]; ix <= nmax[0]; ++ix)
@@ -162,10 +167,10 @@ size_t ewald_layout(const rp_grid *grid, int kmax, size_t off[9], int *K_out) {
             }
     if (K_out) *K_out = K;
     const size_t nx = grid->n_grid[0], ny = grid->n_grid[1], nz = grid->n_grid[2];
-    const size_t P = kmax - 1, nw = 2 * P + 1;
+    const size_t P1 = (size_t)kmax, nw = kmax > 0 ? 2 * (size_t)kmax - 1 : 0;  // P+1 and 2P+1, P = kmax-1
     const size_t bytes[9] = {sizeof(int) * 3 * K, sizeof(double) * K, sizeof(double) * 3 * K,
                              sizeof(double2) * (kmax + 1) * nx, sizeof(double2) * (2 * kmax + 1) * ny,
-                             sizeof(double2) * (2 * kmax + 1) * nz, sizeof(float4) * (P + 1) * nx,
+                             sizeof(double2) * (2 * kmax + 1) * nz, sizeof(float4) * P1 * nx,
                              sizeof(float4) * nw * ny, sizeof(float4) * nw * nz};
     size_t end = 0;
     for (int t = 0; t < 9; ++t) {

@@ -139,7 +139,7 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
     RP_CUDA(cudaMemcpyAsync(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice, stream));
 
     double *B = ctx->buf_t<double>("g64_B", (size_t)N * K2);
-    atom_tables_fp64(ew, d_atoms, N, B, K2, stream);
+    if (K > 0) atom_tables_fp64(ew, d_atoms, N, B, K2, stream);
 
     // chunk rows so T and Phi stay within ~2 GB together
     const size_t row_bytes = sizeof(double) * ((size_t)K2 + N);
@@ -163,13 +163,15 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
     const double one = 1.0, zero = 0.0;
     for (int64_t m0 = 0; m0 < M; m0 += chunk) {
         const int64_t rows = std::min<int64_t>(chunk, M - m0);
-        {
-            StageTimer tt(ctx, "fp64_tables", stream);
-            grid_tables_fp64(ew, kept_idx_dev, m0, rows, T, K2, stream);
-        }
-        {
+        if (K > 0) {
+            {
+                StageTimer tt(ctx, "fp64_tables", stream);
+                grid_tables_fp64(ew, kept_idx_dev, m0, rows, T, K2, stream);
+            }
             StageTimer tt(ctx, "fp64_recip_dgemm", stream);
             RP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, N, (int)rows, K2, &one, B, K2, T, K2, &zero, P, N));
+        } else {  // the non-periodic basis has no reciprocal part
+            RP_CUDA(cudaMemsetAsync(P, 0, sizeof(double) * (size_t)rows * N, stream));
         }
         StageTimer t_r(ctx, "fp64_realspace", stream);
         realspace_fp64_kernel<<<ceil_div(rows * N, 128), 128, 0, stream>>>(

@@ -62,6 +62,14 @@ def load_golden(name: str):
     return cube, g
 
 
+def load_nonperiodic(name: str):
+    """(cube with KMAX 0 = the non-periodic basis, repeat.py's --fit-type 0 charges)."""
+    cube, _ = load_golden(name)
+    cube.kmax = 0
+    z = np.load(os.path.join(GOLDEN, "nonperiodic.npz"), allow_pickle=False)
+    return cube, z[f"q_ref0_{name}"]
+
+
 @pytest.fixture(scope="session")
 def oracle_mod():
     import oracle

@@ -15,6 +15,7 @@ bits) and charges.  Large cubes store V only when small enough; otherwise the
 test regenerates it from the stored atoms/charges/seed with the same generator.
 
 Usage:  python tests/golden/make_golden.py [case ...]
+        python tests/golden/make_golden.py --nonperiodic    (fit-type 0 charges of the small cases)
 """
 from __future__ import annotations
 
@@ -55,7 +56,7 @@ def mask_digest(mask: np.ndarray) -> str:
     return hashlib.sha256(np.packbits(mask.astype(np.uint8)).tobytes()).hexdigest()
 
 
-def reference_fit(R, cube_path, cube, kmax):
+def reference_fit(R, cube_path, cube, kmax, fit_flag=1):
     """Run repeat.py's ChargeCalculator on a cube file; KMAX other than 7 is
     applied by re-running the reference's own k-space rule (repeat.py:1127-1143)
     with the larger KMAX after construction."""
@@ -89,7 +90,7 @@ def reference_fit(R, cube_path, cube, kmax):
             self.kcoefs = np.asarray(kc, dtype=np.float64)
         R.EwaldCalculator._setup_kspace = setup_kmax
     try:
-        calc = R.ChargeCalculator(cube_path, fit_flag=1, vdw_factor=cube.vdw_factor, vdw_max=cube.vdw_max,
+        calc = R.ChargeCalculator(cube_path, fit_flag=fit_flag, vdw_factor=cube.vdw_factor, vdw_max=cube.vdw_max,
                                   R_cutoff=cube.cutoff, q_tot=cube.total_charge, symm_file=symm,
                                   resp_file=resp, use_jit=False)
         q = calc.fit_charges()
@@ -103,6 +104,27 @@ def reference_fit(R, cube_path, cube, kmax):
     mask[flat] = 1
     V_read = calc.cube["V_pot"].ravel(order="F").copy()
     return q, mask, V_read, len(calc.ewald.kvecs)
+
+
+NONPERIODIC_CASES = ("water24", "tricmini", "mofmini")
+
+
+def main_nonperiodic():
+    """--fit-type 0 (the non-periodic 1/r basis) of the small cases: repeat.py's charges
+    on the same cube files, stored as tests/golden/nonperiodic.npz (q_ref0_<case>)."""
+    from ref_harness import load_reference
+    R = load_reference()
+    allc = cases()
+    out = {}
+    for name in NONPERIODIC_CASES:
+        cube = allc[name]()
+        d = tempfile.mkdtemp()
+        path = os.path.join(d, f"{name}.cube")
+        synth.write_cube(path, cube)
+        q, _mask, _V, _K = reference_fit(R, path, cube, 7, fit_flag=0)
+        out[f"q_ref0_{name}"] = q
+        print(name, "fit-type 0 charges", np.round(q[:4], 6), flush=True)
+    np.savez_compressed(os.path.join(HERE, "nonperiodic.npz"), **out)
 
 
 def main(names):
@@ -147,4 +169,7 @@ def main(names):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:])
+    if sys.argv[1:] == ["--nonperiodic"]:
+        main_nonperiodic()
+    else:
+        main(sys.argv[1:])

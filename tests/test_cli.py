@@ -35,11 +35,11 @@ def test_device_lists_refused():
 
 
 def test_unsupported_modes_exit_with_message(capsys):
-    assert cli.main(["x.cube", "--fit-type", "0"]) == 2
     assert cli.main(["x.cube", "--charge", "qeq"]) == 2
     assert cli.main([os.path.join(ROOT, "no_such.cube")]) == 1
+    assert cli.main([os.path.join(ROOT, "no_such.cube"), "--fit-type", "0"]) == 1
     out = capsys.readouterr().out
-    assert "fit-type 0" in out and "qeq" in out and "not found" in out
+    assert "qeq" in out and "not found" in out
 
 
 @pytest.mark.gpu
@@ -69,3 +69,26 @@ def test_cli_end_to_end(tmp_path, oracle_mod):
     vcoul = of_.phi() @ g["q_ref"]
     d = (vcoul - vcoul.mean()) - (of_.Vc - of_.Vc.mean())
     assert abs(rms - np.sqrt((d * d).mean())) <= 1e-3 * rms + 1e-9
+
+
+@pytest.mark.gpu
+def test_cli_nonperiodic_end_to_end(tmp_path):
+    """--fit-type 0 through the whole program: printed charges against repeat.py's."""
+    from conftest import load_nonperiodic
+    cube, q0 = load_nonperiodic("tricmini")
+    cf = os.path.join(tmp_path, "t.cube")
+    sf = os.path.join(tmp_path, "s.txt")
+    synth.write_cube(cf, cube)
+    synth.write_symmetry_file(sf, cube.symm_groups)
+    cmd = [sys.executable, "-m", "pyrepeat_gb300", cf, "--gpu", "0", "--fit-type", "0", "--symm-file", sf,
+           "--total-charge", str(cube.total_charge)]
+    if cube.resp:
+        rf = os.path.join(tmp_path, "r.txt")
+        synth.write_resp_file(rf, cube.resp)
+        cmd += ["--resp-file", rf]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rows = re.findall(r"^\s*(\d+)\s+([A-Z][a-z]?)\s+(-?\d+\.\d+)\s*$", r.stdout, re.M)
+    q = np.array([float(x[2]) for x in rows])
+    assert len(q) == cube.n_atoms
+    assert np.abs(q - q0).max() <= 1e-5 + 5e-7

@@ -40,6 +40,16 @@ def test_fp64_fit_matches_reference(name, tol, gpu_ctx):
     assert abs(r.charges.sum() - cube.total_charge) < 1e-10
 
 
+@pytest.mark.parametrize("name,tol", [("water24", 1e-8), ("mofmini", 1e-6), ("tricmini", 1e-8)])
+def test_nonperiodic_fp64_fit_matches_reference(name, tol, gpu_ctx):
+    """--fit-type 0 in plain FP64 against repeat.py's charges."""
+    from conftest import load_nonperiodic
+    from pyrepeat_gb300 import _lib
+    cube, q0 = load_nonperiodic(name)
+    r = gpu_ctx.fit_cube(cube, precision=_lib.PREC_FP64)
+    assert np.abs(r.charges - q0).max() <= tol * max(1.0, np.abs(q0).max())
+
+
 def test_fp64_normal_equations_match_oracle(gpu_ctx, oracle_mod):
     from pyrepeat_gb300 import _lib
     cube, _ = load_golden("tricmini")

@@ -27,6 +27,19 @@ def test_mixed_fit_matches_reference(name, gpu_ctx):
     assert abs(r.charges.sum() - cube.total_charge) < 1e-10
 
 
+@pytest.mark.parametrize("name", ["water24", "tricmini"])
+def test_nonperiodic_mixed_fit_matches_reference(name, gpu_ctx):
+    """--fit-type 0 (the 1/r basis, KMAX 0): staged path and batched single-pass path
+    against repeat.py's charges."""
+    from conftest import load_nonperiodic
+    from pyrepeat_gb300 import _lib
+    cube, q0 = load_nonperiodic(name)
+    r = gpu_ctx.fit_cube(cube, precision=_lib.PREC_MIXED)
+    assert np.abs(r.charges - q0).max() <= 1e-5
+    q, _, _ = gpu_ctx.fit_batch([cube], _lib.PREC_MIXED)
+    assert np.abs(q[0] - q0).max() <= 1e-5
+
+
 @pytest.mark.parametrize("name", ["tricmini", "batch1"])
 def test_mixed_normal_equations_close_to_fp64(name, gpu_ctx):
     from pyrepeat_gb300 import _lib

@@ -40,6 +40,15 @@ def test_oracle_charges_match_reference(name, tol, oracle_mod):
     assert abs(q.sum() - cube.total_charge) < 1e-10
 
 
+@pytest.mark.parametrize("name,tol", [("water24", 1e-10), ("mofmini", 1e-7), ("tricmini", 1e-10)])
+def test_oracle_nonperiodic_charges_match_reference(name, tol, oracle_mod):
+    """--fit-type 0 (the 1/r basis, KMAX 0 here): the oracle against repeat.py's charges."""
+    from conftest import load_nonperiodic
+    cube, q_ref0 = load_nonperiodic(name)
+    q = oracle_mod.OracleFit(cube).fit()
+    assert np.abs(q - q_ref0).max() <= tol * max(1.0, np.abs(q_ref0).max())
+
+
 def test_reference_binary_agrees_on_plain_fit(oracle_mod):
     """repeat_cpu_omp prints 6 decimals; it fits the same plain problem."""
     cube, g = load_golden("water24")
