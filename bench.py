@@ -271,13 +271,92 @@ def serve_arm(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def qeq_cell(n_atoms: int, seed: int):
+    """A periodic cell of n_atoms on a jittered 5 Bohr lattice (H, C, O, Zn at random), the
+    well-conditioned QEq system of a MOF-like density.  Returns (atoms, Z, n_grid, axis)."""
+    rng = np.random.default_rng(seed)
+    side = int(np.ceil((1.2 * n_atoms) ** (1.0 / 3.0)))
+    L = 5.0 * side
+    site = np.stack(np.meshgrid(*[np.arange(side)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    site = site[rng.choice(len(site), size=n_atoms, replace=False)]
+    atoms = (site + 0.5 + rng.uniform(-0.15, 0.15, size=(n_atoms, 3))) * 5.0
+    Z = rng.choice([1, 6, 8, 30], size=n_atoms)
+    ng = 2 * side * 5
+    return atoms, Z, np.array([ng, ng, ng]), np.eye(3) * (L / ng)
+
+
+def qeq_arm(args, world, rank, local):
+    """QEq charges (repeat.py:2539-2634) of one periodic cell per step through rp_qeq, from
+    host atoms and parameters to host charges: the Coulomb matrix (per-atom k tables, one
+    FP64 DGEMM, the real-space pair kernel over all 27+ images) and the equalisation solve.
+    CPU baseline: the oracle's NumPy Coulomb matrix on a bounded block of rows,
+    extrapolated in pairs, plus its full solve."""
+    import torch
+    from pyrepeat_gb300 import qeq as Q
+    from pyrepeat_gb300.fit import Context
+    torch.cuda.set_device(local)
+    ctx = Context(local)
+    N = args.qeq_atoms
+    atoms, Z, ngrid, axis = qeq_cell(N, 7 + rank)
+    chi, js, _, _ = Q.charge_parameters(Z)
+    for _ in range(max(args.warmup, 3)):
+        ctx.qeq(ngrid, axis, atoms, chi, js, 0.0, 20.0, 7)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        q, _, info = ctx.qeq(ngrid, axis, atoms, chi, js, 0.0, 20.0, 7)
+    torch.cuda.synchronize()
+    wall = max_over_ranks(time.perf_counter() - t0, world, "cuda")
+    ctx.set_timing(True)
+    ctx.stage_times()
+    ctx.qeq(ngrid, axis, atoms, chi, js, 0.0, 20.0, 7)
+    st = {k: round(v[0], 3) for k, v in ctx.stage_times().items()}
+    ctx.set_timing(False)
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        rows = min(N, 64)
+        t1 = time.perf_counter()
+        O.qeq_matrix(atoms[:rows], np.eye(3) * (axis[0, 0] * ngrid[0]), 20.0, 7, js[:rows])
+        t_rows = time.perf_counter() - t1
+        t1 = time.perf_counter()
+        O.qeq_charges(np.eye(N) + 0.01, chi, 0.0)   # LU time does not depend on the values
+        t_solve = time.perf_counter() - t1
+        pairs_sample = rows * (rows - 1) / 2
+        t_cpu = t_rows * (N * (N - 1) / 2) / pairs_sample + t_solve
+        cpu = {"value": 1.0 / t_cpu, "unit": "charge sets/s", "cores": 1, "kind": "port",
+               "sample": f"oracle Coulomb matrix of the first {rows} atoms ({int(pairs_sample)} pairs, "
+                         f"{t_rows:.2f} s) extrapolated to {N * (N - 1) // 2} pairs, plus its {N}-atom solve "
+                         f"({t_solve:.2f} s)"}
+    per = wall / args.steps
+    K = 754
+    line = {
+        "metric": "QEq charge sets/s (periodic Ewald Coulomb matrix + equalisation solve, host in/out)",
+        "value": args.steps * world / wall, "unit": "charge sets/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "pairs_per_s": N * (N - 1) / 2 / per, "stage_ms_one_step": st, "residual": info["residual"],
+        "e2e": {"value": args.steps * world / wall, "unit": "charge sets/s",
+                "h2d_bytes_per_step": 8 * (3 * N + 2 * N), "d2h_bytes_per_step": 8 * N},
+        "config": {"workload": f"qeq: {N} atoms on a jittered 5 Bohr lattice (H/C/O/Zn), cubic cell "
+                               f"{axis[0, 0] * ngrid[0]:.0f} Bohr, Rc 20 (27 images), KMAX 7 (K={K})"},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "mof", "water", "serve"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "mof", "water", "serve", "qeq"])
+    ap.add_argument("--qeq-atoms", type=int, default=2000)
     ap.add_argument("--serve-requests", type=int, default=600)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate, requests/s")
     ap.add_argument("--serve-pool", type=int, default=48, help="distinct batch-distribution cubes")
@@ -300,6 +379,9 @@ def main():
         return
     if args.workload == "serve":
         serve_arm(args, world, rank, local)
+        return
+    if args.workload == "qeq":
+        qeq_arm(args, world, rank, local)
         return
 
     import torch

@@ -130,6 +130,21 @@ int rp_solve(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n
 int rp_potential(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const double *q, int N,
                  const int32_t *idx_dev, int64_t npts, double *out_dev, rp_stream_t stream);
 
+/* QEq charges: replaces ChargeCalculator.compute_qeq_charges (repeat.py:2539-2634)
+ * below its per-element parameter lookup, i.e. the Coulomb matrix
+ *   J_ii = j_self[i],  J_ij = sum over every shift (|n_i| <= floor(Rc/|a_i|)+1, no cutoff)
+ *   with r > 1e-10 of erfc(sqrt(alpha) r)/r + sum_k kcoef_k cos(k.(r_i - r_j))
+ * (repeat.py:2575-2595, 2615-2634; with an ewald object of kmax 0, J_ij = 1/r_ij as in
+ * the non-periodic branch) and the equalisation system of repeat.py:2597-2613: sum q =
+ * qtot and (J q)_i + chi_i equal for every atom, solved in its bordered form
+ * [[J, 1],[1^T, 0]] [q; mu] = [-chi; qtot] by the same solve as rp_solve.
+ *   atoms [3N] host (Bohr, as in the cube), chi [N] host (electronegativity, Hartree),
+ *   j_self [N] host (J_ii = 2 x hardness); q [N] host out; J [N*N] host out
+ *   (row-major, may be NULL); info as rp_solve's (may be NULL).
+ *   RP_E_SINGULAR where the reference falls back to least squares. */
+int rp_qeq(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const double *chi,
+           const double *j_self, double qtot, double *q, double *J, double *info, rp_stream_t stream);
+
 /* rp_solve without any device allocation, for callers that cannot allocate
  * device memory while they run (a serving loop that must not stall on the
  * device-wide synchronisation cudaMalloc/cudaFree may cause, or an embedder whose

@@ -4,7 +4,9 @@ Used by tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` as the checker; the product never imports it.  It strings the C
 restatement together in the order of ``repeat.py``'s ``ChargeCalculator``:
 filter (repeat.py:1922-2113) -> pruned shifts (1708-1731) -> streamed normal
-equations (2184-2276) -> symmetry/RESP/bordered solve (2278-2313).
+equations (2184-2276) -> symmetry/RESP/bordered solve (2278-2313); and QEq
+charges (2539-2634) as NumPy: the pairwise Coulomb matrix and the reference's own
+difference-form system.
 """
 from __future__ import annotations
 
@@ -177,6 +179,52 @@ def solve(A, b, Z, groups=None, resp=None, qtot=0.0):
     sing = lib().orc_solve(N, A.ctypes.data, b.ctypes.data, len(ptr) - 1, ptr.ctypes.data, idx.ctypes.data,
                            rs.ctypes.data, rt.ctypes.data, qtot, q.ctypes.data)
     return q, bool(sing)
+
+
+def qeq_matrix(atoms, box, cutoff, kmax, j_self):
+    """Coulomb matrix of compute_qeq_charges (repeat.py:2575-2595): J_ii = j_self; for the
+    periodic fit (kmax > 0) J_ij = sum over the full shift list of erfc(sqrt(alpha) r)/r for
+    r > 1e-10 (no cutoff) + sum_k kcoef cos(k.(r_i - r_j)) (_ewald_pairwise,
+    repeat.py:2615-2634); for kmax 0, 1/r_ij for r > 1e-10.  Pairs i < j, mirrored."""
+    from scipy.special import erfc
+    atoms = _c(atoms)
+    N = len(atoms)
+    J = np.zeros((N, N))
+    np.fill_diagonal(J, _c(j_self))
+    if kmax > 0:
+        kv, kc = kspace(box, cutoff, kmax)
+        sh = shifts(box, cutoff)
+        sa = math.sqrt((math.pi / cutoff) ** 2)
+    for i in range(N - 1):
+        d = atoms[i] - atoms[i + 1:]
+        if kmax > 0:
+            r = np.linalg.norm(d[:, None, :] + sh[None, :, :], axis=2)
+            ok = r > 1e-10
+            real = np.where(ok, erfc(sa * r) / np.where(ok, r, 1.0), 0.0).sum(axis=1)
+            v = real + (kc[None, :] * np.cos(d @ kv.T)).sum(axis=1)
+        else:
+            r = np.linalg.norm(d, axis=1)
+            v = np.where(r > 1e-10, 1.0 / np.where(r > 1e-10, r, 1.0), 0.0)
+        J[i, i + 1:] = v
+        J[i + 1:, i] = v
+    return J
+
+
+def qeq_charges(J, chi, qtot=0.0):
+    """repeat.py:2597-2613: sum q = qtot and rows J[i-1] - J[i] against chi[i] - chi[i-1],
+    solved by LU (least squares where LU reports a singular matrix)."""
+    N = len(chi)
+    A = np.zeros((N, N))
+    b = np.zeros(N)
+    A[0, :] = 1.0
+    b[0] = qtot
+    for i in range(1, N):
+        A[i, :] = J[i - 1, :] - J[i, :]
+        b[i] = chi[i] - chi[i - 1]
+    try:
+        return np.linalg.solve(A, b)
+    except np.linalg.LinAlgError:
+        return np.linalg.lstsq(A, b, rcond=None)[0]
 
 
 class OracleFit:

@@ -13,8 +13,9 @@ FP64 fit instead of the mixed-precision one; ``--kmax`` (new, default 7, the
 reference's KMAX) sets the k-space cutoff; ``--cores``, ``--block-k`` and
 ``--no-jit`` steer the reference's CPU backends and are accepted without effect;
 ``--fit-type 0`` fits the non-periodic 1/r basis (the same filter, normal
-equations and constraints, no Ewald sum); ``--charge qeq`` is not part of this path
-and exits with a message.
+equations and constraints, no Ewald sum); ``--qeq-file`` restrains the fit as the
+reference does when no RESP file is given; ``--charge qeq`` prints (and with
+``--output`` writes) QEq charges, with the Coulomb matrix and the solve on the GPU.
 """
 from __future__ import annotations
 
@@ -65,9 +66,6 @@ def parse_device(spec: str | None) -> int:
 def main(argv=None) -> int:
     args = build_parser().parse_args(argv)
     device = parse_device(args.gpu)
-    if args.charge == "qeq":
-        print("Error: --charge qeq is not part of the GB300 path; use --charge repeat")
-        return 2
     from .calculator import ChargeCalculator
     from .constants import ATOM_SYMBOLS
 
@@ -86,6 +84,26 @@ def main(argv=None) -> int:
                             symm_file=args.symm_file, resp_file=args.resp_file, qeq_file=args.qeq_file,
                             n_cores=args.cores, block_k=args.block_k, use_jit=not args.no_jit, device=device,
                             fp64=args.fp64, kmax=args.kmax)
+    if args.charge == "qeq":
+        print("\n========================================")
+        print("Using QEq (Charge Equilibration) method")
+        print("========================================")
+        charges = calc.compute_qeq_charges()
+        print("\nQEq Charges:")
+        for i, q in enumerate(charges):
+            z = int(calc.cube["atom_index"][i])
+            sym = ATOM_SYMBOLS[z] if z < len(ATOM_SYMBOLS) else "X"
+            print(f"{i + 1:4d} {sym:2s} {q:12.6f}")
+        print(f"\nTotal charge: {np.sum(charges):.6f}")
+        if args.output:
+            with open(args.output, "w") as f:
+                for i, q in enumerate(charges):
+                    z = int(calc.cube["atom_index"][i])
+                    sym = ATOM_SYMBOLS[z] if z < len(ATOM_SYMBOLS) else "X"
+                    pos = calc.cube["atom_pos"][i]
+                    f.write(f"{i + 1:4d} {sym:2s} {pos[0]:12.6f} {pos[1]:12.6f} {pos[2]:12.6f} {q:12.6f}\n")
+            print(f"QEq charges written to {args.output}")
+        return 0
     print("\n========================================")
     print("Using REPEAT method (Streaming)")
     print("========================================")

@@ -24,7 +24,7 @@ PREC_MIXED = 1
 EXPORTS = ["rp_version", "rp_ctx_create", "rp_ctx_destroy", "rp_last_error", "rp_filter", "rp_ewald_setup",
            "rp_ewald_destroy", "rp_ewald_info", "rp_gram", "rp_solve", "rp_potential", "rp_fit",
            "rp_fit_batch", "rp_set_timing", "rp_stage_times", "rp_launch_count", "rp_solve_noalloc",
-           "rp_batch_submit", "rp_batch_poll", "rp_batch_wait"]
+           "rp_batch_submit", "rp_batch_poll", "rp_batch_wait", "rp_qeq"]
 
 
 class RepeatError(RuntimeError):
@@ -105,6 +105,8 @@ def load(path: str | None = None):
     L.rp_batch_poll.argtypes = [P, ctypes.c_longlong, ctypes.POINTER(I), ctypes.POINTER(I)]
     L.rp_batch_wait.restype = I
     L.rp_batch_wait.argtypes = [P, ctypes.c_longlong, ctypes.POINTER(I)]
+    L.rp_qeq.restype = I
+    L.rp_qeq.argtypes = [P, P, P, I, P, P, D, P, P, P, P]
     _lib = L
     return L
 

@@ -34,6 +34,7 @@ CUDA_SOURCES = [
     "gram_mixed.cu",
     "solve.cu",
     "potential.cu",
+    "qeq.cu",
 ]
 
 

@@ -12,15 +12,16 @@ Phi q for the statistics without forming Phi.
 Arguments that only steer the reference's CPU backends (``n_cores``,
 ``block_k``, ``use_jit``) are accepted and have no effect.  ``fit_flag=0`` fits the
 non-periodic 1/r basis (repeat.py:991-994) with the same machinery (KMAX 0 in the
-device library).  QEq charges are not part of this path: they raise
-NotImplementedError.  There is no CPU fallback: without a CUDA device every
-call raises.
+device library).  A QEq file restrains the fit as the reference's ``_apply_qeq``
+does, and ``compute_qeq_charges()`` gives QEq charges (repeat.py:2539-2634) from
+``rp_qeq``: the Coulomb matrix on the device and the equalisation solve.  There is
+no CPU fallback: without a CUDA device every call raises.
 """
 from __future__ import annotations
 
 import numpy as np
 
-from . import _lib, cube as cube_io
+from . import _lib, cube as cube_io, qeq as qeq_mod
 from .fit import Context
 from .synth import Cube
 
@@ -62,16 +63,13 @@ class ChargeCalculator:
         resp = cube_io.read_resp(resp_file) if resp_file else None
         self.resp_data = ({el: {"strength": s, "target": t} for el, (s, t) in resp.items()} if resp_file
                           else None)
-        self.qeq_data = None
-        if qeq_file:
-            self.qeq_data = {}
-            with open(qeq_file) as f:
-                for line in f:
-                    p = line.split()
-                    if len(p) >= 3:
-                        self.qeq_data[p[0]] = {"electroneg": float(p[1]), "hardness": float(p[2])}
+        self.qeq_data = qeq_mod.read_qeq_file(qeq_file) if qeq_file else None
         self._groups = groups or None
         self._resp = resp or None
+        # repeat.py:2288-2294: RESP when its table is non-empty, else the QEq restraint when
+        # the QEq table is non-empty; both are diagonal restraints of the bordered system
+        self._restraint = self._resp or (qeq_mod.restraint_table(self.cube["atom_index"], self.qeq_data)
+                                         if self.qeq_data else None) or None
         self._kept = None      # device kept indices (flat order) and centred ESP, for the statistics
         self._Vc = None
         self.charges = None
@@ -88,7 +86,8 @@ class ChargeCalculator:
         c = self.cube
         return Cube(np.asarray(c["atom_index"], dtype=np.int64), np.asarray(c["atom_pos"], dtype=np.float64),
                     np.asarray(c["n_grid"], dtype=np.int64), np.asarray(c["axis_vector"], dtype=np.float64),
-                    np.ascontiguousarray(c["V_flat"], dtype=np.float64), symm_groups=self._groups, resp=self._resp,
+                    np.ascontiguousarray(c["V_flat"], dtype=np.float64), symm_groups=self._groups,
+                    resp=self._restraint,
                     kmax=self.kmax if self.fit_flag == 1 else 0, cutoff=self.R_cutoff,
                     vdw_factor=self.vdw_factor, vdw_max=self.vdw_max,
                     total_charge=self.q_tot, name=str(self.cube_file))
@@ -161,5 +160,19 @@ class ChargeCalculator:
             out["V_coul"] = vcoul.cpu().numpy()
         return out
 
-    def compute_qeq_charges(self):
-        raise NotImplementedError("QEq charges (repeat.py:2539-2634) are not part of the GB300 fit path")
+    def compute_qeq_charges(self, param_set=None) -> np.ndarray:
+        """QEq charges (repeat.py:2539-2634): per-atom chi and J_ii from the QEq file, then
+        ``param_set`` (default: the reference's table; a caller's set selects EQeq and its
+        hydrogen rule), else 0.15 / 0.50 with a warning; then rp_qeq builds the Coulomb
+        matrix under this calculator's Ewald parameters (1/r for fit_flag 0) and solves
+        the equalisation system under the total charge."""
+        c = self.cube
+        chi, jself, method, missing = qeq_mod.charge_parameters(c["atom_index"], self.qeq_data, param_set)
+        for sym in missing:
+            print(f"Warning: No parameters for {sym}, using defaults")
+        if self.verbose:
+            print(f"Computing {method} Coulomb matrix...")
+        q, _J, info = self.ctx.qeq(c["n_grid"], c["axis_vector"], c["atom_pos"], chi, jself, self.q_tot,
+                                   self.R_cutoff, self.kmax if self.fit_flag == 1 else 0)
+        self.qeq_info = info
+        return q

@@ -8,6 +8,8 @@
 namespace rp {
 void potential_run(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const double *q, int N,
                    const int32_t *idx_dev, int64_t npts, double *out_dev, cudaStream_t stream);
+void qeq_run(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const double *chi, const double *j_self,
+             double qtot, double *q_out, double *J_out, double *info, cudaStream_t stream);
 }  // namespace rp
 
 namespace rp {
@@ -178,6 +180,15 @@ int rp_potential(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, const dou
     return guarded(ctx, [&] {
         RP_REQUIRE(ew->device == ctx->device, "rp_potential: ewald built on another device");
         rp::potential_run(ctx, ew, atoms, q, N, idx_dev, npts, out_dev, (cudaStream_t)stream);
+    });
+}
+
+int rp_qeq(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const double *chi, const double *j_self,
+           double qtot, double *q, double *J, double *info, rp_stream_t stream) {
+    if (!ctx || !ew) return RP_E_ARG;
+    return guarded(ctx, [&] {
+        RP_REQUIRE(ew->device == ctx->device, "rp_qeq: ewald built on another device");
+        rp::qeq_run(ctx, ew, atoms, N, chi, j_self, qtot, q, J, info, (cudaStream_t)stream);
     });
 }
 

@@ -50,6 +50,7 @@ struct SolveDesc {
     int *perm;            // n+1 pivot rows
     double *q;            // N out
     double *info;         // 4 out: residual inf-norm, min|piv|, max|piv|, singular flag
+    double *pre;          // null, or {failed, min|piv|, max|piv|} of a wide factorisation already in As
 };
 
 namespace {
@@ -464,16 +465,25 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
     // ---- FP32 LU + FP64-residual refinement
     {
         float *L = reinterpret_cast<float *>(d.As);  // the first half of the FP64 work matrix
-        for (long long t = threadIdx.x; t < (long long)n1 * n1; t += kLU) L[t] = (float)d.A0[t];
+        if (!d.pre)
+            for (long long t = threadIdx.x; t < (long long)n1 * n1; t += kLU) L[t] = (float)d.A0[t];
         for (int t = threadIdx.x; t < n1; t += kLU) {
             d.x[t] = 0.0;
             d.r[t] = d.bs[t];
         }
         __syncthreads();
-        const bool factored = n1 <= kLUBlockedMax
-                                  ? lu_factor_f32_blocked(L, d.perm, n1, fsh, reinterpret_cast<float *>(sv), si,
-                                                          &piv_i, pmin, pmax)
-                                  : lu_factor_f32(L, d.perm, n1, sv, si, &piv_v, &piv_i, pmin, pmax);
+        bool factored;
+        if (d.pre) {  // factored across the GPU before this launch (lu_wide_factor)
+            factored = d.pre[0] == 0.0;
+            if (factored) {
+                pmin = fmin(pmin, d.pre[1]);
+                pmax = fmax(pmax, d.pre[2]);
+            }
+        } else {
+            factored = n1 <= kLUBlockedMax ? lu_factor_f32_blocked(L, d.perm, n1, fsh, reinterpret_cast<float *>(sv),
+                                                                   si, &piv_i, pmin, pmax)
+                                           : lu_factor_f32(L, d.perm, n1, sv, si, &piv_v, &piv_i, pmin, pmax);
+        }
         if (factored) {
             double an = 0.0;  // |A| (max row sum)
             for (int rr = threadIdx.x; rr < n1; rr += kLU) {
@@ -586,6 +596,135 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
     for (int i = threadIdx.x; i < d.N; i += kLU) d.q[i] = d.x[d.map[i]];
 }
 
+// ---------------------------------------------------------------------------
+// Wide factorisation of one large system across the whole GPU (kLUWideMin <= n1 <=
+// kLUWideMax), before lu_solve_refine_kernel refines it.  One CTA factoring n1^3 / 3 FMAs
+// alone is SM-bound (20 ms at n1 = 1456, 0.75 s at 2001); here only the panels are serial.
+// The FP32 copy of A0 goes into As, then per panel of nb columns (32, or 16 / 8 / 4 when
+// the panel's rows do not fit shared memory at 32):
+//   lu_panel_kernel   one CTA: the panel in shared memory, factored with the same partial
+//                     pivoting as lu_factor_f32_blocked (perm[k] = pivot row, full-row
+//                     swaps), written back, its swaps applied to every other column;
+//   lu_trsm_kernel    U12 = L11^-1 A12, a thread per column over many CTAs;
+//   cuBLAS SGEMM      A22 -= L21 U12 (FP32, plain GEMM).
+// A zero or non-finite pivot sets pre[0]; the later panels then return at once and the
+// refinement kernel goes to its FP64 factorisation.
+constexpr int kLUWideMin = 768;
+constexpr size_t kPanelSmem = 225 * 1024;
+constexpr int kLUWideMax = (int)(kPanelSmem / (sizeof(float) * 5));  // panel rows at nb = 4
+
+int wide_panel_nb(int m) {
+    for (int nb = 32; nb >= 4; nb /= 2)
+        if (sizeof(float) * (size_t)m * (nb + 1) <= kPanelSmem) return nb;
+    return 0;
+}
+
+__global__ void lu_to_f32_kernel(const double *__restrict__ A0, float *__restrict__ L, long long n,
+                                 double *__restrict__ pre) {
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long t = t0; t < n; t += (long long)gridDim.x * blockDim.x) L[t] = (float)A0[t];
+    if (t0 == 0) {
+        pre[0] = 0.0;
+        pre[1] = 1e308;
+        pre[2] = 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(kLU) lu_panel_kernel(float *__restrict__ A, int *__restrict__ perm, int n1,
+                                                       int k0, int NB, double *__restrict__ pre) {
+    if (pre[0] != 0.0) return;  // an earlier panel met a zero pivot
+    extern __shared__ float P[];  // [m][NB + 1] panel rows k0..n1-1
+    __shared__ float svf[kLU / 32];
+    __shared__ int si[kLU / 32];
+    __shared__ int piv_i;
+    const int m = n1 - k0, nb = min(NB, m), ld = NB + 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int t = threadIdx.x; t < m * NB; t += kLU) {
+        const int r = t / NB, c = t - r * NB;
+        P[r * ld + c] = c < nb ? A[(size_t)(k0 + r) * n1 + k0 + c] : 0.f;
+    }
+    __syncthreads();
+    float fmin_p = 3.0e38f, fmax_p = 0.f;
+    for (int j = 0; j < nb; ++j) {
+        float best = -1.0f;
+        int bi = 0x7fffffff;
+        for (int r = j + threadIdx.x; r < m; r += kLU) {
+            const float v = fabsf(P[r * ld + j]);
+            if (v > best || (v == best && r < bi)) { best = v; bi = r; }
+        }
+        block_argmax_f(best, bi, svf, si, &piv_i);
+        const int p = piv_i;
+        if (threadIdx.x == 0) perm[k0 + j] = k0 + p;
+        if (p != j && threadIdx.x < NB) {
+            const float t = P[j * ld + threadIdx.x];
+            P[j * ld + threadIdx.x] = P[p * ld + threadIdx.x];
+            P[p * ld + threadIdx.x] = t;
+        }
+        __syncthreads();
+        const float pv = P[j * ld + j];
+        const float apv = fabsf(pv);
+        if (!(apv > 0.f) || !isfinite(pv)) {  // uniform: every thread read the same pivot
+            if (threadIdx.x == 0) pre[0] = 1.0;
+            return;
+        }
+        fmin_p = fminf(fmin_p, apv);
+        fmax_p = fmaxf(fmax_p, apv);
+        const float inv = 1.0f / pv;
+        for (int r = j + 1 + warp; r < m; r += kLU / 32) {
+            float *row = P + r * ld;
+            const float l = row[j] * inv;
+            if (lane > j && lane < nb) row[lane] -= l * P[j * ld + lane];
+            __syncwarp();
+            if (lane == 0) row[j] = l;
+        }
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < m * NB; t += kLU) {
+        const int r = t / NB, c = t - r * NB;
+        if (c < nb) A[(size_t)(k0 + r) * n1 + k0 + c] = P[r * ld + c];
+    }
+    for (int c = threadIdx.x; c < n1; c += kLU) {
+        if (c >= k0 && c < k0 + nb) continue;
+        for (int j = 0; j < nb; ++j) {
+            const int p = perm[k0 + j];
+            if (p != k0 + j) {
+                const float t = A[(size_t)(k0 + j) * n1 + c];
+                A[(size_t)(k0 + j) * n1 + c] = A[(size_t)p * n1 + c];
+                A[(size_t)p * n1 + c] = t;
+            }
+        }
+    }
+    if (threadIdx.x == 0) {
+        pre[1] = fmin(pre[1], (double)fmin_p);
+        pre[2] = fmax(pre[2], (double)fmax_p);
+    }
+}
+
+template <int NB>
+__global__ void __launch_bounds__(256) lu_trsm_kernel(float *__restrict__ A, int n1, int k0,
+                                                      const double *__restrict__ pre) {
+    if (pre[0] != 0.0) return;
+    __shared__ float Ls[NB][NB + 1];
+    const int nb = min(NB, n1 - k0), c1 = k0 + nb;
+    for (int t = threadIdx.x; t < NB * NB; t += blockDim.x) {
+        const int i = t / NB, j = t - i * NB;
+        Ls[i][j] = (i < nb && j < nb) ? A[(size_t)(k0 + i) * n1 + k0 + j] : 0.f;
+    }
+    __syncthreads();
+    const int c = c1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n1) return;
+    float u[NB];
+#pragma unroll
+    for (int j = 0; j < NB; ++j) u[j] = j < nb ? A[(size_t)(k0 + j) * n1 + c] : 0.f;
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+#pragma unroll
+        for (int i = j + 1; i < NB; ++i) u[i] -= Ls[i][j] * u[j];
+#pragma unroll
+    for (int j = 0; j < NB; ++j)
+        if (j < nb) A[(size_t)(k0 + j) * n1 + c] = u[j];
+}
+
 // dynamic shared memory of lu_solve_refine_kernel: the right-hand side and correction in
 // FP32 (2 n1 floats) and, for the blocked factorisation, the panel and the U12 tile
 size_t solve_smem_bytes(int n1) {
@@ -601,6 +740,40 @@ void lu_smem_optin() {
         const size_t most = std::max(solve_smem_bytes(kLUBlockedMax), solve_smem_bytes(1));
         RP_CUDA(cudaFuncSetAttribute(lu_solve_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most));
         done = true;
+    }
+}
+
+void lu_wide_factor(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t stream) {
+    static bool optin = false;
+    if (!optin) {
+        RP_CUDA(cudaFuncSetAttribute(lu_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmem));
+        optin = true;
+    }
+    float *L = reinterpret_cast<float *>(d.As);
+    const long long nn = (long long)n1 * n1;
+    lu_to_f32_kernel<<<(int)std::min<long long>(ceil_div(nn, 256), 4096), 256, 0, stream>>>(d.A0, L, nn, d.pre);
+    RP_LAUNCH_CHECK();
+    cublasHandle_t h = ctx->blas();
+    RP_CUBLAS(cublasSetStream(h, stream));
+    const float minus_one = -1.0f, one = 1.0f;
+    for (int k0 = 0; k0 < n1;) {
+        const int m = n1 - k0, NB = wide_panel_nb(m), nb = std::min(NB, m), c1 = k0 + nb;
+        lu_panel_kernel<<<1, kLU, sizeof(float) * (size_t)m * (NB + 1), stream>>>(L, d.perm, n1, k0, NB, d.pre);
+        RP_LAUNCH_CHECK();
+        if (c1 < n1) {
+            const int w = n1 - c1, grid = (int)ceil_div(w, 256);
+            switch (NB) {
+                case 32: lu_trsm_kernel<32><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
+                case 16: lu_trsm_kernel<16><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
+                case 8: lu_trsm_kernel<8><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
+                default: lu_trsm_kernel<4><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
+            }
+            RP_LAUNCH_CHECK();
+            // row-major A22 (w x w) -= L21 (w x nb) U12 (nb x w), as column-major C^T -= U12^T L21^T
+            RP_CUBLAS(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, w, w, nb, &minus_one, L + (size_t)k0 * n1 + c1, n1,
+                                  L + (size_t)c1 * n1 + k0, n1, &one, L + (size_t)c1 * n1 + c1, n1));
+        }
+        k0 = c1;
     }
 }
 
@@ -728,6 +901,7 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
     double *r = ctx->buf_t<double>("s_r" + tag, n_red);
     int *perm = ctx->buf_t<int>("s_perm" + tag, n_red);
     double *d_info = ctx->buf_t<double>("s_info" + tag, (size_t)nj * 4);
+    double *d_pre = ctx->buf_t<double>("s_pre" + tag, (size_t)nj * 3);
     SolveDesc *d_desc = ctx->buf_t<SolveDesc>("s_desc" + tag, (size_t)nj);
     // host staging of the small per-system tables, one upload each
     std::vector<int> h_map(n_map), h_mptr(n_mptr), h_midx(n_midx, 0);
@@ -810,6 +984,14 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
             RP_CUDA(cudaMemcpyAsync(descs[j].bs, hbs.data(), sizeof(double) * hbs.size(), cudaMemcpyHostToDevice, stream));
             RP_CUDA(cudaStreamSynchronize(stream));
         }
+    }
+    // large systems: factored across the GPU first (lu_solve_refine_kernel then refines them)
+    for (int j = 0; j < nj; ++j) {
+        const int n1 = plans[j].n + 1;
+        if (n1 < kLUWideMin || n1 > kLUWideMax) continue;
+        descs[j].pre = d_pre + 3 * (size_t)j;
+        StageTimer tt(ctx, "solve_lu_wide", stream);
+        lu_wide_factor(ctx, descs[j], n1, stream);
     }
     std::memcpy(stage + st_off[5], descs.data(), st_bytes[5]);
     RP_CUDA(cudaMemcpyAsync(d_desc, stage + st_off[5], st_bytes[5], cudaMemcpyHostToDevice, stream));

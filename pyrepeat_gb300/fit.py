@@ -166,6 +166,29 @@ class Context:
         self.check(rc, "rp_potential")
         return out
 
+    def qeq(self, n_grid, axis, atoms, chi, j_self, qtot=0.0, cutoff=20.0, kmax=7, want_J=False):
+        """QEq charges through rp_qeq: the Coulomb matrix of the atoms under the Ewald
+        object of (grid, cutoff, kmax; kmax 0 = the 1/r matrix) and the equalisation
+        solve.  Returns (charges, J or None, info)."""
+        atoms = np.ascontiguousarray(atoms, dtype=np.float64)
+        N = len(atoms)
+        chi = np.ascontiguousarray(chi, dtype=np.float64)
+        j_self = np.ascontiguousarray(j_self, dtype=np.float64)
+        if chi.shape != (N,) or j_self.shape != (N,):
+            raise ValueError("chi and j_self need one value per atom")
+        q = np.zeros(N)
+        J = np.zeros((N, N)) if want_J else None
+        info = np.zeros(3)
+        ew = self.ewald(n_grid, axis, cutoff, kmax)
+        try:
+            rc = self.lib.rp_qeq(self.ptr, ew.ptr, atoms.ctypes.data, N, chi.ctypes.data, j_self.ctypes.data,
+                                 float(qtot), q.ctypes.data, J.ctypes.data if J is not None else None,
+                                 info.ctypes.data, self._stream())
+            self.check(rc, "rp_qeq")
+        finally:
+            ew.close()
+        return q, J, {"residual": float(info[0]), "pivot_min": float(info[1]), "pivot_max": float(info[2])}
+
     # ------------------------------------------------------------------ whole fits
     def fit_cube(self, cube, precision=_lib.PREC_MIXED, V_dev=None, keep_normal=False):
         """Fit one synth.Cube-like object (atom_index, atom_pos, n_grid, axis_vector, V,

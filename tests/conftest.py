@@ -70,6 +70,18 @@ def load_nonperiodic(name: str):
     return cube, z[f"q_ref0_{name}"]
 
 
+def load_qeq():
+    """repeat.py's QEq results on the small cases (tests/golden/qeq.npz), the QEq
+    parameter file they used (parsed) and its text, and their total charge."""
+    z = dict(np.load(os.path.join(GOLDEN, "qeq.npz"), allow_pickle=False))
+    text = str(z["qeq_file"])
+    qd = {}
+    for line in text.splitlines():
+        p = line.split()
+        qd[p[0]] = {"electroneg": float(p[1]), "hardness": float(p[2])}
+    return z, qd, text, float(z["qtot"])
+
+
 @pytest.fixture(scope="session")
 def oracle_mod():
     import oracle

@@ -16,6 +16,7 @@ test regenerates it from the stored atoms/charges/seed with the same generator.
 
 Usage:  python tests/golden/make_golden.py [case ...]
         python tests/golden/make_golden.py --nonperiodic    (fit-type 0 charges of the small cases)
+        python tests/golden/make_golden.py --qeq            (QEq charges and QEq-restrained fits)
 """
 from __future__ import annotations
 
@@ -60,7 +61,6 @@ def reference_fit(R, cube_path, cube, kmax, fit_flag=1):
     """Run repeat.py's ChargeCalculator on a cube file; KMAX other than 7 is
     applied by re-running the reference's own k-space rule (repeat.py:1127-1143)
     with the larger KMAX after construction."""
-    import itertools  # noqa: F401
     symm = resp = None
     tmp = os.path.dirname(cube_path)
     if cube.symm_groups:
@@ -69,8 +69,32 @@ def reference_fit(R, cube_path, cube, kmax, fit_flag=1):
     if cube.resp:
         resp = os.path.join(tmp, "resp.txt")
         synth.write_resp_file(resp, cube.resp)
-    if kmax != 7:
-        orig = R.EwaldCalculator._setup_kspace
+    with kmax_patch(R, kmax):
+        calc = R.ChargeCalculator(cube_path, fit_flag=fit_flag, vdw_factor=cube.vdw_factor, vdw_max=cube.vdw_max,
+                                  R_cutoff=cube.cutoff, q_tot=cube.total_charge, symm_file=symm,
+                                  resp_file=resp, use_jit=False)
+        q = calc.fit_charges()
+    nx, ny, nz = (int(v) for v in cube.n_grid)
+    idx = np.rint(calc.grid_pos @ np.linalg.inv(cube.axis_vector)).astype(np.int64)
+    flat = idx[:, 0] + idx[:, 1] * nx + idx[:, 2] * nx * ny
+    mask = np.zeros(nx * ny * nz, dtype=np.uint8)
+    mask[flat] = 1
+    V_read = calc.cube["V_pot"].ravel(order="F").copy()
+    return q, mask, V_read, len(calc.ewald.kvecs)
+
+
+class kmax_patch:
+    """Within the block, repeat.py's EwaldCalculator builds its k-set with this KMAX
+    (the reference's own rule, repeat.py:1127-1143, with the constant replaced)."""
+
+    def __init__(self, R, kmax):
+        self.R, self.kmax, self.orig = R, kmax, None
+
+    def __enter__(self):
+        R, kmax = self.R, self.kmax
+        if kmax == 7:
+            return self
+        self.orig = R.EwaldCalculator._setup_kspace
 
         def setup_kmax(self, _K=kmax):
             KMAX, KSQMAX = _K, _K * _K
@@ -89,21 +113,11 @@ def reference_fit(R, cube_path, cube, kmax, fit_flag=1):
             self.kvecs = np.asarray(kv, dtype=np.float64)
             self.kcoefs = np.asarray(kc, dtype=np.float64)
         R.EwaldCalculator._setup_kspace = setup_kmax
-    try:
-        calc = R.ChargeCalculator(cube_path, fit_flag=fit_flag, vdw_factor=cube.vdw_factor, vdw_max=cube.vdw_max,
-                                  R_cutoff=cube.cutoff, q_tot=cube.total_charge, symm_file=symm,
-                                  resp_file=resp, use_jit=False)
-        q = calc.fit_charges()
-    finally:
-        if kmax != 7:
-            R.EwaldCalculator._setup_kspace = orig
-    nx, ny, nz = (int(v) for v in cube.n_grid)
-    idx = np.rint(calc.grid_pos @ np.linalg.inv(cube.axis_vector)).astype(np.int64)
-    flat = idx[:, 0] + idx[:, 1] * nx + idx[:, 2] * nx * ny
-    mask = np.zeros(nx * ny * nz, dtype=np.uint8)
-    mask[flat] = 1
-    V_read = calc.cube["V_pot"].ravel(order="F").copy()
-    return q, mask, V_read, len(calc.ewald.kvecs)
+        return self
+
+    def __exit__(self, *exc):
+        if self.orig is not None:
+            self.R.EwaldCalculator._setup_kspace = self.orig
 
 
 NONPERIODIC_CASES = ("water24", "tricmini", "mofmini")
@@ -125,6 +139,56 @@ def main_nonperiodic():
         out[f"q_ref0_{name}"] = q
         print(name, "fit-type 0 charges", np.round(q[:4], 6), flush=True)
     np.savez_compressed(os.path.join(HERE, "nonperiodic.npz"), **out)
+
+
+QEQ_CASES = ("water24", "tricmini", "mofmini")
+QEQ_FILE_TEXT = "O 0.31 0.30\nC 0.21 0.22\n"   # two elements; the others fall back to the default table
+QEQ_QTOT = 0.5
+PB_Z = 82                                       # lead: no entry in the default QEq table
+
+
+def main_qeq():
+    """QEq of the small cases through repeat.py, stored as tests/golden/qeq.npz:
+    q_qeq<f>_<case>  compute_qeq_charges() with the QEq file, fit type f (1 periodic, 0 1/r);
+    q_eqeq_<case>    compute_qeq_charges(param_set=DEFAULT_QEQ_PARAMS): EQeq (hydrogen rule);
+    q_qeqr<f>_<case> fit_charges() restrained by the QEq file (symmetry groups kept, no RESP);
+    q_qeq1_pb        water24 with its last atom made lead (no parameters: 0.15 / 0.50), no file.
+    Every run uses total charge QEQ_QTOT and the case's KMAX."""
+    from ref_harness import load_reference
+    R = load_reference()
+    allc = cases()
+    out = {"qtot": QEQ_QTOT, "qeq_file": QEQ_FILE_TEXT}
+    for name in QEQ_CASES + ("pb",):
+        cube = allc["water24" if name == "pb" else name]()
+        if name == "pb":
+            cube.atom_index = cube.atom_index.copy()
+            cube.atom_index[-1] = PB_Z
+            out["atom_index_pb"] = cube.atom_index.astype(np.int32)
+        d = tempfile.mkdtemp()
+        path = os.path.join(d, f"{name}.cube")
+        synth.write_cube(path, cube)
+        qf = None
+        if name != "pb":
+            qf = os.path.join(d, "qeq.txt")
+            with open(qf, "w") as f:
+                f.write(QEQ_FILE_TEXT)
+        symm = None
+        if cube.symm_groups:
+            symm = os.path.join(d, "symm.txt")
+            synth.write_symmetry_file(symm, cube.symm_groups)
+        for fit_flag in ((1,) if name == "pb" else (1, 0)):
+            with kmax_patch(R, cube.kmax):
+                calc = R.ChargeCalculator(path, fit_flag=fit_flag, vdw_factor=cube.vdw_factor,
+                                          vdw_max=cube.vdw_max, R_cutoff=cube.cutoff, q_tot=QEQ_QTOT,
+                                          symm_file=symm, qeq_file=qf, use_jit=False)
+                out[f"q_qeq{fit_flag}_{name}"] = calc.compute_qeq_charges()
+                if name == "pb":
+                    continue
+                if fit_flag == 1:
+                    out[f"q_eqeq_{name}"] = calc.compute_qeq_charges(param_set=R.DEFAULT_QEQ_PARAMS)
+                out[f"q_qeqr{fit_flag}_{name}"] = calc.fit_charges()
+            print(name, fit_flag, np.round(out[f"q_qeq{fit_flag}_{name}"][:4], 6), flush=True)
+    np.savez_compressed(os.path.join(HERE, "qeq.npz"), **out)
 
 
 def main(names):
@@ -171,5 +235,7 @@ def main(names):
 if __name__ == "__main__":
     if sys.argv[1:] == ["--nonperiodic"]:
         main_nonperiodic()
+    elif sys.argv[1:] == ["--qeq"]:
+        main_qeq()
     else:
         main(sys.argv[1:])

@@ -1,6 +1,6 @@
 """The reference-compatible command line (python -m pyrepeat_gb300).
 
-CPU: flag handling and the refusals (device lists, the non-periodic fit, QEq).
+CPU: flag handling and the refusals (device lists, a missing cube).
 GPU: the whole program on a golden cube written as a Gaussian cube file, with
 symmetry and RESP files: printed charges against the reference's (1e-5 e), the
 --output file (x y z V_coul V_qm per kept point) and the RMS against the oracle."""
@@ -34,12 +34,12 @@ def test_device_lists_refused():
             cli.parse_device(spec)
 
 
-def test_unsupported_modes_exit_with_message(capsys):
-    assert cli.main(["x.cube", "--charge", "qeq"]) == 2
+def test_missing_cube_exits_with_message(capsys):
     assert cli.main([os.path.join(ROOT, "no_such.cube")]) == 1
     assert cli.main([os.path.join(ROOT, "no_such.cube"), "--fit-type", "0"]) == 1
+    assert cli.main([os.path.join(ROOT, "no_such.cube"), "--charge", "qeq"]) == 1
     out = capsys.readouterr().out
-    assert "qeq" in out and "not found" in out
+    assert out.count("not found") == 3
 
 
 @pytest.mark.gpu

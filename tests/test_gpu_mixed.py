@@ -201,11 +201,12 @@ def test_potential_matches_phi_q(gpu_ctx, oracle_mod):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("N", [61, 700, 1600])
+@pytest.mark.parametrize("N", [61, 700, 767, 1000, 1600, 1800, 3500])
 def test_bordered_solve_large_systems(gpu_ctx, N):
-    """The bordered solve on systems of many 32-column panels (the blocked FP32 LU with
-    FP64 refinement; N = 1600 takes the unblocked factorisation) against an FP64 LU of
-    the same bordered system."""
+    """The bordered solve on systems of many panels against an FP64 LU of the same
+    bordered system: the one-CTA blocked FP32 LU (N + 1 < 768) and the wide factorisation
+    across the GPU (panels of 32 columns, of 16 while the panel has more than 1745 rows and
+    of 8 past 3388, cuBLAS trailing updates), both with FP64 refinement."""
     import scipy.linalg as sl
     import torch
     rng = np.random.default_rng(N)

@@ -49,6 +49,48 @@ def test_oracle_nonperiodic_charges_match_reference(name, tol, oracle_mod):
     assert np.abs(q - q_ref0).max() <= tol * max(1.0, np.abs(q_ref0).max())
 
 
+@pytest.mark.parametrize("name", SMALL + ["pb"])
+def test_oracle_qeq_charges_match_reference(name, oracle_mod):
+    """QEq charges (repeat.py:2539-2634): the oracle's Coulomb matrix and difference-form
+    solve against repeat.py's compute_qeq_charges, periodic and 1/r, QEq and EQeq."""
+    from conftest import load_qeq
+    from pyrepeat_gb300 import qeq as Q
+    z, qd, _, qtot = load_qeq()
+    cube, _ = load_golden("water24" if name == "pb" else name)
+    Z = z["atom_index_pb"] if name == "pb" else cube.atom_index
+    qd = None if name == "pb" else qd
+    for f in ((1,) if name == "pb" else (1, 0)):
+        chi, js, _, missing = Q.charge_parameters(Z, qd)
+        assert missing == (["Pb"] if name == "pb" else [])
+        J = oracle_mod.qeq_matrix(cube.atom_pos, cube.box_vectors, cube.cutoff, cube.kmax if f else 0, js)
+        q = oracle_mod.qeq_charges(J, chi, qtot)
+        assert np.abs(q - z[f"q_qeq{f}_{name}"]).max() <= 1e-10
+        assert abs(q.sum() - qtot) <= 1e-12
+    if name != "pb":
+        chi, js, method, _ = Q.charge_parameters(Z, qd, Q.DEFAULT_QEQ_PARAMS)
+        assert method == "EQeq"
+        J = oracle_mod.qeq_matrix(cube.atom_pos, cube.box_vectors, cube.cutoff, cube.kmax, js)
+        assert np.abs(oracle_mod.qeq_charges(J, chi, qtot) - z[f"q_eqeq_{name}"]).max() <= 1e-10
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_oracle_qeq_restrained_fit_matches_reference(name, oracle_mod):
+    """--qeq-file without RESP (repeat.py:2288-2294, 2522-2535) restrains the fit; as the
+    diagonal restraint (s, t) = (hardness, chi / hardness) the oracle matches repeat.py."""
+    import copy
+    from conftest import load_qeq
+    from pyrepeat_gb300 import qeq as Q
+    z, qd, _, qtot = load_qeq()
+    cube, _ = load_golden(name)
+    for f in (1, 0):
+        c = copy.copy(cube)
+        c.resp = Q.restraint_table(cube.atom_index, qd)
+        c.total_charge = qtot
+        c.kmax = cube.kmax if f else 0
+        q = oracle_mod.OracleFit(c).fit()
+        assert np.abs(q - z[f"q_qeqr{f}_{name}"]).max() <= 1e-10
+
+
 def test_reference_binary_agrees_on_plain_fit(oracle_mod):
     """repeat_cpu_omp prints 6 decimals; it fits the same plain problem."""
     cube, g = load_golden("water24")
