@@ -147,6 +147,10 @@ def make_workload(name: str, n_cubes: int, seed0: int, ctx):
         return [synth.make_mof(seed0, ctx=ctx)], "mof: cubic 25.8 Bohr, 128^3 grid, 424 atoms, KMAX 12 (K=3779)"
     if name == "water":
         return [synth.make_water(seed0, ctx=ctx)], "water: cubic 18 Bohr, 72^3 grid, 9 atoms, K=754"
+    if name == "tric":
+        return [synth.make_tric(seed0, ctx=ctx)], (
+            "tric: triclinic 40 x 42 x 45 Bohr (85/95/100 deg), 200 x 210 x 225 grid (9.45 M points), "
+            "2000 atoms C/H/N/O, 150 symmetry groups, RESP on C/N/O, KMAX 7 (K=754), Rc 20")
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -355,7 +359,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "mof", "water", "serve", "qeq"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "mof", "water", "tric", "serve", "qeq"])
     ap.add_argument("--qeq-atoms", type=int, default=2000)
     ap.add_argument("--serve-requests", type=int, default=600)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate, requests/s")
@@ -450,20 +454,36 @@ def main():
     # plain FP64 GPU fit of a subset: speed and the accuracy of the mixed path against it
     nf = min(args.fp64_cubes, n)
     sel = list(range(nf))
-    step(_lib.PREC_FP64, sel[:1])
-    torch.cuda.synchronize()
-    tf = time.perf_counter()
-    q64, _, _ = step(_lib.PREC_FP64, sel)
-    torch.cuda.synchronize()
-    fp64_s = time.perf_counter() - tf
-    fp64_value = nf / fp64_s
-    mixed_sub = [q_mixed[i] for i in sel]
-    dq = max(float(np.abs(a - b).max()) for a, b in zip(mixed_sub, q64))
-    mixed_sub_value = None
-    tm = time.perf_counter()
-    step(_lib.PREC_MIXED, sel)
-    torch.cuda.synchronize()
-    mixed_sub_value = nf / (time.perf_counter() - tm)
+    fp64_value = dq = mixed_sub_value = None
+    if nf > 0:
+        step(_lib.PREC_FP64, sel[:1])
+        torch.cuda.synchronize()
+        tf = time.perf_counter()
+        q64, _, _ = step(_lib.PREC_FP64, sel)
+        torch.cuda.synchronize()
+        fp64_s = time.perf_counter() - tf
+        fp64_value = nf / fp64_s
+        mixed_sub = [q_mixed[i] for i in sel]
+        dq = max(float(np.abs(a - b).max()) for a, b in zip(mixed_sub, q64))
+        tm = time.perf_counter()
+        step(_lib.PREC_MIXED, sel)
+        torch.cuda.synchronize()
+        mixed_sub_value = nf / (time.perf_counter() - tm)
+
+    # relative RMS of the fitted ESP over the kept points, both centred (SURVEY's RRMS:
+    # sqrt(sum (V_fit - V)^2 / sum V^2)), from rp_potential at the mixed charges
+    rrms = []
+    for i in range(min(8, n)):
+        c = cubes[i]
+        kept, Vc, _, _ = ctx.filter(c.n_grid, c.axis_vector, c.atom_pos, c.atom_index, c.V_dev, c.vdw_factor,
+                                    c.vdw_max)
+        ew = ctx.ewald(c.n_grid, c.axis_vector, c.cutoff, c.kmax)
+        try:
+            vfit = ctx.potential(ew, c.atom_pos, q_mixed[i], kept)
+        finally:
+            ew.close()
+        d = (vfit - vfit.mean()) - (Vc - Vc.mean())
+        rrms.append(float(torch.sqrt((d * d).sum() / (Vc * Vc).sum())))
 
     # single-fit latency (each cube alone through the batch entry point)
     lat = []
@@ -562,7 +582,9 @@ def main():
                    "generation_s": round(gen_s, 1)},
         "p50_ms": p50, "p99_ms": p99, "latency": "single-fit, each cube alone through rp_fit_batch",
         "fp64": {"fits_per_s": fp64_value, "cubes": nf, "mixed_fits_per_s_same_cubes": mixed_sub_value,
-                 "speedup": mixed_sub_value / fp64_value, "max_dq_mixed_vs_fp64_e": dq},
+                 "speedup": (mixed_sub_value / fp64_value) if nf else None, "max_dq_mixed_vs_fp64_e": dq},
+        "rrms": {"median": float(np.median(rrms)), "max": float(np.max(rrms)), "cubes": len(rrms),
+                 "definition": "sqrt(sum (V_fit - V)^2 / sum V^2) over kept points, both centred"},
         "e2e": {"value": e2e_value, "unit": "fits/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": roof,

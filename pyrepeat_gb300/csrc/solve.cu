@@ -18,9 +18,11 @@
 // with FP64 residuals until the backward error |b - A x| <= n eps64 |A| |x| (the
 // classic mixed-precision iterative refinement; FP64 runs at a small fraction of
 // the FP32 rate on this part).  If the FP32 factorisation meets a zero pivot or the
-// refinement does not reach that bound in kRefineMax steps (cond(A) near 1/eps32),
-// the system is factored again in FP64 with one step of FP64 refinement.  Either
-// way the refined residual and the pivot range are reported.
+// refinement stalls (a step that does not halve the residual, or kRefineMax steps:
+// cond(A) near 1/eps32), the system is factored again in FP64 with one step of FP64
+// refinement.  Either way the refined residual and the pivot range are reported.
+// Systems of kLUWideMin or more unknowns are factored across the whole GPU instead
+// of by their CTA (lu_wide_factor), in FP32 and, when that stalls, in FP64.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -50,7 +52,8 @@ struct SolveDesc {
     int *perm;            // n+1 pivot rows
     double *q;            // N out
     double *info;         // 4 out: residual inf-norm, min|piv|, max|piv|, singular flag
-    double *pre;          // null, or {failed, min|piv|, max|piv|} of a wide factorisation already in As
+    double *pre;          // null, or {flag, min|piv|, max|piv|} of a wide factorisation already in As
+    int wide64;           // As holds wide FP64 factors: skip the FP32 stage and the in-CTA FP64 LU
 };
 
 namespace {
@@ -433,7 +436,13 @@ __device__ void lu_apply_f32(const float *__restrict__ LU, const int *__restrict
         __syncthreads();
     }
 }
-constexpr int kRefineMax = 30;
+constexpr int kRefineMax = 30;  // and stop early once a step no longer halves the residual
+// systems factored across the GPU (FP32 first, FP64 when the FP32 refinement does not
+// converge): n1 in [kLUWideMin, kLUWideMax], FP64 up to kLUWide64Max; the bounds are the
+// panel rows that fit shared memory at 4 columns
+constexpr int kLUWideMin = 768;
+constexpr int kLUWideMax = (int)((225 * 1024) / (sizeof(float) * 5));
+constexpr int kLUWide64Max = (int)((225 * 1024) / (sizeof(double) * 5));
 
 // r = bs - A0 x in FP64: a warp per row, lanes along the row, fixed-order shuffle sum
 __device__ void residual(const SolveDesc &d, int n1) {
@@ -463,7 +472,7 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
     bool done = false;
 
     // ---- FP32 LU + FP64-residual refinement
-    {
+    if (!d.wide64) {
         float *L = reinterpret_cast<float *>(d.As);  // the first half of the FP64 work matrix
         if (!d.pre)
             for (long long t = threadIdx.x; t < (long long)n1 * n1; t += kLU) L[t] = (float)d.A0[t];
@@ -492,6 +501,7 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
                 an = fmax(an, s);
             }
             an = block_max(an, sv);
+            double rprev = 1e308;
             for (int it = 0; it < kRefineMax && !done; ++it) {
                 double rm = 0.0;
                 for (int t = threadIdx.x; t < n1; t += kLU) rm = fmax(rm, fabs(d.r[t]));
@@ -515,14 +525,29 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
                 xn = block_max(xn, sv);
                 res = rn;
                 if (rn <= (double)n1 * 1.1102230246251565e-16 * an * xn) done = true;
+                // stalled (cond(A) near 1/eps32 or beyond): no use refining further, FP64 takes over
+                else if (it >= 2 && rn > 0.5 * rprev) break;
+                rprev = rn;
             }
         }
         __syncthreads();
     }
 
+    // A wide system whose FP32 factors did not converge is factored again in FP64 across the
+    // GPU by the host, which then relaunches it with wide64 set; nothing is written here.
+    if (!done && d.pre && !d.wide64 && n1 <= kLUWide64Max) {
+        if (threadIdx.x == 0) d.pre[0] = 2.0;
+        return;
+    }
+
     // ---- fallback: FP64 LU with one step of FP64 refinement
     if (!done) {
         double *A = d.As;
+        if (d.wide64) {  // factored across the GPU (lu_wide_factor<double>)
+            pmin = d.pre[1];
+            pmax = d.pre[2];
+            singular = d.pre[0] != 0.0;
+        } else {
         for (long long t = threadIdx.x; t < (long long)n1 * n1; t += kLU) A[t] = d.A0[t];
         __syncthreads();
         pmin = 1e308;
@@ -565,6 +590,7 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
             }
             __syncthreads();
         }
+        }
         for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] = d.bs[t];
         lu_apply(A, d.perm, n1, d.x, d.r);
         for (int rr = threadIdx.x; rr < n1; rr += kLU) {
@@ -597,32 +623,34 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
 }
 
 // ---------------------------------------------------------------------------
-// Wide factorisation of one large system across the whole GPU (kLUWideMin <= n1 <=
-// kLUWideMax), before lu_solve_refine_kernel refines it.  One CTA factoring n1^3 / 3 FMAs
-// alone is SM-bound (20 ms at n1 = 1456, 0.75 s at 2001); here only the panels are serial.
-// The FP32 copy of A0 goes into As, then per panel of nb columns (32, or 16 / 8 / 4 when
-// the panel's rows do not fit shared memory at 32):
-//   lu_panel_kernel   one CTA: the panel in shared memory, factored with the same partial
-//                     pivoting as lu_factor_f32_blocked (perm[k] = pivot row, full-row
-//                     swaps), written back, its swaps applied to every other column;
+// Wide factorisation of one large system across the whole GPU, before lu_solve_refine_kernel
+// refines it.  One CTA factoring n1^3 / 3 FMAs alone is SM-bound (20 ms at n1 = 1456 in FP32,
+// and FP64 runs at 1/64 of the FP32 rate); here only the panels are serial.  A0 is copied into
+// As (FP32 for the first attempt, FP64 when that does not converge), then per panel of nb
+// columns (32, or 16 / 8 / 4 when the panel's rows do not fit shared memory at 32):
+//   lu_panel_kernel   one CTA: the panel in shared memory, factored with the partial pivoting
+//                     of the one-CTA factorisations (perm[k] = pivot row, full-row swaps; in
+//                     FP64 a pivot below 1e-300 is replaced and flagged, as there), written
+//                     back, its swaps applied to every other column;
 //   lu_trsm_kernel    U12 = L11^-1 A12, a thread per column over many CTAs;
-//   cuBLAS SGEMM      A22 -= L21 U12 (FP32, plain GEMM).
-// A zero or non-finite pivot sets pre[0]; the later panels then return at once and the
-// refinement kernel goes to its FP64 factorisation.
-constexpr int kLUWideMin = 768;
+//   cuBLAS GEMM       A22 -= L21 U12 (SGEMM or DGEMM, plain GEMM).
+// pre = {flag, min|pivot|, max|pivot|}.  FP32: flag 1 = zero or non-finite pivot (the later
+// panels return at once), set to 2 by lu_solve_refine_kernel when the refinement does not
+// converge.  FP64: flag 1 = a pivot was replaced (singular).
 constexpr size_t kPanelSmem = 225 * 1024;
-constexpr int kLUWideMax = (int)(kPanelSmem / (sizeof(float) * 5));  // panel rows at nb = 4
 
+template <typename T>
 int wide_panel_nb(int m) {
     for (int nb = 32; nb >= 4; nb /= 2)
-        if (sizeof(float) * (size_t)m * (nb + 1) <= kPanelSmem) return nb;
+        if (sizeof(T) * (size_t)m * (nb + 1) <= kPanelSmem) return nb;
     return 0;
 }
 
-__global__ void lu_to_f32_kernel(const double *__restrict__ A0, float *__restrict__ L, long long n,
-                                 double *__restrict__ pre) {
+template <typename T>
+__global__ void lu_copy_kernel(const double *__restrict__ A0, T *__restrict__ L, long long n,
+                               double *__restrict__ pre) {
     const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    for (long long t = t0; t < n; t += (long long)gridDim.x * blockDim.x) L[t] = (float)A0[t];
+    for (long long t = t0; t < n; t += (long long)gridDim.x * blockDim.x) L[t] = (T)A0[t];
     if (t0 == 0) {
         pre[0] = 0.0;
         pre[1] = 1e308;
@@ -630,49 +658,65 @@ __global__ void lu_to_f32_kernel(const double *__restrict__ A0, float *__restric
     }
 }
 
-__global__ void __launch_bounds__(kLU) lu_panel_kernel(float *__restrict__ A, int *__restrict__ perm, int n1,
-                                                       int k0, int NB, double *__restrict__ pre) {
-    if (pre[0] != 0.0) return;  // an earlier panel met a zero pivot
-    extern __shared__ float P[];  // [m][NB + 1] panel rows k0..n1-1
-    __shared__ float svf[kLU / 32];
+template <typename T>
+__global__ void __launch_bounds__(kLU) lu_panel_kernel(T *__restrict__ A, int *__restrict__ perm, int n1, int k0,
+                                                       int NB, double *__restrict__ pre) {
+    constexpr bool f32 = sizeof(T) == 4;
+    if (f32 && pre[0] != 0.0) return;  // an earlier panel met a zero pivot
+    extern __shared__ __align__(16) unsigned char panel_raw[];
+    T *P = reinterpret_cast<T *>(panel_raw);  // [m][NB + 1] panel rows k0..n1-1
+    __shared__ double svd[kLU / 32];
     __shared__ int si[kLU / 32];
     __shared__ int piv_i;
+    __shared__ double piv_v;
     const int m = n1 - k0, nb = min(NB, m), ld = NB + 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int t = threadIdx.x; t < m * NB; t += kLU) {
         const int r = t / NB, c = t - r * NB;
-        P[r * ld + c] = c < nb ? A[(size_t)(k0 + r) * n1 + k0 + c] : 0.f;
+        P[r * ld + c] = c < nb ? A[(size_t)(k0 + r) * n1 + k0 + c] : T(0);
     }
     __syncthreads();
-    float fmin_p = 3.0e38f, fmax_p = 0.f;
+    double pmin_l = 1e308, pmax_l = 0.0;
+    bool sing = false;
     for (int j = 0; j < nb; ++j) {
-        float best = -1.0f;
+        T best = T(-1);
         int bi = 0x7fffffff;
         for (int r = j + threadIdx.x; r < m; r += kLU) {
-            const float v = fabsf(P[r * ld + j]);
+            const T v = fabs(P[r * ld + j]);
             if (v > best || (v == best && r < bi)) { best = v; bi = r; }
         }
-        block_argmax_f(best, bi, svf, si, &piv_i);
+        if constexpr (f32)
+            block_argmax_f(best, bi, reinterpret_cast<float *>(svd), si, &piv_i);
+        else
+            block_argmax(best, bi, svd, si, &piv_v, &piv_i);
         const int p = piv_i;
         if (threadIdx.x == 0) perm[k0 + j] = k0 + p;
         if (p != j && threadIdx.x < NB) {
-            const float t = P[j * ld + threadIdx.x];
+            const T t = P[j * ld + threadIdx.x];
             P[j * ld + threadIdx.x] = P[p * ld + threadIdx.x];
             P[p * ld + threadIdx.x] = t;
         }
         __syncthreads();
-        const float pv = P[j * ld + j];
-        const float apv = fabsf(pv);
-        if (!(apv > 0.f) || !isfinite(pv)) {  // uniform: every thread read the same pivot
-            if (threadIdx.x == 0) pre[0] = 1.0;
-            return;
+        T pv = P[j * ld + j];
+        const T apv = fabs(pv);
+        if constexpr (f32) {
+            if (!(apv > 0.f) || !isfinite(pv)) {  // uniform: every thread read the same pivot
+                if (threadIdx.x == 0) pre[0] = 1.0;
+                return;
+            }
+        } else {
+            if (!(apv > 1e-300)) {  // exactly singular: a tiny pivot, flagged (as the one-CTA FP64 LU)
+                sing = true;
+                pv = pv < 0 ? T(-1e-300) : T(1e-300);
+                if (threadIdx.x == 0) P[j * ld + j] = pv;
+            }
         }
-        fmin_p = fminf(fmin_p, apv);
-        fmax_p = fmaxf(fmax_p, apv);
-        const float inv = 1.0f / pv;
+        pmin_l = fmin(pmin_l, (double)apv);
+        pmax_l = fmax(pmax_l, (double)apv);
+        const T inv = T(1) / pv;
         for (int r = j + 1 + warp; r < m; r += kLU / 32) {
-            float *row = P + r * ld;
-            const float l = row[j] * inv;
+            T *row = P + r * ld;
+            const T l = row[j] * inv;
             if (lane > j && lane < nb) row[lane] -= l * P[j * ld + lane];
             __syncwarp();
             if (lane == 0) row[j] = l;
@@ -688,34 +732,35 @@ __global__ void __launch_bounds__(kLU) lu_panel_kernel(float *__restrict__ A, in
         for (int j = 0; j < nb; ++j) {
             const int p = perm[k0 + j];
             if (p != k0 + j) {
-                const float t = A[(size_t)(k0 + j) * n1 + c];
+                const T t = A[(size_t)(k0 + j) * n1 + c];
                 A[(size_t)(k0 + j) * n1 + c] = A[(size_t)p * n1 + c];
                 A[(size_t)p * n1 + c] = t;
             }
         }
     }
     if (threadIdx.x == 0) {
-        pre[1] = fmin(pre[1], (double)fmin_p);
-        pre[2] = fmax(pre[2], (double)fmax_p);
+        pre[1] = fmin(pre[1], pmin_l);
+        pre[2] = fmax(pre[2], pmax_l);
+        if (!f32 && sing) pre[0] = 1.0;
     }
 }
 
-template <int NB>
-__global__ void __launch_bounds__(256) lu_trsm_kernel(float *__restrict__ A, int n1, int k0,
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) lu_trsm_kernel(T *__restrict__ A, int n1, int k0,
                                                       const double *__restrict__ pre) {
-    if (pre[0] != 0.0) return;
-    __shared__ float Ls[NB][NB + 1];
+    if (sizeof(T) == 4 && pre[0] != 0.0) return;
+    __shared__ T Ls[NB][NB + 1];
     const int nb = min(NB, n1 - k0), c1 = k0 + nb;
     for (int t = threadIdx.x; t < NB * NB; t += blockDim.x) {
         const int i = t / NB, j = t - i * NB;
-        Ls[i][j] = (i < nb && j < nb) ? A[(size_t)(k0 + i) * n1 + k0 + j] : 0.f;
+        Ls[i][j] = (i < nb && j < nb) ? A[(size_t)(k0 + i) * n1 + k0 + j] : T(0);
     }
     __syncthreads();
     const int c = c1 + blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n1) return;
-    float u[NB];
+    T u[NB];
 #pragma unroll
-    for (int j = 0; j < NB; ++j) u[j] = j < nb ? A[(size_t)(k0 + j) * n1 + c] : 0.f;
+    for (int j = 0; j < NB; ++j) u[j] = j < nb ? A[(size_t)(k0 + j) * n1 + c] : T(0);
 #pragma unroll
     for (int j = 0; j < NB; ++j)
 #pragma unroll
@@ -743,35 +788,45 @@ void lu_smem_optin() {
     }
 }
 
+inline cublasStatus_t gemm_nn(cublasHandle_t h, int m, int n, int k, const float *alpha, const float *A, int lda,
+                              const float *B, int ldb, const float *beta, float *C, int ldc) {
+    return cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+inline cublasStatus_t gemm_nn(cublasHandle_t h, int m, int n, int k, const double *alpha, const double *A, int lda,
+                              const double *B, int ldb, const double *beta, double *C, int ldc) {
+    return cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+template <typename T>
 void lu_wide_factor(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t stream) {
     static bool optin = false;
     if (!optin) {
-        RP_CUDA(cudaFuncSetAttribute(lu_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmem));
+        RP_CUDA(cudaFuncSetAttribute(lu_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmem));
         optin = true;
     }
-    float *L = reinterpret_cast<float *>(d.As);
+    T *L = reinterpret_cast<T *>(d.As);
     const long long nn = (long long)n1 * n1;
-    lu_to_f32_kernel<<<(int)std::min<long long>(ceil_div(nn, 256), 4096), 256, 0, stream>>>(d.A0, L, nn, d.pre);
+    lu_copy_kernel<T><<<(int)std::min<long long>(ceil_div(nn, 256), 4096), 256, 0, stream>>>(d.A0, L, nn, d.pre);
     RP_LAUNCH_CHECK();
     cublasHandle_t h = ctx->blas();
     RP_CUBLAS(cublasSetStream(h, stream));
-    const float minus_one = -1.0f, one = 1.0f;
+    const T minus_one = T(-1), one = T(1);
     for (int k0 = 0; k0 < n1;) {
-        const int m = n1 - k0, NB = wide_panel_nb(m), nb = std::min(NB, m), c1 = k0 + nb;
-        lu_panel_kernel<<<1, kLU, sizeof(float) * (size_t)m * (NB + 1), stream>>>(L, d.perm, n1, k0, NB, d.pre);
+        const int m = n1 - k0, NB = wide_panel_nb<T>(m), nb = std::min(NB, m), c1 = k0 + nb;
+        lu_panel_kernel<T><<<1, kLU, sizeof(T) * (size_t)m * (NB + 1), stream>>>(L, d.perm, n1, k0, NB, d.pre);
         RP_LAUNCH_CHECK();
         if (c1 < n1) {
             const int w = n1 - c1, grid = (int)ceil_div(w, 256);
             switch (NB) {
-                case 32: lu_trsm_kernel<32><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
-                case 16: lu_trsm_kernel<16><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
-                case 8: lu_trsm_kernel<8><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
-                default: lu_trsm_kernel<4><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
+                case 32: lu_trsm_kernel<T, 32><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
+                case 16: lu_trsm_kernel<T, 16><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
+                case 8: lu_trsm_kernel<T, 8><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
+                default: lu_trsm_kernel<T, 4><<<grid, 256, 0, stream>>>(L, n1, k0, d.pre); break;
             }
             RP_LAUNCH_CHECK();
             // row-major A22 (w x w) -= L21 (w x nb) U12 (nb x w), as column-major C^T -= U12^T L21^T
-            RP_CUBLAS(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, w, w, nb, &minus_one, L + (size_t)k0 * n1 + c1, n1,
-                                  L + (size_t)c1 * n1 + k0, n1, &one, L + (size_t)c1 * n1 + c1, n1));
+            RP_CUBLAS(gemm_nn(h, w, w, nb, &minus_one, L + (size_t)k0 * n1 + c1, n1, L + (size_t)c1 * n1 + k0, n1,
+                              &one, L + (size_t)c1 * n1 + c1, n1));
         }
         k0 = c1;
     }
@@ -986,12 +1041,14 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
         }
     }
     // large systems: factored across the GPU first (lu_solve_refine_kernel then refines them)
+    bool any_wide = false;
     for (int j = 0; j < nj; ++j) {
         const int n1 = plans[j].n + 1;
         if (n1 < kLUWideMin || n1 > kLUWideMax) continue;
         descs[j].pre = d_pre + 3 * (size_t)j;
         StageTimer tt(ctx, "solve_lu_wide", stream);
-        lu_wide_factor(ctx, descs[j], n1, stream);
+        lu_wide_factor<float>(ctx, descs[j], n1, stream);
+        any_wide = true;
     }
     std::memcpy(stage + st_off[5], descs.data(), st_bytes[5]);
     RP_CUDA(cudaMemcpyAsync(d_desc, stage + st_off[5], st_bytes[5], cudaMemcpyHostToDevice, stream));
@@ -1002,6 +1059,34 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
         lu_smem_optin();
         lu_solve_refine_kernel<<<nj, kLU, solve_smem_bytes(n1max), stream>>>(d_desc);
         RP_LAUNCH_CHECK();
+    }
+    if (any_wide) {
+        // wide systems whose FP32 refinement did not converge (flag 2): FP64 factors across the
+        // GPU, then the refinement kernel again on those systems alone (the host waits here)
+        double *h_pre = static_cast<double *>(ctx->host_buf("s_preh" + tag, sizeof(double) * 3 * nj));
+        RP_CUDA(cudaMemcpyAsync(h_pre, d_pre, sizeof(double) * 3 * nj, cudaMemcpyDeviceToHost, stream));
+        RP_CUDA(cudaStreamSynchronize(stream));
+        std::vector<SolveDesc> redo;
+        int n1max = 1;
+        for (int j = 0; j < nj; ++j) {
+            if (!descs[j].pre || h_pre[3 * j] != 2.0) continue;
+            SolveDesc d = descs[j];
+            d.wide64 = 1;
+            const int n1 = plans[j].n + 1;
+            StageTimer tt(ctx, "solve_lu_wide64", stream);
+            lu_wide_factor<double>(ctx, d, n1, stream);
+            redo.push_back(d);
+            n1max = std::max(n1max, n1);
+        }
+        if (!redo.empty()) {
+            SolveDesc *d_redo = ctx->buf_t<SolveDesc>("s_desc64" + tag, redo.size());
+            SolveDesc *h_redo = static_cast<SolveDesc *>(ctx->host_buf("s_stage64" + tag, sizeof(SolveDesc) * redo.size()));
+            std::memcpy(h_redo, redo.data(), sizeof(SolveDesc) * redo.size());
+            RP_CUDA(cudaMemcpyAsync(d_redo, h_redo, sizeof(SolveDesc) * redo.size(), cudaMemcpyHostToDevice, stream));
+            StageTimer tt(ctx, "solve_lu", stream);
+            lu_solve_refine_kernel<<<(int)redo.size(), kLU, solve_smem_bytes(n1max), stream>>>(d_redo);
+            RP_LAUNCH_CHECK();
+        }
     }
     double *h_info = static_cast<double *>(ctx->host_buf("s_info" + tag, sizeof(double) * 4 * nj));
     RP_CUDA(cudaMemcpyAsync(h_info, d_info, sizeof(double) * 4 * nj, cudaMemcpyDeviceToHost, stream));

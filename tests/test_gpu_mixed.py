@@ -201,6 +201,30 @@ def test_potential_matches_phi_q(gpu_ctx, oracle_mod):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("N", [300, 900])
+def test_bordered_solve_ill_conditioned_takes_fp64(gpu_ctx, N):
+    """cond(A) = 1e10, beyond what FP32 factors can refine: the FP64 factorisation takes over
+    (one CTA below 768 unknowns, across the GPU above) and the charges match an FP64 LU of
+    the same bordered system to cond x eps."""
+    import scipy.linalg as sl
+    import torch
+    rng = np.random.default_rng(7 + N)
+    Q, _ = np.linalg.qr(rng.normal(size=(N, N)))
+    A = (Q * np.logspace(0, -10, N)) @ Q.T
+    A = 0.5 * (A + A.T)
+    b = rng.normal(size=N)
+    q, info = gpu_ctx.solve(torch.from_numpy(A).cuda(), torch.from_numpy(b).cuda(), np.full(N, 6), qtot=0.5)
+    K = np.zeros((N + 1, N + 1))
+    K[:N, :N] = A
+    K[:N, N] = K[N, :N] = 1.0
+    rhs = np.concatenate([b, [0.5]])
+    ref = sl.solve(K, rhs)[:N]
+    q = q.cpu().numpy()
+    assert np.abs(q - ref).max() <= 1e-4 * np.abs(ref).max()
+    assert abs(q.sum() - 0.5) <= 1e-8 * np.abs(q).max()
+    assert info["pivot_min"] > 0.0
+
+
 @pytest.mark.parametrize("N", [61, 700, 767, 1000, 1600, 1800, 3500])
 def test_bordered_solve_large_systems(gpu_ctx, N):
     """The bordered solve on systems of many panels against an FP64 LU of the same
