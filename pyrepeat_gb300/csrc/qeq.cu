@@ -7,9 +7,9 @@
 //          real-space sum)
 //        + sum_k w_k cos(k . (r_i - r_j))                       (repeat.py:2628-2632)
 // The k-sum factorises into per-atom tables, sum_k w_k (cos_i cos_j + sin_i sin_j): one FP64
-// DGEMM of [w cos | w sin] (N x 2K) against [cos | sin] (N x 2K).  The pair kernel adds the
-// real-space sum of pair (i < j) to the DGEMM term and writes J_ij and J_ji, so J is exactly
-// symmetric like the reference's.  With KMAX 0 (the non-periodic fit) alpha is 0, the shift
+// product of [w cos | w sin] (N x 2K) with [cos | sin] (N x 2K), one triangle of it (cuBLAS
+// DSYRKX).  The pair kernel adds the real-space sum of pair (i < j) to that term and writes
+// J_ij and J_ji, so J is exactly symmetric like the reference's.  With KMAX 0 (the non-periodic fit) alpha is 0, the shift
 // list is the zero shift alone and there are no k-vectors, so J_ij = 1/r_ij (repeat.py:
 // 2588-2595).
 //
@@ -56,10 +56,15 @@ __global__ void qeq_pairs_kernel(const double *__restrict__ atoms, int N, const 
     }
     const double dx = atoms[3 * i] - atoms[3 * j], dy = atoms[3 * i + 1] - atoms[3 * j + 1],
                  dz = atoms[3 * i + 2] - atoms[3 * j + 2];
+    // images with sqrt(alpha) r > 7 are skipped: each would add erfc(7)/r < 1e-24, against
+    // entries of order 1e-2..1 whose ulp is above 1e-18 (KMAX 0: alpha 0, nothing is skipped)
+    const double r_far2 = sa > 0.0 ? (7.0 / sa) * (7.0 / sa) : 1e300;
     double acc = 0.0;
     for (int s = 0; s < S; ++s) {
         const double x = dx + shifts[3 * s], y = dy + shifts[3 * s + 1], z = dz + shifts[3 * s + 2];
-        const double r = sqrt(x * x + y * y + z * z);
+        const double r2 = x * x + y * y + z * z;
+        if (r2 > r_far2) continue;
+        const double r = sqrt(r2);
         if (r > 1e-10) acc += erfc(sa * r) / r;
     }
     const double v = R ? acc + R[t] : acc;
@@ -99,12 +104,14 @@ void qeq_run(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const 
             qeq_tables_kernel<<<ceil_div(n, 256), 256, 0, stream>>>(ew->d_kvec, ew->d_kcoef, K, d_atoms, N, W, U);
             RP_LAUNCH_CHECK();
         }
-        // row-major W, U (N x 2K) are column-major 2K x N; R[i*N + j] = sum_k W[i][k] U[j][k]
+        // row-major W, U (N x 2K) are column-major 2K x N.  W U^T is symmetric, so only one
+        // triangle is formed (DSYRKX, half the flops of a GEMM): column-major (j, i), j >= i,
+        // i.e. R[i*N + j] = sum_k W[j][k] U[i][k] for the pairs i <= j the pair kernel reads
         StageTimer tt(ctx, "qeq_recip_dgemm", stream);
         cublasHandle_t h = ctx->blas();
         RP_CUBLAS(cublasSetStream(h, stream));
         const double one = 1.0, zero = 0.0;
-        RP_CUBLAS(cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, N, N, K2, &one, U, K2, W, K2, &zero, dR, N));
+        RP_CUBLAS(cublasDsyrkx(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, N, K2, &one, W, K2, U, K2, &zero, dR, N));
         R = dR;
     }
     {

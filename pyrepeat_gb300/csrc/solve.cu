@@ -120,45 +120,66 @@ __device__ void block_argmax(double v, int idx, double *sv, int *si, double *out
     __syncthreads();
 }
 
-__device__ void lu_apply(const double *__restrict__ LU, const int *__restrict__ perm, int n1, double *__restrict__ y,
-                         double *__restrict__ tmp) {
-    // solve (P L U) z = y in place; y is overwritten with z.  Serial substitution
-    // over rows, inner dot products spread over the block.
-    __shared__ double red[kLU / 32];
+__device__ void lu_apply(const double *__restrict__ LU, const int *__restrict__ perm, int n1, double *__restrict__ y) {
+    // solve (P L U) z = y in place (y global), blocked by 32 columns: the diagonal block is
+    // solved by one warp with shuffles, then every warp updates the remaining rows with the
+    // block's 32 values (a warp per row, coalesced).  Three barriers per 32 columns.
+    __shared__ double blk[32][33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __syncthreads();
     if (threadIdx.x == 0)
         for (int k = 0; k < n1; ++k) {
-            int p = perm[k];
-            if (p != k) { double t = y[k]; y[k] = y[p]; y[p] = t; }
+            const int p = perm[k];
+            if (p != k) { const double t = y[k]; y[k] = y[p]; y[p] = t; }
         }
     __syncthreads();
-    for (int i = 0; i < n1; ++i) {  // forward: L unit lower
-        double s = 0.0;
-        for (int c = threadIdx.x; c < i; c += kLU) s += LU[(size_t)i * n1 + c] * y[c];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    for (int c0 = 0; c0 < n1; c0 += 32) {  // forward: L, unit diagonal
+        const int bs = min(32, n1 - c0);
+        for (int t = threadIdx.x; t < bs * 32; t += kLU) {
+            const int r = t >> 5, c = t & 31;
+            blk[r][c] = c < bs ? LU[(size_t)(c0 + r) * n1 + c0 + c] : 0.0;
+        }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int w = 0; w < kLU / 32; ++w) t += red[w];
-            y[i] -= t;
+        if (warp == 0) {
+            double yv = lane < bs ? y[c0 + lane] : 0.0;
+            for (int c = 0; c < bs - 1; ++c) {
+                const double yc = __shfl_sync(0xffffffffu, yv, c);
+                if (lane > c && lane < bs) yv -= blk[lane][c] * yc;
+            }
+            if (lane < bs) y[c0 + lane] = yv;
+        }
+        __syncthreads();
+        for (int r = c0 + bs + warp; r < n1; r += kLU / 32) {
+            double t = lane < bs ? LU[(size_t)r * n1 + c0 + lane] * y[c0 + lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) y[r] -= t;
         }
         __syncthreads();
     }
-    for (int i = n1 - 1; i >= 0; --i) {  // backward: U
-        double s = 0.0;
-        for (int c = i + 1 + threadIdx.x; c < n1; c += kLU) s += LU[(size_t)i * n1 + c] * y[c];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    for (int c1 = n1; c1 > 0; c1 -= 32) {  // backward: U
+        const int c0 = max(0, c1 - 32), bs = c1 - c0;
+        for (int t = threadIdx.x; t < bs * 32; t += kLU) {
+            const int r = t >> 5, c = t & 31;
+            blk[r][c] = c < bs ? LU[(size_t)(c0 + r) * n1 + c0 + c] : 0.0;
+        }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int w = 0; w < kLU / 32; ++w) t += red[w];
-            y[i] = (y[i] - t) / LU[(size_t)i * n1 + i];
+        if (warp == 0) {
+            double yv = lane < bs ? y[c0 + lane] : 0.0;
+            for (int c = bs - 1; c >= 0; --c) {
+                if (lane == c) yv = yv / blk[c][c];
+                const double xc = __shfl_sync(0xffffffffu, yv, c);
+                if (lane < c) yv -= blk[lane][c] * xc;
+            }
+            if (lane < bs) y[c0 + lane] = yv;
+        }
+        __syncthreads();
+        for (int r = warp; r < c0; r += kLU / 32) {
+            double t = lane < bs ? LU[(size_t)r * n1 + c0 + lane] * y[c0 + lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) y[r] -= t;
         }
         __syncthreads();
     }
-    (void)tmp;
 }
 
 // max over the block (every thread gets the result)
@@ -592,14 +613,14 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
         }
         }
         for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] = d.bs[t];
-        lu_apply(A, d.perm, n1, d.x, d.r);
+        lu_apply(A, d.perm, n1, d.x);
         for (int rr = threadIdx.x; rr < n1; rr += kLU) {
             double s = d.bs[rr];
             const double *row = d.A0 + (size_t)rr * n1;
             for (int c = 0; c < n1; ++c) s -= row[c] * d.x[c];
             d.r[rr] = s;
         }
-        lu_apply(A, d.perm, n1, d.r, nullptr);
+        lu_apply(A, d.perm, n1, d.r);
         for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] += d.r[t];
         __syncthreads();
         double rmax = 0.0;
