@@ -319,13 +319,15 @@ __device__ bool lu_factor_f32_blocked(float *A, int *perm, int n1, float *smem, 
             fmin_p = fminf(fmin_p, apv);
             fmax_p = fmaxf(fmax_p, apv);
             const float inv = 1.0f / pv;
-            // scale the column and update the panel's remaining columns: a warp per row
-            for (int r = j + 1 + warp; r < m; r += kLU / 32) {
+            // scale the column and update the panel's remaining columns: a thread per row, so a
+            // warp instruction covers 32 rows of one column with every lane busy (stride 33:
+            // no bank conflicts; the pivot row is a broadcast)
+            const float *pj = P + j * (kLUNB + 1);
+            for (int r = j + 1 + threadIdx.x; r < m; r += kLU) {
                 float *row = P + r * (kLUNB + 1);
-                const float l = row[j] * inv;  // every lane computes it; lane j+... writes it below
-                if (lane > j && lane < nb) row[lane] -= l * P[j * (kLUNB + 1) + lane];
-                __syncwarp();
-                if (lane == 0) row[j] = l;
+                const float l = row[j] * inv;
+                row[j] = l;
+                for (int c = j + 1; c < nb; ++c) row[c] -= l * pj[c];
             }
             __syncthreads();
         }
@@ -735,12 +737,14 @@ __global__ void __launch_bounds__(kLU) lu_panel_kernel(T *__restrict__ A, int *_
         pmin_l = fmin(pmin_l, (double)apv);
         pmax_l = fmax(pmax_l, (double)apv);
         const T inv = T(1) / pv;
-        for (int r = j + 1 + warp; r < m; r += kLU / 32) {
+        // a thread per row: one warp instruction covers 32 rows of a column, every lane busy
+        // (the FP64 pipe takes the same time for a warp instruction with one lane or 32)
+        const T *pj = P + j * ld;
+        for (int r = j + 1 + threadIdx.x; r < m; r += kLU) {
             T *row = P + r * ld;
             const T l = row[j] * inv;
-            if (lane > j && lane < nb) row[lane] -= l * P[j * ld + lane];
-            __syncwarp();
-            if (lane == 0) row[j] = l;
+            row[j] = l;
+            for (int c = j + 1; c < nb; ++c) row[c] -= l * pj[c];
         }
         __syncthreads();
     }
