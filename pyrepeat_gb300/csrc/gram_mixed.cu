@@ -110,13 +110,13 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
     const int tile = blockIdx.x % g.ntri, split = blockIdx.x / g.ntri;
     int ti, tj;
     gram_tile_decode(tile, g.ntj, ti, tj);
-    const bool inblock = (tj < 2 * ti + 2);       // columns inside the row block: B rows are part of A's tile
-    const uint32_t b_in_a = (uint32_t)(tj - 2 * ti) * (kGN * 128);  // byte offset of B's rows inside A's tile
     const int a_row0 = ti * kBM, b_row0 = tj * kGN;
     const int kb0 = split * g.kb_per_split, kb1 = min(kb0 + g.kb_per_split, g.kb_total);
     const int nkb = kb1 - kb0;  // >= 1
     const int nflush = (nkb + g.flush - 1) / g.flush;
-    const uint32_t stage_tx = inblock ? kGSlices * kTileBytes : kGSlices * (kTileBytes + kBTileBytes);
+    // B is loaded for every tile (also where its rows lie inside A's tile): the four B slices
+    // then sit back to back, and slices (0, 1) and (2, 3) form 128-row operands
+    const uint32_t stage_tx = kGSlices * (kTileBytes + kBTileBytes);
     const CUtensorMap *ta[kGSlices] = {&tm0, &tm1, &tm2, &tm3};
     const CUtensorMap *tb[kGSlices] = {&tb0, &tb1, &tb2, &tb3};
 
@@ -146,8 +146,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
 #pragma unroll
             for (int q = 0; q < kGSlices; ++q) {
                 tc::tma_load_2d(st + q * kTileBytes, ta[q], x, a_row0, &full[s]);
-                if (!inblock)
-                    tc::tma_load_2d(st + kGSlices * kTileBytes + q * kBTileBytes, tb[q], x, b_row0, &full[s]);
+                tc::tma_load_2d(st + kGSlices * kTileBytes + q * kBTileBytes, tb[q], x, b_row0, &full[s]);
             }
             issued = kb + 1;
         }
@@ -156,6 +155,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
                 tc::mbar_wait(&full[kb % kGramStages], (kb / kGramStages) & 1, nullptr);
     } else if (warp == 1 && lane == 0) {
         const uint32_t idesc = tc::idesc_f16_f32(kBM, kGN);
+        const uint32_t idesc2 = tc::idesc_f16_f32(kBM, 2 * kGN);  // two B slices, two adjacent groups
         uint32_t d[kGroups];  // group accumulators, 64 TMEM columns each
 #pragma unroll
         for (int q = 0; q < kGroups; ++q) d[q] = tmem + (uint32_t)(q * kGN);
@@ -176,22 +176,34 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
 #pragma unroll
                 for (int q = 0; q < kGSlices; ++q) {
                     x[q] = tc::sdesc_k_sw128(st + q * kTileBytes);
-                    y[q] = inblock ? tc::sdesc_k_sw128(st + q * kTileBytes + b_in_a)
-                                   : tc::sdesc_k_sw128(st + kGSlices * kTileBytes + q * kBTileBytes);
+                    y[q] = tc::sdesc_k_sw128(st + kGSlices * kTileBytes + q * kBTileBytes);
                 }
 #pragma unroll
                 for (int kk = 0; kk < kBK / 16; ++kk) {
                     const uint64_t o = (uint64_t)(kk * 2);
-                    bool started[kGroups] = {false, false, false, false, false, false, false};
+                    if (kb == kbf0 && kk == 0) {
+                        // the first products of a flush start each group's sum: one MMA per
+                        // (slice a, slice b), the first into a group overwriting it
+                        bool started[kGroups] = {false, false, false, false, false, false, false};
 #pragma unroll
-                    for (int a = 0; a < kGSlices; ++a)
+                        for (int a = 0; a < kGSlices; ++a)
 #pragma unroll
-                        for (int b = 0; b < kGSlices; ++b) {
-                            const int grp = a + b;
-                            const uint32_t acc = (kb == kbf0 && kk == 0 && !started[grp]) ? 0u : 1u;
-                            started[grp] = true;
-                            tc::umma_f16(d[grp], x[a] + o, y[b] + o, idesc, acc);
+                            for (int b = 0; b < kGSlices; ++b) {
+                                const int grp = a + b;
+                                const uint32_t acc = started[grp] ? 1u : 0u;
+                                started[grp] = true;
+                                tc::umma_f16(d[grp], x[a] + o, y[b] + o, idesc, acc);
+                            }
+                    } else {
+                        // then N = 128: slice a against slices (b, b+1) back to back writes the
+                        // products of weights a+b and a+b+1 into the adjacent groups at d[a+b]
+                        // (the same products, in the same order per group, as the pairs above)
+#pragma unroll
+                        for (int a = 0; a < kGSlices; ++a) {
+                            tc::umma_f16(d[a], x[a] + o, y[0] + o, idesc2, 1u);
+                            tc::umma_f16(d[a + 2], x[a] + o, y[2] + o, idesc2, 1u);
                         }
+                    }
                 }
                 tc::umma_commit(&empty[s]);
             }
