@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
     const int nkb = kb1 - kb0;  // >= 1
     const int nflush = (nkb + g.flush - 1) / g.flush;
     // B is loaded for every tile (also where its rows lie inside A's tile): the four B slices
-    // then sit back to back, and slices (0, 1) and (2, 3) form 128-row operands
+    // then sit back to back and form one 256-row operand
     const uint32_t stage_tx = kGSlices * (kTileBytes + kBTileBytes);
     const CUtensorMap *ta[kGSlices] = {&tm0, &tm1, &tm2, &tm3};
     const CUtensorMap *tb[kGSlices] = {&tb0, &tb1, &tb2, &tb3};
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
                 tc::mbar_wait(&full[kb % kGramStages], (kb / kGramStages) & 1, nullptr);
     } else if (warp == 1 && lane == 0) {
         const uint32_t idesc = tc::idesc_f16_f32(kBM, kGN);
-        const uint32_t idesc2 = tc::idesc_f16_f32(kBM, 2 * kGN);  // two B slices, two adjacent groups
+        const uint32_t idesc4 = tc::idesc_f16_f32(kBM, 4 * kGN);  // all four B slices, four adjacent groups
         uint32_t d[kGroups];  // group accumulators, 64 TMEM columns each
 #pragma unroll
         for (int q = 0; q < kGroups; ++q) d[q] = tmem + (uint32_t)(q * kGN);
@@ -195,14 +195,12 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
                                 tc::umma_f16(d[grp], x[a] + o, y[b] + o, idesc, acc);
                             }
                     } else {
-                        // then N = 128: slice a against slices (b, b+1) back to back writes the
-                        // products of weights a+b and a+b+1 into the adjacent groups at d[a+b]
-                        // (the same products, in the same order per group, as the pairs above)
+                        // then N = 256: slice a against the four B slices back to back (a 256-row
+                        // operand) writes the products of weights a .. a+3 into the four adjacent
+                        // groups from d[a] (the same products, in the same order per group, as the
+                        // pairs above), reading A once instead of four times
 #pragma unroll
-                        for (int a = 0; a < kGSlices; ++a) {
-                            tc::umma_f16(d[a], x[a] + o, y[0] + o, idesc2, 1u);
-                            tc::umma_f16(d[a + 2], x[a] + o, y[2] + o, idesc2, 1u);
-                        }
+                        for (int a = 0; a < kGSlices; ++a) tc::umma_f16(d[a], x[a] + o, y[0] + o, idesc4, 1u);
                     }
                 }
                 tc::umma_commit(&empty[s]);
