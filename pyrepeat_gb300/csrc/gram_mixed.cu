@@ -53,16 +53,21 @@ constexpr int kTileBytes = kBM * kBK * 2;  // 16 KB per operand tile
 // column's typical value sits orders of magnitude below its maximum).  All 16
 // slice products are kept (the low digits carry full-size rounding noise
 // whatever |x| is), grouped by weight g = s+u into seven TMEM accumulators of a
-// 128 x 64 tile.  Every product is an integer <= 2^12, one MMA adds <= 2^16, a
-// group gets at most 16 MMAs per stage, so kGramFlush = 8 stages stay below 2^24
-// and the FP32 sums are exact.  At each flush the epilogue folds the groups into
+// 128 x 64 tile.  Per point, a group's products sum to at most 12288 in magnitude
+// (weight 3: x0 x3 + x3 x0 <= 2 * 32 * 64, x1 x2 + x2 x1 <= 2 * 64 * 64; weight 4:
+// three products <= 64 * 64; the others less), so a stage of 64 points adds at most
+// 786,432 = 3 * 2^18 to a group and kGramFlush = 16 stages stay below 2^24 (12.6 M):
+// the FP32 sums are exact, and a CTA of kGramSplit = 16 stages drains them once, at its
+// end.  (A row whose |x| passed 1/2 is clamped, counted and its cube refitted from the
+// staged Phi, whose own scale keeps |x| < 1/2.)  At each flush the epilogue folds the groups into
 // one int64 per element (sum_g D_g 2^(7(6-g))), so the Gram carries no rounding
 // bias (its diagonal is the most sensitive quantity of the fit).
 constexpr int kGN = 64;          // Gram tile columns
 constexpr int kGSlices = 4;
 constexpr int kGroups = 2 * kGSlices - 1;
 constexpr int kGramStages = 2;
-constexpr int kGramFlush = 8;
+constexpr int kGramFlush = 16;
+constexpr int kGramSplit = 16;   // stages per CTA: 1024 points, the int64 fold's headroom (2^52 per point)
 constexpr int kGramEpiWarps = 8;
 constexpr int kGramThreads = 64 + 32 * kGramEpiWarps;  // 320
 constexpr int kBTileBytes = kGN * kBK * 2;             // 8 KB
@@ -1107,7 +1112,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     const int nt = (int)ceil_div(Np, kBM), ntj = (int)ceil_div(Np, kGN);
     int ntri = 0;  // 128 x 64 Gram tiles with columns at or right of the row block, up to the last row
     for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
-    const int kb_split = 2 * kGramFlush;  // 1024 points per CTA (int64 headroom), exact sums flushed every 512
+    const int kb_split = kGramSplit;  // 1024 points per CTA (int64 headroom), exact sums drained once
 
     for (long long m0 = 0; m0 < M; m0 += chunk) {
         const long long rows = std::min<long long>(chunk, M - m0);

@@ -150,8 +150,22 @@ def test_exact_gram_kernel_is_exact(gpu_ctx):
     x64 = [a[:Np].astype(np.float64) for a in X]
     ref = sum((x64[a] @ x64[b].T) * 2.0 ** (7 * (6 - a - b)) for a in range(4) for b in range(4)) * 2.0 ** -54
     I = torch.zeros((Np, Np), dtype=torch.float64, device="cuda")
-    gpu_ctx.check(L.rp_debug_gram_slices(gpu_ctx.ptr, *[x.data_ptr() for x in xd], Np, cols, 8, 16, I.data_ptr()))
-    assert np.abs(I.cpu().numpy() - ref).max() <= 1e-15 * np.abs(ref).max()
+    for flush in (8, 16):   # 16: the product's flush period, exact at the digits' largest magnitudes
+        I.zero_()
+        gpu_ctx.check(L.rp_debug_gram_slices(gpu_ctx.ptr, *[x.data_ptr() for x in xd], Np, cols, flush, 16,
+                                             I.data_ptr()))
+        assert np.abs(I.cpu().numpy() - ref).max() <= 1e-15 * np.abs(ref).max()
+    # every digit at its largest magnitude, one sign: the largest exact sums a flush can hold
+    Xm = [np.zeros((256, cols), np.float16) for _ in range(4)]
+    Xm[0][:Np] = 32
+    for q in (1, 2, 3):
+        Xm[q][:Np] = 64
+    xm = [torch.from_numpy(a).cuda() for a in Xm]
+    xm64 = [a[:Np].astype(np.float64) for a in Xm]
+    refm = sum((xm64[a] @ xm64[b].T) * 2.0 ** (7 * (6 - a - b)) for a in range(4) for b in range(4)) * 2.0 ** -54
+    I.zero_()
+    gpu_ctx.check(L.rp_debug_gram_slices(gpu_ctx.ptr, *[x.data_ptr() for x in xm], Np, cols, 16, 16, I.data_ptr()))
+    assert np.abs(I.cpu().numpy() - refm).max() <= 1e-15 * np.abs(refm).max()
 
 
 def test_batch_equals_single_fits(gpu_ctx):
