@@ -183,6 +183,14 @@ def reference_arm(args, world, rank):
     """Reference CPU implementation of the path on the host cores (rank 0 only)."""
     if rank != 0:
         return
+    if args.workload == "serve":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving mode (repeat.py is a "
+                                                               "one-shot program); its per-fit CPU time is the batch arm"}),
+              flush=True)
+        return
+    if args.workload == "qeq":
+        reference_qeq_arm(args, world)
+        return
     import torch
     threads = max(1, os.cpu_count() or 1)
     ctx = None
@@ -213,6 +221,44 @@ def reference_arm(args, world, rank):
 
 
 # ----------------------------------------------------------------------------- GPU arm
+
+def reference_qeq_arm(args, world):
+    """QEq charges on the host: the oracle's NumPy restatement of compute_qeq_charges
+    (Coulomb matrix by pairs, the reference's difference-form solve), one core; each step
+    times the matrix rows of a bounded block of atoms and the full solve, extrapolated in
+    pairs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from pyrepeat_gb300 import qeq as Q
+    N = args.qeq_atoms
+    atoms, Z, ngrid, axis = qeq_cell(N, 7)
+    chi, js, _, _ = Q.charge_parameters(Z)
+    box = np.eye(3) * (axis[0, 0] * ngrid[0])
+    rows = min(N, 64)
+    times = []
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        O.qeq_matrix(atoms[:rows], box, 20.0, 7, js[:rows])
+        t_rows = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.qeq_charges(np.eye(N) + 0.01, chi, 0.0)   # LU time does not depend on the values
+        t_solve = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(t_rows * (N * (N - 1) / 2) / (rows * (rows - 1) / 2) + t_solve)
+    per = statistics.mean(times)
+    line = {
+        "impl": "reference", "metric": "QEq charge sets/s (periodic Ewald Coulomb matrix + equalisation solve, "
+                                      "host in/out)",
+        "value": 1.0 / per, "unit": "charge sets/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": f"qeq: {N} atoms, Rc 20, KMAX 7"},
+        "cpu_baseline": {"value": 1.0 / per, "unit": "charge sets/s", "cores": 1, "kind": "port",
+                         "sample": f"Coulomb matrix rows of {rows} atoms per step, extrapolated to {N} atoms' pairs, "
+                                   f"plus the {N}-atom solve"},
+        "e2e": {"value": 1.0 / per, "unit": "charge sets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
 
 def serve_arm(args, world, rank, local):
     """Served fits (SURVEY's serve workload, scaled to a few seconds): Poisson arrivals
