@@ -27,6 +27,12 @@ def test_flags_match_the_reference():
     assert a.gpu == "0" and a.cutoff == 20.0 and a.vdw_max == 1000.0 and a.kmax == 7
 
 
+def test_root_command_is_the_same_program():
+    r = subprocess.run([sys.executable, "repeat_gb300.py", "--help"], cwd=ROOT, capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0 and "--fit-type" in r.stdout and "--qeq-file" in r.stdout
+
+
 def test_device_lists_refused():
     assert cli.parse_device(None) == 0 and cli.parse_device("3") == 3
     for spec in ("0,1", "all", "x"):
