@@ -12,6 +12,7 @@
 #include <deque>
 #include <exception>
 #include <functional>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <set>
@@ -303,6 +304,12 @@ struct rp_ewald {
 };
 
 namespace rp {
+
+// Raise a kernel's dynamic shared-memory limit to at least `bytes` on the current device.
+// The limit belongs to the device context, and the batch server's worker and a caller's
+// thread may launch the same kernel, so raised limits are recorded per (kernel, device)
+// under a lock.  Sizes within the 48 KB default need nothing.
+void smem_optin(const void *kernel, size_t bytes);
 
 // Ewald tables (ewald_tables.cu): host part, device image size, placement in a device block.
 // dst (optional, ewald_layout bytes): where the device image is written; else ew->image

@@ -748,15 +748,13 @@ void launch_phi(const int32_t *kept, long long m0, long long rows, const double 
     const size_t smem = phi_smem_bytes(n1c, scap);
     // the static shared memory (the statistics and row-sum tiles, ~1.3 KB) counts against
     // the same 48 KB default, so the opt-in is raised whenever the dynamic part could cross it
-    static size_t attr = 0;
-    if (smem > attr) {
-        RP_REQUIRE(smem <= 192 * 1024, "phi kernel: KMAX too large for shared memory");
+    RP_REQUIRE(smem <= 192 * 1024, "phi kernel: KMAX too large for shared memory");
+    {
         const size_t want = std::max<size_t>(smem, 96 * 1024);
-        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<7, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
-        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
-        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<7, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
-        RP_CUDA(cudaFuncSetAttribute(phi_chunk_kernel<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want));
-        attr = want;
+        smem_optin((const void *)phi_chunk_kernel<7, false>, want);
+        smem_optin((const void *)phi_chunk_kernel<0, false>, want);
+        smem_optin((const void *)phi_chunk_kernel<7, true>, want);
+        smem_optin((const void *)phi_chunk_kernel<0, true>, want);
     }
     AxisDF adf;
     for (int q = 0; q < 9; ++q) {
@@ -985,11 +983,7 @@ CUtensorMap make_map(const void *ptr, long long rows, long long cols, int box_ro
 }
 
 void launch_gram(const __half *const *X, int rows, long long cols, const GramArgs &g, int grid, cudaStream_t s) {
-    static bool attr = false;
-    if (!attr) {
-        RP_CUDA(cudaFuncSetAttribute(gram_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmem));
-        attr = true;
-    }
+    smem_optin((const void *)gram_exact_kernel, kGramSmem);
     CUtensorMap a[kGSlices], b[kGSlices];
     for (int q = 0; q < kGSlices; ++q) {
         a[q] = make_map(X[q], rows, cols, kBM);   // rows past `rows` read as zeros

@@ -234,11 +234,7 @@ void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const do
     const int nb = (n1c + kN1B - 1) / kN1B;
     const size_t smem_a = sizeof(float2) * (size_t)nw * nz;
     RP_REQUIRE(smem_a <= (200u << 10), "recip_rows: grid too large along z for KMAX");
-    static size_t attr_a = 0;
-    if (smem_a > (48u << 10) && smem_a > attr_a) {
-        RP_CUDA(cudaFuncSetAttribute(recip_stage_a_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a));
-        attr_a = smem_a;
-    }
+    smem_optin((const void *)recip_stage_a_kernel, smem_a);
     recip_stage_a_kernel<<<ceil_div((long long)nz * nw * ncols * nb, 128), 128, smem_a, stream>>>(W, ew->d_ezf, ncols,
                                                                                                   P, nz, F);
     RP_LAUNCH_CHECK();
@@ -248,11 +244,7 @@ void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const do
     const size_t nyp = (size_t)(ny + kJB - 1) / kJB * kJB;
     const size_t smem = sizeof(float2) * (((size_t)nw * ab * n1c + 1) & ~(size_t)1) + sizeof(float2) * (size_t)nw * nyp;
     RP_REQUIRE(smem <= (200u << 10), "recip_rows: KMAX too large");
-    static size_t attr = 0;
-    if (smem > (48u << 10) && smem > attr) {
-        RP_CUDA(cudaFuncSetAttribute(recip_stage_b_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = smem;
-    }
+    smem_optin((const void *)recip_stage_b_kernel, smem);
     recip_stage_b_kernel<<<dim3(ceil_div(ncols, ab), nz), 128, smem, stream>>>(F, ew->d_eyf, ncols, P, ny, ab, E);
     RP_LAUNCH_CHECK();
 }

@@ -14,6 +14,20 @@ void qeq_run(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const 
 
 namespace rp {
 std::atomic<long long> g_launches{0};
+
+void smem_optin(const void *kernel, size_t bytes) {
+    if (bytes <= (48u << 10)) return;
+    int dev = 0;
+    RP_CUDA(cudaGetDevice(&dev));
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, size_t> raised;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &have = raised[{kernel, dev}];
+    if (bytes > have) {
+        RP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        have = bytes;
+    }
+}
 void status_clear(rp_ctx *ctx, cudaStream_t s) { RP_CUDA(cudaMemsetAsync(ctx->d_status, 0, 2 * sizeof(int), s)); }
 void status_check(rp_ctx *ctx, cudaStream_t s) {
     int st[2] = {0, 0};

@@ -805,12 +805,8 @@ size_t solve_smem_bytes(int n1) {
 
 // the launch's shared memory opt-in, raised once to the largest the kernel can ask for
 void lu_smem_optin() {
-    static bool done = false;
-    if (!done) {
-        const size_t most = std::max(solve_smem_bytes(kLUBlockedMax), solve_smem_bytes(1));
-        RP_CUDA(cudaFuncSetAttribute(lu_solve_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most));
-        done = true;
-    }
+    smem_optin((const void *)lu_solve_refine_kernel,
+               std::max(solve_smem_bytes(kLUBlockedMax), solve_smem_bytes(1)));
 }
 
 inline cublasStatus_t gemm_nn(cublasHandle_t h, int m, int n, int k, const float *alpha, const float *A, int lda,
@@ -824,11 +820,7 @@ inline cublasStatus_t gemm_nn(cublasHandle_t h, int m, int n, int k, const doubl
 
 template <typename T>
 void lu_wide_factor(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t stream) {
-    static bool optin = false;
-    if (!optin) {
-        RP_CUDA(cudaFuncSetAttribute(lu_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmem));
-        optin = true;
-    }
+    smem_optin((const void *)lu_panel_kernel<T>, kPanelSmem);
     T *L = reinterpret_cast<T *>(d.As);
     const long long nn = (long long)n1 * n1;
     lu_copy_kernel<T><<<(int)std::min<long long>(ceil_div(nn, 256), 4096), 256, 0, stream>>>(d.A0, L, nn, d.pre);
