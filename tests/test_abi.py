@@ -24,6 +24,21 @@ def test_header_declares_entry_points():
         assert s in syms
 
 
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_header_compiles_as_c_and_cpp(lang, tmp_path):
+    """The boundary header is plain C (a cgo / ctypes / JNI binding includes it as C)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / ("t.c" if lang == "c" else "t.cpp")
+    src.write_text('#include "repeat_gb300.h"\nint main(void) { return rp_version() > 0 ? 0 : 1; }\n')
+    r = subprocess.run([cc, "-std=c99" if lang == "c" else "-std=c++17", "-Wall", "-Werror", "-fsyntax-only",
+                        "-I", os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_library_exports_every_declared_symbol():
     from pyrepeat_gb300 import _lib
     from pyrepeat_gb300.build import build_cuda
