@@ -39,6 +39,38 @@ def test_header_compiles_as_c_and_cpp(lang, tmp_path):
     assert r.returncode == 0, r.stderr
 
 
+def test_c_program_links_and_calls_without_gpu(tmp_path):
+    """A C program links against the library and calls it through the header: the version,
+    and a context on a machine without a usable device fails with a status, not an abort."""
+    import shutil
+    import subprocess
+    from pyrepeat_gb300 import _lib
+    from pyrepeat_gb300.build import build_cuda
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no host compiler")
+    build_cuda()
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    src = tmp_path / "t.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "repeat_gb300.h"\n'
+        'int main(void) {\n'
+        '  rp_ctx *ctx = 0; char e[256] = {0};\n'
+        '  int v = rp_version();\n'
+        '  int rc = rp_ctx_create(99, 0, &ctx);\n'
+        '  printf("%d %d %d\\n", v, rc, ctx == 0);\n'
+        '  return v > 0 && rc != 0 && ctx == 0 ? 0 : 1;\n'
+        '}\n')
+    exe = tmp_path / "t"
+    r = subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                        "-L", libdir, "-lrepeat_gb300", "-Wl,-rpath," + libdir], capture_output=True, text=True)
+    if r.returncode != 0 and "cannot find -lrepeat_gb300" in r.stderr:
+        pytest.skip("library named differently on this platform")
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stdout + run.stderr
+
+
 def test_library_exports_every_declared_symbol():
     from pyrepeat_gb300 import _lib
     from pyrepeat_gb300.build import build_cuda
