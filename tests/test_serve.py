@@ -74,6 +74,39 @@ def test_wait_bound_closes_a_partial_batch():
     assert ctx.batches == [[3], [4]]
 
 
+class _FailingCtx:
+    def batch_submit(self, cubes, precision, V_dev):
+        raise RuntimeError("device lost")
+
+
+class _FailingResultCtx(_FakeCtx):
+    def batch_submit(self, cubes, precision, V_dev):
+        super().batch_submit(cubes, precision, V_dev)
+
+        class P:
+            def result(self_inner):
+                raise RuntimeError("batch failed")
+        return P()
+
+
+def test_errors_reach_every_request_of_the_batch():
+    for ctx, msg in ((_FailingCtx(), "device lost"), (_FailingResultCtx(), "batch failed")):
+        srv = serve.FitServer(ctx, max_batch=4, max_wait_s=0.05)
+        futs = [srv.submit(_FakeCube(3)) for _ in range(3)]
+        srv.close()
+        for f in futs:
+            with pytest.raises(RuntimeError, match=msg):
+                f.result(timeout=5)
+        assert srv.latencies == []
+
+
+def test_closed_server_refuses_requests():
+    srv = serve.FitServer(_FakeCtx())
+    srv.close()
+    with pytest.raises(RuntimeError):
+        srv.submit(_FakeCube(3))
+
+
 @pytest.mark.gpu
 def test_served_fits_equal_fits_alone(gpu_ctx):
     """Alone vs mixed: each request's charges equal the cube fitted alone, bitwise."""
