@@ -261,7 +261,7 @@ def reference_qeq_arm(args, world):
 
 
 def serve_arm(args, world, rank, local):
-    """Served fits (SURVEY's serve workload, scaled to a few seconds): Poisson arrivals
+    """Served fits (Poisson arrivals at 50/s, scaled to a few seconds of requests): arrivals
     drawn from the batch distribution with a share of large cubes (800-1500 atoms, 160^3)
     go through a FitServer (micro-batches, HBM admission, asynchronous batches);
     reported: completed fits/s and p50/p99 latency from arrival to charges on the host.
@@ -516,8 +516,8 @@ def main():
         torch.cuda.synchronize()
         mixed_sub_value = nf / (time.perf_counter() - tm)
 
-    # relative RMS of the fitted ESP over the kept points, both centred (SURVEY's RRMS:
-    # sqrt(sum (V_fit - V)^2 / sum V^2)), from rp_potential at the mixed charges
+    # relative RMS of the fitted ESP over the kept points, both centred
+    # (sqrt(sum (V_fit - V)^2 / sum V^2)), from rp_potential at the mixed charges
     rrms = []
     for i in range(min(8, n)):
         c = cubes[i]
