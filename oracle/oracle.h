@@ -2,7 +2,7 @@
  *
  * A plain-C restatement of the reference algorithm (pyREPEAT repeat.py and
  * repeat_cpu_omp.cpp), used by tests/, __graft_entry__.smoke() and the CPU
- * baseline leg of bench.py as the checker.  Nothing in the product links or
+ * baseline leg of bench.py, to check results.  Nothing in the product links or
  * calls it.  All arithmetic is IEEE FP64 with floating-point contraction
  * disabled (-ffp-contract=off), so the filter mask is reproducible bit for bit.
  *

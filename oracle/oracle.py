@@ -1,7 +1,7 @@
 """Python driver of the C oracle — TEST INFRASTRUCTURE ONLY.
 
 Used by tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` as the checker; the product never imports it.  It strings the C
+``bench.py``, to check results; the product never imports it.  It strings the C
 restatement together in the order of ``repeat.py``'s ``ChargeCalculator``:
 filter (repeat.py:1922-2113) -> pruned shifts (1708-1731) -> streamed normal
 equations (2184-2276) -> symmetry/RESP/bordered solve (2278-2313); and QEq

@@ -56,7 +56,7 @@ def parse_device(spec: str | None) -> int:
         return 0
     s = str(spec).strip().lower()
     if s == "all" or "," in s:
-        raise SystemExit(f"Error: --gpu {spec}: this build fits on one GPU; give one device id (e.g. --gpu 0)")
+        raise SystemExit(f"Error: --gpu {spec}: one fit runs on one GPU; give one device id (e.g. --gpu 0)")
     try:
         return int(s)
     except ValueError:

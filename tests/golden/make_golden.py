@@ -1,5 +1,5 @@
 """Generate the golden fixtures from the reference itself (run in the container
-that holds the reference tree; the GPU machine only reads the results).
+that holds the reference tree; other machines only read the results).
 
 For every case the seeded generator (pyrepeat_gb300.synth) builds a cube, the
 cube is written as a Gaussian cube file, and:
