@@ -564,7 +564,7 @@ def main():
         flops_gram += 2.0 * m * (na + 1) ** 2                   # X X^T over the atoms + the ESP row
         b_phi += 8.0 * m * na + 4.0 * m                         # Phi written once, kept index read
         b_slice += 8.0 * m * na + 8.0 * m * (na + 1) + 8.0 * m  # Phi read, 4 FP16 digits written, Vc read
-        b_rows += 16.0 * ny * nz * na * c.kmax                  # E rows written (double-float complex)
+        b_rows += 8.0 * ny * nz * na * c.kmax                   # E rows written (FP32 complex, KMAX per row)
         b_filter += 9.0 * nx * ny * nz + 12.0 * m            # V read + mask, kept index + Vc written
     algo = {"gram_exact": ("tensor", flops_gram / 1e12, "TFLOP/s", bf16_peak, "bf16 dense burst"),
             "phi": ("hbm", b_phi / 1e9, "GB/s", hbm_peak, "copy"),

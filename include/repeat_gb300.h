@@ -153,8 +153,12 @@ int rp_qeq(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const do
  * library, so N is limited to 512 atoms (RP_E_ARG beyond that).  No counterpart in
  * the reference.  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) with that device current; make it before any stream
- * capture.  Every call shares the array: calls that overlap on the GPU race, so
- * serialise them.  Returns RP_E_SINGULAR for a singular bordered system. */
+ * capture.  Under lazy module loading that first call may also load the library's
+ * device code and, with it, the array.  The address is kept for the life of the
+ * process, so a cudaDeviceReset voids this entry point.  A call is synchronous: it
+ * returns once its solve on `stream` has finished.  Every call shares the array:
+ * calls that overlap on the GPU race, so serialise them.  Returns RP_E_SINGULAR
+ * for a singular bordered system. */
 int rp_solve_noalloc(const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
                      const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,
                      double *info, rp_stream_t stream);

@@ -35,10 +35,16 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_reference(reference_dir: str = "/root/reference") -> str | None:
+def build_reference(reference_dir: str | None = None) -> str | None:
     """Compile repeat_cpu_omp.cpp from the reference tree into _ref/ (only where
-    the reference sources exist)."""
-    if not os.path.exists(os.path.join(reference_dir, "repeat_cpu_omp.cpp")):
+    the reference sources exist).  The tree is `reference_dir`, else the
+    PYREPEAT_REFERENCE environment variable, else the Makefile's REFERENCE."""
+    reference_dir = reference_dir or os.environ.get("PYREPEAT_REFERENCE")
+    if reference_dir is None:
+        p = subprocess.run(["make", "-s", "-C", HERE, "--no-print-directory", "print-reference"],
+                           stdout=subprocess.PIPE, text=True)
+        reference_dir = p.stdout.strip()
+    if not reference_dir or not os.path.exists(os.path.join(reference_dir, "repeat_cpu_omp.cpp")):
         return REF_BIN if os.path.exists(REF_BIN) else None
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE={reference_dir}"], check=True)
     return REF_BIN

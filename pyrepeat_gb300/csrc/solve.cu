@@ -1147,8 +1147,12 @@ void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int
 // keeps until the process exits.  Host code only sees a host-side stand-in for
 // that symbol; the device address comes from cudaGetSymbolAddress, looked up once
 // per device with that device current, on the first call made on it (make that
-// first call before any stream capture).  All calls share the array and it keeps
-// the last call's contents (every region is fully rewritten before it is read),
+// first call before any stream capture).  With lazy module loading that first call
+// may also be what loads the library's device code, and the array with it.  The
+// address is kept for the life of the process: a cudaDeviceReset voids it, so do
+// not call this entry point after resetting the device.  A call is synchronous: it
+// returns once the solve on `stream` has finished.  All calls share the array and it
+// keeps the last call's contents (every region is fully rewritten before it is read),
 // so calls that overlap on the GPU race: serialise them on one stream.
 namespace rp {
 namespace {

@@ -16,16 +16,23 @@ Bytecode writes are disabled so nothing is written under the reference tree.
 import os
 import sys
 
-REFERENCE_DIR = os.environ.get("PYREPEAT_REFERENCE", "/root/reference")
+
+def _reference_dir() -> str:
+    """The reference tree: the PYREPEAT_REFERENCE environment variable (required)."""
+    d = os.environ.get("PYREPEAT_REFERENCE")
+    if not d or not os.path.exists(os.path.join(d, "repeat.py")):
+        raise RuntimeError("set PYREPEAT_REFERENCE to the directory that holds the reference's repeat.py")
+    return d
 
 
 def load_reference():
     sys.dont_write_bytecode = True
+    reference_dir = _reference_dir()
     import scipy.spatial
     import scipy.special
     scipy.spatial.erfc = scipy.special.erfc
-    if REFERENCE_DIR not in sys.path:
-        sys.path.insert(0, REFERENCE_DIR)
+    if reference_dir not in sys.path:
+        sys.path.insert(0, reference_dir)
     import repeat as R  # noqa: E402
     R._NOGIL_ENABLED = True
     workers = max(1, os.cpu_count() or 1)
