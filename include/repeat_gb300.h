@@ -38,8 +38,27 @@ extern "C" {
 #define RP_E_UNSUPPORTED -7
 
 /* Arithmetic of the Phi -> normal-equations stage. */
-#define RP_PREC_FP64 0  /* plain FP64: FP64 tables, FP64 real space, FP64 Gram */
-#define RP_PREC_MIXED 1 /* tensor cores: split BF16 k-contraction, FP32 erfc, split FP16 Gram */
+#define RP_PREC_FP64 0  /* plain FP64: FP64 tables, FP64 real space, FP64 Gram (cuBLAS DGEMM) */
+#define RP_PREC_MIXED 1 /* FP32 real space from double-float coordinates, separable FP32 reciprocal
+                           sum, exact fixed-point Gram on the tensor cores (tcgen05), FP64 solve.
+                           In rp_fit / rp_fit_batch a cube whose kappa / (n+1) exceeds the ctx's
+                           limit (rp_set_kappa_limit) is refitted in FP64 and flagged
+                           RP_FIT_ESCALATED. */
+
+/* Words per system of rp_solve's and rp_solve_noalloc's info: [0] residual inf-norm after
+ * refinement, [1] min |pivot|, [2] max |pivot|, [3] kappa = ||A||_1 ||K^-1||_1 with A the
+ * folded normal matrix (RESP included) and K the bordered matrix (||K^-1||_1 by Hager's
+ * estimator on the factors that solved it).  A relative perturbation e of A moves the
+ * charges by at most about e * kappa * max|q|. */
+#define RP_SOLVE_INFO_WORDS 4
+/* Words per cube of rp_fit_batch's (and rp_batch_submit's) info_out: [0] residual,
+ * [1] min |pivot|, [2] max |pivot|, [3] singular flag, [4] kappa (as above), [5] the
+ * factorisation that solved it (0 FP32 LU in one CTA, 1 FP32 LU across the GPU, 2 FP64 LU in
+ * one CTA, 3 FP64 LU across the GPU; FP32 factors are refined with FP64 residuals),
+ * [6] the precision that produced the charges (RP_PREC_*), [7] RP_FIT_* flags. */
+#define RP_FIT_INFO_WORDS 8
+#define RP_FIT_ESCALATED 1 /* mixed-precision cube refitted in FP64: kappa/(n+1) above the limit */
+#define RP_FIT_TWO_PASS 2  /* mixed-precision cube refitted in two passes after a fixed-point clamp */
 
 typedef void *rp_stream_t; /* a cudaStream_t */
 typedef struct rp_ctx rp_ctx;
@@ -51,7 +70,7 @@ typedef struct {
     double axis[9];
 } rp_grid;
 
-/* Library version, major*10000 + minor*100 + patch. */
+/* Library version, major*10000 + minor*100 + patch (2.0.0: the info words above). */
 int rp_version(void);
 
 /* Create a context on `device`.  hbm_budget: bytes of scratch the ctx may hold
@@ -115,8 +134,9 @@ int rp_gram(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const i
  *   A_dev, b_dev   inputs (not modified)
  *   group_ptr [n_groups+1], group_idx [group_ptr[n_groups]] (host, 0-based, first = base)
  *   resp_s, resp_t [N] (host, may be NULL)
- *   q_dev [N] f64 out;  info (host, may be NULL): [0] residual inf-norm after
- *   refinement, [1] min |pivot|, [2] max |pivot|. */
+ *   q_dev [N] f64 out;  info [RP_SOLVE_INFO_WORDS] (host, may be NULL).
+ *   No escalation happens here: a caller of rp_gram + rp_solve reads kappa and may run
+ *   rp_gram again with RP_PREC_FP64. */
 int rp_solve(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups,
              const int *group_ptr, const int *group_idx, const double *resp_s, const double *resp_t,
              double qtot, double *q_dev, double *info, rp_stream_t stream);
@@ -191,8 +211,8 @@ int rp_fit(rp_ctx *ctx, const rp_fit_desc *desc, double *q_out, int64_t *M_out, 
  *   descs[n]     as for rp_fit (each with its own precision)
  *   V_dev        NULL, or n device pointers (an entry may be NULL: use descs[i].V on the host)
  *   q_out        host, the charges of all cubes concatenated (sum of N_i doubles)
- *   M_out[n]     host kept counts (may be NULL); info_out[4n] host (may be NULL):
- *                per cube refined residual, min |pivot|, max |pivot|, singular flag */
+ *   M_out[n]     host kept counts (may be NULL); info_out[RP_FIT_INFO_WORDS * n] host
+ *                (may be NULL), per cube as described at RP_FIT_INFO_WORDS */
 int rp_fit_batch(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
                  int64_t *M_out, double *info_out, rp_stream_t stream);
 
@@ -211,6 +231,15 @@ int rp_batch_submit(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *
                     int64_t *M_out, double *info_out, long long *ticket);
 int rp_batch_poll(rp_ctx *ctx, long long ticket, int *done, int *status);
 int rp_batch_wait(rp_ctx *ctx, long long ticket, int *status);
+
+/* Limit on kappa / (n+1) (kappa as in RP_SOLVE_INFO_WORDS, n+1 the unknowns of the
+ * bordered system after symmetry folding) above which rp_fit / rp_fit_batch refit a
+ * mixed-precision cube in FP64; 0 = never refit.  On seeded cubes of 9 to 2000 atoms the
+ * mixed charges differed from FP64 by about 2e-11 kappa/(n+1) e, so the default, 2e5, keeps
+ * that near 4e-6 e; cubes beyond it (hundreds of densely packed atoms leaving few ESP
+ * points) are fitted in FP64.  No reference counterpart: repeat.py fits in the precision
+ * it is asked for. */
+int rp_set_kappa_limit(rp_ctx *ctx, double kappa_max);
 
 /* Profiling hooks (no reference counterpart).  With timing on, every stage
  * records CUDA events on the stream it runs on; rp_stage_times synchronises,

@@ -19,12 +19,17 @@ STATUS = {
 }
 PREC_FP64 = 0
 PREC_MIXED = 1
+SOLVE_INFO_WORDS = 4   # residual, min |pivot|, max |pivot|, kappa
+FIT_INFO_WORDS = 8     # residual, min |pivot|, max |pivot|, singular, kappa, path, precision, flags
+FIT_ESCALATED = 1      # flag: a mixed-precision cube refitted in FP64 (kappa / (n+1) above the limit)
+DEFAULT_KAPPA_LIMIT = 2e5
+FIT_TWO_PASS = 2       # flag: a mixed-precision cube refitted in two passes after a clamp
 
 # every symbol include/repeat_gb300.h declares
 EXPORTS = ["rp_version", "rp_ctx_create", "rp_ctx_destroy", "rp_last_error", "rp_filter", "rp_ewald_setup",
            "rp_ewald_destroy", "rp_ewald_info", "rp_gram", "rp_solve", "rp_potential", "rp_fit",
            "rp_fit_batch", "rp_set_timing", "rp_stage_times", "rp_launch_count", "rp_solve_noalloc",
-           "rp_batch_submit", "rp_batch_poll", "rp_batch_wait", "rp_qeq"]
+           "rp_batch_submit", "rp_batch_poll", "rp_batch_wait", "rp_qeq", "rp_set_kappa_limit"]
 
 
 class RepeatError(RuntimeError):
@@ -107,6 +112,8 @@ def load(path: str | None = None):
     L.rp_batch_wait.argtypes = [P, ctypes.c_longlong, ctypes.POINTER(I)]
     L.rp_qeq.restype = I
     L.rp_qeq.argtypes = [P, P, P, I, P, P, D, P, P, P, P]
+    L.rp_set_kappa_limit.restype = I
+    L.rp_set_kappa_limit.argtypes = [P, D]
     _lib = L
     return L
 
@@ -121,6 +128,20 @@ def check(ctx_ptr, rc: int, what: str = ""):
     if rc == -4:
         raise SingularError(rc, msg)
     raise RepeatError(rc, msg)
+
+
+def fit_info(row) -> dict:
+    """One cube's FIT_INFO_WORDS record as a dict."""
+    return {"residual": float(row[0]), "pivot_min": float(row[1]), "pivot_max": float(row[2]),
+            "singular": bool(row[3]), "kappa": float(row[4]), "solve_path": int(row[5]),
+            "precision": "fp64" if int(row[6]) == PREC_FP64 else "mixed",
+            "escalated": bool(int(row[7]) & FIT_ESCALATED), "two_pass": bool(int(row[7]) & FIT_TWO_PASS)}
+
+
+def solve_info(info) -> dict:
+    """rp_solve's SOLVE_INFO_WORDS record as a dict."""
+    return {"residual": float(info[0]), "pivot_min": float(info[1]), "pivot_max": float(info[2]),
+            "kappa": float(info[3])}
 
 
 def launch_count() -> int:

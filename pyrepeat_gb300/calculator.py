@@ -135,7 +135,7 @@ class ChargeCalculator:
         q, M, info = self.ctx.fit_batch([self.to_cube()], prec)
         self.charges = np.asarray(q[0], dtype=np.float64)
         self.n_kept = int(M[0])
-        self.info = {"residual": float(info[0][0]), "pivot_min": float(info[0][1]), "pivot_max": float(info[0][2])}
+        self.info = _lib.fit_info(info[0])
         return self.charges
 
     def compute_stats(self, charges, need_v_coul=True) -> dict:

@@ -175,15 +175,45 @@ class HostPool {
 
 }  // namespace rp
 
+// Default limit on kappa / (n+1), kappa = ||A||_1 ||K^-1||_1 of the bordered system of n+1
+// unknowns, above which a mixed-precision fit is redone in FP64.  The mixed Gram's relative
+// error is ~1e-7, and on 30 seeded cubes of 9 to 2000 atoms the mixed charges moved from the
+// FP64 ones by about 2e-11 kappa/(n+1) e (kappa/(n+1) from 1e3 to 3e6, within 3x): the limit
+// keeps that below ~4e-6 e.  (Beyond ~1e8 the error saturates near 0.1-1 e.)
+constexpr double kDefaultKappaLimit = 2e5;
+
+namespace rp {
+// Batches of the asynchronous server in flight at once.  Each runs in a slot of the ctx with
+// its own scratch (names carry the slot), pinned staging, streams, status words, cuBLAS
+// handle and host object pools; slot 0 is also what rp_fit_batch and the staged calls use.
+constexpr int kBatchSlots = 3;
+constexpr int kSlotLanes = 10;  // streams per slot: 4 gram + 4 filter + 1 copy + the batch's own
+// A served batch whose largest cube has at least this many grid points x atoms runs on
+// streams of the default (lowest) priority, every other served batch on streams of the
+// device's greatest priority: the block scheduler then hands free SMs to a small request's
+// kernels before the pending blocks of a large cube's, so small requests are not held
+// behind large ones.
+constexpr double kLowPriorityWork = 1e9;
+}  // namespace rp
+
 struct rp_ctx {
     int device = 0;
     int sm_count = 0;
     size_t budget = 0;
     size_t used = 0;
     std::string last_error;
-    cublasHandle_t cublas = nullptr;
+    cublasHandle_t cublas[rp::kBatchSlots] = {};
     std::unordered_map<std::string, rp::Buffer> scratch;
-    int *d_status = nullptr;  // device status word for bounded waits / singular flags
+    int *d_status = nullptr;  // device status words (two per slot) for bounded waits / clamps
+    // The slot the calling code runs in.  Set by the one thread that uses the ctx at a time
+    // (the caller, or the batch server's worker while tickets are outstanding); scratch,
+    // staging, streams, status words and the cuBLAS handle below all follow it.
+    int cur_slot = 0;
+    int cur_prio = 0;  // streams of the current batch: 0 default priority, 1 the greatest
+    std::string slot_key(const std::string &name) const {
+        return cur_slot == 0 ? name : name + "@" + std::to_string(cur_slot);
+    }
+    int *status_words() const { return d_status + 2 * cur_slot; }
     // optional per-stage CUDA-event timing (rp_set_timing / rp_stage_times)
     bool timing = false;
     struct Mark {
@@ -192,8 +222,9 @@ struct rp_ctx {
     };
     std::vector<Mark> marks;
 
-    // Grow-only named scratch buffer owned by the ctx.
-    void *buf(const std::string &name, size_t bytes) {
+    // Grow-only named scratch buffer owned by the ctx (one per name and slot).
+    void *buf(const std::string &name_in, size_t bytes) {
+        const std::string name = slot_key(name_in);
         bytes = (bytes + 255) & ~size_t(255);
         if (bytes == 0) bytes = 256;
         auto &b = scratch[name];
@@ -226,11 +257,12 @@ struct rp_ctx {
     // small pageable ones); callers synchronise their stream before it is reused.
     std::unordered_map<std::string, rp::Buffer> host_scratch;
     double bound_scale = 1.0;  // factor on the single-pass Phi bounds (tests shrink it to force clamps)
+    long long chunk_cap = 0;   // cap on the staged mixed Gram's points per chunk (tests; 0 = none)
     std::unique_ptr<rp::HostPool> pool;  // host workers (created on first use)
     std::unique_ptr<rp::BatchServer> server;  // asynchronous batches (created on first submit)
-    // per-cube host objects of the batched fit, kept across batches for their capacity
-    std::vector<std::unique_ptr<rp_ewald>> ew_pool;
-    std::vector<std::unique_ptr<rp::FilterPlan>> plan_pool;
+    // per-cube host objects of the batched fit, kept across batches for their capacity (per slot)
+    std::vector<std::unique_ptr<rp_ewald>> ew_pool[rp::kBatchSlots];
+    std::vector<std::unique_ptr<rp::FilterPlan>> plan_pool[rp::kBatchSlots];
     void parallel(int n, const std::function<void(int)> &f) {
         if (!pool) {
             const int hw = std::max(1, (int)std::thread::hardware_concurrency());
@@ -239,7 +271,13 @@ struct rp_ctx {
         pool->run(n, f);
     }
     int last_fallbacks = 0;    // cubes of the last batch redone in two passes after a clamp
-    void *host_buf(const std::string &name, size_t bytes) {
+    int last_escalations = 0;  // mixed-precision cubes of the last batch refitted in FP64
+    // mixed-precision fits whose kappa / (n+1) (the solve's ||A||_1 ||K^-1||_1 over the
+    // bordered system's unknowns) exceeds this are refitted in plain FP64
+    // (rp_set_kappa_limit; 0 = never)
+    double kappa_limit = kDefaultKappaLimit;
+    void *host_buf(const std::string &name_in, size_t bytes) {
+        const std::string name = slot_key(name_in);
         bytes = std::max<size_t>(256, (bytes + 255) & ~size_t(255));
         auto &b = host_scratch[name];
         if (b.bytes >= bytes) return b.ptr;
@@ -254,14 +292,18 @@ struct rp_ctx {
         b.bytes = bytes;
         return b.ptr;
     }
-    cublasHandle_t blas();
+    cublasHandle_t blas();  // the current slot's handle
     // Worker streams for fits that run concurrently inside one batch (created on first use,
-    // non-blocking, destroyed with the ctx).
+    // non-blocking, destroyed with the ctx): lane i of the current slot.
     std::vector<cudaStream_t> lanes;
-    cudaStream_t lane(int i) {
+    cudaStream_t lane(int i_in) {
+        const int i = i_in + rp::kSlotLanes * (cur_slot + rp::kBatchSlots * cur_prio);
         while ((int)lanes.size() <= i) {
+            const bool high = (int)lanes.size() >= rp::kSlotLanes * rp::kBatchSlots;
+            int least = 0, greatest = 0;
+            if (high) cudaDeviceGetStreamPriorityRange(&least, &greatest);
             cudaStream_t st = nullptr;
-            cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+            cudaError_t e = cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, high ? greatest : 0);
             if (e != cudaSuccess) rp::fail(RP_E_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
             lanes.push_back(st);
         }
@@ -408,6 +450,11 @@ double radius_of(int z);  // vdW radius (Bohr) of element z, the filter's table
 void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
                const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,
                double *info, cudaStream_t stream);
+// Words per system written by the bordered solve: refined residual inf-norm, min |pivot|,
+// max |pivot|, singular flag, kappa = ||A||_1 ||K^-1||_1, the unknowns n+1 of the bordered
+// system, FP32 refinement steps, and the factorisation path (0 FP32 in one CTA, 1 FP32
+// across the GPU, 2 FP64 in one CTA, 3 FP64 across the GPU).
+constexpr int kSolveInfo = 8;
 // Batched constraints + bordered solves: one CTA per system, one launch.
 struct SolveJob {
     const double *A, *b;
@@ -418,11 +465,48 @@ struct SolveJob {
     double *q;
 };
 void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream);
-// The same without waiting: returns the pinned host copy of the 4 info words per job, valid
+// One bordered system of the solve kernel (device-side descriptor).
+struct SolveDesc {
+    const double *A;      // N x N input
+    const double *b;      // N input
+    int N;                // original atoms
+    int n;                // reduced atoms
+    const int *mem_ptr;   // n+1, CSR of members per reduced index
+    const int *mem_idx;   // members (original atom indices)
+    const double *resp_s; // n (per reduced index, already mapped) or null
+    const double *resp_t; // n
+    const int *map;       // N: reduced index of each original atom
+    double qtot;
+    double *As;           // (n+1)^2 work: bordered matrix, then LU
+    double *A0;           // (n+1)^2 copy of the bordered matrix (for refinement)
+    double *bs;           // n+1 rhs
+    double *x;            // n+1 solution
+    double *r;            // n+1 residual / correction
+    int *perm;            // n+1 pivot rows
+    double *q;            // N out
+    double *info;         // kSolveInfo out: residual inf-norm, min|piv|, max|piv|, singular flag,
+                          // kappa, unknowns n+1, refinement steps, factorisation path
+    double *pre;          // null, or {flag, min|piv|, max|piv|} of a wide factorisation already in As
+    int wide64;           // As holds wide FP64 factors: skip the FP32 stage and the in-CTA FP64 LU
+};
+// Wide systems of a solve launch whose FP32 refinement may not have converged: their flags are
+// on their way to pinned memory; solve_wide_fp64 (after the stream has reached them) factors
+// the flagged ones again in FP64, refines them and refreshes the pinned info words.
+struct SolvePending {
+    bool any_wide = false;
+    std::string tag;
+    double *h_pre = nullptr, *h_info = nullptr, *d_info = nullptr;
+    std::vector<SolveDesc> descs;
+    std::vector<int> n1;
+};
+// The same without waiting: returns the pinned host copy of the kSolveInfo words per job, valid
 // once `stream` has reached this point.  `tag` keeps the scratch of solves in flight apart.
-// (Systems with overlapping symmetry groups are folded on the host, which waits.)
+// With `pend`, wide systems that need FP64 factors are left for solve_wide_fp64 (the words
+// are final after it); without, the call waits for them.  (Systems with overlapping symmetry
+// groups are folded on the host, which waits.)
 const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, cudaStream_t stream,
-                                const std::string &tag);
+                                const std::string &tag, SolvePending *pend = nullptr);
+void solve_wide_fp64(rp_ctx *ctx, SolvePending &pd, cudaStream_t stream);  // synchronises stream
 
 // Device table builders (ewald_tables.cu).
 void atom_tables_fp64(const rp_ewald *ew, const double *d_atoms, int N, double *d_B, int ldb, cudaStream_t s);

@@ -8,18 +8,21 @@
 // with g = (i*a0 + j*a1) + k*a2 and |d|^2 = (dx*dx + dy*dy) + dz*dz evaluated in
 // IEEE FP64 without contraction.
 //
-// GB300 design: every grid point is classified in FP32 against the atoms of the
-// 27 neighbouring bins of a cell list (bin edge >= max rmin, so no other atom
-// can reject it).  A pair whose FP32 squared distance lies within a proven error
+// GB300 design: one CTA per brick of 8 x 4 x 4 grid points.  The CTA culls the
+// images of the cell-list bins around its points (bin edge >= max rmin, so no
+// other image can reject a point) to those within rmin of the brick's bounding
+// box, keeps them in shared memory, and classifies every point in FP32 against
+// that short list.  A pair whose FP32 squared distance lies within a proven error
 // band of rmin^2 is re-evaluated in FP64 exactly as above, so the mask is
 // bit-identical to the FP64 rule while almost all work runs on the FP32 pipe.
 // "near" is proved for the whole grid on the host when one image's rmax covers
 // every grid corner (always true at the default vdw_max = 1000); otherwise it
 // is tested the same way (FP32 with an FP64 recheck band) against every image.
 //
-// The kernel is bound by HBM traffic of the mask pass: 1 B mask write per point
-// (plus the compaction pass: 1 B mask read + 8 B V read per point, 4 B index +
-// 8 B V write per kept point).
+// Traffic per grid point: 1 B mask write (plus the compaction pass: 1 B mask read
+// + 8 B V read per point, 4 B index + 8 B V write per kept point).  The mask pass
+// is bound by its FP32 distance tests, ~5 candidate images per point after the
+// brick's cull.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -48,76 +51,201 @@ __device__ __noinline__ double exact_d2(const double *axd, int i, int j, int k, 
     return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
-__global__ void __launch_bounds__(kFilterThreads) filter_mask_kernel(
-    FilterParams p, const float4 *__restrict__ eff, const D4 *__restrict__ eff64,
-    const double *__restrict__ rmax2, const float *__restrict__ rmax2f, const int *__restrict__ boff,
-    const int *__restrict__ bidx, uint8_t *__restrict__ mask, int *__restrict__ block_counts,
-    unsigned long long *__restrict__ rechecks) {
-    long long f = (long long)blockIdx.x * kFilterThreads + threadIdx.x;
-    int keep = 0;
-    unsigned nre = 0;
-    if (f < p.n_total) {
-        int layer = p.nx * p.ny;
-        int k = (int)(f / layer);
-        int rem = (int)(f - (long long)k * layer);
-        int j = rem / p.nx;
-        int i = rem - j * p.nx;
-        float gx = (i * p.ax[0] + j * p.ax[3]) + k * p.ax[6];
-        float gy = (i * p.ax[1] + j * p.ax[4]) + k * p.ax[7];
-        float gz = (i * p.ax[2] + j * p.ax[5]) + k * p.ax[8];
-        int bc[3];
-        float g3[3] = {gx, gy, gz};
+// Reject test of one grid point against the atoms of its 27 neighbouring bins (bin edge >=
+// max rmin): FP32 distances, FP64 recheck inside the band.  Returns false when some image
+// rejects the point.
+__device__ __forceinline__ bool valid_by_bins(const FilterParams &p, int i, int j, int k, float gx, float gy,
+                                              float gz, const float4 *__restrict__ eff,
+                                              const D4 *__restrict__ eff64, const int *__restrict__ boff,
+                                              const int *__restrict__ bidx, unsigned &nre) {
+    int bc[3];
+    const float g3[3] = {gx, gy, gz};
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            float t = (g3[d] - p.bmin[d]) * p.inv_bsize;
-            t = fminf(fmaxf(t, -1.0f), (float)p.bn[d]);
-            bc[d] = min(max((int)floorf(t), 0), p.bn[d] - 1);
+    for (int d = 0; d < 3; ++d) {
+        float t = (g3[d] - p.bmin[d]) * p.inv_bsize;
+        t = fminf(fmaxf(t, -1.0f), (float)p.bn[d]);
+        bc[d] = min(max((int)floorf(t), 0), p.bn[d] - 1);
+    }
+    for (int dz = -1; dz <= 1; ++dz) {
+        const int z2 = bc[2] + dz;
+        if (z2 < 0 || z2 >= p.bn[2]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y2 = bc[1] + dy;
+            if (y2 < 0 || y2 >= p.bn[1]) continue;
+            const int row = p.bn[0] * (y2 + p.bn[1] * z2);
+            const int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, p.bn[0] - 1);
+            const int t0 = boff[row + x0], t1 = boff[row + x1 + 1];
+            for (int t = t0; t < t1; ++t) {
+                const int a = bidx[t];
+                const float4 e = eff[a];
+                const float ddx = gx - e.x, ddy = gy - e.y, ddz = gz - e.z;
+                const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                if (d2 <= e.w - p.err_min) return false;
+                if (d2 <= e.w + p.err_min) {
+                    const D4 e8 = eff64[a];
+                    ++nre;
+                    if (exact_d2(p.axd, i, j, k, e8.x, e8.y, e8.z) <= e8.w) return false;
+                }
+            }
         }
-        bool valid = true;
-        for (int dz = -1; dz <= 1 && valid; ++dz) {
-            int z2 = bc[2] + dz;
-            if (z2 < 0 || z2 >= p.bn[2]) continue;
-            for (int dy = -1; dy <= 1 && valid; ++dy) {
-                int y2 = bc[1] + dy;
-                if (y2 < 0 || y2 >= p.bn[1]) continue;
-                int row = p.bn[0] * (y2 + p.bn[1] * z2);
-                int x0 = max(bc[0] - 1, 0), x1 = min(bc[0] + 1, p.bn[0] - 1);
-                int t0 = boff[row + x0], t1 = boff[row + x1 + 1];
-                for (int t = t0; t < t1; ++t) {
-                    int a = bidx[t];
-                    float4 e = eff[a];
-                    float ddx = gx - e.x, ddy = gy - e.y, ddz = gz - e.z;
-                    float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                    if (d2 <= e.w - p.err_min) { valid = false; break; }
-                    if (d2 <= e.w + p.err_min) {
-                        D4 e8 = eff64[a];
-                        ++nre;
-                        if (exact_d2(p.axd, i, j, k, e8.x, e8.y, e8.z) <= e8.w) { valid = false; break; }
+    }
+    return true;
+}
+
+// The near test (some image with |g-e|^2 <= rmax^2), needed only when the host could not
+// prove it for the whole grid (vdw_max below its default): every image, FP32 with the
+// FP64 recheck band.
+__device__ __forceinline__ bool near_any(const FilterParams &p, int i, int j, int k, float gx, float gy, float gz,
+                                         const float4 *__restrict__ eff, const D4 *__restrict__ eff64,
+                                         const double *__restrict__ rmax2, const float *__restrict__ rmax2f,
+                                         unsigned &nre) {
+    for (int a = 0; a < p.A; ++a) {
+        const float4 e = eff[a];
+        const float ddx = gx - e.x, ddy = gy - e.y, ddz = gz - e.z;
+        const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+        const float r2 = rmax2f[a];
+        if (d2 <= r2 - p.err_max) return true;
+        if (d2 <= r2 + p.err_max) {
+            const D4 e8 = eff64[a];
+            ++nre;
+            if (exact_d2(p.axd, i, j, k, e8.x, e8.y, e8.z) <= rmax2[a]) return true;
+        }
+    }
+    return false;
+}
+
+// Bricks of 8 x 4 x 4 grid points (one CTA of 128 threads each, x fastest), bricks in
+// x-then-y-then-z order, points inside a brick in the same order: the unit of the culled
+// mask kernel and of the brick-ordered compaction.
+constexpr int kBrickX = 8, kBrickY = 4, kBrickZ = 4;
+constexpr int kBrickPts = kBrickX * kBrickY * kBrickZ;  // 128
+constexpr int kCullCap = 512;  // candidate images a brick keeps in shared memory
+
+__device__ __forceinline__ long long brick_point(int b, int t, int nx, int ny, int nz, int nbx, int nby) {
+    const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+    const int i = bx * kBrickX + (t % kBrickX), j = by * kBrickY + ((t / kBrickX) % kBrickY),
+              l = bz * kBrickZ + t / (kBrickX * kBrickY);
+    if (i >= nx || j >= ny || l >= nz) return -1;
+    return (long long)i + (long long)nx * (j + (long long)ny * l);
+}
+
+// The mask, one brick per CTA.  The CTA first culls the images of the bins around its points'
+// bounding box to those that can reject any of them (FP32 distance from the image to the box
+// within rmin^2 + the error band, with a relative margin above the FP32 rounding of both
+// distances), keeping them in shared memory; each point then tests only those (about a
+// quarter of its 27 bins' images).  A culled image is farther than the band from every point
+// of the brick, so it could neither reject a point nor trigger its FP64 recheck: the mask is
+// the one of the per-point bin test (valid_by_bins), which a brick with more than kCullCap
+// candidates falls back to.  Writes the mask and the brick's kept count.
+__global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(
+    FilterParams p, int nbx, int nby, const float4 *__restrict__ eff, const D4 *__restrict__ eff64,
+    const double *__restrict__ rmax2, const float *__restrict__ rmax2f, const int *__restrict__ boff,
+    const int *__restrict__ bidx, uint8_t *__restrict__ mask, int *__restrict__ brick_counts,
+    unsigned long long *__restrict__ rechecks) {
+    __shared__ float4 cand[kCullCap];
+    __shared__ int cidx[kCullCap];
+    __shared__ int ncand;
+    __shared__ float red[6][kBrickPts / 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int b = blockIdx.x;
+    const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+    const int i = bx * kBrickX + (t % kBrickX), j = by * kBrickY + ((t / kBrickX) % kBrickY),
+              k = bz * kBrickZ + t / (kBrickX * kBrickY);
+    const bool inside = i < p.nx && j < p.ny && k < p.nz;
+    const float gx = (i * p.ax[0] + j * p.ax[3]) + k * p.ax[6];
+    const float gy = (i * p.ax[1] + j * p.ax[4]) + k * p.ax[7];
+    const float gz = (i * p.ax[2] + j * p.ax[5]) + k * p.ax[8];
+    // bounding box of the brick's points (exactly their FP32 coordinates)
+    float v[6] = {inside ? gx : 3e38f, inside ? gy : 3e38f, inside ? gz : 3e38f,
+                  inside ? gx : -3e38f, inside ? gy : -3e38f, inside ? gz : -3e38f};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const float w = __shfl_xor_sync(0xffffffffu, v[q], o);
+            v[q] = q < 3 ? fminf(v[q], w) : fmaxf(v[q], w);
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) red[q][warp] = v[q];
+    if (t == 0) ncand = 0;
+    __syncthreads();
+    float lo[3], hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = red[d][0];
+        hi[d] = red[3 + d][0];
+        for (int w = 1; w < kBrickPts / 32; ++w) {
+            lo[d] = fminf(lo[d], red[d][w]);
+            hi[d] = fmaxf(hi[d], red[3 + d][w]);
+        }
+    }
+    // bins that can hold a rejecting image: one bin beyond the box's own on every side
+    int c0[3], c1[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float ta = fminf(fmaxf((lo[d] - p.bmin[d]) * p.inv_bsize, -1.0f), (float)p.bn[d]);
+        const float tb = fminf(fmaxf((hi[d] - p.bmin[d]) * p.inv_bsize, -1.0f), (float)p.bn[d]);
+        c0[d] = max(min(max((int)floorf(ta), 0), p.bn[d] - 1) - 1, 0);
+        c1[d] = min(min(max((int)floorf(tb), 0), p.bn[d] - 1) + 1, p.bn[d] - 1);
+    }
+    for (int z2 = c0[2]; z2 <= c1[2]; ++z2)
+        for (int y2 = c0[1]; y2 <= c1[1]; ++y2) {
+            const int row = p.bn[0] * (y2 + p.bn[1] * z2);
+            const int t0 = boff[row + c0[0]], t1 = boff[row + c1[0] + 1];
+            for (int u = t0 + t; u < t1; u += kBrickPts) {
+                const int a = bidx[u];
+                const float4 e = eff[a];
+                const float dx = fmaxf(fmaxf(lo[0] - e.x, e.x - hi[0]), 0.f);
+                const float dy = fmaxf(fmaxf(lo[1] - e.y, e.y - hi[1]), 0.f);
+                const float dz = fmaxf(fmaxf(lo[2] - e.z, e.z - hi[2]), 0.f);
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                if (d2 <= (e.w + p.err_min) * 1.0001f) {
+                    const int pos = atomicAdd(&ncand, 1);
+                    if (pos < kCullCap) {
+                        cand[pos] = e;
+                        cidx[pos] = a;
                     }
                 }
             }
         }
-        bool near = p.near_all != 0;
-        if (valid && !near) {
-            for (int a = 0; a < p.A && !near; ++a) {
-                float4 e = eff[a];
-                float ddx = gx - e.x, ddy = gy - e.y, ddz = gz - e.z;
-                float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                float r2 = rmax2f[a];
-                if (d2 <= r2 - p.err_max) { near = true; break; }
-                if (d2 <= r2 + p.err_max) {
-                    D4 e8 = eff64[a];
+    __syncthreads();
+    const int nc = ncand;
+    int keep = 0;
+    unsigned nre = 0;
+    if (inside) {
+        bool valid = true;
+        if (nc <= kCullCap) {
+            for (int c = 0; c < nc; ++c) {
+                const float4 e = cand[c];
+                const float ddx = gx - e.x, ddy = gy - e.y, ddz = gz - e.z;
+                const float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                if (d2 <= e.w - p.err_min) { valid = false; break; }
+                if (d2 <= e.w + p.err_min) {
+                    const D4 e8 = eff64[cidx[c]];
                     ++nre;
-                    if (exact_d2(p.axd, i, j, k, e8.x, e8.y, e8.z) <= rmax2[a]) near = true;
+                    if (exact_d2(p.axd, i, j, k, e8.x, e8.y, e8.z) <= e8.w) { valid = false; break; }
                 }
             }
+        } else {
+            valid = valid_by_bins(p, i, j, k, gx, gy, gz, eff, eff64, boff, bidx, nre);
         }
+        const bool near = p.near_all != 0 || (valid && near_any(p, i, j, k, gx, gy, gz, eff, eff64, rmax2, rmax2f, nre));
         keep = (valid && near) ? 1 : 0;
-        mask[f] = (uint8_t)keep;
+        mask[(long long)i + (long long)p.nx * (j + (long long)p.ny * k)] = (uint8_t)keep;
     }
-    int cnt = __syncthreads_count(keep);
-    if (threadIdx.x == 0) block_counts[blockIdx.x] = cnt;
+    const int cnt = __syncthreads_count(keep);
+    if (t == 0) brick_counts[b] = cnt;
     if (nre) atomicAdd(rechecks, (unsigned long long)nre);
+}
+
+// Kept points per block of kFilterThreads consecutive flat indices (the flat-order compaction).
+__global__ void __launch_bounds__(kFilterThreads) flat_count_kernel(const uint8_t *__restrict__ mask, long long n_total,
+                                                                    int *__restrict__ counts) {
+    const long long f = (long long)blockIdx.x * kFilterThreads + threadIdx.x;
+    const int keep = f < n_total ? mask[f] : 0;
+    const int cnt = __syncthreads_count(keep);
+    if (threadIdx.x == 0) counts[blockIdx.x] = cnt;
 }
 
 // Exclusive scan of the per-block counts (one block; nb up to a few 10^5).
@@ -182,30 +310,10 @@ __global__ void __launch_bounds__(kFilterThreads) compact_kernel(
     }
 }
 
-// Brick-ordered compaction: bricks of 8 x 4 x 4 grid points (one CTA of 128 threads
-// each, x fastest), bricks in x-then-y-then-z order, points inside a brick in the
-// same order.  The kept points of a brick are contiguous, so any 128 consecutive
-// kept points span a compact region of the cell (the real-space culling of the
-// mixed fit keeps fewer images for compact tiles).  Deterministic (ballots only).
-constexpr int kBrickX = 8, kBrickY = 4, kBrickZ = 4;
-constexpr int kBrickPts = kBrickX * kBrickY * kBrickZ;  // 128
-
-__device__ __forceinline__ long long brick_point(int b, int t, int nx, int ny, int nz, int nbx, int nby) {
-    const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
-    const int i = bx * kBrickX + (t % kBrickX), j = by * kBrickY + ((t / kBrickX) % kBrickY),
-              l = bz * kBrickZ + t / (kBrickX * kBrickY);
-    if (i >= nx || j >= ny || l >= nz) return -1;
-    return (long long)i + (long long)nx * (j + (long long)ny * l);
-}
-
-__global__ void __launch_bounds__(kBrickPts) brick_count_kernel(const uint8_t *__restrict__ mask, int nx, int ny,
-                                                                int nz, int nbx, int nby, int *__restrict__ counts) {
-    const long long f = brick_point(blockIdx.x, threadIdx.x, nx, ny, nz, nbx, nby);
-    const int keep = (f >= 0) ? mask[f] : 0;
-    const int cnt = __syncthreads_count(keep);
-    if (threadIdx.x == 0) counts[blockIdx.x] = cnt;
-}
-
+// Brick-ordered compaction (bricks as in filter_brick_kernel, whose kept counts it uses).
+// The kept points of a brick are contiguous, so any 128 consecutive kept points span a
+// compact region of the cell (the real-space culling of the mixed fit keeps fewer images
+// for compact tiles).  Deterministic (ballots only).
 __global__ void __launch_bounds__(kBrickPts) brick_compact_kernel(
     const uint8_t *__restrict__ mask, const double *__restrict__ V, int nx, int ny, int nz, int nbx, int nby,
     const long long *__restrict__ offsets, long long capacity, int32_t *__restrict__ kept_idx,
@@ -548,10 +656,16 @@ void filter_launch(rp_ctx *ctx, const FilterPlan &plan, const char *packed_dev, 
     RP_CUDA(cudaMemsetAsync(d_re, 0, sizeof(unsigned long long), stream));
 
     StageTimer t_f(ctx, "filter", stream);
-    filter_mask_kernel<<<nblk, kFilterThreads, 0, stream>>>(p, d_e32, d_e64, d_rmax2, d_rmax2f, d_boff, d_bidx,
-                                                            d_mask, d_counts, d_re);
+    const int nbx = (nx + kBrickX - 1) / kBrickX, nby = (ny + kBrickY - 1) / kBrickY,
+              nbz = (nz + kBrickZ - 1) / kBrickZ;
+    const int nbr = nbx * nby * nbz;
+    int *d_bc = ctx->buf_t<int>("flt_bcounts" + tag, (size_t)nbr);
+    filter_brick_kernel<<<nbr, kBrickPts, 0, stream>>>(p, nbx, nby, d_e32, d_e64, d_rmax2, d_rmax2f, d_boff, d_bidx,
+                                                       d_mask, d_bc, d_re);
     RP_LAUNCH_CHECK();
     if (!brick_order) {
+        flat_count_kernel<<<nblk, kFilterThreads, 0, stream>>>(d_mask, n_total, d_counts);
+        RP_LAUNCH_CHECK();
         scan_counts_kernel<<<1, 1024, 0, stream>>>(d_counts, nblk, d_offsets, d_total);
         RP_LAUNCH_CHECK();
         compact_kernel<<<nblk, kFilterThreads, 0, stream>>>(d_mask, V_dev, n_total, d_offsets, capacity,
@@ -560,14 +674,8 @@ void filter_launch(rp_ctx *ctx, const FilterPlan &plan, const char *packed_dev, 
         vmean_kernel<<<1, 1024, 0, stream>>>(d_vsum, nblk, d_total, d_mean);
         RP_LAUNCH_CHECK();
     } else {
-        const int nbx = (nx + kBrickX - 1) / kBrickX, nby = (ny + kBrickY - 1) / kBrickY,
-                  nbz = (nz + kBrickZ - 1) / kBrickZ;
-        const int nbr = nbx * nby * nbz;
-        int *d_bc = ctx->buf_t<int>("flt_bcounts" + tag, (size_t)nbr);
         long long *d_bo = ctx->buf_t<long long>("flt_boffsets" + tag, (size_t)nbr);
         double *d_bv = ctx->buf_t<double>("flt_bvsum" + tag, (size_t)nbr);
-        brick_count_kernel<<<nbr, kBrickPts, 0, stream>>>(d_mask, nx, ny, nz, nbx, nby, d_bc);
-        RP_LAUNCH_CHECK();
         scan_counts_kernel<<<1, 1024, 0, stream>>>(d_bc, nbr, d_bo, d_total);
         RP_LAUNCH_CHECK();
         brick_compact_kernel<<<nbr, kBrickPts, 0, stream>>>(d_mask, V_dev, nx, ny, nz, nbx, nby, d_bo, capacity,

@@ -798,11 +798,41 @@ __global__ void colstats_finish_kernel(const double *__restrict__ psum, const fl
     cdf[a] = make_float2(ch, cl);
     c[a] = (double)ch + (double)cl;  // the shift actually applied, exactly
     // |Phi - c| <= 2 max|Phi| =: bound in [2^(e-1), 2^e); scale 2^(-e-1) puts |x| below 1/2,
-    // so the fixed-point slices stay within |x_s| <= 64 even if a later chunk doubles the range
+    // so the fixed-point slices stay within |x_s| <= 64 (later chunks: colstats_scale_kernel)
     float bound = 2.f * mx;
     int e = 0;
     if (bound > 0.f) frexpf(bound, &e);
     scale[a] = ldexpf(1.f, -e - 1);
+}
+
+// Later chunks of a two-pass fit keep the first chunk's centre c and take a scale of their
+// own: |Phi - c| <= 2 max(max|Phi|, |c|) =: bound in [2^(e-1), 2^e), scale 2^(-e-1).  Each
+// chunk's Gram tiles and row sums are converted to Phi units with that chunk's scale
+// (gram_reduce_kernel, rowsum_flush_kernel), so chunks need not share one.
+__global__ void colstats_scale_kernel(const float *__restrict__ pmax, int nblk, int N, const double *__restrict__ c,
+                                      float *__restrict__ scale) {
+    const int a = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (a >= N) return;  // whole warp
+    float mx = 0.f;
+    for (int k = lane; k < nblk; k += 32) mx = fmaxf(mx, pmax[(size_t)a * nblk + k]);
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane != 0) return;
+    float bound = 2.f * fmaxf(mx, (float)fabs(c[a]) * 1.0001f);
+    int e = 0;
+    if (bound > 0.f) frexpf(bound, &e);
+    scale[a] = ldexpf(1.f, -e - 1);
+}
+
+// After each chunk: its exact fixed-point row sums, converted to Phi units with the chunk's
+// scales (exact: an int64 below 2^53 times a power of two), are added to sums[Np] and
+// the integer sums are cleared for the next chunk.
+__global__ void rowsum_flush_kernel(unsigned long long *__restrict__ rowsum, const float *__restrict__ scale,
+                                    const double *__restrict__ vmax_p, int N, double *__restrict__ sums) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a > N) return;
+    const double sc = a < N ? (double)scale[a] : (double)vscale_of(*vmax_p);
+    sums[a] += ldexp((double)(long long)rowsum[a], -27) / sc;
+    rowsum[a] = 0ull;
 }
 
 constexpr int kSliceThreads = 256;
@@ -907,23 +937,20 @@ __global__ void gram_reduce_kernel(const double *__restrict__ part, int ntiles, 
 }
 
 // A = G - s s^T / M, b = G[:, V] - s s_V / M with s the exact column sums of the
-// fixed-point rows (value = digits sum 2^-27 / scale), i.e. repeat.py:2266-2276 for the
+// fixed-point rows in Phi units (rowsum_flush_kernel), i.e. repeat.py:2266-2276 for the
 // shifted, quantised columns; optionally sum_phi = s + M c.
-__global__ void finish_mixed_kernel(const double *__restrict__ G, int Np, const unsigned long long *__restrict__ rowsum,
-                                    const float *__restrict__ scale, const double *__restrict__ vmax_p,
+__global__ void finish_mixed_kernel(const double *__restrict__ G, int Np, const double *__restrict__ sums,
                                     const double *__restrict__ c, long long M, int N, double *__restrict__ A,
                                     double *__restrict__ b, double *__restrict__ sum_phi) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const double invM = 1.0 / (double)M;
-    const double sv = ldexp((double)(long long)rowsum[N], -27) / (double)vscale_of(*vmax_p);
+    const double sv = sums[N];
     if (t < (long long)N * N) {
         const int i = (int)(t / N), j = (int)(t - (long long)i * N);
-        const double si = ldexp((double)(long long)rowsum[i], -27) / (double)scale[i];
-        const double sj = ldexp((double)(long long)rowsum[j], -27) / (double)scale[j];
-        A[t] = G[(size_t)i * Np + j] - si * sj * invM;
+        A[t] = G[(size_t)i * Np + j] - sums[i] * sums[j] * invM;
     }
     if (t < N) {
-        const double si = ldexp((double)(long long)rowsum[t], -27) / (double)scale[t];
+        const double si = sums[t];
         b[t] = G[(size_t)t * Np + N] - si * sv * invM;
         if (sum_phi) sum_phi[t] = si + (double)M * c[t];
     }
@@ -1052,7 +1079,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     RP_CUDA(cudaMemcpyAsync(d_atoms, atoms, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_shifts, sh.data(), sizeof(double) * sh.size(), cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice, stream));
-    int *d_status = ctx->d_status;  // cleared by the caller (rp_gram / the batch driver)
+    int *d_status = ctx->status_words();  // cleared by the caller (rp_gram / the batch driver)
 
     // reciprocal rows of every atom (stages A and B) and the double-float images, once per fit
     float2 *E = ctx->buf_t<float2>("m_E" + slot, recip_rows_bytes(ew, N) / sizeof(float2));
@@ -1068,6 +1095,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     const int Np = N + 1;                       // atoms + the ESP row
     const long long per_point = 8LL * N + 8LL * Np;  // Phi (double-float, two-pass) + four FP16 digits
     long long chunk = std::max<long long>(kBM, ((6LL << 30) / per_point) / kBM * kBM);
+    if (ctx->chunk_cap > 0) chunk = std::max<long long>(kBM, std::min<long long>(chunk, ctx->chunk_cap / kBM * kBM));
     chunk = std::min<long long>(chunk, round_up(M, kBM));
     const long long chunk_pad = round_up(chunk, kBK);
 
@@ -1077,17 +1105,19 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     float2 *phit = single ? nullptr : ctx->buf_t<float2>("m_phit" + slot, (size_t)N * chunk_pad);
     __half *X[kGSlices];
     for (int q = 0; q < kGSlices; ++q) X[q] = ctx->buf_t<__half>("m_X" + slot + std::to_string(q), (size_t)Np * chunk_pad);
-    int *d_clamped = ctx->d_status + 1;  // second status word: fixed-point range overflows
+    int *d_clamped = ctx->status_words() + 1;  // second status word: fixed-point range overflows
     const int nblk = (int)ceil_div(chunk, kPhiPts);
     double *psum = single ? nullptr : ctx->buf_t<double>("m_psum" + slot, (size_t)N * nblk);
     float *pmax = single ? nullptr : ctx->buf_t<float>("m_pmax" + slot, (size_t)N * nblk);
     unsigned long long *rowsum = ctx->buf_t<unsigned long long>("m_rowsum" + slot, (size_t)Np);
+    double *sums = ctx->buf_t<double>("m_sums" + slot, (size_t)Np);
     double *cvec = ctx->buf_t<double>("m_c" + slot, N);
     float2 *cdf = ctx->buf_t<float2>("m_cdf" + slot, N);
     float *scale = ctx->buf_t<float>("m_scale" + slot, N);
     double *G = ctx->buf_t<double>("m_G" + slot, (size_t)Np * Np);
     RP_CUDA(cudaMemsetAsync(G, 0, sizeof(double) * Np * Np, stream));
     RP_CUDA(cudaMemsetAsync(rowsum, 0, sizeof(unsigned long long) * Np, stream));
+    RP_CUDA(cudaMemsetAsync(sums, 0, sizeof(double) * Np, stream));
 
     // ESP row scale from max |Vc| (the filter's, or computed here)
     const double *vmax = vstats_dev ? vstats_dev + 1 : nullptr;
@@ -1126,13 +1156,15 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
             launch_phi(kept_idx_dev, m0, rows, d_axis, ew->grid.axis, nx, ny, d_atoms, N, d_shifts, S, zero_idx, ew->cutoff,
                        ew->sqrt_alpha, img, ew->d_exf, E, n1c, 3, phit, chunk_pad, psum, pmax, nullptr, stream);
         }
-        // 2. centre/scale on the first chunk, fixed-point digits of X
+        // 2. centre on the first chunk, a scale per chunk, fixed-point digits of X
         if (!single) {
             StageTimer tt(ctx, "center_slice", stream);
             if (m0 == 0) {
                 colstats_finish_kernel<<<ceil_div(N, 4), 128, 0, stream>>>(psum, pmax, nb, N, rows, cvec, cdf, scale);
-                RP_LAUNCH_CHECK();
+            } else {
+                colstats_scale_kernel<<<ceil_div(N, 4), 128, 0, stream>>>(pmax, nb, N, cvec, scale);
             }
+            RP_LAUNCH_CHECK();
             slice_rows_kernel<<<dim3(ceil_div(rows_kpad / 2, kSliceThreads), Np), kSliceThreads, 0, stream>>>(
                 phit, chunk_pad, rows, rows_kpad, N, cdf, scale, Vc_dev, m0, vmax, X[0], X[1], X[2], X[3], d_clamped,
                 rowsum);
@@ -1161,10 +1193,12 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
             gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256, 0, stream>>>(part, ntri, nsplit, ntj, Np,
                                                                                          scale, vmax, N, G);
             RP_LAUNCH_CHECK();
+            rowsum_flush_kernel<<<ceil_div(Np, 128), 128, 0, stream>>>(rowsum, scale, vmax, N, sums);
+            RP_LAUNCH_CHECK();
         }
     }
     finish_mixed_kernel<<<ceil_div(std::max<long long>((long long)N * N, N), 256), 256, 0, stream>>>(
-        G, Np, rowsum, scale, vmax, cvec, M, N, A_dev, b_dev, sum_phi_dev);
+        G, Np, sums, cvec, M, N, A_dev, b_dev, sum_phi_dev);
     RP_LAUNCH_CHECK();
 }
 
@@ -1176,6 +1210,15 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
 extern "C" int rp_debug_bound_scale(rp_ctx *ctx, double factor) {
     if (!ctx || !(factor > 0.0)) return RP_E_ARG;
     ctx->bound_scale = factor;
+    return RP_OK;
+}
+
+// Diagnostics (not part of the public ABI): an upper bound on the kept points per chunk of
+// the staged mixed Gram (0 = the memory-based size), so tests can run many chunks on a
+// small cube.
+extern "C" int rp_debug_chunk_cap(rp_ctx *ctx, long long points) {
+    if (!ctx || points < 0) return RP_E_ARG;
+    ctx->chunk_cap = points;
     return RP_OK;
 }
 

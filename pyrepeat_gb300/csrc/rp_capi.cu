@@ -28,23 +28,26 @@ void smem_optin(const void *kernel, size_t bytes) {
         have = bytes;
     }
 }
-void status_clear(rp_ctx *ctx, cudaStream_t s) { RP_CUDA(cudaMemsetAsync(ctx->d_status, 0, 2 * sizeof(int), s)); }
+void status_clear(rp_ctx *ctx, cudaStream_t s) {
+    RP_CUDA(cudaMemsetAsync(ctx->status_words(), 0, 2 * sizeof(int), s));
+}
 void status_check(rp_ctx *ctx, cudaStream_t s) {
     int st[2] = {0, 0};
-    RP_CUDA(cudaMemcpyAsync(st, ctx->d_status, sizeof(st), cudaMemcpyDeviceToHost, s));
+    RP_CUDA(cudaMemcpyAsync(st, ctx->status_words(), sizeof(st), cudaMemcpyDeviceToHost, s));
     RP_CUDA(cudaStreamSynchronize(s));
     if (st[0] != 0) fail(st[0], "a tensor-core pipeline wait ran out of time");
     if (st[1] != 0)
-        fail(RP_E_STATE, std::to_string(st[1]) + " Phi values exceeded the fixed-point range set on the first chunk");
+        fail(RP_E_STATE, std::to_string(st[1]) + " Phi values exceeded the fixed-point range of their chunk");
 }
 }  // namespace rp
 
 cublasHandle_t rp_ctx::blas() {
-    if (!cublas) {
-        RP_CUBLAS(cublasCreate(&cublas));
-        RP_CUBLAS(cublasSetMathMode(cublas, CUBLAS_DEFAULT_MATH));  // native FP64, no emulation
+    cublasHandle_t &h = cublas[cur_slot];
+    if (!h) {
+        RP_CUBLAS(cublasCreate(&h));
+        RP_CUBLAS(cublasSetMathMode(h, CUBLAS_DEFAULT_MATH));  // native FP64, no emulation
     }
-    return cublas;
+    return h;
 }
 
 namespace {
@@ -52,7 +55,11 @@ namespace {
 template <class F>
 int guarded(rp_ctx *ctx, F &&f) {
     try {
-        if (ctx) RP_CUDA(cudaSetDevice(ctx->device));
+        if (ctx) {
+            ctx->cur_slot = 0;  // calls on the caller's thread run in slot 0, default priority
+            ctx->cur_prio = 0;
+            RP_CUDA(cudaSetDevice(ctx->device));
+        }
         f();
         if (ctx) ctx->last_error.clear();
         return RP_OK;
@@ -70,7 +77,7 @@ int guarded(rp_ctx *ctx, F &&f) {
 
 extern "C" {
 
-int rp_version(void) { return 10000; }
+int rp_version(void) { return 20000; }
 
 int rp_ctx_create(int device, size_t hbm_budget, rp_ctx **out) {
     if (!out) return RP_E_ARG;
@@ -88,7 +95,8 @@ int rp_ctx_create(int device, size_t hbm_budget, rp_ctx **out) {
         size_t fr = 0, tot = 0;
         RP_CUDA(cudaMemGetInfo(&fr, &tot));
         c->budget = hbm_budget ? hbm_budget : (size_t)(0.9 * (double)fr);
-        RP_CUDA(cudaMalloc(&c->d_status, 64));
+        RP_CUDA(cudaMalloc(&c->d_status, sizeof(int) * 2 * rp::kBatchSlots));
+        RP_CUDA(cudaMemset(c->d_status, 0, sizeof(int) * 2 * rp::kBatchSlots));
     });
     if (rc != RP_OK) {
         delete c;
@@ -105,7 +113,8 @@ int rp_ctx_destroy(rp_ctx *ctx) {
     for (auto &kv : ctx->scratch) cudaFree(kv.second.ptr);
     for (auto &kv : ctx->host_scratch) cudaFreeHost(kv.second.ptr);
     for (cudaStream_t st : ctx->lanes) cudaStreamDestroy(st);
-    if (ctx->cublas) cublasDestroy(ctx->cublas);
+    for (cublasHandle_t h : ctx->cublas)
+        if (h) cublasDestroy(h);
     cudaFree(ctx->d_status);
     delete ctx;
     return RP_OK;
@@ -209,245 +218,425 @@ int rp_qeq(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const do
 }  // extern "C"
 
 namespace rp {
-// The batched fit; throws rp::Error.  Used by rp_fit_batch (on the caller's thread) and by
-// the asynchronous batch server (on its worker thread).
-void fit_batch_body(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
-                    int64_t *M_out, double *info_out, cudaStream_t stream) {
-    std::vector<rp_ewald *> ews((size_t)n, nullptr);
-    {
-        if (n == 0) return;
-        std::vector<long long> npts((size_t)n), off_pts((size_t)n + 1, 0), off_n((size_t)n + 1, 0),
-            off_nn((size_t)n + 1, 0);
-        for (int i = 0; i < n; ++i) {
-            const rp_fit_desc &d = descs[i];
-            RP_REQUIRE(d.atoms && d.Z && d.N > 0, "rp_fit: null input or N <= 0");
-            RP_REQUIRE(d.precision == RP_PREC_FP64 || d.precision == RP_PREC_MIXED, "rp_fit: unknown precision");
-            RP_REQUIRE((V_dev && V_dev[i]) || d.V, "rp_fit: no ESP values");
-            npts[i] = (long long)d.grid.n_grid[0] * d.grid.n_grid[1] * d.grid.n_grid[2];
-            RP_REQUIRE(npts[i] > 0 && npts[i] < (1LL << 31), "rp_fit: bad grid");
-            off_pts[i + 1] = off_pts[i] + npts[i];
-            off_n[i + 1] = off_n[i] + d.N;
-            off_nn[i + 1] = off_nn[i] + (long long)d.N * d.N;
-        }
-        // Work splits into host preparation and device stages so that the device never waits
-        // on the host inside the batch, and the cubes run as a pipeline of up to four groups:
-        // (1) the filters' host halves on the host workers, one pinned upload, and the filter
-        // launches of every group on their own streams; (2) while they run, the Ewald tables
-        // of every cube on the host workers, one pinned upload; (3) as each group's kept
-        // counts arrive, its normal equations go to the gram streams, so later groups'
-        // filters overlap earlier groups' grams.
-        constexpr int kLanes = 4;
-        const int lanes = ctx->timing ? 1 : kLanes;  // stage timing: one lane, each stage alone
-        auto glane = [&](int i) { return ctx->lane(i % lanes); };
-        auto flane = [&](int i) { return ctx->timing ? ctx->lane(0) : ctx->lane(kLanes + i % kLanes); };
-        const int ngroups = (n >= 64 && !ctx->timing) ? 4 : 1;
-        std::vector<int> g0((size_t)ngroups + 1);
-        for (int g = 0; g <= ngroups; ++g) g0[g] = (int)((long long)n * g / ngroups);
-        int32_t *kept = ctx->buf_t<int32_t>("fit_kept", (size_t)off_pts[n]);
-        double *Vc = ctx->buf_t<double>("fit_Vc", (size_t)off_pts[n]);
-        double *Vh = nullptr;
-        bool any_host = false;
-        for (int i = 0; i < n; ++i) any_host |= !(V_dev && V_dev[i]);
-        if (any_host) Vh = ctx->buf_t<double>("fit_V", (size_t)off_pts[n]);
-        long long *Md = ctx->buf_t<long long>("fit_M", (size_t)n);
-        long long *Mh = static_cast<long long *>(ctx->host_buf("fit_M", sizeof(long long) * n));
-        double *A = ctx->buf_t<double>("fit_A", (size_t)off_nn[n]);
-        double *b = ctx->buf_t<double>("fit_b", (size_t)off_n[n]);
-        double *q = ctx->buf_t<double>("fit_q", (size_t)off_n[n]);
-        double *vst = ctx->buf_t<double>("fit_vstats", 2 * (size_t)n);
-        int *clamps = ctx->buf_t<int>("fit_clamps", (size_t)n);
-        rp::status_clear(ctx, stream);
-        RP_CUDA(cudaMemsetAsync(clamps, 0, sizeof(int) * n, stream));
-        std::vector<cudaEvent_t> events;
-        auto record = [&](cudaStream_t st) {
-            cudaEvent_t ev;
-            RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-            events.push_back(ev);
-            RP_CUDA(cudaEventRecord(ev, st));
-            return ev;
-        };
-        struct EventGuard {  // destroyed on every exit (a recorded event may still be pending)
-            std::vector<cudaEvent_t> &e;
-            ~EventGuard() {
-                for (cudaEvent_t ev : e) cudaEventDestroy(ev);
-            }
-        } guard{events};
-        // 1. filters, group by group: the host plans a group (its workers), packs it into the
-        //    group's pinned arena and queues the upload, the grids and the filter launches, then
-        //    plans the next group while the device runs this one
-        while ((int)ctx->plan_pool.size() < n) ctx->plan_pool.emplace_back(new rp::FilterPlan());
-        auto plan = [&](int i) -> rp::FilterPlan & { return *ctx->plan_pool[(size_t)i]; };
-        {
-            const cudaEvent_t up = record(stream);  // every stream starts after the caller's work so far
-            for (int ln = 0; ln < kLanes; ++ln) {
-                RP_CUDA(cudaStreamWaitEvent(ctx->lane(ln), up, 0));
-                RP_CUDA(cudaStreamWaitEvent(flane(ln), up, 0));
-            }
-        }
-        const cudaStream_t copy_lane = ctx->lane(2 * kLanes);  // uploads: plans, grids, tables
-        RP_CUDA(cudaStreamWaitEvent(copy_lane, events.back(), 0));
-        std::vector<size_t> pl_off((size_t)n + 1, 0);
-        std::vector<cudaEvent_t> kept_ready((size_t)ngroups);
-        for (int g = 0; g < ngroups; ++g) {
-            const int i0 = g0[g], i1 = g0[g + 1];
-            ctx->parallel(i1 - i0, [&](int t) {
-                const rp_fit_desc &d = descs[i0 + t];
-                rp::filter_plan(&d.grid, d.atoms, d.Z, d.N, d.vdw_factor, d.vdw_max, plan(i0 + t));
-            });
-            pl_off[i0] = 0;
-            for (int i = i0; i < i1; ++i) pl_off[i + 1] = pl_off[i] + plan(i).bytes();
-            const std::string gtag = "fit_filter#" + std::to_string(g);
-            char *pl_dev = static_cast<char *>(ctx->buf(gtag, pl_off[i1]));
-            char *pl_host = static_cast<char *>(ctx->host_buf(gtag, pl_off[i1]));
-            ctx->parallel(i1 - i0, [&](int t) { plan(i0 + t).pack(pl_host + pl_off[i0 + t]); });
-            RP_CUDA(cudaMemcpyAsync(pl_dev, pl_host, pl_off[i1], cudaMemcpyHostToDevice, copy_lane));
-            for (int i = i0; i < i1; ++i)  // grids from host memory, this group's only
-                if (!(V_dev && V_dev[i]))
-                    RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], descs[i].V, sizeof(double) * npts[i],
-                                            cudaMemcpyHostToDevice, copy_lane));
-            const cudaEvent_t inputs = record(copy_lane);
-            for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(flane(ln), inputs, 0));
-            for (int i = i0; i < i1; ++i) {
-                const rp_fit_desc &d = descs[i];
-                const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
-                const int ln = i % lanes;
-                rp::filter_launch(ctx, plan(i), pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i], Md + i,
-                                  nullptr, flane(i), "#f" + std::to_string(ln), d.precision == RP_PREC_MIXED,
-                                  vst + 2 * i);
-            }
-            for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(stream, record(flane(ln)), 0));
-            RP_CUDA(cudaMemcpyAsync(Mh + i0, Md + i0, sizeof(long long) * (i1 - i0), cudaMemcpyDeviceToHost, stream));
-            kept_ready[g] = record(stream);
-        }
-        // 2. Ewald tables, written by the host workers straight into one pinned arena,
-        //    uploaded with a single copy on a stream of its own
-        std::vector<size_t> ew_off((size_t)n + 1, 0);
-        while ((int)ctx->ew_pool.size() < n) ctx->ew_pool.emplace_back(new rp_ewald());
-        for (int i = 0; i < n; ++i) {
-            size_t off9[9];
-            ews[i] = ctx->ew_pool[(size_t)i].get();
-            ews[i]->device = ctx->device;
-            ew_off[i + 1] = ew_off[i] + rp::ewald_layout(&descs[i].grid, descs[i].kmax, off9);
-        }
-        char *ew_dev = static_cast<char *>(ctx->buf("fit_ewald", ew_off[n]));
-        char *ew_host = static_cast<char *>(ctx->host_buf("fit_ewald", ew_off[n]));
-        ctx->parallel(n, [&](int i) {
-            rp::ewald_build_host(ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax, ew_host + ew_off[i]);
-        });
-        for (int i = 0; i < n; ++i) rp::ewald_place(ews[i], ew_dev + ew_off[i]);
-        RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, ew_off[n], cudaMemcpyHostToDevice, copy_lane));
-        const cudaEvent_t tables = record(copy_lane);
-        for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(glane(ln), tables, 0));
-        RP_CUDA(cudaStreamWaitEvent(stream, tables, 0));
-        // 3. normal equations, group by group as the kept counts arrive.  Mixed-precision fits
-        //    are spread over the gram streams (each with its own scratch), so one cube's small
-        //    kernels and launch gaps overlap another's; the FP64 comparator stays on the
-        //    caller's stream (its cuBLAS handle is shared).  Every cube's result is independent
-        //    of the stream it ran on.  A mixed fit takes the single pass (Phi straight to
-        //    digits, scaled by the a-priori bounds from the scaled vdW radii); a cube whose
-        //    values clamp (a cell the bound's argument does not cover) is redone below in
-        //    two passes.
-        std::vector<double> rn((size_t)off_n[n]);
-        for (int i = 0; i < n; ++i)
-            for (int a = 0; a < descs[i].N; ++a)
-                rn[off_n[i] + a] = descs[i].vdw_factor * rp::radius_of(descs[i].Z[a]);
-        std::vector<long long> M((size_t)n);
-        auto job = [&](int i) {
-            const rp_fit_desc &d = descs[i];
-            return rp::SolveJob{A + off_nn[i], b + off_n[i], d.N, d.n_groups, d.group_ptr, d.group_idx,
-                                d.resp_s, d.resp_t, d.qtot, q + off_n[i]};
-        };
-        std::vector<const double *> ginfo((size_t)ngroups);
-        for (int g = 0; g < ngroups; ++g) {
-            RP_CUDA(cudaEventSynchronize(kept_ready[g]));
-            for (int i = g0[g]; i < g0[g + 1]; ++i) {
-                M[i] = Mh[i];
-                if (M_out) M_out[i] = M[i];
-                RP_REQUIRE(M[i] > 0, "rp_fit: no grid point of cube " + std::to_string(i) + " survives the vdW filter");
-            }
-            for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(glane(ln), kept_ready[g], 0));
-            for (int i = g0[g]; i < g0[g + 1]; ++i) {
-                const rp_fit_desc &d = descs[i];
-                if (d.precision == RP_PREC_MIXED) {
-                    const int ln = i % lanes;
-                    rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i],
-                                   A + off_nn[i], b + off_n[i], nullptr, glane(ln), vst + 2 * i,
-                                   "#" + std::to_string(ln), rn.data() + off_n[i], clamps + i);
-                } else {
-                    rp::gram_fp64(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
-                                  b + off_n[i], nullptr, stream);
-                }
-            }
-            // 4. the group's constraint folds and bordered solves (one launch) on the caller's
-            //    stream, behind its normal equations and overlapping the next group's
-            for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(stream, record(glane(ln)), 0));
-            std::vector<rp::SolveJob> jobs;
-            for (int i = g0[g]; i < g0[g + 1]; ++i) jobs.push_back(job(i));
-            ginfo[g] = rp::solve_batch_async(ctx, jobs, stream, "#g" + std::to_string(g));
-        }
-        int *hclamps = static_cast<int *>(ctx->host_buf("fit_clamps", sizeof(int) * n));
-        RP_CUDA(cudaMemcpyAsync(hclamps, clamps, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
-        RP_CUDA(cudaStreamSynchronize(stream));
-        std::vector<double> info((size_t)n * 4);
-        for (int g = 0; g < ngroups; ++g)
-            std::copy(ginfo[g], ginfo[g] + 4 * (size_t)(g0[g + 1] - g0[g]), info.begin() + 4 * (size_t)g0[g]);
-        // 5. a cube whose values clamped: the two-pass fit, centred and scaled by the data, and
-        //    its solve again
-        ctx->last_fallbacks = 0;
-        std::vector<int> redo;
-        for (int i = 0; i < n; ++i)
-            if (hclamps[i] != 0) {
-                ++ctx->last_fallbacks;
-                redo.push_back(i);
-                const rp_fit_desc &d = descs[i];
-                rp::gram_mixed(ctx, ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], M[i], A + off_nn[i],
-                               b + off_n[i], nullptr, stream, vst + 2 * i, "");
-            }
-        if (!redo.empty()) {
-            std::vector<rp::SolveJob> jobs;
-            for (int i : redo) jobs.push_back(job(i));
-            std::vector<double> rinfo;
-            rp::solve_batch(ctx, jobs, rinfo, stream);
-            for (size_t t = 0; t < redo.size(); ++t)
-                std::copy(rinfo.begin() + 4 * t, rinfo.begin() + 4 * t + 4, info.begin() + 4 * (size_t)redo[t]);
-        }
-        rp::status_check(ctx, stream);
-        RP_CUDA(cudaMemcpyAsync(q_out, q, sizeof(double) * off_n[n], cudaMemcpyDeviceToHost, stream));
-        RP_CUDA(cudaStreamSynchronize(stream));
-        if (info_out) std::copy(info.begin(), info.end(), info_out);
-        for (int i = 0; i < n; ++i)
-            if (info[4 * (size_t)i + 3] != 0.0)
-                rp::fail(RP_E_SINGULAR, "rp_fit: bordered system of cube " + std::to_string(i) + " is singular");
+
+// One batch of the batched fit, from its enqueue to its completion.  Everything a batch
+// keeps between the two phases lives here; its device scratch, pinned staging, streams,
+// status words and host object pools are those of the ctx slot it runs in.
+struct BatchRun {
+    int slot = 0;
+    int prio = 0;  // stream priority class (rp_ctx::cur_prio) the batch runs at
+    int n = 0;
+    const rp_fit_desc *descs = nullptr;
+    double *q_out = nullptr;
+    int64_t *M_out = nullptr;
+    double *info_out = nullptr;
+    cudaStream_t stream = nullptr;
+    std::vector<long long> off_pts, off_n, off_nn, M;
+    std::vector<rp_ewald *> ews;
+    int32_t *kept = nullptr;
+    double *Vc = nullptr, *A = nullptr, *b = nullptr, *q = nullptr, *vst = nullptr;
+    int *clamps = nullptr;
+    int ngroups = 0;
+    std::vector<int> g0;
+    std::vector<const double *> ginfo;  // pinned solve words of each pipeline group
+    std::vector<SolvePending> gpend;    // each group's wide systems that may need FP64 factors
+    int *hclamps = nullptr;             // pinned clamp counts
+    double *hq = nullptr;               // pinned charges
+    std::vector<cudaEvent_t> events;
+    cudaEvent_t done = nullptr;         // every device step of the enqueue phase has run
+    ~BatchRun() {
+        for (cudaEvent_t ev : events) cudaEventDestroy(ev);
     }
-    // the pooled Ewald objects borrow the arena: nothing to free
+    SolveJob job(int i) const {
+        const rp_fit_desc &d = descs[i];
+        return SolveJob{A + off_nn[i], b + off_n[i], d.N, d.n_groups, d.group_ptr, d.group_idx,
+                        d.resp_s, d.resp_t, d.qtot, q + off_n[i]};
+    }
+};
+
+// Enqueue phase of the batched fit (throws rp::Error): filters, Ewald tables, normal
+// equations and bordered solves of every cube go to the device, with the only host waits
+// on each pipeline group's kept counts; the charges, clamp counts and solve words are
+// copied to pinned memory behind them and r.done is recorded.  Runs in slot ctx->cur_slot.
+void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
+                   int64_t *M_out, double *info_out, cudaStream_t stream, BatchRun &r) {
+    r.slot = ctx->cur_slot;
+    r.prio = ctx->cur_prio;
+    r.n = n;
+    r.descs = descs;
+    r.q_out = q_out;
+    r.M_out = M_out;
+    r.info_out = info_out;
+    r.stream = stream;
+    if (n == 0) return;
+    std::vector<long long> npts((size_t)n);
+    r.off_pts.assign((size_t)n + 1, 0);
+    r.off_n.assign((size_t)n + 1, 0);
+    r.off_nn.assign((size_t)n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        const rp_fit_desc &d = descs[i];
+        RP_REQUIRE(d.atoms && d.Z && d.N > 0, "rp_fit: null input or N <= 0");
+        RP_REQUIRE(d.precision == RP_PREC_FP64 || d.precision == RP_PREC_MIXED, "rp_fit: unknown precision");
+        RP_REQUIRE((V_dev && V_dev[i]) || d.V, "rp_fit: no ESP values");
+        npts[i] = (long long)d.grid.n_grid[0] * d.grid.n_grid[1] * d.grid.n_grid[2];
+        RP_REQUIRE(npts[i] > 0 && npts[i] < (1LL << 31), "rp_fit: bad grid");
+        r.off_pts[i + 1] = r.off_pts[i] + npts[i];
+        r.off_n[i + 1] = r.off_n[i] + d.N;
+        r.off_nn[i + 1] = r.off_nn[i] + (long long)d.N * d.N;
+    }
+    const std::vector<long long> &off_pts = r.off_pts, &off_n = r.off_n, &off_nn = r.off_nn;
+    // Work splits into host preparation and device stages so that the device never waits
+    // on the host inside the batch, and the cubes run as a pipeline of up to four groups:
+    // (1) the filters' host halves on the host workers, one pinned upload, and the filter
+    // launches of every group on their own streams; (2) while they run, the Ewald tables
+    // of every cube on the host workers, one pinned upload; (3) as each group's kept
+    // counts arrive, its normal equations go to the gram streams, so later groups'
+    // filters overlap earlier groups' grams.
+    constexpr int kLanes = 4;
+    const int lanes = ctx->timing ? 1 : kLanes;  // stage timing: one lane, each stage alone
+    auto glane = [&](int i) { return ctx->lane(i % lanes); };
+    auto flane = [&](int i) { return ctx->timing ? ctx->lane(0) : ctx->lane(kLanes + i % kLanes); };
+    const int ngroups = (n >= 64 && !ctx->timing) ? 4 : 1;
+    r.ngroups = ngroups;
+    r.g0.assign((size_t)ngroups + 1, 0);
+    std::vector<int> &g0 = r.g0;
+    for (int g = 0; g <= ngroups; ++g) g0[g] = (int)((long long)n * g / ngroups);
+    int32_t *kept = r.kept = ctx->buf_t<int32_t>("fit_kept", (size_t)off_pts[n]);
+    double *Vc = r.Vc = ctx->buf_t<double>("fit_Vc", (size_t)off_pts[n]);
+    double *Vh = nullptr;
+    bool any_host = false;
+    for (int i = 0; i < n; ++i) any_host |= !(V_dev && V_dev[i]);
+    if (any_host) Vh = ctx->buf_t<double>("fit_V", (size_t)off_pts[n]);
+    long long *Md = ctx->buf_t<long long>("fit_M", (size_t)n);
+    long long *Mh = static_cast<long long *>(ctx->host_buf("fit_M", sizeof(long long) * n));
+    double *A = r.A = ctx->buf_t<double>("fit_A", (size_t)off_nn[n]);
+    double *b = r.b = ctx->buf_t<double>("fit_b", (size_t)off_n[n]);
+    r.q = ctx->buf_t<double>("fit_q", (size_t)off_n[n]);
+    double *vst = r.vst = ctx->buf_t<double>("fit_vstats", 2 * (size_t)n);
+    int *clamps = r.clamps = ctx->buf_t<int>("fit_clamps", (size_t)n);
+    rp::status_clear(ctx, stream);
+    RP_CUDA(cudaMemsetAsync(clamps, 0, sizeof(int) * n, stream));
+    auto record = [&](cudaStream_t st) {
+        cudaEvent_t ev;
+        RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        r.events.push_back(ev);
+        RP_CUDA(cudaEventRecord(ev, st));
+        return ev;
+    };
+    // 1. filters, group by group: the host plans a group (its workers), packs it into the
+    //    group's pinned arena and queues the upload, the grids and the filter launches, then
+    //    plans the next group while the device runs this one
+    auto &plan_pool = ctx->plan_pool[ctx->cur_slot];
+    while ((int)plan_pool.size() < n) plan_pool.emplace_back(new rp::FilterPlan());
+    auto plan = [&](int i) -> rp::FilterPlan & { return *plan_pool[(size_t)i]; };
+    {
+        const cudaEvent_t up = record(stream);  // every stream starts after the caller's work so far
+        for (int ln = 0; ln < kLanes; ++ln) {
+            RP_CUDA(cudaStreamWaitEvent(ctx->lane(ln), up, 0));
+            RP_CUDA(cudaStreamWaitEvent(flane(ln), up, 0));
+        }
+    }
+    const cudaStream_t copy_lane = ctx->lane(2 * kLanes);  // uploads: plans, grids, tables
+    RP_CUDA(cudaStreamWaitEvent(copy_lane, r.events.back(), 0));
+    std::vector<size_t> pl_off((size_t)n + 1, 0);
+    std::vector<cudaEvent_t> kept_ready((size_t)ngroups);
+    for (int g = 0; g < ngroups; ++g) {
+        const int i0 = g0[g], i1 = g0[g + 1];
+        ctx->parallel(i1 - i0, [&](int t) {
+            const rp_fit_desc &d = descs[i0 + t];
+            rp::filter_plan(&d.grid, d.atoms, d.Z, d.N, d.vdw_factor, d.vdw_max, plan(i0 + t));
+        });
+        pl_off[i0] = 0;
+        for (int i = i0; i < i1; ++i) pl_off[i + 1] = pl_off[i] + plan(i).bytes();
+        const std::string gtag = "fit_filter#" + std::to_string(g);
+        char *pl_dev = static_cast<char *>(ctx->buf(gtag, pl_off[i1]));
+        char *pl_host = static_cast<char *>(ctx->host_buf(gtag, pl_off[i1]));
+        ctx->parallel(i1 - i0, [&](int t) { plan(i0 + t).pack(pl_host + pl_off[i0 + t]); });
+        RP_CUDA(cudaMemcpyAsync(pl_dev, pl_host, pl_off[i1], cudaMemcpyHostToDevice, copy_lane));
+        for (int i = i0; i < i1; ++i)  // grids from host memory, this group's only
+            if (!(V_dev && V_dev[i]))
+                RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], descs[i].V, sizeof(double) * npts[i],
+                                        cudaMemcpyHostToDevice, copy_lane));
+        const cudaEvent_t inputs = record(copy_lane);
+        for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(flane(ln), inputs, 0));
+        for (int i = i0; i < i1; ++i) {
+            const rp_fit_desc &d = descs[i];
+            const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
+            const int ln = i % lanes;
+            rp::filter_launch(ctx, plan(i), pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i], Md + i,
+                              nullptr, flane(i), "#f" + std::to_string(ln), d.precision == RP_PREC_MIXED,
+                              vst + 2 * i);
+        }
+        for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(stream, record(flane(ln)), 0));
+        RP_CUDA(cudaMemcpyAsync(Mh + i0, Md + i0, sizeof(long long) * (i1 - i0), cudaMemcpyDeviceToHost, stream));
+        kept_ready[g] = record(stream);
+    }
+    // 2. Ewald tables, written by the host workers straight into one pinned arena,
+    //    uploaded with a single copy on a stream of its own
+    std::vector<size_t> ew_off((size_t)n + 1, 0);
+    auto &ew_pool = ctx->ew_pool[ctx->cur_slot];
+    while ((int)ew_pool.size() < n) ew_pool.emplace_back(new rp_ewald());
+    r.ews.assign((size_t)n, nullptr);
+    for (int i = 0; i < n; ++i) {
+        size_t off9[9];
+        r.ews[i] = ew_pool[(size_t)i].get();
+        r.ews[i]->device = ctx->device;
+        ew_off[i + 1] = ew_off[i] + rp::ewald_layout(&descs[i].grid, descs[i].kmax, off9);
+    }
+    char *ew_dev = static_cast<char *>(ctx->buf("fit_ewald", ew_off[n]));
+    char *ew_host = static_cast<char *>(ctx->host_buf("fit_ewald", ew_off[n]));
+    ctx->parallel(n, [&](int i) {
+        rp::ewald_build_host(r.ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax, ew_host + ew_off[i]);
+    });
+    for (int i = 0; i < n; ++i) rp::ewald_place(r.ews[i], ew_dev + ew_off[i]);
+    RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, ew_off[n], cudaMemcpyHostToDevice, copy_lane));
+    const cudaEvent_t tables = record(copy_lane);
+    for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(glane(ln), tables, 0));
+    RP_CUDA(cudaStreamWaitEvent(stream, tables, 0));
+    // 3. normal equations, group by group as the kept counts arrive.  Mixed-precision fits
+    //    are spread over the gram streams (each with its own scratch), so one cube's small
+    //    kernels and launch gaps overlap another's; the FP64 comparator stays on the
+    //    caller's stream (its cuBLAS handle is shared).  Every cube's result is independent
+    //    of the stream it ran on.  A mixed fit takes the single pass (Phi straight to
+    //    digits, scaled by the a-priori bounds from the scaled vdW radii); a cube whose
+    //    values clamp (a cell the bound's argument does not cover) is redone at completion
+    //    in two passes.
+    std::vector<double> rn((size_t)off_n[n]);
+    for (int i = 0; i < n; ++i)
+        for (int a = 0; a < descs[i].N; ++a)
+            rn[off_n[i] + a] = descs[i].vdw_factor * rp::radius_of(descs[i].Z[a]);
+    r.M.assign((size_t)n, 0);
+    r.ginfo.assign((size_t)ngroups, nullptr);
+    r.gpend.assign((size_t)ngroups, SolvePending{});
+    for (int g = 0; g < ngroups; ++g) {
+        RP_CUDA(cudaEventSynchronize(kept_ready[g]));
+        for (int i = g0[g]; i < g0[g + 1]; ++i) {
+            r.M[i] = Mh[i];
+            if (M_out) M_out[i] = r.M[i];
+            RP_REQUIRE(r.M[i] > 0, "rp_fit: no grid point of cube " + std::to_string(i) + " survives the vdW filter");
+        }
+        for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(glane(ln), kept_ready[g], 0));
+        for (int i = g0[g]; i < g0[g + 1]; ++i) {
+            const rp_fit_desc &d = descs[i];
+            if (d.precision == RP_PREC_MIXED) {
+                const int ln = i % lanes;
+                rp::gram_mixed(ctx, r.ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], r.M[i],
+                               A + off_nn[i], b + off_n[i], nullptr, glane(ln), vst + 2 * i,
+                               "#" + std::to_string(ln), rn.data() + off_n[i], clamps + i);
+            } else {
+                rp::gram_fp64(ctx, r.ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], r.M[i],
+                              A + off_nn[i], b + off_n[i], nullptr, stream);
+            }
+        }
+        // 4. the group's constraint folds and bordered solves (one launch) on the caller's
+        //    stream, behind its normal equations and overlapping the next group's
+        for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(stream, record(glane(ln)), 0));
+        std::vector<rp::SolveJob> jobs;
+        for (int i = g0[g]; i < g0[g + 1]; ++i) jobs.push_back(r.job(i));
+        r.ginfo[g] = rp::solve_batch_async(ctx, jobs, stream, "#g" + std::to_string(g), &r.gpend[g]);
+    }
+    // 5. the results to pinned memory; r.done marks the end of the device work
+    r.hclamps = static_cast<int *>(ctx->host_buf("fit_clamps", sizeof(int) * n));
+    RP_CUDA(cudaMemcpyAsync(r.hclamps, clamps, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
+    r.hq = static_cast<double *>(ctx->host_buf("fit_qh", sizeof(double) * off_n[n]));
+    RP_CUDA(cudaMemcpyAsync(r.hq, r.q, sizeof(double) * off_n[n], cudaMemcpyDeviceToHost, stream));
+    r.done = record(stream);
 }
 
-// Worker of the asynchronous batches: runs the queued batches in order on the ctx's device.
+// Completion phase (throws rp::Error): waits for r.done, refits cubes whose values clamped
+// (two passes) or whose conditioning calls for FP64 (escalation), and writes the charges,
+// kept counts and info words.  Runs in slot r.slot (ctx->cur_slot must be r.slot).
+void batch_complete(rp_ctx *ctx, BatchRun &r) {
+    const int n = r.n;
+    if (n == 0) return;
+    const cudaStream_t stream = r.stream;
+    RP_CUDA(cudaEventSynchronize(r.done));
+    bool changed = false;
+    for (SolvePending &pd : r.gpend)  // wide systems whose FP32 refinement stalled: FP64 factors
+        if (pd.any_wide) {
+            rp::solve_wide_fp64(ctx, pd, stream);
+            changed = true;
+        }
+    constexpr int W = RP_FIT_INFO_WORDS;
+    std::vector<double> info((size_t)n * W, 0.0);
+    // a cube's record from its solve's words (rp::kSolveInfo per system); unknowns[i] = n+1
+    std::vector<double> unknowns((size_t)n, 1.0);
+    auto take = [&](int i, const double *h) {
+        double *o = info.data() + (size_t)W * i;
+        unknowns[i] = std::max(1.0, h[5]);
+        o[0] = h[0];  // refined residual
+        o[1] = h[1];  // min |pivot|
+        o[2] = h[2];  // max |pivot|
+        o[3] = h[3];  // singular flag
+        o[4] = h[4];  // kappa
+        o[5] = h[7];  // factorisation path
+    };
+    for (int g = 0; g < r.ngroups; ++g)
+        for (int i = r.g0[g]; i < r.g0[g + 1]; ++i) {
+            take(i, r.ginfo[g] + (size_t)rp::kSolveInfo * (i - r.g0[g]));
+            info[(size_t)W * i + 6] = r.descs[i].precision;
+        }
+    auto resolve = [&](const std::vector<int> &cubes, int flag, int precision) {
+        std::vector<rp::SolveJob> jobs;
+        for (int i : cubes) jobs.push_back(r.job(i));
+        std::vector<double> rinfo;
+        rp::solve_batch(ctx, jobs, rinfo, stream);
+        for (size_t t = 0; t < cubes.size(); ++t) {
+            take(cubes[t], rinfo.data() + (size_t)rp::kSolveInfo * t);
+            info[(size_t)W * cubes[t] + 6] = precision;
+            info[(size_t)W * cubes[t] + 7] = (double)((int)info[(size_t)W * cubes[t] + 7] | flag);
+        }
+        changed = true;
+    };
+    // a cube whose values clamped: the two-pass fit, centred and scaled by the data, and
+    // its solve again
+    ctx->last_fallbacks = 0;
+    std::vector<int> redo;
+    for (int i = 0; i < n; ++i)
+        if (r.hclamps[i] != 0) {
+            ++ctx->last_fallbacks;
+            redo.push_back(i);
+            const rp_fit_desc &d = r.descs[i];
+            rp::gram_mixed(ctx, r.ews[i], d.atoms, d.N, r.kept + r.off_pts[i], r.Vc + r.off_pts[i], r.M[i],
+                           r.A + r.off_nn[i], r.b + r.off_n[i], nullptr, stream, r.vst + 2 * i, "");
+        }
+    if (!redo.empty()) resolve(redo, RP_FIT_TWO_PASS, RP_PREC_MIXED);
+    rp::status_check(ctx, stream);
+    // escalation: a mixed-precision cube whose bordered system is so ill-conditioned that
+    // the Gram's rounding (~1e-7 relative) could move its charges visibly (kappa / (n+1)
+    // above the ctx's limit) is fitted again in plain FP64
+    std::vector<int> esc;
+    if (ctx->kappa_limit > 0.0)
+        for (int i = 0; i < n; ++i)
+            if (r.descs[i].precision == RP_PREC_MIXED && info[(size_t)W * i + 3] == 0.0 &&
+                !(info[(size_t)W * i + 4] / unknowns[i] <= ctx->kappa_limit))
+                esc.push_back(i);
+    ctx->last_escalations = (int)esc.size();
+    if (!esc.empty()) {
+        for (int i : esc) {
+            const rp_fit_desc &d = r.descs[i];
+            rp::gram_fp64(ctx, r.ews[i], d.atoms, d.N, r.kept + r.off_pts[i], r.Vc + r.off_pts[i], r.M[i],
+                          r.A + r.off_nn[i], r.b + r.off_n[i], nullptr, stream);
+        }
+        resolve(esc, RP_FIT_ESCALATED, RP_PREC_FP64);
+    }
+    if (changed) {
+        RP_CUDA(cudaMemcpyAsync(r.hq, r.q, sizeof(double) * r.off_n[n], cudaMemcpyDeviceToHost, stream));
+        RP_CUDA(cudaStreamSynchronize(stream));
+    }
+    std::copy(r.hq, r.hq + r.off_n[n], r.q_out);
+    if (r.info_out) std::copy(info.begin(), info.end(), r.info_out);
+    for (int i = 0; i < n; ++i)
+        if (info[(size_t)W * i + 3] != 0.0)
+            rp::fail(RP_E_SINGULAR, "rp_fit: bordered system of cube " + std::to_string(i) + " is singular");
+}
+
+// The batched fit on the caller's thread, in slot 0 (the pooled Ewald objects borrow the
+// slot's arena: nothing to free).
+void fit_batch_body(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
+                    int64_t *M_out, double *info_out, cudaStream_t stream) {
+    ctx->cur_slot = 0;
+    ctx->cur_prio = 0;
+    BatchRun r;
+    batch_enqueue(ctx, n, descs, V_dev, q_out, M_out, info_out, stream, r);
+    batch_complete(ctx, r);
+}
+
+// Worker of the asynchronous batches.  Up to kBatchSlots batches are in flight at once, each
+// in a slot of its own (scratch, pinned staging, streams, status words), so a batch
+// submitted while others run starts on the device at once and overlaps them; batches are
+// started in submission order and retired as they finish, in any order.
 void batch_server_loop(rp_ctx *ctx) {
     BatchServer &sv = *ctx->server;
     cudaSetDevice(ctx->device);
-    std::unique_lock<std::mutex> lk(sv.mu);
-    for (;;) {
-        sv.cv.wait(lk, [&] { return sv.stop || !sv.queue.empty(); });
-        if (sv.stop) return;
-        BatchServer::Job job = std::move(sv.queue.front());
-        sv.queue.pop_front();
-        lk.unlock();
+    struct Flight {
+        BatchServer::Job job;
+        std::unique_ptr<BatchRun> run;
         int status = RP_OK;
         std::string msg;
-        try {
-            fit_batch_body(ctx, (int)job.descs.size(), job.descs.data(), job.has_vdev ? job.vdev.data() : nullptr,
-                           job.q_out, job.M_out, job.info_out, ctx->lane(2 * 4 + 1));
-        } catch (const Error &e) {
-            status = e.code;
-            msg = e.msg;
-        } catch (const std::exception &e) {
-            status = RP_E_ARG;
-            msg = e.what();
+    };
+    std::vector<std::unique_ptr<Flight>> flights;
+    bool busy[kBatchSlots] = {};
+    auto failed = [](Flight &f, int code, const std::string &m) {
+        if (f.status == RP_OK) {
+            f.status = code;
+            f.msg = m;
         }
-        lk.lock();
-        sv.done[job.ticket] = {status, msg};
-        sv.finished.notify_all();
+    };
+    std::unique_lock<std::mutex> lk(sv.mu);
+    for (;;) {
+        // 1. retire every batch whose device work has finished (or that failed to enqueue)
+        bool progressed = false;
+        for (size_t k = 0; k < flights.size();) {
+            Flight &f = *flights[k];
+            const bool ready =
+                f.status != RP_OK || !f.run->done || cudaEventQuery(f.run->done) != cudaErrorNotReady;
+            if (!ready) {
+                ++k;
+                continue;
+            }
+            lk.unlock();
+            ctx->cur_slot = f.run->slot;
+            ctx->cur_prio = f.run->prio;
+            try {
+                if (f.status == RP_OK) {
+                    batch_complete(ctx, *f.run);
+                } else {  // a failed enqueue may have left work on the slot's streams
+                    for (int ln = 0; ln < kSlotLanes; ++ln) cudaStreamSynchronize(ctx->lane(ln));
+                    cudaGetLastError();
+                }
+            } catch (const Error &e) {
+                failed(f, e.code, e.msg);
+            } catch (const std::exception &e) {
+                failed(f, RP_E_ARG, e.what());
+            }
+            lk.lock();
+            busy[f.run->slot] = false;
+            sv.done[f.job.ticket] = {f.status, f.msg};
+            sv.finished.notify_all();
+            flights.erase(flights.begin() + (long)k);
+            progressed = true;
+        }
+        if (sv.stop && flights.empty()) return;
+        // 2. start the oldest queued batch in a free slot
+        int free_slot = -1;
+        for (int q = 0; q < kBatchSlots && free_slot < 0; ++q)
+            if (!busy[q]) free_slot = q;
+        if (!sv.stop && !sv.queue.empty() && free_slot >= 0) {
+            std::unique_ptr<Flight> f(new Flight());
+            f->job = std::move(sv.queue.front());
+            sv.queue.pop_front();
+            busy[free_slot] = true;
+            lk.unlock();
+            f->run.reset(new BatchRun());
+            f->run->slot = free_slot;
+            ctx->cur_slot = free_slot;
+            {  // a batch of small cubes runs at the greatest stream priority (kLowPriorityWork)
+                double work = 0.0;
+                for (const rp_fit_desc &d : f->job.descs)
+                    work = std::max(work, (double)d.grid.n_grid[0] * d.grid.n_grid[1] * d.grid.n_grid[2] * d.N);
+                ctx->cur_prio = work < kLowPriorityWork ? 1 : 0;
+            }
+            f->run->prio = ctx->cur_prio;
+            try {
+                const BatchServer::Job &j = f->job;
+                batch_enqueue(ctx, (int)j.descs.size(), j.descs.data(), j.has_vdev ? j.vdev.data() : nullptr,
+                              j.q_out, j.M_out, j.info_out, ctx->lane(kSlotLanes - 1), *f->run);
+            } catch (const Error &e) {
+                failed(*f, e.code, e.msg);
+            } catch (const std::exception &e) {
+                failed(*f, RP_E_ARG, e.what());
+            }
+            f->run->slot = free_slot;
+            lk.lock();
+            flights.push_back(std::move(f));
+            continue;
+        }
+        if (progressed) continue;
+        if (flights.empty())
+            sv.cv.wait(lk, [&] { return sv.stop || !sv.queue.empty(); });
+        else  // device work in flight: poll its events, and wake early for new submissions
+            sv.cv.wait_for(lk, std::chrono::microseconds(100));
     }
 }
 
@@ -536,6 +725,12 @@ int rp_batch_wait(rp_ctx *ctx, long long ticket, int *status) { return batch_res
 int rp_launch_count(long long *out) {
     if (!out) return RP_E_ARG;
     *out = rp::g_launches.load();
+    return RP_OK;
+}
+
+int rp_set_kappa_limit(rp_ctx *ctx, double kappa_max) {
+    if (!ctx || !(kappa_max >= 0.0)) return RP_E_ARG;
+    ctx->kappa_limit = kappa_max;
     return RP_OK;
 }
 

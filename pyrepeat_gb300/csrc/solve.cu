@@ -33,29 +33,6 @@
 
 namespace rp {
 
-struct SolveDesc {
-    const double *A;      // N x N input
-    const double *b;      // N input
-    int N;                // original atoms
-    int n;                // reduced atoms
-    const int *mem_ptr;   // n+1, CSR of members per reduced index
-    const int *mem_idx;   // members (original atom indices)
-    const double *resp_s; // n (per reduced index, already mapped) or null
-    const double *resp_t; // n
-    const int *map;       // N: reduced index of each original atom
-    double qtot;
-    double *As;           // (n+1)^2 work: bordered matrix, then LU
-    double *A0;           // (n+1)^2 copy of the bordered matrix (for refinement)
-    double *bs;           // n+1 rhs
-    double *x;            // n+1 solution
-    double *r;            // n+1 residual / correction
-    int *perm;            // n+1 pivot rows
-    double *q;            // N out
-    double *info;         // 4 out: residual inf-norm, min|piv|, max|piv|, singular flag
-    double *pre;          // null, or {flag, min|piv|, max|piv|} of a wide factorisation already in As
-    int wide64;           // As holds wide FP64 factors: skip the FP32 stage and the in-CTA FP64 LU
-};
-
 namespace {
 
 __global__ void build_bordered_kernel(SolveDesc d) {
@@ -459,6 +436,86 @@ __device__ void lu_apply_f32(const float *__restrict__ LU, const int *__restrict
         __syncthreads();
     }
 }
+// sum over the block, fixed order (every thread gets the result)
+__device__ double block_sum(double v, double *sv) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sv[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < kLU / 32; ++w) t += sv[w];
+    return t;
+}
+
+// d.r <- K^{-1} d.r with the factors that solved the system: FP32 (in the first half of As,
+// through the FP32 shared vectors ys/xs) or FP64 (in As).  Non-finite FP32 results (a system
+// far beyond FP32) read as 1e300.
+__device__ void apply_inverse(const SolveDesc &d, int n1, bool f32, float *ys, float *xs) {
+    if (f32) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < n1; t += kLU) ys[t] = (float)d.r[t];
+        lu_apply_f32(reinterpret_cast<const float *>(d.As), d.perm, n1, ys, xs);
+        for (int t = threadIdx.x; t < n1; t += kLU) {
+            const float v = xs[t];
+            d.r[t] = isfinite(v) ? (double)v : 1e300;
+        }
+        __syncthreads();
+    } else {
+        lu_apply(d.As, d.perm, n1, d.r);
+        __syncthreads();
+    }
+}
+
+// Estimate of ||K^{-1}||_1 for the symmetric bordered matrix K (so K^{-T} = K^{-1}):
+// Hager's method (W. W. Hager, "Condition estimates", SIAM J. Sci. Stat. Comput. 5 (1984)
+// 311-316) with Higham's extra test vector (N. J. Higham, ACM TOMS 14 (1988) 381-396),
+// at most four sign iterations.  A lower bound that is almost always within a small factor.
+// Uses d.r as the work vector.
+__device__ double inverse_norm1_estimate(const SolveDesc &d, int n1, bool f32, float *fsh, double *sv, int *si,
+                                         double *piv_v, int *piv_i) {
+    float *ys = fsh, *xs = fsh + n1;
+    for (int t = threadIdx.x; t < n1; t += kLU) d.r[t] = 1.0 / (double)n1;
+    apply_inverse(d, n1, f32, ys, xs);
+    double a = 0.0;
+    for (int t = threadIdx.x; t < n1; t += kLU) a += fabs(d.r[t]);
+    double est = block_sum(a, sv);
+    int jprev = -1;
+    for (int it = 0; it < 4; ++it) {
+        for (int t = threadIdx.x; t < n1; t += kLU) d.r[t] = d.r[t] >= 0.0 ? 1.0 : -1.0;
+        apply_inverse(d, n1, f32, ys, xs);  // z = K^{-T} sign(y)
+        double best = -1.0, zsum = 0.0;
+        int bi = 0x7fffffff;
+        for (int t = threadIdx.x; t < n1; t += kLU) {
+            const double v = fabs(d.r[t]);
+            zsum += d.r[t];
+            if (v > best || (v == best && t < bi)) { best = v; bi = t; }
+        }
+        zsum = block_sum(zsum, sv);
+        block_argmax(best, bi, sv, si, piv_v, piv_i);
+        const double zmax = *piv_v;
+        const int j = *piv_i;
+        const double ztx = jprev < 0 ? zsum / (double)n1 : d.r[jprev];
+        __syncthreads();
+        if (!(zmax > ztx)) break;  // uniform: every thread read the same values
+        for (int t = threadIdx.x; t < n1; t += kLU) d.r[t] = t == j ? 1.0 : 0.0;
+        apply_inverse(d, n1, f32, ys, xs);
+        double b = 0.0;
+        for (int t = threadIdx.x; t < n1; t += kLU) b += fabs(d.r[t]);
+        b = block_sum(b, sv);
+        if (!(b > est)) break;
+        est = b;
+        jprev = j;
+    }
+    for (int t = threadIdx.x; t < n1; t += kLU)
+        d.r[t] = ((t & 1) ? -1.0 : 1.0) * (1.0 + (double)t / (double)max(n1 - 1, 1));
+    apply_inverse(d, n1, f32, ys, xs);
+    double c = 0.0;
+    for (int t = threadIdx.x; t < n1; t += kLU) c += fabs(d.r[t]);
+    c = 2.0 * block_sum(c, sv) / (3.0 * (double)n1);
+    est = fmax(est, c);
+    return est < 1e300 ? est : 1e300;
+}
+
 constexpr int kRefineMax = 30;  // and stop early once a step no longer halves the residual
 // systems factored across the GPU (FP32 first, FP64 when the FP32 refinement does not
 // converge): n1 in [kLUWideMin, kLUWideMax], FP64 up to kLUWide64Max; the bounds are the
@@ -491,7 +548,7 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
     __shared__ double piv_v;
     __shared__ int piv_i;
     double pmin = 1e308, pmax = 0.0, res = 0.0;
-    int singular = 0;
+    int singular = 0, steps = 0;
     bool done = false;
 
     // ---- FP32 LU + FP64-residual refinement
@@ -534,6 +591,7 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
                     break;
                 }
                 const double inv = 1.0 / rm;
+                ++steps;
                 for (int t = threadIdx.x; t < n1; t += kLU) ys[t] = (float)(d.r[t] * inv);
                 lu_apply_f32(L, d.perm, n1, ys, xs);
                 for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] += (double)xs[t] * rm;
@@ -564,6 +622,7 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
     }
 
     // ---- fallback: FP64 LU with one step of FP64 refinement
+    const bool f32_solved = done;
     if (!done) {
         double *A = d.As;
         if (d.wide64) {  // factored across the GPU (lu_wide_factor<double>)
@@ -634,11 +693,27 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
         }
         res = block_max(rmax, sv);
     }
+    // ---- conditioning: kappa = ||A||_1 ||K^{-1}||_1 with A the folded normal matrix (RESP
+    // included, the border excluded) and K the bordered matrix.  A relative error e in A moves
+    // the solution by about e * kappa * |q| at worst, so kappa says how much of the Gram's
+    // rounding reaches the charges (the fit escalates a mixed-precision cube beyond a limit).
+    double anorm = 0.0;
+    for (int c = threadIdx.x; c < d.n; c += kLU) {
+        double sacc = 0.0;
+        for (int rr = 0; rr < d.n; ++rr) sacc += fabs(d.A0[(size_t)rr * n1 + c]);
+        anorm = fmax(anorm, sacc);
+    }
+    anorm = block_max(anorm, sv);
+    const double kinv = inverse_norm1_estimate(d, n1, f32_solved, fsh, sv, si, &piv_v, &piv_i);
     if (threadIdx.x == 0) {
         d.info[0] = res;
         d.info[1] = pmin;
         d.info[2] = pmax;
         d.info[3] = singular;
+        d.info[4] = fmin(anorm * kinv, 1e300);
+        d.info[5] = n1;
+        d.info[6] = steps;
+        d.info[7] = f32_solved ? (d.pre ? 1.0 : 0.0) : (d.wide64 ? 3.0 : 2.0);
     }
     __syncthreads();
     // expand to all atoms
@@ -944,7 +1019,7 @@ static void host_fold(int N, const std::vector<double> &A, const std::vector<dou
 }
 
 const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, cudaStream_t stream,
-                                const std::string &tag) {
+                                const std::string &tag, SolvePending *pend) {
     const int nj = (int)jobs.size();
     if (nj == 0) return nullptr;
     std::vector<FoldPlan> plans((size_t)nj);
@@ -972,7 +1047,7 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
     double *x = ctx->buf_t<double>("s_x" + tag, n_red);
     double *r = ctx->buf_t<double>("s_r" + tag, n_red);
     int *perm = ctx->buf_t<int>("s_perm" + tag, n_red);
-    double *d_info = ctx->buf_t<double>("s_info" + tag, (size_t)nj * 4);
+    double *d_info = ctx->buf_t<double>("s_info" + tag, (size_t)nj * kSolveInfo);
     double *d_pre = ctx->buf_t<double>("s_pre" + tag, (size_t)nj * 3);
     SolveDesc *d_desc = ctx->buf_t<SolveDesc>("s_desc" + tag, (size_t)nj);
     // host staging of the small per-system tables, one upload each
@@ -998,7 +1073,7 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
         d.resp_s = J.resp_s ? d_rs + o_red : nullptr; d.resp_t = J.resp_s ? d_rt + o_red : nullptr;
         d.map = d_map + o_map; d.qtot = J.qtot;
         d.As = As + o_sq; d.A0 = A0 + o_sq; d.bs = bs + o_red; d.x = x + o_red; d.r = r + o_red;
-        d.perm = perm + o_red; d.q = J.q; d.info = d_info + 4 * (size_t)j;
+        d.perm = perm + o_red; d.q = J.q; d.info = d_info + kSolveInfo * (size_t)j;
         o_map += J.N;
         o_mptr += p.mem_ptr.size();
         o_midx += std::max<size_t>(p.mem_idx.size(), 1);
@@ -1059,6 +1134,7 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
     }
     // large systems: factored across the GPU first (lu_solve_refine_kernel then refines them)
     bool any_wide = false;
+    if (pend) *pend = SolvePending{};
     for (int j = 0; j < nj; ++j) {
         const int n1 = plans[j].n + 1;
         if (n1 < kLUWideMin || n1 > kLUWideMax) continue;
@@ -1077,46 +1153,68 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
         lu_solve_refine_kernel<<<nj, kLU, solve_smem_bytes(n1max), stream>>>(d_desc);
         RP_LAUNCH_CHECK();
     }
+    double *h_info = static_cast<double *>(ctx->host_buf("s_info" + tag, sizeof(double) * kSolveInfo * nj));
     if (any_wide) {
-        // wide systems whose FP32 refinement did not converge (flag 2): FP64 factors across the
-        // GPU, then the refinement kernel again on those systems alone (the host waits here)
+        // wide systems whose FP32 refinement did not converge (flag 2) are factored again in FP64:
+        // their flags go to pinned memory, and solve_wide_fp64 (now, or, with `pend`, when the
+        // caller's completion reaches it) reads them and redoes those systems
         double *h_pre = static_cast<double *>(ctx->host_buf("s_preh" + tag, sizeof(double) * 3 * nj));
         RP_CUDA(cudaMemcpyAsync(h_pre, d_pre, sizeof(double) * 3 * nj, cudaMemcpyDeviceToHost, stream));
-        RP_CUDA(cudaStreamSynchronize(stream));
-        std::vector<SolveDesc> redo;
-        int n1max = 1;
-        for (int j = 0; j < nj; ++j) {
-            if (!descs[j].pre || h_pre[3 * j] != 2.0) continue;
-            SolveDesc d = descs[j];
-            d.wide64 = 1;
-            const int n1 = plans[j].n + 1;
-            StageTimer tt(ctx, "solve_lu_wide64", stream);
-            lu_wide_factor<double>(ctx, d, n1, stream);
-            redo.push_back(d);
-            n1max = std::max(n1max, n1);
-        }
-        if (!redo.empty()) {
-            SolveDesc *d_redo = ctx->buf_t<SolveDesc>("s_desc64" + tag, redo.size());
-            SolveDesc *h_redo = static_cast<SolveDesc *>(ctx->host_buf("s_stage64" + tag, sizeof(SolveDesc) * redo.size()));
-            std::memcpy(h_redo, redo.data(), sizeof(SolveDesc) * redo.size());
-            RP_CUDA(cudaMemcpyAsync(d_redo, h_redo, sizeof(SolveDesc) * redo.size(), cudaMemcpyHostToDevice, stream));
-            StageTimer tt(ctx, "solve_lu", stream);
-            lu_solve_refine_kernel<<<(int)redo.size(), kLU, solve_smem_bytes(n1max), stream>>>(d_redo);
-            RP_LAUNCH_CHECK();
+        SolvePending local;
+        SolvePending &pd = pend ? *pend : local;
+        pd.any_wide = true;
+        pd.tag = tag;
+        pd.h_pre = h_pre;
+        pd.h_info = h_info;
+        pd.d_info = d_info;
+        pd.descs = descs;
+        pd.n1.resize((size_t)nj);
+        for (int j = 0; j < nj; ++j) pd.n1[j] = plans[j].n + 1;
+        if (!pend) {
+            RP_CUDA(cudaStreamSynchronize(stream));
+            solve_wide_fp64(ctx, pd, stream);
         }
     }
-    double *h_info = static_cast<double *>(ctx->host_buf("s_info" + tag, sizeof(double) * 4 * nj));
-    RP_CUDA(cudaMemcpyAsync(h_info, d_info, sizeof(double) * 4 * nj, cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaMemcpyAsync(h_info, d_info, sizeof(double) * kSolveInfo * nj, cudaMemcpyDeviceToHost, stream));
     return h_info;
+}
+
+void solve_wide_fp64(rp_ctx *ctx, SolvePending &pd, cudaStream_t stream) {
+    if (!pd.any_wide) return;
+    pd.any_wide = false;
+    const int nj = (int)pd.descs.size();
+    std::vector<SolveDesc> redo;
+    int n1max = 1;
+    for (int j = 0; j < nj; ++j) {
+        if (!pd.descs[j].pre || pd.h_pre[3 * j] != 2.0) continue;
+        SolveDesc d = pd.descs[j];
+        d.wide64 = 1;
+        StageTimer tt(ctx, "solve_lu_wide64", stream);
+        lu_wide_factor<double>(ctx, d, pd.n1[j], stream);
+        redo.push_back(d);
+        n1max = std::max(n1max, pd.n1[j]);
+    }
+    if (redo.empty()) return;
+    SolveDesc *d_redo = ctx->buf_t<SolveDesc>("s_desc64" + pd.tag, redo.size());
+    SolveDesc *h_redo = static_cast<SolveDesc *>(ctx->host_buf("s_stage64" + pd.tag, sizeof(SolveDesc) * redo.size()));
+    std::memcpy(h_redo, redo.data(), sizeof(SolveDesc) * redo.size());
+    RP_CUDA(cudaMemcpyAsync(d_redo, h_redo, sizeof(SolveDesc) * redo.size(), cudaMemcpyHostToDevice, stream));
+    {
+        StageTimer tt(ctx, "solve_lu", stream);
+        lu_solve_refine_kernel<<<(int)redo.size(), kLU, solve_smem_bytes(n1max), stream>>>(d_redo);
+        RP_LAUNCH_CHECK();
+    }
+    RP_CUDA(cudaMemcpyAsync(pd.h_info, pd.d_info, sizeof(double) * kSolveInfo * nj, cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaStreamSynchronize(stream));
 }
 
 void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream) {
     const int nj = (int)jobs.size();
-    info.assign((size_t)nj * 4, 0.0);
+    info.assign((size_t)nj * kSolveInfo, 0.0);
     if (nj == 0) return;
     const double *h = solve_batch_async(ctx, jobs, stream, "");
     RP_CUDA(cudaStreamSynchronize(stream));
-    std::copy(h, h + 4 * (size_t)nj, info.begin());
+    std::copy(h, h + kSolveInfo * (size_t)nj, info.begin());
 }
 
 void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
@@ -1130,6 +1228,7 @@ void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int
         info[0] = hinfo[0];
         info[1] = hinfo[1];
         info[2] = hinfo[2];
+        info[3] = hinfo[4];
     }
     if (hinfo[3] != 0.0) fail(RP_E_SINGULAR, "rp_solve: bordered system is singular (zero pivot)");
 }
@@ -1217,7 +1316,7 @@ extern "C" int rp_solve_noalloc(const double *A_dev, const double *b_dev, int N,
         double *x = cv.take<double>((size_t)n1);
         double *r = cv.take<double>((size_t)n1);
         int *perm = cv.take<int>((size_t)n1);
-        double *d_info = cv.take<double>(4);
+        double *d_info = cv.take<double>(kSolveInfo);
         SolveDesc *d_desc = cv.take<SolveDesc>(1);
         std::vector<double> rs((size_t)p.n, 0.0), rt((size_t)p.n, 0.0);
         if (resp_s)
@@ -1264,13 +1363,14 @@ extern "C" int rp_solve_noalloc(const double *A_dev, const double *b_dev, int N,
         lu_smem_optin();
         lu_solve_refine_kernel<<<1, kLU, solve_smem_bytes(n1), stream>>>(d_desc);
         RP_LAUNCH_CHECK();
-        double hinfo[4];
+        double hinfo[kSolveInfo];
         RP_CUDA(cudaMemcpyAsync(hinfo, d_info, sizeof(hinfo), cudaMemcpyDeviceToHost, stream));
         RP_CUDA(cudaStreamSynchronize(stream));
         if (info) {
             info[0] = hinfo[0];
             info[1] = hinfo[1];
             info[2] = hinfo[2];
+            info[3] = hinfo[4];
         }
         return hinfo[3] != 0.0 ? RP_E_SINGULAR : RP_OK;
     } catch (const rp::Error &e) {

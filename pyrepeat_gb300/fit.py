@@ -130,11 +130,16 @@ class Context:
         N = int(b.numel())
         ng, ptr, idx, rs, rt = constraint_arrays(Z, symm_groups, resp)
         q = t.empty(N, dtype=t.float64, device=self.dev)
-        info = np.zeros(3)
+        info = np.zeros(_lib.SOLVE_INFO_WORDS)
         rc = self.lib.rp_solve(self.ptr, A.data_ptr(), b.data_ptr(), N, ng, ptr.ctypes.data, idx.ctypes.data,
                                _ptr(rs), _ptr(rt), float(qtot), q.data_ptr(), info.ctypes.data, self._stream())
         self.check(rc, "rp_solve")
-        return q, {"residual": float(info[0]), "pivot_min": float(info[1]), "pivot_max": float(info[2])}
+        return q, _lib.solve_info(info)
+
+    def set_kappa_limit(self, kappa_max: float):
+        """Mixed-precision fits whose kappa / (n+1) exceeds this are refitted in FP64 (0 = never;
+        default 2e5)."""
+        self.check(self.lib.rp_set_kappa_limit(self.ptr, float(kappa_max)), "rp_set_kappa_limit")
 
     def set_timing(self, on: bool = True):
         self.check(self.lib.rp_set_timing(self.ptr, 1 if on else 0), "rp_set_timing")
@@ -178,7 +183,7 @@ class Context:
             raise ValueError("chi and j_self need one value per atom")
         q = np.zeros(N)
         J = np.zeros((N, N)) if want_J else None
-        info = np.zeros(3)
+        info = np.zeros(_lib.SOLVE_INFO_WORDS)
         ew = self.ewald(n_grid, axis, cutoff, kmax)
         try:
             rc = self.lib.rp_qeq(self.ptr, ew.ptr, atoms.ctypes.data, N, chi.ctypes.data, j_self.ctypes.data,
@@ -187,7 +192,7 @@ class Context:
             self.check(rc, "rp_qeq")
         finally:
             ew.close()
-        return q, J, {"residual": float(info[0]), "pivot_min": float(info[1]), "pivot_max": float(info[2])}
+        return q, J, _lib.solve_info(info)
 
     # ------------------------------------------------------------------ whole fits
     def fit_cube(self, cube, precision=_lib.PREC_MIXED, V_dev=None, keep_normal=False):
@@ -257,7 +262,7 @@ class Context:
         total = sum(c.n_atoms for c in cubes)
         q = out if out is not None else np.zeros(total)
         M = np.zeros(n, dtype=np.int64)
-        info = np.zeros(4 * n)
+        info = np.zeros(_lib.FIT_INFO_WORDS * n)
         rc = self.lib.rp_fit_batch(self.ptr, n, ctypes.cast(arr, ctypes.c_void_p), vptr, q.ctypes.data,
                                    M.ctypes.data, info.ctypes.data, self._stream())
         self.check(rc, "rp_fit_batch")
@@ -265,7 +270,7 @@ class Context:
         for c in cubes:
             res.append(q[o:o + c.n_atoms])
             o += c.n_atoms
-        return res, M, info.reshape(n, 4)
+        return res, M, info.reshape(n, _lib.FIT_INFO_WORDS)
 
     def batch_submit(self, cubes, precision=_lib.PREC_MIXED, V_dev=None) -> "PendingBatch":
         """Queue a batch on the context's worker thread (rp_batch_submit) and return at once.
@@ -294,7 +299,7 @@ class PendingBatch:
         self.ctx, self.cubes, self._keep = ctx, cubes, keep
         self.q = np.zeros(sum(c.n_atoms for c in cubes))
         self.M = np.zeros(len(cubes), dtype=np.int64)
-        self.info = np.zeros(4 * len(cubes))
+        self.info = np.zeros(_lib.FIT_INFO_WORDS * len(cubes))
         self.ticket = None
         self.status = None
 
@@ -308,7 +313,7 @@ class PendingBatch:
         return self.status is not None
 
     def result(self):
-        """(charges per cube, kept counts, info[n, 4]); raises the batch's error."""
+        """(charges per cube, kept counts, info[n, FIT_INFO_WORDS]); raises the batch's error."""
         if self.status is None:
             st = ctypes.c_int()
             self.ctx.check(self.ctx.lib.rp_batch_wait(self.ctx.ptr, self.ticket, ctypes.byref(st)), "rp_batch_wait")
@@ -318,7 +323,7 @@ class PendingBatch:
         for c in self.cubes:
             res.append(self.q[o:o + c.n_atoms])
             o += c.n_atoms
-        return res, self.M, self.info.reshape(-1, 4)
+        return res, self.M, self.info.reshape(-1, _lib.FIT_INFO_WORDS)
 
 
 class Ewald:

@@ -1,20 +1,24 @@
-"""Served fits: a micro-batching request loop on one GPU context.
+"""Served fits: a continuous-batching request loop on one GPU context.
 
 Requests (one cube each, its grid on the device or on the host) arrive from any
 thread through ``FitServer.submit``, which returns a ``concurrent.futures.Future``.
-A dispatcher thread groups waiting requests into batches: at most ``max_batch``
-cubes, at most ``max_wait_s`` after the oldest waiting request arrived, and an
-estimated device footprint within ``hbm_budget`` bytes (admission control: a
-request that does not fit waits for the next batch; one that alone exceeds the
-budget is rejected).  Each batch goes to the context's worker with
-``rp_batch_submit``, so the next batch is assembled while the device runs the
-current one; a completion thread resolves every request's future when its batch is
-done.  A cube's charges do not depend on the batch it was served in (the batched
-fit is bitwise independent of its neighbours and of the stream a cube runs on).
+A dispatcher thread groups waiting requests into batches of one size class
+(large cubes, by their estimated device footprint, are batched apart from the
+rest, so a small request never waits inside a batch for a large cube): at most
+``max_batch`` cubes, at most ``max_wait_s`` after the oldest waiting request
+arrived.  Admission is by device memory: a batch is submitted only while the
+estimated bytes of every batch in flight plus its own stay within ``hbm_budget``
+(a request that alone exceeds the budget is rejected).  Batches go to the
+context's worker with ``rp_batch_submit``; the worker keeps up to three of them
+in flight on the device at once (each in a slot of its own), so a batch that
+arrives while others run starts at once and overlaps them.  A completion thread
+polls the tickets and resolves each request's future as soon as its batch is
+done, in whatever order batches finish.  A cube's charges do not depend on the
+batch it was served in (the batched fit is bitwise independent of its neighbours
+and of the streams and slot it runs on).
 
 No reference counterpart: repeat.py is a one-shot program.  The serving workload
-(Poisson arrivals from the batch distribution) is measured by ``bench.py
---workload serve``.
+(Poisson arrivals from the batch distribution) is measured by ``bench.py``.
 """
 from __future__ import annotations
 
@@ -26,17 +30,33 @@ from concurrent.futures import Future
 
 from . import _lib
 
+GRAM_LANES = 4  # streams of a batch's normal equations, each with its own scratch
 
-def device_bytes(cube) -> int:
-    """Estimated device bytes a cube adds to a batch: its grid-sized arrays (grid values,
-    kept indices, centred ESP) and, bounded by the whole grid, the per-stream scratch of
-    its normal equations (fixed-point digits of every atom row, reciprocal rows)."""
+
+def footprint(cube) -> tuple[int, int]:
+    """(fixed, scratch) estimated device bytes of a cube in a batch: its grid-sized
+    arrays (grid values, kept indices, centred ESP), and, bounded by the whole grid,
+    the scratch of its normal equations (fixed-point digits of every atom row,
+    reciprocal rows), which a batch holds once per gram stream, not per cube."""
     nx, ny, nz = (int(v) for v in cube.n_grid)
     npts = nx * ny * nz
     N = int(cube.n_atoms)
-    fixed = 20 * npts
-    scratch = 8 * (N + 1) * npts + 8 * ny * nz * N * int(cube.kmax)
+    return 20 * npts, 8 * (N + 1) * npts + 8 * ny * nz * N * int(cube.kmax)
+
+
+def device_bytes(cube) -> int:
+    """Estimated device bytes of a cube fitted alone."""
+    fixed, scratch = footprint(cube)
     return fixed + scratch
+
+
+def batch_bytes(cubes) -> int:
+    """Estimated device bytes of a batch: every cube's fixed arrays plus the largest
+    scratch once per gram stream in use."""
+    fp = [footprint(c) for c in cubes]
+    if not fp:
+        return 0
+    return sum(f for f, _ in fp) + min(GRAM_LANES, len(fp)) * max(s for _, s in fp)
 
 
 class _Request:
@@ -51,21 +71,32 @@ class _Request:
 
 
 class FitServer:
-    """Micro-batching fit server on ``ctx`` (a ``pyrepeat_gb300.fit.Context``)."""
+    """Continuous-batching fit server on ``ctx`` (a ``pyrepeat_gb300.fit.Context``).
+
+    ``large_bytes``: requests whose estimated footprint exceeds it form batches of
+    their own, of at most ``max_large_batch`` cubes."""
 
     def __init__(self, ctx, max_batch: int = 64, max_wait_s: float = 0.002, hbm_budget: float = 150e9,
-                 precision: int = _lib.PREC_MIXED):
+                 precision: int = _lib.PREC_MIXED, large_bytes: float = 8e9, max_large_batch: int = 1):
         self.ctx = ctx
         self.max_batch = int(max_batch)
         self.max_wait_s = float(max_wait_s)
         self.hbm_budget = float(hbm_budget)
         self.precision = precision
+        self.large_bytes = float(large_bytes)
+        self.max_large_batch = int(max_large_batch)
         self._in: queue.Queue = queue.Queue()
         self._submitted: queue.Queue = queue.Queue()
         self._closed = False
         self.latencies: list[float] = []  # seconds, arrival to charges on the host, per request
         self.batch_sizes: list[int] = []
+        self.large_latencies: list[float] = []   # the same, large requests only
+        self.small_latencies: list[float] = []   # the same, every other request
+        self.max_in_flight = 0            # most batches in flight at once (submitted, not retired)
         self._lock = threading.Lock()
+        self._cv = threading.Condition()
+        self._inflight_bytes = 0
+        self._inflight = 0
         self._dispatcher = threading.Thread(target=self._dispatch, name="fit-dispatch", daemon=True)
         self._completer = threading.Thread(target=self._complete, name="fit-complete", daemon=True)
         self._dispatcher.start()
@@ -100,41 +131,55 @@ class FitServer:
         self.close()
 
     # ------------------------------------------------------------------ threads
+    def _large(self, r) -> bool:
+        return r.bytes > self.large_bytes
+
     def _dispatch(self):
-        carry: collections.deque = collections.deque()  # admitted-later requests, oldest first
+        pend = {False: collections.deque(), True: collections.deque()}  # waiting requests by class
         stopping = False
         while True:
-            if carry:
-                first = carry.popleft()
-            else:
+            if not pend[False] and not pend[True]:
                 if stopping:
                     break
-                first = self._in.get()
-                if first is None:
+                r = self._in.get()
+                if r is None:
                     break
-            batch, used = [first], first.bytes
-            deadline = first.t_arrive + self.max_wait_s
-            while len(batch) < self.max_batch:
-                if carry:
-                    r = carry.popleft()
-                else:
-                    timeout = deadline - time.perf_counter()
-                    try:
-                        r = self._in.get(timeout=max(timeout, 0.0)) if timeout > 0 else self._in.get_nowait()
-                    except queue.Empty:
-                        break
-                    if r is None:
-                        stopping = True
-                        break
-                if used + r.bytes > self.hbm_budget:
-                    carry.appendleft(r)  # admission: waits for the next batch
+                pend[self._large(r)].append(r)
+            # the class of the oldest waiting request fills a batch until its wait bound
+            cls = min((c for c in (False, True) if pend[c]), key=lambda c: pend[c][0].t_arrive)
+            limit = self.max_large_batch if cls else self.max_batch
+            deadline = pend[cls][0].t_arrive + self.max_wait_s
+            while len(pend[cls]) < limit and not stopping:
+                timeout = deadline - time.perf_counter()
+                try:
+                    r = self._in.get(timeout=timeout) if timeout > 0 else self._in.get_nowait()
+                except queue.Empty:
                     break
-                batch.append(r)
-                used += r.bytes
-            self._submit(batch)
+                if r is None:
+                    stopping = True
+                    break
+                pend[self._large(r)].append(r)
+            batch = [pend[cls].popleft()]
+            while pend[cls] and len(batch) < limit and batch_bytes(
+                    [x.cube for x in batch] + [pend[cls][0].cube]) <= self.hbm_budget:
+                batch.append(pend[cls].popleft())
+            need = batch_bytes([x.cube for x in batch])
+            with self._cv:  # admission: bytes of every batch in flight stay within the budget
+                while self._inflight and self._inflight_bytes + need > self.hbm_budget:
+                    self._cv.wait()
+                self._inflight_bytes += need
+                self._inflight += 1
+                self.max_in_flight = max(self.max_in_flight, self._inflight)
+            self._submit(batch, need)
         self._submitted.put(None)
 
-    def _submit(self, batch):
+    def _release(self, need):
+        with self._cv:
+            self._inflight_bytes -= need
+            self._inflight -= 1
+            self._cv.notify_all()
+
+    def _submit(self, batch, need):
         cubes = [r.cube for r in batch]
         V_dev = [r.V_dev for r in batch]
         try:
@@ -142,26 +187,59 @@ class FitServer:
         except Exception as e:  # noqa: BLE001 - handed to every request of the batch
             for r in batch:
                 r.future.set_exception(e)
+            self._release(need)
             return
-        self._submitted.put((pb, batch))
+        self._submitted.put((pb, batch, need))
+
+    def _finish(self, pb, batch, need):
+        try:
+            q, M, info = pb.result()
+        except Exception as e:  # noqa: BLE001
+            for r in batch:
+                r.future.set_exception(e)
+            self._release(need)
+            return
+        now = time.perf_counter()
+        with self._lock:
+            self.batch_sizes.append(len(batch))
+            for r in batch:
+                r.t_done = now
+                self.latencies.append(now - r.t_arrive)
+                (self.large_latencies if self._large(r) else self.small_latencies).append(now - r.t_arrive)
+        self._release(need)
+        for r, qi in zip(batch, q):
+            r.future.set_result(qi.copy())
 
     def _complete(self):
+        outstanding = []
+        ended = False
         while True:
-            item = self._submitted.get()
-            if item is None:
+            # new batches (block only when nothing is in flight)
+            while True:
+                try:
+                    item = self._submitted.get(block=not outstanding and not ended)
+                except queue.Empty:
+                    break
+                if item is None:
+                    ended = True
+                    break
+                outstanding.append(item)
+                if not self._submitted.qsize():
+                    break
+            # retire every finished batch, in the order they finish
+            still = []
+            for item in outstanding:
+                try:
+                    done = item[0].poll()
+                except Exception:  # noqa: BLE001 - result() raises it to the requests
+                    done = True
+                if done:
+                    self._finish(*item)
+                else:
+                    still.append(item)
+            progressed = len(still) != len(outstanding)
+            outstanding = still
+            if ended and not outstanding:
                 return
-            pb, batch = item
-            try:
-                q, M, info = pb.result()
-            except Exception as e:  # noqa: BLE001
-                for r in batch:
-                    r.future.set_exception(e)
-                continue
-            now = time.perf_counter()
-            with self._lock:
-                self.batch_sizes.append(len(batch))
-                for r, qi in zip(batch, q):
-                    r.t_done = now
-                    self.latencies.append(now - r.t_arrive)
-            for r, qi in zip(batch, q):
-                r.future.set_result(qi.copy())
+            if outstanding and not progressed:
+                time.sleep(0.0002)

@@ -253,10 +253,15 @@ def ewald_potential_grid(n_grid, axis, atom_pos, q, cutoff, kmax, threads=None) 
 
 # ----------------------------------------------------------------------------- workloads
 
-def _finish(cube: Cube, rng: np.random.Generator, noise: float, threads=None, ctx=None) -> Cube:
+def _finish(cube: Cube, rng: np.random.Generator, noise: float, threads=None, ctx=None, esp: bool = True) -> Cube:
     """ESP = Ewald potential of the planted charges + N(0, noise).  With a
     pyrepeat_gb300.fit.Context the potential is evaluated on its GPU (rp_potential)
-    and the cube keeps V only on the device (V_dev); otherwise on the host."""
+    and the cube keeps V only on the device (V_dev); otherwise on the host.  With
+    esp=False the grid holds the noise alone: the same geometry and fit work (a timing
+    stand-in where the host cannot afford the Ewald sum over every grid point)."""
+    if not esp:
+        cube.V = rng.normal(0.0, noise, size=cube.n_points)
+        return cube
     if ctx is not None:
         import torch
         ew = ctx.ewald(cube.n_grid, cube.axis_vector, cube.cutoff, cube.kmax)
@@ -309,7 +314,7 @@ def _random_neutral(rng, n, sigma):
 
 
 def make_mof(seed: int = 2, n_grid: int = 128, kmax: int = 12, noise: float = 1e-4,
-             L: float = 25.8, counts=(32, 104, 192, 96), threads=None, ctx=None) -> Cube:
+             L: float = 25.8, counts=(32, 104, 192, 96), threads=None, ctx=None, esp: bool = True) -> Cube:
     """MOF-like cubic cell: Zn:O:C:H = 4:13:24:12 (x8 = 424 atoms) at >= 2.2 Bohr."""
     rng = np.random.default_rng(seed)
     cell = lower_triangular_cell(L, L, L)
@@ -320,7 +325,7 @@ def make_mof(seed: int = 2, n_grid: int = 128, kmax: int = 12, noise: float = 1e
     axis = cell / n_grid
     cube = Cube(Z, pos, np.array([n_grid] * 3), axis, None, charges_true=q, kmax=kmax,
                 name=f"mof-{len(Z)}-{n_grid}-k{kmax}")
-    return _finish(cube, rng, noise, threads, ctx)
+    return _finish(cube, rng, noise, threads, ctx, esp)
 
 
 def random_symmetry_groups(rng, n_atoms, n_groups, lo=2, hi=6):
@@ -338,7 +343,7 @@ def random_symmetry_groups(rng, n_atoms, n_groups, lo=2, hi=6):
 
 def make_tric(seed: int = 3, n_grid=(200, 210, 225), n_atoms: int = 2000, noise: float = 1e-4,
               n_groups: int = 150, threads=None, lengths=(40.0, 42.0, 45.0),
-              angles=(85.0, 95.0, 100.0), kmax: int = 7, ctx=None) -> Cube:
+              angles=(85.0, 95.0, 100.0), kmax: int = 7, ctx=None, esp: bool = True) -> Cube:
     """Triclinic cell 40 x 42 x 45 Bohr, 85/95/100 deg; C/H/N/O 40/40/10/10%;
     150 symmetry groups of 2-6 atoms; RESP 0.1 -> 0 on C, N, O."""
     rng = np.random.default_rng(seed)
@@ -360,7 +365,7 @@ def make_tric(seed: int = 3, n_grid=(200, 210, 225), n_atoms: int = 2000, noise:
     cube = Cube(Z, pos, ng, axis, None, charges_true=q, symm_groups=groups,
                 resp={"C": (0.1, 0.0), "N": (0.1, 0.0), "O": (0.1, 0.0)}, kmax=kmax,
                 name=f"tric-{len(Z)}-{'x'.join(map(str, n_grid))}")
-    return _finish(cube, rng, noise, threads, ctx)
+    return _finish(cube, rng, noise, threads, ctx, esp)
 
 
 BATCH_ELEMENTS = (1, 6, 7, 8, 16, 30)

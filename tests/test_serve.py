@@ -1,10 +1,11 @@
 """The serving layer: asynchronous batches (rp_batch_submit / poll / wait) and the
-micro-batching FitServer.
+continuous-batching FitServer.
 
-CPU: the dispatcher's batching rules (batch size, wait bound, HBM admission and
-rejection) against a fake context.  GPU: requests served from two threads in mixed
-batches give exactly the charges of each cube fitted alone, and the C-ABI tickets
-retire as documented."""
+CPU: the dispatcher's batching rules (batch size, wait bound, size classes, HBM
+admission across the batches in flight, rejection, completion in any order) against
+a fake context.  GPU: requests served from two threads in mixed batches give exactly
+the charges of each cube fitted alone; a small batch submitted behind a large one
+finishes first while both are in flight; the C-ABI tickets retire as documented."""
 import threading
 import time
 
@@ -23,22 +24,28 @@ class _FakeCube:
 
 
 class _FakePending:
-    def __init__(self, cubes):
+    def __init__(self, cubes, gate=None):
         self.cubes = cubes
+        self.gate = gate   # a threading.Event: the batch is done once it is set
+
+    def poll(self):
+        return self.gate is None or self.gate.is_set()
 
     def result(self):
         return [np.full(c.n_atoms, float(c.n_atoms)) for c in self.cubes], np.zeros(len(self.cubes)), None
 
 
 class _FakeCtx:
-    """Records the batches the server submits; results are available at once."""
+    """Records the batches the server submits; results are available at once, or once
+    the gate given for a batch is set."""
 
-    def __init__(self):
+    def __init__(self, gates=None):
         self.batches = []
+        self.gates = gates or {}
 
     def batch_submit(self, cubes, precision, V_dev):
         self.batches.append([c.n_atoms for c in cubes])
-        return _FakePending(cubes)
+        return _FakePending(cubes, self.gates.get(len(self.batches) - 1))
 
 
 def test_batches_respect_size_and_admission():
@@ -84,6 +91,9 @@ class _FailingResultCtx(_FakeCtx):
         super().batch_submit(cubes, precision, V_dev)
 
         class P:
+            def poll(self_inner):
+                return True
+
             def result(self_inner):
                 raise RuntimeError("batch failed")
         return P()
@@ -98,6 +108,39 @@ def test_errors_reach_every_request_of_the_batch():
             with pytest.raises(RuntimeError, match=msg):
                 f.result(timeout=5)
         assert srv.latencies == []
+
+
+def test_large_requests_are_batched_apart():
+    """A large cube forms a batch of its own: the small requests around it are not
+    held inside its batch."""
+    ctx = _FakeCtx()
+    small = _FakeCube(5)
+    big = _FakeCube(40, n_grid=(60, 60, 60))
+    srv = serve.FitServer(ctx, max_batch=8, max_wait_s=0.05, large_bytes=serve.device_bytes(small) * 10)
+    futs = [srv.submit(c) for c in (small, big, small, small)]
+    srv.close()
+    assert [f.result()[0] for f in futs] == [5.0, 40.0, 5.0, 5.0]
+    assert sorted(ctx.batches) == [[5, 5, 5], [40]]
+    assert len(srv.large_latencies) == 1
+
+
+def test_admission_counts_batches_in_flight():
+    """A batch whose bytes, added to the batches still in flight, exceed the budget waits
+    until one of them retires; batches that fit run side by side."""
+    one = serve.batch_bytes([_FakeCube(5)])
+    gates = {0: threading.Event(), 1: threading.Event()}
+    ctx = _FakeCtx(gates=gates)
+    srv = serve.FitServer(ctx, max_batch=1, max_wait_s=0.0, hbm_budget=2.5 * one)
+    f = [srv.submit(_FakeCube(5)) for _ in range(3)]
+    time.sleep(0.05)
+    assert len(ctx.batches) == 2 and not any(x.done() for x in f)   # two fit side by side, a third waits
+    gates[1].set()
+    assert f[1].result(timeout=5)[0] == 5.0 and f[2].result(timeout=5)[0] == 5.0
+    assert not f[0].done()                         # batches retire as they finish, in any order
+    gates[0].set()
+    assert f[0].result(timeout=5)[0] == 5.0
+    srv.close()
+    assert srv.max_in_flight == 2
 
 
 def test_closed_server_refuses_requests():
@@ -132,6 +175,34 @@ def test_served_fits_equal_fits_alone(gpu_ctx):
     for (name, fut) in results.values():
         assert np.array_equal(fut.result(timeout=60), alone[name]), name
     assert sum(srv.batch_sizes) == 24 and len(srv.latencies) == 24
+
+
+@pytest.mark.gpu
+def test_small_batch_overtakes_a_large_one(gpu_ctx):
+    """Continuous batching on the device: a small batch submitted right behind a large
+    cube's batch runs beside it (its own slot, higher stream priority) and finishes first;
+    both results equal the fits alone, bitwise."""
+    from pyrepeat_gb300 import _lib, synth
+    large = synth.make_batch_item(90001, large=True, ctx=gpu_ctx)
+    small, _ = load_golden("water24")
+    alone_large = gpu_ctx.fit_batch([large], _lib.PREC_MIXED, V_dev=[large.V_dev])[0][0].copy()
+    alone_small = gpu_ctx.fit_host(small, precision=_lib.PREC_MIXED).charges
+    order = []
+    for rep in range(2):   # the first round sizes both slots' buffers
+        pl = gpu_ctx.batch_submit([large], _lib.PREC_MIXED, V_dev=[large.V_dev])
+        ps = gpu_ctx.batch_submit([small], _lib.PREC_MIXED)
+        done = {}
+        t0 = time.perf_counter()
+        while len(done) < 2:
+            for name, pb in (("large", pl), ("small", ps)):
+                if name not in done and pb.poll():
+                    done[name] = time.perf_counter() - t0
+            assert time.perf_counter() - t0 < 120
+            time.sleep(0.0002)
+        order.append(done)
+        assert np.array_equal(pl.result()[0][0], alone_large)
+        assert np.array_equal(ps.result()[0][0], alone_small)
+    assert order[1]["small"] < order[1]["large"], order
 
 
 @pytest.mark.gpu

@@ -34,7 +34,7 @@ def _noalloc_raw(gpu_ctx, cube, A, b, q, info):
 def _noalloc(gpu_ctx, cube, A, b):
     import torch
     q = torch.empty(cube.n_atoms, dtype=torch.float64, device=A.device)
-    info = np.zeros(3)
+    info = np.zeros(4)
     assert _noalloc_raw(gpu_ctx, cube, A, b, q, info) == 0
     return q.cpu().numpy(), info
 
@@ -75,7 +75,7 @@ def test_noalloc_call_allocates_nothing(gpu_ctx):
     import torch
     cube, A, b = _normal_equations(gpu_ctx, "tricmini")
     q = torch.empty(cube.n_atoms, dtype=torch.float64, device=A.device)
-    info = np.zeros(3)
+    info = np.zeros(4)
     assert _noalloc_raw(gpu_ctx, cube, A, b, q, info) == 0   # warm: module and array loaded
     torch.cuda.synchronize()
     free0, _ = torch.cuda.mem_get_info()
