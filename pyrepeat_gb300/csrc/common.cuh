@@ -187,7 +187,10 @@ namespace rp {
 // its own scratch (names carry the slot), pinned staging, streams, status words, cuBLAS
 // handle and host object pools; slot 0 is also what rp_fit_batch and the staged calls use.
 constexpr int kBatchSlots = 3;
-constexpr int kSlotLanes = 10;  // streams per slot: 4 gram + 4 filter + 1 copy + the batch's own
+// streams of a slot: 4 for normal equations, 4 for filters, uploads, the pipeline groups'
+// reciprocal rows, and the batch's own stream (the server's)
+constexpr int kLaneFilter0 = 4, kLaneCopy = 8, kLaneRecip = 9, kLaneBatch = 10;
+constexpr int kSlotLanes = 11;
 // A served batch whose largest cube has at least this many grid points x atoms runs on
 // streams of the default (lowest) priority, every other served batch on streams of the
 // device's greatest priority: the block scheduler then hands free SMs to a small request's
@@ -425,6 +428,20 @@ void filter_plan(const rp_grid *grid, const double *atoms, const int *Z, int N, 
 void filter_launch(rp_ctx *ctx, const FilterPlan &plan, const char *packed_dev, const double *V_dev,
                    int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev, uint8_t *mask_dev, cudaStream_t stream,
                    const std::string &tag, bool brick_order, double *vstats_dev);
+// Many cubes at once (a pipeline group of a batch), brick order, no mask output: one launch
+// per stage for up to 40 cubes.  Each item's kept count lands in *M, kept indices and
+// centred ESP in its kept/Vc (room for its whole grid), (sum, max |.|) of the centred ESP in
+// its vstats (2 doubles, optional).
+struct FilterItem {
+    const FilterPlan *plan;
+    const char *packed_dev;
+    const double *V;
+    int32_t *kept;
+    double *Vc;
+    long long *M;
+    double *vstats;
+};
+void filter_group(rp_ctx *ctx, const std::vector<FilterItem> &items, cudaStream_t stream, const std::string &tag);
 // Asynchronous form: the kept count lands in *M_dev; kept_idx_dev and Vc_dev hold a
 // whole grid (capacity = nx*ny*nz).  `tag` keeps the scratch of concurrent calls apart.
 // brick_order: kept points in 8x4x4 brick order instead of flat order (the mixed fit
@@ -442,10 +459,13 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
 // scaled vdW radii, which bound |Phi| a priori, so Phi goes straight to fixed-point
 // digits in one pass; clamped values are counted in *clamp_dev (the caller then redoes
 // the fit without rn).  Without them: two passes (Phi, then its centre and scale).
+// d_atoms_pre / E_pre (optional): the atoms already on the device and the reciprocal rows
+// already computed (recip_rows_group over a batch's pipeline group).
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
                 cudaStream_t stream, const double *vstats_dev = nullptr, const std::string &slot = "",
-                const double *rn = nullptr, int *clamp_dev = nullptr);
+                const double *rn = nullptr, int *clamp_dev = nullptr, const double *d_atoms_pre = nullptr,
+                const float2 *E_pre = nullptr);
 double radius_of(int z);  // vdW radius (Bohr) of element z, the filter's table
 void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
                const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,
@@ -519,6 +539,17 @@ size_t recip_rows_bytes(const rp_ewald *ew, int ncols);
 // `slot` keeps the scratch of fits running concurrently on different streams apart.
 void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const double *d_q, int N, float2 *E,
                 cudaStream_t stream, const std::string &slot = "");
+// The same for many fits at once: one launch per stage for up to 64 fits (a pipeline group
+// of a batch), each with its own tables, atoms and output E (recip_rows_bytes each).
+struct RecipRowsJob {
+    const rp_ewald *ew;
+    const double *d_atoms;
+    const double *d_q;
+    int N;
+    float2 *E;
+};
+void recip_rows_group(rp_ctx *ctx, const std::vector<RecipRowsJob> &jobs, cudaStream_t stream,
+                      const std::string &tag);
 
 // Shared epilogue kernels (phi_fp64.cu).
 void column_sums_fp64(const double *X, int64_t rows, int cols, int ld, double *out, bool accumulate,

@@ -121,6 +121,48 @@ constexpr int kBrickX = 8, kBrickY = 4, kBrickZ = 4;
 constexpr int kBrickPts = kBrickX * kBrickY * kBrickZ;  // 128
 constexpr int kCullCap = 512;  // candidate images a brick keeps in shared memory
 
+// One cube's filter in a grouped launch: its plan, grid values, scratch and outputs.  A launch
+// carries up to kFilterJobs of them by value; job j owns blocks [blk[j], blk[j+1]) of the
+// kernel's grid, so a pipeline group of cubes costs one launch per stage.
+struct FilterJob {
+    FilterParams p;
+    const float4 *e32;
+    const D4 *e64;
+    const double *rmax2;
+    const float *rmax2f;
+    const int *boff, *bidx;
+    const double *V;
+    uint8_t *mask;
+    int *counts;          // kept points per compaction block (bricks, or flat blocks of 256)
+    long long *offsets;   // their exclusive scan
+    double *vsum;         // per compaction block: sum of the kept ESP values
+    int ncount;           // compaction blocks
+    int32_t *kept;
+    double *Vc;
+    long long *M;         // kept count (device)
+    double *mean;
+    double2 *vpart;       // kCenterParts partial (sum, max |.|) of the centred ESP
+    double *vstats;       // (sum, max |.|), or nullptr
+    int nbx, nby;
+};
+constexpr int kFilterJobs = 40;
+struct FilterLaunch {
+    int n;
+    int blk[kFilterJobs + 1];
+    FilterJob job[kFilterJobs];
+};
+constexpr int kCenterParts = 32;  // CTAs per cube of the centring pass
+
+__device__ __forceinline__ int filter_job_of(const FilterLaunch &L, int b) {
+    int lo = 0, hi = L.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (L.blk[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 __device__ __forceinline__ long long brick_point(int b, int t, int nx, int ny, int nz, int nbx, int nby) {
     const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
     const int i = bx * kBrickX + (t % kBrickX), j = by * kBrickY + ((t / kBrickX) % kBrickY),
@@ -137,17 +179,22 @@ __device__ __forceinline__ long long brick_point(int b, int t, int nx, int ny, i
 // of the brick, so it could neither reject a point nor trigger its FP64 recheck: the mask is
 // the one of the per-point bin test (valid_by_bins), which a brick with more than kCullCap
 // candidates falls back to.  Writes the mask and the brick's kept count.
-__global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(
-    FilterParams p, int nbx, int nby, const float4 *__restrict__ eff, const D4 *__restrict__ eff64,
-    const double *__restrict__ rmax2, const float *__restrict__ rmax2f, const int *__restrict__ boff,
-    const int *__restrict__ bidx, uint8_t *__restrict__ mask, int *__restrict__ brick_counts,
-    unsigned long long *__restrict__ rechecks) {
+__global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(const __grid_constant__ FilterLaunch L,
+                                                                  int write_counts) {
     __shared__ float4 cand[kCullCap];
     __shared__ int cidx[kCullCap];
     __shared__ int ncand;
     __shared__ float red[6][kBrickPts / 32];
+    const int jb = filter_job_of(L, blockIdx.x);
+    const FilterJob &J = L.job[jb];
+    const FilterParams &p = J.p;
+    const float4 *__restrict__ eff = J.e32;
+    const D4 *__restrict__ eff64 = J.e64;
+    const int *__restrict__ boff = J.boff;
+    const int *__restrict__ bidx = J.bidx;
+    const int nbx = J.nbx, nby = J.nby;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const int b = blockIdx.x;
+    const int b = blockIdx.x - L.blk[jb];
     const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
     const int i = bx * kBrickX + (t % kBrickX), j = by * kBrickY + ((t / kBrickX) % kBrickY),
               k = bz * kBrickZ + t / (kBrickX * kBrickY);
@@ -230,13 +277,14 @@ __global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(
         } else {
             valid = valid_by_bins(p, i, j, k, gx, gy, gz, eff, eff64, boff, bidx, nre);
         }
-        const bool near = p.near_all != 0 || (valid && near_any(p, i, j, k, gx, gy, gz, eff, eff64, rmax2, rmax2f, nre));
+        const bool near =
+            p.near_all != 0 || (valid && near_any(p, i, j, k, gx, gy, gz, eff, eff64, J.rmax2, J.rmax2f, nre));
         keep = (valid && near) ? 1 : 0;
-        mask[(long long)i + (long long)p.nx * (j + (long long)p.ny * k)] = (uint8_t)keep;
+        J.mask[(long long)i + (long long)p.nx * (j + (long long)p.ny * k)] = (uint8_t)keep;
     }
     const int cnt = __syncthreads_count(keep);
-    if (t == 0) brick_counts[b] = cnt;
-    if (nre) atomicAdd(rechecks, (unsigned long long)nre);
+    if (t == 0 && write_counts) J.counts[b] = cnt;
+    (void)nre;
 }
 
 // Kept points per block of kFilterThreads consecutive flat indices (the flat-order compaction).
@@ -248,16 +296,17 @@ __global__ void __launch_bounds__(kFilterThreads) flat_count_kernel(const uint8_
     if (threadIdx.x == 0) counts[blockIdx.x] = cnt;
 }
 
-// Exclusive scan of the per-block counts (one block; nb up to a few 10^5).
-__global__ void __launch_bounds__(1024) scan_counts_kernel(const int *__restrict__ counts, int nb,
-                                                           long long *__restrict__ offsets,
-                                                           long long *__restrict__ total) {
+// Exclusive scan of each job's per-block counts (one CTA per job; up to a few 10^5 blocks),
+// and the job's kept count.
+__global__ void __launch_bounds__(1024) scan_counts_kernel(const __grid_constant__ FilterLaunch L) {
+    const FilterJob &J = L.job[blockIdx.x];
+    const int nb = J.ncount;
     __shared__ long long part[1024];
     int t = threadIdx.x;
     int per = (nb + 1023) / 1024;
     int b0 = t * per, b1 = min(b0 + per, nb);
     long long s = 0;
-    for (int b = b0; b < b1; ++b) s += counts[b];
+    for (int b = b0; b < b1; ++b) s += J.counts[b];
     part[t] = s;
     __syncthreads();
     for (int off = 1; off < 1024; off <<= 1) {  // Hillis-Steele inclusive scan
@@ -268,10 +317,10 @@ __global__ void __launch_bounds__(1024) scan_counts_kernel(const int *__restrict
     }
     long long run = (t == 0) ? 0 : part[t - 1];
     for (int b = b0; b < b1; ++b) {
-        offsets[b] = run;
-        run += counts[b];
+        J.offsets[b] = run;
+        run += J.counts[b];
     }
-    if (t == 1023) *total = part[1023];
+    if (t == 1023) *J.M = part[1023];
 }
 
 __global__ void __launch_bounds__(kFilterThreads) compact_kernel(
@@ -314,15 +363,15 @@ __global__ void __launch_bounds__(kFilterThreads) compact_kernel(
 // The kept points of a brick are contiguous, so any 128 consecutive kept points span a
 // compact region of the cell (the real-space culling of the mixed fit keeps fewer images
 // for compact tiles).  Deterministic (ballots only).
-__global__ void __launch_bounds__(kBrickPts) brick_compact_kernel(
-    const uint8_t *__restrict__ mask, const double *__restrict__ V, int nx, int ny, int nz, int nbx, int nby,
-    const long long *__restrict__ offsets, long long capacity, int32_t *__restrict__ kept_idx,
-    double *__restrict__ Vc, double *__restrict__ block_vsum) {
+__global__ void __launch_bounds__(kBrickPts) brick_compact_kernel(const __grid_constant__ FilterLaunch L) {
     __shared__ int warp_base[kBrickPts / 32];
     __shared__ double warp_sum[kBrickPts / 32];
-    const long long f = brick_point(blockIdx.x, threadIdx.x, nx, ny, nz, nbx, nby);
-    const int keep = (f >= 0) ? mask[f] : 0;
-    const double v = keep ? V[f] : 0.0;
+    const int jb = filter_job_of(L, blockIdx.x);
+    const FilterJob &J = L.job[jb];
+    const int b = blockIdx.x - L.blk[jb];
+    const long long f = brick_point(b, threadIdx.x, J.p.nx, J.p.ny, J.p.nz, J.nbx, J.nby);
+    const int keep = (f >= 0) ? J.mask[f] : 0;
+    const double v = keep ? J.V[f] : 0.0;
     const unsigned bal = __ballot_sync(0xffffffffu, keep);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int pos_in_warp = __popc(bal & ((1u << lane) - 1u));
@@ -336,27 +385,26 @@ __global__ void __launch_bounds__(kBrickPts) brick_compact_kernel(
     int base = 0;
     for (int w = 0; w < warp; ++w) base += warp_base[w];
     if (keep) {
-        const long long pos = offsets[blockIdx.x] + base + pos_in_warp;
-        if (pos < capacity) {
-            kept_idx[pos] = (int32_t)f;
-            Vc[pos] = v;
+        const long long pos = J.offsets[b] + base + pos_in_warp;
+        if (pos < J.p.n_total) {
+            J.kept[pos] = (int32_t)f;
+            J.Vc[pos] = v;
         }
     }
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int w = 0; w < kBrickPts / 32; ++w) t += warp_sum[w];
-        block_vsum[blockIdx.x] = t;
+        J.vsum[b] = t;
     }
 }
 
-// Mean of kept V over all blocks in a fixed order (deterministic), one block.
-__global__ void __launch_bounds__(1024) vmean_kernel(const double *__restrict__ block_vsum, int nb,
-                                                     const long long *__restrict__ total,
-                                                     double *__restrict__ mean_out) {
+// Mean of each job's kept V over its blocks in a fixed order (deterministic), one CTA per job.
+__global__ void __launch_bounds__(1024) vmean_kernel(const __grid_constant__ FilterLaunch L) {
+    const FilterJob &J = L.job[blockIdx.x];
     __shared__ double part[1024];
     int t = threadIdx.x;
     double s = 0.0;
-    for (int b = t; b < nb; b += 1024) s += block_vsum[b];
+    for (int b = t; b < J.ncount; b += 1024) s += J.vsum[b];
     part[t] = s;
     __syncthreads();
     for (int off = 512; off > 0; off >>= 1) {
@@ -364,29 +412,27 @@ __global__ void __launch_bounds__(1024) vmean_kernel(const double *__restrict__ 
         __syncthreads();
     }
     if (t == 0) {
-        long long M = *total;
-        *mean_out = M > 0 ? part[0] / (double)M : 0.0;
+        long long M = *J.M;
+        *J.mean = M > 0 ? part[0] / (double)M : 0.0;
     }
 }
 
-// Centre the kept ESP (Vc -= mean) and, when part != nullptr, write each block's sum of
-// the centred values and their largest magnitude (the ESP row statistics of the mixed
+// Centre each job's kept ESP (Vc -= mean), kCenterParts CTAs per job, and write each CTA's
+// sum of the centred values and their largest magnitude (the ESP row statistics of the mixed
 // Gram), reduced in a fixed order by vstats_kernel.
 constexpr int kCenterThreads = 256;
-__global__ void __launch_bounds__(kCenterThreads) center_kernel(double *__restrict__ Vc,
-                                                                const long long *__restrict__ Mp,
-                                                                const double *__restrict__ mean,
-                                                                double2 *__restrict__ part) {
-    const double m = *mean;
-    const long long M = *Mp;
+__global__ void __launch_bounds__(kCenterThreads) center_kernel(const __grid_constant__ FilterLaunch L) {
+    const FilterJob &J = L.job[blockIdx.x / kCenterParts];
+    const int part = blockIdx.x % kCenterParts;
+    const double m = *J.mean;
+    const long long M = *J.M;
     double s = 0.0, mx = 0.0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
-        const double v = Vc[i] - m;
-        Vc[i] = v;
+    for (long long i = (long long)part * blockDim.x + threadIdx.x; i < M; i += (long long)kCenterParts * blockDim.x) {
+        const double v = J.Vc[i] - m;
+        J.Vc[i] = v;
         s += v;
         mx = fmax(mx, fabs(v));
     }
-    if (!part) return;
     __shared__ double ss[kCenterThreads / 32], sm[kCenterThreads / 32];
     for (int o = 16; o > 0; o >>= 1) {
         s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -403,24 +449,26 @@ __global__ void __launch_bounds__(kCenterThreads) center_kernel(double *__restri
             t += ss[w];
             u = fmax(u, sm[w]);
         }
-        part[blockIdx.x] = make_double2(t, u);
+        J.vpart[part] = make_double2(t, u);
     }
 }
 
-// One warp: lane-strided partial sums, then a fixed shuffle tree (deterministic).
-__global__ void vstats_kernel(const double2 *__restrict__ part, int nb, double *__restrict__ vstats) {
+// One warp per job: its parts in a fixed shuffle tree (deterministic).
+__global__ void vstats_kernel(const __grid_constant__ FilterLaunch L) {
+    const FilterJob &J = L.job[blockIdx.x];
+    if (!J.vstats) return;
     double t = 0.0, u = 0.0;
-    for (int b = threadIdx.x; b < nb; b += 32) {
-        t += part[b].x;
-        u = fmax(u, part[b].y);
+    for (int b = threadIdx.x; b < kCenterParts; b += 32) {
+        t += J.vpart[b].x;
+        u = fmax(u, J.vpart[b].y);
     }
     for (int o = 16; o > 0; o >>= 1) {
         t += __shfl_xor_sync(0xffffffffu, t, o);
         u = fmax(u, __shfl_xor_sync(0xffffffffu, u, o));
     }
     if (threadIdx.x == 0) {
-        vstats[0] = t;
-        vstats[1] = u;
+        J.vstats[0] = t;
+        J.vstats[1] = u;
     }
 }
 
@@ -626,72 +674,129 @@ void FilterPlan::pack(char *dst) const {
     put(bidx.data(), bidx.size() * sizeof(int));
 }
 
-void filter_launch(rp_ctx *ctx, const FilterPlan &plan, const char *packed_dev, const double *V_dev,
-                   int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev, uint8_t *mask_dev, cudaStream_t stream,
-                   const std::string &tag, bool brick_order, double *vstats_dev) {
-    RP_REQUIRE(V_dev && M_dev && packed_dev, "rp_filter: null argument");
-    const FilterParams &p = plan.p;
-    const int nx = p.nx, ny = p.ny, nz = p.nz;
-    const long long n_total = p.n_total, capacity = n_total;
+namespace {
+// A job's plan arrays, read from its packed device image.
+void job_from_plan(const FilterPlan &plan, const char *packed_dev, FilterJob &J) {
     const char *src = packed_dev;
     auto take = [&](size_t n) {
         const char *r = src;
         src += al32(n);
         return r;
     };
-    const float4 *d_e32 = reinterpret_cast<const float4 *>(take(plan.e32.size() * sizeof(float4)));
-    const D4 *d_e64 = reinterpret_cast<const D4 *>(take(plan.e64.size() * sizeof(D4)));
-    const double *d_rmax2 = reinterpret_cast<const double *>(take(plan.rmax2.size() * sizeof(double)));
-    const float *d_rmax2f = reinterpret_cast<const float *>(take(plan.rmax2f.size() * sizeof(float)));
-    const int *d_boff = reinterpret_cast<const int *>(take(plan.boff.size() * sizeof(int)));
-    const int *d_bidx = reinterpret_cast<const int *>(take(plan.bidx.size() * sizeof(int)));
-    const int nblk = (int)((n_total + kFilterThreads - 1) / kFilterThreads);
-    uint8_t *d_mask = mask_dev ? mask_dev : ctx->buf_t<uint8_t>("flt_mask" + tag, (size_t)n_total);
-    int *d_counts = ctx->buf_t<int>("flt_counts" + tag, (size_t)nblk);
-    long long *d_offsets = ctx->buf_t<long long>("flt_offsets" + tag, (size_t)nblk);
-    double *d_vsum = ctx->buf_t<double>("flt_vsum" + tag, (size_t)nblk);
-    long long *d_total = M_dev;
-    double *d_mean = ctx->buf_t<double>("flt_mean" + tag, 1);
-    unsigned long long *d_re = ctx->buf_t<unsigned long long>("flt_rechecks" + tag, 1);
-    RP_CUDA(cudaMemsetAsync(d_re, 0, sizeof(unsigned long long), stream));
+    J.p = plan.p;
+    J.e32 = reinterpret_cast<const float4 *>(take(plan.e32.size() * sizeof(float4)));
+    J.e64 = reinterpret_cast<const D4 *>(take(plan.e64.size() * sizeof(D4)));
+    J.rmax2 = reinterpret_cast<const double *>(take(plan.rmax2.size() * sizeof(double)));
+    J.rmax2f = reinterpret_cast<const float *>(take(plan.rmax2f.size() * sizeof(float)));
+    J.boff = reinterpret_cast<const int *>(take(plan.boff.size() * sizeof(int)));
+    J.bidx = reinterpret_cast<const int *>(take(plan.bidx.size() * sizeof(int)));
+    J.nbx = (plan.p.nx + kBrickX - 1) / kBrickX;
+    J.nby = (plan.p.ny + kBrickY - 1) / kBrickY;
+}
+int bricks_of(const FilterParams &p) {
+    return ((p.nx + kBrickX - 1) / kBrickX) * ((p.ny + kBrickY - 1) / kBrickY) * ((p.nz + kBrickZ - 1) / kBrickZ);
+}
+}  // namespace
 
+void filter_group(rp_ctx *ctx, const std::vector<FilterItem> &items, cudaStream_t stream, const std::string &tag) {
+    if (items.empty()) return;
+    const size_t n = items.size();
+    std::vector<size_t> o_pts(n + 1, 0), o_br(n + 1, 0);
+    for (size_t i = 0; i < n; ++i) {
+        const FilterParams &p = items[i].plan->p;
+        RP_REQUIRE(items[i].V && items[i].M && items[i].packed_dev, "rp_filter: null argument");
+        o_pts[i + 1] = o_pts[i] + (size_t)p.n_total;
+        o_br[i + 1] = o_br[i] + (size_t)bricks_of(p);
+    }
+    uint8_t *mask = ctx->buf_t<uint8_t>("flt_mask" + tag, o_pts[n]);
+    int *counts = ctx->buf_t<int>("flt_bcounts" + tag, o_br[n]);
+    long long *offs = ctx->buf_t<long long>("flt_boffsets" + tag, o_br[n]);
+    double *vsum = ctx->buf_t<double>("flt_bvsum" + tag, o_br[n]);
+    double *mean = ctx->buf_t<double>("flt_mean" + tag, n);
+    double2 *vpart = ctx->buf_t<double2>("flt_vpart" + tag, n * kCenterParts);
     StageTimer t_f(ctx, "filter", stream);
-    const int nbx = (nx + kBrickX - 1) / kBrickX, nby = (ny + kBrickY - 1) / kBrickY,
-              nbz = (nz + kBrickZ - 1) / kBrickZ;
-    const int nbr = nbx * nby * nbz;
-    int *d_bc = ctx->buf_t<int>("flt_bcounts" + tag, (size_t)nbr);
-    filter_brick_kernel<<<nbr, kBrickPts, 0, stream>>>(p, nbx, nby, d_e32, d_e64, d_rmax2, d_rmax2f, d_boff, d_bidx,
-                                                       d_mask, d_bc, d_re);
-    RP_LAUNCH_CHECK();
-    if (!brick_order) {
-        flat_count_kernel<<<nblk, kFilterThreads, 0, stream>>>(d_mask, n_total, d_counts);
+    for (size_t j0 = 0; j0 < n; j0 += kFilterJobs) {
+        const size_t j1 = std::min(n, j0 + kFilterJobs);
+        FilterLaunch L{};
+        L.n = (int)(j1 - j0);
+        for (size_t i = j0; i < j1; ++i) {
+            FilterJob &J = L.job[i - j0];
+            job_from_plan(*items[i].plan, items[i].packed_dev, J);
+            J.V = items[i].V;
+            J.mask = mask + o_pts[i];
+            J.counts = counts + o_br[i];
+            J.offsets = offs + o_br[i];
+            J.vsum = vsum + o_br[i];
+            J.ncount = (int)(o_br[i + 1] - o_br[i]);
+            J.kept = items[i].kept;
+            J.Vc = items[i].Vc;
+            J.M = items[i].M;
+            J.mean = mean + i;
+            J.vpart = vpart + i * kCenterParts;
+            J.vstats = items[i].vstats;
+            L.blk[i - j0 + 1] = L.blk[i - j0] + J.ncount;
+        }
+        const int nbr = L.blk[L.n];
+        filter_brick_kernel<<<nbr, kBrickPts, 0, stream>>>(L, 1);
         RP_LAUNCH_CHECK();
-        scan_counts_kernel<<<1, 1024, 0, stream>>>(d_counts, nblk, d_offsets, d_total);
+        scan_counts_kernel<<<L.n, 1024, 0, stream>>>(L);
         RP_LAUNCH_CHECK();
-        compact_kernel<<<nblk, kFilterThreads, 0, stream>>>(d_mask, V_dev, n_total, d_offsets, capacity,
-                                                            kept_idx_dev, Vc_dev, d_vsum);
+        brick_compact_kernel<<<nbr, kBrickPts, 0, stream>>>(L);
         RP_LAUNCH_CHECK();
-        vmean_kernel<<<1, 1024, 0, stream>>>(d_vsum, nblk, d_total, d_mean);
+        vmean_kernel<<<L.n, 1024, 0, stream>>>(L);
         RP_LAUNCH_CHECK();
-    } else {
-        long long *d_bo = ctx->buf_t<long long>("flt_boffsets" + tag, (size_t)nbr);
-        double *d_bv = ctx->buf_t<double>("flt_bvsum" + tag, (size_t)nbr);
-        scan_counts_kernel<<<1, 1024, 0, stream>>>(d_bc, nbr, d_bo, d_total);
+        center_kernel<<<L.n * kCenterParts, kCenterThreads, 0, stream>>>(L);
         RP_LAUNCH_CHECK();
-        brick_compact_kernel<<<nbr, kBrickPts, 0, stream>>>(d_mask, V_dev, nx, ny, nz, nbx, nby, d_bo, capacity,
-                                                            kept_idx_dev, Vc_dev, d_bv);
-        RP_LAUNCH_CHECK();
-        vmean_kernel<<<1, 1024, 0, stream>>>(d_bv, nbr, d_total, d_mean);
+        vstats_kernel<<<L.n, 32, 0, stream>>>(L);
         RP_LAUNCH_CHECK();
     }
-    const int ncb = ctx->sm_count * 4;
-    double2 *d_part = vstats_dev ? ctx->buf_t<double2>("flt_vpart" + tag, (size_t)ncb) : nullptr;
-    center_kernel<<<ncb, kCenterThreads, 0, stream>>>(Vc_dev, d_total, d_mean, d_part);
-    RP_LAUNCH_CHECK();
-    if (vstats_dev) {
-        vstats_kernel<<<1, 32, 0, stream>>>(d_part, ncb, vstats_dev);
-        RP_LAUNCH_CHECK();
+}
+
+void filter_launch(rp_ctx *ctx, const FilterPlan &plan, const char *packed_dev, const double *V_dev,
+                   int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev, uint8_t *mask_dev, cudaStream_t stream,
+                   const std::string &tag, bool brick_order, double *vstats_dev) {
+    RP_REQUIRE(V_dev && M_dev && packed_dev, "rp_filter: null argument");
+    if (brick_order && !mask_dev) {
+        filter_group(ctx, {FilterItem{&plan, packed_dev, V_dev, kept_idx_dev, Vc_dev, M_dev, vstats_dev}}, stream,
+                     tag);
+        return;
     }
+    // flat order (rp_filter): the culled mask, then the compaction over flat blocks
+    const long long n_total = plan.p.n_total;
+    const int nblk = (int)((n_total + kFilterThreads - 1) / kFilterThreads);
+    FilterLaunch L{};
+    L.n = 1;
+    FilterJob &J = L.job[0];
+    job_from_plan(plan, packed_dev, J);
+    J.V = V_dev;
+    J.mask = mask_dev ? mask_dev : ctx->buf_t<uint8_t>("flt_mask" + tag, (size_t)n_total);
+    J.counts = ctx->buf_t<int>("flt_counts" + tag, (size_t)nblk);
+    J.offsets = ctx->buf_t<long long>("flt_offsets" + tag, (size_t)nblk);
+    J.vsum = ctx->buf_t<double>("flt_vsum" + tag, (size_t)nblk);
+    J.ncount = nblk;
+    J.kept = kept_idx_dev;
+    J.Vc = Vc_dev;
+    J.M = M_dev;
+    J.mean = ctx->buf_t<double>("flt_mean" + tag, 1);
+    J.vpart = ctx->buf_t<double2>("flt_vpart" + tag, kCenterParts);
+    J.vstats = vstats_dev;
+    StageTimer t_f(ctx, "filter", stream);
+    L.blk[1] = bricks_of(plan.p);
+    filter_brick_kernel<<<L.blk[1], kBrickPts, 0, stream>>>(L, 0);
+    RP_LAUNCH_CHECK();
+    flat_count_kernel<<<nblk, kFilterThreads, 0, stream>>>(J.mask, n_total, J.counts);
+    RP_LAUNCH_CHECK();
+    scan_counts_kernel<<<1, 1024, 0, stream>>>(L);
+    RP_LAUNCH_CHECK();
+    compact_kernel<<<nblk, kFilterThreads, 0, stream>>>(J.mask, V_dev, n_total, J.offsets, n_total, kept_idx_dev,
+                                                        Vc_dev, J.vsum);
+    RP_LAUNCH_CHECK();
+    vmean_kernel<<<1, 1024, 0, stream>>>(L);
+    RP_LAUNCH_CHECK();
+    center_kernel<<<kCenterParts, kCenterThreads, 0, stream>>>(L);
+    RP_LAUNCH_CHECK();
+    vstats_kernel<<<1, 32, 0, stream>>>(L);
+    RP_LAUNCH_CHECK();
 }
 
 void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const int *Z, int N, const double *V_dev,

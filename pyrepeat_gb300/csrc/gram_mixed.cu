@@ -1063,7 +1063,7 @@ static bool phi_bounds(const rp_ewald *ew, int S, const double *rn, int N, doubl
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
                 cudaStream_t stream, const double *vstats_dev, const std::string &slot, const double *rn,
-                int *clamp_dev) {
+                int *clamp_dev, const double *d_atoms_pre, const float2 *E_pre) {
     RP_REQUIRE(N > 0 && M > 0, "rp_gram: need N > 0 and M > 0");
     std::vector<double> sh;
     int zero_idx = -1;
@@ -1073,20 +1073,29 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     const int nx = ew->grid.n_grid[0], ny = ew->grid.n_grid[1];
     const int n1c = ew->kmax;
 
-    double *d_atoms = ctx->buf_t<double>("g_atoms" + slot, 3 * (size_t)N);
+    const double *d_atoms = d_atoms_pre;
+    if (!d_atoms) {
+        double *a = ctx->buf_t<double>("g_atoms" + slot, 3 * (size_t)N);
+        RP_CUDA(cudaMemcpyAsync(a, atoms, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
+        d_atoms = a;
+    }
     double *d_shifts = ctx->buf_t<double>("g_shifts" + slot, sh.size());
     double *d_axis = ctx->buf_t<double>("g_axis" + slot, 9);
-    RP_CUDA(cudaMemcpyAsync(d_atoms, atoms, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_shifts, sh.data(), sizeof(double) * sh.size(), cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice, stream));
     int *d_status = ctx->status_words();  // cleared by the caller (rp_gram / the batch driver)
 
-    // reciprocal rows of every atom (stages A and B) and the double-float images, once per fit
-    float2 *E = ctx->buf_t<float2>("m_E" + slot, recip_rows_bytes(ew, N) / sizeof(float2));
+    // reciprocal rows of every atom (stages A and B; or the caller's, computed for a whole
+    // pipeline group) and the double-float images, once per fit
+    const float2 *E = E_pre;
     float4 *img = ctx->buf_t<float4>("m_img" + slot, 2 * (size_t)N * S);
     {
         StageTimer tt(ctx, "recip_rows", stream);
-        recip_rows(ctx, ew, d_atoms, nullptr, N, E, stream, slot);
+        if (!E) {
+            float2 *e = ctx->buf_t<float2>("m_E" + slot, recip_rows_bytes(ew, N) / sizeof(float2));
+            recip_rows(ctx, ew, d_atoms, nullptr, N, e, stream, slot);
+            E = e;
+        }
         images_df_kernel<<<ceil_div((long long)N * S, 128), 128, 0, stream>>>(d_atoms, N, d_shifts, S, img);
         RP_LAUNCH_CHECK();
     }

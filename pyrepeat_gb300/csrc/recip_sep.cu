@@ -30,24 +30,55 @@
 namespace rp {
 namespace {
 
-struct Rec9 {
-    double b[9];
+// One fit's reciprocal rows: its tables, scratch and output.  A launch carries up to
+// kRecipJobs of them by value; every kernel below runs the blocks of all its jobs, job j
+// owning blocks [blk[k][j], blk[k][j+1]) of kernel k, so a pipeline group of cubes costs one
+// launch per stage instead of one per cube.
+struct RecipJob {
+    const double *atoms;   // [3N]
+    const double *q;       // [N] charges (one weighted column) or nullptr (a column per atom)
+    const int *kidx;       // [3K]
+    const double *kcoef;   // [K]
+    const float4 *EY, *EZ; // double-float phases of the grid rows / planes
+    double2 *U;
+    float4 *Udf;
+    float2 *W, *F, *E;
+    double rb[9];          // reciprocal basis (rows)
+    int N, ncols, K, P, ny, nz, ab;
 };
+constexpr int kRecipJobs = 64;
+struct RecipLaunch {
+    int n;
+    int blk[kRecipJobs + 1];  // block offsets of the jobs in this kernel's grid
+    RecipJob job[kRecipJobs];
+};
+
+// the job that owns block b (binary search over the offsets)
+__device__ __forceinline__ int recip_job_of(const RecipLaunch &L, int b) {
+    int lo = 0, hi = L.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (L.blk[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 // U[a][d][n + P] = e^{-i n (b_d . r_a)} for n in [-P, P]: the per-axis atom phases, so that
 // e^{-i k.r_a} = U[a][0][n1] U[a][1][n2] U[a][2][n3] needs 3 (2P+1) sincos per atom instead of K.
-__global__ void atom_phases_kernel(const double *__restrict__ atoms, int N, Rec9 rb, int P,
-                                   double2 *__restrict__ U, float4 *__restrict__ Udf) {
-    const int nw = 2 * P + 1;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= N * 3 * nw) return;
+__global__ void atom_phases_kernel(const __grid_constant__ RecipLaunch L) {
+    const int jb = recip_job_of(L, blockIdx.x);
+    const RecipJob &J = L.job[jb];
+    const int P = J.P, nw = 2 * P + 1;
+    const int t = (blockIdx.x - L.blk[jb]) * blockDim.x + threadIdx.x;
+    if (t >= J.N * 3 * nw) return;
     const int n = t % nw - P, d = (t / nw) % 3, a = t / (3 * nw);
-    const double *p = atoms + 3 * a;
-    const double th = (p[0] * rb.b[3 * d] + p[1] * rb.b[3 * d + 1]) + p[2] * rb.b[3 * d + 2];
+    const double *p = J.atoms + 3 * a;
+    const double th = (p[0] * J.rb[3 * d] + p[1] * J.rb[3 * d + 1]) + p[2] * J.rb[3 * d + 2];
     double s, c;
     sincos((double)n * th, &s, &c);
-    U[t] = make_double2(c, -s);
-    Udf[t] = dfa::split(c, -s);
+    J.U[t] = make_double2(c, -s);
+    J.Udf[t] = dfa::split(c, -s);
 }
 
 __device__ __forceinline__ double2 cmul(double2 x, double2 y) {
@@ -57,42 +88,43 @@ __device__ __forceinline__ double2 cmul(double2 x, double2 y) {
 // W[col][n2'][n3'][n1] = w_k e^{-i k.r} (col = atom), or sum_a q_a w_k e^{-i k.r_a} (one
 // charge-weighted column when q != nullptr), stored rounded to FP32.  Per atom the two
 // phase products and the weight are double-float products on the FP32 pipe (~2^-44
-// relative); the charge-weighted sum stays FP64.
-__global__ void build_w_kernel(const int *__restrict__ kidx, const double *__restrict__ kcoef, int K, int P,
-                               const double2 *__restrict__ U, const float4 *__restrict__ Udf,
-                               const double *__restrict__ q, int N, int ncols, float2 *__restrict__ W) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)ncols * K) return;
+// relative); the charge-weighted sum stays FP64.  (W is zero outside the k-set: the host
+// clears it before this launch.)
+__global__ void build_w_kernel(const __grid_constant__ RecipLaunch L) {
+    const int jb = recip_job_of(L, blockIdx.x);
+    const RecipJob &J = L.job[jb];
+    const long long t = (long long)(blockIdx.x - L.blk[jb]) * blockDim.x + threadIdx.x;
+    const int K = J.K, P = J.P;
+    if (t >= (long long)J.ncols * K) return;
     const int col = (int)(t / K), k = (int)(t - (long long)col * K);
     const int n1c = P + 1, nw = 2 * P + 1;
-    const int n1 = kidx[3 * k], n2 = kidx[3 * k + 1] + P, n3 = kidx[3 * k + 2] + P;
-    double2 z;
-    if (q == nullptr) {
-        const float4 *u = Udf + (size_t)col * 3 * nw;
+    const int n1 = J.kidx[3 * k], n2 = J.kidx[3 * k + 1] + P, n3 = J.kidx[3 * k + 2] + P;
+    float2 *out = J.W + (((long long)col * nw + n2) * nw + n3) * n1c + n1;
+    if (J.q == nullptr) {
+        const float4 *u = J.Udf + (size_t)col * 3 * nw;
         dfa::acc re{0.f, 0.f}, im{0.f, 0.f};
         dfa::cmac(re, im, u[n1 + P], u[nw + n2]);
         const float4 z12 = dfa::pack(re, im);
         re = im = dfa::acc{0.f, 0.f};
         dfa::cmac(re, im, z12, u[2 * nw + n3]);
         const float4 z3 = dfa::pack(re, im);
-        const double w = kcoef[k];
+        const double w = J.kcoef[k];
         const float wh = (float)w, wl = (float)(w - (double)wh);
         re = im = dfa::acc{0.f, 0.f};
         dfa::mac(re, wh, wl, z3.x, z3.y);
         dfa::mac(im, wh, wl, z3.z, z3.w);
-        W[(((long long)col * nw + n2) * nw + n3) * n1c + n1] = make_float2(dfa::norm(re).x, dfa::norm(im).x);
+        *out = make_float2(dfa::norm(re).x, dfa::norm(im).x);
         return;
-    } else {
-        z = make_double2(0.0, 0.0);
-        for (int a = 0; a < N; ++a) {
-            const double2 *u = U + (size_t)a * 3 * nw;
-            const double2 v = cmul(cmul(u[n1 + P], u[nw + n2]), u[2 * nw + n3]);
-            z.x += q[a] * v.x;
-            z.y += q[a] * v.y;
-        }
     }
-    const double w = kcoef[k];
-    W[(((long long)col * nw + n2) * nw + n3) * n1c + n1] = make_float2((float)(w * z.x), (float)(w * z.y));
+    double2 z = make_double2(0.0, 0.0);
+    for (int a = 0; a < J.N; ++a) {
+        const double2 *u = J.U + (size_t)a * 3 * nw;
+        const double2 v = cmul(cmul(u[n1 + P], u[nw + n2]), u[2 * nw + n3]);
+        z.x += J.q[a] * v.x;
+        z.y += J.q[a] * v.y;
+    }
+    const double w = J.kcoef[k];
+    *out = make_float2((float)(w * z.x), (float)(w * z.y));
 }
 
 // Each stage-A thread produces up to kN1B consecutive n1 outputs of one (plane, n2,
@@ -102,16 +134,18 @@ constexpr int kN1B = 8;
 
 // Stage A, one thread per (n2, column, n1 block, plane l) with l fastest: a warp reads
 // one W row (broadcast) and consecutive ez phases (coalesced); FP32 products.
-__global__ void recip_stage_a_kernel(const float2 *__restrict__ W, const float4 *__restrict__ EZ, int ncols, int P,
-                                     int nz, float2 *__restrict__ F) {
-    extern __shared__ float2 ezs[];  // the whole ez table [nw][nz] (FP32), read once per CTA
+__global__ void recip_stage_a_kernel(const __grid_constant__ RecipLaunch L) {
+    extern __shared__ float2 ezs[];  // the job's ez table [nw][nz] (FP32), read once per CTA
+    const int jb = recip_job_of(L, blockIdx.x);
+    const RecipJob &J = L.job[jb];
+    const int P = J.P, nz = J.nz, ncols = J.ncols;
     const int n1c = P + 1, nw = 2 * P + 1, nb = (n1c + kN1B - 1) / kN1B;
     for (int q = threadIdx.x; q < nw * nz; q += blockDim.x) {
-        const float4 e = EZ[q];
+        const float4 e = J.EZ[q];
         ezs[q] = make_float2(e.x, e.z);
     }
     __syncthreads();
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long t = (long long)(blockIdx.x - L.blk[jb]) * blockDim.x + threadIdx.x;
     if (t >= (long long)nz * nw * ncols * nb) return;
     const int l = (int)(t % nz);
     t /= nz;
@@ -123,7 +157,7 @@ __global__ void recip_stage_a_kernel(const float2 *__restrict__ W, const float4 
     float re[kN1B], im[kN1B];
 #pragma unroll
     for (int u = 0; u < kN1B; ++u) re[u] = im[u] = 0.f;
-    const float2 *w = W + ((long long)a * nw + n2) * nw * n1c + n10;
+    const float2 *w = J.W + ((long long)a * nw + n2) * nw * n1c + n10;
     for (int n3 = 0; n3 < nw; ++n3) {
         const float2 z = ezs[n3 * nz + l];
         const float2 *wr = w + (long long)n3 * n1c;
@@ -137,47 +171,49 @@ __global__ void recip_stage_a_kernel(const float2 *__restrict__ W, const float4 
                 im[u] = fmaf(z.y, v.x, im[u]);
             }
     }
-    float2 *o = F + (((long long)l * nw + n2) * ncols + a) * n1c + n10;
+    float2 *o = J.F + (((long long)l * nw + n2) * ncols + a) * n1c + n10;
 #pragma unroll
     for (int u = 0; u < kN1B; ++u)
         if (u < cnt) o[u] = make_float2(re[u], im[u]);
 }
 
-// Stage B, one CTA per (plane l, block of `ab` columns).  The plane's F slab for those
-// columns ([n2][a][n1], FP32) and the ey phases ([n2][j], rows padded to kJB) sit in shared
-// memory.  A thread owns one (column, n1) and kJB consecutive rows j: its F value is one
-// load per n2, the ey values are warp broadcasts read two rows at a time, and a warp's
+// Stage B, one CTA per (plane l, block of `ab` columns) of a job.  The plane's F slab for
+// those columns ([n2][a][n1], FP32) and the ey phases ([n2][j], rows padded to kJB) sit in
+// shared memory.  A thread owns one (column, n1) and kJB consecutive rows j: its F value is
+// one load per n2, the ey values are warp broadcasts read two rows at a time, and a warp's
 // stores of E land on consecutive (column, n1) of one row, contiguous in memory.
 constexpr int kJB = 8;
-__global__ void __launch_bounds__(128) recip_stage_b_kernel(const float2 *__restrict__ F,
-                                                            const float4 *__restrict__ EY, int ncols, int P, int ny,
-                                                            int ab, float2 *__restrict__ E) {
+__global__ void __launch_bounds__(128) recip_stage_b_kernel(const __grid_constant__ RecipLaunch L) {
     extern __shared__ float4 smem_b[];
+    const int jb = recip_job_of(L, blockIdx.x);
+    const RecipJob &J = L.job[jb];
+    const int P = J.P, ncols = J.ncols, ny = J.ny, ab = J.ab;
     const int n1c = P + 1, nw = 2 * P + 1;
-    const int l = blockIdx.y, a0 = blockIdx.x * ab, na = min(ab, ncols - a0);
+    const int nbx = (ncols + ab - 1) / ab, bloc = blockIdx.x - L.blk[jb];
+    const int l = bloc / nbx, a0 = (bloc - l * nbx) * ab, na = min(ab, ncols - a0);
     const int an = na * n1c;                                  // (column, n1) pairs of the CTA
     const int nyp = (ny + kJB - 1) / kJB * kJB;
     float2 *fs = reinterpret_cast<float2 *>(smem_b);          // [nw][an]
     float2 *eys = fs + ((nw * ab * n1c + 1) & ~1);           // [nw][nyp], 16-byte aligned rows
     for (int t = threadIdx.x; t < nw * an; t += blockDim.x) {
         const int n2 = t / an, r = t - n2 * an;
-        fs[t] = F[(((long long)l * nw + n2) * ncols + a0) * n1c + r];
+        fs[t] = J.F[(((long long)l * nw + n2) * ncols + a0) * n1c + r];
     }
     for (int q = threadIdx.x; q < nw * nyp; q += blockDim.x) {
         const int n2 = q / nyp, j = q - n2 * nyp;
-        const float4 y = j < ny ? EY[n2 * ny + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 y = j < ny ? J.EY[n2 * ny + j] : make_float4(0.f, 0.f, 0.f, 0.f);
         eys[q] = make_float2(y.x, y.z);
     }
     __syncthreads();
     const int tasks = an * (nyp / kJB);
     for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
-        const int jb = task / an, r = task - jb * an;  // r = a n1c + n1
+        const int jj = task / an, r = task - jj * an;  // r = a n1c + n1
         float re[kJB], im[kJB];
 #pragma unroll
         for (int u = 0; u < kJB; ++u) re[u] = im[u] = 0.f;
         for (int n2 = 0; n2 < nw; ++n2) {
             const float2 f = fs[n2 * an + r];
-            const float4 *yp = reinterpret_cast<const float4 *>(eys + n2 * nyp + jb * kJB);
+            const float4 *yp = reinterpret_cast<const float4 *>(eys + n2 * nyp + jj * kJB);
 #pragma unroll
             for (int u = 0; u < kJB / 2; ++u) {
                 const float4 y = yp[u];  // rows 2u and 2u+1: (re, im, re, im)
@@ -191,12 +227,22 @@ __global__ void __launch_bounds__(128) recip_stage_b_kernel(const float2 *__rest
                 im[2 * u + 1] = fmaf(y.w, f.x, im[2 * u + 1]);
             }
         }
-        float2 *o = E + (((long long)l * ny + jb * kJB) * ncols + a0) * n1c + r;
+        float2 *o = J.E + (((long long)l * ny + jj * kJB) * ncols + a0) * n1c + r;
         const long long row_stride = (long long)ncols * n1c;
 #pragma unroll
         for (int u = 0; u < kJB; ++u)
-            if (jb * kJB + u < ny) o[u * row_stride] = make_float2(re[u], im[u]);
+            if (jj * kJB + u < ny) o[u * row_stride] = make_float2(re[u], im[u]);
     }
+}
+
+// stage B's columns per CTA: as many as fit 48 KB of shared memory (at most 16)
+int stage_b_columns(int P) {
+    const size_t col_bytes = sizeof(float2) * (size_t)(2 * P + 1) * (P + 1);
+    return (int)std::max<size_t>(1, std::min<size_t>(16, (48u << 10) / col_bytes));
+}
+size_t stage_b_smem(int P, int ny, int ab) {
+    const size_t nw = 2 * P + 1, n1c = P + 1, nyp = (size_t)(ny + kJB - 1) / kJB * kJB;
+    return sizeof(float2) * (((size_t)nw * ab * n1c + 1) & ~(size_t)1) + sizeof(float2) * nw * nyp;
 }
 
 }  // namespace
@@ -207,46 +253,85 @@ size_t recip_rows_bytes(const rp_ewald *ew, int ncols) {
     return sizeof(float2) * (size_t)nrows * ncols * n1c;
 }
 
+void recip_rows_group(rp_ctx *ctx, const std::vector<RecipRowsJob> &jobs, cudaStream_t stream,
+                      const std::string &tag) {
+    if (jobs.empty()) return;
+    // scratch of every job in one arena per kind; the W arena is cleared with one memset
+    std::vector<size_t> oW(jobs.size() + 1, 0), oF(jobs.size() + 1, 0), oU(jobs.size() + 1, 0);
+    for (size_t j = 0; j < jobs.size(); ++j) {
+        const rp_ewald *ew = jobs[j].ew;
+        const int P = std::max(ew->kmax - 1, 0), n1c = P + 1, nw = 2 * P + 1;
+        const int ncols = jobs[j].d_q ? 1 : jobs[j].N;
+        const bool live = ew->K > 0;
+        oW[j + 1] = oW[j] + (live ? (size_t)ncols * nw * nw * n1c : 0);
+        oF[j + 1] = oF[j] + (live ? (size_t)ew->grid.n_grid[2] * nw * ncols * n1c : 0);
+        oU[j + 1] = oU[j] + (live ? (size_t)jobs[j].N * 3 * nw : 0);
+    }
+    const size_t nj = jobs.size();
+    float2 *W = ctx->buf_t<float2>("rs_W" + tag, std::max<size_t>(oW[nj], 1));
+    float2 *F = ctx->buf_t<float2>("rs_F" + tag, std::max<size_t>(oF[nj], 1));
+    double2 *U = ctx->buf_t<double2>("rs_U" + tag, std::max<size_t>(oU[nj], 1));
+    float4 *Udf = ctx->buf_t<float4>("rs_Udf" + tag, std::max<size_t>(oU[nj], 1));
+    if (oW[nj]) RP_CUDA(cudaMemsetAsync(W, 0, sizeof(float2) * oW[nj], stream));
+    for (size_t j0 = 0; j0 < nj; j0 += kRecipJobs) {
+        const size_t j1 = std::min(nj, j0 + kRecipJobs);
+        RecipLaunch L{};
+        int blk[4][kRecipJobs + 1] = {};
+        size_t smem_a = 0, smem_b = 0;
+        L.n = 0;
+        for (size_t j = j0; j < j1; ++j) {
+            const RecipRowsJob &rj = jobs[j];
+            const rp_ewald *ew = rj.ew;
+            const int ncols = rj.d_q ? 1 : rj.N;
+            if (ew->K == 0) {  // no k-vectors (the non-periodic basis): E is zero
+                RP_CUDA(cudaMemsetAsync(rj.E, 0, recip_rows_bytes(ew, ncols), stream));
+                continue;
+            }
+            const int P = ew->kmax - 1, n1c = P + 1, nw = 2 * P + 1;
+            const int ny = ew->grid.n_grid[1], nz = ew->grid.n_grid[2];
+            RecipJob &J = L.job[L.n];
+            J.atoms = rj.d_atoms; J.q = rj.d_q; J.kidx = ew->d_kidx; J.kcoef = ew->d_kcoef;
+            J.EY = ew->d_eyf; J.EZ = ew->d_ezf;
+            J.U = U + oU[j]; J.Udf = Udf + oU[j]; J.W = W + oW[j]; J.F = F + oF[j]; J.E = rj.E;
+            for (int q = 0; q < 9; ++q) J.rb[q] = ew->rec[q];
+            J.N = rj.N; J.ncols = ncols; J.K = ew->K; J.P = P; J.ny = ny; J.nz = nz; J.ab = stage_b_columns(P);
+            const int nb = (n1c + kN1B - 1) / kN1B;
+            const int k = L.n;
+            blk[0][k + 1] = blk[0][k] + (int)ceil_div((long long)rj.N * 3 * nw, 128);
+            blk[1][k + 1] = blk[1][k] + (int)ceil_div((long long)ncols * ew->K, 128);
+            blk[2][k + 1] = blk[2][k] + (int)ceil_div((long long)nz * nw * ncols * nb, 128);
+            blk[3][k + 1] = blk[3][k] + (int)ceil_div(ncols, J.ab) * nz;
+            smem_a = std::max(smem_a, sizeof(float2) * (size_t)nw * nz);
+            smem_b = std::max(smem_b, stage_b_smem(P, ny, J.ab));
+            ++L.n;
+        }
+        if (L.n == 0) continue;
+        RP_REQUIRE(smem_a <= (200u << 10), "recip_rows: grid too large along z for KMAX");
+        RP_REQUIRE(smem_b <= (200u << 10), "recip_rows: KMAX too large");
+        smem_optin((const void *)recip_stage_a_kernel, smem_a);
+        smem_optin((const void *)recip_stage_b_kernel, smem_b);
+        auto with = [&](int k) {
+            std::copy(blk[k], blk[k] + L.n + 1, L.blk);
+            return blk[k][L.n];
+        };
+        int g = with(0);
+        atom_phases_kernel<<<g, 128, 0, stream>>>(L);
+        RP_LAUNCH_CHECK();
+        g = with(1);
+        build_w_kernel<<<g, 128, 0, stream>>>(L);
+        RP_LAUNCH_CHECK();
+        g = with(2);
+        recip_stage_a_kernel<<<g, 128, smem_a, stream>>>(L);
+        RP_LAUNCH_CHECK();
+        g = with(3);
+        recip_stage_b_kernel<<<g, 128, smem_b, stream>>>(L);
+        RP_LAUNCH_CHECK();
+    }
+}
+
 void recip_rows(rp_ctx *ctx, const rp_ewald *ew, const double *d_atoms, const double *d_q, int N, float2 *E,
                 cudaStream_t stream, const std::string &slot) {
-    const int P = ew->kmax - 1, n1c = P + 1, nw = 2 * P + 1;
-    const int ny = ew->grid.n_grid[1], nz = ew->grid.n_grid[2];
-    const int ncols = d_q ? 1 : N;
-    const long long nrows = (long long)ny * nz;
-    if (ew->K == 0) {
-        RP_CUDA(cudaMemsetAsync(E, 0, recip_rows_bytes(ew, ncols), stream));
-        return;
-    }
-    const size_t nW = (size_t)ncols * nw * nw * n1c, nF = (size_t)nz * nw * ncols * n1c;
-    float2 *W = ctx->buf_t<float2>("rs_W" + slot, nW);
-    float2 *F = ctx->buf_t<float2>("rs_F" + slot, nF);
-    double2 *U = ctx->buf_t<double2>("rs_U" + slot, (size_t)N * 3 * nw);
-    float4 *Udf = ctx->buf_t<float4>("rs_Udf" + slot, (size_t)N * 3 * nw);
-    RP_CUDA(cudaMemsetAsync(W, 0, sizeof(float2) * nW, stream));
-    Rec9 rb;
-    for (int q = 0; q < 9; ++q) rb.b[q] = ew->rec[q];
-    atom_phases_kernel<<<ceil_div((long long)N * 3 * nw, 128), 128, 0, stream>>>(d_atoms, N, rb, P, U, Udf);
-    RP_LAUNCH_CHECK();
-    const long long nk = (long long)ncols * ew->K;
-    build_w_kernel<<<ceil_div(nk, 128), 128, 0, stream>>>(ew->d_kidx, ew->d_kcoef, ew->K, P, U, Udf, d_q, N,
-                                                      ncols, W);
-    RP_LAUNCH_CHECK();
-    const int nb = (n1c + kN1B - 1) / kN1B;
-    const size_t smem_a = sizeof(float2) * (size_t)nw * nz;
-    RP_REQUIRE(smem_a <= (200u << 10), "recip_rows: grid too large along z for KMAX");
-    smem_optin((const void *)recip_stage_a_kernel, smem_a);
-    recip_stage_a_kernel<<<ceil_div((long long)nz * nw * ncols * nb, 128), 128, smem_a, stream>>>(W, ew->d_ezf, ncols,
-                                                                                                  P, nz, F);
-    RP_LAUNCH_CHECK();
-    // stage B: as many columns per CTA as fit 48 KB of shared memory (at most 16)
-    const size_t col_bytes = sizeof(float2) * (size_t)nw * n1c;
-    const int ab = (int)std::max<size_t>(1, std::min<size_t>(16, (48u << 10) / col_bytes));
-    const size_t nyp = (size_t)(ny + kJB - 1) / kJB * kJB;
-    const size_t smem = sizeof(float2) * (((size_t)nw * ab * n1c + 1) & ~(size_t)1) + sizeof(float2) * (size_t)nw * nyp;
-    RP_REQUIRE(smem <= (200u << 10), "recip_rows: KMAX too large");
-    smem_optin((const void *)recip_stage_b_kernel, smem);
-    recip_stage_b_kernel<<<dim3(ceil_div(ncols, ab), nz), 128, smem, stream>>>(F, ew->d_eyf, ncols, P, ny, ab, E);
-    RP_LAUNCH_CHECK();
+    recip_rows_group(ctx, {RecipRowsJob{ew, d_atoms, d_q, N, E}}, stream, slot);
 }
 
 }  // namespace rp

@@ -295,7 +295,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
     constexpr int kLanes = 4;
     const int lanes = ctx->timing ? 1 : kLanes;  // stage timing: one lane, each stage alone
     auto glane = [&](int i) { return ctx->lane(i % lanes); };
-    auto flane = [&](int i) { return ctx->timing ? ctx->lane(0) : ctx->lane(kLanes + i % kLanes); };
+    auto flane = [&](int i) { return ctx->timing ? ctx->lane(0) : ctx->lane(kLaneFilter0 + i % kLanes); };
     const int ngroups = (n >= 64 && !ctx->timing) ? 4 : 1;
     r.ngroups = ngroups;
     r.g0.assign((size_t)ngroups + 1, 0);
@@ -336,7 +336,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
             RP_CUDA(cudaStreamWaitEvent(flane(ln), up, 0));
         }
     }
-    const cudaStream_t copy_lane = ctx->lane(2 * kLanes);  // uploads: plans, grids, tables
+    const cudaStream_t copy_lane = ctx->lane(kLaneCopy);  // uploads: plans, grids, tables
     RP_CUDA(cudaStreamWaitEvent(copy_lane, r.events.back(), 0));
     std::vector<size_t> pl_off((size_t)n + 1, 0);
     std::vector<cudaEvent_t> kept_ready((size_t)ngroups);
@@ -359,14 +359,21 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
                                         cudaMemcpyHostToDevice, copy_lane));
         const cudaEvent_t inputs = record(copy_lane);
         for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(flane(ln), inputs, 0));
+        // the group's mixed-precision cubes in one launch per filter stage (brick order), the
+        // FP64 ones (flat order, the comparator) one by one
+        std::vector<rp::FilterItem> items;
         for (int i = i0; i < i1; ++i) {
             const rp_fit_desc &d = descs[i];
             const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
-            const int ln = i % lanes;
-            rp::filter_launch(ctx, plan(i), pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i], Md + i,
-                              nullptr, flane(i), "#f" + std::to_string(ln), d.precision == RP_PREC_MIXED,
-                              vst + 2 * i);
+            if (d.precision == RP_PREC_MIXED) {
+                items.push_back(rp::FilterItem{&plan(i), pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i],
+                                               Md + i, vst + 2 * i});
+            } else {
+                rp::filter_launch(ctx, plan(i), pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i], Md + i,
+                                  nullptr, flane(i), "#f" + std::to_string(i % lanes), false, vst + 2 * i);
+            }
         }
+        rp::filter_group(ctx, items, flane(g), "#fg" + std::to_string(g));
         for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(stream, record(flane(ln)), 0));
         RP_CUDA(cudaMemcpyAsync(Mh + i0, Md + i0, sizeof(long long) * (i1 - i0), cudaMemcpyDeviceToHost, stream));
         kept_ready[g] = record(stream);
@@ -383,16 +390,45 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
         r.ews[i]->device = ctx->device;
         ew_off[i + 1] = ew_off[i] + rp::ewald_layout(&descs[i].grid, descs[i].kmax, off9);
     }
-    char *ew_dev = static_cast<char *>(ctx->buf("fit_ewald", ew_off[n]));
-    char *ew_host = static_cast<char *>(ctx->host_buf("fit_ewald", ew_off[n]));
+    // the atoms of every cube follow the tables in the same arena
+    const size_t at_off = (ew_off[n] + 255) / 256 * 256;
+    char *ew_dev = static_cast<char *>(ctx->buf("fit_ewald", at_off + sizeof(double) * 3 * off_n[n]));
+    char *ew_host = static_cast<char *>(ctx->host_buf("fit_ewald", at_off + sizeof(double) * 3 * off_n[n]));
+    double *atoms_dev = reinterpret_cast<double *>(ew_dev + at_off);
     ctx->parallel(n, [&](int i) {
         rp::ewald_build_host(r.ews[i], &descs[i].grid, descs[i].cutoff, descs[i].kmax, ew_host + ew_off[i]);
+        std::copy(descs[i].atoms, descs[i].atoms + 3 * (size_t)descs[i].N,
+                  reinterpret_cast<double *>(ew_host + at_off) + 3 * off_n[i]);
     });
     for (int i = 0; i < n; ++i) rp::ewald_place(r.ews[i], ew_dev + ew_off[i]);
-    RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, ew_off[n], cudaMemcpyHostToDevice, copy_lane));
+    RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, at_off + sizeof(double) * 3 * off_n[n], cudaMemcpyHostToDevice,
+                            copy_lane));
     const cudaEvent_t tables = record(copy_lane);
     for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(glane(ln), tables, 0));
     RP_CUDA(cudaStreamWaitEvent(stream, tables, 0));
+    // reciprocal rows of every mixed-precision cube, a pipeline group per launch set, on a
+    // stream of their own: they need only the tables and atoms, so they run beside the
+    // filters, and each group's normal equations wait for its rows
+    std::vector<size_t> e_off((size_t)n + 1, 0);
+    for (int i = 0; i < n; ++i)
+        e_off[i + 1] = e_off[i] + (descs[i].precision == RP_PREC_MIXED
+                                       ? recip_rows_bytes(r.ews[i], descs[i].N) / sizeof(float2) : 0);
+    float2 *E_all = ctx->buf_t<float2>("fit_E", std::max<size_t>(e_off[n], 1));
+    const cudaStream_t recip_lane = ctx->timing ? ctx->lane(0) : ctx->lane(kLaneRecip);
+    RP_CUDA(cudaStreamWaitEvent(recip_lane, tables, 0));
+    std::vector<cudaEvent_t> rows_ready((size_t)ngroups);
+    for (int g = 0; g < ngroups; ++g) {
+        std::vector<rp::RecipRowsJob> rj;
+        for (int i = g0[g]; i < g0[g + 1]; ++i)
+            if (descs[i].precision == RP_PREC_MIXED)
+                rj.push_back(rp::RecipRowsJob{r.ews[i], atoms_dev + 3 * off_n[i], nullptr, descs[i].N,
+                                              E_all + e_off[i]});
+        {
+            StageTimer tt(ctx, "recip_rows", recip_lane);
+            rp::recip_rows_group(ctx, rj, recip_lane, "#r" + std::to_string(g));
+        }
+        rows_ready[g] = record(recip_lane);
+    }
     // 3. normal equations, group by group as the kept counts arrive.  Mixed-precision fits
     //    are spread over the gram streams (each with its own scratch), so one cube's small
     //    kernels and launch gaps overlap another's; the FP64 comparator stays on the
@@ -415,14 +451,18 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
             if (M_out) M_out[i] = r.M[i];
             RP_REQUIRE(r.M[i] > 0, "rp_fit: no grid point of cube " + std::to_string(i) + " survives the vdW filter");
         }
-        for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(glane(ln), kept_ready[g], 0));
+        for (int ln = 0; ln < lanes; ++ln) {
+            RP_CUDA(cudaStreamWaitEvent(glane(ln), kept_ready[g], 0));
+            RP_CUDA(cudaStreamWaitEvent(glane(ln), rows_ready[g], 0));
+        }
         for (int i = g0[g]; i < g0[g + 1]; ++i) {
             const rp_fit_desc &d = descs[i];
             if (d.precision == RP_PREC_MIXED) {
                 const int ln = i % lanes;
                 rp::gram_mixed(ctx, r.ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], r.M[i],
                                A + off_nn[i], b + off_n[i], nullptr, glane(ln), vst + 2 * i,
-                               "#" + std::to_string(ln), rn.data() + off_n[i], clamps + i);
+                               "#" + std::to_string(ln), rn.data() + off_n[i], clamps + i,
+                               atoms_dev + 3 * off_n[i], E_all + e_off[i]);
             } else {
                 rp::gram_fp64(ctx, r.ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], r.M[i],
                               A + off_nn[i], b + off_n[i], nullptr, stream);
@@ -621,7 +661,7 @@ void batch_server_loop(rp_ctx *ctx) {
             try {
                 const BatchServer::Job &j = f->job;
                 batch_enqueue(ctx, (int)j.descs.size(), j.descs.data(), j.has_vdev ? j.vdev.data() : nullptr,
-                              j.q_out, j.M_out, j.info_out, ctx->lane(kSlotLanes - 1), *f->run);
+                              j.q_out, j.M_out, j.info_out, ctx->lane(kLaneBatch), *f->run);
             } catch (const Error &e) {
                 failed(*f, e.code, e.msg);
             } catch (const std::exception &e) {

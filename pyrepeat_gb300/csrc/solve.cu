@@ -35,7 +35,10 @@ namespace rp {
 
 namespace {
 
-__global__ void build_bordered_kernel(SolveDesc d) {
+// Folded bordered matrices of many systems in one launch: blockIdx.y picks the system (from
+// `sys`, the ones with disjoint groups), the blocks along x stride over its (n+1)^2 entries.
+__global__ void build_bordered_kernel(const SolveDesc *__restrict__ descs, const int *__restrict__ sys) {
+    const SolveDesc d = descs[sys[blockIdx.y]];
     const int n1 = d.n + 1;
     long long total = (long long)n1 * n1;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
@@ -1080,12 +1083,20 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
         o_red += (size_t)n1;
         o_sq += (size_t)n1 * n1;
     }
+    // wide systems are factored across the GPU before the refinement kernel: their flags
+    std::vector<int> disjoint;
+    for (int j = 0; j < nj; ++j) {
+        const int n1 = plans[j].n + 1;
+        if (n1 >= kLUWideMin && n1 <= kLUWideMax) descs[j].pre = d_pre + 3 * (size_t)j;
+        if (plans[j].disjoint) disjoint.push_back(j);
+    }
     // the small tables go up from one pinned staging block per tag (asynchronous copies that
     // never wait for the stream; a later solve with another tag cannot overwrite them)
-    const size_t st_bytes[6] = {sizeof(int) * n_map, sizeof(int) * n_mptr, sizeof(int) * n_midx,
-                                sizeof(double) * n_red, sizeof(double) * n_red, sizeof(SolveDesc) * nj};
-    size_t st_off[6], st_end = 0;
-    for (int t = 0; t < 6; ++t) {
+    const size_t st_bytes[7] = {sizeof(int) * n_map, sizeof(int) * n_mptr, sizeof(int) * n_midx,
+                                sizeof(double) * n_red, sizeof(double) * n_red, sizeof(SolveDesc) * nj,
+                                sizeof(int) * std::max<size_t>(disjoint.size(), 1)};
+    size_t st_off[7], st_end = 0;
+    for (int t = 0; t < 7; ++t) {
         st_off[t] = st_end;
         st_end += (st_bytes[t] + 15) / 16 * 16;
     }
@@ -1100,15 +1111,23 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
     RP_CUDA(cudaMemcpyAsync(d_midx, stage + st_off[2], st_bytes[2], cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_rs, stage + st_off[3], st_bytes[3], cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_rt, stage + st_off[4], st_bytes[4], cudaMemcpyHostToDevice, stream));
+    std::memcpy(stage + st_off[5], descs.data(), st_bytes[5]);
+    RP_CUDA(cudaMemcpyAsync(d_desc, stage + st_off[5], st_bytes[5], cudaMemcpyHostToDevice, stream));
+    if (!disjoint.empty()) {  // every system with disjoint groups: one launch
+        int *d_sys = ctx->buf_t<int>("s_sys" + tag, disjoint.size());
+        std::memcpy(stage + st_off[6], disjoint.data(), st_bytes[6]);
+        RP_CUDA(cudaMemcpyAsync(d_sys, stage + st_off[6], st_bytes[6], cudaMemcpyHostToDevice, stream));
+        long long most = 1;
+        for (int j : disjoint) most = std::max<long long>(most, (long long)(plans[j].n + 1) * (plans[j].n + 1));
+        const dim3 grid((unsigned)std::min<long long>(ceil_div(most, 256), 1024), (unsigned)disjoint.size());
+        build_bordered_kernel<<<grid, 256, 0, stream>>>(d_desc, d_sys);
+        RP_LAUNCH_CHECK();
+    }
     for (int j = 0; j < nj; ++j) {
         const SolveJob &J = jobs[j];
         const FoldPlan &p = plans[j];
         const int n1 = p.n + 1;
-        if (p.disjoint) {
-            long long tot = (long long)n1 * n1;
-            build_bordered_kernel<<<std::min<long long>(ceil_div(tot, 256), 4096), 256, 0, stream>>>(descs[j]);
-            RP_LAUNCH_CHECK();
-        } else {
+        if (!p.disjoint) {
             // overlapping groups: the reference's sequential folding on the host
             std::vector<double> hA((size_t)J.N * J.N), hb((size_t)J.N), Ar, br, w;
             RP_CUDA(cudaMemcpyAsync(hA.data(), J.A, sizeof(double) * hA.size(), cudaMemcpyDeviceToHost, stream));
@@ -1136,15 +1155,11 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
     bool any_wide = false;
     if (pend) *pend = SolvePending{};
     for (int j = 0; j < nj; ++j) {
-        const int n1 = plans[j].n + 1;
-        if (n1 < kLUWideMin || n1 > kLUWideMax) continue;
-        descs[j].pre = d_pre + 3 * (size_t)j;
+        if (!descs[j].pre) continue;
         StageTimer tt(ctx, "solve_lu_wide", stream);
-        lu_wide_factor<float>(ctx, descs[j], n1, stream);
+        lu_wide_factor<float>(ctx, descs[j], plans[j].n + 1, stream);
         any_wide = true;
     }
-    std::memcpy(stage + st_off[5], descs.data(), st_bytes[5]);
-    RP_CUDA(cudaMemcpyAsync(d_desc, stage + st_off[5], st_bytes[5], cudaMemcpyHostToDevice, stream));
     {
         StageTimer tt(ctx, "solve_lu", stream);
         int n1max = 1;
@@ -1318,6 +1333,7 @@ extern "C" int rp_solve_noalloc(const double *A_dev, const double *b_dev, int N,
         int *perm = cv.take<int>((size_t)n1);
         double *d_info = cv.take<double>(kSolveInfo);
         SolveDesc *d_desc = cv.take<SolveDesc>(1);
+        int *d_sys = cv.take<int>(1);
         std::vector<double> rs((size_t)p.n, 0.0), rt((size_t)p.n, 0.0);
         if (resp_s)
             for (int k = 0; k < p.n; ++k) {
@@ -1337,8 +1353,11 @@ extern "C" int rp_solve_noalloc(const double *A_dev, const double *b_dev, int N,
         d.A = A_dev; d.b = b_dev; d.N = N; d.n = p.n; d.mem_ptr = d_mptr; d.mem_idx = d_midx;
         d.resp_s = resp_s ? d_rs : nullptr; d.resp_t = resp_s ? d_rt : nullptr; d.map = d_map; d.qtot = qtot;
         d.As = As; d.A0 = A0; d.bs = bs; d.x = x; d.r = r; d.perm = perm; d.q = q_dev; d.info = d_info;
+        RP_CUDA(cudaMemcpyAsync(d_desc, &d, sizeof(SolveDesc), cudaMemcpyHostToDevice, stream));
         if (p.disjoint) {
-            build_bordered_kernel<<<std::min<long long>(ceil_div((long long)n1 * n1, 256), 4096), 256, 0, stream>>>(d);
+            RP_CUDA(cudaMemsetAsync(d_sys, 0, sizeof(int), stream));  // the one system
+            const dim3 grid((unsigned)std::min<long long>(ceil_div((long long)n1 * n1, 256), 1024), 1u);
+            build_bordered_kernel<<<grid, 256, 0, stream>>>(d_desc, d_sys);
             RP_LAUNCH_CHECK();
         } else {
             std::vector<double> hA((size_t)N * N), hb((size_t)N), Ar, br, w;
@@ -1359,7 +1378,6 @@ extern "C" int rp_solve_noalloc(const double *A_dev, const double *b_dev, int N,
             RP_CUDA(cudaMemcpyAsync(A0, hs.data(), sizeof(double) * hs.size(), cudaMemcpyHostToDevice, stream));
             RP_CUDA(cudaMemcpyAsync(bs, hbs.data(), sizeof(double) * hbs.size(), cudaMemcpyHostToDevice, stream));
         }
-        RP_CUDA(cudaMemcpyAsync(d_desc, &d, sizeof(SolveDesc), cudaMemcpyHostToDevice, stream));
         lu_smem_optin();
         lu_solve_refine_kernel<<<1, kLU, solve_smem_bytes(n1), stream>>>(d_desc);
         RP_LAUNCH_CHECK();
