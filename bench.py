@@ -486,6 +486,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=120000,
                     help="kept points of the CPU baseline sample (capped at the cube's kept count; ~5-10 s of CPU)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default tile shapes")
     ap.add_argument("--ref-cubes", type=int, default=8, help="cubes the reference arm cycles over")
     ap.add_argument("--ref-sample", type=int, default=40000,
                     help="kept points per reference-arm step (~2-4 s of host work on 16 cores)")
@@ -520,6 +521,16 @@ def main():
         cs = cubes if sel is None else [cubes[i] for i in sel]
         vs = V_dev if sel is None else [V_dev[i] for i in sel]
         return ctx.fit_batch(cs, prec, V_dev=vs)
+
+    # tile shapes: the autotuner times each (atoms, kept points, KMAX) bucket of the batch once
+    tune = None
+    if not args.no_autotune:
+        import tempfile
+        t_tune = time.time()
+        table = ctx.autotune(cubes, os.path.join(tempfile.gettempdir(), f"repeat_gb300_tiles_{rank}.txt"))
+        tune = {"buckets": len(table), "seconds": round(time.time() - t_tune, 2),
+                "table": {str(k): {"phi_atoms": v[0], "gram_points_per_cta": 64 * v[1], "best_ms": round(v[2], 4),
+                                   "default_ms": round(v[3], 4), "N": v[4], "M": v[5]} for k, v in table.items()}}
 
     # warm-up
     for _ in range(max(args.warmup, 1)):
@@ -725,6 +736,7 @@ def main():
         "cpu_baseline": cpu,
         "clocks": clocks,
         "served": served,
+        "autotune": tune,
     }
     print(json.dumps(line), flush=True)
 

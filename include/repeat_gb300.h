@@ -241,6 +241,17 @@ int rp_batch_wait(rp_ctx *ctx, long long ticket, int *status);
  * it is asked for. */
 int rp_set_kappa_limit(rp_ctx *ctx, double kappa_max);
 
+/* Autotuner of the mixed-precision path's tile shapes (no reference counterpart): for every
+ * bucket of (atoms, kept points, KMAX) that the given cubes fall in and the ctx has no entry
+ * for, the first such cube's normal equations are timed (CUDA events) with each tile shape
+ * (Phi atoms per CTA 8/16/32 x Gram points per CTA 256/512/1024) and the fastest is kept
+ * for the bucket; rp_fit / rp_fit_batch use the ctx's table.  Tile shapes change no result
+ * (every Phi value and exact digit sum is the same whatever the tiling).  cache_path (may
+ * be NULL): the whole table is written there as text lines "key phi_atoms gram_split
+ * [best_ms default_ms N M]"; rp_load_tiles reads such a file into a ctx. */
+int rp_autotune(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, const char *cache_path);
+int rp_load_tiles(rp_ctx *ctx, const char *cache_path);
+
 /* Profiling hooks (no reference counterpart).  With timing on, every stage
  * records CUDA events on the stream it runs on; rp_stage_times synchronises,
  * returns per stage name the summed milliseconds and launch count

@@ -29,7 +29,8 @@ FIT_TWO_PASS = 2       # flag: a mixed-precision cube refitted in two passes aft
 EXPORTS = ["rp_version", "rp_ctx_create", "rp_ctx_destroy", "rp_last_error", "rp_filter", "rp_ewald_setup",
            "rp_ewald_destroy", "rp_ewald_info", "rp_gram", "rp_solve", "rp_potential", "rp_fit",
            "rp_fit_batch", "rp_set_timing", "rp_stage_times", "rp_launch_count", "rp_solve_noalloc",
-           "rp_batch_submit", "rp_batch_poll", "rp_batch_wait", "rp_qeq", "rp_set_kappa_limit"]
+           "rp_batch_submit", "rp_batch_poll", "rp_batch_wait", "rp_qeq", "rp_set_kappa_limit", "rp_autotune",
+           "rp_load_tiles"]
 
 
 class RepeatError(RuntimeError):
@@ -114,6 +115,10 @@ def load(path: str | None = None):
     L.rp_qeq.argtypes = [P, P, P, I, P, P, D, P, P, P, P]
     L.rp_set_kappa_limit.restype = I
     L.rp_set_kappa_limit.argtypes = [P, D]
+    L.rp_autotune.restype = I
+    L.rp_autotune.argtypes = [P, I, P, P, ctypes.c_char_p]
+    L.rp_load_tiles.restype = I
+    L.rp_load_tiles.argtypes = [P, ctypes.c_char_p]
     _lib = L
     return L
 
@@ -128,6 +133,13 @@ def check(ctx_ptr, rc: int, what: str = ""):
     if rc == -4:
         raise SingularError(rc, msg)
     raise RepeatError(rc, msg)
+
+
+def tile_key(N: int, M: int, kmax: int) -> int:
+    """The autotuner's bucket of a fit (the C library's rp::tile_key)."""
+    nb = 0 if N < 32 else 1 if N < 64 else 2 if N < 128 else 3 if N < 256 else 4 if N < 512 else 5
+    mb = 0 if M < 32768 else 1 if M < 131072 else 2 if M < 524288 else 3
+    return (nb * 4 + mb) * 64 + min(max(int(kmax), 0), 63)
 
 
 def fit_info(row) -> dict:

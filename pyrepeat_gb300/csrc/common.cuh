@@ -183,6 +183,19 @@ class HostPool {
 constexpr double kDefaultKappaLimit = 2e5;
 
 namespace rp {
+// Tile shapes of the mixed-precision normal equations: atoms per CTA of the Phi kernel (8, 16
+// or 32) and Gram stages of 64 points per CTA (up to 16).  Neither changes a result: every
+// Phi value and every exact digit sum is the same whatever the tiling.
+struct TileConfig {
+    int phi_atoms = 16;
+    int gram_split = 16;
+};
+// The autotuner's bucket of a fit: atoms, kept points, KMAX.
+inline long long tile_key(int N, long long M, int kmax) {
+    const int nb = N < 32 ? 0 : N < 64 ? 1 : N < 128 ? 2 : N < 256 ? 3 : N < 512 ? 4 : 5;
+    const int mb = M < 32768 ? 0 : M < 131072 ? 1 : M < 524288 ? 2 : 3;
+    return ((long long)nb * 4 + mb) * 64 + std::min(std::max(kmax, 0), 63);
+}
 // Batches of the asynchronous server in flight at once.  Each runs in a slot of the ctx with
 // its own scratch (names carry the slot), pinned staging, streams, status words, cuBLAS
 // handle and host object pools; slot 0 is also what rp_fit_batch and the staged calls use.
@@ -279,6 +292,12 @@ struct rp_ctx {
     // bordered system's unknowns) exceeds this are refitted in plain FP64
     // (rp_set_kappa_limit; 0 = never)
     double kappa_limit = kDefaultKappaLimit;
+    // tile shapes per autotuner bucket (rp_autotune / rp_load_tiles); absent: the defaults
+    std::map<long long, rp::TileConfig> tiles;
+    rp::TileConfig tiles_for(int N, long long M, int kmax) const {
+        auto it = tiles.find(rp::tile_key(N, M, kmax));
+        return it == tiles.end() ? rp::TileConfig{} : it->second;
+    }
     void *host_buf(const std::string &name_in, size_t bytes) {
         const std::string name = slot_key(name_in);
         bytes = std::max<size_t>(256, (bytes + 255) & ~size_t(255));
@@ -460,12 +479,12 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
 // digits in one pass; clamped values are counted in *clamp_dev (the caller then redoes
 // the fit without rn).  Without them: two passes (Phi, then its centre and scale).
 // d_atoms_pre / E_pre (optional): the atoms already on the device and the reciprocal rows
-// already computed (recip_rows_group over a batch's pipeline group).
+// already computed (recip_rows_group over a batch's pipeline group); tiles: the tile shapes.
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
                 cudaStream_t stream, const double *vstats_dev = nullptr, const std::string &slot = "",
                 const double *rn = nullptr, int *clamp_dev = nullptr, const double *d_atoms_pre = nullptr,
-                const float2 *E_pre = nullptr);
+                const float2 *E_pre = nullptr, TileConfig tiles = TileConfig{});
 double radius_of(int z);  // vdW radius (Bohr) of element z, the filter's table
 void solve_run(rp_ctx *ctx, const double *A_dev, const double *b_dev, int N, int n_groups, const int *group_ptr,
                const int *group_idx, const double *resp_s, const double *resp_t, double qtot, double *q_dev,

@@ -51,17 +51,19 @@ constexpr int kTileBytes = kBM * kBK * 2;  // 16 KB per operand tile
 // x = 2^-6 (x0 + 2^-7 x1 + 2^-14 x2 + 2^-21 x3), x_s integers with |x0| <= 32,
 // |x1..x3| <= 64 (|x| <= 1/2; 28 bits below the row maximum, because a centred
 // column's typical value sits orders of magnitude below its maximum).  All 16
-// slice products are kept (the low digits carry full-size rounding noise
-// whatever |x| is), grouped by weight g = s+u into seven TMEM accumulators of a
-// 128 x 64 tile.  Per point, a group's products sum to at most 12288 in magnitude
-// (weight 3: x0 x3 + x3 x0 <= 2 * 32 * 64, x1 x2 + x2 x1 <= 2 * 64 * 64; weight 4:
-// three products <= 64 * 64; the others less), so a stage of 64 points adds at most
-// 786,432 = 3 * 2^18 to a group and kGramFlush = 16 stages stay below 2^24 (12.6 M):
-// the FP32 sums are exact, and a CTA of kGramSplit = 16 stages drains them once, at its
-// end.  (A row whose |x| passed 1/2 is clamped, counted and its cube refitted from the
-// staged Phi, whose own scale keeps |x| < 1/2.)  At each flush the epilogue folds the groups into
-// one int64 per element (sum_g D_g 2^(7(6-g))), so the Gram carries no rounding
-// bias (its diagonal is the most sensitive quantity of the fit).
+// slice products are kept: for the many values far below their row's maximum the
+// low digits carry the signal, not rounding noise (leaving out the three products of
+// weight 5 and 6 moved the batch's charges from 4e-7 to 4e-6 e of FP64).  They are
+// grouped by weight g = s+u into seven TMEM accumulators of a 128 x 64 tile.  Per
+// point, a group's products sum to at most 12288 in magnitude (weight 3: x0 x3 +
+// x3 x0 <= 2 * 32 * 64, x1 x2 + x2 x1 <= 2 * 64 * 64; weight 4: three products
+// <= 64 * 64; the others less), so a stage of 64 points adds at most 786,432 =
+// 3 * 2^18 to a group and kGramFlush = 16 stages stay below 2^24 (12.6 M): the FP32
+// sums are exact, and a CTA of kGramSplit = 16 stages drains them once, at its end.
+// (A row whose |x| passed 1/2 is clamped, counted and its cube refitted from the
+// staged Phi, whose own scale keeps |x| < 1/2.)  At each flush the epilogue folds the
+// groups into one int64 per element (sum_g D_g 2^(7(6-g))), so the Gram carries no
+// rounding bias (its diagonal is the most sensitive quantity of the fit).
 constexpr int kGN = 64;          // Gram tile columns
 constexpr int kGSlices = 4;
 constexpr int kGroups = 2 * kGSlices - 1;
@@ -271,17 +273,52 @@ __device__ __forceinline__ long long warp_sum_fixed(int I) {
     return (long long)shi * 16384 + slo;
 }
 
-__device__ __forceinline__ void digits4(int v, __half *o0, __half *o1, __half *o2, __half *o3, long long idx) {
-    const int s0 = (v + (1 << 20)) >> 21;
+__device__ __forceinline__ void split4(int v, int &s0, int &s1, int &s2, int &s3) {
+    s0 = (v + (1 << 20)) >> 21;
     int r = v - (s0 << 21);  // [-2^20, 2^20)
-    const int s1 = (r + (1 << 13)) >> 14;
+    s1 = (r + (1 << 13)) >> 14;
     r -= s1 << 14;           // [-2^13, 2^13)
-    const int s2 = (r + (1 << 6)) >> 7;
-    const int s3 = r - (s2 << 7);  // [-64, 64)
+    s2 = (r + (1 << 6)) >> 7;
+    s3 = r - (s2 << 7);      // [-64, 64)
+}
+
+__device__ __forceinline__ void digits4(int v, __half *o0, __half *o1, __half *o2, __half *o3, long long idx) {
+    int s0, s1, s2, s3;
+    split4(v, s0, s1, s2, s3);
     o0[idx] = __int2half_rn(s0);
     o1[idx] = __int2half_rn(s1);
     o2[idx] = __int2half_rn(s2);
     o3[idx] = __int2half_rn(s3);
+}
+
+// Two digits d_lo, d_hi in [-64, 64] as an FP16 pair without a conversion instruction: the
+// FP16 bits 0x6440 + d encode 1088 + d (exponent 2^10, unit spacing), so one packed
+// subtraction of 1088 leaves d exactly.
+__device__ __forceinline__ uint32_t digit_pair(int d_lo, int d_hi) {
+    const uint32_t w = (uint32_t)(0x6440 + d_lo) | ((uint32_t)(0x6440 + d_hi) << 16);
+    const __half2 h = __hsub2(*reinterpret_cast<const __half2 *>(&w), __half2half2(__ushort_as_half(0x6440)));
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// The digits of two consecutive points m (even lane) and m + 1 (odd lane) of one row: the lanes
+// swap half their digits, then the even lane stores slices 0 and 1 and the odd lane slices 2
+// and 3, each as one 32-bit pair (m, m + 1).  Both lanes of a pair must call it together; idx
+// is the even point's element index (even, so the pair is 4-byte aligned).
+__device__ __forceinline__ void digits4_pair(int v, bool odd, __half *o0, __half *o1, __half *o2, __half *o3,
+                                             long long idx_even) {
+    int s0, s1, s2, s3;
+    split4(v, s0, s1, s2, s3);
+    const uint32_t give = odd ? ((uint32_t)(s0 & 0xffff) | ((uint32_t)s1 << 16))
+                              : ((uint32_t)(s2 & 0xffff) | ((uint32_t)s3 << 16));
+    const uint32_t got = __shfl_xor_sync(0xffffffffu, give, 1);
+    const int g_lo = (int)(short)(got & 0xffff), g_hi = (int)(short)(got >> 16);
+    if (!odd) {  // own (m) and partner's (m + 1) slices 0 and 1
+        *reinterpret_cast<uint32_t *>(o0 + idx_even) = digit_pair(s0, g_lo);
+        *reinterpret_cast<uint32_t *>(o1 + idx_even) = digit_pair(s1, g_hi);
+    } else {     // partner's (m) and own (m + 1) slices 2 and 3
+        *reinterpret_cast<uint32_t *>(o2 + idx_even) = digit_pair(g_lo, s2);
+        *reinterpret_cast<uint32_t *>(o3 + idx_even) = digit_pair(g_hi, s3);
+    }
 }
 
 // round((h + l) * sc) for a double-float (h, l) and a power of two sc, |(h + l) sc| <= 2^27:
@@ -364,7 +401,7 @@ __device__ __forceinline__ float erfc_nr2(float xs) {
 }
 
 constexpr int kPhiPts = 128;     // points per CTA (one per thread)
-constexpr int kPhiAtoms = 16;    // atoms per CTA
+constexpr int kPhiAtoms = 16;    // atoms per CTA by default (8 and 32 are the other tile shapes)
 constexpr int kMaxShifts = 128;  // pruned real-space shifts (checked on the host)
 
 // The reference's FP64 cutoff decision for one (point, image) pair (repeat.py:944-966:
@@ -456,7 +493,7 @@ struct PhiDigits {
 // reference's default 7): an atom's NC E values are loaded at the top of its iteration
 // and used after the real-space loop, which hides their L2 latency; stage C is unrolled.
 // NC = 0: any KMAX, loads in the loop.  The register cap keeps 7 CTAs per SM.
-template <int NC, bool DIG>
+template <int NC, bool DIG, int AT>
 __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
     const int32_t *__restrict__ kept, long long m0, long long rows, const double *__restrict__ axis, AxisDF adf,
     int nx, int ny,
@@ -466,17 +503,17 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
     const float2 *__restrict__ E, int n1c, int parts, float2 *__restrict__ phit, long long ld,
     double *__restrict__ psum, float *__restrict__ pmax, PhiDigits dg) {
     extern __shared__ float4 dsm[];
-    float4 *img_hi = dsm;                                 // [kPhiAtoms][scap] (x, y, z, shift index)
-    float4 *img_lo = img_hi + (size_t)kPhiAtoms * scap;   // [kPhiAtoms][scap]
-    float2 *exs = reinterpret_cast<float2 *>(img_lo + (size_t)kPhiAtoms * scap);  // [n1c][kPhiPts] ex[n1][i]
-    __shared__ int ncand[kPhiAtoms];
+    float4 *img_hi = dsm;                                 // [AT][scap] (x, y, z, shift index)
+    float4 *img_lo = img_hi + (size_t)AT * scap;   // [AT][scap]
+    float2 *exs = reinterpret_cast<float2 *>(img_lo + (size_t)AT * scap);  // [n1c][kPhiPts] ex[n1][i]
+    __shared__ int ncand[AT];
     __shared__ float bb[2][3][kPhiPts / 32];
-    __shared__ float wsum[kPhiPts / 32][kPhiAtoms];
-    __shared__ float wmax[kPhiPts / 32][kPhiAtoms];
-    __shared__ long long wrow[kPhiPts / 32][kPhiAtoms + 1];  // digit-row partial sums (DIG)
+    __shared__ float wsum[kPhiPts / 32][AT];
+    __shared__ float wmax[kPhiPts / 32][AT];
+    __shared__ long long wrow[kPhiPts / 32][AT + 1];  // digit-row partial sums (DIG)
     const long long mb = (long long)blockIdx.x * kPhiPts;
-    const int a0 = blockIdx.y * kPhiAtoms;
-    const int na = min(kPhiAtoms, N - a0);
+    const int a0 = blockIdx.y * AT;
+    const int na = min(AT, N - a0);
     const int layer = nx * ny;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long m = mb + threadIdx.x;
@@ -551,7 +588,7 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
             }
         }
         const float reach = rcf + 1e-3f, reach2 = reach * reach;
-        for (int a = warp; a < kPhiAtoms; a += kPhiPts / 32) {
+        for (int a = warp; a < AT; a += kPhiPts / 32) {
             int base = 0;
             if (a < na) {
                 const float4 *src = img + 2 * (size_t)(a0 + a) * S;
@@ -680,7 +717,10 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
             if (valid) I = x_fixed(out.x, out.y, dg.scale[a0 + a], dg.clamped);
             const long long rs = warp_sum_fixed(I);
             if (lane == 0) wrow[warp][a] = rs;
-            if (m < dg.rows_kpad) digits4(I, dg.X0, dg.X1, dg.X2, dg.X3, (long long)(a0 + a) * dg.ldx + m);
+            // rows_kpad is even and every pair of lanes holds points (m, m + 1), m even: a pair is
+            // wholly inside or wholly past the padded row, so both lanes take the branch together
+            if (m < dg.rows_kpad)
+                digits4_pair(I, lane & 1, dg.X0, dg.X1, dg.X2, dg.X3, (long long)(a0 + a) * dg.ldx + (m & ~1LL));
         } else if (valid) {
             *prow = out;
         }
@@ -707,16 +747,17 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
                 I = x_fixed(h, (float)(v - (double)h), vscale_of(*dg.vmax_p), dg.clamped);
             }
             const long long rs = warp_sum_fixed(I);
-            if (lane == 0) wrow[warp][kPhiAtoms] = rs;
-            if (m < dg.rows_kpad) digits4(I, dg.X0, dg.X1, dg.X2, dg.X3, (long long)dg.N * dg.ldx + m);
+            if (lane == 0) wrow[warp][AT] = rs;
+            if (m < dg.rows_kpad)
+                digits4_pair(I, lane & 1, dg.X0, dg.X1, dg.X2, dg.X3, (long long)dg.N * dg.ldx + (m & ~1LL));
         }
         __syncthreads();
         // exact row sums (two's complement int64 atomics: order-independent), one per CTA and row
-        if (threadIdx.x < na || (blockIdx.y == 0 && threadIdx.x == kPhiAtoms)) {
+        if (threadIdx.x < na || (blockIdx.y == 0 && threadIdx.x == AT)) {
             const int a = threadIdx.x;
             long long t = 0;
             for (int w = 0; w < kPhiPts / 32; ++w) t += wrow[w][a];
-            if (t != 0) atomicAdd(dg.rowsum + (a == kPhiAtoms ? dg.N : a0 + a), (unsigned long long)t);
+            if (t != 0) atomicAdd(dg.rowsum + (a == AT ? dg.N : a0 + a), (unsigned long long)t);
         }
     } else if (psum) {
         __syncthreads();
@@ -734,37 +775,46 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
     }
 }
 
-size_t phi_smem_bytes(int n1c, int scap) {
-    return sizeof(float4) * 2 * (size_t)kPhiAtoms * scap + sizeof(float2) * (size_t)n1c * kPhiPts;
+size_t phi_smem_bytes(int n1c, int scap, int at) {
+    return sizeof(float4) * 2 * (size_t)at * scap + sizeof(float2) * (size_t)n1c * kPhiPts;
+}
+
+// The instantiation for (KMAX 7 or any, digits or staged Phi, atoms per CTA)
+using PhiKernel = decltype(&phi_chunk_kernel<7, false, 16>);
+template <int AT>
+PhiKernel phi_kernel_for(bool regs, bool dig) {
+    return dig ? (regs ? phi_chunk_kernel<7, true, AT> : phi_chunk_kernel<0, true, AT>)
+               : (regs ? phi_chunk_kernel<7, false, AT> : phi_chunk_kernel<0, false, AT>);
+}
+PhiKernel phi_kernel(bool regs, bool dig, int at) {
+    switch (at) {
+        case 8: return phi_kernel_for<8>(regs, dig);
+        case 32: return phi_kernel_for<32>(regs, dig);
+        default: return phi_kernel_for<16>(regs, dig);
+    }
 }
 
 void launch_phi(const int32_t *kept, long long m0, long long rows, const double *d_axis, const double *h_axis, int nx, int ny,
                 const double *d_atoms, int N, const double *d_shifts, int S, int zero_idx, double rc, double sa,
                 const float4 *img, const float4 *EX, const float2 *E, int n1c, int parts, float2 *phit, long long ld,
-                double *psum, float *pmax, const PhiDigits *dig, cudaStream_t s) {
+                double *psum, float *pmax, const PhiDigits *dig, cudaStream_t s, int at) {
+    if (at != 8 && at != 32) at = 16;
     RP_REQUIRE(S >= 1 && S <= kMaxShifts, "more than 128 real-space shifts after pruning (cutoff too large for the cell)");
     const int scap = (S + 31) / 32 * 32;
     const bool regs = (n1c == 7);  // KMAX 7: the specialised kernel
-    const size_t smem = phi_smem_bytes(n1c, scap);
+    const size_t smem = phi_smem_bytes(n1c, scap, at);
     // the static shared memory (the statistics and row-sum tiles, ~1.3 KB) counts against
     // the same 48 KB default, so the opt-in is raised whenever the dynamic part could cross it
     RP_REQUIRE(smem <= 192 * 1024, "phi kernel: KMAX too large for shared memory");
-    {
-        const size_t want = std::max<size_t>(smem, 96 * 1024);
-        smem_optin((const void *)phi_chunk_kernel<7, false>, want);
-        smem_optin((const void *)phi_chunk_kernel<0, false>, want);
-        smem_optin((const void *)phi_chunk_kernel<7, true>, want);
-        smem_optin((const void *)phi_chunk_kernel<0, true>, want);
-    }
+    auto kern = phi_kernel(regs, dig != nullptr, at);
+    smem_optin((const void *)kern, std::max<size_t>(smem, 96 * 1024));
     AxisDF adf;
     for (int q = 0; q < 9; ++q) {
         adf.h[q] = (float)h_axis[q];
         adf.l[q] = (float)(h_axis[q] - (double)adf.h[q]);
     }
-    dim3 grd(ceil_div(rows, kPhiPts), ceil_div(N, kPhiAtoms));
+    dim3 grd(ceil_div(rows, kPhiPts), ceil_div(N, at));
     const PhiDigits dg = dig ? *dig : PhiDigits{};
-    auto kern = dig ? (regs ? phi_chunk_kernel<7, true> : phi_chunk_kernel<0, true>)
-                    : (regs ? phi_chunk_kernel<7, false> : phi_chunk_kernel<0, false>);
     kern<<<grd, kPhiPts, smem, s>>>(kept, m0, rows, d_axis, adf, nx, ny, d_atoms, N, d_shifts, S, scap, zero_idx, rc,
                                     sa, (float)rc, (float)(sa * kSqrtLog2e), real_near2(), img, EX, E, n1c, parts,
                                     phit, ld, psum, pmax, dg);
@@ -1063,7 +1113,7 @@ static bool phi_bounds(const rp_ewald *ew, int S, const double *rn, int N, doubl
 void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                 const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
                 cudaStream_t stream, const double *vstats_dev, const std::string &slot, const double *rn,
-                int *clamp_dev, const double *d_atoms_pre, const float2 *E_pre) {
+                int *clamp_dev, const double *d_atoms_pre, const float2 *E_pre, TileConfig tiles) {
     RP_REQUIRE(N > 0 && M > 0, "rp_gram: need N > 0 and M > 0");
     std::vector<double> sh;
     int zero_idx = -1;
@@ -1145,7 +1195,9 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     const int nt = (int)ceil_div(Np, kBM), ntj = (int)ceil_div(Np, kGN);
     int ntri = 0;  // 128 x 64 Gram tiles with columns at or right of the row block, up to the last row
     for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
-    const int kb_split = kGramSplit;  // 1024 points per CTA (int64 headroom), exact sums drained once
+    // points per CTA: kGramSplit stages (1024 points, the int64 headroom, exact sums drained
+    // once) or fewer, for more CTAs on cubes with few Gram tiles (the autotuner's choice)
+    const int kb_split = std::min(std::max(tiles.gram_split, 1), kGramSplit);
 
     for (long long m0 = 0; m0 < M; m0 += chunk) {
         const long long rows = std::min<long long>(chunk, M - m0);
@@ -1159,11 +1211,12 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
                                rowsum, clamp_dev, N};
             launch_phi(kept_idx_dev, m0, rows, d_axis, ew->grid.axis, nx, ny, d_atoms, N, d_shifts, S, zero_idx,
                        ew->cutoff, ew->sqrt_alpha, img, ew->d_exf, E, n1c, 3, nullptr, chunk_pad, nullptr, nullptr,
-                       &dg, stream);
+                       &dg, stream, tiles.phi_atoms);
         } else {
             StageTimer tt(ctx, "phi", stream);
             launch_phi(kept_idx_dev, m0, rows, d_axis, ew->grid.axis, nx, ny, d_atoms, N, d_shifts, S, zero_idx, ew->cutoff,
-                       ew->sqrt_alpha, img, ew->d_exf, E, n1c, 3, phit, chunk_pad, psum, pmax, nullptr, stream);
+                       ew->sqrt_alpha, img, ew->d_exf, E, n1c, 3, phit, chunk_pad, psum, pmax, nullptr, stream,
+                       tiles.phi_atoms);
         }
         // 2. centre on the first chunk, a scale per chunk, fixed-point digits of X
         if (!single) {
@@ -1261,7 +1314,7 @@ extern "C" int rp_debug_mixed_phi(rp_ctx *ctx, const rp_ewald *ew, const double 
         float2 *ph = ctx->buf_t<float2>("dbg_phi", (size_t)N * rows);
         launch_phi(kept_idx_dev, 0, rows, d_axis, ew->grid.axis, ew->grid.n_grid[0], ew->grid.n_grid[1], d_atoms, N, d_shifts, S,
                    zero_idx, ew->cutoff, ew->sqrt_alpha, img, ew->d_exf, E, ew->kmax, parts, ph, rows, nullptr,
-                   nullptr, nullptr, 0);
+                   nullptr, nullptr, 0, kPhiAtoms);
         df_to_double_kernel<<<ceil_div((long long)N * rows, 256), 256>>>(ph, (long long)N * rows, phi_dev);
         RP_LAUNCH_CHECK();
         RP_CUDA(cudaDeviceSynchronize());
@@ -1272,9 +1325,9 @@ extern "C" int rp_debug_mixed_phi(rp_ctx *ctx, const rp_ewald *ew, const double 
     }
 }
 
-// Diagnostics: the exact-Gram kernel on caller-provided FP16 slices X0, X1, X2
-// ([Np_pad][cols], cols a multiple of 64) -> 2^-40 * sum over points and all nine
-// slice products of x_s y_u 2^(7(4-s-u)) (FP64, Np x Np).
+// Diagnostics: the exact-Gram kernel on caller-provided FP16 slices X0 .. X3
+// ([Np_pad][cols], cols a multiple of 64) -> 2^-54 * sum over points and all sixteen
+// slice products of x_s y_u 2^(7(6-s-u)) (FP64, Np x Np).
 extern "C" int rp_debug_gram_slices(rp_ctx *ctx, const void *X0, const void *X1, const void *X2, const void *X3,
                                     int Np, long long cols, int flush, int kb_split, double *I_dev) {
     using namespace rp;

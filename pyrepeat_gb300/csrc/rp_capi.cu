@@ -401,21 +401,23 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
                   reinterpret_cast<double *>(ew_host + at_off) + 3 * off_n[i]);
     });
     for (int i = 0; i < n; ++i) rp::ewald_place(r.ews[i], ew_dev + ew_off[i]);
+    // the tables go up on the reciprocal rows' stream, beside the grids still queued on the
+    // copy stream (with grids from host memory those are most of the batch's bytes)
+    const cudaStream_t recip_lane = ctx->timing ? ctx->lane(0) : ctx->lane(kLaneRecip);
+    RP_CUDA(cudaStreamWaitEvent(recip_lane, r.events.front(), 0));  // after the caller's work so far
     RP_CUDA(cudaMemcpyAsync(ew_dev, ew_host, at_off + sizeof(double) * 3 * off_n[n], cudaMemcpyHostToDevice,
-                            copy_lane));
-    const cudaEvent_t tables = record(copy_lane);
+                            recip_lane));
+    const cudaEvent_t tables = record(recip_lane);
     for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(glane(ln), tables, 0));
     RP_CUDA(cudaStreamWaitEvent(stream, tables, 0));
-    // reciprocal rows of every mixed-precision cube, a pipeline group per launch set, on a
-    // stream of their own: they need only the tables and atoms, so they run beside the
-    // filters, and each group's normal equations wait for its rows
+    // reciprocal rows of every mixed-precision cube, a pipeline group per launch set, on that
+    // stream: they need only the tables and atoms, so they run beside the filters, and each
+    // group's normal equations wait for its rows
     std::vector<size_t> e_off((size_t)n + 1, 0);
     for (int i = 0; i < n; ++i)
         e_off[i + 1] = e_off[i] + (descs[i].precision == RP_PREC_MIXED
                                        ? recip_rows_bytes(r.ews[i], descs[i].N) / sizeof(float2) : 0);
     float2 *E_all = ctx->buf_t<float2>("fit_E", std::max<size_t>(e_off[n], 1));
-    const cudaStream_t recip_lane = ctx->timing ? ctx->lane(0) : ctx->lane(kLaneRecip);
-    RP_CUDA(cudaStreamWaitEvent(recip_lane, tables, 0));
     std::vector<cudaEvent_t> rows_ready((size_t)ngroups);
     for (int g = 0; g < ngroups; ++g) {
         std::vector<rp::RecipRowsJob> rj;
@@ -462,7 +464,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
                 rp::gram_mixed(ctx, r.ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], r.M[i],
                                A + off_nn[i], b + off_n[i], nullptr, glane(ln), vst + 2 * i,
                                "#" + std::to_string(ln), rn.data() + off_n[i], clamps + i,
-                               atoms_dev + 3 * off_n[i], E_all + e_off[i]);
+                               atoms_dev + 3 * off_n[i], E_all + e_off[i], ctx->tiles_for(d.N, r.M[i], d.kmax));
             } else {
                 rp::gram_fp64(ctx, r.ews[i], d.atoms, d.N, kept + off_pts[i], Vc + off_pts[i], r.M[i],
                               A + off_nn[i], b + off_n[i], nullptr, stream);
@@ -766,6 +768,144 @@ int rp_launch_count(long long *out) {
     if (!out) return RP_E_ARG;
     *out = rp::g_launches.load();
     return RP_OK;
+}
+
+int rp_autotune(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, const char *cache_path) {
+    if (!ctx || n < 0 || (n > 0 && !descs)) return RP_E_ARG;
+    return guarded(ctx, [&] {
+        using namespace rp;
+        const cudaStream_t st = ctx->lane(0);
+        std::map<long long, int> first;  // bucket -> the first cube of the batch in it
+        std::vector<long long> Ms((size_t)n, 0);
+        long long *d_M = ctx->buf_t<long long>("tune_M", 1);
+        double *d_vst = ctx->buf_t<double>("tune_vst", 2);
+        int *d_clamp = ctx->buf_t<int>("tune_clamp", 1);
+        // the kept points of each cube (brick order, as the batch fits them), then one cube per bucket
+        std::vector<int> pick;
+        for (int i = 0; i < n; ++i) {
+            const rp_fit_desc &d = descs[i];
+            if (d.precision != RP_PREC_MIXED) continue;
+            RP_REQUIRE(d.atoms && d.Z && d.N > 0 && ((V_dev && V_dev[i]) || d.V), "rp_autotune: bad descriptor");
+            const long long np = (long long)d.grid.n_grid[0] * d.grid.n_grid[1] * d.grid.n_grid[2];
+            const double *V = V_dev && V_dev[i] ? V_dev[i] : nullptr;
+            if (!V) {
+                double *v = ctx->buf_t<double>("tune_V", (size_t)np);
+                RP_CUDA(cudaMemcpyAsync(v, d.V, sizeof(double) * np, cudaMemcpyHostToDevice, st));
+                V = v;
+            }
+            int32_t *kept = ctx->buf_t<int32_t>("tune_kept", (size_t)np);
+            double *Vc = ctx->buf_t<double>("tune_Vc", (size_t)np);
+            filter_async(ctx, &d.grid, d.atoms, d.Z, d.N, V, d.vdw_factor, d.vdw_max, kept, Vc, d_M, nullptr, st,
+                         "#tune", true, d_vst);
+            RP_CUDA(cudaMemcpyAsync(&Ms[i], d_M, sizeof(long long), cudaMemcpyDeviceToHost, st));
+            RP_CUDA(cudaStreamSynchronize(st));
+            const long long key = tile_key(d.N, Ms[i], d.kmax);
+            if (Ms[i] > 0 && !first.count(key) && !ctx->tiles.count(key)) {
+                first[key] = i;
+                pick.push_back(i);
+            }
+        }
+        std::string report;
+        for (int i : pick) {
+            const rp_fit_desc &d = descs[i];
+            const long long np = (long long)d.grid.n_grid[0] * d.grid.n_grid[1] * d.grid.n_grid[2];
+            const double *V = V_dev && V_dev[i] ? V_dev[i] : nullptr;
+            if (!V) {
+                double *v = ctx->buf_t<double>("tune_V", (size_t)np);
+                RP_CUDA(cudaMemcpyAsync(v, d.V, sizeof(double) * np, cudaMemcpyHostToDevice, st));
+                V = v;
+            }
+            int32_t *kept = ctx->buf_t<int32_t>("tune_kept", (size_t)np);
+            double *Vc = ctx->buf_t<double>("tune_Vc", (size_t)np);
+            filter_async(ctx, &d.grid, d.atoms, d.Z, d.N, V, d.vdw_factor, d.vdw_max, kept, Vc, d_M, nullptr, st,
+                         "#tune", true, d_vst);
+            rp_ewald ew;
+            ew.device = ctx->device;
+            ewald_build(&ew, &d.grid, d.cutoff, d.kmax);
+            struct Free {
+                rp_ewald *e;
+                ~Free() { ewald_free(e); }
+            } fr{&ew};
+            double *d_atoms = ctx->buf_t<double>("tune_atoms", 3 * (size_t)d.N);
+            RP_CUDA(cudaMemcpyAsync(d_atoms, d.atoms, sizeof(double) * 3 * d.N, cudaMemcpyHostToDevice, st));
+            float2 *E = ctx->buf_t<float2>("tune_E", recip_rows_bytes(&ew, d.N) / sizeof(float2));
+            recip_rows(ctx, &ew, d_atoms, nullptr, d.N, E, st, "#tune");
+            std::vector<double> rn((size_t)d.N);
+            for (int a = 0; a < d.N; ++a) rn[a] = d.vdw_factor * radius_of(d.Z[a]);
+            double *A = ctx->buf_t<double>("tune_A", (size_t)d.N * d.N);
+            double *b = ctx->buf_t<double>("tune_b", (size_t)d.N);
+            cudaEvent_t e0, e1;
+            RP_CUDA(cudaEventCreate(&e0));
+            RP_CUDA(cudaEventCreate(&e1));
+            TileConfig best{};
+            float best_ms = 1e30f, default_ms = 0.f;
+            for (int at : {8, 16, 32})
+                for (int split : {4, 8, 16}) {
+                    const TileConfig tc{at, split};
+                    float ms = 1e30f;
+                    for (int rep = 0; rep < 3; ++rep) {  // the first is a warm-up
+                        RP_CUDA(cudaMemsetAsync(d_clamp, 0, sizeof(int), st));
+                        RP_CUDA(cudaEventRecord(e0, st));
+                        gram_mixed(ctx, &ew, d.atoms, d.N, kept, Vc, Ms[i], A, b, nullptr, st, d_vst, "#tune",
+                                   rn.data(), d_clamp, d_atoms, E, tc);
+                        RP_CUDA(cudaEventRecord(e1, st));
+                        RP_CUDA(cudaEventSynchronize(e1));
+                        float t = 0.f;
+                        RP_CUDA(cudaEventElapsedTime(&t, e0, e1));
+                        if (rep > 0) ms = std::min(ms, t);
+                    }
+                    if (at == 16 && split == 16) default_ms = ms;
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        best = tc;
+                    }
+                }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            const long long key = tile_key(d.N, Ms[i], d.kmax);
+            ctx->tiles[key] = best;
+            report += std::to_string(key) + " " + std::to_string(best.phi_atoms) + " " +
+                      std::to_string(best.gram_split) + " " + std::to_string(best_ms) + " " +
+                      std::to_string(default_ms) + " " + std::to_string(d.N) + " " + std::to_string(Ms[i]) + "\n";
+        }
+        status_check(ctx, st);
+        if (cache_path && *cache_path) {
+            FILE *f = std::fopen(cache_path, "w");
+            RP_REQUIRE(f, std::string("rp_autotune: cannot write ") + cache_path);
+            std::fputs("# key phi_atoms gram_split best_ms default_ms N M\n", f);
+            for (auto &kv : ctx->tiles) {
+                std::string line = std::to_string(kv.first) + " " + std::to_string(kv.second.phi_atoms) + " " +
+                                   std::to_string(kv.second.gram_split);
+                // keep this run's timings on the buckets it measured
+                const std::string tag = std::to_string(kv.first) + " ";
+                size_t pos = report.find(tag);
+                if (pos == 0 || (pos != std::string::npos && report[pos - 1] == '\n')) {
+                    const size_t end = report.find('\n', pos);
+                    line = report.substr(pos, end - pos);
+                }
+                std::fputs((line + "\n").c_str(), f);
+            }
+            std::fclose(f);
+        }
+    });
+}
+
+int rp_load_tiles(rp_ctx *ctx, const char *cache_path) {
+    if (!ctx || !cache_path) return RP_E_ARG;
+    return guarded(ctx, [&] {
+        FILE *f = std::fopen(cache_path, "r");
+        RP_REQUIRE(f, std::string("rp_load_tiles: cannot read ") + cache_path);
+        char line[512];
+        while (std::fgets(line, sizeof line, f)) {
+            if (line[0] == '#') continue;
+            long long key = 0;
+            int at = 0, split = 0;
+            if (std::sscanf(line, "%lld %d %d", &key, &at, &split) == 3 && (at == 8 || at == 16 || at == 32) &&
+                split >= 1 && split <= 16)
+                ctx->tiles[key] = rp::TileConfig{at, split};
+        }
+        std::fclose(f);
+    });
 }
 
 int rp_set_kappa_limit(rp_ctx *ctx, double kappa_max) {

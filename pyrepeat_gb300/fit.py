@@ -272,6 +272,38 @@ class Context:
             o += c.n_atoms
         return res, M, info.reshape(n, _lib.FIT_INFO_WORDS)
 
+    def autotune(self, cubes, cache_path: str | None = None, V_dev=None) -> dict:
+        """Tile shapes of the mixed path timed per (atoms, kept points, KMAX) bucket of the
+        cubes (rp_autotune); with cache_path the table is written there.  Returns
+        {bucket key: (phi_atoms, gram_split, best_ms, default_ms, N, M)} for the buckets
+        this call measured (read back from the cache when one is given)."""
+        n = len(cubes)
+        keep = []
+        arr = (_lib.RpFitDesc * n)()
+        for i, c in enumerate(cubes):
+            arr[i] = self._desc(c, _lib.PREC_MIXED, keep)
+        vptr = None
+        if V_dev is None and any(getattr(c, "V_dev", None) is not None for c in cubes):
+            V_dev = [getattr(c, "V_dev", None) for c in cubes]
+        if V_dev is not None:
+            vptr = (ctypes.c_void_p * n)(*[v.data_ptr() if v is not None else None for v in V_dev])
+        path = cache_path.encode() if cache_path else None
+        self.check(self.lib.rp_autotune(self.ptr, n, ctypes.cast(arr, ctypes.c_void_p), vptr, path), "rp_autotune")
+        table = {}
+        if cache_path:
+            with open(cache_path) as f:
+                for line in f:
+                    if line.startswith("#"):
+                        continue
+                    v = line.split()
+                    if len(v) >= 7:
+                        table[int(v[0])] = (int(v[1]), int(v[2]), float(v[3]), float(v[4]), int(v[5]), int(v[6]))
+        return table
+
+    def load_tiles(self, cache_path: str):
+        """Tile shapes from an rp_autotune cache file."""
+        self.check(self.lib.rp_load_tiles(self.ptr, cache_path.encode()), "rp_load_tiles")
+
     def batch_submit(self, cubes, precision=_lib.PREC_MIXED, V_dev=None) -> "PendingBatch":
         """Queue a batch on the context's worker thread (rp_batch_submit) and return at once.
         The returned handle keeps every array the worker reads alive until it is done."""
