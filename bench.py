@@ -44,8 +44,8 @@ METRIC = "fits/s & p50/p99 latency vs plain FP64 GPU fit at max|dq|<=1e-5 e"
 # ncu figures of phi_chunk_kernel: DRAM bytes and thread instructions per point-atom pair
 # of the captured launch (the file holds the command and the raw figures)
 PHI_CAPTURE = "profiles/phi_chunk_kernel_batch8.txt"
-PHI_DRAM_PER_PAIR = 10.12
-PHI_INST_PER_PAIR = 344.0
+PHI_DRAM_PER_PAIR = 10.15
+PHI_INST_PER_PAIR = 344.4
 
 
 # ----------------------------------------------------------------------------- distributed helpers

@@ -274,6 +274,7 @@ struct rp_ctx {
     std::unordered_map<std::string, rp::Buffer> host_scratch;
     double bound_scale = 1.0;  // factor on the single-pass Phi bounds (tests shrink it to force clamps)
     long long chunk_cap = 0;   // cap on the staged mixed Gram's points per chunk (tests; 0 = none)
+    long long wait_budget = 4000000000LL;  // clock budget of the Gram pipeline's waits (tests shorten it)
     std::unique_ptr<rp::HostPool> pool;  // host workers (created on first use)
     std::unique_ptr<rp::BatchServer> server;  // asynchronous batches (created on first submit)
     // per-cube host objects of the batched fit, kept across batches for their capacity (per slot)

@@ -120,6 +120,7 @@ __device__ __forceinline__ bool near_any(const FilterParams &p, int i, int j, in
 constexpr int kBrickX = 8, kBrickY = 4, kBrickZ = 4;
 constexpr int kBrickPts = kBrickX * kBrickY * kBrickZ;  // 128
 constexpr int kCullCap = 512;  // candidate images a brick keeps in shared memory
+constexpr int kCullRows = 64;  // (y, z) bin rows a brick's cull shares out over its threads
 
 // One cube's filter in a grouped launch: its plan, grid values, scratch and outputs.  A launch
 // carries up to kFilterJobs of them by value; job j owns blocks [blk[j], blk[j+1]) of the
@@ -184,7 +185,8 @@ __global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(const __grid_co
     __shared__ float4 cand[kCullCap];
     __shared__ int cidx[kCullCap];
     __shared__ int ncand;
-    __shared__ float red[6][kBrickPts / 32];
+    __shared__ float box[6];
+    __shared__ int row_t0[kCullRows], row_pre[kCullRows + 1];
     const int jb = filter_job_of(L, blockIdx.x);
     const FilterJob &J = L.job[jb];
     const FilterParams &p = J.p;
@@ -202,30 +204,43 @@ __global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(const __grid_co
     const float gx = (i * p.ax[0] + j * p.ax[3]) + k * p.ax[6];
     const float gy = (i * p.ax[1] + j * p.ax[4]) + k * p.ax[7];
     const float gz = (i * p.ax[2] + j * p.ax[5]) + k * p.ax[8];
-    // bounding box of the brick's points (exactly their FP32 coordinates)
-    float v[6] = {inside ? gx : 3e38f, inside ? gy : 3e38f, inside ? gz : 3e38f,
-                  inside ? gx : -3e38f, inside ? gy : -3e38f, inside ? gz : -3e38f};
+    // bounding box of the brick: its index box's eight corners (clipped to the grid) in FP32 by
+    // the points' own expression, padded by 16 ulps of the largest coordinate, which covers the
+    // rounding by which an inner point's FP32 coordinates can pass the corners' box
+    if (warp == 0) {
+        const int ci = (lane & 1) ? min(bx * kBrickX + kBrickX - 1, p.nx - 1) : bx * kBrickX;
+        const int cj = (lane & 2) ? min(by * kBrickY + kBrickY - 1, p.ny - 1) : by * kBrickY;
+        const int ck = (lane & 4) ? min(bz * kBrickZ + kBrickZ - 1, p.nz - 1) : bz * kBrickZ;
+        float v[6];
+        v[0] = v[3] = (ci * p.ax[0] + cj * p.ax[3]) + ck * p.ax[6];
+        v[1] = v[4] = (ci * p.ax[1] + cj * p.ax[4]) + ck * p.ax[7];
+        v[2] = v[5] = (ci * p.ax[2] + cj * p.ax[5]) + ck * p.ax[8];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
+        for (int o = 1; o < 8; o <<= 1)
 #pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            const float w = __shfl_xor_sync(0xffffffffu, v[q], o);
-            v[q] = q < 3 ? fminf(v[q], w) : fmaxf(v[q], w);
+            for (int q = 0; q < 6; ++q) {
+                const float w = __shfl_xor_sync(0xffffffffu, v[q], o);
+                v[q] = q < 3 ? fminf(v[q], w) : fmaxf(v[q], w);
+            }
+        if (lane == 0) {
+            float big = 0.f;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) big = fmaxf(big, fabsf(v[q]));
+            const float pad = 16.f * big * 1.1920929e-7f + 1e-30f;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                box[q] = v[q] - pad;
+                box[3 + q] = v[3 + q] + pad;
+            }
+            ncand = 0;
         }
-    if (lane == 0)
-#pragma unroll
-        for (int q = 0; q < 6; ++q) red[q][warp] = v[q];
-    if (t == 0) ncand = 0;
+    }
     __syncthreads();
     float lo[3], hi[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        lo[d] = red[d][0];
-        hi[d] = red[3 + d][0];
-        for (int w = 1; w < kBrickPts / 32; ++w) {
-            lo[d] = fminf(lo[d], red[d][w]);
-            hi[d] = fmaxf(hi[d], red[3 + d][w]);
-        }
+        lo[d] = box[d];
+        hi[d] = box[3 + d];
     }
     // bins that can hold a rejecting image: one bin beyond the box's own on every side
     int c0[3], c1[3];
@@ -236,26 +251,67 @@ __global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(const __grid_co
         c0[d] = max(min(max((int)floorf(ta), 0), p.bn[d] - 1) - 1, 0);
         c1[d] = min(min(max((int)floorf(tb), 0), p.bn[d] - 1) + 1, p.bn[d] - 1);
     }
-    for (int z2 = c0[2]; z2 <= c1[2]; ++z2)
-        for (int y2 = c0[1]; y2 <= c1[1]; ++y2) {
-            const int row = p.bn[0] * (y2 + p.bn[1] * z2);
-            const int t0 = boff[row + c0[0]], t1 = boff[row + c1[0] + 1];
-            for (int u = t0 + t; u < t1; u += kBrickPts) {
-                const int a = bidx[u];
-                const float4 e = eff[a];
-                const float dx = fmaxf(fmaxf(lo[0] - e.x, e.x - hi[0]), 0.f);
-                const float dy = fmaxf(fmaxf(lo[1] - e.y, e.y - hi[1]), 0.f);
-                const float dz = fmaxf(fmaxf(lo[2] - e.z, e.z - hi[2]), 0.f);
-                const float d2 = dx * dx + dy * dy + dz * dz;
-                if (d2 <= (e.w + p.err_min) * 1.0001f) {
-                    const int pos = atomicAdd(&ncand, 1);
-                    if (pos < kCullCap) {
-                        cand[pos] = e;
-                        cidx[pos] = a;
-                    }
-                }
+    // the images of those bins: a contiguous run of the cell list per (y, z) bin row; the rows'
+    // runs are concatenated (prefix in shared memory) and shared out over the threads
+    const int ry = c1[1] - c0[1] + 1, R = ry * (c1[2] - c0[2] + 1);
+    auto cull = [&](int a) {
+        const float4 e = eff[a];
+        const float dx = fmaxf(fmaxf(lo[0] - e.x, e.x - hi[0]), 0.f);
+        const float dy = fmaxf(fmaxf(lo[1] - e.y, e.y - hi[1]), 0.f);
+        const float dz = fmaxf(fmaxf(lo[2] - e.z, e.z - hi[2]), 0.f);
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 <= (e.w + p.err_min) * 1.0001f) {
+            const int pos = atomicAdd(&ncand, 1);
+            if (pos < kCullCap) {
+                cand[pos] = e;
+                cidx[pos] = a;
             }
         }
+    };
+    if (R <= kCullRows) {
+        if (warp < kCullRows / 32) {  // row runs and their prefix (a warp scan per 32 rows)
+            const int r = t;
+            int cnt = 0;
+            if (r < R) {
+                const int y2 = c0[1] + r % ry, z2 = c0[2] + r / ry;
+                const int row = p.bn[0] * (y2 + p.bn[1] * z2);
+                const int t0 = boff[row + c0[0]];
+                row_t0[r] = t0;
+                cnt = boff[row + c1[0] + 1] - t0;
+            }
+            int inc = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int w = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += w;
+            }
+            row_pre[r + 1] = inc;  // inclusive within its warp; the warps are joined below
+        }
+        __syncthreads();
+        if (t == 0) {
+            row_pre[0] = 0;
+            for (int w = 1; w < kCullRows / 32; ++w)
+                for (int r = 32 * w + 1; r <= 32 * w + 32; ++r) row_pre[r] += row_pre[32 * w];
+        }
+        __syncthreads();
+        const int total = row_pre[R];
+        for (int u = t; u < total; u += kBrickPts) {
+            int lo_r = 0, hi_r = R - 1;  // the row whose run holds u
+            while (lo_r < hi_r) {
+                const int mid = (lo_r + hi_r + 1) >> 1;
+                if (row_pre[mid] <= u) lo_r = mid;
+                else hi_r = mid - 1;
+            }
+            cull(bidx[row_t0[lo_r] + (u - row_pre[lo_r])]);
+        }
+    } else {
+        for (int z2 = c0[2]; z2 <= c1[2]; ++z2)
+            for (int y2 = c0[1]; y2 <= c1[1]; ++y2) {
+                const int row = p.bn[0] * (y2 + p.bn[1] * z2);
+                const int t0 = boff[row + c0[0]], t1 = boff[row + c1[0] + 1];
+                for (int u = t0 + t; u < t1; u += kBrickPts) cull(bidx[u]);
+            }
+    }
     __syncthreads();
     const int nc = ncand;
     int keep = 0;

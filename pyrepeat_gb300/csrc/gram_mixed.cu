@@ -20,7 +20,7 @@
 //  3. Gram    G = X X^T on tcgen05 (kind::f16, FP32 accumulators in TMEM) with all
 //             16 digit products kept: every partial sum is an integer below 2^24,
 //             so the Gram of the staged Phi is exact; partial tiles of point splits
-//             are summed in FP64 in a fixed order.
+//             are int64 and summed exactly, then rounded to FP64 once.
 //  4. finish  A = G - s s^T/M, b = G[:,V] - s sum(V)/M with s = sum_m (Phi - c)
 //             (FP64), i.e. repeat.py:2266-2276 for the shifted columns.
 //
@@ -78,8 +78,9 @@ constexpr int kGramSmem = kGramStages * kGramStageBytes + 1024 + 256;
 
 struct GramArgs {
     int nt, ntj, ntri, kb_total, kb_per_split, flush;  // flush: stages per exact FP32 run (<= kGramFlush)
-    double *out;  // partial tiles [split*ntri + tri][col][row], FP64 (exact integers)
+    long long *out;  // partial tiles [split*ntri + tri][col][row], exact int64 (below 2^62)
     int *status;
+    long long budget;  // clock budget of the pipeline's waits (tc::kWaitBudgetCycles; <= 0: give up at once)
 };
 
 __device__ __forceinline__ uint8_t *align1024(uint8_t *raw) {
@@ -142,11 +143,12 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_holder;
 
+    int accf_commits = 0;  // phases of accf the MMA thread (warp 1, lane 0) has committed
     if (warp == 0 && lane == 0) {
         int issued = 0;
         for (int kb = 0; kb < nkb; ++kb) {
             const int s = kb % kGramStages, u = kb / kGramStages;
-            if (u > 0 && !tc::mbar_wait(&empty[s], (u - 1) & 1, g.status)) break;
+            if (u > 0 && !tc::mbar_wait(&empty[s], (u - 1) & 1, g.status, g.budget)) break;
             uint8_t *st = smem + s * kGramStageBytes;
             tc::mbar_arrive_expect_tx(&full[s], stage_tx);
             const int x = (kb0 + kb) * kBK;
@@ -168,12 +170,13 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
         for (int q = 0; q < kGroups; ++q) d[q] = tmem + (uint32_t)(q * kGN);
         bool ok = true;
         for (int f = 0; f < nflush && ok; ++f) {
-            if (f > 0 && !tc::mbar_wait(acce, (f - 1) & 1, g.status)) break;  // epilogue drained the sums
+            if (f > 0 && !tc::mbar_wait(acce, (f - 1) & 1, g.status, g.budget)) break;  // epilogue drained the sums
+            ++accf_commits;
             tc::fence_after_sync();
             const int kbf0 = f * g.flush, kbf1 = min(kbf0 + g.flush, nkb);
             for (int kb = kbf0; kb < kbf1; ++kb) {
                 const int s = kb % kGramStages, u = kb / kGramStages;
-                if (!tc::mbar_wait(&full[s], u & 1, g.status)) {
+                if (!tc::mbar_wait(&full[s], u & 1, g.status, g.budget)) {
                     ok = false;
                     break;
                 }
@@ -223,7 +226,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
         for (int i = 0; i < 32; ++i) acc[i] = 0;
         bool ok = true;
         for (int f = 0; f < nflush; ++f) {
-            if (!tc::mbar_wait(accf, f & 1, g.status)) {
+            if (!tc::mbar_wait(accf, f & 1, g.status, g.budget)) {
                 ok = false;
                 break;
             }
@@ -241,13 +244,15 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
             tc::mbar_arrive(acce);
         }
         if (ok && *reinterpret_cast<volatile int *>(g.status) == 0) {
-            double *o = g.out + (long long)blockIdx.x * (kBM * kGN);
+            long long *o = g.out + (long long)blockIdx.x * (kBM * kGN);
             const int r = lane_base + lane;
 #pragma unroll
-            for (int i = 0; i < 32; ++i) o[(col0 + i) * kBM + r] = (double)acc[i];
+            for (int i = 0; i < 32; ++i) o[(col0 + i) * kBM + r] = acc[i];
         }
     }
-    if (warp == 1 && lane == 0) tc::mbar_wait(accf, (nflush - 1) & 1, nullptr);
+    // the MMA thread waits for its last commit (every MMA done) before TMEM is freed; after a
+    // timeout that is the last phase it committed, not the last of the plan
+    if (warp == 1 && lane == 0 && accf_commits > 0) tc::mbar_wait(accf, (accf_commits - 1) & 1, nullptr);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -289,36 +294,6 @@ __device__ __forceinline__ void digits4(int v, __half *o0, __half *o1, __half *o
     o1[idx] = __int2half_rn(s1);
     o2[idx] = __int2half_rn(s2);
     o3[idx] = __int2half_rn(s3);
-}
-
-// Two digits d_lo, d_hi in [-64, 64] as an FP16 pair without a conversion instruction: the
-// FP16 bits 0x6440 + d encode 1088 + d (exponent 2^10, unit spacing), so one packed
-// subtraction of 1088 leaves d exactly.
-__device__ __forceinline__ uint32_t digit_pair(int d_lo, int d_hi) {
-    const uint32_t w = (uint32_t)(0x6440 + d_lo) | ((uint32_t)(0x6440 + d_hi) << 16);
-    const __half2 h = __hsub2(*reinterpret_cast<const __half2 *>(&w), __half2half2(__ushort_as_half(0x6440)));
-    return *reinterpret_cast<const uint32_t *>(&h);
-}
-
-// The digits of two consecutive points m (even lane) and m + 1 (odd lane) of one row: the lanes
-// swap half their digits, then the even lane stores slices 0 and 1 and the odd lane slices 2
-// and 3, each as one 32-bit pair (m, m + 1).  Both lanes of a pair must call it together; idx
-// is the even point's element index (even, so the pair is 4-byte aligned).
-__device__ __forceinline__ void digits4_pair(int v, bool odd, __half *o0, __half *o1, __half *o2, __half *o3,
-                                             long long idx_even) {
-    int s0, s1, s2, s3;
-    split4(v, s0, s1, s2, s3);
-    const uint32_t give = odd ? ((uint32_t)(s0 & 0xffff) | ((uint32_t)s1 << 16))
-                              : ((uint32_t)(s2 & 0xffff) | ((uint32_t)s3 << 16));
-    const uint32_t got = __shfl_xor_sync(0xffffffffu, give, 1);
-    const int g_lo = (int)(short)(got & 0xffff), g_hi = (int)(short)(got >> 16);
-    if (!odd) {  // own (m) and partner's (m + 1) slices 0 and 1
-        *reinterpret_cast<uint32_t *>(o0 + idx_even) = digit_pair(s0, g_lo);
-        *reinterpret_cast<uint32_t *>(o1 + idx_even) = digit_pair(s1, g_hi);
-    } else {     // partner's (m) and own (m + 1) slices 2 and 3
-        *reinterpret_cast<uint32_t *>(o2 + idx_even) = digit_pair(g_lo, s2);
-        *reinterpret_cast<uint32_t *>(o3 + idx_even) = digit_pair(g_hi, s3);
-    }
 }
 
 // round((h + l) * sc) for a double-float (h, l) and a power of two sc, |(h + l) sc| <= 2^27:
@@ -380,9 +355,12 @@ __device__ __forceinline__ float ex2_ftz(float x) {
 // t = 1/(1 + x/2), fractional error below 1.2e-7.  It is evaluated in base 2: the argument
 // comes pre-scaled, xs = sqrt(log2 e) x, and log2(e) is folded into the coefficients, so
 //   erfc(x) = t 2^(-xs^2 + log2(e) P(t)),   t = 1 / (1 + xs / (2 sqrt(log2 e))),
-// 14 instructions (one reciprocal, one exponential).  For the real-space range
-// x = sqrt(alpha) r <= pi it is within 5e-7 (x < 1.5) and 1.3e-6 (x near pi, terms ~1e-6
-// of the largest) of FP64 erfc.
+// 14 instructions (one reciprocal, one exponential).  In FP32 the rounding of the exponent
+// -xs^2 + p and of the reciprocal and exponential instructions dominates the error
+// (measured against FP64 erfc and against CUDA's erfcf in the tests).  A degree-7 fit for
+// the bounded range x <= pi (two FMAs fewer) was measured and dropped: its coefficients,
+// up to 15 with alternating signs, lose bits in FP32 Horner evaluation (1.3e-6 for
+// x < 1.5) and moved the batch's charges from 3.9e-7 to 4.6e-7 e of FP64.
 constexpr double kLog2e = 1.4426950408889634074;
 constexpr double kSqrtLog2e = 1.2011224087864498;  // sqrt(log2 e)
 __device__ __forceinline__ float erfc_nr2(float xs) {
@@ -717,10 +695,7 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
             if (valid) I = x_fixed(out.x, out.y, dg.scale[a0 + a], dg.clamped);
             const long long rs = warp_sum_fixed(I);
             if (lane == 0) wrow[warp][a] = rs;
-            // rows_kpad is even and every pair of lanes holds points (m, m + 1), m even: a pair is
-            // wholly inside or wholly past the padded row, so both lanes take the branch together
-            if (m < dg.rows_kpad)
-                digits4_pair(I, lane & 1, dg.X0, dg.X1, dg.X2, dg.X3, (long long)(a0 + a) * dg.ldx + (m & ~1LL));
+            if (m < dg.rows_kpad) digits4(I, dg.X0, dg.X1, dg.X2, dg.X3, (long long)(a0 + a) * dg.ldx + m);
         } else if (valid) {
             *prow = out;
         }
@@ -748,8 +723,7 @@ __global__ void __launch_bounds__(kPhiPts, 7) phi_chunk_kernel(
             }
             const long long rs = warp_sum_fixed(I);
             if (lane == 0) wrow[warp][AT] = rs;
-            if (m < dg.rows_kpad)
-                digits4_pair(I, lane & 1, dg.X0, dg.X1, dg.X2, dg.X3, (long long)dg.N * dg.ldx + (m & ~1LL));
+            if (m < dg.rows_kpad) digits4(I, dg.X0, dg.X1, dg.X2, dg.X3, (long long)dg.N * dg.ldx + m);
         }
         __syncthreads();
         // exact row sums (two's complement int64 atomics: order-independent), one per CTA and row
@@ -951,10 +925,14 @@ __global__ void __launch_bounds__(kSliceThreads) slice_rows_kernel(const float2 
     *reinterpret_cast<__half2 *>(X3 + idx) = __halves2half2(d3[0], d3[1]);
 }
 
-// Sum the partial Gram tiles of all point splits in a fixed order (FP64; each
-// partial is an exact integer) and add them, unscaled, into G (Np x Np).  Tiles
-// inside a 128-row block already hold both (a,b) and (b,a); the others are mirrored.
-__global__ void gram_reduce_kernel(const double *__restrict__ part, int ntiles, int nsplit, int ntj, int Np,
+// Sum the partial Gram tiles of all point splits exactly and add them, unscaled, into G
+// (Np x Np).  Each partial is an int64 below 2^62; the sum is carried as 32-bit halves
+// (sum of p >> 32 and of p & (2^32 - 1), neither can overflow for fewer than 2^31
+// splits), so it is the exact integer whatever the splits, and it is rounded to FP64
+// once: (hi 2^32 exactly) + lo.  The Gram of a chunk therefore does not depend on the
+// points per CTA.  Tiles inside a 128-row block already hold both (a,b) and (b,a); the
+// others are mirrored.
+__global__ void gram_reduce_kernel(const long long *__restrict__ part, int ntiles, int nsplit, int ntj, int Np,
                                    const float *__restrict__ scale, const double *__restrict__ vmax_p, int N,
                                    double *__restrict__ G) {
     const float vscale = vscale_of(*vmax_p);
@@ -966,19 +944,29 @@ __global__ void gram_reduce_kernel(const double *__restrict__ part, int ntiles, 
     const int c = e / kBM, r = e - c * kBM;
     const int a = ti * kBM + r, b = tj * kGN + c;
     if (a >= Np || b >= Np) return;
-    double s = 0.0;
-    // the splits in order; eight loads in flight at a time (the sum order is unchanged)
-    const double *src = part + (size_t)tile * (kBM * kGN) + e;
+    long long hi = 0, lo = 0;
+    // eight loads in flight at a time
+    const long long *src = part + (size_t)tile * (kBM * kGN) + e;
     const size_t step = (size_t)ntiles * (kBM * kGN);
     int k = 0;
     for (; k + 8 <= nsplit; k += 8) {
-        double v[8];
+        long long v[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) v[u] = src[(size_t)(k + u) * step];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) s += v[u];
+        for (int u = 0; u < 8; ++u) {
+            hi += v[u] >> 32;
+            lo += v[u] & 0xffffffffLL;
+        }
     }
-    for (; k < nsplit; ++k) s += src[(size_t)k * step];
+    for (; k < nsplit; ++k) {
+        const long long v = src[(size_t)k * step];
+        hi += v >> 32;
+        lo += v & 0xffffffffLL;
+    }
+    hi += lo >> 32;  // normalise: lo in [0, 2^32), |hi| < 2^53 (the total is below 2^85)
+    lo &= 0xffffffffLL;
+    double s = (double)hi * 4294967296.0 + (double)lo;
     const double sa = (a < N) ? (double)scale[a] : (double)vscale;
     const double sb = (b < N) ? (double)scale[b] : (double)vscale;
     s = ldexp(s, -54) / (sa * sb);
@@ -1232,11 +1220,11 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
                 rowsum);
             RP_LAUNCH_CHECK();
         }
-        // 3. exact Gram partial tiles over point splits, then the fixed-order FP64 reduction
+        // 3. exact Gram partial tiles over point splits, then their exact sum, rounded once
         {
             const int kb_total = (int)(rows_kpad / kBK);
             const int nsplit = (kb_total + kb_split - 1) / kb_split;
-            double *part = ctx->buf_t<double>("m_part" + slot, (size_t)nsplit * ntri * kBM * kGN);
+            long long *part = ctx->buf_t<long long>("m_part" + slot, (size_t)nsplit * ntri * kBM * kGN);
             GramArgs g{};
             g.nt = nt;
             g.ntj = ntj;
@@ -1246,6 +1234,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
             g.flush = kGramFlush;
             g.out = part;
             g.status = d_status;
+            g.budget = ctx->wait_budget;
             const __half *Xq[kGSlices] = {X[0], X[1], X[2], X[3]};
             {
                 StageTimer tt(ctx, "gram_exact", stream);
@@ -1275,6 +1264,15 @@ extern "C" int rp_debug_bound_scale(rp_ctx *ctx, double factor) {
     return RP_OK;
 }
 
+// Diagnostics (not part of the public ABI): the clock budget of the Gram pipeline's waits
+// (cycles < 0: the default, ~2 s; 0: every wait gives up at once, which exercises the
+// timeout path: RP_E_TIMEOUT, the kernel unwinds, the ctx stays usable).
+extern "C" int rp_debug_wait_budget(rp_ctx *ctx, long long cycles) {
+    if (!ctx) return RP_E_ARG;
+    ctx->wait_budget = cycles < 0 ? rp::tc::kWaitBudgetCycles : cycles;
+    return RP_OK;
+}
+
 // Diagnostics (not part of the public ABI): an upper bound on the kept points per chunk of
 // the staged mixed Gram (0 = the memory-based size), so tests can run many chunks on a
 // small cube.
@@ -1286,6 +1284,26 @@ extern "C" int rp_debug_chunk_cap(rp_ctx *ctx, long long points) {
 
 // Diagnostics: how many cubes of the last batched fit were redone in two passes.
 extern "C" int rp_debug_last_fallbacks(const rp_ctx *ctx) { return ctx ? ctx->last_fallbacks : RP_E_ARG; }
+
+namespace rp {
+namespace {
+__global__ void erfc_kernel(const float *__restrict__ x, long long n, float *__restrict__ out) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) out[t] = erfc_nr2((float)kSqrtLog2e * x[t]);
+}
+}  // namespace
+}  // namespace rp
+
+// Diagnostics (not part of the public ABI): the real-space kernels' FP32 erfc at n
+// arguments x (device arrays), for the test against FP64 erfc and CUDA's erfcf.
+extern "C" int rp_debug_erfc(const float *x_dev, long long n, float *out_dev) {
+    using namespace rp;
+    if (!x_dev || !out_dev || n < 0) return RP_E_ARG;
+    if (n == 0) return RP_OK;
+    erfc_kernel<<<(unsigned)((n + 255) / 256), 256>>>(x_dev, n, out_dev);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return RP_E_CUDA;
+    return RP_OK;
+}
 
 // Diagnostics (not part of the public ABI): the mixed path's Phi for the first
 // `rows` kept points, atom-major [N][rows]; parts = 1 real space, 2 reciprocal,
@@ -1338,12 +1356,12 @@ extern "C" int rp_debug_gram_slices(rp_ctx *ctx, const void *X0, const void *X1,
         for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
         const int kb_total = (int)(cols / kBK);
         const int nsplit = (kb_total + kb_split - 1) / kb_split;
-        double *part = ctx->buf_t<double>("dbg_part", (size_t)nsplit * ntri * kBM * kGN);
+        long long *part = ctx->buf_t<long long>("dbg_part", (size_t)nsplit * ntri * kBM * kGN);
         RP_CUDA(cudaMemset(ctx->d_status, 0, sizeof(int)));
         GramArgs g{};
         g.nt = nt; g.ntj = ntj; g.ntri = ntri; g.kb_total = kb_total; g.kb_per_split = kb_split;
         g.flush = std::min(std::max(flush, 1), kGramFlush);
-        g.out = part; g.status = ctx->d_status;
+        g.out = part; g.status = ctx->d_status; g.budget = ctx->wait_budget;
         const __half *Xq[kGSlices] = {(const __half *)X0, (const __half *)X1, (const __half *)X2, (const __half *)X3};
         launch_gram(Xq, Np, cols, g, ntri * nsplit, 0);
         float *ones = ctx->buf_t<float>("dbg_ones", Np);

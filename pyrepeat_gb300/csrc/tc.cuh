@@ -50,15 +50,23 @@ constexpr long long kWaitBudgetCycles = 4000000000LL;
 
 // Bounded wait on a phase parity. Returns false when the budget runs out or
 // (with a status word) another thread of the kernel already gave up; a timeout
-// is recorded in *status.  status may be null (unwinding: wait, record nothing).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status) {
+// is recorded in *status.  status may be null (unwinding: wait up to the default
+// budget, record nothing).  With a status word and budget <= 0 the wait gives up
+// at once, as if its budget had run out (the test of the unwinding path).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status,
+                                          long long budget = kWaitBudgetCycles) {
+    if (status && budget <= 0) {
+        atomicCAS(status, 0, RP_E_TIMEOUT);
+        return false;
+    }
     if (mbar_try_wait(bar, parity)) return true;
+    if (!status) budget = kWaitBudgetCycles;
     long long t0 = clock64();
     for (uint32_t it = 1;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 255u) == 0) {
             if (status && *reinterpret_cast<volatile int *>(status) != 0) return false;
-            if (clock64() - t0 > kWaitBudgetCycles) {
+            if (clock64() - t0 > budget) {
                 if (status) atomicCAS(status, 0, RP_E_TIMEOUT);
                 return false;
             }

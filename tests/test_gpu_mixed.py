@@ -259,3 +259,57 @@ def test_bordered_solve_large_systems(gpu_ctx, N):
     ref = sl.solve(K, np.concatenate([b, [0.5]]))[:N]
     q = q.cpu().numpy()
     assert np.abs(q - ref).max() <= 1e-9 * max(1.0, np.abs(ref).max())
+
+
+def test_real_space_erfc_error_bound(gpu_ctx):
+    """The real-space kernels' FP32 erfc (the all-range Chebyshev fit evaluated in base 2
+    with the approximate reciprocal and exponential instructions) against FP64 erfc over
+    the real-space range 0 <= x = sqrt(alpha) r <= pi, and against CUDA's own erfcf:
+    within 1.5e-6 relative below x = 1.5 and 2.5e-6 up to pi (where the terms are ~1e-6
+    of the largest), and within 2e-6 of erfcf's own error."""
+    import torch
+    from scipy.special import erfc
+    L = gpu_ctx.lib
+    L.rp_debug_erfc.restype = ctypes.c_int
+    L.rp_debug_erfc.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p]
+    x = torch.linspace(0.0, float(np.pi), 200001, dtype=torch.float32, device="cuda")
+    out = torch.empty_like(x)
+    assert L.rp_debug_erfc(x.data_ptr(), x.numel(), out.data_ptr()) == 0
+    xs = x.cpu().numpy().astype(np.float64)
+    ref = erfc(xs)
+    rel = np.abs(out.cpu().numpy().astype(np.float64) / ref - 1.0)
+    assert rel[xs < 1.5].max() <= 1.5e-6
+    assert rel.max() <= 2.5e-6
+    cuda_rel = np.abs(torch.special.erfc(x).cpu().numpy().astype(np.float64) / ref - 1.0)
+    assert rel.max() <= cuda_rel.max() + 2e-6
+
+
+def test_pipeline_wait_timeout_is_reported_and_the_context_recovers():
+    """The Gram kernel's bounded waits: with a budget of zero every wait of the tensor-core
+    pipeline gives up at once (as if it had run out), the kernel unwinds (waits for its
+    own copies and MMAs, frees TMEM) and the fit returns RP_E_TIMEOUT; the same context
+    then fits the cube normally, with the same charges as a fresh context."""
+    from pyrepeat_gb300 import _lib
+    from pyrepeat_gb300.fit import Context
+    cube, _ = load_golden("water24")
+    ref = Context(0)
+    try:
+        q_ref = np.asarray(ref.fit_batch([cube], _lib.PREC_MIXED)[0][0]).copy()
+    finally:
+        ref.close()
+    ctx = Context(0)
+    try:
+        L = ctx.lib
+        L.rp_debug_wait_budget.restype = ctypes.c_int
+        L.rp_debug_wait_budget.argtypes = [ctypes.c_void_p, ctypes.c_longlong]
+        assert L.rp_debug_wait_budget(ctx.ptr, 0) == 0
+        try:
+            with pytest.raises(_lib.RepeatError) as err:
+                ctx.fit_batch([cube], _lib.PREC_MIXED)
+            assert err.value.code == -5
+        finally:
+            assert L.rp_debug_wait_budget(ctx.ptr, -1) == 0
+        q = np.asarray(ctx.fit_batch([cube], _lib.PREC_MIXED)[0][0])
+        assert np.array_equal(q, q_ref)
+    finally:
+        ctx.close()
