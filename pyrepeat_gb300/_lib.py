@@ -164,9 +164,6 @@ def launch_count() -> int:
 
 def make_grid(n_grid, axis) -> RpGrid:
     g = RpGrid()
-    for i in range(3):
-        g.n_grid[i] = int(n_grid[i])
-    flat = [float(x) for row in axis for x in row]
-    for i in range(9):
-        g.axis[i] = flat[i]
+    g.n_grid[:] = [int(v) for v in n_grid]
+    g.axis[:] = [float(x) for row in axis for x in row]
     return g

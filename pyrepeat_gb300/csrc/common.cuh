@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <condition_variable>
@@ -287,6 +288,17 @@ struct rp_ctx {
         }
         pool->run(n, f);
     }
+    // host-side timeline of the batched fit (rp_debug_trace): phase labels and host times,
+    // for finding where the host waits; off by default
+    bool trace = false;
+    std::vector<std::pair<std::string, double>> trace_log;
+    void trace_mark(const std::string &label) {
+        if (!trace) return;
+        const double t = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+        std::lock_guard<std::mutex> lk(trace_mu);
+        trace_log.emplace_back(label, t);
+    }
+    std::mutex trace_mu;
     int last_fallbacks = 0;    // cubes of the last batch redone in two passes after a clamp
     int last_escalations = 0;  // mixed-precision cubes of the last batch refitted in FP64
     // mixed-precision fits whose kappa / (n+1) (the solve's ||A||_1 ||K^-1||_1 over the

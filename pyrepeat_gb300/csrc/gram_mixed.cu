@@ -19,8 +19,9 @@
 //             power-of-two row scale.
 //  3. Gram    G = X X^T on tcgen05 (kind::f16, FP32 accumulators in TMEM) with all
 //             16 digit products kept: every partial sum is an integer below 2^24,
-//             so the Gram of the staged Phi is exact; partial tiles of point splits
-//             are int64 and summed exactly, then rounded to FP64 once.
+//             so the Gram of the staged Phi is exact; each CTA (one point split of
+//             one tile) adds its int64 sums to the tile's exact 64-bit totals with
+//             atomics, which are rounded to FP64 once.
 //  4. finish  A = G - s s^T/M, b = G[:,V] - s sum(V)/M with s = sum_m (Phi - c)
 //             (FP64), i.e. repeat.py:2266-2276 for the shifted columns.
 //
@@ -78,7 +79,9 @@ constexpr int kGramSmem = kGramStages * kGramStageBytes + 1024 + 256;
 
 struct GramArgs {
     int nt, ntj, ntri, kb_total, kb_per_split, flush;  // flush: stages per exact FP32 run (<= kGramFlush)
-    long long *out;  // partial tiles [split*ntri + tri][col][row], exact int64 (below 2^62)
+    // exact tile sums [tri][col][row] as two's complement 64-bit halves: every CTA adds the
+    // high (acc >> 32) and low (acc & (2^32 - 1)) parts of its int64 partial (|acc| < 2^62)
+    unsigned long long *out_hi, *out_lo;
     int *status;
     long long budget;  // clock budget of the pipeline's waits (tc::kWaitBudgetCycles; <= 0: give up at once)
 };
@@ -244,10 +247,14 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
             tc::mbar_arrive(acce);
         }
         if (ok && *reinterpret_cast<volatile int *>(g.status) == 0) {
-            long long *o = g.out + (long long)blockIdx.x * (kBM * kGN);
+            const long long t0 = (long long)tile * (kBM * kGN);
             const int r = lane_base + lane;
 #pragma unroll
-            for (int i = 0; i < 32; ++i) o[(col0 + i) * kBM + r] = acc[i];
+            for (int i = 0; i < 32; ++i) {
+                const long long e = t0 + (col0 + i) * kBM + r;
+                atomicAdd(g.out_hi + e, (unsigned long long)(acc[i] >> 32));
+                atomicAdd(g.out_lo + e, (unsigned long long)(acc[i] & 0xffffffffLL));
+            }
         }
     }
     // the MMA thread waits for its last commit (every MMA done) before TMEM is freed; after a
@@ -832,7 +839,7 @@ __global__ void colstats_finish_kernel(const double *__restrict__ psum, const fl
 // Later chunks of a two-pass fit keep the first chunk's centre c and take a scale of their
 // own: |Phi - c| <= 2 max(max|Phi|, |c|) =: bound in [2^(e-1), 2^e), scale 2^(-e-1).  Each
 // chunk's Gram tiles and row sums are converted to Phi units with that chunk's scale
-// (gram_reduce_kernel, rowsum_flush_kernel), so chunks need not share one.
+// (gram_finish_tiles_kernel, rowsum_flush_kernel), so chunks need not share one.
 __global__ void colstats_scale_kernel(const float *__restrict__ pmax, int nblk, int N, const double *__restrict__ c,
                                       float *__restrict__ scale) {
     const int a = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
@@ -925,16 +932,14 @@ __global__ void __launch_bounds__(kSliceThreads) slice_rows_kernel(const float2 
     *reinterpret_cast<__half2 *>(X3 + idx) = __halves2half2(d3[0], d3[1]);
 }
 
-// Sum the partial Gram tiles of all point splits exactly and add them, unscaled, into G
-// (Np x Np).  Each partial is an int64 below 2^62; the sum is carried as 32-bit halves
-// (sum of p >> 32 and of p & (2^32 - 1), neither can overflow for fewer than 2^31
-// splits), so it is the exact integer whatever the splits, and it is rounded to FP64
-// once: (hi 2^32 exactly) + lo.  The Gram of a chunk therefore does not depend on the
-// points per CTA.  Tiles inside a 128-row block already hold both (a,b) and (b,a); the
-// others are mirrored.
-__global__ void gram_reduce_kernel(const long long *__restrict__ part, int ntiles, int nsplit, int ntj, int Np,
-                                   const float *__restrict__ scale, const double *__restrict__ vmax_p, int N,
-                                   double *__restrict__ G) {
+// The Gram tiles' exact sums (high and low 64-bit halves accumulated by the Gram kernel's
+// CTAs, whatever the points per CTA) rounded to FP64 once, (hi 2^32 exactly) + lo after
+// normalising lo to [0, 2^32), and added, unscaled, into G (Np x Np).  Tiles inside a
+// 128-row block already hold both (a,b) and (b,a); the others are mirrored.
+__global__ void gram_finish_tiles_kernel(const unsigned long long *__restrict__ th,
+                                         const unsigned long long *__restrict__ tl, int ntj, int Np,
+                                         const float *__restrict__ scale, const double *__restrict__ vmax_p, int N,
+                                         double *__restrict__ G) {
     const float vscale = vscale_of(*vmax_p);
     const int tile = blockIdx.y;
     int ti, tj;
@@ -944,27 +949,9 @@ __global__ void gram_reduce_kernel(const long long *__restrict__ part, int ntile
     const int c = e / kBM, r = e - c * kBM;
     const int a = ti * kBM + r, b = tj * kGN + c;
     if (a >= Np || b >= Np) return;
-    long long hi = 0, lo = 0;
-    // eight loads in flight at a time
-    const long long *src = part + (size_t)tile * (kBM * kGN) + e;
-    const size_t step = (size_t)ntiles * (kBM * kGN);
-    int k = 0;
-    for (; k + 8 <= nsplit; k += 8) {
-        long long v[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = src[(size_t)(k + u) * step];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            hi += v[u] >> 32;
-            lo += v[u] & 0xffffffffLL;
-        }
-    }
-    for (; k < nsplit; ++k) {
-        const long long v = src[(size_t)k * step];
-        hi += v >> 32;
-        lo += v & 0xffffffffLL;
-    }
-    hi += lo >> 32;  // normalise: lo in [0, 2^32), |hi| < 2^53 (the total is below 2^85)
+    const size_t k = (size_t)tile * (kBM * kGN) + e;
+    long long hi = (long long)th[k], lo = (long long)tl[k];
+    hi += lo >> 32;  // lo in [0, 2^32), |hi| < 2^53 (the total is below 2^85)
     lo &= 0xffffffffLL;
     double s = (double)hi * 4294967296.0 + (double)lo;
     const double sa = (a < N) ? (double)scale[a] : (double)vscale;
@@ -1220,11 +1207,13 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
                 rowsum);
             RP_LAUNCH_CHECK();
         }
-        // 3. exact Gram partial tiles over point splits, then their exact sum, rounded once
+        // 3. exact Gram tiles (CTAs over point splits add exactly into the tiles' 64-bit
+        //    totals), then the totals rounded once into G
         {
             const int kb_total = (int)(rows_kpad / kBK);
             const int nsplit = (kb_total + kb_split - 1) / kb_split;
-            long long *part = ctx->buf_t<long long>("m_part" + slot, (size_t)nsplit * ntri * kBM * kGN);
+            unsigned long long *tsum = ctx->buf_t<unsigned long long>("m_tsum" + slot, 2 * (size_t)ntri * kBM * kGN);
+            RP_CUDA(cudaMemsetAsync(tsum, 0, sizeof(unsigned long long) * 2 * (size_t)ntri * kBM * kGN, stream));
             GramArgs g{};
             g.nt = nt;
             g.ntj = ntj;
@@ -1232,7 +1221,8 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
             g.kb_total = kb_total;
             g.kb_per_split = kb_split;
             g.flush = kGramFlush;
-            g.out = part;
+            g.out_hi = tsum;
+            g.out_lo = tsum + (size_t)ntri * kBM * kGN;
             g.status = d_status;
             g.budget = ctx->wait_budget;
             const __half *Xq[kGSlices] = {X[0], X[1], X[2], X[3]};
@@ -1240,9 +1230,9 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
                 StageTimer tt(ctx, "gram_exact", stream);
                 launch_gram(Xq, Np, rows_kpad, g, ntri * nsplit, stream);
             }
-            StageTimer tr(ctx, "gram_reduce_fp64", stream);
-            gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256, 0, stream>>>(part, ntri, nsplit, ntj, Np,
-                                                                                         scale, vmax, N, G);
+            StageTimer tr(ctx, "gram_totals", stream);
+            gram_finish_tiles_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256, 0, stream>>>(
+                g.out_hi, g.out_lo, ntj, Np, scale, vmax, N, G);
             RP_LAUNCH_CHECK();
             rowsum_flush_kernel<<<ceil_div(Np, 128), 128, 0, stream>>>(rowsum, scale, vmax, N, sums);
             RP_LAUNCH_CHECK();
@@ -1356,12 +1346,14 @@ extern "C" int rp_debug_gram_slices(rp_ctx *ctx, const void *X0, const void *X1,
         for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
         const int kb_total = (int)(cols / kBK);
         const int nsplit = (kb_total + kb_split - 1) / kb_split;
-        long long *part = ctx->buf_t<long long>("dbg_part", (size_t)nsplit * ntri * kBM * kGN);
+        unsigned long long *tsum = ctx->buf_t<unsigned long long>("dbg_tsum", 2 * (size_t)ntri * kBM * kGN);
+        RP_CUDA(cudaMemset(tsum, 0, sizeof(unsigned long long) * 2 * (size_t)ntri * kBM * kGN));
         RP_CUDA(cudaMemset(ctx->d_status, 0, sizeof(int)));
         GramArgs g{};
         g.nt = nt; g.ntj = ntj; g.ntri = ntri; g.kb_total = kb_total; g.kb_per_split = kb_split;
         g.flush = std::min(std::max(flush, 1), kGramFlush);
-        g.out = part; g.status = ctx->d_status; g.budget = ctx->wait_budget;
+        g.out_hi = tsum; g.out_lo = tsum + (size_t)ntri * kBM * kGN;
+        g.status = ctx->d_status; g.budget = ctx->wait_budget;
         const __half *Xq[kGSlices] = {(const __half *)X0, (const __half *)X1, (const __half *)X2, (const __half *)X3};
         launch_gram(Xq, Np, cols, g, ntri * nsplit, 0);
         float *ones = ctx->buf_t<float>("dbg_ones", Np);
@@ -1370,7 +1362,8 @@ extern "C" int rp_debug_gram_slices(rp_ctx *ctx, const void *X0, const void *X1,
         RP_CUDA(cudaMemset(I_dev, 0, sizeof(double) * Np * Np));
         double *vmax = ctx->buf_t<double>("dbg_vmax", 1);  // unused: every row is an atom row (N = Np)
         RP_CUDA(cudaMemset(vmax, 0, sizeof(double)));
-        gram_reduce_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256>>>(part, ntri, nsplit, ntj, Np, ones, vmax, Np, I_dev);
+        gram_finish_tiles_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256>>>(g.out_hi, g.out_lo, ntj, Np, ones,
+                                                                               vmax, Np, I_dev);
         RP_LAUNCH_CHECK();
         RP_CUDA(cudaDeviceSynchronize());
         int st = 0;

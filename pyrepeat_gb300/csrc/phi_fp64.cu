@@ -19,31 +19,115 @@
 namespace rp {
 namespace {
 
-__global__ void realspace_fp64_kernel(const int32_t *__restrict__ kept, long long m0, long long rows,
-                                      const double *__restrict__ axis, int nx, int ny,
-                                      const double *__restrict__ atoms, int N, const double *__restrict__ shifts,
-                                      int S, int zero_idx, double rc, double sa, double *__restrict__ phi) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= rows * N) return;
-    long long m = t / N;
-    int a = (int)(t - m * N);
-    int f = kept[m0 + m];
-    int layer = nx * ny;
-    int l = f / layer, rem = f - l * layer, j = rem / nx, i = rem - j * nx;
+// Real-space sum in FP64 (repeat.py:944-966) over tiles of kRsPts kept points x kRsAtoms
+// atoms.  For each chunk of up to kRsShiftChunk shifts, the CTA first drops, per atom,
+// every shift whose image lies farther than Rc + 1e-3 Bohr from the bounding box of its
+// points (an FP32 test: FP32 rounding of the coordinates moves a distance by < 1e-4
+// Bohr here, so no image within Rc is dropped); each thread then tests the remaining
+// images of each atom against its point in FP32 with the same margin and evaluates the
+// survivors in FP64 with the reference's expressions.  Every image within Rc is summed,
+// in shift order, exactly as by a loop over all shifts, while the FP64 pipe (a small
+// fraction of the FP32 rate on this part) only sees the few images near each point.
+// The sums are accumulated in a shared-memory tile and added into phi[m][a] (row-major,
+// ld N) with coalesced stores.
+constexpr int kRsPts = 128;
+constexpr int kRsAtoms = 16;
+constexpr int kRsShiftChunk = 128;
+__global__ void __launch_bounds__(kRsPts) realspace_fp64_kernel(
+    const int32_t *__restrict__ kept, long long m0, long long rows, const double *__restrict__ axis, int nx, int ny,
+    const double *__restrict__ atoms, int N, const double *__restrict__ shifts, int S, int zero_idx, double rc,
+    double sa, double *__restrict__ phi) {
+    extern __shared__ float4 rs_cand[];  // [kRsAtoms][kRsShiftChunk] image (x, y, z) in FP32, shift index
+    __shared__ double tile[kRsAtoms][kRsPts + 1];
+    __shared__ int ncand[kRsAtoms];
+    __shared__ float bb[2][3][kRsPts / 32];
+    const long long mb = (long long)blockIdx.x * kRsPts;
+    const int a0 = blockIdx.y * kRsAtoms, na = min(kRsAtoms, N - a0);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long m = mb + threadIdx.x;
+    const bool valid = m < rows;
+    const int f = kept[m0 + (valid ? m : mb)];  // a lane past the end repeats the tile's first point
+    const int layer = nx * ny;
+    const int l = f / layer, rem = f - l * layer, j = rem / nx, i = rem - j * nx;
     double g[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) g[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)l * axis[6 + d];
-    double acc = 0.0;
-    for (int s = 0; s < S; ++s) {
-        double ex = g[0] - (atoms[3 * a] + shifts[3 * s]);
-        double ey = g[1] - (atoms[3 * a + 1] + shifts[3 * s + 1]);
-        double ez = g[2] - (atoms[3 * a + 2] + shifts[3 * s + 2]);
-        double r = sqrt(ex * ex + ey * ey + ez * ez);
-        if (!(r <= rc)) continue;
-        if (s == zero_idx && !(r > 1e-10)) continue;
-        acc += erfc(sa * r) / r;
+    const float gf[3] = {(float)g[0], (float)g[1], (float)g[2]};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float mn = gf[d], mx = gf[d];
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        }
+        if (lane == 0) {
+            bb[0][d][warp] = mn;
+            bb[1][d][warp] = mx;
+        }
     }
-    phi[t] += acc;
+    for (int a = 0; a < kRsAtoms; ++a) tile[a][threadIdx.x] = 0.0;
+    __syncthreads();
+    float bmin[3], bmax[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        bmin[d] = bb[0][d][0];
+        bmax[d] = bb[1][d][0];
+        for (int w = 1; w < kRsPts / 32; ++w) {
+            bmin[d] = fminf(bmin[d], bb[0][d][w]);
+            bmax[d] = fmaxf(bmax[d], bb[1][d][w]);
+        }
+    }
+    const float reach = (float)rc + 1e-3f, reach2 = reach * reach;
+    for (int s_lo = 0; s_lo < S; s_lo += kRsShiftChunk) {
+        const int s_hi = min(S, s_lo + kRsShiftChunk);
+        for (int a = warp; a < na; a += kRsPts / 32) {
+            int base = 0;
+            const double *pa = atoms + 3 * (size_t)(a0 + a);
+            for (int s0 = s_lo; s0 < s_hi; s0 += 32) {
+                const int s = s0 + lane;
+                bool keep = false;
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (s < s_hi) {
+                    q = make_float4((float)(pa[0] + shifts[3 * s]), (float)(pa[1] + shifts[3 * s + 1]),
+                                    (float)(pa[2] + shifts[3 * s + 2]), __int_as_float(s));
+                    const float dx = fmaxf(fmaxf(bmin[0] - q.x, q.x - bmax[0]), 0.f);
+                    const float dy = fmaxf(fmaxf(bmin[1] - q.y, q.y - bmax[1]), 0.f);
+                    const float dz = fmaxf(fmaxf(bmin[2] - q.z, q.z - bmax[2]), 0.f);
+                    keep = dx * dx + dy * dy + dz * dz <= reach2;
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                if (keep) rs_cand[a * kRsShiftChunk + base + __popc(bal & ((1u << lane) - 1u))] = q;
+                base += __popc(bal);
+            }
+            if (lane == 0) ncand[a] = base;
+        }
+        __syncthreads();
+        for (int a = 0; a < na; ++a) {
+            const double *pa = atoms + 3 * (size_t)(a0 + a);
+            double acc = tile[a][threadIdx.x];
+            const int nc = ncand[a];
+            for (int c = 0; c < nc; ++c) {
+                const float4 h = rs_cand[a * kRsShiftChunk + c];
+                const float fx = gf[0] - h.x, fy = gf[1] - h.y, fz = gf[2] - h.z;
+                if (fx * fx + fy * fy + fz * fz > reach2) continue;
+                const int s = __float_as_int(h.w);
+                const double ex = g[0] - (pa[0] + shifts[3 * s]);
+                const double ey = g[1] - (pa[1] + shifts[3 * s + 1]);
+                const double ez = g[2] - (pa[2] + shifts[3 * s + 2]);
+                const double r = sqrt(ex * ex + ey * ey + ez * ez);
+                if (!(r <= rc)) continue;
+                if (s == zero_idx && !(r > 1e-10)) continue;
+                acc += erfc(sa * r) / r;
+            }
+            tile[a][threadIdx.x] = acc;
+        }
+        __syncthreads();
+    }
+    // tile[a][t] -> phi[(mb + t) * N + a0 + a]: kRsAtoms consecutive doubles per point
+    for (int e = threadIdx.x; e < kRsPts * kRsAtoms; e += kRsPts) {
+        const int t = e / kRsAtoms, a = e - t * kRsAtoms;
+        if (mb + t < rows && a < na) phi[(mb + t) * N + a0 + a] += tile[a][t];
+    }
 }
 
 // Column sums of a row-major rows x cols block (ld), FP64, deterministic:
@@ -90,6 +174,14 @@ __global__ void finish_kernel(const double *__restrict__ G, const double *__rest
         A[t] = G[t] - s[i] * s[j] * invM;
     }
     if (t < N) b[t] = r[t] - s[t] * (*sumV) * invM;
+}
+
+// G (N x N, column-major) holds its upper triangle (row <= column): copy it to the lower
+__global__ void mirror_upper_kernel(double *__restrict__ G, int N) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)N * N) return;
+    const int c = (int)(t / N), r = (int)(t - (long long)c * N);
+    if (r > c) G[t] = G[(size_t)r * N + c];
 }
 
 __global__ void shifted_sums_kernel(const double *__restrict__ sphi, const double *__restrict__ c, long long M,
@@ -174,10 +266,15 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
             RP_CUDA(cudaMemsetAsync(P, 0, sizeof(double) * (size_t)rows * N, stream));
         }
         StageTimer t_r(ctx, "fp64_realspace", stream);
-        realspace_fp64_kernel<<<ceil_div(rows * N, 128), 128, 0, stream>>>(
-            kept_idx_dev, m0, rows, d_axis, ew->grid.n_grid[0], ew->grid.n_grid[1], d_atoms, N, d_shifts, S,
-            zero_idx, ew->cutoff, ew->sqrt_alpha, P);
-        RP_LAUNCH_CHECK();
+        {
+            const size_t smem = sizeof(float4) * kRsAtoms * kRsShiftChunk;  // 32 KB of candidates
+            // with the 16.5 KB static tile the block passes the 48 KB default: opt in
+            smem_optin((const void *)realspace_fp64_kernel, 64 * 1024);
+            realspace_fp64_kernel<<<dim3(ceil_div(rows, kRsPts), ceil_div(N, kRsAtoms)), kRsPts, smem, stream>>>(
+                kept_idx_dev, m0, rows, d_axis, ew->grid.n_grid[0], ew->grid.n_grid[1], d_atoms, N, d_shifts, S,
+                zero_idx, ew->cutoff, ew->sqrt_alpha, P);
+            RP_LAUNCH_CHECK();
+        }
         column_sums_fp64(P, rows, N, N, csum, false, ctx, stream);
         // sphi += csum (accumulating stage-2 output keeps the order fixed)
         {
@@ -190,11 +287,14 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
         }
         shift_columns_kernel<<<ceil_div(rows * N, 256), 256, 0, stream>>>(P, rows, N, c);
         RP_LAUNCH_CHECK();
-        // column-major view: X = P^T is N x rows with ld N;  G += X X^T,  r += X Vc
-        StageTimer t_g(ctx, "fp64_gram_dgemm", stream);
-        RP_CUBLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_T, N, N, (int)rows, &one, P, N, P, N, &one, G, N));
+        // column-major view: X = P^T is N x rows with ld N;  G += X X^T (one triangle,
+        // mirrored after the last chunk),  r += X Vc
+        StageTimer t_g(ctx, "fp64_gram_dsyrk", stream);
+        RP_CUBLAS(cublasDsyrk(h, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, N, (int)rows, &one, P, N, &one, G, N));
         RP_CUBLAS(cublasDgemv(h, CUBLAS_OP_N, N, (int)rows, &one, P, N, Vc_dev + m0, 1, &one, r, 1));
     }
+    mirror_upper_kernel<<<ceil_div((long long)N * N, 256), 256, 0, stream>>>(G, N);
+    RP_LAUNCH_CHECK();
     column_sums_fp64(Vc_dev, M, 1, 1, sumV, false, ctx, stream);
     shifted_sums_kernel<<<ceil_div(N, 128), 128, 0, stream>>>(sphi, c, M, N, s_c);
     RP_LAUNCH_CHECK();

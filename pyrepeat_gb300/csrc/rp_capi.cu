@@ -260,6 +260,7 @@ struct BatchRun {
 // copied to pinned memory behind them and r.done is recorded.  Runs in slot ctx->cur_slot.
 void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *const *V_dev, double *q_out,
                    int64_t *M_out, double *info_out, cudaStream_t stream, BatchRun &r) {
+    ctx->trace_mark("enqueue");
     r.slot = ctx->cur_slot;
     r.prio = ctx->cur_prio;
     r.n = n;
@@ -316,9 +317,12 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
     int *clamps = r.clamps = ctx->buf_t<int>("fit_clamps", (size_t)n);
     rp::status_clear(ctx, stream);
     RP_CUDA(cudaMemsetAsync(clamps, 0, sizeof(int) * n, stream));
-    auto record = [&](cudaStream_t st) {
+    // events the host waits on (kept counts, the batch's end) block the waiting thread
+    // instead of spinning, so a waiting host thread leaves its core to the other host work
+    // of the process (the next batch's planning, the caller's threads)
+    auto record = [&](cudaStream_t st, bool host_waits = false) {
         cudaEvent_t ev;
-        RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        RP_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming | (host_waits ? cudaEventBlockingSync : 0)));
         r.events.push_back(ev);
         RP_CUDA(cudaEventRecord(ev, st));
         return ev;
@@ -346,6 +350,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
             const rp_fit_desc &d = descs[i0 + t];
             rp::filter_plan(&d.grid, d.atoms, d.Z, d.N, d.vdw_factor, d.vdw_max, plan(i0 + t));
         });
+        ctx->trace_mark("planned group " + std::to_string(g));
         pl_off[i0] = 0;
         for (int i = i0; i < i1; ++i) pl_off[i + 1] = pl_off[i] + plan(i).bytes();
         const std::string gtag = "fit_filter#" + std::to_string(g);
@@ -376,7 +381,8 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
         rp::filter_group(ctx, items, flane(g), "#fg" + std::to_string(g));
         for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(stream, record(flane(ln)), 0));
         RP_CUDA(cudaMemcpyAsync(Mh + i0, Md + i0, sizeof(long long) * (i1 - i0), cudaMemcpyDeviceToHost, stream));
-        kept_ready[g] = record(stream);
+        kept_ready[g] = record(stream, true);
+        ctx->trace_mark("filters queued group " + std::to_string(g));
     }
     // 2. Ewald tables, written by the host workers straight into one pinned arena,
     //    uploaded with a single copy on a stream of its own
@@ -401,6 +407,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
                   reinterpret_cast<double *>(ew_host + at_off) + 3 * off_n[i]);
     });
     for (int i = 0; i < n; ++i) rp::ewald_place(r.ews[i], ew_dev + ew_off[i]);
+    ctx->trace_mark("tables built");
     // the tables go up on the reciprocal rows' stream, beside the grids still queued on the
     // copy stream (with grids from host memory those are most of the batch's bytes)
     const cudaStream_t recip_lane = ctx->timing ? ctx->lane(0) : ctx->lane(kLaneRecip);
@@ -448,6 +455,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
     r.gpend.assign((size_t)ngroups, SolvePending{});
     for (int g = 0; g < ngroups; ++g) {
         RP_CUDA(cudaEventSynchronize(kept_ready[g]));
+        ctx->trace_mark("kept counts group " + std::to_string(g));
         for (int i = g0[g]; i < g0[g + 1]; ++i) {
             r.M[i] = Mh[i];
             if (M_out) M_out[i] = r.M[i];
@@ -482,7 +490,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
     RP_CUDA(cudaMemcpyAsync(r.hclamps, clamps, sizeof(int) * n, cudaMemcpyDeviceToHost, stream));
     r.hq = static_cast<double *>(ctx->host_buf("fit_qh", sizeof(double) * off_n[n]));
     RP_CUDA(cudaMemcpyAsync(r.hq, r.q, sizeof(double) * off_n[n], cudaMemcpyDeviceToHost, stream));
-    r.done = record(stream);
+    r.done = record(stream, true);
 }
 
 // Completion phase (throws rp::Error): waits for r.done, refits cubes whose values clamped
@@ -492,7 +500,9 @@ void batch_complete(rp_ctx *ctx, BatchRun &r) {
     const int n = r.n;
     if (n == 0) return;
     const cudaStream_t stream = r.stream;
+    ctx->trace_mark("complete");
     RP_CUDA(cudaEventSynchronize(r.done));
+    ctx->trace_mark("device done");
     bool changed = false;
     for (SolvePending &pd : r.gpend)  // wide systems whose FP32 refinement stalled: FP64 factors
         if (pd.any_wide) {
@@ -568,6 +578,7 @@ void batch_complete(rp_ctx *ctx, BatchRun &r) {
     }
     std::copy(r.hq, r.hq + r.off_n[n], r.q_out);
     if (r.info_out) std::copy(info.begin(), info.end(), r.info_out);
+    ctx->trace_mark("charges out");
     for (int i = 0; i < n; ++i)
         if (info[(size_t)W * i + 3] != 0.0)
             rp::fail(RP_E_SINGULAR, "rp_fit: bordered system of cube " + std::to_string(i) + " is singular");
@@ -906,6 +917,30 @@ int rp_load_tiles(rp_ctx *ctx, const char *cache_path) {
         }
         std::fclose(f);
     });
+}
+
+// Diagnostics (not part of the public ABI): host timeline of the batched fit.  on != 0
+// starts recording (and clears the log), 0 stops; rp_debug_trace_read writes the log as
+// "label<TAB>milliseconds since the first mark" lines into buf (cap bytes, NUL-terminated).
+extern "C" int rp_debug_trace(rp_ctx *ctx, int on) {
+    if (!ctx) return RP_E_ARG;
+    std::lock_guard<std::mutex> lk(ctx->trace_mu);
+    ctx->trace = on != 0;
+    if (on) ctx->trace_log.clear();
+    return RP_OK;
+}
+extern "C" int rp_debug_trace_read(rp_ctx *ctx, char *buf, size_t cap) {
+    if (!ctx || !buf || cap == 0) return RP_E_ARG;
+    std::lock_guard<std::mutex> lk(ctx->trace_mu);
+    std::string out;
+    const double t0 = ctx->trace_log.empty() ? 0.0 : ctx->trace_log.front().second;
+    char line[160];
+    for (const auto &e : ctx->trace_log) {
+        std::snprintf(line, sizeof(line), "%s\t%.3f\n", e.first.c_str(), e.second - t0);
+        out += line;
+    }
+    std::snprintf(buf, cap, "%s", out.c_str());
+    return RP_OK;
 }
 
 int rp_set_kappa_limit(rp_ctx *ctx, double kappa_max) {

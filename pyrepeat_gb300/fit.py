@@ -8,6 +8,7 @@ memory through the C ABI's ``rp_fit``.
 from __future__ import annotations
 
 import ctypes
+import itertools
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -36,21 +37,25 @@ class FitResult:
 def constraint_arrays(Z, symm_groups=None, resp=None):
     """CSR symmetry groups (0-based, base first) and per-atom RESP arrays."""
     N = len(Z)
-    groups = [list(g) for g in (symm_groups or []) if len(g) >= 1]
+    groups = [g for g in (symm_groups or []) if len(g) >= 1]
     ptr = np.zeros(len(groups) + 1, dtype=np.int32)
-    idx = []
-    for i, g in enumerate(groups):
-        idx.extend(int(x) for x in g)
-        ptr[i + 1] = len(idx)
-    idx = np.asarray(idx if idx else [0], dtype=np.int32)
+    if groups:
+        np.cumsum(np.fromiter(map(len, groups), dtype=np.int32, count=len(groups)), out=ptr[1:])
+        idx = np.fromiter(itertools.chain.from_iterable(groups), dtype=np.int32, count=int(ptr[-1]))
+    else:
+        idx = np.zeros(1, dtype=np.int32)
     rs = rt = None
     if resp:
-        rs = np.zeros(N); rt = np.zeros(N)
-        for i, z in enumerate(Z):
-            sym = z_to_symbol(int(z))
-            if sym in resp:
-                s, t = resp[sym]
-                rs[i], rt[i] = float(s), float(t)
+        # per element (Z) values, then gathered per atom
+        zs = np.asarray(Z, dtype=np.int64)
+        uz = np.unique(zs)
+        ts = np.zeros(int(uz.max()) + 1 if len(uz) else 1)
+        tt = np.zeros_like(ts)
+        for z in uz:
+            st = resp.get(z_to_symbol(int(z)))
+            if st:
+                ts[z], tt[z] = float(st[0]), float(st[1])
+        rs, rt = ts[zs], tt[zs]
     return len(groups), ptr, idx, rs, rt
 
 
@@ -218,9 +223,11 @@ class Context:
             res.A, res.b = A, b
         return res
 
-    def _desc(self, cube, precision, keep):
-        """rp_fit_desc for a cube; arrays it points to are appended to `keep`."""
-        d = _lib.RpFitDesc()
+    def _desc(self, cube, precision, keep, d=None):
+        """rp_fit_desc for a cube (filled into `d` when given); arrays it points to are
+        appended to `keep`."""
+        if d is None:
+            d = _lib.RpFitDesc()
         d.grid = _lib.make_grid(cube.n_grid, cube.axis_vector)
         atoms = np.ascontiguousarray(cube.atom_pos, dtype=np.float64)
         Z = np.ascontiguousarray(cube.atom_index, dtype=np.int32)
@@ -255,7 +262,7 @@ class Context:
         keep = []
         arr = (_lib.RpFitDesc * n)()
         for i, c in enumerate(cubes):
-            arr[i] = self._desc(c, precision[i] if isinstance(precision, (list, tuple)) else precision, keep)
+            self._desc(c, precision[i] if isinstance(precision, (list, tuple)) else precision, keep, arr[i])
         vptr = None
         if V_dev is not None:
             vptr = (ctypes.c_void_p * n)(*[v.data_ptr() if v is not None else None for v in V_dev])

@@ -12,8 +12,11 @@ with silently wrong charges.  Parity bars:
   mixed path (measured 2.3e-5 and 1.8e-5).
 * cfg3 cell (triclinic 40 x 42 x 45 Bohr, 85/95/100 deg, symmetry + RESP): the
   mixed path against the FP64 path, 1e-5 e with 500 atoms, and at the full 2000
-  atoms / 9.45 M points (kappa/(n+1) ~ 1e9: escalated; the two FP64 sums visit the
-  points in different orders, measured 1.8e-5) 5e-5 e.
+  atoms / 9.45 M points 1e-4 e: kappa ~ 2e12 (kappa/(n+1) ~ 1e9) escalates the mixed
+  fit, and the two FP64 fits then differ only in the order of their sums (kept points
+  in brick and in flat order), which moves charges of RMS 6.3 e by 1.7e-5 to 4.9e-5 e
+  (measured with a DGEMM and with a DSYRK Gram); unescalated the mixed fit is 9.9e-2
+  away.
 * well-conditioned cubes are not escalated (the mixed path's speed is kept).
 """
 import ctypes
@@ -161,10 +164,10 @@ def test_tric_cell_500_atoms_mixed_matches_fp64(gpu_ctx):
 def test_tric_full_size_mixed_against_fp64(gpu_ctx):
     """cfg3 at full size (2000 atoms, 200 x 210 x 225 grid, 150 groups, RESP): kappa/(n+1)
     ~ 1e9 sends the mixed fit to FP64; it agrees with the plain FP64 fit to the FP64
-    spread of this system."""
+    spread of this system (the order of the sums; see the module docstring)."""
     from pyrepeat_gb300 import _lib
     cube = _tric_cell(gpu_ctx, 2000, 150, (200, 210, 225), 1000)
     q64, M, i64 = _batch(gpu_ctx, cube, _lib.PREC_FP64)
     qm, _, im = _batch(gpu_ctx, cube, _lib.PREC_MIXED)
     assert im["escalated"]
-    assert np.abs(qm - q64).max() <= 5e-5
+    assert np.abs(qm - q64).max() <= 1e-4
