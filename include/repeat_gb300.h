@@ -38,7 +38,7 @@ extern "C" {
 #define RP_E_UNSUPPORTED -7
 
 /* Arithmetic of the Phi -> normal-equations stage. */
-#define RP_PREC_FP64 0  /* plain FP64: FP64 tables, FP64 real space, FP64 Gram (cuBLAS DGEMM) */
+#define RP_PREC_FP64 0  /* plain FP64: FP64 tables, FP64 real space, FP64 Gram (cuBLAS DGEMM / DSYRK) */
 #define RP_PREC_MIXED 1 /* FP32 real space from double-float coordinates, separable FP32 reciprocal
                            sum, exact fixed-point Gram on the tensor cores (tcgen05), FP64 solve.
                            In rp_fit / rp_fit_batch a cube whose kappa / (n+1) exceeds the ctx's

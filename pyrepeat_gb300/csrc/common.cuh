@@ -483,9 +483,16 @@ void filter_async(rp_ctx *ctx, const rp_grid *grid, const double *atoms, const i
                   double vdw_factor, double vdw_max, int32_t *kept_idx_dev, double *Vc_dev, long long *M_dev,
                   uint8_t *mask_dev, cudaStream_t stream, const std::string &tag, bool brick_order,
                   double *vstats_dev);
+// Exact Gram of a chunk of FP64 columns on the tensor cores (gram_mixed.cu): G (N x N) +=
+// Phi^T Phi and r (N) += Phi^T V for Phi rows x N (row-major, ld N) and V (rows).
+void gram_words_fp64(rp_ctx *ctx, const double *P, long long rows, int N, const double *V, double *G, double *r,
+                     cudaStream_t stream);
+// separable: the reciprocal sum by the FP64 separable transform and the Gram by
+// gram_words_fp64 (the escalated fit)
+// instead of the flat k-table DGEMM and DSYRK (the plain FP64 comparator)
 void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
-               cudaStream_t stream);
+               cudaStream_t stream, bool separable = false);
 // vstats_dev: the filter's (sum, max |.|) of Vc (only the max is used), or nullptr to
 // compute the max here.  rn (host, N) and clamp_dev (one device counter): the atoms'
 // scaled vdW radii, which bound |Phi| a priori, so Phi goes straight to fixed-point
@@ -516,7 +523,10 @@ struct SolveJob {
     double qtot;
     double *q;
 };
-void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream);
+// fp64_first: wide systems (known ill-conditioned, e.g. an escalated fit) are factored in
+// FP64 at once instead of after a stalled FP32 attempt
+void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream,
+                 bool fp64_first = false);
 // One bordered system of the solve kernel (device-side descriptor).
 struct SolveDesc {
     const double *A;      // N x N input
@@ -557,7 +567,7 @@ struct SolvePending {
 // are final after it); without, the call waits for them.  (Systems with overlapping symmetry
 // groups are folded on the host, which waits.)
 const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, cudaStream_t stream,
-                                const std::string &tag, SolvePending *pend = nullptr);
+                                const std::string &tag, SolvePending *pend = nullptr, bool fp64_first = false);
 void solve_wide_fp64(rp_ctx *ctx, SolvePending &pd, cudaStream_t stream);  // synchronises stream
 
 // Device table builders (ewald_tables.cu).

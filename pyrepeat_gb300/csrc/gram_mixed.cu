@@ -1243,6 +1243,143 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     RP_LAUNCH_CHECK();
 }
 
+// ---------------------------------------------------------------- exact Gram of FP64 columns
+// For the escalated (FP64) fit: the columns of a chunk of Phi (rows x N, row-major, ld N,
+// centred) and the centred ESP are scaled by powers of two to |x| < 1/2 and cut into two
+// 28-bit words, x = 2^-27 (I1 + 2^-27 I2) + O(2^-55); the 2(N+1) rows [I1 of every column;
+// I2 of every column] go through the exact digit Gram (every digit product exact, tile
+// totals exact, one FP64 rounding), and
+//   G[a][b] += (G11 + 2^-27 (G12 + G21) + 2^-54 G22)[a][b] / (s_a s_b)
+// with the ESP as column N (G[a][N] = (Phi^T V)[a]).  An FP64-accurate Gram from the
+// tensor cores: 4x the work of the mixed path's Gram, instead of DSYRK at the FP64 rate.
+namespace {
+
+// max |x| of each column (N of Phi, then the ESP as column N), as order-preserving bits
+__global__ void colmax_fp64_kernel(const double *__restrict__ P, long long rows, int N, const double *__restrict__ V,
+                                   unsigned long long *__restrict__ mx) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > N) return;
+    const long long r0 = (long long)blockIdx.y * 256, r1 = min(rows, r0 + 256);
+    double m = 0.0;
+    for (long long r = r0; r < r1; ++r) m = fmax(m, fabs(c < N ? P[r * N + c] : V[r]));
+    atomicMax(mx + c, (unsigned long long)__double_as_longlong(m));  // m >= 0: bits order like values
+}
+
+__device__ __forceinline__ double pow2_scale(unsigned long long mbits) {
+    const double m = __longlong_as_double((long long)mbits);
+    int e = 0;
+    if (m > 0.0) frexp(m, &e);  // m in [2^(e-1), 2^e): m 2^(-e-1) < 1/2
+    return ldexp(1.0, -e - 1);
+}
+
+// two 28-bit words of each value, as four 7-bit digits each: column c < N and the ESP
+// (c = N) to rows c and c + N + 1 of the slices; a 32 x 32 tile per CTA through shared
+// memory, so both the reads of Phi and the writes of the slices coalesce
+__global__ void split_words_kernel(const double *__restrict__ P, long long rows, long long cols_pad, int N,
+                                   const double *__restrict__ V, const unsigned long long *__restrict__ mx,
+                                   __half *__restrict__ X0, __half *__restrict__ X1, __half *__restrict__ X2,
+                                   __half *__restrict__ X3) {
+    __shared__ double t[32][33];
+    const long long m0 = (long long)blockIdx.x * 32;
+    const int c0 = blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {  // t[point][column]
+        const long long m = m0 + k;
+        const int c = c0 + threadIdx.x;
+        double v = 0.0;
+        if (m < rows && c <= N) v = c < N ? P[m * N + c] : V[m];
+        t[k][threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += blockDim.y) {  // column c0 + k, point m0 + x
+        const int c = c0 + k;
+        const long long m = m0 + threadIdx.x;
+        if (c > N || m >= cols_pad) continue;
+        const double x = t[threadIdx.x][k] * pow2_scale(mx[c]) * 134217728.0;  // |x| < 2^26
+        const double i1 = rint(x);
+        const double i2 = rint((x - i1) * 134217728.0);                          // |x - i1| <= 1/2
+        digits4((int)i1, X0, X1, X2, X3, (long long)c * cols_pad + m);
+        digits4((int)i2, X0, X1, X2, X3, (long long)(c + N + 1) * cols_pad + m);
+    }
+}
+
+// G2 (2(N+1) square, row-major) = 2^-54 x the exact tile totals: Gram of the word rows
+__global__ void words_gram_kernel(const unsigned long long *__restrict__ th, const unsigned long long *__restrict__ tl,
+                                  int ntj, int Np2, double *__restrict__ G2) {
+    const int tile = blockIdx.y;
+    int ti, tj;
+    gram_tile_decode(tile, ntj, ti, tj);
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= kBM * kGN) return;
+    const int c = e / kBM, r = e - c * kBM;
+    const int a = ti * kBM + r, b = tj * kGN + c;
+    if (a >= Np2 || b >= Np2) return;
+    const size_t k = (size_t)tile * (kBM * kGN) + e;
+    long long hi = (long long)th[k], lo = (long long)tl[k];
+    hi += lo >> 32;
+    lo &= 0xffffffffLL;
+    const double s = ldexp((double)hi * 4294967296.0 + (double)lo, -54);
+    G2[(size_t)a * Np2 + b] = s;
+    G2[(size_t)b * Np2 + a] = s;
+}
+
+// G[a][b] (N x N, either order: symmetric) and r[a] (b = N) += the combined words / (s_a s_b)
+__global__ void combine_words_kernel(const double *__restrict__ G2, int N, const unsigned long long *__restrict__ mx,
+                                     double *__restrict__ G, double *__restrict__ r) {
+    const int Np = N + 1, Np2 = 2 * Np;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)N * Np) return;
+    const int a = (int)(t / Np), b = (int)(t - (long long)a * Np);
+    const double g11 = G2[(size_t)a * Np2 + b], g12 = G2[(size_t)a * Np2 + Np + b];
+    const double g21 = G2[(size_t)(Np + a) * Np2 + b], g22 = G2[(size_t)(Np + a) * Np2 + Np + b];
+    const double v = (g11 + 7.450580596923828125e-9 * (g12 + g21) + 5.5511151231257827e-17 * g22) /
+                     (pow2_scale(mx[a]) * pow2_scale(mx[b]));
+    if (b < N) G[(size_t)a * N + b] += v;
+    else r[a] += v;
+}
+
+}  // namespace
+
+void gram_words_fp64(rp_ctx *ctx, const double *P, long long rows, int N, const double *V, double *G, double *r,
+                     cudaStream_t stream) {
+    const int Np = N + 1, Np2 = 2 * Np;
+    const long long cols_pad = round_up(rows, kBK);
+    unsigned long long *mx = ctx->buf_t<unsigned long long>("w64_mx", (size_t)Np);
+    RP_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Np, stream));
+    colmax_fp64_kernel<<<dim3(ceil_div(Np, 256), ceil_div(rows, 256)), 256, 0, stream>>>(P, rows, N, V, mx);
+    RP_LAUNCH_CHECK();
+    __half *X[kGSlices];
+    for (int q = 0; q < kGSlices; ++q) X[q] = ctx->buf_t<__half>("w64_X" + std::to_string(q), (size_t)Np2 * cols_pad);
+    split_words_kernel<<<dim3(ceil_div(cols_pad, 32), ceil_div(Np, 32)), dim3(32, 8), 0, stream>>>(
+        P, rows, cols_pad, N, V, mx, X[0], X[1], X[2], X[3]);
+    RP_LAUNCH_CHECK();
+    const int nt = (int)ceil_div(Np2, kBM), ntj = (int)ceil_div(Np2, kGN);
+    int ntri = 0;
+    for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
+    const int kb_total = (int)(cols_pad / kBK), nsplit = (kb_total + kGramSplit - 1) / kGramSplit;
+    unsigned long long *tsum = ctx->buf_t<unsigned long long>("w64_tsum", 2 * (size_t)ntri * kBM * kGN);
+    RP_CUDA(cudaMemsetAsync(tsum, 0, sizeof(unsigned long long) * 2 * (size_t)ntri * kBM * kGN, stream));
+    RP_CUDA(cudaMemsetAsync(ctx->status_words(), 0, sizeof(int), stream));
+    GramArgs g{};
+    g.nt = nt;
+    g.ntj = ntj;
+    g.ntri = ntri;
+    g.kb_total = kb_total;
+    g.kb_per_split = kGramSplit;
+    g.flush = kGramFlush;
+    g.out_hi = tsum;
+    g.out_lo = tsum + (size_t)ntri * kBM * kGN;
+    g.status = ctx->status_words();
+    g.budget = ctx->wait_budget;
+    const __half *Xq[kGSlices] = {X[0], X[1], X[2], X[3]};
+    launch_gram(Xq, Np2, cols_pad, g, ntri * nsplit, stream);
+    double *G2 = ctx->buf_t<double>("w64_G2", (size_t)Np2 * Np2);
+    words_gram_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256, 0, stream>>>(g.out_hi, g.out_lo, ntj, Np2, G2);
+    RP_LAUNCH_CHECK();
+    combine_words_kernel<<<ceil_div((long long)N * Np, 256), 256, 0, stream>>>(G2, N, mx, G, r);
+    RP_LAUNCH_CHECK();
+    status_check(ctx, stream);
+}
+
 }  // namespace rp
 
 // Diagnostics (not part of the public ABI): a factor on the single-pass Phi bounds of

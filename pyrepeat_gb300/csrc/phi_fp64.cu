@@ -23,23 +23,44 @@ namespace {
 // atoms.  For each chunk of up to kRsShiftChunk shifts, the CTA first drops, per atom,
 // every shift whose image lies farther than Rc + 1e-3 Bohr from the bounding box of its
 // points (an FP32 test: FP32 rounding of the coordinates moves a distance by < 1e-4
-// Bohr here, so no image within Rc is dropped); each thread then tests the remaining
-// images of each atom against its point in FP32 with the same margin and evaluates the
-// survivors in FP64 with the reference's expressions.  Every image within Rc is summed,
-// in shift order, exactly as by a loop over all shifts, while the FP64 pipe (a small
-// fraction of the FP32 rate on this part) only sees the few images near each point.
-// The sums are accumulated in a shared-memory tile and added into phi[m][a] (row-major,
-// ld N) with coalesced stores.
+// Bohr here, so no image within Rc is dropped).  Each thread then tests the remaining
+// images of each atom against its point in FP32 with the same margin.  QUEUE false: the
+// survivors are evaluated in place (the plain comparator's kept points, in grid order,
+// give tiles of nearby points that reach mostly the same images).  QUEUE true (the
+// escalated fit, whatever the order of its kept points): each thread queues its
+// survivors (atom, image) in order, the CTA
+// evaluates the queued pairs in FP64, every lane on one pair, so the FP64 pipe (a small
+// fraction of the FP32 rate on this part, and as slow for one active lane as for 32)
+// runs full warps instead of a warp per image that any of its points reaches, and each
+// thread adds its pairs' terms in queue order (a rejected pair adds +0.0, which changes
+// no sum).  Either way the FP64 expressions are the reference's.  Every image within Rc is therefore summed, in shift order, exactly as by a
+// loop over all shifts.  The sums are accumulated in a shared-memory tile and added into
+// phi[m][a] (row-major, ld N) with coalesced stores.
 constexpr int kRsPts = 128;
 constexpr int kRsAtoms = 16;
-constexpr int kRsShiftChunk = 128;
+constexpr int kRsQueue = 16;  // queued pairs per point per round
+// shifts per chunk: in place 128, queued 64 (its queue takes the rest of the shared memory)
+template <bool QUEUE> __host__ __device__ constexpr int rs_chunk() { return QUEUE ? 64 : 128; }
+size_t realspace_fp64_smem(bool queue) {
+    return queue ? sizeof(float4) * kRsAtoms * rs_chunk<true>() + sizeof(double) * kRsQueue * kRsPts +
+                       sizeof(unsigned short) * kRsQueue * kRsPts
+                 : sizeof(float4) * kRsAtoms * rs_chunk<false>();
+}
+template <bool QUEUE>
 __global__ void __launch_bounds__(kRsPts) realspace_fp64_kernel(
     const int32_t *__restrict__ kept, long long m0, long long rows, const double *__restrict__ axis, int nx, int ny,
     const double *__restrict__ atoms, int N, const double *__restrict__ shifts, int S, int zero_idx, double rc,
     double sa, double *__restrict__ phi) {
+    constexpr int kRsShiftChunk = rs_chunk<QUEUE>();
     extern __shared__ float4 rs_cand[];  // [kRsAtoms][kRsShiftChunk] image (x, y, z) in FP32, shift index
+    double *qterm = reinterpret_cast<double *>(rs_cand + kRsAtoms * kRsShiftChunk);      // [kRsQueue][kRsPts]
+    unsigned short *qitem = reinterpret_cast<unsigned short *>(qterm + kRsQueue * kRsPts);  // (atom << 7) | image
     __shared__ double tile[kRsAtoms][kRsPts + 1];
+    __shared__ double gs[3][kRsPts];
     __shared__ int ncand[kRsAtoms];
+    __shared__ int qoff[kRsPts + 1];
+    __shared__ int wsum[kRsPts / 32];
+    __shared__ int more;
     __shared__ float bb[2][3][kRsPts / 32];
     const long long mb = (long long)blockIdx.x * kRsPts;
     const int a0 = blockIdx.y * kRsAtoms, na = min(kRsAtoms, N - a0);
@@ -51,7 +72,10 @@ __global__ void __launch_bounds__(kRsPts) realspace_fp64_kernel(
     const int l = f / layer, rem = f - l * layer, j = rem / nx, i = rem - j * nx;
     double g[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) g[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)l * axis[6 + d];
+    for (int d = 0; d < 3; ++d) {
+        g[d] = ((double)i * axis[d] + (double)j * axis[3 + d]) + (double)l * axis[6 + d];
+        gs[d][threadIdx.x] = g[d];
+    }
     const float gf[3] = {(float)g[0], (float)g[1], (float)g[2]};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -102,26 +126,94 @@ __global__ void __launch_bounds__(kRsPts) realspace_fp64_kernel(
             if (lane == 0) ncand[a] = base;
         }
         __syncthreads();
-        for (int a = 0; a < na; ++a) {
-            const double *pa = atoms + 3 * (size_t)(a0 + a);
-            double acc = tile[a][threadIdx.x];
-            const int nc = ncand[a];
-            for (int c = 0; c < nc; ++c) {
-                const float4 h = rs_cand[a * kRsShiftChunk + c];
-                const float fx = gf[0] - h.x, fy = gf[1] - h.y, fz = gf[2] - h.z;
-                if (fx * fx + fy * fy + fz * fz > reach2) continue;
-                const int s = __float_as_int(h.w);
-                const double ex = g[0] - (pa[0] + shifts[3 * s]);
-                const double ey = g[1] - (pa[1] + shifts[3 * s + 1]);
-                const double ez = g[2] - (pa[2] + shifts[3 * s + 2]);
-                const double r = sqrt(ex * ex + ey * ey + ez * ez);
-                if (!(r <= rc)) continue;
-                if (s == zero_idx && !(r > 1e-10)) continue;
-                acc += erfc(sa * r) / r;
+        // Evaluated where they are found (QUEUE false), the pairs cost a warp-wide FP64 pass
+        // for every image that any lane of the warp reaches, which suits tiles whose points
+        // lie close together; queued, they cost their number plus the queue's bookkeeping.
+        {
+            if (!QUEUE) {  // evaluate in place, in order
+                for (int a = 0; a < na; ++a) {
+                    const double *pa = atoms + 3 * (size_t)(a0 + a);
+                    double acc = tile[a][threadIdx.x];
+                    for (int c = 0; c < ncand[a]; ++c) {
+                        const float4 h = rs_cand[a * kRsShiftChunk + c];
+                        const float fx = gf[0] - h.x, fy = gf[1] - h.y, fz = gf[2] - h.z;
+                        if (fx * fx + fy * fy + fz * fz > reach2) continue;
+                        const int s = __float_as_int(h.w);
+                        const double ex = g[0] - (pa[0] + shifts[3 * s]);
+                        const double ey = g[1] - (pa[1] + shifts[3 * s + 1]);
+                        const double ez = g[2] - (pa[2] + shifts[3 * s + 2]);
+                        const double r = sqrt(ex * ex + ey * ey + ez * ez);
+                        if (!(r <= rc)) continue;
+                        if (s == zero_idx && !(r > 1e-10)) continue;
+                        acc += erfc(sa * r) / r;
+                    }
+                    tile[a][threadIdx.x] = acc;
+                }
+                __syncthreads();
+                continue;
             }
-            tile[a][threadIdx.x] = acc;
         }
-        __syncthreads();
+        // rounds: queue up to kRsQueue pairs per point (resuming where the last round stopped),
+        // evaluate them with the whole CTA, add the terms in queue order
+        int ra = 0, rcnd = 0;  // this thread's resume point (atom, image)
+        for (;;) {
+            int cnt = 0;
+            while (ra < na && cnt < kRsQueue) {
+                const int nc = ncand[ra];
+                while (rcnd < nc && cnt < kRsQueue) {
+                    const float4 h = rs_cand[ra * kRsShiftChunk + rcnd];
+                    const float fx = gf[0] - h.x, fy = gf[1] - h.y, fz = gf[2] - h.z;
+                    if (fx * fx + fy * fy + fz * fz <= reach2)
+                        qitem[cnt++ * kRsPts + threadIdx.x] = (unsigned short)((ra << 7) | rcnd);
+                    ++rcnd;
+                }
+                if (rcnd >= nc) {
+                    ++ra;
+                    rcnd = 0;
+                }
+            }
+            // offsets of every thread's queue (block exclusive scan of cnt)
+            int incl = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            if (lane == 31) wsum[warp] = incl;
+            if (threadIdx.x == 0) more = 0;
+            __syncthreads();
+            int wbase = 0;
+            for (int w = 0; w < warp; ++w) wbase += wsum[w];
+            qoff[threadIdx.x] = wbase + incl - cnt;
+            if (threadIdx.x == kRsPts - 1) qoff[kRsPts] = wbase + incl;
+            if (ra < na) more = 1;
+            __syncthreads();
+            const int total = qoff[kRsPts];
+            for (int idx = threadIdx.x; idx < total; idx += kRsPts) {
+                int lo = 0, hi = kRsPts - 1;  // the owner: the last thread whose offset is <= idx
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (qoff[mid] <= idx) lo = mid;
+                    else hi = mid - 1;
+                }
+                const int k = idx - qoff[lo];
+                const unsigned short it = qitem[k * kRsPts + lo];
+                const int a = it >> 7, c = it & 127;
+                const int s = __float_as_int(rs_cand[a * kRsShiftChunk + c].w);
+                const double *pa = atoms + 3 * (size_t)(a0 + a);
+                const double ex = gs[0][lo] - (pa[0] + shifts[3 * s]);
+                const double ey = gs[1][lo] - (pa[1] + shifts[3 * s + 1]);
+                const double ez = gs[2][lo] - (pa[2] + shifts[3 * s + 2]);
+                const double r = sqrt(ex * ex + ey * ey + ez * ez);
+                double term = 0.0;
+                if ((r <= rc) && !(s == zero_idx && !(r > 1e-10))) term = erfc(sa * r) / r;
+                qterm[k * kRsPts + lo] = term;
+            }
+            __syncthreads();
+            for (int k = 0; k < cnt; ++k) tile[qitem[k * kRsPts + threadIdx.x] >> 7][threadIdx.x] += qterm[k * kRsPts + threadIdx.x];
+            const int again = more;
+            __syncthreads();  // the queue is refilled next round
+            if (!again) break;
+        }
     }
     // tile[a][t] -> phi[(mb + t) * N + a0 + a]: kRsAtoms consecutive doubles per point
     for (int e = threadIdx.x; e < kRsPts * kRsAtoms; e += kRsPts) {
@@ -190,6 +282,116 @@ __global__ void shifted_sums_kernel(const double *__restrict__ sphi, const doubl
     if (t < N) s[t] = sphi[t] - (double)M * c[t];
 }
 
+// ---- FP64 separable reciprocal sum (the escalated fit) ----
+// The transform of recip_sep.cu with every product and sum in FP64: with the exact
+// per-axis lattice phases ex, ey, ez of the grid (tables of the Ewald object) and
+// W_a(n) = w_k e^{-i k.r_a},
+//   F[l][n2][a][n1] = sum_n3 ez[n3][l] W[n2][n3][a][n1]      (every grid plane l)
+//   E[r][a][n1]     = sum_n2 ey[n2][j_r] F[l_r][n2][a][n1]    (the rows r that hold kept points)
+//   Phi[m][a]      += Re sum_n1 ex[n1][i_m] E[r_m][a][n1]     (every kept point)
+// n1 in [0, P], n2, n3 in [-P, P], P = KMAX - 1 (stored with offset P; the FP64 tables
+// carry offset KMAX).  On the 2000-atom triclinic cube this is ~35 GFLOP instead of the
+// flat k-table's 158 (repeat.py:968-981 evaluated as one DGEMM).
+struct RecBasis {
+    double rb[9];
+};
+
+// U[a][d][n + P] = e^{-i n (b_d . r_a)}
+__global__ void atom_phases64_kernel(const double *__restrict__ atoms, int N, RecBasis B, int P,
+                                     double2 *__restrict__ U) {
+    const int nw = 2 * P + 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * 3 * nw) return;
+    const int n = t % nw - P, d = (t / nw) % 3, a = t / (3 * nw);
+    const double *p = atoms + 3 * a;
+    const double th = (p[0] * B.rb[3 * d] + p[1] * B.rb[3 * d + 1]) + p[2] * B.rb[3 * d + 2];
+    double sn, cs;
+    sincos((double)n * th, &sn, &cs);
+    U[t] = make_double2(cs, -sn);
+}
+
+__device__ __forceinline__ double2 cmul64(double2 x, double2 y) {
+    return make_double2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
+}
+
+// W[n2'][n3'][a][n1] = w_k e^{-i k.r_a} for the k-set (zero elsewhere: cleared before)
+__global__ void build_w64_kernel(const int *__restrict__ kidx, const double *__restrict__ kcoef, int K, int N,
+                                 int P, const double2 *__restrict__ U, double2 *__restrict__ W) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)N * K) return;
+    const int a = (int)(t / K), k = (int)(t - (long long)a * K);
+    const int nw = 2 * P + 1, n1c = P + 1;
+    const int n1 = kidx[3 * k], n2 = kidx[3 * k + 1] + P, n3 = kidx[3 * k + 2] + P;
+    const double2 *u = U + (size_t)a * 3 * nw;
+    const double2 v = cmul64(cmul64(u[n1 + P], u[nw + n2]), u[2 * nw + n3]);
+    const double w = kcoef[k];
+    W[(((size_t)n2 * nw + n3) * N + a) * n1c + n1] = make_double2(w * v.x, w * v.y);
+}
+
+// stage A: one thread per (l, n2, a, n1), n1 fastest
+__global__ void stage_a64_kernel(const double2 *__restrict__ W, const double2 *__restrict__ ez, int nz, int N,
+                                 int P, int kmax, double2 *__restrict__ F) {
+    const int nw = 2 * P + 1, n1c = P + 1;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nz * nw * N * n1c) return;
+    const long long an = (long long)N * n1c;
+    const int r = (int)(t % an);           // a n1c + n1
+    const int n2 = (int)((t / an) % nw), l = (int)(t / (an * nw));
+    double re = 0.0, im = 0.0;
+    for (int n3 = 0; n3 < nw; ++n3) {
+        const double2 z = ez[(size_t)(n3 - P + kmax) * nz + l];
+        const double2 v = W[((size_t)n2 * nw + n3) * an + r];
+        re += z.x * v.x - z.y * v.y;
+        im += z.x * v.y + z.y * v.x;
+    }
+    F[t] = make_double2(re, im);
+}
+
+// stage B over the listed rows (row = j + l ny): one thread per (row, a, n1), n1 fastest
+__global__ void stage_b64_kernel(const double2 *__restrict__ F, const double2 *__restrict__ ey, int ny, int N,
+                                 int P, int kmax, const int *__restrict__ rows, int R, double2 *__restrict__ E) {
+    const int nw = 2 * P + 1, n1c = P + 1;
+    const long long an = (long long)N * n1c;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)R * an) return;
+    const int ri = (int)(t / an), r = (int)(t - (long long)ri * an);
+    const int row = rows[ri], l = row / ny, j = row - l * ny;
+    double re = 0.0, im = 0.0;
+    for (int n2 = 0; n2 < nw; ++n2) {
+        const double2 y = ey[(size_t)(n2 - P + kmax) * ny + j];
+        const double2 f = F[((size_t)l * nw + n2) * an + r];
+        re += y.x * f.x - y.y * f.y;
+        im += y.x * f.y + y.y * f.x;
+    }
+    E[t] = make_double2(re, im);
+}
+
+// mark the grid rows that hold kept points m0 .. m0+rows-1
+__global__ void mark_rows_kernel(const int32_t *__restrict__ kept, long long m0, long long rows, int nx,
+                                 unsigned char *__restrict__ mark) {
+    const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < rows) mark[kept[m0 + m] / nx] = 1;
+}
+
+// stage C: phi[m][a] = Re sum_n1 ex[n1][i] E[rowmap[row]][a][n1]  (one thread per (m, a), a fastest)
+__global__ void stage_c64_kernel(const double2 *__restrict__ E, const double2 *__restrict__ ex, int nx, int N,
+                                 int P, const int32_t *__restrict__ kept, long long m0, long long rows,
+                                 const int *__restrict__ rowmap, double *__restrict__ phi) {
+    const int n1c = P + 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= rows * N) return;
+    const long long m = t / N;
+    const int a = (int)(t - m * N);
+    const int f = kept[m0 + m], row = f / nx, i = f - row * nx;
+    const double2 *e = E + ((size_t)rowmap[row] * N + a) * n1c;
+    double s = 0.0;
+    for (int n1 = 0; n1 < n1c; ++n1) {
+        const double2 x = ex[(size_t)n1 * nx + i], v = e[n1];
+        s += x.x * v.x - x.y * v.y;
+    }
+    phi[t] = s;
+}
+
 }  // namespace
 
 void column_sums_fp64(const double *X, int64_t rows, int cols, int ld, double *out, bool accumulate, rp_ctx *ctx,
@@ -216,7 +418,7 @@ void finish_normal_equations(const double *G, const double *r, const double *s_c
 
 void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const int32_t *kept_idx_dev,
                const double *Vc_dev, int64_t M, double *A_dev, double *b_dev, double *sum_phi_dev,
-               cudaStream_t stream) {
+               cudaStream_t stream, bool separable) {
     RP_REQUIRE(N > 0 && M > 0, "rp_gram: need N > 0 and M > 0");
     const int K = ew->K, K2 = 2 * ew->K;
     std::vector<double> sh;
@@ -230,14 +432,40 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
     RP_CUDA(cudaMemcpyAsync(d_shifts, sh.data(), sizeof(double) * sh.size(), cudaMemcpyHostToDevice, stream));
     RP_CUDA(cudaMemcpyAsync(d_axis, ew->grid.axis, sizeof(double) * 9, cudaMemcpyHostToDevice, stream));
 
-    double *B = ctx->buf_t<double>("g64_B", (size_t)N * K2);
-    if (K > 0) atom_tables_fp64(ew, d_atoms, N, B, K2, stream);
+    // reciprocal part: the flat k-table product (one DGEMM per chunk: the comparator), or
+    // the separable transform in FP64 (the escalated fit): W and the plane stage once per fit
+    const int kp = ew->kmax - 1, nw = 2 * kp + 1, n1c = kp + 1;  // the separable sum's n range
+    const int nx = ew->grid.n_grid[0], ny = ew->grid.n_grid[1], nz = ew->grid.n_grid[2];
+    const bool sep = separable && K > 0 && kp >= 0;
+    double *B = nullptr;
+    double2 *F64 = nullptr;
+    if (sep) {
+        StageTimer tt(ctx, "fp64_recip_sep", stream);
+        double2 *U = ctx->buf_t<double2>("g64_U", (size_t)N * 3 * nw);
+        double2 *W = ctx->buf_t<double2>("g64_W", (size_t)nw * nw * N * n1c);
+        F64 = ctx->buf_t<double2>("g64_F", (size_t)nz * nw * N * n1c);
+        RP_CUDA(cudaMemsetAsync(W, 0, sizeof(double2) * (size_t)nw * nw * N * n1c, stream));
+        RecBasis rb;
+        for (int q = 0; q < 9; ++q) rb.rb[q] = ew->rec[q];
+        atom_phases64_kernel<<<ceil_div(N * 3 * nw, 128), 128, 0, stream>>>(d_atoms, N, rb, kp, U);
+        RP_LAUNCH_CHECK();
+        build_w64_kernel<<<ceil_div((long long)N * K, 128), 128, 0, stream>>>(ew->d_kidx, ew->d_kcoef, K, N, kp, U, W);
+        RP_LAUNCH_CHECK();
+        stage_a64_kernel<<<ceil_div((long long)nz * nw * N * n1c, 128), 128, 0, stream>>>(W, ew->d_ez, nz, N, kp,
+                                                                                          ew->kmax, F64);
+        RP_LAUNCH_CHECK();
+    } else {
+        B = ctx->buf_t<double>("g64_B", (size_t)N * K2);
+        if (K > 0) atom_tables_fp64(ew, d_atoms, N, B, K2, stream);
+    }
 
-    // chunk rows so T and Phi stay within ~2 GB together
-    const size_t row_bytes = sizeof(double) * ((size_t)K2 + N);
-    int64_t chunk = std::max<int64_t>(256, (int64_t)((size_t)2 << 30) / (int64_t)row_bytes);
+    // chunk rows so T and Phi stay within ~2 GB together (separable: Phi and the chunk's
+    // reciprocal rows, at most one per point, within ~4 GB)
+    const size_t row_bytes = sep ? sizeof(double) * N + sizeof(double2) * (size_t)N * n1c
+                                 : sizeof(double) * ((size_t)K2 + N);
+    int64_t chunk = std::max<int64_t>(256, (int64_t)((size_t)(sep ? 4 : 2) << 30) / (int64_t)row_bytes);
     chunk = std::min<int64_t>(chunk, M);
-    double *T = ctx->buf_t<double>("g64_T", (size_t)chunk * K2);
+    double *T = sep ? nullptr : ctx->buf_t<double>("g64_T", (size_t)chunk * K2);
     double *P = ctx->buf_t<double>("g64_P", (size_t)chunk * N);
     double *G = ctx->buf_t<double>("g64_G", (size_t)N * N);
     double *r = ctx->buf_t<double>("g64_r", (size_t)N);
@@ -250,12 +478,44 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
     RP_CUDA(cudaMemsetAsync(r, 0, sizeof(double) * N, stream));
     RP_CUDA(cudaMemsetAsync(sphi, 0, sizeof(double) * N, stream));
 
+    const bool syrk = N >= 512;  // the Gram's cuBLAS call (below)
     cublasHandle_t h = ctx->blas();
     RP_CUBLAS(cublasSetStream(h, stream));
     const double one = 1.0, zero = 0.0;
     for (int64_t m0 = 0; m0 < M; m0 += chunk) {
         const int64_t rows = std::min<int64_t>(chunk, M - m0);
-        if (K > 0) {
+        if (sep) {
+            StageTimer tt(ctx, "fp64_recip_sep", stream);
+            // the grid rows of this chunk's points, numbered on the host
+            const size_t nrows = (size_t)ny * nz;
+            unsigned char *mark = ctx->buf_t<unsigned char>("g64_mark", nrows);
+            RP_CUDA(cudaMemsetAsync(mark, 0, nrows, stream));
+            mark_rows_kernel<<<ceil_div(rows, 256), 256, 0, stream>>>(kept_idx_dev, m0, rows, nx, mark);
+            RP_LAUNCH_CHECK();
+            unsigned char *hmark = static_cast<unsigned char *>(ctx->host_buf("g64_mark", nrows));
+            int *hmap = static_cast<int *>(ctx->host_buf("g64_rowmap", sizeof(int) * nrows * 2));
+            RP_CUDA(cudaMemcpyAsync(hmark, mark, nrows, cudaMemcpyDeviceToHost, stream));
+            RP_CUDA(cudaStreamSynchronize(stream));
+            int R = 0;
+            int *hlist = hmap + nrows;
+            for (size_t r = 0; r < nrows; ++r) {
+                hmap[r] = hmark[r] ? R : -1;
+                if (hmark[r]) hlist[R++] = (int)r;
+            }
+            int *rowmap = ctx->buf_t<int>("g64_rowmap", nrows);
+            int *rowlist = ctx->buf_t<int>("g64_rowlist", (size_t)std::max(R, 1));
+            RP_CUDA(cudaMemcpyAsync(rowmap, hmap, sizeof(int) * nrows, cudaMemcpyHostToDevice, stream));
+            RP_CUDA(cudaMemcpyAsync(rowlist, hlist, sizeof(int) * R, cudaMemcpyHostToDevice, stream));
+            double2 *E64 = ctx->buf_t<double2>("g64_E", (size_t)std::max(R, 1) * N * n1c);
+            stage_b64_kernel<<<ceil_div((long long)R * N * n1c, 128), 128, 0, stream>>>(F64, ew->d_ey, ny, N, kp,
+                                                                                       ew->kmax, rowlist, R, E64);
+            RP_LAUNCH_CHECK();
+            stage_c64_kernel<<<ceil_div(rows * N, 128), 128, 0, stream>>>(E64, ew->d_ex, nx, N, kp, kept_idx_dev, m0,
+                                                                          rows, rowmap, P);
+            RP_LAUNCH_CHECK();
+            // the pinned row arrays are rewritten by the next chunk: its uploads must be done
+            RP_CUDA(cudaStreamSynchronize(stream));
+        } else if (K > 0) {
             {
                 StageTimer tt(ctx, "fp64_tables", stream);
                 grid_tables_fp64(ew, kept_idx_dev, m0, rows, T, K2, stream);
@@ -265,12 +525,12 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
         } else {  // the non-periodic basis has no reciprocal part
             RP_CUDA(cudaMemsetAsync(P, 0, sizeof(double) * (size_t)rows * N, stream));
         }
-        StageTimer t_r(ctx, "fp64_realspace", stream);
         {
-            const size_t smem = sizeof(float4) * kRsAtoms * kRsShiftChunk;  // 32 KB of candidates
-            // with the 16.5 KB static tile the block passes the 48 KB default: opt in
-            smem_optin((const void *)realspace_fp64_kernel, 64 * 1024);
-            realspace_fp64_kernel<<<dim3(ceil_div(rows, kRsPts), ceil_div(N, kRsAtoms)), kRsPts, smem, stream>>>(
+            StageTimer t_r(ctx, "fp64_realspace", stream);
+            const size_t smem = realspace_fp64_smem(sep);  // candidates (and the pair queue): 32 or 36 KB
+            auto kern = sep ? realspace_fp64_kernel<true> : realspace_fp64_kernel<false>;
+            smem_optin((const void *)kern, smem);
+            kern<<<dim3(ceil_div(rows, kRsPts), ceil_div(N, kRsAtoms)), kRsPts, smem, stream>>>(
                 kept_idx_dev, m0, rows, d_axis, ew->grid.n_grid[0], ew->grid.n_grid[1], d_atoms, N, d_shifts, S,
                 zero_idx, ew->cutoff, ew->sqrt_alpha, P);
             RP_LAUNCH_CHECK();
@@ -287,14 +547,26 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
         }
         shift_columns_kernel<<<ceil_div(rows * N, 256), 256, 0, stream>>>(P, rows, N, c);
         RP_LAUNCH_CHECK();
-        // column-major view: X = P^T is N x rows with ld N;  G += X X^T (one triangle,
-        // mirrored after the last chunk),  r += X Vc
-        StageTimer t_g(ctx, "fp64_gram_dsyrk", stream);
-        RP_CUBLAS(cublasDsyrk(h, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, N, (int)rows, &one, P, N, &one, G, N));
-        RP_CUBLAS(cublasDgemv(h, CUBLAS_OP_N, N, (int)rows, &one, P, N, Vc_dev + m0, 1, &one, r, 1));
+        if (sep) {  // the exact two-word Gram on the tensor cores (G full, r included)
+            StageTimer t_g(ctx, "fp64_gram_words", stream);
+            gram_words_fp64(ctx, P, rows, N, Vc_dev + m0, G, r, stream);
+        } else {
+            // column-major view: X = P^T is N x rows with ld N;  G += X X^T,  r += X Vc.  DSYRK
+            // (one triangle, mirrored after the last chunk) halves the work, but for few
+            // columns cuBLAS's rank-k update parallelises poorly over the long k (31 ms for
+            // 77 x 109,682 against ~1.5 ms as a DGEMM), so small systems take the DGEMM.
+            StageTimer t_g(ctx, "fp64_gram_blas", stream);
+            if (syrk)
+                RP_CUBLAS(cublasDsyrk(h, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, N, (int)rows, &one, P, N, &one, G, N));
+            else
+                RP_CUBLAS(cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_T, N, N, (int)rows, &one, P, N, P, N, &one, G, N));
+            RP_CUBLAS(cublasDgemv(h, CUBLAS_OP_N, N, (int)rows, &one, P, N, Vc_dev + m0, 1, &one, r, 1));
+        }
     }
-    mirror_upper_kernel<<<ceil_div((long long)N * N, 256), 256, 0, stream>>>(G, N);
-    RP_LAUNCH_CHECK();
+    if (!sep && syrk) {
+        mirror_upper_kernel<<<ceil_div((long long)N * N, 256), 256, 0, stream>>>(G, N);
+        RP_LAUNCH_CHECK();
+    }
     column_sums_fp64(Vc_dev, M, 1, 1, sumV, false, ctx, stream);
     shifted_sums_kernel<<<ceil_div(N, 128), 128, 0, stream>>>(sphi, c, M, N, s_c);
     RP_LAUNCH_CHECK();

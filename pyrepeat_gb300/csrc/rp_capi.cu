@@ -15,18 +15,23 @@ void qeq_run(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, const 
 namespace rp {
 std::atomic<long long> g_launches{0};
 
+// Raise a kernel's dynamic shared-memory limit to `bytes` when the block's static and dynamic
+// shared memory together pass the 48 KB available without opting in.
 void smem_optin(const void *kernel, size_t bytes) {
-    if (bytes <= (48u << 10)) return;
     int dev = 0;
     RP_CUDA(cudaGetDevice(&dev));
     static std::mutex mu;
-    static std::map<std::pair<const void *, int>, size_t> raised;
+    static std::map<std::pair<const void *, int>, std::pair<size_t, size_t>> raised;  // (static, raised to)
     std::lock_guard<std::mutex> lk(mu);
-    size_t &have = raised[{kernel, dev}];
-    if (bytes > have) {
-        RP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-        have = bytes;
+    auto it = raised.find({kernel, dev});
+    if (it == raised.end()) {
+        cudaFuncAttributes fa;
+        RP_CUDA(cudaFuncGetAttributes(&fa, kernel));
+        it = raised.emplace(std::make_pair(kernel, dev), std::make_pair((size_t)fa.sharedSizeBytes, (size_t)0)).first;
     }
+    if (bytes + it->second.first <= (48u << 10) || bytes <= it->second.second) return;
+    RP_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    it->second.second = bytes;
 }
 void status_clear(rp_ctx *ctx, cudaStream_t s) {
     RP_CUDA(cudaMemsetAsync(ctx->status_words(), 0, 2 * sizeof(int), s));
@@ -288,11 +293,11 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
     const std::vector<long long> &off_pts = r.off_pts, &off_n = r.off_n, &off_nn = r.off_nn;
     // Work splits into host preparation and device stages so that the device never waits
     // on the host inside the batch, and the cubes run as a pipeline of up to four groups:
-    // (1) the filters' host halves on the host workers, one pinned upload, and the filter
-    // launches of every group on their own streams; (2) while they run, the Ewald tables
-    // of every cube on the host workers, one pinned upload; (3) as each group's kept
-    // counts arrive, its normal equations go to the gram streams, so later groups'
-    // filters overlap earlier groups' grams.
+    // (1) the first group's filter plans on the host workers, one pinned upload, its grids
+    // and its filter launches; (2) while they run, the Ewald tables of every cube on the
+    // host workers, one pinned upload, and the reciprocal rows; then the other groups'
+    // filters as in (1); (3) as each group's kept counts arrive, its normal equations go
+    // to the gram streams, so later groups' filters overlap earlier groups' grams.
     constexpr int kLanes = 4;
     const int lanes = ctx->timing ? 1 : kLanes;  // stage timing: one lane, each stage alone
     auto glane = [&](int i) { return ctx->lane(i % lanes); };
@@ -304,10 +309,26 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
     for (int g = 0; g <= ngroups; ++g) g0[g] = (int)((long long)n * g / ngroups);
     int32_t *kept = r.kept = ctx->buf_t<int32_t>("fit_kept", (size_t)off_pts[n]);
     double *Vc = r.Vc = ctx->buf_t<double>("fit_Vc", (size_t)off_pts[n]);
-    double *Vh = nullptr;
-    bool any_host = false;
-    for (int i = 0; i < n; ++i) any_host |= !(V_dev && V_dev[i]);
-    if (any_host) Vh = ctx->buf_t<double>("fit_V", (size_t)off_pts[n]);
+    // Grids from host memory: the filter reads a grid only at its kept points (in the
+    // compaction, after the geometric mask), so a grid in page-locked host memory that the
+    // device can address is read in place over the host link instead of being copied whole
+    // first; any other host grid is copied to the device on the copy stream.
+    std::vector<const double *> Vsrc((size_t)n, nullptr);
+    bool any_copy = false;
+    for (int i = 0; i < n; ++i) {
+        if (V_dev && V_dev[i]) {
+            Vsrc[i] = V_dev[i];
+            continue;
+        }
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, descs[i].V) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+            pa.devicePointer != nullptr)
+            Vsrc[i] = static_cast<const double *>(pa.devicePointer);
+        else
+            any_copy = true;
+        cudaGetLastError();  // an unregistered pointer may leave an error behind
+    }
+    double *Vh = any_copy ? ctx->buf_t<double>("fit_V", (size_t)off_pts[n]) : nullptr;
     long long *Md = ctx->buf_t<long long>("fit_M", (size_t)n);
     long long *Mh = static_cast<long long *>(ctx->host_buf("fit_M", sizeof(long long) * n));
     double *A = r.A = ctx->buf_t<double>("fit_A", (size_t)off_nn[n]);
@@ -344,7 +365,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
     RP_CUDA(cudaStreamWaitEvent(copy_lane, r.events.back(), 0));
     std::vector<size_t> pl_off((size_t)n + 1, 0);
     std::vector<cudaEvent_t> kept_ready((size_t)ngroups);
-    for (int g = 0; g < ngroups; ++g) {
+    auto filter_group_g = [&](int g) {
         const int i0 = g0[g], i1 = g0[g + 1];
         ctx->parallel(i1 - i0, [&](int t) {
             const rp_fit_desc &d = descs[i0 + t];
@@ -358,10 +379,12 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
         char *pl_host = static_cast<char *>(ctx->host_buf(gtag, pl_off[i1]));
         ctx->parallel(i1 - i0, [&](int t) { plan(i0 + t).pack(pl_host + pl_off[i0 + t]); });
         RP_CUDA(cudaMemcpyAsync(pl_dev, pl_host, pl_off[i1], cudaMemcpyHostToDevice, copy_lane));
-        for (int i = i0; i < i1; ++i)  // grids from host memory, this group's only
-            if (!(V_dev && V_dev[i]))
+        for (int i = i0; i < i1; ++i)  // grids from unmapped host memory, this group's only
+            if (!Vsrc[i]) {
                 RP_CUDA(cudaMemcpyAsync(Vh + off_pts[i], descs[i].V, sizeof(double) * npts[i],
                                         cudaMemcpyHostToDevice, copy_lane));
+                Vsrc[i] = Vh + off_pts[i];
+            }
         const cudaEvent_t inputs = record(copy_lane);
         for (int ln = 0; ln < lanes; ++ln) RP_CUDA(cudaStreamWaitEvent(flane(ln), inputs, 0));
         // the group's mixed-precision cubes in one launch per filter stage (brick order), the
@@ -369,7 +392,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
         std::vector<rp::FilterItem> items;
         for (int i = i0; i < i1; ++i) {
             const rp_fit_desc &d = descs[i];
-            const double *V = (V_dev && V_dev[i]) ? V_dev[i] : Vh + off_pts[i];
+            const double *V = Vsrc[i];
             if (d.precision == RP_PREC_MIXED) {
                 items.push_back(rp::FilterItem{&plan(i), pl_dev + pl_off[i], V, kept + off_pts[i], Vc + off_pts[i],
                                                Md + i, vst + 2 * i});
@@ -383,9 +406,13 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
         RP_CUDA(cudaMemcpyAsync(Mh + i0, Md + i0, sizeof(long long) * (i1 - i0), cudaMemcpyDeviceToHost, stream));
         kept_ready[g] = record(stream, true);
         ctx->trace_mark("filters queued group " + std::to_string(g));
-    }
+    };
+    filter_group_g(0);
     // 2. Ewald tables, written by the host workers straight into one pinned arena,
-    //    uploaded with a single copy on a stream of its own
+    //    uploaded with a single copy on a stream of its own.  They go up right behind the
+    //    first group's grids and before the other groups' (copies from host memory are
+    //    served in the order they are queued), so the first group's reciprocal rows and
+    //    normal equations do not wait for the whole batch's grids to arrive.
     std::vector<size_t> ew_off((size_t)n + 1, 0);
     auto &ew_pool = ctx->ew_pool[ctx->cur_slot];
     while ((int)ew_pool.size() < n) ew_pool.emplace_back(new rp_ewald());
@@ -408,7 +435,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
     });
     for (int i = 0; i < n; ++i) rp::ewald_place(r.ews[i], ew_dev + ew_off[i]);
     ctx->trace_mark("tables built");
-    // the tables go up on the reciprocal rows' stream, beside the grids still queued on the
+    // the tables go up on the reciprocal rows' stream, beside the first group's grids on the
     // copy stream (with grids from host memory those are most of the batch's bytes)
     const cudaStream_t recip_lane = ctx->timing ? ctx->lane(0) : ctx->lane(kLaneRecip);
     RP_CUDA(cudaStreamWaitEvent(recip_lane, r.events.front(), 0));  // after the caller's work so far
@@ -438,6 +465,7 @@ void batch_enqueue(rp_ctx *ctx, int n, const rp_fit_desc *descs, const double *c
         }
         rows_ready[g] = record(recip_lane);
     }
+    for (int g = 1; g < ngroups; ++g) filter_group_g(g);
     // 3. normal equations, group by group as the kept counts arrive.  Mixed-precision fits
     //    are spread over the gram streams (each with its own scratch), so one cube's small
     //    kernels and launch gaps overlap another's; the FP64 comparator stays on the
@@ -532,7 +560,8 @@ void batch_complete(rp_ctx *ctx, BatchRun &r) {
         std::vector<rp::SolveJob> jobs;
         for (int i : cubes) jobs.push_back(r.job(i));
         std::vector<double> rinfo;
-        rp::solve_batch(ctx, jobs, rinfo, stream);
+        // an escalated cube's system is known to be beyond FP32 refinement: FP64 factors at once
+        rp::solve_batch(ctx, jobs, rinfo, stream, flag == RP_FIT_ESCALATED);
         for (size_t t = 0; t < cubes.size(); ++t) {
             take(cubes[t], rinfo.data() + (size_t)rp::kSolveInfo * t);
             info[(size_t)W * cubes[t] + 6] = precision;
@@ -556,7 +585,8 @@ void batch_complete(rp_ctx *ctx, BatchRun &r) {
     rp::status_check(ctx, stream);
     // escalation: a mixed-precision cube whose bordered system is so ill-conditioned that
     // the Gram's rounding (~1e-7 relative) could move its charges visibly (kappa / (n+1)
-    // above the ctx's limit) is fitted again in plain FP64
+    // above the ctx's limit) is fitted again in FP64 (the reciprocal sum by the FP64
+    // separable transform)
     std::vector<int> esc;
     if (ctx->kappa_limit > 0.0)
         for (int i = 0; i < n; ++i)
@@ -568,7 +598,7 @@ void batch_complete(rp_ctx *ctx, BatchRun &r) {
         for (int i : esc) {
             const rp_fit_desc &d = r.descs[i];
             rp::gram_fp64(ctx, r.ews[i], d.atoms, d.N, r.kept + r.off_pts[i], r.Vc + r.off_pts[i], r.M[i],
-                          r.A + r.off_nn[i], r.b + r.off_n[i], nullptr, stream);
+                          r.A + r.off_nn[i], r.b + r.off_n[i], nullptr, stream, true);
         }
         resolve(esc, RP_FIT_ESCALATED, RP_PREC_FP64);
     }

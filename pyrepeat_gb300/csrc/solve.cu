@@ -100,18 +100,34 @@ __device__ void block_argmax(double v, int idx, double *sv, int *si, double *out
     __syncthreads();
 }
 
-__device__ void lu_apply(const double *__restrict__ LU, const int *__restrict__ perm, int n1, double *__restrict__ y) {
-    // solve (P L U) z = y in place (y global), blocked by 32 columns: the diagonal block is
-    // solved by one warp with shuffles, then every warp updates the remaining rows with the
-    // block's 32 values (a warp per row, coalesced).  Three barriers per 32 columns.
+__device__ void lu_apply(const double *__restrict__ LU, const int *__restrict__ perm, int n1, double *__restrict__ y,
+                         double *__restrict__ ysh) {
+    // solve (P L U) z = y in place (y global; ysh: n1 doubles of shared memory), blocked by 32
+    // columns: the diagonal block is solved by one warp with shuffles, then every thread
+    // updates one remaining row with the block's 32 values (a warp instruction covers 32 rows:
+    // the FP64 pipe takes as long for one lane as for 32).  The row interchanges run in
+    // shared memory.  Three barriers per 32 columns.
     __shared__ double blk[32][33];
+    __shared__ double yb[32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __syncthreads();
-    if (threadIdx.x == 0)
-        for (int k = 0; k < n1; ++k) {
-            const int p = perm[k];
-            if (p != k) { const double t = y[k]; y[k] = y[p]; y[p] = t; }
+    for (int t = threadIdx.x; t < n1; t += kLU) ysh[t] = y[t];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int k = 0;
+        for (; k + 8 <= n1; k += 8) {  // the interchanges' indices are independent loads
+            int p[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) p[u] = perm[k + u];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (p[u] != k + u) { const double t = ysh[k + u]; ysh[k + u] = ysh[p[u]]; ysh[p[u]] = t; }
         }
+        for (; k < n1; ++k) {
+            const int p = perm[k];
+            if (p != k) { const double t = ysh[k]; ysh[k] = ysh[p]; ysh[p] = t; }
+        }
+    }
     __syncthreads();
     for (int c0 = 0; c0 < n1; c0 += 32) {  // forward: L, unit diagonal
         const int bs = min(32, n1 - c0);
@@ -121,18 +137,20 @@ __device__ void lu_apply(const double *__restrict__ LU, const int *__restrict__ 
         }
         __syncthreads();
         if (warp == 0) {
-            double yv = lane < bs ? y[c0 + lane] : 0.0;
+            double yv = lane < bs ? ysh[c0 + lane] : 0.0;
             for (int c = 0; c < bs - 1; ++c) {
                 const double yc = __shfl_sync(0xffffffffu, yv, c);
                 if (lane > c && lane < bs) yv -= blk[lane][c] * yc;
             }
-            if (lane < bs) y[c0 + lane] = yv;
+            if (lane < bs) ysh[c0 + lane] = yv;
+            yb[lane] = lane < bs ? yv : 0.0;
         }
         __syncthreads();
-        for (int r = c0 + bs + warp; r < n1; r += kLU / 32) {
-            double t = lane < bs ? LU[(size_t)r * n1 + c0 + lane] * y[c0 + lane] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-            if (lane == 0) y[r] -= t;
+        for (int r = c0 + bs + threadIdx.x; r < n1; r += kLU) {
+            const double *row = LU + (size_t)r * n1 + c0;
+            double t = 0.0;
+            for (int c = 0; c < bs; ++c) t += row[c] * yb[c];
+            ysh[r] -= t;
         }
         __syncthreads();
     }
@@ -144,22 +162,26 @@ __device__ void lu_apply(const double *__restrict__ LU, const int *__restrict__ 
         }
         __syncthreads();
         if (warp == 0) {
-            double yv = lane < bs ? y[c0 + lane] : 0.0;
+            double yv = lane < bs ? ysh[c0 + lane] : 0.0;
             for (int c = bs - 1; c >= 0; --c) {
                 if (lane == c) yv = yv / blk[c][c];
                 const double xc = __shfl_sync(0xffffffffu, yv, c);
                 if (lane < c) yv -= blk[lane][c] * xc;
             }
-            if (lane < bs) y[c0 + lane] = yv;
+            if (lane < bs) ysh[c0 + lane] = yv;
+            yb[lane] = lane < bs ? yv : 0.0;
         }
         __syncthreads();
-        for (int r = warp; r < c0; r += kLU / 32) {
-            double t = lane < bs ? LU[(size_t)r * n1 + c0 + lane] * y[c0 + lane] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-            if (lane == 0) y[r] -= t;
+        for (int r = threadIdx.x; r < c0; r += kLU) {
+            const double *row = LU + (size_t)r * n1 + c0;
+            double t = 0.0;
+            for (int c = 0; c < bs; ++c) t += row[c] * yb[c];
+            ysh[r] -= t;
         }
         __syncthreads();
     }
+    for (int t = threadIdx.x; t < n1; t += kLU) y[t] = ysh[t];
+    __syncthreads();
 }
 
 // max over the block (every thread gets the result)
@@ -464,7 +486,7 @@ __device__ void apply_inverse(const SolveDesc &d, int n1, bool f32, float *ys, f
         }
         __syncthreads();
     } else {
-        lu_apply(d.As, d.perm, n1, d.r);
+        lu_apply(d.As, d.perm, n1, d.r, reinterpret_cast<double *>(ys));
         __syncthreads();
     }
 }
@@ -544,7 +566,7 @@ __device__ void residual(const SolveDesc &d, int n1) {
 __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *__restrict__ descs) {
     const SolveDesc d = descs[blockIdx.x];
     const int n1 = d.n + 1;
-    extern __shared__ float fsh[];  // [2 * n1]: right-hand side / correction in FP32
+    extern __shared__ __align__(16) float fsh[];  // [2 * n1]: right-hand side / correction in FP32 (or n1 doubles)
     float *ys = fsh, *xs = fsh + n1;
     __shared__ double sv[kLU / 32];
     __shared__ int si[kLU / 32];
@@ -677,14 +699,14 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
         }
         }
         for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] = d.bs[t];
-        lu_apply(A, d.perm, n1, d.x);
+        lu_apply(A, d.perm, n1, d.x, reinterpret_cast<double *>(fsh));
         for (int rr = threadIdx.x; rr < n1; rr += kLU) {
             double s = d.bs[rr];
             const double *row = d.A0 + (size_t)rr * n1;
             for (int c = 0; c < n1; ++c) s -= row[c] * d.x[c];
             d.r[rr] = s;
         }
-        lu_apply(A, d.perm, n1, d.r);
+        lu_apply(A, d.perm, n1, d.r, reinterpret_cast<double *>(fsh));
         for (int t = threadIdx.x; t < n1; t += kLU) d.x[t] += d.r[t];
         __syncthreads();
         double rmax = 0.0;
@@ -1022,7 +1044,7 @@ static void host_fold(int N, const std::vector<double> &A, const std::vector<dou
 }
 
 const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, cudaStream_t stream,
-                                const std::string &tag, SolvePending *pend) {
+                                const std::string &tag, SolvePending *pend, bool fp64_first) {
     const int nj = (int)jobs.size();
     if (nj == 0) return nullptr;
     std::vector<FoldPlan> plans((size_t)nj);
@@ -1087,7 +1109,10 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
     std::vector<int> disjoint;
     for (int j = 0; j < nj; ++j) {
         const int n1 = plans[j].n + 1;
-        if (n1 >= kLUWideMin && n1 <= kLUWideMax) descs[j].pre = d_pre + 3 * (size_t)j;
+        if (n1 >= kLUWideMin && n1 <= kLUWideMax) {
+            descs[j].pre = d_pre + 3 * (size_t)j;
+            if (fp64_first && n1 <= kLUWide64Max) descs[j].wide64 = 1;
+        }
         if (plans[j].disjoint) disjoint.push_back(j);
     }
     // the small tables go up from one pinned staging block per tag (asynchronous copies that
@@ -1156,9 +1181,14 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
     if (pend) *pend = SolvePending{};
     for (int j = 0; j < nj; ++j) {
         if (!descs[j].pre) continue;
-        StageTimer tt(ctx, "solve_lu_wide", stream);
-        lu_wide_factor<float>(ctx, descs[j], plans[j].n + 1, stream);
-        any_wide = true;
+        if (descs[j].wide64) {
+            StageTimer tt(ctx, "solve_lu_wide64", stream);
+            lu_wide_factor<double>(ctx, descs[j], plans[j].n + 1, stream);
+        } else {
+            StageTimer tt(ctx, "solve_lu_wide", stream);
+            lu_wide_factor<float>(ctx, descs[j], plans[j].n + 1, stream);
+            any_wide = true;
+        }
     }
     {
         StageTimer tt(ctx, "solve_lu", stream);
@@ -1223,11 +1253,12 @@ void solve_wide_fp64(rp_ctx *ctx, SolvePending &pd, cudaStream_t stream) {
     RP_CUDA(cudaStreamSynchronize(stream));
 }
 
-void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream) {
+void solve_batch(rp_ctx *ctx, const std::vector<SolveJob> &jobs, std::vector<double> &info, cudaStream_t stream,
+                 bool fp64_first) {
     const int nj = (int)jobs.size();
     info.assign((size_t)nj * kSolveInfo, 0.0);
     if (nj == 0) return;
-    const double *h = solve_batch_async(ctx, jobs, stream, "");
+    const double *h = solve_batch_async(ctx, jobs, stream, "", nullptr, fp64_first);
     RP_CUDA(cudaStreamSynchronize(stream));
     std::copy(h, h + kSolveInfo * (size_t)nj, info.begin());
 }

