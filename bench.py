@@ -732,7 +732,11 @@ def main():
         "rrms": {"median": float(np.median(rrms)), "max": float(np.max(rrms)), "cubes": len(rrms),
                  "definition": "sqrt(sum (V_fit - V)^2 / sum V^2) over kept points, both centred"},
         "e2e": {"value": e2e_value, "unit": "fits/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "step_ms": e2e_steps},
+                "step_ms": e2e_steps,
+                "inputs": "each step's grids (h2d_bytes_per_step) from page-locked host memory; the filter reads "
+                          "them in place over the host link at the kept points only (kept_bytes_read_per_step), "
+                          "charges back to page-locked host memory",
+                "kept_bytes_read_per_step": 8 * int(sum(Ms))},
         "gpu_launches": launches,
         "roofline": roof,
         "stage_rooflines": rooflines,

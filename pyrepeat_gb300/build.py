@@ -97,7 +97,7 @@ def build_cuda(force: bool = False, verbose: bool = False, ptxas_verbose: bool =
                 if o.strip():
                     print(o)
     if force or jobs or _stale(LIB_PATH, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", LIB_PATH, *objs, "-lcublas", "-lcuda"])
+        _run([nvcc, *ARCH, "-shared", "-o", LIB_PATH, *objs, "-lcublas", "-lcusolver", "-lcuda"])
     return LIB_PATH
 
 

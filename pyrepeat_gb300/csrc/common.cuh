@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cublas_v2.h>
+#include <cusolverDn.h>
 
 #include <algorithm>
 #include <atomic>
@@ -220,6 +221,7 @@ struct rp_ctx {
     size_t used = 0;
     std::string last_error;
     cublasHandle_t cublas[rp::kBatchSlots] = {};
+    cusolverDnHandle_t cusolver[rp::kBatchSlots] = {};  // FP64 factorisations of wide systems
     std::unordered_map<std::string, rp::Buffer> scratch;
     int *d_status = nullptr;  // device status words (two per slot) for bounded waits / clamps
     // The slot the calling code runs in.  Set by the one thread that uses the ctx at a time
@@ -328,6 +330,7 @@ struct rp_ctx {
         return b.ptr;
     }
     cublasHandle_t blas();  // the current slot's handle
+    cusolverDnHandle_t solver();  // the current slot's cuSOLVER handle
     // Worker streams for fits that run concurrently inside one batch (created on first use,
     // non-blocking, destroyed with the ctx): lane i of the current slot.
     std::vector<cudaStream_t> lanes;
@@ -550,6 +553,8 @@ struct SolveDesc {
                           // kappa, unknowns n+1, refinement steps, factorisation path
     double *pre;          // null, or {flag, min|piv|, max|piv|} of a wide factorisation already in As
     int wide64;           // As holds wide FP64 factors: skip the FP32 stage and the in-CTA FP64 LU
+    int host64;           // FP32 factors in the CTA, but a stalled refinement goes to the host's FP64
+                          // factorisation across the GPU (pre holds its flag) instead of an in-CTA FP64 LU
 };
 // Wide systems of a solve launch whose FP32 refinement may not have converged: their flags are
 // on their way to pinned memory; solve_wide_fp64 (after the stream has reached them) factors

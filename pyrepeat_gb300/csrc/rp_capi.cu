@@ -55,6 +55,15 @@ cublasHandle_t rp_ctx::blas() {
     return h;
 }
 
+cusolverDnHandle_t rp_ctx::solver() {
+    cusolverDnHandle_t &h = cusolver[cur_slot];
+    if (!h && cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) {
+        h = nullptr;
+        rp::fail(RP_E_CUDA, "cusolverDnCreate failed");
+    }
+    return h;
+}
+
 namespace {
 
 template <class F>
@@ -120,6 +129,8 @@ int rp_ctx_destroy(rp_ctx *ctx) {
     for (cudaStream_t st : ctx->lanes) cudaStreamDestroy(st);
     for (cublasHandle_t h : ctx->cublas)
         if (h) cublasDestroy(h);
+    for (cusolverDnHandle_t h : ctx->cusolver)
+        if (h) cusolverDnDestroy(h);
     cudaFree(ctx->d_status);
     delete ctx;
     return RP_OK;

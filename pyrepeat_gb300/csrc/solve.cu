@@ -546,6 +546,10 @@ constexpr int kRefineMax = 30;  // and stop early once a step no longer halves t
 // converge): n1 in [kLUWideMin, kLUWideMax], FP64 up to kLUWide64Max; the bounds are the
 // panel rows that fit shared memory at 4 columns
 constexpr int kLUWideMin = 768;
+// systems of kLUHost64Min to kLUWideMin unknowns keep their FP32 factorisation in the CTA, but
+// when its refinement stalls the FP64 factors come from across the GPU (cuSOLVER getrf): an
+// in-CTA FP64 LU of 425 unknowns takes ~13 ms on one SM's FP64 pipe
+constexpr int kLUHost64Min = 256;
 constexpr int kLUWideMax = (int)((225 * 1024) / (sizeof(float) * 5));
 constexpr int kLUWide64Max = (int)((225 * 1024) / (sizeof(double) * 5));
 
@@ -579,7 +583,8 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
     // ---- FP32 LU + FP64-residual refinement
     if (!d.wide64) {
         float *L = reinterpret_cast<float *>(d.As);  // the first half of the FP64 work matrix
-        if (!d.pre)
+        const bool wide32 = d.pre && !d.host64;  // FP32 factors from across the GPU
+        if (!wide32)
             for (long long t = threadIdx.x; t < (long long)n1 * n1; t += kLU) L[t] = (float)d.A0[t];
         for (int t = threadIdx.x; t < n1; t += kLU) {
             d.x[t] = 0.0;
@@ -587,7 +592,7 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
         }
         __syncthreads();
         bool factored;
-        if (d.pre) {  // factored across the GPU before this launch (lu_wide_factor)
+        if (wide32) {  // factored across the GPU before this launch (lu_wide_factor)
             factored = d.pre[0] == 0.0;
             if (factored) {
                 pmin = fmin(pmin, d.pre[1]);
@@ -738,7 +743,7 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
         d.info[4] = fmin(anorm * kinv, 1e300);
         d.info[5] = n1;
         d.info[6] = steps;
-        d.info[7] = f32_solved ? (d.pre ? 1.0 : 0.0) : (d.wide64 ? 3.0 : 2.0);
+        d.info[7] = f32_solved ? ((d.pre && !d.host64) ? 1.0 : 0.0) : (d.wide64 ? 3.0 : 2.0);
     }
     __syncthreads();
     // expand to all atoms
@@ -918,8 +923,93 @@ inline cublasStatus_t gemm_nn(cublasHandle_t h, int m, int n, int k, const doubl
     return cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 
+// ---- FP64 wide factorisation by cuSOLVER's getrf
+// The bordered matrix K is symmetric, so its row-major image is also K read column-major:
+// getrf factors it as P K = L U in column-major storage, which a transpose turns into the
+// row-major unit-lower L and upper U that lu_solve_refine_kernel applies; LAPACK's 1-based
+// row interchanges become d.perm.  Panels factored across the GPU instead of in one CTA each
+// (an FP64 panel of 1851 x 32 costs ~0.25 ms on one SM's FP64 pipe).  The refinement step
+// that follows uses A0 itself, so a Gram that is symmetric only to rounding costs nothing.
+__global__ void transpose_square_kernel(double *__restrict__ A, int n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * n) return;
+    const int i = (int)(t / n), j = (int)(t - (long long)i * n);
+    if (i < j) {
+        const double x = A[(size_t)i * n + j];
+        A[(size_t)i * n + j] = A[(size_t)j * n + i];
+        A[(size_t)j * n + i] = x;
+    }
+}
+
+// pivot rows to 0-based interchanges, the pivots' range, and an exactly zero pivot replaced by
+// 1e-300 and flagged (the in-CTA FP64 factorisation's rule); one CTA
+__global__ void __launch_bounds__(1024) getrf_finish_kernel(double *__restrict__ LU, int n,
+                                                            const int *__restrict__ ipiv, int *__restrict__ perm,
+                                                            double *__restrict__ pre) {
+    __shared__ double smin[32], smax[32];
+    __shared__ int ssing[32];
+    double mn = 1e308, mx = 0.0;
+    int sing = 0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        perm[k] = ipiv[k] - 1;
+        double *dk = LU + (size_t)k * n + k;
+        const double a = fabs(*dk);
+        if (!(a > 1e-300)) {
+            sing = 1;
+            *dk = (*dk < 0.0) ? -1e-300 : 1e-300;
+        }
+        mn = fmin(mn, a);
+        mx = fmax(mx, a);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        sing |= __shfl_xor_sync(0xffffffffu, sing, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        smin[threadIdx.x >> 5] = mn;
+        smax[threadIdx.x >> 5] = mx;
+        ssing[threadIdx.x >> 5] = sing;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            mn = fmin(mn, smin[w]);
+            mx = fmax(mx, smax[w]);
+            sing |= ssing[w];
+        }
+        pre[0] = sing ? 1.0 : 0.0;
+        pre[1] = mn;
+        pre[2] = mx;
+    }
+}
+
+void lu_wide_factor_getrf(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t stream) {
+    double *L = d.As;
+    const long long nn = (long long)n1 * n1;
+    lu_copy_kernel<double><<<(int)std::min<long long>(ceil_div(nn, 256), 4096), 256, 0, stream>>>(d.A0, L, nn, d.pre);
+    RP_LAUNCH_CHECK();
+    cusolverDnHandle_t h = ctx->solver();
+    if (cusolverDnSetStream(h, stream) != CUSOLVER_STATUS_SUCCESS) fail(RP_E_CUDA, "cusolverDnSetStream failed");
+    int lwork = 0;
+    if (cusolverDnDgetrf_bufferSize(h, n1, n1, L, n1, &lwork) != CUSOLVER_STATUS_SUCCESS)
+        fail(RP_E_CUDA, "cusolverDnDgetrf_bufferSize failed");
+    double *work = ctx->buf_t<double>("s_getrf_work", (size_t)std::max(lwork, 1));
+    int *ipiv = ctx->buf_t<int>("s_getrf_ipiv", (size_t)n1 + 1);  // [n1] pivots, then the info word
+    if (cusolverDnDgetrf(h, n1, n1, L, n1, work, ipiv, ipiv + n1) != CUSOLVER_STATUS_SUCCESS)
+        fail(RP_E_CUDA, "cusolverDnDgetrf failed");
+    transpose_square_kernel<<<(int)ceil_div(nn, 256), 256, 0, stream>>>(L, n1);
+    RP_LAUNCH_CHECK();
+    getrf_finish_kernel<<<1, 1024, 0, stream>>>(L, n1, ipiv, d.perm, d.pre);
+    RP_LAUNCH_CHECK();
+}
+
 template <typename T>
 void lu_wide_factor(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t stream) {
+    if (sizeof(T) == 8) {
+        lu_wide_factor_getrf(ctx, d, n1, stream);
+        return;
+    }
     smem_optin((const void *)lu_panel_kernel<T>, kPanelSmem);
     T *L = reinterpret_cast<T *>(d.As);
     const long long nn = (long long)n1 * n1;
@@ -1109,8 +1199,9 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
     std::vector<int> disjoint;
     for (int j = 0; j < nj; ++j) {
         const int n1 = plans[j].n + 1;
-        if (n1 >= kLUWideMin && n1 <= kLUWideMax) {
+        if (n1 >= kLUHost64Min && n1 <= kLUWideMax) {
             descs[j].pre = d_pre + 3 * (size_t)j;
+            descs[j].host64 = n1 < kLUWideMin;
             if (fp64_first && n1 <= kLUWide64Max) descs[j].wide64 = 1;
         }
         if (plans[j].disjoint) disjoint.push_back(j);
@@ -1177,13 +1268,17 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
         }
     }
     // large systems: factored across the GPU first (lu_solve_refine_kernel then refines them)
-    bool any_wide = false;
+    bool any_wide = false, any_pre = false;
+    for (int j = 0; j < nj; ++j) any_pre |= descs[j].pre != nullptr;
     if (pend) *pend = SolvePending{};
+    if (any_pre) RP_CUDA(cudaMemsetAsync(d_pre, 0, sizeof(double) * 3 * nj, stream));
     for (int j = 0; j < nj; ++j) {
         if (!descs[j].pre) continue;
         if (descs[j].wide64) {
             StageTimer tt(ctx, "solve_lu_wide64", stream);
             lu_wide_factor<double>(ctx, descs[j], plans[j].n + 1, stream);
+        } else if (descs[j].host64) {
+            any_wide = true;  // its flag is read after the launch, as a wide system's
         } else {
             StageTimer tt(ctx, "solve_lu_wide", stream);
             lu_wide_factor<float>(ctx, descs[j], plans[j].n + 1, stream);
