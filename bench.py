@@ -111,6 +111,10 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.rows.append([x.strip() for x in line.split(",")])
 
+    def mark(self):
+        """Samples before this call (the sampler's start-up) are left out of stop()'s figures."""
+        self.first = len(self.rows)
+
     def stop(self) -> dict:
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -123,7 +127,7 @@ class ClockSampler:
             self.thread.join(timeout=5)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        for r in self.rows[getattr(self, "first", 0):]:
             try:
                 sm.append(float(r[0]))
                 smax.append(float(r[1]))
@@ -532,14 +536,16 @@ def main():
                 "table": {str(k): {"phi_atoms": v[0], "gram_points_per_cta": 64 * v[1], "best_ms": round(v[2], 4),
                                    "default_ms": round(v[3], 4), "N": v[4], "M": v[5]} for k, v in table.items()}}
 
-    # warm-up
+    # warm-up (the clock sampler starts here, so that its own start-up, which holds the
+    # driver for a moment, falls outside the timed region)
+    clock = ClockSampler(local)
+    clock.start()
     for _ in range(max(args.warmup, 1)):
         q_mixed, M, info = step()
     torch.cuda.synchronize()
 
     # timed region: K batched steps, events on the stream the library runs on
-    clock = ClockSampler(local)
-    clock.start()
+    clock.mark()
     launches0 = _lib.launch_count()
     barrier(world)
     torch.cuda.synchronize()

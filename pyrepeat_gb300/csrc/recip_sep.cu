@@ -42,6 +42,7 @@ struct RecipJob {
     const float4 *EY, *EZ; // double-float phases of the grid rows / planes
     double2 *U;
     float4 *Udf;
+    float2 *kdf;           // [K] the weights w_k as double-float (hi, lo), split once per fit
     float2 *W, *F, *E;
     double rb[9];          // reciprocal basis (rows)
     int N, ncols, K, P, ny, nz, ab;
@@ -71,6 +72,14 @@ __global__ void atom_phases_kernel(const __grid_constant__ RecipLaunch L) {
     const RecipJob &J = L.job[jb];
     const int P = J.P, nw = 2 * P + 1;
     const int t = (blockIdx.x - L.blk[jb]) * blockDim.x + threadIdx.x;
+    // the weights' double-float split for build_w_kernel, whose threads would otherwise each
+    // run the FP64 conversions (the FP64 pipe is a small fraction of the FP32 rate here)
+    const int nthreads = (L.blk[jb + 1] - L.blk[jb]) * blockDim.x;
+    for (int k = t; k < J.K; k += nthreads) {
+        const double w = J.kcoef[k];
+        const float wh = (float)w;
+        J.kdf[k] = make_float2(wh, (float)(w - (double)wh));
+    }
     if (t >= J.N * 3 * nw) return;
     const int n = t % nw - P, d = (t / nw) % 3, a = t / (3 * nw);
     const double *p = J.atoms + 3 * a;
@@ -108,8 +117,8 @@ __global__ void build_w_kernel(const __grid_constant__ RecipLaunch L) {
         re = im = dfa::acc{0.f, 0.f};
         dfa::cmac(re, im, z12, u[2 * nw + n3]);
         const float4 z3 = dfa::pack(re, im);
-        const double w = J.kcoef[k];
-        const float wh = (float)w, wl = (float)(w - (double)wh);
+        const float2 wk = J.kdf[k];
+        const float wh = wk.x, wl = wk.y;
         re = im = dfa::acc{0.f, 0.f};
         dfa::mac(re, wh, wl, z3.x, z3.y);
         dfa::mac(im, wh, wl, z3.z, z3.w);
@@ -257,7 +266,8 @@ void recip_rows_group(rp_ctx *ctx, const std::vector<RecipRowsJob> &jobs, cudaSt
                       const std::string &tag) {
     if (jobs.empty()) return;
     // scratch of every job in one arena per kind; the W arena is cleared with one memset
-    std::vector<size_t> oW(jobs.size() + 1, 0), oF(jobs.size() + 1, 0), oU(jobs.size() + 1, 0);
+    std::vector<size_t> oW(jobs.size() + 1, 0), oF(jobs.size() + 1, 0), oU(jobs.size() + 1, 0),
+        oK(jobs.size() + 1, 0);
     for (size_t j = 0; j < jobs.size(); ++j) {
         const rp_ewald *ew = jobs[j].ew;
         const int P = std::max(ew->kmax - 1, 0), n1c = P + 1, nw = 2 * P + 1;
@@ -266,12 +276,14 @@ void recip_rows_group(rp_ctx *ctx, const std::vector<RecipRowsJob> &jobs, cudaSt
         oW[j + 1] = oW[j] + (live ? (size_t)ncols * nw * nw * n1c : 0);
         oF[j + 1] = oF[j] + (live ? (size_t)ew->grid.n_grid[2] * nw * ncols * n1c : 0);
         oU[j + 1] = oU[j] + (live ? (size_t)jobs[j].N * 3 * nw : 0);
+        oK[j + 1] = oK[j] + (live ? (size_t)ew->K : 0);
     }
     const size_t nj = jobs.size();
     float2 *W = ctx->buf_t<float2>("rs_W" + tag, std::max<size_t>(oW[nj], 1));
     float2 *F = ctx->buf_t<float2>("rs_F" + tag, std::max<size_t>(oF[nj], 1));
     double2 *U = ctx->buf_t<double2>("rs_U" + tag, std::max<size_t>(oU[nj], 1));
     float4 *Udf = ctx->buf_t<float4>("rs_Udf" + tag, std::max<size_t>(oU[nj], 1));
+    float2 *kdf = ctx->buf_t<float2>("rs_kdf" + tag, std::max<size_t>(oK[nj], 1));
     if (oW[nj]) RP_CUDA(cudaMemsetAsync(W, 0, sizeof(float2) * oW[nj], stream));
     for (size_t j0 = 0; j0 < nj; j0 += kRecipJobs) {
         const size_t j1 = std::min(nj, j0 + kRecipJobs);
@@ -292,7 +304,8 @@ void recip_rows_group(rp_ctx *ctx, const std::vector<RecipRowsJob> &jobs, cudaSt
             RecipJob &J = L.job[L.n];
             J.atoms = rj.d_atoms; J.q = rj.d_q; J.kidx = ew->d_kidx; J.kcoef = ew->d_kcoef;
             J.EY = ew->d_eyf; J.EZ = ew->d_ezf;
-            J.U = U + oU[j]; J.Udf = Udf + oU[j]; J.W = W + oW[j]; J.F = F + oF[j]; J.E = rj.E;
+            J.U = U + oU[j]; J.Udf = Udf + oU[j]; J.kdf = kdf + oK[j]; J.W = W + oW[j]; J.F = F + oF[j];
+            J.E = rj.E;
             for (int q = 0; q < 9; ++q) J.rb[q] = ew->rec[q];
             J.N = rj.N; J.ncols = ncols; J.K = ew->K; J.P = P; J.ny = ny; J.nz = nz; J.ab = stage_b_columns(P);
             const int nb = (n1c + kN1B - 1) / kN1B;

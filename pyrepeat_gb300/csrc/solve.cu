@@ -542,16 +542,15 @@ __device__ double inverse_norm1_estimate(const SolveDesc &d, int n1, bool f32, f
 }
 
 constexpr int kRefineMax = 30;  // and stop early once a step no longer halves the residual
-// systems factored across the GPU (FP32 first, FP64 when the FP32 refinement does not
-// converge): n1 in [kLUWideMin, kLUWideMax], FP64 up to kLUWide64Max; the bounds are the
-// panel rows that fit shared memory at 4 columns
+// systems factored across the GPU (FP32 first by our panels, the bound being the panel rows
+// that fit shared memory at 4 columns; FP64 by cuSOLVER when the FP32 refinement does not
+// converge): n1 in [kLUWideMin, kLUWideMax]
 constexpr int kLUWideMin = 768;
 // systems of kLUHost64Min to kLUWideMin unknowns keep their FP32 factorisation in the CTA, but
 // when its refinement stalls the FP64 factors come from across the GPU (cuSOLVER getrf): an
 // in-CTA FP64 LU of 425 unknowns takes ~13 ms on one SM's FP64 pipe
 constexpr int kLUHost64Min = 256;
 constexpr int kLUWideMax = (int)((225 * 1024) / (sizeof(float) * 5));
-constexpr int kLUWide64Max = (int)((225 * 1024) / (sizeof(double) * 5));
 
 // r = bs - A0 x in FP64: a warp per row, lanes along the row, fixed-order shuffle sum
 __device__ void residual(const SolveDesc &d, int n1) {
@@ -569,6 +568,7 @@ __device__ void residual(const SolveDesc &d, int n1) {
 
 __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *__restrict__ descs) {
     const SolveDesc d = descs[blockIdx.x];
+    if (d.wide64) return;  // FP64 factors and refinement on the host path (factor_refine_wide64)
     const int n1 = d.n + 1;
     extern __shared__ __align__(16) float fsh[];  // [2 * n1]: right-hand side / correction in FP32 (or n1 doubles)
     float *ys = fsh, *xs = fsh + n1;
@@ -644,9 +644,9 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
         __syncthreads();
     }
 
-    // A wide system whose FP32 factors did not converge is factored again in FP64 across the
-    // GPU by the host, which then relaunches it with wide64 set; nothing is written here.
-    if (!done && d.pre && !d.wide64 && n1 <= kLUWide64Max) {
+    // A wide (or mid-size) system whose FP32 factors did not converge is factored in FP64 and
+    // refined by the host path (factor_refine_wide64); nothing is written here.
+    if (!done && d.pre) {
         if (threadIdx.x == 0) d.pre[0] = 2.0;
         return;
     }
@@ -655,11 +655,7 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
     const bool f32_solved = done;
     if (!done) {
         double *A = d.As;
-        if (d.wide64) {  // factored across the GPU (lu_wide_factor<double>)
-            pmin = d.pre[1];
-            pmax = d.pre[2];
-            singular = d.pre[0] != 0.0;
-        } else {
+        {
         for (long long t = threadIdx.x; t < (long long)n1 * n1; t += kLU) A[t] = d.A0[t];
         __syncthreads();
         pmin = 1e308;
@@ -743,7 +739,7 @@ __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *_
         d.info[4] = fmin(anorm * kinv, 1e300);
         d.info[5] = n1;
         d.info[6] = steps;
-        d.info[7] = f32_solved ? ((d.pre && !d.host64) ? 1.0 : 0.0) : (d.wide64 ? 3.0 : 2.0);
+        d.info[7] = f32_solved ? ((d.pre && !d.host64) ? 1.0 : 0.0) : 2.0;
     }
     __syncthreads();
     // expand to all atoms
@@ -924,23 +920,11 @@ inline cublasStatus_t gemm_nn(cublasHandle_t h, int m, int n, int k, const doubl
 }
 
 // ---- FP64 wide factorisation by cuSOLVER's getrf
-// The bordered matrix K is symmetric, so its row-major image is also K read column-major:
-// getrf factors it as P K = L U in column-major storage, which a transpose turns into the
-// row-major unit-lower L and upper U that lu_solve_refine_kernel applies; LAPACK's 1-based
-// row interchanges become d.perm.  Panels factored across the GPU instead of in one CTA each
-// (an FP64 panel of 1851 x 32 costs ~0.25 ms on one SM's FP64 pipe).  The refinement step
-// that follows uses A0 itself, so a Gram that is symmetric only to rounding costs nothing.
-__global__ void transpose_square_kernel(double *__restrict__ A, int n) {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)n * n) return;
-    const int i = (int)(t / n), j = (int)(t - (long long)i * n);
-    if (i < j) {
-        const double x = A[(size_t)i * n + j];
-        A[(size_t)i * n + j] = A[(size_t)j * n + i];
-        A[(size_t)j * n + i] = x;
-    }
-}
-
+// The bordered matrix K is symmetric, so its row-major image is also K read column-major and
+// cuSOLVER's getrf factors it in place (P K = L U, column-major), with its panels across the
+// GPU instead of in one CTA each (an FP64 panel of 1851 x 32 costs ~0.25 ms on one SM's FP64
+// pipe).  The refinement's residuals use A0 itself, so a Gram that is symmetric only to
+// rounding costs nothing.
 // pivot rows to 0-based interchanges, the pivots' range, and an exactly zero pivot replaced by
 // 1e-300 and flagged (the in-CTA FP64 factorisation's rule); one CTA
 __global__ void __launch_bounds__(1024) getrf_finish_kernel(double *__restrict__ LU, int n,
@@ -984,32 +968,148 @@ __global__ void __launch_bounds__(1024) getrf_finish_kernel(double *__restrict__
     }
 }
 
-void lu_wide_factor_getrf(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t stream) {
-    double *L = d.As;
+// vectors of the refinement and of Hager's estimate: mode 0 fills 1/n, 1 takes the signs of v,
+// 2 the unit vector e_j, 3 Higham's alternating vector (-1)^t (1 + t/(n-1)), 4 ones
+__global__ void vec_fill_kernel(double *__restrict__ v, int n, int mode, int j) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    if (mode == 0) v[t] = 1.0 / (double)n;
+    else if (mode == 1) v[t] = v[t] >= 0.0 ? 1.0 : -1.0;
+    else if (mode == 2) v[t] = t == j ? 1.0 : 0.0;
+    else if (mode == 3) v[t] = ((t & 1) ? -1.0 : 1.0) * (1.0 + (double)t / (double)max(n - 1, 1));
+    else v[t] = 1.0;
+}
+
+// ||A||_1 of the folded normal matrix (the first n rows and columns of the bordered A0)
+__global__ void anorm1_kernel(const double *__restrict__ A0, int n, int n1, unsigned long long *__restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    double s = 0.0;
+    for (int r = 0; r < n; ++r) s += fabs(A0[(size_t)r * n1 + c]);
+    atomicMax(out, (unsigned long long)__double_as_longlong(s));  // s >= 0: bits order like values
+}
+
+__global__ void expand_kernel(const double *__restrict__ x, const int *__restrict__ map, int N, double *__restrict__ q) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) q[i] = x[map[i]];
+}
+
+// A system whose FP32 refinement cannot converge (or an escalated fit's, at once): FP64 factors
+// from cuSOLVER's getrf (K is symmetric, so its row-major image read column-major is K itself),
+// one step of FP64 refinement, the residual and Hager's estimate of ||K^-1||_1 (the same steps
+// and vectors as lu_solve_refine_kernel's, with getrs solves and cuBLAS reductions across the
+// GPU instead of triangular solves in one CTA), then the info words and the charges.  Waits.
+void factor_refine_wide64(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t stream) {
+    double *LU = d.As;
     const long long nn = (long long)n1 * n1;
-    lu_copy_kernel<double><<<(int)std::min<long long>(ceil_div(nn, 256), 4096), 256, 0, stream>>>(d.A0, L, nn, d.pre);
-    RP_LAUNCH_CHECK();
-    cusolverDnHandle_t h = ctx->solver();
-    if (cusolverDnSetStream(h, stream) != CUSOLVER_STATUS_SUCCESS) fail(RP_E_CUDA, "cusolverDnSetStream failed");
+    {
+        StageTimer tt(ctx, "solve_lu_wide64", stream);
+        lu_copy_kernel<double><<<(int)std::min<long long>(ceil_div(nn, 256), 4096), 256, 0, stream>>>(d.A0, LU, nn,
+                                                                                                        d.pre);
+        RP_LAUNCH_CHECK();
+    }
+    cusolverDnHandle_t hs = ctx->solver();
+    if (cusolverDnSetStream(hs, stream) != CUSOLVER_STATUS_SUCCESS) fail(RP_E_CUDA, "cusolverDnSetStream failed");
+    cublasHandle_t hb = ctx->blas();
+    RP_CUBLAS(cublasSetStream(hb, stream));
     int lwork = 0;
-    if (cusolverDnDgetrf_bufferSize(h, n1, n1, L, n1, &lwork) != CUSOLVER_STATUS_SUCCESS)
+    if (cusolverDnDgetrf_bufferSize(hs, n1, n1, LU, n1, &lwork) != CUSOLVER_STATUS_SUCCESS)
         fail(RP_E_CUDA, "cusolverDnDgetrf_bufferSize failed");
     double *work = ctx->buf_t<double>("s_getrf_work", (size_t)std::max(lwork, 1));
     int *ipiv = ctx->buf_t<int>("s_getrf_ipiv", (size_t)n1 + 1);  // [n1] pivots, then the info word
-    if (cusolverDnDgetrf(h, n1, n1, L, n1, work, ipiv, ipiv + n1) != CUSOLVER_STATUS_SUCCESS)
-        fail(RP_E_CUDA, "cusolverDnDgetrf failed");
-    transpose_square_kernel<<<(int)ceil_div(nn, 256), 256, 0, stream>>>(L, n1);
+    unsigned long long *anorm_bits = ctx->buf_t<unsigned long long>("s_anorm", 1);
+    {
+        StageTimer tt(ctx, "solve_lu_wide64", stream);
+        if (cusolverDnDgetrf(hs, n1, n1, LU, n1, work, ipiv, ipiv + n1) != CUSOLVER_STATUS_SUCCESS)
+            fail(RP_E_CUDA, "cusolverDnDgetrf failed");
+        getrf_finish_kernel<<<1, 1024, 0, stream>>>(LU, n1, ipiv, d.perm, d.pre);
+        RP_LAUNCH_CHECK();
+    }
+    StageTimer tt(ctx, "solve_refine64", stream);
+    auto solve = [&](double *v) {
+        if (cusolverDnDgetrs(hs, CUBLAS_OP_N, n1, 1, LU, n1, ipiv, v, n1, ipiv + n1) != CUSOLVER_STATUS_SUCCESS)
+            fail(RP_E_CUDA, "cusolverDnDgetrs failed");
+    };
+    const double one = 1.0, minus_one = -1.0;
+    auto residual = [&]() {  // r = bs - A0 x (A0 row-major: its transpose in cuBLAS's terms)
+        RP_CUDA(cudaMemcpyAsync(d.r, d.bs, sizeof(double) * n1, cudaMemcpyDeviceToDevice, stream));
+        RP_CUBLAS(cublasDgemv(hb, CUBLAS_OP_T, n1, n1, &minus_one, d.A0, n1, d.x, 1, &one, d.r, 1));
+    };
+    const int nb = (int)ceil_div(n1, 256);
+    RP_CUDA(cudaMemcpyAsync(d.x, d.bs, sizeof(double) * n1, cudaMemcpyDeviceToDevice, stream));
+    solve(d.x);
+    residual();
+    solve(d.r);
+    RP_CUBLAS(cublasDaxpy(hb, n1, &one, d.r, 1, d.x, 1));
+    residual();
+    int im = 0;
+    RP_CUBLAS(cublasIdamax(hb, n1, d.r, 1, &im));  // 1-based
+    double res = 0.0, pre[3];
+    RP_CUDA(cudaMemcpyAsync(&res, d.r + (im - 1), sizeof(double), cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaMemcpyAsync(pre, d.pre, sizeof(pre), cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaMemsetAsync(anorm_bits, 0, sizeof(unsigned long long), stream));
+    anorm1_kernel<<<(int)ceil_div(std::max(d.n, 1), 256), 256, 0, stream>>>(d.A0, d.n, n1, anorm_bits);
     RP_LAUNCH_CHECK();
-    getrf_finish_kernel<<<1, 1024, 0, stream>>>(L, n1, ipiv, d.perm, d.pre);
+    unsigned long long abits = 0;
+    RP_CUDA(cudaMemcpyAsync(&abits, anorm_bits, sizeof(abits), cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaStreamSynchronize(stream));
+    res = std::fabs(res);
+    double anorm;
+    std::memcpy(&anorm, &abits, sizeof(anorm));
+    // Hager's estimate of ||K^-1||_1 (K symmetric: K^-T = K^-1), on d.r
+    auto asum = [&]() {
+        double v = 0.0;
+        RP_CUBLAS(cublasDasum(hb, n1, d.r, 1, &v));
+        return v;
+    };
+    double *ones = ctx->buf_t<double>("s_ones", (size_t)n1);
+    vec_fill_kernel<<<nb, 256, 0, stream>>>(ones, n1, 4, 0);
+    vec_fill_kernel<<<nb, 256, 0, stream>>>(d.r, n1, 0, 0);
+    solve(d.r);
+    double est = asum();
+    int jprev = -1;
+    for (int it = 0; it < 4; ++it) {
+        vec_fill_kernel<<<nb, 256, 0, stream>>>(d.r, n1, 1, 0);
+        solve(d.r);
+        int jm = 0;
+        RP_CUBLAS(cublasIdamax(hb, n1, d.r, 1, &jm));
+        const int j = jm - 1;
+        double zj = 0.0, ztx = 0.0;
+        RP_CUDA(cudaMemcpyAsync(&zj, d.r + j, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        if (jprev >= 0) RP_CUDA(cudaMemcpyAsync(&ztx, d.r + jprev, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        double zsum = 0.0;
+        RP_CUBLAS(cublasDdot(hb, n1, d.r, 1, ones, 1, &zsum));
+        RP_CUDA(cudaStreamSynchronize(stream));
+        if (jprev < 0) ztx = zsum / (double)n1;
+        if (!(std::fabs(zj) > ztx)) break;
+        vec_fill_kernel<<<nb, 256, 0, stream>>>(d.r, n1, 2, j);
+        solve(d.r);
+        const double bval = asum();
+        if (!(bval > est)) break;
+        est = bval;
+        jprev = j;
+    }
+    vec_fill_kernel<<<nb, 256, 0, stream>>>(d.r, n1, 3, 0);
+    solve(d.r);
+    est = std::max(est, 2.0 * asum() / (3.0 * (double)n1));
+    const double kinv = est < 1e300 ? est : 1e300;
+    double *hinfo = static_cast<double *>(ctx->host_buf("s_info64", sizeof(double) * kSolveInfo));
+    hinfo[0] = res;
+    hinfo[1] = pre[1];
+    hinfo[2] = pre[2];
+    hinfo[3] = pre[0];
+    hinfo[4] = std::fmin(anorm * kinv, 1e300);
+    hinfo[5] = n1;
+    hinfo[6] = 1;
+    hinfo[7] = 3.0;  // FP64 factors from across the GPU
+    RP_CUDA(cudaMemcpyAsync(d.info, hinfo, sizeof(double) * kSolveInfo, cudaMemcpyHostToDevice, stream));
+    expand_kernel<<<(int)ceil_div(d.N, 256), 256, 0, stream>>>(d.x, d.map, d.N, d.q);
     RP_LAUNCH_CHECK();
+    RP_CUDA(cudaStreamSynchronize(stream));  // the pinned info words are reused by the next system
 }
 
 template <typename T>
 void lu_wide_factor(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t stream) {
-    if (sizeof(T) == 8) {
-        lu_wide_factor_getrf(ctx, d, n1, stream);
-        return;
-    }
     smem_optin((const void *)lu_panel_kernel<T>, kPanelSmem);
     T *L = reinterpret_cast<T *>(d.As);
     const long long nn = (long long)n1 * n1;
@@ -1202,7 +1302,7 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
         if (n1 >= kLUHost64Min && n1 <= kLUWideMax) {
             descs[j].pre = d_pre + 3 * (size_t)j;
             descs[j].host64 = n1 < kLUWideMin;
-            if (fp64_first && n1 <= kLUWide64Max) descs[j].wide64 = 1;
+            if (fp64_first) descs[j].wide64 = 1;
         }
         if (plans[j].disjoint) disjoint.push_back(j);
     }
@@ -1273,11 +1373,8 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
     if (pend) *pend = SolvePending{};
     if (any_pre) RP_CUDA(cudaMemsetAsync(d_pre, 0, sizeof(double) * 3 * nj, stream));
     for (int j = 0; j < nj; ++j) {
-        if (!descs[j].pre) continue;
-        if (descs[j].wide64) {
-            StageTimer tt(ctx, "solve_lu_wide64", stream);
-            lu_wide_factor<double>(ctx, descs[j], plans[j].n + 1, stream);
-        } else if (descs[j].host64) {
+        if (!descs[j].pre || descs[j].wide64) continue;  // wide64: factored and refined after the launch
+        if (descs[j].host64) {
             any_wide = true;  // its flag is read after the launch, as a wide system's
         } else {
             StageTimer tt(ctx, "solve_lu_wide", stream);
@@ -1293,6 +1390,8 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
         lu_solve_refine_kernel<<<nj, kLU, solve_smem_bytes(n1max), stream>>>(d_desc);
         RP_LAUNCH_CHECK();
     }
+    for (int j = 0; j < nj; ++j)  // systems known to need FP64 (an escalated fit): getrf, host-driven refinement
+        if (descs[j].wide64) factor_refine_wide64(ctx, descs[j], plans[j].n + 1, stream);
     double *h_info = static_cast<double *>(ctx->host_buf("s_info" + tag, sizeof(double) * kSolveInfo * nj));
     if (any_wide) {
         // wide systems whose FP32 refinement did not converge (flag 2) are factored again in FP64:
@@ -1323,27 +1422,13 @@ void solve_wide_fp64(rp_ctx *ctx, SolvePending &pd, cudaStream_t stream) {
     if (!pd.any_wide) return;
     pd.any_wide = false;
     const int nj = (int)pd.descs.size();
-    std::vector<SolveDesc> redo;
-    int n1max = 1;
+    bool any = false;
     for (int j = 0; j < nj; ++j) {
         if (!pd.descs[j].pre || pd.h_pre[3 * j] != 2.0) continue;
-        SolveDesc d = pd.descs[j];
-        d.wide64 = 1;
-        StageTimer tt(ctx, "solve_lu_wide64", stream);
-        lu_wide_factor<double>(ctx, d, pd.n1[j], stream);
-        redo.push_back(d);
-        n1max = std::max(n1max, pd.n1[j]);
+        factor_refine_wide64(ctx, pd.descs[j], pd.n1[j], stream);
+        any = true;
     }
-    if (redo.empty()) return;
-    SolveDesc *d_redo = ctx->buf_t<SolveDesc>("s_desc64" + pd.tag, redo.size());
-    SolveDesc *h_redo = static_cast<SolveDesc *>(ctx->host_buf("s_stage64" + pd.tag, sizeof(SolveDesc) * redo.size()));
-    std::memcpy(h_redo, redo.data(), sizeof(SolveDesc) * redo.size());
-    RP_CUDA(cudaMemcpyAsync(d_redo, h_redo, sizeof(SolveDesc) * redo.size(), cudaMemcpyHostToDevice, stream));
-    {
-        StageTimer tt(ctx, "solve_lu", stream);
-        lu_solve_refine_kernel<<<(int)redo.size(), kLU, solve_smem_bytes(n1max), stream>>>(d_redo);
-        RP_LAUNCH_CHECK();
-    }
+    if (!any) return;
     RP_CUDA(cudaMemcpyAsync(pd.h_info, pd.d_info, sizeof(double) * kSolveInfo * nj, cudaMemcpyDeviceToHost, stream));
     RP_CUDA(cudaStreamSynchronize(stream));
 }
