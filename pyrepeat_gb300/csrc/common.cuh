@@ -555,6 +555,7 @@ struct SolveDesc {
     int wide64;           // As holds wide FP64 factors: skip the FP32 stage and the in-CTA FP64 LU
     int host64;           // FP32 factors in the CTA, but a stalled refinement goes to the host's FP64
                           // factorisation across the GPU (pre holds its flag) instead of an in-CTA FP64 LU
+    int host32;           // wide FP32 factors refined on the host path (refine_wide32): the kernel skips it
 };
 // Wide systems of a solve launch whose FP32 refinement may not have converged: their flags are
 // on their way to pinned memory; solve_wide_fp64 (after the stream has reached them) factors
@@ -565,6 +566,7 @@ struct SolvePending {
     double *h_pre = nullptr, *h_info = nullptr, *d_info = nullptr;
     std::vector<SolveDesc> descs;
     std::vector<int> n1;
+    std::vector<int> refine32;  // systems with wide FP32 factors, refined on the host path
 };
 // The same without waiting: returns the pinned host copy of the kSolveInfo words per job, valid
 // once `stream` has reached this point.  `tag` keeps the scratch of solves in flight apart.

@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(const __grid_co
                                                                   int write_counts) {
     __shared__ float4 cand[kCullCap];
     __shared__ int cidx[kCullCap];
-    __shared__ int ncand;
+    __shared__ int ncand, covered;
     __shared__ float box[6];
     __shared__ int row_t0[kCullRows], row_pre[kCullRows + 1];
     const int jb = filter_job_of(L, blockIdx.x);
@@ -233,6 +233,7 @@ __global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(const __grid_co
                 box[3 + q] = v[3 + q] + pad;
             }
             ncand = 0;
+            covered = 0;
         }
     }
     __syncthreads();
@@ -254,8 +255,16 @@ __global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(const __grid_co
     // the images of those bins: a contiguous run of the cell list per (y, z) bin row; the rows'
     // runs are concatenated (prefix in shared memory) and shared out over the threads
     const int ry = c1[1] - c0[1] + 1, R = ry * (c1[2] - c0[2] + 1);
+    // A brick whose farthest point lies strictly inside an exclusion sphere (by the FP32 rule's
+    // margin, and a relative 1e-4 more for the order of the FP32 operations) loses all its
+    // points to that image: every point's FP32 distance is at most the box's farthest, so the
+    // per-point loop would reject each of them by the same test.
     auto cull = [&](int a) {
         const float4 e = eff[a];
+        const float fx = fmaxf(fabsf(e.x - lo[0]), fabsf(e.x - hi[0]));
+        const float fy = fmaxf(fabsf(e.y - lo[1]), fabsf(e.y - hi[1]));
+        const float fz = fmaxf(fabsf(e.z - lo[2]), fabsf(e.z - hi[2]));
+        if (fx * fx + fy * fy + fz * fz <= (e.w - p.err_min) * 0.9999f) covered = 1;
         const float dx = fmaxf(fmaxf(lo[0] - e.x, e.x - hi[0]), 0.f);
         const float dy = fmaxf(fmaxf(lo[1] - e.y, e.y - hi[1]), 0.f);
         const float dz = fmaxf(fmaxf(lo[2] - e.z, e.z - hi[2]), 0.f);
@@ -316,7 +325,9 @@ __global__ void __launch_bounds__(kBrickPts) filter_brick_kernel(const __grid_co
     const int nc = ncand;
     int keep = 0;
     unsigned nre = 0;
-    if (inside) {
+    if (inside && covered) {
+        J.mask[(long long)i + (long long)p.nx * (j + (long long)p.ny * k)] = 0;
+    } else if (inside) {
         bool valid = true;
         if (nc <= kCullCap) {
             for (int c = 0; c < nc; ++c) {

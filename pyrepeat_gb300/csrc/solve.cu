@@ -568,7 +568,7 @@ __device__ void residual(const SolveDesc &d, int n1) {
 
 __global__ void __launch_bounds__(kLU) lu_solve_refine_kernel(const SolveDesc *__restrict__ descs) {
     const SolveDesc d = descs[blockIdx.x];
-    if (d.wide64) return;  // FP64 factors and refinement on the host path (factor_refine_wide64)
+    if (d.wide64 || d.host32) return;  // refined on the host path (factor_refine_wide64, refine_wide32)
     const int n1 = d.n + 1;
     extern __shared__ __align__(16) float fsh[];  // [2 * n1]: right-hand side / correction in FP32 (or n1 doubles)
     float *ys = fsh, *xs = fsh + n1;
@@ -1108,6 +1108,174 @@ void factor_refine_wide64(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t 
     RP_CUDA(cudaStreamSynchronize(stream));  // the pinned info words are reused by the next system
 }
 
+// ---- host-driven refinement with wide FP32 factors
+// The refinement of lu_solve_refine_kernel for a system whose FP32 factors were computed across
+// the GPU (lu_wide_factor<float>): the same steps (scaled FP32 corrections, FP64 residuals, the
+// backward-error stop, the stall rule) and the same condition estimate, with cuBLAS DGEMV
+// residuals and STRSV solves across the GPU instead of one CTA's (whose FP64 residual alone takes
+// ~1 ms on one SM's FP64 pipe at 2001 unknowns).  Returns false when the refinement stalls: the
+// caller then factors the system in FP64 (factor_refine_wide64).  Waits.
+
+// y (FP32) = v / scale, or v with non-finite values as they are (scale 0: plain conversion)
+__global__ void to_f32_kernel(const double *__restrict__ v, int n, double scale, float *__restrict__ y) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) y[t] = (float)(scale != 0.0 ? v[t] / scale : v[t]);
+}
+// mode 0: x += y * scale;  mode 1: x = finite(y) ? y : 1e300 (the estimate's solves)
+__global__ void from_f32_kernel(const float *__restrict__ y, int n, double scale, int mode, double *__restrict__ x) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    if (mode == 0) x[t] += (double)y[t] * scale;
+    else x[t] = isfinite(y[t]) ? (double)y[t] : 1e300;
+}
+// the factorisation's row interchanges applied to y in order (one CTA, in shared memory)
+__global__ void __launch_bounds__(1024) swap_rows_kernel(float *__restrict__ y, const int *__restrict__ perm, int n) {
+    extern __shared__ float ysm[];
+    for (int t = threadIdx.x; t < n; t += blockDim.x) ysm[t] = y[t];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < n; ++k) {
+            const int p = perm[k];
+            if (p != k) { const float v = ysm[k]; ysm[k] = ysm[p]; ysm[p] = v; }
+        }
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += blockDim.x) y[t] = ysm[t];
+}
+// max row sum |A0| (the backward-error bound's ||A||)
+__global__ void rowabs_max_kernel(const double *__restrict__ A0, int n1, unsigned long long *__restrict__ out) {
+    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (r >= n1) return;
+    double s = 0.0;
+    for (int c = lane; c < n1; c += 32) s += fabs(A0[(size_t)r * n1 + c]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) atomicMax(out, (unsigned long long)__double_as_longlong(s));
+}
+
+bool refine_wide32(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t stream) {
+    StageTimer tt(ctx, "solve_refine32", stream);
+    const float *LU = reinterpret_cast<const float *>(d.As);
+    cublasHandle_t hb = ctx->blas();
+    RP_CUBLAS(cublasSetStream(hb, stream));
+    float *ys = ctx->buf_t<float>("s_r32_y", (size_t)n1);
+    unsigned long long *bits = ctx->buf_t<unsigned long long>("s_r32_bits", 2);
+    const int nb = (int)ceil_div(n1, 256);
+    // pivot range and zero-pivot flag of the wide FP32 factorisation, ||A0|| (rows)
+    double pre[3];
+    RP_CUDA(cudaMemcpyAsync(pre, d.pre, sizeof(pre), cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaMemsetAsync(bits, 0, 2 * sizeof(unsigned long long), stream));
+    rowabs_max_kernel<<<(int)ceil_div(n1, 8), 256, 0, stream>>>(d.A0, n1, bits);
+    RP_LAUNCH_CHECK();
+    if (d.n > 0) {
+        anorm1_kernel<<<(int)ceil_div(d.n, 256), 256, 0, stream>>>(d.A0, d.n, n1, bits + 1);
+        RP_LAUNCH_CHECK();
+    }
+    unsigned long long hbits[2] = {0, 0};
+    RP_CUDA(cudaMemcpyAsync(hbits, bits, sizeof(hbits), cudaMemcpyDeviceToHost, stream));
+    RP_CUDA(cudaStreamSynchronize(stream));
+    if (pre[0] != 0.0) return false;  // a zero FP32 pivot: FP64 takes over
+    double an, anorm;
+    std::memcpy(&an, &hbits[0], sizeof(an));
+    std::memcpy(&anorm, &hbits[1], sizeof(anorm));
+    auto apply = [&]() {  // ys = (P L U)^-1 ys in FP32
+        swap_rows_kernel<<<1, 1024, sizeof(float) * (size_t)n1, stream>>>(ys, d.perm, n1);
+        RP_LAUNCH_CHECK();
+        RP_CUBLAS(cublasStrsv(hb, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_UNIT, n1, LU, n1, ys, 1));
+        RP_CUBLAS(cublasStrsv(hb, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n1, LU, n1, ys, 1));
+    };
+    auto absmax = [&](const double *v) {
+        int im = 0;
+        RP_CUBLAS(cublasIdamax(hb, n1, v, 1, &im));
+        double x = 0.0;
+        RP_CUDA(cudaMemcpyAsync(&x, v + (im - 1), sizeof(double), cudaMemcpyDeviceToHost, stream));
+        RP_CUDA(cudaStreamSynchronize(stream));
+        return std::fabs(x);
+    };
+    const double one = 1.0, minus_one = -1.0;
+    RP_CUDA(cudaMemsetAsync(d.x, 0, sizeof(double) * n1, stream));
+    RP_CUDA(cudaMemcpyAsync(d.r, d.bs, sizeof(double) * n1, cudaMemcpyDeviceToDevice, stream));
+    bool done = false;
+    double res = 0.0, rprev = 1e308;
+    int steps = 0;
+    for (int it = 0; it < kRefineMax && !done; ++it) {
+        const double rm = absmax(d.r);
+        if (rm == 0.0) {
+            done = true;
+            break;
+        }
+        ++steps;
+        to_f32_kernel<<<nb, 256, 0, stream>>>(d.r, n1, rm, ys);
+        RP_LAUNCH_CHECK();
+        apply();
+        from_f32_kernel<<<nb, 256, 0, stream>>>(ys, n1, rm, 0, d.x);
+        RP_LAUNCH_CHECK();
+        RP_CUDA(cudaMemcpyAsync(d.r, d.bs, sizeof(double) * n1, cudaMemcpyDeviceToDevice, stream));
+        RP_CUBLAS(cublasDgemv(hb, CUBLAS_OP_T, n1, n1, &minus_one, d.A0, n1, d.x, 1, &one, d.r, 1));
+        const double rn = absmax(d.r), xn = absmax(d.x);
+        res = rn;
+        if (rn <= (double)n1 * 1.1102230246251565e-16 * an * xn) done = true;
+        else if (it >= 2 && rn > 0.5 * rprev) break;  // stalled: FP64 takes over
+        rprev = rn;
+    }
+    if (!done) return false;
+    // Hager's estimate of ||K^-1||_1 with the FP32 factors (lu_solve_refine_kernel's steps)
+    auto solve_r = [&]() {
+        to_f32_kernel<<<nb, 256, 0, stream>>>(d.r, n1, 0.0, ys);
+        RP_LAUNCH_CHECK();
+        apply();
+        from_f32_kernel<<<nb, 256, 0, stream>>>(ys, n1, 0.0, 1, d.r);
+        RP_LAUNCH_CHECK();
+    };
+    auto asum = [&]() {
+        double v = 0.0;
+        RP_CUBLAS(cublasDasum(hb, n1, d.r, 1, &v));
+        return v;
+    };
+    double *ones = ctx->buf_t<double>("s_ones", (size_t)n1);
+    vec_fill_kernel<<<nb, 256, 0, stream>>>(ones, n1, 4, 0);
+    vec_fill_kernel<<<nb, 256, 0, stream>>>(d.r, n1, 0, 0);
+    solve_r();
+    double est = asum();
+    int jprev = -1;
+    for (int it = 0; it < 4; ++it) {
+        vec_fill_kernel<<<nb, 256, 0, stream>>>(d.r, n1, 1, 0);
+        solve_r();
+        int jm = 0;
+        RP_CUBLAS(cublasIdamax(hb, n1, d.r, 1, &jm));
+        const int j = jm - 1;
+        double zj = 0.0, ztx = 0.0, zsum = 0.0;
+        RP_CUDA(cudaMemcpyAsync(&zj, d.r + j, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        if (jprev >= 0) RP_CUDA(cudaMemcpyAsync(&ztx, d.r + jprev, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        RP_CUBLAS(cublasDdot(hb, n1, d.r, 1, ones, 1, &zsum));
+        RP_CUDA(cudaStreamSynchronize(stream));
+        if (jprev < 0) ztx = zsum / (double)n1;
+        if (!(std::fabs(zj) > ztx)) break;
+        vec_fill_kernel<<<nb, 256, 0, stream>>>(d.r, n1, 2, j);
+        solve_r();
+        const double bval = asum();
+        if (!(bval > est)) break;
+        est = bval;
+        jprev = j;
+    }
+    vec_fill_kernel<<<nb, 256, 0, stream>>>(d.r, n1, 3, 0);
+    solve_r();
+    est = std::max(est, 2.0 * asum() / (3.0 * (double)n1));
+    const double kinv = est < 1e300 ? est : 1e300;
+    double *hinfo = static_cast<double *>(ctx->host_buf("s_info32", sizeof(double) * kSolveInfo));
+    hinfo[0] = res;
+    hinfo[1] = pre[1];
+    hinfo[2] = pre[2];
+    hinfo[3] = 0.0;
+    hinfo[4] = std::fmin(anorm * kinv, 1e300);
+    hinfo[5] = n1;
+    hinfo[6] = steps;
+    hinfo[7] = 1.0;  // FP32 factors from across the GPU
+    RP_CUDA(cudaMemcpyAsync(d.info, hinfo, sizeof(double) * kSolveInfo, cudaMemcpyHostToDevice, stream));
+    expand_kernel<<<(int)ceil_div(d.N, 256), 256, 0, stream>>>(d.x, d.map, d.N, d.q);
+    RP_LAUNCH_CHECK();
+    RP_CUDA(cudaStreamSynchronize(stream));  // the pinned info words are reused by the next system
+    return true;
+}
+
 template <typename T>
 void lu_wide_factor(rp_ctx *ctx, const SolveDesc &d, int n1, cudaStream_t stream) {
     smem_optin((const void *)lu_panel_kernel<T>, kPanelSmem);
@@ -1303,6 +1471,7 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
             descs[j].pre = d_pre + 3 * (size_t)j;
             descs[j].host64 = n1 < kLUWideMin;
             if (fp64_first) descs[j].wide64 = 1;
+            else if (n1 >= kLUWideMin) descs[j].host32 = 1;
         }
         if (plans[j].disjoint) disjoint.push_back(j);
     }
@@ -1392,6 +1561,9 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
     }
     for (int j = 0; j < nj; ++j)  // systems known to need FP64 (an escalated fit): getrf, host-driven refinement
         if (descs[j].wide64) factor_refine_wide64(ctx, descs[j], plans[j].n + 1, stream);
+    std::vector<int> refine32;
+    for (int j = 0; j < nj; ++j)
+        if (descs[j].host32) refine32.push_back(j);
     double *h_info = static_cast<double *>(ctx->host_buf("s_info" + tag, sizeof(double) * kSolveInfo * nj));
     if (any_wide) {
         // wide systems whose FP32 refinement did not converge (flag 2) are factored again in FP64:
@@ -1409,6 +1581,7 @@ const double *solve_batch_async(rp_ctx *ctx, const std::vector<SolveJob> &jobs, 
         pd.descs = descs;
         pd.n1.resize((size_t)nj);
         for (int j = 0; j < nj; ++j) pd.n1[j] = plans[j].n + 1;
+        pd.refine32 = refine32;
         if (!pend) {
             RP_CUDA(cudaStreamSynchronize(stream));
             solve_wide_fp64(ctx, pd, stream);
@@ -1423,8 +1596,13 @@ void solve_wide_fp64(rp_ctx *ctx, SolvePending &pd, cudaStream_t stream) {
     pd.any_wide = false;
     const int nj = (int)pd.descs.size();
     bool any = false;
+    for (int j : pd.refine32) {  // wide FP32 factors: refined here, FP64 factors when that stalls
+        if (!refine_wide32(ctx, pd.descs[j], pd.n1[j], stream)) factor_refine_wide64(ctx, pd.descs[j], pd.n1[j], stream);
+        any = true;
+    }
+    pd.refine32.clear();
     for (int j = 0; j < nj; ++j) {
-        if (!pd.descs[j].pre || pd.h_pre[3 * j] != 2.0) continue;
+        if (!pd.descs[j].pre || pd.descs[j].host32 || pd.h_pre[3 * j] != 2.0) continue;
         factor_refine_wide64(ctx, pd.descs[j], pd.n1[j], stream);
         any = true;
     }
