@@ -15,6 +15,7 @@
 #include <cmath>
 
 #include "common.cuh"
+#include "df.cuh"
 
 namespace rp {
 namespace {
@@ -283,8 +284,9 @@ __global__ void shifted_sums_kernel(const double *__restrict__ sphi, const doubl
 }
 
 // ---- FP64 separable reciprocal sum (the escalated fit) ----
-// The transform of recip_sep.cu with every product and sum in FP64: with the exact
-// per-axis lattice phases ex, ey, ez of the grid (tables of the Ewald object) and
+// The transform of recip_sep.cu in FP64 (stage B in double-float, ~2^-46 relative, on the
+// FP32 pipe): with the exact per-axis lattice phases ex, ey, ez of the grid (tables of the
+// Ewald object) and
 // W_a(n) = w_k e^{-i k.r_a},
 //   F[l][n2][a][n1] = sum_n3 ez[n3][l] W[n2][n3][a][n1]      (every grid plane l)
 //   E[r][a][n1]     = sum_n2 ey[n2][j_r] F[l_r][n2][a][n1]    (the rows r that hold kept points)
@@ -328,9 +330,9 @@ __global__ void build_w64_kernel(const int *__restrict__ kidx, const double *__r
     W[(((size_t)n2 * nw + n3) * N + a) * n1c + n1] = make_double2(w * v.x, w * v.y);
 }
 
-// stage A: one thread per (l, n2, a, n1), n1 fastest
+// stage A: one thread per (l, n2, a, n1), n1 fastest; F is stored as double-float for stage B
 __global__ void stage_a64_kernel(const double2 *__restrict__ W, const double2 *__restrict__ ez, int nz, int N,
-                                 int P, int kmax, double2 *__restrict__ F) {
+                                 int P, int kmax, float4 *__restrict__ F) {
     const int nw = 2 * P + 1, n1c = P + 1;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nz * nw * N * n1c) return;
@@ -344,26 +346,24 @@ __global__ void stage_a64_kernel(const double2 *__restrict__ W, const double2 *_
         re += z.x * v.x - z.y * v.y;
         im += z.x * v.y + z.y * v.x;
     }
-    F[t] = make_double2(re, im);
+    F[t] = dfa::split(re, im);
 }
 
-// stage B over the listed rows (row = j + l ny): one thread per (row, a, n1), n1 fastest
-__global__ void stage_b64_kernel(const double2 *__restrict__ F, const double2 *__restrict__ ey, int ny, int N,
-                                 int P, int kmax, const int *__restrict__ rows, int R, double2 *__restrict__ E) {
+// stage B over the listed rows (row = j + l ny): one thread per (row, a, n1), n1 fastest.  In
+// double-float on the FP32 pipe (~2^-46 relative, dfa::cmac) from the double-float phases and F:
+// the FP64 pipe is a small fraction of the FP32 rate here, and this stage is most of the sum's
+// work on a sparse cube (29 GFLOP on the 2000-atom triclinic one); E is stored in FP64.
+__global__ void stage_b64_kernel(const float4 *__restrict__ F, const float4 *__restrict__ eyf, int ny, int N,
+                                 int P, const int *__restrict__ rows, int R, double2 *__restrict__ E) {
     const int nw = 2 * P + 1, n1c = P + 1;
     const long long an = (long long)N * n1c;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)R * an) return;
     const int ri = (int)(t / an), r = (int)(t - (long long)ri * an);
     const int row = rows[ri], l = row / ny, j = row - l * ny;
-    double re = 0.0, im = 0.0;
-    for (int n2 = 0; n2 < nw; ++n2) {
-        const double2 y = ey[(size_t)(n2 - P + kmax) * ny + j];
-        const double2 f = F[((size_t)l * nw + n2) * an + r];
-        re += y.x * f.x - y.y * f.y;
-        im += y.x * f.y + y.y * f.x;
-    }
-    E[t] = make_double2(re, im);
+    dfa::acc re{0.f, 0.f}, im{0.f, 0.f};
+    for (int n2 = 0; n2 < nw; ++n2) dfa::cmac(re, im, eyf[(size_t)n2 * ny + j], F[((size_t)l * nw + n2) * an + r]);
+    E[t] = make_double2(dfa::to_double(re), dfa::to_double(im));
 }
 
 // mark the grid rows that hold kept points m0 .. m0+rows-1
@@ -438,12 +438,12 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
     const int nx = ew->grid.n_grid[0], ny = ew->grid.n_grid[1], nz = ew->grid.n_grid[2];
     const bool sep = separable && K > 0 && kp >= 0;
     double *B = nullptr;
-    double2 *F64 = nullptr;
+    float4 *F64 = nullptr;
     if (sep) {
         StageTimer tt(ctx, "fp64_recip_sep", stream);
         double2 *U = ctx->buf_t<double2>("g64_U", (size_t)N * 3 * nw);
         double2 *W = ctx->buf_t<double2>("g64_W", (size_t)nw * nw * N * n1c);
-        F64 = ctx->buf_t<double2>("g64_F", (size_t)nz * nw * N * n1c);
+        F64 = ctx->buf_t<float4>("g64_F", (size_t)nz * nw * N * n1c);
         RP_CUDA(cudaMemsetAsync(W, 0, sizeof(double2) * (size_t)nw * nw * N * n1c, stream));
         RecBasis rb;
         for (int q = 0; q < 9; ++q) rb.rb[q] = ew->rec[q];
@@ -507,8 +507,8 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
             RP_CUDA(cudaMemcpyAsync(rowmap, hmap, sizeof(int) * nrows, cudaMemcpyHostToDevice, stream));
             RP_CUDA(cudaMemcpyAsync(rowlist, hlist, sizeof(int) * R, cudaMemcpyHostToDevice, stream));
             double2 *E64 = ctx->buf_t<double2>("g64_E", (size_t)std::max(R, 1) * N * n1c);
-            stage_b64_kernel<<<ceil_div((long long)R * N * n1c, 128), 128, 0, stream>>>(F64, ew->d_ey, ny, N, kp,
-                                                                                       ew->kmax, rowlist, R, E64);
+            stage_b64_kernel<<<ceil_div((long long)R * N * n1c, 128), 128, 0, stream>>>(F64, ew->d_eyf, ny, N, kp,
+                                                                                       rowlist, R, E64);
             RP_LAUNCH_CHECK();
             stage_c64_kernel<<<ceil_div(rows * N, 128), 128, 0, stream>>>(E64, ew->d_ex, nx, N, kp, kept_idx_dev, m0,
                                                                           rows, rowmap, P);

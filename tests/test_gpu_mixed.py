@@ -218,8 +218,8 @@ def test_potential_matches_phi_q(gpu_ctx, oracle_mod):
 @pytest.mark.parametrize("N", [300, 900])
 def test_bordered_solve_ill_conditioned_takes_fp64(gpu_ctx, N):
     """cond(A) = 1e10, beyond what FP32 factors can refine: the FP64 factorisation takes over
-    (one CTA below 768 unknowns, across the GPU above) and the charges match an FP64 LU of
-    the same bordered system to cond x eps."""
+    (cuSOLVER's getrf for 256 or more unknowns, refined on the host path; one CTA below) and
+    the charges match an FP64 LU of the same bordered system to cond x eps."""
     import scipy.linalg as sl
     import torch
     rng = np.random.default_rng(7 + N)
@@ -244,7 +244,8 @@ def test_bordered_solve_large_systems(gpu_ctx, N):
     """The bordered solve on systems of many panels against an FP64 LU of the same
     bordered system: the one-CTA blocked FP32 LU (N + 1 < 768) and the wide factorisation
     across the GPU (panels of 32 columns, of 16 while the panel has more than 1745 rows and
-    of 8 past 3388, cuBLAS trailing updates), both with FP64 refinement."""
+    of 8 past 3388, cuBLAS trailing updates), both with FP64 refinement (the wide systems'
+    on the host path: cuBLAS DGEMV residuals and STRSV solves)."""
     import scipy.linalg as sl
     import torch
     rng = np.random.default_rng(N)
