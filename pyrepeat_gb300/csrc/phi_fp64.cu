@@ -284,9 +284,10 @@ __global__ void shifted_sums_kernel(const double *__restrict__ sphi, const doubl
 }
 
 // ---- FP64 separable reciprocal sum (the escalated fit) ----
-// The transform of recip_sep.cu in FP64 (stage B in double-float, ~2^-46 relative, on the
-// FP32 pipe): with the exact per-axis lattice phases ex, ey, ez of the grid (tables of the
-// Ewald object) and
+// The transform of recip_sep.cu at FP64-level accuracy: stages A and B in double-float
+// (~2^-46 relative, on the FP32 pipe, whose rate is many times the FP64 pipe's here), the
+// weights and stage C in FP64; with the exact per-axis lattice phases ex, ey, ez of the grid
+// (tables of the Ewald object) and
 // W_a(n) = w_k e^{-i k.r_a},
 //   F[l][n2][a][n1] = sum_n3 ez[n3][l] W[n2][n3][a][n1]      (every grid plane l)
 //   E[r][a][n1]     = sum_n2 ey[n2][j_r] F[l_r][n2][a][n1]    (the rows r that hold kept points)
@@ -316,9 +317,10 @@ __device__ __forceinline__ double2 cmul64(double2 x, double2 y) {
     return make_double2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
 }
 
-// W[n2'][n3'][a][n1] = w_k e^{-i k.r_a} for the k-set (zero elsewhere: cleared before)
+// W[n2'][n3'][a][n1] = w_k e^{-i k.r_a} for the k-set (zero elsewhere: cleared before), from
+// FP64 phase products, stored as double-float for stage A
 __global__ void build_w64_kernel(const int *__restrict__ kidx, const double *__restrict__ kcoef, int K, int N,
-                                 int P, const double2 *__restrict__ U, double2 *__restrict__ W) {
+                                 int P, const double2 *__restrict__ U, float4 *__restrict__ W) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)N * K) return;
     const int a = (int)(t / K), k = (int)(t - (long long)a * K);
@@ -327,26 +329,22 @@ __global__ void build_w64_kernel(const int *__restrict__ kidx, const double *__r
     const double2 *u = U + (size_t)a * 3 * nw;
     const double2 v = cmul64(cmul64(u[n1 + P], u[nw + n2]), u[2 * nw + n3]);
     const double w = kcoef[k];
-    W[(((size_t)n2 * nw + n3) * N + a) * n1c + n1] = make_double2(w * v.x, w * v.y);
+    W[(((size_t)n2 * nw + n3) * N + a) * n1c + n1] = dfa::split(w * v.x, w * v.y);
 }
 
-// stage A: one thread per (l, n2, a, n1), n1 fastest; F is stored as double-float for stage B
-__global__ void stage_a64_kernel(const double2 *__restrict__ W, const double2 *__restrict__ ez, int nz, int N,
-                                 int P, int kmax, float4 *__restrict__ F) {
+// stage A: one thread per (l, n2, a, n1), n1 fastest, in double-float (dfa::cmac) from the
+// double-float phases and W; F is stored as double-float for stage B
+__global__ void stage_a64_kernel(const float4 *__restrict__ W, const float4 *__restrict__ ezf, int nz, int N,
+                                 int P, float4 *__restrict__ F) {
     const int nw = 2 * P + 1, n1c = P + 1;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nz * nw * N * n1c) return;
     const long long an = (long long)N * n1c;
     const int r = (int)(t % an);           // a n1c + n1
     const int n2 = (int)((t / an) % nw), l = (int)(t / (an * nw));
-    double re = 0.0, im = 0.0;
-    for (int n3 = 0; n3 < nw; ++n3) {
-        const double2 z = ez[(size_t)(n3 - P + kmax) * nz + l];
-        const double2 v = W[((size_t)n2 * nw + n3) * an + r];
-        re += z.x * v.x - z.y * v.y;
-        im += z.x * v.y + z.y * v.x;
-    }
-    F[t] = dfa::split(re, im);
+    dfa::acc re{0.f, 0.f}, im{0.f, 0.f};
+    for (int n3 = 0; n3 < nw; ++n3) dfa::cmac(re, im, ezf[(size_t)n3 * nz + l], W[((size_t)n2 * nw + n3) * an + r]);
+    F[t] = dfa::pack(re, im);
 }
 
 // stage B over the listed rows (row = j + l ny): one thread per (row, a, n1), n1 fastest.  In
@@ -442,17 +440,17 @@ void gram_fp64(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, cons
     if (sep) {
         StageTimer tt(ctx, "fp64_recip_sep", stream);
         double2 *U = ctx->buf_t<double2>("g64_U", (size_t)N * 3 * nw);
-        double2 *W = ctx->buf_t<double2>("g64_W", (size_t)nw * nw * N * n1c);
+        float4 *W = ctx->buf_t<float4>("g64_W", (size_t)nw * nw * N * n1c);
         F64 = ctx->buf_t<float4>("g64_F", (size_t)nz * nw * N * n1c);
-        RP_CUDA(cudaMemsetAsync(W, 0, sizeof(double2) * (size_t)nw * nw * N * n1c, stream));
+        RP_CUDA(cudaMemsetAsync(W, 0, sizeof(float4) * (size_t)nw * nw * N * n1c, stream));
         RecBasis rb;
         for (int q = 0; q < 9; ++q) rb.rb[q] = ew->rec[q];
         atom_phases64_kernel<<<ceil_div(N * 3 * nw, 128), 128, 0, stream>>>(d_atoms, N, rb, kp, U);
         RP_LAUNCH_CHECK();
         build_w64_kernel<<<ceil_div((long long)N * K, 128), 128, 0, stream>>>(ew->d_kidx, ew->d_kcoef, K, N, kp, U, W);
         RP_LAUNCH_CHECK();
-        stage_a64_kernel<<<ceil_div((long long)nz * nw * N * n1c, 128), 128, 0, stream>>>(W, ew->d_ez, nz, N, kp,
-                                                                                          ew->kmax, F64);
+        stage_a64_kernel<<<ceil_div((long long)nz * nw * N * n1c, 128), 128, 0, stream>>>(W, ew->d_ezf, nz, N, kp,
+                                                                                          F64);
         RP_LAUNCH_CHECK();
     } else {
         B = ctx->buf_t<double>("g64_B", (size_t)N * K2);
