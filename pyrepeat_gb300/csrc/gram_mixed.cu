@@ -60,7 +60,7 @@ constexpr int kTileBytes = kBM * kBK * 2;  // 16 KB per operand tile
 // x3 x0 <= 2 * 32 * 64, x1 x2 + x2 x1 <= 2 * 64 * 64; weight 4: three products
 // <= 64 * 64; the others less), so a stage of 64 points adds at most 786,432 =
 // 3 * 2^18 to a group and kGramFlush = 16 stages stay below 2^24 (12.6 M): the FP32
-// sums are exact, and a CTA of kGramSplit = 16 stages drains them once, at its end.
+// sums are exact, and a work unit of kGramSplit = 16 stages drains them once, at its end.
 // (A row whose |x| passed 1/2 is clamped, counted and its cube refitted from the
 // staged Phi, whose own scale keeps |x| < 1/2.)  At each flush the epilogue folds the
 // groups into one int64 per element (sum_g D_g 2^(7(6-g))), so the Gram carries no
@@ -70,16 +70,20 @@ constexpr int kGSlices = 4;
 constexpr int kGroups = 2 * kGSlices - 1;
 constexpr int kGramStages = 2;
 constexpr int kGramFlush = 16;
-constexpr int kGramSplit = 16;   // stages per CTA: 1024 points, the int64 fold's headroom (2^52 per point)
+constexpr int kGramSplit = 16;   // stages per work unit: 1024 points, the int64 fold's headroom (2^52 per point)
 constexpr int kGramEpiWarps = 8;
 constexpr int kGramThreads = 64 + 32 * kGramEpiWarps;  // 320
 constexpr int kBTileBytes = kGN * kBK * 2;             // 8 KB
 constexpr int kGramStageBytes = kGSlices * kTileBytes + kGSlices * kBTileBytes;
 constexpr int kGramSmem = kGramStages * kGramStageBytes + 1024 + 256;
 
+constexpr int kSched = 4;         // work-unit ring entries (producer -> MMA thread and epilogue)
+
 struct GramArgs {
     int nt, ntj, ntri, kb_total, kb_per_split, flush;  // flush: stages per exact FP32 run (<= kGramFlush)
-    // exact tile sums [tri][col][row] as two's complement 64-bit halves: every CTA adds the
+    int nunits;       // work units: ntri Gram tiles x ceil(kb_total / kb_per_split) point splits
+    int *next_unit;   // work counter, zero at launch
+    // exact tile sums [tri][col][row] as two's complement 64-bit halves: every unit adds the
     // high (acc >> 32) and low (acc & (2^32 - 1)) parts of its int64 partial (|acc| < 2^62)
     unsigned long long *out_hi, *out_lo;
     int *status;
@@ -105,6 +109,29 @@ __device__ __forceinline__ void gram_tile_decode(int t, int ntj, int &ti, int &t
     tj = 2 * ti + t;
 }
 
+// Work unit u = (tile u % ntri, point split u / ntri): consecutive units share their points,
+// so the CTAs working at one time read the same digit columns through L2.
+struct GramUnit {
+    int tile, a_row0, b_row0, kb0, nkb;
+};
+__device__ __forceinline__ GramUnit gram_unit(const GramArgs &g, int unit) {
+    GramUnit w;
+    w.tile = unit % g.ntri;
+    int ti, tj;
+    gram_tile_decode(w.tile, g.ntj, ti, tj);
+    w.a_row0 = ti * kBM;
+    w.b_row0 = tj * kGN;
+    w.kb0 = (unit / g.ntri) * g.kb_per_split;
+    w.nkb = min(w.kb0 + g.kb_per_split, g.kb_total) - w.kb0;  // >= 1
+    return w;
+}
+
+// Persistent: one CTA per SM takes work units from a global counter until none are left.
+// Warp 0 (one thread) takes the units, posts each in a shared ring and streams its digit
+// tiles by TMA through two stages, running ahead across unit boundaries; warp 1 (one
+// thread) issues the MMAs; warps 2..9 drain the seven group accumulators from TMEM into
+// int64 sums once per flush and add the unit's sums to its tile's totals while the MMAs of
+// the next unit run.
 __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
     const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
     const __grid_constant__ CUtensorMap tm2, const __grid_constant__ CUtensorMap tm3,
@@ -116,15 +143,12 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
     uint64_t *empty = full + kGramStages;
     uint64_t *accf = empty + kGramStages;  // accumulators ready for the epilogue
     uint64_t *acce = accf + 1;             // epilogue done reading them
-    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(acce + 1);
+    uint64_t *sfull = acce + 1;            // work unit posted in the ring
+    uint64_t *sempty = sfull + kSched;     // ring entry read by the MMA thread and every epilogue warp
+    uint64_t *fin = sempty + kSched;       // every MMA the CTA issued is complete
+    volatile int *sched = reinterpret_cast<volatile int *>(fin + 1);
+    uint32_t *tmem_holder = reinterpret_cast<uint32_t *>(const_cast<int *>(sched + kSched));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int tile = blockIdx.x % g.ntri, split = blockIdx.x / g.ntri;
-    int ti, tj;
-    gram_tile_decode(tile, g.ntj, ti, tj);
-    const int a_row0 = ti * kBM, b_row0 = tj * kGN;
-    const int kb0 = split * g.kb_per_split, kb1 = min(kb0 + g.kb_per_split, g.kb_total);
-    const int nkb = kb1 - kb0;  // >= 1
-    const int nflush = (nkb + g.flush - 1) / g.flush;
     // B is loaded for every tile (also where its rows lie inside A's tile): the four B slices
     // then sit back to back and form one 256-row operand
     const uint32_t stage_tx = kGSlices * (kTileBytes + kBTileBytes);
@@ -138,6 +162,11 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
         }
         tc::mbar_init(accf, 1);
         tc::mbar_init(acce, 32 * kGramEpiWarps);
+        for (int r = 0; r < kSched; ++r) {
+            tc::mbar_init(&sfull[r], 1);
+            tc::mbar_init(&sempty[r], 1 + kGramEpiWarps);
+        }
+        tc::mbar_init(fin, 1);
         tc::fence_mbar_init();
     }
     if (warp == 1) tc::tmem_alloc(tmem_holder, 512);
@@ -146,120 +175,158 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_holder;
 
-    int accf_commits = 0;  // phases of accf the MMA thread (warp 1, lane 0) has committed
     if (warp == 0 && lane == 0) {
-        int issued = 0;
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % kGramStages, u = kb / kGramStages;
-            if (u > 0 && !tc::mbar_wait(&empty[s], (u - 1) & 1, g.status, g.budget)) break;
-            uint8_t *st = smem + s * kGramStageBytes;
-            tc::mbar_arrive_expect_tx(&full[s], stage_tx);
-            const int x = (kb0 + kb) * kBK;
+        int it = 0;  // stages issued
+        bool ok = true;
+        for (int j = 0; ok; ++j) {
+            const int r = j % kSched;
+            if (j >= kSched && !tc::mbar_wait(&sempty[r], ((j / kSched) - 1) & 1, g.status, g.budget)) break;
+            const int unit = atomicAdd(g.next_unit, 1);
+            sched[r] = unit < g.nunits ? unit : -1;
+            tc::mbar_arrive(&sfull[r]);  // release: the entry is visible to the waiters
+            if (unit >= g.nunits) break;
+            const GramUnit w = gram_unit(g, unit);
+            for (int kb = 0; kb < w.nkb; ++kb, ++it) {
+                const int s = it % kGramStages, u = it / kGramStages;
+                if (u > 0 && !tc::mbar_wait(&empty[s], (u - 1) & 1, g.status, g.budget)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t *st = smem + s * kGramStageBytes;
+                tc::mbar_arrive_expect_tx(&full[s], stage_tx);
+                const int x = (w.kb0 + kb) * kBK;
 #pragma unroll
-            for (int q = 0; q < kGSlices; ++q) {
-                tc::tma_load_2d(st + q * kTileBytes, ta[q], x, a_row0, &full[s]);
-                tc::tma_load_2d(st + kGSlices * kTileBytes + q * kBTileBytes, tb[q], x, b_row0, &full[s]);
+                for (int q = 0; q < kGSlices; ++q) {
+                    tc::tma_load_2d(st + q * kTileBytes, ta[q], x, w.a_row0, &full[s]);
+                    tc::tma_load_2d(st + kGSlices * kTileBytes + q * kBTileBytes, tb[q], x, w.b_row0, &full[s]);
+                }
             }
-            issued = kb + 1;
         }
+        // after a timeout, the copies still in flight land before the CTA exits
         if (*reinterpret_cast<volatile int *>(g.status) != 0)
-            for (int kb = max(0, issued - kGramStages); kb < issued; ++kb)
-                tc::mbar_wait(&full[kb % kGramStages], (kb / kGramStages) & 1, nullptr);
+            for (int k = max(0, it - kGramStages); k < it; ++k)
+                tc::mbar_wait(&full[k % kGramStages], (k / kGramStages) & 1, nullptr);
     } else if (warp == 1 && lane == 0) {
         const uint32_t idesc = tc::idesc_f16_f32(kBM, kGN);
         const uint32_t idesc4 = tc::idesc_f16_f32(kBM, 4 * kGN);  // all four B slices, four adjacent groups
         uint32_t d[kGroups];  // group accumulators, 64 TMEM columns each
 #pragma unroll
         for (int q = 0; q < kGroups; ++q) d[q] = tmem + (uint32_t)(q * kGN);
+        int it = 0, fc = 0;  // stages consumed, flushes committed
         bool ok = true;
-        for (int f = 0; f < nflush && ok; ++f) {
-            if (f > 0 && !tc::mbar_wait(acce, (f - 1) & 1, g.status, g.budget)) break;  // epilogue drained the sums
-            ++accf_commits;
-            tc::fence_after_sync();
-            const int kbf0 = f * g.flush, kbf1 = min(kbf0 + g.flush, nkb);
-            for (int kb = kbf0; kb < kbf1; ++kb) {
-                const int s = kb % kGramStages, u = kb / kGramStages;
-                if (!tc::mbar_wait(&full[s], u & 1, g.status, g.budget)) {
+        for (int j = 0; ok; ++j) {
+            const int r = j % kSched;
+            if (!tc::mbar_wait(&sfull[r], (j / kSched) & 1, g.status, g.budget)) break;
+            const int unit = sched[r];
+            tc::mbar_arrive(&sempty[r]);
+            if (unit < 0) break;
+            const GramUnit w = gram_unit(g, unit);
+            const int nflush = (w.nkb + g.flush - 1) / g.flush;
+            for (int f = 0; f < nflush; ++f) {
+                if (fc > 0 && !tc::mbar_wait(acce, (fc - 1) & 1, g.status, g.budget)) {  // sums drained
                     ok = false;
                     break;
                 }
                 tc::fence_after_sync();
-                const uint32_t st = tc::smem_u32(smem + s * kGramStageBytes);
-                uint64_t x[kGSlices], y[kGSlices];
-#pragma unroll
-                for (int q = 0; q < kGSlices; ++q) {
-                    x[q] = tc::sdesc_k_sw128(st + q * kTileBytes);
-                    y[q] = tc::sdesc_k_sw128(st + kGSlices * kTileBytes + q * kBTileBytes);
-                }
-#pragma unroll
-                for (int kk = 0; kk < kBK / 16; ++kk) {
-                    const uint64_t o = (uint64_t)(kk * 2);
-                    if (kb == kbf0 && kk == 0) {
-                        // the first products of a flush start each group's sum: one MMA per
-                        // (slice a, slice b), the first into a group overwriting it
-                        bool started[kGroups] = {false, false, false, false, false, false, false};
-#pragma unroll
-                        for (int a = 0; a < kGSlices; ++a)
-#pragma unroll
-                            for (int b = 0; b < kGSlices; ++b) {
-                                const int grp = a + b;
-                                const uint32_t acc = started[grp] ? 1u : 0u;
-                                started[grp] = true;
-                                tc::umma_f16(d[grp], x[a] + o, y[b] + o, idesc, acc);
-                            }
-                    } else {
-                        // then N = 256: slice a against the four B slices back to back (a 256-row
-                        // operand) writes the products of weights a .. a+3 into the four adjacent
-                        // groups from d[a] (the same products, in the same order per group, as the
-                        // pairs above), reading A once instead of four times
-#pragma unroll
-                        for (int a = 0; a < kGSlices; ++a) tc::umma_f16(d[a], x[a] + o, y[0] + o, idesc4, 1u);
+                const int kbf0 = f * g.flush, kbf1 = min(kbf0 + g.flush, w.nkb);
+                for (int kb = kbf0; kb < kbf1; ++kb, ++it) {
+                    const int s = it % kGramStages, u = it / kGramStages;
+                    if (!tc::mbar_wait(&full[s], u & 1, g.status, g.budget)) {
+                        ok = false;
+                        break;
                     }
+                    tc::fence_after_sync();
+                    const uint32_t st = tc::smem_u32(smem + s * kGramStageBytes);
+                    uint64_t x[kGSlices], y[kGSlices];
+#pragma unroll
+                    for (int q = 0; q < kGSlices; ++q) {
+                        x[q] = tc::sdesc_k_sw128(st + q * kTileBytes);
+                        y[q] = tc::sdesc_k_sw128(st + kGSlices * kTileBytes + q * kBTileBytes);
+                    }
+#pragma unroll
+                    for (int kk = 0; kk < kBK / 16; ++kk) {
+                        const uint64_t o = (uint64_t)(kk * 2);
+                        if (kb == kbf0 && kk == 0) {
+                            // the first products of a flush start each group's sum: one MMA per
+                            // (slice a, slice b), the first into a group overwriting it
+                            bool started[kGroups] = {false, false, false, false, false, false, false};
+#pragma unroll
+                            for (int a = 0; a < kGSlices; ++a)
+#pragma unroll
+                                for (int b = 0; b < kGSlices; ++b) {
+                                    const int grp = a + b;
+                                    const uint32_t acc = started[grp] ? 1u : 0u;
+                                    started[grp] = true;
+                                    tc::umma_f16(d[grp], x[a] + o, y[b] + o, idesc, acc);
+                                }
+                        } else {
+                            // then N = 256: slice a against the four B slices back to back (a 256-row
+                            // operand) writes the products of weights a .. a+3 into the four adjacent
+                            // groups from d[a] (the same products, in the same order per group, as the
+                            // pairs above), reading A once instead of four times
+#pragma unroll
+                            for (int a = 0; a < kGSlices; ++a) tc::umma_f16(d[a], x[a] + o, y[0] + o, idesc4, 1u);
+                        }
+                    }
+                    tc::umma_commit(&empty[s]);
                 }
-                tc::umma_commit(&empty[s]);
+                if (!ok) break;
+                tc::umma_commit(accf);
+                ++fc;
             }
-            tc::umma_commit(accf);
         }
+        tc::umma_commit(fin);  // tracks every MMA issued above
     } else if (warp >= 2) {
         const int ew = warp - 2;
         const int lane_base = (warp & 3) * 32;
         const int col0 = (ew >> 2) * 32;  // this warp's 32 columns of the 64
-        long long acc[32];
-#pragma unroll
-        for (int i = 0; i < 32; ++i) acc[i] = 0;
+        const uint32_t base = tmem + ((uint32_t)lane_base << 16) + (uint32_t)col0;
+        int fc = 0;  // flushes drained
         bool ok = true;
-        for (int f = 0; f < nflush; ++f) {
-            if (!tc::mbar_wait(accf, f & 1, g.status, g.budget)) {
-                ok = false;
-                break;
-            }
-            tc::fence_after_sync();
-            const uint32_t base = tmem + ((uint32_t)lane_base << 16) + (uint32_t)col0;
+        // every wait's outcome is made warp-uniform by a vote before the warp-wide
+        // TMEM loads and the __syncwarp below
+        for (int j = 0; ok; ++j) {
+            const int r = j % kSched;
+            if (!__all_sync(0xffffffffu, tc::mbar_wait(&sfull[r], (j / kSched) & 1, g.status, g.budget))) break;
+            const int unit = sched[r];
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&sempty[r]);
+            if (unit < 0) break;
+            const GramUnit w = gram_unit(g, unit);
+            const int nflush = (w.nkb + g.flush - 1) / g.flush;
+            long long acc[32];
 #pragma unroll
-            for (int q = 0; q < kGroups; ++q) {
-                float v[32];
-                tc::tmem_ld_32x32(base + (uint32_t)(q * kGN), v);
-                const int sh = 7 * (kGroups - 1 - q);
+            for (int i = 0; i < 32; ++i) acc[i] = 0;
+            for (int f = 0; f < nflush; ++f, ++fc) {
+                if (!__all_sync(0xffffffffu, tc::mbar_wait(accf, fc & 1, g.status, g.budget))) {
+                    ok = false;
+                    break;
+                }
+                tc::fence_after_sync();
 #pragma unroll
-                for (int i = 0; i < 32; ++i) acc[i] += (long long)__float2int_rn(v[i]) << sh;
+                for (int q = 0; q < kGroups; ++q) {
+                    float v[32];
+                    tc::tmem_ld_32x32(base + (uint32_t)(q * kGN), v);
+                    const int sh = 7 * (kGroups - 1 - q);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) acc[i] += (long long)__float2int_rn(v[i]) << sh;
+                }
+                tc::fence_before_sync();
+                tc::mbar_arrive(acce);
             }
-            tc::fence_before_sync();
-            tc::mbar_arrive(acce);
-        }
-        if (ok && *reinterpret_cast<volatile int *>(g.status) == 0) {
-            const long long t0 = (long long)tile * (kBM * kGN);
-            const int r = lane_base + lane;
+            if (__any_sync(0xffffffffu, !ok || *reinterpret_cast<volatile int *>(g.status) != 0)) break;
+            const long long t0 = (long long)w.tile * (kBM * kGN);
+            const int rr = lane_base + lane;
 #pragma unroll
             for (int i = 0; i < 32; ++i) {
-                const long long e = t0 + (col0 + i) * kBM + r;
+                const long long e = t0 + (col0 + i) * kBM + rr;
                 atomicAdd(g.out_hi + e, (unsigned long long)(acc[i] >> 32));
                 atomicAdd(g.out_lo + e, (unsigned long long)(acc[i] & 0xffffffffLL));
             }
         }
     }
-    // the MMA thread waits for its last commit (every MMA done) before TMEM is freed; after a
-    // timeout that is the last phase it committed, not the last of the plan
-    if (warp == 1 && lane == 0 && accf_commits > 0) tc::mbar_wait(accf, (accf_commits - 1) & 1, nullptr);
+    // TMEM is freed only after every MMA of the CTA has completed (also after a timeout)
+    if (warp == 1 && lane == 0) tc::mbar_wait(fin, 0, nullptr);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -933,7 +1000,7 @@ __global__ void __launch_bounds__(kSliceThreads) slice_rows_kernel(const float2 
 }
 
 // The Gram tiles' exact sums (high and low 64-bit halves accumulated by the Gram kernel's
-// CTAs, whatever the points per CTA) rounded to FP64 once, (hi 2^32 exactly) + lo after
+// work units, whatever the points per unit) rounded to FP64 once, (hi 2^32 exactly) + lo after
 // normalising lo to [0, 2^32), and added, unscaled, into G (Np x Np).  Tiles inside a
 // 128-row block already hold both (a,b) and (b,a); the others are mirrored.
 __global__ void gram_finish_tiles_kernel(const unsigned long long *__restrict__ th,
@@ -1034,8 +1101,24 @@ CUtensorMap make_map(const void *ptr, long long rows, long long cols, int box_ro
     return m;
 }
 
-void launch_gram(const __half *const *X, int rows, long long cols, const GramArgs &g, int grid, cudaStream_t s) {
+// Zeroed tile totals (high and low halves, 2 x ntri x 128 x 64 words) with the kernel's work
+// counter after them, in one buffer cleared by one memset on the stream
+void gram_totals_init(rp_ctx *ctx, const std::string &name, GramArgs &g, cudaStream_t s) {
+    const size_t n = (size_t)g.ntri * kBM * kGN;
+    unsigned long long *t = ctx->buf_t<unsigned long long>(name, 2 * n + 1);
+    RP_CUDA(cudaMemsetAsync(t, 0, sizeof(unsigned long long) * (2 * n + 1), s));
+    g.out_hi = t;
+    g.out_lo = t + n;
+    g.next_unit = reinterpret_cast<int *>(t + 2 * n);
+}
+
+// One CTA per SM (the stages fill shared memory), at most one per work unit
+void launch_gram(rp_ctx *ctx, const __half *const *X, int rows, long long cols, GramArgs g, cudaStream_t s) {
     smem_optin((const void *)gram_exact_kernel, kGramSmem);
+    RP_REQUIRE(g.kb_per_split >= 1 && g.kb_per_split <= kGramSplit && g.flush >= 1 && g.flush <= kGramFlush,
+               "gram: bad split");
+    g.nunits = g.ntri * (int)ceil_div(g.kb_total, g.kb_per_split);
+    const int grid = std::max(1, std::min(g.nunits, ctx->sm_count));
     CUtensorMap a[kGSlices], b[kGSlices];
     for (int q = 0; q < kGSlices; ++q) {
         a[q] = make_map(X[q], rows, cols, kBM);   // rows past `rows` read as zeros
@@ -1207,13 +1290,10 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
                 rowsum);
             RP_LAUNCH_CHECK();
         }
-        // 3. exact Gram tiles (CTAs over point splits add exactly into the tiles' 64-bit
+        // 3. exact Gram tiles (work units over point splits add exactly into the tiles' 64-bit
         //    totals), then the totals rounded once into G
         {
             const int kb_total = (int)(rows_kpad / kBK);
-            const int nsplit = (kb_total + kb_split - 1) / kb_split;
-            unsigned long long *tsum = ctx->buf_t<unsigned long long>("m_tsum" + slot, 2 * (size_t)ntri * kBM * kGN);
-            RP_CUDA(cudaMemsetAsync(tsum, 0, sizeof(unsigned long long) * 2 * (size_t)ntri * kBM * kGN, stream));
             GramArgs g{};
             g.nt = nt;
             g.ntj = ntj;
@@ -1221,14 +1301,13 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
             g.kb_total = kb_total;
             g.kb_per_split = kb_split;
             g.flush = kGramFlush;
-            g.out_hi = tsum;
-            g.out_lo = tsum + (size_t)ntri * kBM * kGN;
             g.status = d_status;
             g.budget = ctx->wait_budget;
+            gram_totals_init(ctx, "m_tsum" + slot, g, stream);
             const __half *Xq[kGSlices] = {X[0], X[1], X[2], X[3]};
             {
                 StageTimer tt(ctx, "gram_exact", stream);
-                launch_gram(Xq, Np, rows_kpad, g, ntri * nsplit, stream);
+                launch_gram(ctx, Xq, Np, rows_kpad, g, stream);
             }
             StageTimer tr(ctx, "gram_totals", stream);
             gram_finish_tiles_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256, 0, stream>>>(
@@ -1355,9 +1434,7 @@ void gram_words_fp64(rp_ctx *ctx, const double *P, long long rows, int N, const 
     const int nt = (int)ceil_div(Np2, kBM), ntj = (int)ceil_div(Np2, kGN);
     int ntri = 0;
     for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
-    const int kb_total = (int)(cols_pad / kBK), nsplit = (kb_total + kGramSplit - 1) / kGramSplit;
-    unsigned long long *tsum = ctx->buf_t<unsigned long long>("w64_tsum", 2 * (size_t)ntri * kBM * kGN);
-    RP_CUDA(cudaMemsetAsync(tsum, 0, sizeof(unsigned long long) * 2 * (size_t)ntri * kBM * kGN, stream));
+    const int kb_total = (int)(cols_pad / kBK);
     RP_CUDA(cudaMemsetAsync(ctx->status_words(), 0, sizeof(int), stream));
     GramArgs g{};
     g.nt = nt;
@@ -1366,12 +1443,11 @@ void gram_words_fp64(rp_ctx *ctx, const double *P, long long rows, int N, const 
     g.kb_total = kb_total;
     g.kb_per_split = kGramSplit;
     g.flush = kGramFlush;
-    g.out_hi = tsum;
-    g.out_lo = tsum + (size_t)ntri * kBM * kGN;
     g.status = ctx->status_words();
     g.budget = ctx->wait_budget;
+    gram_totals_init(ctx, "w64_tsum", g, stream);
     const __half *Xq[kGSlices] = {X[0], X[1], X[2], X[3]};
-    launch_gram(Xq, Np2, cols_pad, g, ntri * nsplit, stream);
+    launch_gram(ctx, Xq, Np2, cols_pad, g, stream);
     double *G2 = ctx->buf_t<double>("w64_G2", (size_t)Np2 * Np2);
     words_gram_kernel<<<dim3(ceil_div(kBM * kGN, 256), ntri), 256, 0, stream>>>(g.out_hi, g.out_lo, ntj, Np2, G2);
     RP_LAUNCH_CHECK();
@@ -1482,17 +1558,15 @@ extern "C" int rp_debug_gram_slices(rp_ctx *ctx, const void *X0, const void *X1,
         int ntri = 0;
         for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
         const int kb_total = (int)(cols / kBK);
-        const int nsplit = (kb_total + kb_split - 1) / kb_split;
-        unsigned long long *tsum = ctx->buf_t<unsigned long long>("dbg_tsum", 2 * (size_t)ntri * kBM * kGN);
-        RP_CUDA(cudaMemset(tsum, 0, sizeof(unsigned long long) * 2 * (size_t)ntri * kBM * kGN));
+        RP_REQUIRE(kb_split >= 1 && kb_split <= kGramSplit, "kb_split must lie in [1, 16]");
         RP_CUDA(cudaMemset(ctx->d_status, 0, sizeof(int)));
         GramArgs g{};
         g.nt = nt; g.ntj = ntj; g.ntri = ntri; g.kb_total = kb_total; g.kb_per_split = kb_split;
         g.flush = std::min(std::max(flush, 1), kGramFlush);
-        g.out_hi = tsum; g.out_lo = tsum + (size_t)ntri * kBM * kGN;
         g.status = ctx->d_status; g.budget = ctx->wait_budget;
+        gram_totals_init(ctx, "dbg_tsum", g, 0);
         const __half *Xq[kGSlices] = {(const __half *)X0, (const __half *)X1, (const __half *)X2, (const __half *)X3};
-        launch_gram(Xq, Np, cols, g, ntri * nsplit, 0);
+        launch_gram(ctx, Xq, Np, cols, g, 0);
         float *ones = ctx->buf_t<float>("dbg_ones", Np);
         std::vector<float> h((size_t)Np, 1.0f);
         RP_CUDA(cudaMemcpy(ones, h.data(), sizeof(float) * Np, cudaMemcpyHostToDevice));
