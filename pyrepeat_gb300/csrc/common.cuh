@@ -186,7 +186,7 @@ constexpr double kDefaultKappaLimit = 2e5;
 
 namespace rp {
 // Tile shapes of the mixed-precision normal equations: atoms per CTA of the Phi kernel (8, 16
-// or 32) and Gram stages of 64 points per CTA (up to 16).  Neither changes a result: every
+// or 32) and Gram points per work unit, in blocks of 64 (up to 16).  Neither changes a result: every
 // Phi value and every exact digit sum is the same whatever the tiling.
 struct TileConfig {
     int phi_atoms = 16;

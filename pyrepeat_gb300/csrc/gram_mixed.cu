@@ -45,8 +45,9 @@ namespace rp {
 namespace {
 
 constexpr int kBM = 128;       // Gram tile rows (TMEM lanes)
-constexpr int kBK = 64;        // K elements per stage (128 B of FP16 = one swizzle row)
-constexpr int kTileBytes = kBM * kBK * 2;  // 16 KB per operand tile
+constexpr int kKPad = 64;      // digit rows are padded to a multiple of 64 points (the tensor maps' unit)
+constexpr int kBK = 32;        // points (K elements) per stage: 64 B of FP16 = one 64-byte swizzle row
+constexpr int kTileBytes = kBM * kBK * 2;  // 8 KB per operand tile
 
 // ---- GEMM-2 (Gram): exact integer products of four 7-bit fixed-point slices
 // x = 2^-6 (x0 + 2^-7 x1 + 2^-14 x2 + 2^-21 x3), x_s integers with |x0| <= 32,
@@ -58,9 +59,10 @@ constexpr int kTileBytes = kBM * kBK * 2;  // 16 KB per operand tile
 // grouped by weight g = s+u into seven TMEM accumulators of a 128 x 64 tile.  Per
 // point, a group's products sum to at most 12288 in magnitude (weight 3: x0 x3 +
 // x3 x0 <= 2 * 32 * 64, x1 x2 + x2 x1 <= 2 * 64 * 64; weight 4: three products
-// <= 64 * 64; the others less), so a stage of 64 points adds at most 786,432 =
-// 3 * 2^18 to a group and kGramFlush = 16 stages stay below 2^24 (12.6 M): the FP32
-// sums are exact, and a work unit of kGramSplit = 16 stages drains them once, at its end.
+// <= 64 * 64; the others less), so a stage of 32 points adds at most 393,216 =
+// 3 * 2^17 to a group and kGramFlush = 32 stages (1024 points) stay below 2^24 (12.6 M):
+// the FP32 sums are exact, and a work unit of kGramSplit = 32 stages drains them once, at
+// its end.
 // (A row whose |x| passed 1/2 is clamped, counted and its cube refitted from the
 // staged Phi, whose own scale keeps |x| < 1/2.)  At each flush the epilogue folds the
 // groups into one int64 per element (sum_g D_g 2^(7(6-g))), so the Gram carries no
@@ -68,12 +70,13 @@ constexpr int kTileBytes = kBM * kBK * 2;  // 16 KB per operand tile
 constexpr int kGN = 64;          // Gram tile columns
 constexpr int kGSlices = 4;
 constexpr int kGroups = 2 * kGSlices - 1;
-constexpr int kGramStages = 2;
-constexpr int kGramFlush = 16;
-constexpr int kGramSplit = 16;   // stages per work unit: 1024 points, the int64 fold's headroom (2^52 per point)
+constexpr int kGramStages = 4;   // 4 x 48 KB: three stages in flight while one is multiplied
+constexpr int kGramFlush = 32;
+constexpr int kGramSplit = 32;   // stages per work unit: 1024 points, the int64 fold's headroom (2^52 per point)
+constexpr int kStagesPer64 = kKPad / kBK;  // the autotuner's and the diagnostics' 64-point blocks, in stages
 constexpr int kGramEpiWarps = 8;
 constexpr int kGramThreads = 64 + 32 * kGramEpiWarps;  // 320
-constexpr int kBTileBytes = kGN * kBK * 2;             // 8 KB
+constexpr int kBTileBytes = kGN * kBK * 2;             // 4 KB
 constexpr int kGramStageBytes = kGSlices * kTileBytes + kGSlices * kBTileBytes;
 constexpr int kGramSmem = kGramStages * kGramStageBytes + 1024 + 256;
 
@@ -240,8 +243,8 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
                     uint64_t x[kGSlices], y[kGSlices];
 #pragma unroll
                     for (int q = 0; q < kGSlices; ++q) {
-                        x[q] = tc::sdesc_k_sw128(st + q * kTileBytes);
-                        y[q] = tc::sdesc_k_sw128(st + kGSlices * kTileBytes + q * kBTileBytes);
+                        x[q] = tc::sdesc_k_sw64(st + q * kTileBytes);
+                        y[q] = tc::sdesc_k_sw64(st + kGSlices * kTileBytes + q * kBTileBytes);
                     }
 #pragma unroll
                     for (int kk = 0; kk < kBK / 16; ++kk) {
@@ -1085,9 +1088,9 @@ EncodeFn encode_fn() {
     return fn;
 }
 
-// 2-D FP16 tensor [rows][cols] (cols contiguous, multiple of 64), box 64 x box_rows, 128-B swizzle
+// 2-D FP16 tensor [rows][cols] (cols contiguous, multiple of 64), box 32 x box_rows, 64-B swizzle
 CUtensorMap make_map(const void *ptr, long long rows, long long cols, int box_rows) {
-    RP_REQUIRE(cols % kBK == 0, "tensor map: columns must be a multiple of 64");
+    RP_REQUIRE(cols % kKPad == 0, "tensor map: columns must be a multiple of 64");
     RP_REQUIRE(((uintptr_t)ptr & 15) == 0, "tensor map: base must be 16-byte aligned");
     CUtensorMap m;
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
@@ -1095,7 +1098,7 @@ CUtensorMap make_map(const void *ptr, long long rows, long long cols, int box_ro
     cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
-                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) fail(RP_E_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     return m;
@@ -1214,7 +1217,7 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     long long chunk = std::max<long long>(kBM, ((6LL << 30) / per_point) / kBM * kBM);
     if (ctx->chunk_cap > 0) chunk = std::max<long long>(kBM, std::min<long long>(chunk, ctx->chunk_cap / kBM * kBM));
     chunk = std::min<long long>(chunk, round_up(M, kBM));
-    const long long chunk_pad = round_up(chunk, kBK);
+    const long long chunk_pad = round_up(chunk, kKPad);
 
     // single pass: Phi goes straight to digits, scaled by the a-priori bounds, centre 0
     std::vector<float> hscale;
@@ -1255,11 +1258,11 @@ void gram_mixed(rp_ctx *ctx, const rp_ewald *ew, const double *atoms, int N, con
     for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
     // points per CTA: kGramSplit stages (1024 points, the int64 headroom, exact sums drained
     // once) or fewer, for more CTAs on cubes with few Gram tiles (the autotuner's choice)
-    const int kb_split = std::min(std::max(tiles.gram_split, 1), kGramSplit);
+    const int kb_split = kStagesPer64 * std::min(std::max(tiles.gram_split, 1), kGramSplit / kStagesPer64);
 
     for (long long m0 = 0; m0 < M; m0 += chunk) {
         const long long rows = std::min<long long>(chunk, M - m0);
-        const long long rows_kpad = round_up(rows, kBK);
+        const long long rows_kpad = round_up(rows, kKPad);
         // 1. Phi of the chunk (real space + reciprocal stage C) and its column statistics
         const int nb = (int)ceil_div(rows, kPhiPts);
         if (single) {  // Phi of the chunk straight to the digits of X
@@ -1421,7 +1424,7 @@ __global__ void combine_words_kernel(const double *__restrict__ G2, int N, const
 void gram_words_fp64(rp_ctx *ctx, const double *P, long long rows, int N, const double *V, double *G, double *r,
                      cudaStream_t stream) {
     const int Np = N + 1, Np2 = 2 * Np;
-    const long long cols_pad = round_up(rows, kBK);
+    const long long cols_pad = round_up(rows, kKPad);
     unsigned long long *mx = ctx->buf_t<unsigned long long>("w64_mx", (size_t)Np);
     RP_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Np, stream));
     colmax_fp64_kernel<<<dim3(ceil_div(Np, 256), ceil_div(rows, 256)), 256, 0, stream>>>(P, rows, N, V, mx);
@@ -1558,11 +1561,12 @@ extern "C" int rp_debug_gram_slices(rp_ctx *ctx, const void *X0, const void *X1,
         int ntri = 0;
         for (int ti = 0; ti < nt; ++ti) ntri += ntj - 2 * ti;
         const int kb_total = (int)(cols / kBK);
-        RP_REQUIRE(kb_split >= 1 && kb_split <= kGramSplit, "kb_split must lie in [1, 16]");
+        // flush and kb_split count 64-point blocks (the padding unit): two stages each
+        RP_REQUIRE(kb_split >= 1 && kb_split * kStagesPer64 <= kGramSplit, "kb_split must lie in [1, 16]");
         RP_CUDA(cudaMemset(ctx->d_status, 0, sizeof(int)));
         GramArgs g{};
-        g.nt = nt; g.ntj = ntj; g.ntri = ntri; g.kb_total = kb_total; g.kb_per_split = kb_split;
-        g.flush = std::min(std::max(flush, 1), kGramFlush);
+        g.nt = nt; g.ntj = ntj; g.ntri = ntri; g.kb_total = kb_total; g.kb_per_split = kb_split * kStagesPer64;
+        g.flush = kStagesPer64 * std::min(std::max(flush, 1), kGramFlush / kStagesPer64);
         g.status = ctx->d_status; g.budget = ctx->wait_budget;
         gram_totals_init(ctx, "dbg_tsum", g, 0);
         const __half *Xq[kGSlices] = {(const __half *)X0, (const __half *)X1, (const __half *)X2, (const __half *)X3};

@@ -129,6 +129,18 @@ __device__ __forceinline__ uint64_t sdesc_k_sw128(uint32_t saddr) {
     return d;
 }
 
+// The same for the 64-byte swizzle (rows of 64 B, 8-row groups 512 B apart), tile base
+// 512-B aligned.
+__device__ __forceinline__ uint64_t sdesc_k_sw64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address (16-B units)
+    d |= (uint64_t)1 << 16;                     // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(512u >> 4) << 32;           // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;                     // descriptor version for tcgen05
+    d |= (uint64_t)4 << 61;                     // 64-byte swizzle
+    return d;
+}
+
 // Instruction descriptor, kind::f16: FP16 A and B (both the same type), FP32
 // accumulator, both K-major, M x N tile.
 __host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
