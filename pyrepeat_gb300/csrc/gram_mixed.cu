@@ -70,17 +70,20 @@ constexpr int kTileBytes = kBM * kBK * 2;  // 8 KB per operand tile
 constexpr int kGN = 64;          // Gram tile columns
 constexpr int kGSlices = 4;
 constexpr int kGroups = 2 * kGSlices - 1;
-constexpr int kGramStages = 4;   // 4 x 48 KB: three stages in flight while one is multiplied
+constexpr int kGramStages = 3;   // 3 x 48 KB: two stages in flight while one is multiplied
 constexpr int kGramFlush = 32;
 constexpr int kGramSplit = 32;   // stages per work unit: 1024 points, the int64 fold's headroom (2^52 per point)
 constexpr int kStagesPer64 = kKPad / kBK;  // the autotuner's and the diagnostics' 64-point blocks, in stages
 constexpr int kGramEpiWarps = 8;
+constexpr int kEpiCols = kGN * 4 / kGramEpiWarps;  // Gram tile columns per epilogue warp (TMEM lane quarter)
 constexpr int kGramThreads = 64 + 32 * kGramEpiWarps;  // 320
 constexpr int kBTileBytes = kGN * kBK * 2;             // 4 KB
 constexpr int kGramStageBytes = kGSlices * kTileBytes + kGSlices * kBTileBytes;
 constexpr int kGramSmem = kGramStages * kGramStageBytes + 1024 + 256;
 
 constexpr int kSched = 4;         // work-unit ring entries (producer -> MMA thread and epilogue)
+// the barriers, the ring and the TMEM address after the stages, in the last 256 bytes
+static_assert((2 * kGramStages + 3 + 2 * kSched) * 8 + kSched * 4 + 4 <= 256, "gram smem tail");
 
 struct GramArgs {
     int nt, ntj, ntri, kb_total, kb_per_split, flush;  // flush: stages per exact FP32 run (<= kGramFlush)
@@ -135,7 +138,9 @@ __device__ __forceinline__ GramUnit gram_unit(const GramArgs &g, int unit) {
 // thread) issues the MMAs; warps 2..9 drain the seven group accumulators from TMEM into
 // int64 sums once per flush and add the unit's sums to its tile's totals while the MMAs of
 // the next unit run.
-__global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
+// At most 96 registers and 3 x 48 KB of stages: the SM keeps room for CTAs of other kernels
+// (the Phi kernel of other cubes, bound by instruction issue, which this kernel barely uses).
+__global__ void __maxnreg__(96) gram_exact_kernel(
     const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
     const __grid_constant__ CUtensorMap tm2, const __grid_constant__ CUtensorMap tm3,
     const __grid_constant__ CUtensorMap tb0, const __grid_constant__ CUtensorMap tb1,
@@ -282,7 +287,7 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
     } else if (warp >= 2) {
         const int ew = warp - 2;
         const int lane_base = (warp & 3) * 32;
-        const int col0 = (ew >> 2) * 32;  // this warp's 32 columns of the 64
+        const int col0 = (ew >> 2) * kEpiCols;  // this warp's columns of the 64
         const uint32_t base = tmem + ((uint32_t)lane_base << 16) + (uint32_t)col0;
         int fc = 0;  // flushes drained
         bool ok = true;
@@ -297,34 +302,41 @@ __global__ void __launch_bounds__(kGramThreads, 1) gram_exact_kernel(
             if (unit < 0) break;
             const GramUnit w = gram_unit(g, unit);
             const int nflush = (w.nkb + g.flush - 1) / g.flush;
-            long long acc[32];
-#pragma unroll
-            for (int i = 0; i < 32; ++i) acc[i] = 0;
+            const long long t0 = (long long)w.tile * (kBM * kGN);
+            const int rr = lane_base + lane;
             for (int f = 0; f < nflush; ++f, ++fc) {
-                if (!__all_sync(0xffffffffu, tc::mbar_wait(accf, fc & 1, g.status, g.budget))) {
+                if (!__all_sync(0xffffffffu, tc::mbar_wait(accf, fc & 1, g.status, g.budget)) ||
+                    __any_sync(0xffffffffu, *reinterpret_cast<volatile int *>(g.status) != 0)) {
                     ok = false;
                     break;
                 }
                 tc::fence_after_sync();
+                // the warp's columns 16 at a time (fewer live registers): the flush's int64 sums
+                // of 16 columns go to the tile totals before the next 16 are loaded
 #pragma unroll
-                for (int q = 0; q < kGroups; ++q) {
-                    float v[32];
-                    tc::tmem_ld_32x32(base + (uint32_t)(q * kGN), v);
-                    const int sh = 7 * (kGroups - 1 - q);
+                for (int h = 0; h < kEpiCols / 16; ++h) {
+                    long long acc[16];
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) acc[i] += (long long)__float2int_rn(v[i]) << sh;
+                    for (int i = 0; i < 16; ++i) acc[i] = 0;
+#pragma unroll
+                    for (int q = 0; q < kGroups; ++q) {
+                        float v[16];
+                        tc::tmem_ld_32x16(base + (uint32_t)(q * kGN + 16 * h), v);
+                        const int sh = 7 * (kGroups - 1 - q);
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) acc[i] += (long long)__float2int_rn(v[i]) << sh;
+                    }
+                    if (h == kEpiCols / 16 - 1) {
+                        tc::fence_before_sync();
+                        tc::mbar_arrive(acce);
+                    }
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const long long e = t0 + (col0 + 16 * h + i) * kBM + rr;
+                        atomicAdd(g.out_hi + e, (unsigned long long)(acc[i] >> 32));
+                        atomicAdd(g.out_lo + e, (unsigned long long)(acc[i] & 0xffffffffLL));
+                    }
                 }
-                tc::fence_before_sync();
-                tc::mbar_arrive(acce);
-            }
-            if (__any_sync(0xffffffffu, !ok || *reinterpret_cast<volatile int *>(g.status) != 0)) break;
-            const long long t0 = (long long)w.tile * (kBM * kGN);
-            const int rr = lane_base + lane;
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                const long long e = t0 + (col0 + i) * kBM + rr;
-                atomicAdd(g.out_hi + e, (unsigned long long)(acc[i] >> 32));
-                atomicAdd(g.out_lo + e, (unsigned long long)(acc[i] & 0xffffffffLL));
             }
         }
     }
@@ -1118,6 +1130,9 @@ void gram_totals_init(rp_ctx *ctx, const std::string &name, GramArgs &g, cudaStr
 // One CTA per SM (the stages fill shared memory), at most one per work unit
 void launch_gram(rp_ctx *ctx, const __half *const *X, int rows, long long cols, GramArgs g, cudaStream_t s) {
     smem_optin((const void *)gram_exact_kernel, kGramSmem);
+    // the SM's whole shared memory as such, so that CTAs of other kernels fit beside this one
+    RP_CUDA(cudaFuncSetAttribute((const void *)gram_exact_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared));
     RP_REQUIRE(g.kb_per_split >= 1 && g.kb_per_split <= kGramSplit && g.flush >= 1 && g.flush <= kGramFlush,
                "gram: bad split");
     g.nunits = g.ntri * (int)ceil_div(g.kb_total, g.kb_per_split);
