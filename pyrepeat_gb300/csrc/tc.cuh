@@ -99,24 +99,8 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {  
 __device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// 32 lanes x 32 columns of 32-bit values: thread t of the warp gets lane (base+t), columns col..col+31
-__device__ __forceinline__ void tmem_ld_32x32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// 32 lanes x 16 columns: thread t of the warp gets lane (base+t), columns col..col+15
+// 32 lanes x 16 columns of 32-bit values: thread t of the warp gets lane (base+t), columns
+// col..col+15 (the warp may address only its own quarter of the 128 lanes)
 __device__ __forceinline__ void tmem_ld_32x16(uint32_t taddr, float (&v)[16]) {
     uint32_t r[16];
     asm volatile(
@@ -131,20 +115,8 @@ __device__ __forceinline__ void tmem_ld_32x16(uint32_t taddr, float (&v)[16]) {
 }
 
 // ------------------------------------------------------------------ UMMA
-// Shared-memory matrix descriptor for a K-major tile stored with the 128-byte
-// swizzle (rows of 128 B, 8-row groups 1024 B apart), tile base 1024-B aligned.
-__device__ __forceinline__ uint64_t sdesc_k_sw128(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address (16-B units)
-    d |= (uint64_t)1 << 16;                     // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024u >> 4) << 32;          // stride byte offset: next 8-row group
-    d |= (uint64_t)1 << 46;                     // descriptor version for tcgen05
-    d |= (uint64_t)2 << 61;                     // 128-byte swizzle
-    return d;
-}
-
-// The same for the 64-byte swizzle (rows of 64 B, 8-row groups 512 B apart), tile base
-// 512-B aligned.
+// Shared-memory matrix descriptor for a K-major tile stored with the 64-byte swizzle
+// (rows of 64 B, 8-row groups 512 B apart), tile base 512-B aligned.
 __device__ __forceinline__ uint64_t sdesc_k_sw64(uint32_t saddr) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address (16-B units)
