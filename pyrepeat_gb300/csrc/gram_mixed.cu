@@ -34,6 +34,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 
@@ -87,8 +88,9 @@ static_assert((2 * kGramStages + 3 + 2 * kSched) * 8 + kSched * 4 + 4 <= 256, "g
 
 struct GramArgs {
     int nt, ntj, ntri, kb_total, kb_per_split, flush;  // flush: stages per exact FP32 run (<= kGramFlush)
-    int nunits;       // work units: ntri Gram tiles x ceil(kb_total / kb_per_split) point splits
-    int *next_unit;   // work counter, zero at launch
+    int unit0, nunits;  // this launch's work units unit0 .. unit0 + nunits - 1 of the ntri Gram
+                        // tiles x ceil(kb_total / kb_per_split) point splits
+    int *next_unit;     // this launch's work counter, zero at launch
     // exact tile sums [tri][col][row] as two's complement 64-bit halves: every unit adds the
     // high (acc >> 32) and low (acc & (2^32 - 1)) parts of its int64 partial (|acc| < 2^62)
     unsigned long long *out_hi, *out_lo;
@@ -132,9 +134,9 @@ __device__ __forceinline__ GramUnit gram_unit(const GramArgs &g, int unit) {
     return w;
 }
 
-// Persistent: one CTA per SM takes work units from a global counter until none are left.
+// Persistent: one CTA per SM takes work units from the launch's counter until none are left.
 // Warp 0 (one thread) takes the units, posts each in a shared ring and streams its digit
-// tiles by TMA through two stages, running ahead across unit boundaries; warp 1 (one
+// tiles by TMA through the stages, running ahead across unit boundaries; warp 1 (one
 // thread) issues the MMAs; warps 2..9 drain the seven group accumulators from TMEM into
 // int64 sums once per flush and add the unit's sums to its tile's totals while the MMAs of
 // the next unit run.
@@ -189,10 +191,11 @@ __global__ void __maxnreg__(96) gram_exact_kernel(
         for (int j = 0; ok; ++j) {
             const int r = j % kSched;
             if (j >= kSched && !tc::mbar_wait(&sempty[r], ((j / kSched) - 1) & 1, g.status, g.budget)) break;
-            const int unit = atomicAdd(g.next_unit, 1);
-            sched[r] = unit < g.nunits ? unit : -1;
+            const int k = atomicAdd(g.next_unit, 1);
+            const int unit = k < g.nunits ? g.unit0 + k : -1;
+            sched[r] = unit;
             tc::mbar_arrive(&sfull[r]);  // release: the entry is visible to the waiters
-            if (unit >= g.nunits) break;
+            if (unit < 0) break;
             const GramUnit w = gram_unit(g, unit);
             for (int kb = 0; kb < w.nkb; ++kb, ++it) {
                 const int s = it % kGramStages, u = it / kGramStages;
@@ -1116,34 +1119,65 @@ CUtensorMap make_map(const void *ptr, long long rows, long long cols, int box_ro
     return m;
 }
 
-// Zeroed tile totals (high and low halves, 2 x ntri x 128 x 64 words) with the kernel's work
-// counter after them, in one buffer cleared by one memset on the stream
+// Work units of a Gram: ntri tiles x ceil(kb_total / kb_per_split) point splits.
+int gram_units_total(const GramArgs &g) {
+    RP_REQUIRE(g.kb_per_split >= 1 && g.kb_per_split <= kGramSplit && g.flush >= 1 && g.flush <= kGramFlush,
+               "gram: bad split");
+    const long long u = (long long)g.ntri * ceil_div(g.kb_total, g.kb_per_split);
+    RP_REQUIRE(u < (1LL << 30), "gram: too many work units");
+    return (int)u;
+}
+// Units per launch: kGramRounds rounds of one unit per SM.  A larger Gram is cut into launches
+// of that size, so that it holds the SMs for well under a millisecond at a time: between two
+// launches the block scheduler hands whole SMs to the waiting CTAs of streams of higher
+// priority (the small fits of a served stream), which a single persistent launch over a large
+// cube's ~10^5 units would keep to the room left beside its CTAs for tens of milliseconds.
+constexpr int kGramRounds = 16;
+int gram_units_per_launch(const rp_ctx *ctx) { return std::max(1, ctx->sm_count) * kGramRounds; }
+
+// Zeroed tile totals (high and low halves, 2 x ntri x 128 x 64 words) with one work counter
+// per launch after them, in one buffer cleared by one memset on the stream
 void gram_totals_init(rp_ctx *ctx, const std::string &name, GramArgs &g, cudaStream_t s) {
     const size_t n = (size_t)g.ntri * kBM * kGN;
-    unsigned long long *t = ctx->buf_t<unsigned long long>(name, 2 * n + 1);
-    RP_CUDA(cudaMemsetAsync(t, 0, sizeof(unsigned long long) * (2 * n + 1), s));
+    const size_t nl = (size_t)ceil_div(gram_units_total(g), gram_units_per_launch(ctx));
+    const size_t words = 2 * n + (nl + 1) / 2 + 1;
+    unsigned long long *t = ctx->buf_t<unsigned long long>(name, words);
+    RP_CUDA(cudaMemsetAsync(t, 0, sizeof(unsigned long long) * words, s));
     g.out_hi = t;
     g.out_lo = t + n;
     g.next_unit = reinterpret_cast<int *>(t + 2 * n);
 }
 
-// One CTA per SM (the stages fill shared memory), at most one per work unit
+// One CTA per SM (the stages fill most of its shared memory), at most one per work unit;
+// launches of at most gram_units_per_launch units, each with its own counter
 void launch_gram(rp_ctx *ctx, const __half *const *X, int rows, long long cols, GramArgs g, cudaStream_t s) {
     smem_optin((const void *)gram_exact_kernel, kGramSmem);
-    // the SM's whole shared memory as such, so that CTAs of other kernels fit beside this one
-    RP_CUDA(cudaFuncSetAttribute((const void *)gram_exact_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared));
-    RP_REQUIRE(g.kb_per_split >= 1 && g.kb_per_split <= kGramSplit && g.flush >= 1 && g.flush <= kGramFlush,
-               "gram: bad split");
-    g.nunits = g.ntri * (int)ceil_div(g.kb_total, g.kb_per_split);
-    const int grid = std::max(1, std::min(g.nunits, ctx->sm_count));
+    {
+        // the SM's whole shared memory as such, so that CTAs of other kernels fit beside this one
+        static std::atomic<unsigned long long> carved{0};
+        const int dev = ctx->device;
+        if (dev >= 0 && dev < 64 && !(carved.load() & (1ULL << dev))) {
+            RP_CUDA(cudaFuncSetAttribute((const void *)gram_exact_kernel,
+                                         cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared));
+            carved.fetch_or(1ULL << dev);
+        }
+    }
+    const int total = gram_units_total(g), per = gram_units_per_launch(ctx);
     CUtensorMap a[kGSlices], b[kGSlices];
     for (int q = 0; q < kGSlices; ++q) {
         a[q] = make_map(X[q], rows, cols, kBM);   // rows past `rows` read as zeros
         b[q] = make_map(X[q], rows, cols, kGN);
     }
-    gram_exact_kernel<<<grid, kGramThreads, kGramSmem, s>>>(a[0], a[1], a[2], a[3], b[0], b[1], b[2], b[3], g);
-    RP_LAUNCH_CHECK();
+    int *const counters = g.next_unit;
+    for (int k = 0, u0 = 0; u0 < total; ++k, u0 += per) {
+        g.unit0 = u0;
+        g.nunits = std::min(per, total - u0);
+        g.next_unit = counters + k;
+        const int grid = std::min(g.nunits, ctx->sm_count > 0 ? ctx->sm_count : 1);
+        gram_exact_kernel<<<grid, kGramThreads, kGramSmem, s>>>(a[0], a[1], a[2], a[3], b[0], b[1], b[2], b[3], g);
+        RP_LAUNCH_CHECK();
+    }
 }
 
 
