@@ -138,8 +138,8 @@ __device__ __forceinline__ GramUnit gram_unit(const GramArgs &g, int unit) {
 // Warp 0 (one thread) takes the units, posts each in a shared ring and streams its digit
 // tiles by TMA through the stages, running ahead across unit boundaries; warp 1 (one
 // thread) issues the MMAs; warps 2..9 drain the seven group accumulators from TMEM into
-// int64 sums once per flush and add the unit's sums to its tile's totals while the MMAs of
-// the next unit run.
+// int64 sums once per flush, 16 columns at a time, and add them to the tile's totals with
+// 64-bit atomics (the last columns' while the MMAs of the next unit already run).
 // At most 96 registers and 3 x 48 KB of stages: the SM keeps room for CTAs of other kernels
 // (the Phi kernel of other cubes, bound by instruction issue, which this kernel barely uses).
 __global__ void __maxnreg__(96) gram_exact_kernel(
