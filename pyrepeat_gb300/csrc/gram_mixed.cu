@@ -19,8 +19,9 @@
 //             power-of-two row scale.
 //  3. Gram    G = X X^T on tcgen05 (kind::f16, FP32 accumulators in TMEM) with all
 //             16 digit products kept: every partial sum is an integer below 2^24,
-//             so the Gram of the staged Phi is exact; each CTA (one point split of
-//             one tile) adds its int64 sums to the tile's exact 64-bit totals with
+//             so the Gram of the staged Phi is exact; a persistent kernel (one CTA
+//             per SM) takes work units (one point split of one tile) from a counter
+//             and adds each unit's int64 sums to the tile's exact 64-bit totals with
 //             atomics, which are rounded to FP64 once.
 //  4. finish  A = G - s s^T/M, b = G[:,V] - s sum(V)/M with s = sum_m (Phi - c)
 //             (FP64), i.e. repeat.py:2266-2276 for the shifted columns.
