@@ -168,6 +168,37 @@ def test_exact_gram_kernel_is_exact(gpu_ctx):
     assert np.abs(I.cpu().numpy() - refm).max() <= 1e-15 * np.abs(refm).max()
 
 
+def test_exact_gram_over_several_launches(gpu_ctx):
+    """A Gram of more work units than one launch takes (one 64-point block per unit: 6 tiles x
+    1024 point splits = 6144 units, cut into launches of 16 rounds of one unit per SM) gives
+    bitwise the totals of 16 blocks per unit in a single launch, and both the exact sum (every
+    slice product is an integer below 2^53 in FP64; the 16 scaled products are added in FP64,
+    so the reference itself carries a few ulps)."""
+    import torch
+    L = gpu_ctx.lib
+    L.rp_debug_gram_slices.restype = ctypes.c_int
+    L.rp_debug_gram_slices.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int, ctypes.c_longlong, ctypes.c_int,
+                                                               ctypes.c_int, ctypes.c_void_p]
+    rng = np.random.default_rng(1)
+    Np, cols = 200, 65536
+    X = [np.zeros((256, cols), np.float16) for _ in range(4)]
+    X[0][:Np] = rng.integers(-32, 33, size=(Np, cols))
+    for q in (1, 2, 3):
+        X[q][:Np] = rng.integers(-64, 65, size=(Np, cols))
+    xd = [torch.from_numpy(a).cuda() for a in X]
+    out = []
+    for split in (16, 1):
+        I = torch.zeros((Np, Np), dtype=torch.float64, device="cuda")
+        gpu_ctx.check(L.rp_debug_gram_slices(gpu_ctx.ptr, *[x.data_ptr() for x in xd], Np, cols, 16, split,
+                                             I.data_ptr()))
+        out.append(I.cpu().numpy())
+    assert np.array_equal(out[0], out[1])
+    x64 = [torch.from_numpy(a[:Np].astype(np.float64)).cuda() for a in X]
+    ref = sum((x64[a] @ x64[b].T) * 2.0 ** (7 * (6 - a - b)) for a in range(4) for b in range(4)) * 2.0 ** -54
+    ref = ref.cpu().numpy()
+    assert np.abs(out[1] - ref).max() <= 2e-15 * np.abs(ref).max()
+
+
 def test_batch_equals_single_fits(gpu_ctx):
     """A cube's charges are the same fitted alone (rp_fit) and inside a batch
     (rp_fit_batch): bitwise.  The staged entry points (rp_filter -> rp_gram ->
