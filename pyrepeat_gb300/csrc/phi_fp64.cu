@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(kRsPts) realspace_fp64_kernel(
             __syncthreads();
             for (int k = 0; k < cnt; ++k) tile[qitem[k * kRsPts + threadIdx.x] >> 7][threadIdx.x] += qterm[k * kRsPts + threadIdx.x];
             const int again = more;
-            __syncthreads();  // the queue is refilled next round
+            __syncthreads();  // the queue is refilled on the next pass
             if (!again) break;
         }
     }
